@@ -1,0 +1,282 @@
+/*
+ * vhsdecode_gb300 -- C ABI of the GB300 (sm_103a) RF decode backend.
+ *
+ * Drop-in for the reference's native `cuda-fast` boundary
+ * (src/VHSDecode.CudaFast.Native/include/vhsdecode_cuda_fast.h:130-309 in
+ * vhs-decode-dotnet): same status codes, enums, callback shapes, versioned
+ * structs that start with `struct_size`, a thread-local last error and a
+ * whole-run entry point.  The managed side binds it through P/Invoke exactly
+ * as Core/Dsp/CudaFast/CudaFastNativeRuntime.cs:491-621 binds the cuda-fast
+ * library (NativeLibrary.Load + GetExport, ABI version check).
+ *
+ * Beyond the run() handoff it exposes a session API that keeps a capture and
+ * every intermediate on the device (used by the serving loop, the parity tests
+ * and the benchmark), and a few stage-level entry points used by the tests.
+ *
+ * All functions are safe to call on a machine without a GPU: they then return
+ * VHSDECODE_GB300_STATUS_CUDA_UNAVAILABLE (or do host-only work).
+ */
+#ifndef VHSDECODE_GB300_H
+#define VHSDECODE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(_WIN32)
+#  if defined(VHSDECODE_GB300_EXPORTS)
+#    define VHSDECODE_GB300_API __declspec(dllexport)
+#  else
+#    define VHSDECODE_GB300_API __declspec(dllimport)
+#  endif
+#  define VHSDECODE_GB300_CALL __cdecl
+#else
+#  define VHSDECODE_GB300_API __attribute__((visibility("default")))
+#  define VHSDECODE_GB300_CALL
+#endif
+
+#define VHSDECODE_GB300_ABI_VERSION 0x00010000u
+#define VHSDECODE_GB300_NAME_CAPACITY 128u
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes: values of vhsdecode_cuda_fast_status (vhsdecode_cuda_fast.h:155-165). */
+typedef enum vhsdecode_gb300_status {
+    VHSDECODE_GB300_STATUS_OK = 0,
+    VHSDECODE_GB300_STATUS_NULL_POINTER = -20000,
+    VHSDECODE_GB300_STATUS_INVALID_ARGUMENT = -20001,
+    VHSDECODE_GB300_STATUS_CUDA_UNAVAILABLE = -20002,
+    VHSDECODE_GB300_STATUS_INPUT_ERROR = -20003,
+    VHSDECODE_GB300_STATUS_OUTPUT_ERROR = -20004,
+    VHSDECODE_GB300_STATUS_DECODE_ERROR = -20005,
+    VHSDECODE_GB300_STATUS_CANCELLED = -20006,
+    VHSDECODE_GB300_STATUS_INTERNAL_ERROR = -20007
+} vhsdecode_gb300_status;
+
+/* vhsdecode_cuda_fast_profile (vhsdecode_cuda_fast.h:167-171); PAL_M is rejected. */
+typedef enum vhsdecode_gb300_profile {
+    VHSDECODE_GB300_PROFILE_NTSC = 0,
+    VHSDECODE_GB300_PROFILE_PAL = 1,
+    VHSDECODE_GB300_PROFILE_PAL_M = 2
+} vhsdecode_gb300_profile;
+
+/* vhsdecode_cuda_fast_tape_speed (:173-177); only SP parameters are built in. */
+typedef enum vhsdecode_gb300_tape_speed {
+    VHSDECODE_GB300_TAPE_SPEED_SP = 0,
+    VHSDECODE_GB300_TAPE_SPEED_LP = 1,
+    VHSDECODE_GB300_TAPE_SPEED_EP = 2
+} vhsdecode_gb300_tape_speed;
+
+/* vhsdecode_cuda_fast_input_sample_format (:179-182); run() accepts INT16. */
+typedef enum vhsdecode_gb300_input_sample_format {
+    VHSDECODE_GB300_INPUT_FLOAT32 = 0,
+    VHSDECODE_GB300_INPUT_INT16 = 1
+} vhsdecode_gb300_input_sample_format;
+
+/* Arithmetic of the block demodulator. */
+typedef enum vhsdecode_gb300_precision {
+    VHSDECODE_GB300_PRECISION_FP32_FUSED = 0, /* cluster-fused FP32, FP64 sync/TBC */
+    VHSDECODE_GB300_PRECISION_FP64_PLAIN = 1  /* one block at a time, FP64 throughout */
+} vhsdecode_gb300_precision;
+
+/* Callbacks: shapes of vhsdecode_cuda_fast_read_callback / cancel_callback (:184-192).
+ * read: copy up to sample_count int16 samples starting at sample_offset into
+ * destination and return the count; a short count means end of input, 0 means
+ * end of input or failure. cancel: return nonzero to cancel. */
+typedef size_t (VHSDECODE_GB300_CALL *vhsdecode_gb300_read_callback)(
+    void* user_data, void* destination, uint64_t sample_offset, size_t sample_count);
+typedef int32_t (VHSDECODE_GB300_CALL *vhsdecode_gb300_cancel_callback)(void* user_data);
+
+/* vhsdecode_cuda_fast_runtime_info_v1 (:200-210). */
+typedef struct vhsdecode_gb300_runtime_info_v1 {
+    uint32_t struct_size;
+    uint32_t abi_version;
+    int32_t device_id;
+    int32_t compute_major;
+    int32_t compute_minor;
+    int32_t multiprocessor_count;
+    uint64_t total_vram_bytes;
+    uint64_t free_vram_bytes;
+    char device_name[VHSDECODE_GB300_NAME_CAPACITY];
+} vhsdecode_gb300_runtime_info_v1;
+
+/* vhsdecode_cuda_fast_config_v1 (:212-227), same fields and order. */
+typedef struct vhsdecode_gb300_config_v1 {
+    uint32_t struct_size;
+    uint32_t profile;
+    uint32_t tape_speed;
+    int32_t device_id;
+    double sample_rate_mhz;
+    uint64_t total_samples;
+    const char* output_base_utf8;
+    int32_t overwrite;
+    uint32_t input_sample_format;
+    uint32_t maximum_output_fields;
+    uint32_t device_decimation_factor;
+    vhsdecode_gb300_read_callback read_callback;
+    vhsdecode_gb300_cancel_callback cancel_callback;
+    void* user_data;
+} vhsdecode_gb300_config_v1;
+
+/* vhsdecode_cuda_fast_result_v1 (:229-235). */
+typedef struct vhsdecode_gb300_result_v1 {
+    uint32_t struct_size;
+    uint32_t fields_written;
+    uint32_t output_line_length;
+    uint32_t output_field_lines;
+    double elapsed_seconds;
+} vhsdecode_gb300_result_v1;
+
+/* Session: one device-resident decode context. */
+typedef struct vhsdecode_gb300_session vhsdecode_gb300_session;
+
+typedef struct vhsdecode_gb300_session_config_v1 {
+    uint32_t struct_size;
+    uint32_t profile;
+    uint32_t tape_speed;
+    int32_t device_id;
+    double sample_rate_mhz;
+    uint64_t max_samples;       /* capacity of one capture / window */
+    uint32_t precision;         /* vhsdecode_gb300_precision */
+    uint32_t max_fields;        /* 0 = derived from max_samples */
+} vhsdecode_gb300_session_config_v1;
+
+/* flags for vhsdecode_gb300_session_decode */
+#define VHSDECODE_GB300_DECODE_DEVICE_INPUT 0x1u /* rf is a device pointer (16-byte aligned) */
+#define VHSDECODE_GB300_DECODE_DEMOD_ONLY   0x2u /* stop after the block demodulator */
+
+typedef struct vhsdecode_gb300_decode_result_v1 {
+    uint32_t struct_size;
+    uint32_t fields;            /* fields decoded (TBC rendered) */
+    uint32_t output_line_length;
+    uint32_t output_field_lines;
+    uint64_t blocks;            /* 32768-sample blocks demodulated */
+    uint64_t stream_samples;    /* stitched stream length = blocks * 30720 */
+    uint32_t repaired_blocks;   /* blocks that took the diff-demod spike repair */
+    uint32_t stop_reason;       /* 0 end of data, 1 max fields, 2 field error */
+    double device_ms;           /* stream time of the whole decode */
+    double demod_ms;            /* block demodulator kernel time */
+    double field_ms;            /* pulses + hsync + TBC + dropout kernels */
+    double host_ms;             /* host control plane */
+} vhsdecode_gb300_decode_result_v1;
+
+typedef struct vhsdecode_gb300_field_info_v1 {
+    uint32_t struct_size;
+    int32_t is_first_field;
+    int64_t span_start;         /* stitched-stream index of the field span */
+    int64_t file_loc;           /* RF sample index of line 0 */
+    double line0;               /* span-relative */
+    double first_hsync;
+    double mean_line_length;
+    double next_field_offset;
+    uint32_t line_count;        /* line locations available */
+    uint32_t dropout_count;
+} vhsdecode_gb300_field_info_v1;
+
+/* ---- reference-shaped entry points ---------------------------------- */
+
+/* vhsdecode_cuda_fast_get_abi_version (:274-275) */
+VHSDECODE_GB300_API uint32_t VHSDECODE_GB300_CALL vhsdecode_gb300_get_abi_version(void);
+
+/* vhsdecode_cuda_fast_get_runtime_info (:277-280) */
+VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_get_runtime_info(
+    int32_t device_id, vhsdecode_gb300_runtime_info_v1* info);
+
+/* vhsdecode_cuda_fast_run (:282-285): whole-run handoff.  Pulls int16 RF through
+ * read_callback, decodes every field and writes <base>.tbc (uint16 LE luma,
+ * outlinelen x (frame_lines/2+1) per field) and <base>.tbc.json. */
+VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_run(
+    const vhsdecode_gb300_config_v1* config, vhsdecode_gb300_result_v1* result);
+
+/* vhsdecode_cuda_fast_get_last_error (:302-303), thread-local message. */
+VHSDECODE_GB300_API const char* VHSDECODE_GB300_CALL vhsdecode_gb300_get_last_error(void);
+
+/* ---- session API ------------------------------------------------------ */
+
+/* Replaces the preview context of vhsdecode_cuda_fast_preview_create (:287-290):
+ * a persistent device context for repeated windows. */
+VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_session_create(
+    const vhsdecode_gb300_session_config_v1* config, vhsdecode_gb300_session** session);
+
+/* vhsdecode_cuda_fast_preview_destroy (:297-299) */
+VHSDECODE_GB300_API void VHSDECODE_GB300_CALL vhsdecode_gb300_session_destroy(
+    vhsdecode_gb300_session* session);
+
+/* Use this CUDA stream (cudaStream_t as void*) for all device work; NULL = the
+ * session's own stream. */
+VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_session_set_stream(
+    vhsdecode_gb300_session* session, void* cuda_stream);
+
+/* Decode one capture/window (counterpart of
+ * vhsdecode_cuda_fast_preview_decode_window, :292-295).  rf is int16. */
+VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_session_decode(
+    vhsdecode_gb300_session* session, const int16_t* rf, uint64_t sample_count,
+    uint32_t max_fields, uint32_t flags, vhsdecode_gb300_decode_result_v1* result);
+
+VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_session_get_field(
+    vhsdecode_gb300_session* session, uint32_t index, vhsdecode_gb300_field_info_v1* info);
+
+/* Copy `count` fields of uint16 TBC luma starting at `first` to host memory. */
+VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_session_copy_tbc(
+    vhsdecode_gb300_session* session, uint32_t first, uint32_t count, uint16_t* destination);
+
+/* Refined line locations of one field (span-relative samples). */
+VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_session_copy_lines(
+    vhsdecode_gb300_session* session, uint32_t field, double* destination, uint32_t capacity);
+
+/* Dropouts of one field mapped to TBC coordinates (field line, start x, end x). */
+VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_session_copy_dropouts(
+    vhsdecode_gb300_session* session, uint32_t field, int32_t* line, int32_t* start_x,
+    int32_t* end_x, uint32_t capacity, uint32_t* count);
+
+/* Stitched stream channel (0 video Hz, 1 sync reference Hz, 2 envelope) as double. */
+VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_session_copy_stream(
+    vhsdecode_gb300_session* session, uint32_t channel, uint64_t start, uint64_t count,
+    double* destination);
+
+/* Device pointer of the uint16 TBC buffer (fields x lines x outlinelen). */
+VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_session_tbc_device(
+    vhsdecode_gb300_session* session, void** device_pointer, uint64_t* bytes);
+
+/* ---- stage-level entry points (tests) ------------------------------ */
+
+/* Filter spectra (bins 0..16384) for a profile at a sample rate; host only.
+ * video / sync are interleaved (re, im). env receives b0, b1, a1. */
+VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_design_filters(
+    uint32_t profile, uint32_t tape_speed, double sample_rate_mhz, double* rf_video,
+    double* video, double* sync, double* env);
+
+/* Host control plane on given raw pulses of one span; host only.
+ * state[0] = previous first-field flag (-1 unknown), state[1] = has previous
+ * hsync; updated in place.  out[0..4] = first_field, line0, first_hsync,
+ * mean line length, next field offset.  locs receives the unrefined line
+ * locations.  ref (optional, span_len doubles) feeds the long-hsync rescue. */
+VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_field_sync(
+    uint32_t profile, double sample_rate_mhz, const int64_t* starts, const int64_t* lengths,
+    uint64_t pulse_count, int64_t span_len, const double* ref, int32_t* state, double* out,
+    double* locs, uint32_t locs_capacity, uint32_t* locs_count);
+
+/* Device sinc TBC of `source` (double) through the linear line-location plan;
+ * output values are float32-rounded, as the reference's ResampleLines. */
+VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_tbc_resample_lines(
+    const double* source, uint64_t source_length, const double* locations,
+    uint32_t location_count, uint32_t first_line, uint32_t line_count,
+    uint32_t output_line_length, double nominal_line_length, double level_smoothing,
+    double* destination);
+
+/* Device pulse detection over one array (PulseDetection.FindPulses semantics). */
+VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_find_pulses(
+    const double* reference, uint64_t length, double high, int64_t minimum_length,
+    int64_t maximum_length, int64_t* starts, int64_t* lengths, uint64_t capacity,
+    uint64_t* count);
+
+/* Device polynomial atan2 (the FM demodulator's angle) for n float pairs. */
+VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_vhs_angles(
+    const float* real, const float* imaginary, uint64_t n, float* angles);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VHSDECODE_GB300_H */

@@ -1,0 +1,109 @@
+"""Per-block VHS RF demodulation and block-stream stitching (test infrastructure).
+
+Restates the managed ``exact`` VHS real-FFT path of
+``RfDemodulator.DemodulateCore`` (Core/Dsp/RfDemodulator.cs:288-918) with
+``useNumpyComplexVhsAnalytic`` set (Core/Decode/RfBlockDecodePipeline.cs:107):
+
+* RF half-spectrum x RfVideo -> real inverse = band-passed RF (envelope source)
+  (RfDemodulator.cs:396-478, 551);
+* full complex FFT x RfVideo x Hilbert -> complex inverse = analytic signal
+  (``BuildNumpyVhsComplexAnalyticSignal`` RfDemodulator.cs:1461-1536,
+  ``PortedMath.BuildHilbertMultiplier`` PortedMath.cs:456-472);
+* float32 polynomial-atan2 FM demod (PortedMath.cs:70-230, 519-551);
+* diff-demod spike repair (RfDemodulator.cs:2527-2582, 966-1001);
+* float32 envelope filtfilt (RfDemodulator.cs:1755-1839);
+* demod real FFT x Video / x VideoLowPass05, real inverses, roll -32
+  (RfDemodulator.cs:792-885).
+
+Stitching follows ``RfBlockStreamDecoder.ReadCore`` / ``CopyTrimmedWindow``
+(Core/Decode/RfBlockStreamDecoder.cs:418-560, 1586-1610): block b reads RF
+``[b*S, b*S+N)`` and contributes ``[cut, cut+S)`` to stream ``[b*S, b*S+S)``.
+"""
+import numpy as np
+
+from . import native
+
+BLOCK = 32768
+CUT = 1024
+CUT_END = 1024
+STRIDE = BLOCK - CUT - CUT_END
+
+
+def replace_spikes(demod, diffed, max_value, replace_start=8, replace_end=30):
+    """``RfDemodulator.ReplaceSpikes`` (Core/Dsp/RfDemodulator.cs:966-1001)."""
+    demod = np.asarray(demod, np.float64)
+    to_fix = np.nonzero(demod > max_value)[0]
+    n = len(demod)
+    for i in to_fix:
+        start = max(i - replace_start, 0)
+        end = min(i + replace_end, n - 1)
+        if start >= end:
+            continue
+        if np.max(diffed[start:end]) < np.max(demod[start:end]):
+            demod[start:end] = diffed[start:end]
+    return demod
+
+
+def demod_block(x, filters, fs, diff_max, return_debug=False):
+    """Demodulate one RF block; returns (video, video_lowpass, envelope, weak, debug)."""
+    x = np.asarray(x, np.float64)
+    n = len(x)
+    h = n // 2 + 1
+    rfv = filters.rf_video
+    spec_half = np.fft.rfft(x)
+    filtered_real = np.fft.irfft(spec_half * rfv[:h], n)
+    hilbert = np.zeros(n)
+    hilbert[0] = 1.0
+    hilbert[n // 2] = 1.0
+    hilbert[1:n // 2] = 2.0
+    analytic = np.fft.ifft(np.fft.fft(x) * rfv * hilbert)
+    demod = native.vhs_rust_demod(analytic.real, analytic.imag, fs)
+    repaired = False
+    if diff_max is not None and n > 40 and np.any(demod[20:n - 20] > diff_max):
+        diffed = np.zeros(n, complex)
+        diffed[1:] = analytic[1:] - analytic[:-1]
+        demod_diffed = native.vhs_rust_demod(diffed.real, diffed.imag, fs)
+        demod = replace_spikes(demod, demod_diffed, diff_max)
+        repaired = True
+    envelope = native.vhs_envelope(filtered_real, filters.env_b[0], filters.env_b[1], filters.env_a1)
+    weak = bool(np.any(envelope == 0.0))
+    dspec = np.fft.rfft(demod)
+    video = np.fft.irfft(dspec * filters.video[:h], n)
+    vlp = np.fft.irfft(dspec * filters.video_lp05[:h], n)
+    vlp = np.roll(vlp, -filters.video_lp05_offset)
+    dbg = None
+    if return_debug:
+        dbg = {"analytic": analytic, "demod": demod, "filtered_real": filtered_real,
+               "repaired": repaired}
+    return video, vlp, envelope, weak, dbg
+
+
+def block_count(total_samples):
+    """Number of whole 32768-sample blocks a capture of ``total_samples`` RF samples holds."""
+    if total_samples < BLOCK:
+        return 0
+    return (total_samples - BLOCK) // STRIDE + 1
+
+
+def demod_stream(rf, filters, fs, diff_max, first_block=0, nblocks=None):
+    """Stitched stream channels for blocks ``first_block..first_block+nblocks``.
+
+    Stream sample d corresponds to RF sample d + CUT.
+    """
+    total = block_count(len(rf))
+    if nblocks is None:
+        nblocks = total - first_block
+    video = np.empty(nblocks * STRIDE)
+    vlp = np.empty(nblocks * STRIDE)
+    env = np.empty(nblocks * STRIDE)
+    weak = False
+    for j in range(nblocks):
+        b = first_block + j
+        x = rf[b * STRIDE: b * STRIDE + BLOCK].astype(np.float64)
+        v, l, e, w, _ = demod_block(x, filters, fs, diff_max)
+        sl = slice(j * STRIDE, (j + 1) * STRIDE)
+        video[sl] = v[CUT:CUT + STRIDE]
+        vlp[sl] = l[CUT:CUT + STRIDE]
+        env[sl] = e[CUT:CUT + STRIDE]
+        weak |= w
+    return video, vlp, env, weak

@@ -1,0 +1,199 @@
+"""Field decode and field sequencing for the VHS path (test infrastructure).
+
+Per field (``TbcFieldDecodePipeline.DecodePrepared``,
+Core/Decode/TbcFieldDecodePipeline.cs:1071-1440, standard VHS branch):
+pulses on the sync reference at IreToHz(vsync_ire/2) -> timing -> classify ->
+refine -> mean line length -> cadence -> VBlank line 0 -> upstream line
+locations (output lines + 10) -> next-field offset -> hsync refinement ->
+NTSC fsc phase shift -> sinc TBC of the output lines -> uint16 -> dropouts.
+
+Sequencing follows ``DecodeReadWindowPlanner`` (Core/Decode/DecodeReadWindowPlanner.cs:14-64)
+and ``EstimateNextFieldStart`` (Core/Decode/TbcFieldSequenceDecodeEngine.cs:1934-1941).
+"""
+import math
+
+import numpy as np
+
+from . import demod, formats, sync, tbc, native
+from .filters import FilterSet
+
+
+class FieldError(Exception):
+    pass
+
+
+def read_length(sp):
+    line = int(round(sp.line_period_us * sp.mhz))
+    if sp.system == "PAL":
+        base = line * 400
+    else:
+        base = (line * 350 // 16384) * 16384
+    return (base // demod.BLOCK + 2) * demod.BLOCK
+
+
+def resolve_span(intended, read_len):
+    read_loc = max(0, intended - demod.CUT)
+    a0 = (read_loc // demod.BLOCK) * demod.BLOCK
+    a1 = a0 + read_len
+    first = a0 // demod.STRIDE
+    last = a1 // demod.STRIDE
+    return first * demod.STRIDE, (last - first + 1) * demod.STRIDE
+
+
+class FieldState:
+    def __init__(self):
+        self.prev_first = None
+        self.has_prev_hsync = False
+
+
+def _single_estimate(fe, le, has_prev):
+    fc = fe["count"] if fe else 0
+    lc = le["count"] if le else 0
+    if fc == 6 or (not has_prev and fc > lc):
+        return fe
+    if le is not None:
+        return le
+    return fe
+
+
+def output_first_line(sp, first_field):
+    if sp.system == "NTSC":
+        return 1
+    return 3 if first_field else 4
+
+
+def line_offset(sp, first_field):
+    if sp.system != "PAL":
+        return 0
+    return 2 if first_field else 3
+
+
+def decode_field(sp, fmt, video, vlp, env, state, want_tbc=True):
+    """Decode one field from span channels (arrays relative to the span start)."""
+    threshold = sp.ire_to_hz(sp.vsync_ire / 2.0)
+    raw = sync.find_raw_pulses(sp, vlp, threshold)
+    if not raw:
+        raise FieldError("no sync pulses")
+    timing = sync.estimate_timing(sp, raw)
+    classified = sync.classify_pulses(sp, raw, timing)
+    refined, _ = sync.refine_pulses(sp, raw, timing, vlp, 10.0 * sp.hz_ire)
+    mll = sync.mean_line_length(sp, refined)
+    first_field = sync.resolve_cadence(sp, refined, mll, state.prev_first, 100, state.has_prev_hsync)
+    state.prev_first = first_field
+    field_lines = sp.field_lines()[0 if first_field else 1]
+    g1 = sync.find_first_group(refined, None, 9)
+    if g1 is None:
+        raise FieldError("no vblank")
+    g2 = sync.find_first_group(refined, g1["eq1"] + (field_lines - 2.0) * mll, 9)
+    fe, le, comb = sync.estimate_line0_from_groups(sp, classified, g1, g2, mll, first_field, field_lines)
+    pick = comb if comb is not None else _single_estimate(fe, le, state.has_prev_hsync)
+    if pick is None:
+        raise FieldError("no line 0")
+    line0 = pick["line0"]
+    fh = pick["first_hsync"]
+    state.has_prev_hsync = True
+    processed = sp.output_lines + 10
+    last_line = ((len(video) - line0) / mll) - 1.0
+    if last_line < processed:
+        raise FieldError("insufficient data")
+    fh_line = sync.first_hsync_line(sp, first_field)
+    locs, filled = sync.build_upstream_line_locations(refined, float(math.trunc(fh)), int(fh_line),
+                                                      mll, processed)
+    next_loc = sync.next_field_location(sp, first_field, field_lines, mll, fh)
+    next_off = next_loc - 8.0 * sp.nominal + demod.CUT
+    locs, filled = sync.refine_hsync(sp, vlp, locs, filled, threshold)
+    if sp.system == "NTSC":
+        locs = locs - ((117.25 / 360.0) / sp.fsc_mhz) * sp.mhz
+    res = {"first_field": first_field, "line0": line0, "first_hsync": fh, "mean_line": mll,
+           "locs": locs, "next_offset": next_off, "pulses": raw, "refined": refined}
+    if want_tbc:
+        ofl = output_first_line(sp, first_field)
+        smoothing = fmt["sys"]["frame_lines"] / 2.0
+        nominal_in = float(round(fmt["sys"]["line_period"] * sp.mhz))
+        hz = tbc.resample_field(video, locs, ofl, sp.output_lines, sp.outlinelen, nominal_in, smoothing)
+        res["tbc_hz"] = hz
+        res["tbc"] = tbc.to_u16(hz, sp, formats.output_scale(fmt), fmt["sys"]["outputZero"])
+        res["dropouts"] = dropouts(sp, env, locs, first_field)
+    return res
+
+
+def dropouts(sp, env, locs, first_field, frac=0.18, hyst=1.25):
+    """``DetectTapeDropouts`` + ``RfDropoutDetector.FindDropouts`` + ``MapTapeRfToTbc``
+    (TbcFieldDecodePipeline.cs:6593-6640; TbcDropoutMapping.cs:52-107, 288-370)."""
+    off = line_offset(sp, first_field)
+    start_line = off + 1
+    field_lines = sp.field_lines()[0 if first_field else 1]
+    end_line = min(len(locs) - 1, field_lines + start_line + 1)
+    if start_line < 0 or end_line <= start_line or start_line >= len(locs):
+        return []
+    s0 = min(max(int(math.floor(locs[start_line])), 0), len(env))
+    s1 = min(max(int(math.ceil(locs[end_line])), s0), len(env))
+    if s1 <= s0:
+        return []
+    mean32 = np.mean(np.asarray(env, np.float32), dtype=np.float32)
+    thr = float(np.float32(mean32 * np.float32(frac)))
+    ranges = native.find_dropouts(env, s0, s1, thr, hyst)
+    return map_rf_to_tbc(ranges, locs, sp.outlinelen, start_line, end_line, off)
+
+
+def map_rf_to_tbc(ranges, locs, outlen, start_line, end_line, off):
+    out = []
+    li = start_line
+    ls, le = locs[li], locs[li + 1]
+    for (ds, de) in ranges:
+        found = False
+        while li < end_line:
+            ll = le - ls
+            if (ds >= ls or li == start_line) and ds < le and ll > 0.0:
+                sx = int(math.floor(((ds - ls) / ll) * outlen))
+                cur = [li - off, max(0, sx), None]
+                found = True
+                break
+            li += 1
+            if li < end_line:
+                ls, le = locs[li], locs[li + 1]
+        if not found:
+            break
+        while li < end_line:
+            ll = le - ls
+            if de < le and ll > 0.0:
+                ex = int(math.ceil(((de - ls) / ll) * outlen))
+                cur[2] = min(outlen, ex)
+                out.append(tuple(cur))
+                break
+            cur[2] = outlen
+            out.append(tuple(cur))
+            li += 1
+            if li < end_line:
+                ls, le = locs[li], locs[li + 1]
+                cur = [li - off, 0, None]
+    return out
+
+
+def decode_capture(rf, fmt, fs=40e6, max_fields=None, want_tbc=True, channels=None):
+    """Decode a whole int16 capture; returns (fields, channels)."""
+    sp = sync.SyncParams(fmt, fs)
+    filt = FilterSet(fmt, fs)
+    diff_max = (sp.ire0 + sp.hz_ire * 100.0) * 2.0
+    if channels is None:
+        channels = demod.demod_stream(rf, filt, fs, diff_max)
+    video, vlp, env, _ = channels
+    avail = len(video)
+    rl = read_length(sp)
+    state = FieldState()
+    fields = []
+    intended = 0
+    while max_fields is None or len(fields) < max_fields:
+        s0, slen = resolve_span(intended, rl)
+        if s0 + slen > avail:
+            break
+        sl = slice(s0, s0 + slen)
+        try:
+            f = decode_field(sp, fmt, video[sl], vlp[sl], env[sl], state, want_tbc)
+        except FieldError as exc:
+            fields.append({"error": str(exc), "span_start": s0})
+            break
+        f["span_start"] = s0
+        fields.append(f)
+        intended = s0 + max(1, int(sync.round_away(f["next_offset"])))
+    return fields, channels

@@ -1,0 +1,76 @@
+"""Format parameters used by the oracle (test infrastructure).
+
+The values restate the frozen upstream snapshot the reference embeds
+(``src/VHSDecode.Core/Formats/format-params.snapshot.json``, cases
+``PAL/VHS/sp`` and ``NTSC/VHS/sp``; read through ``FormatCatalog.cs:46-112``).
+Only the keys the RF -> TBC luma path reads are kept.  ``tests/golden/
+format_params.json`` (written by ``tests/golden/make_golden.py`` from the
+reference snapshot) pins this table.
+"""
+
+PAL_VHS_SP = {
+    "system": "PAL", "tape_format": "VHS", "tape_speed": "sp",
+    "sys": {
+        "FPS": 25.0, "ire0": 4100000.0, "hz_ire": 7000.0,
+        "vsync_ire": -42.857142857142854, "line_period": 64.0,
+        "hsyncPulseUS": 4.7, "eqPulseUS": 2.35, "vsyncPulseUS": 27.3,
+        "numPulses": 5, "outlinelen": 1135, "outfreq": 17.734475,
+        "frame_lines": 625, "field_lines": [312, 313], "outputZero": 256,
+        "fsc_mhz": 4.43361875,
+    },
+    "rf": {
+        "video_bpf_low": 1300000.0, "video_bpf_high": 5780000.0,
+        "video_bpf_order": None, "video_bpf_supergauss": False,
+        "video_lpf_extra": 5910000.0, "video_lpf_extra_order": 20,
+        "video_hpf_extra": 1320000.0, "video_hpf_extra_order": 12,
+        "video_rf_peak_freq": 4300000.0, "video_rf_peak_gain": 4.0,
+        "video_rf_peak_bandwidth": 10000000.0,
+        "boost_rf_linear_0": 0.0, "boost_rf_linear_20": 1.0,
+        "start_rf_linear": 626953.0, "boost_rf_linear_double": False,
+        "video_lpf_freq": 3400000.0, "video_lpf_order": 6,
+        "video_lpf_supergauss": False,
+        "deemph_gain": 13.9794, "deemph_mid": 273755.82,
+        "deemph_q": 0.462088186,
+        "color_under_carrier": 626953.0,
+    },
+}
+
+NTSC_VHS_SP = {
+    "system": "NTSC", "tape_format": "VHS", "tape_speed": "sp",
+    "sys": {
+        "FPS": 29.970029970029973, "ire0": 3685714.2857142854,
+        "hz_ire": 7142.857142857143, "vsync_ire": -40.0,
+        "line_period": 63.55555555555555, "hsyncPulseUS": 4.7,
+        "eqPulseUS": 2.3, "vsyncPulseUS": 27.1, "numPulses": 6,
+        "outlinelen": 910, "outfreq": 14.318181818181818,
+        "frame_lines": 525, "field_lines": [263, 262], "outputZero": 1024,
+        "fsc_mhz": 3.5795454545454546,
+    },
+    "rf": {
+        "video_bpf_low": 500000.0, "video_bpf_high": 6500000.0,
+        "video_bpf_order": 8, "video_bpf_supergauss": False,
+        "video_lpf_extra": 6000000.0, "video_lpf_extra_order": 25,
+        "video_hpf_extra": 1200000.0, "video_hpf_extra_order": 20,
+        "video_rf_peak_freq": 3900000.0, "video_rf_peak_gain": 4.0,
+        "video_rf_peak_bandwidth": 10000000.0,
+        "boost_rf_linear_0": 0.0, "boost_rf_linear_20": 1.0,
+        "start_rf_linear": 629370.6293706294, "boost_rf_linear_double": False,
+        "video_lpf_freq": 6600000.0, "video_lpf_order": 9,
+        "video_lpf_supergauss": True,
+        "deemph_gain": 13.9794, "deemph_mid": 273755.82,
+        "deemph_q": 0.462088186,
+        "color_under_carrier": 629370.6293706294,
+    },
+}
+
+FORMATS = {("PAL", "VHS", "sp"): PAL_VHS_SP, ("NTSC", "VHS", "sp"): NTSC_VHS_SP}
+
+
+def get(system: str, tape_format: str = "VHS", speed: str = "sp") -> dict:
+    return FORMATS[(system.upper(), tape_format.upper(), speed.lower())]
+
+
+def output_scale(fmt: dict) -> float:
+    """``VideoOutputConverter.ComputeOutputScale`` (Core/Tbc/VideoOutputConverter.cs:129-138)."""
+    dividend = (0xD300 - 0x0100) if fmt["system"] == "PAL" else (0xC800 - 0x0400)
+    return dividend / (100.0 - fmt["sys"]["vsync_ire"])

@@ -1,0 +1,138 @@
+"""C-ABI library checks that need no GPU: load, exports, struct layouts, host stages."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import HAVE_GPU, ROOT
+
+
+def _declared_functions():
+    text = open(os.path.join(ROOT, "include", "vhsdecode_gb300.h")).read()
+    return sorted(set(re.findall(r"VHSDECODE_GB300_CALL\s+(vhsdecode_gb300_\w+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol(lib):
+    names = _declared_functions()
+    assert len(names) >= 19
+    for n in names:
+        assert hasattr(lib, n), n
+    from vhsd_gb300 import native
+    assert sorted(native.EXPORTS) == names
+
+
+def test_abi_version(lib):
+    from vhsd_gb300 import native
+    assert lib.vhsdecode_gb300_get_abi_version() == native.ABI_VERSION
+
+
+def test_struct_sizes_match_c_layout(lib, tmp_path):
+    # the C compiler's layout of include/vhsdecode_gb300.h against the ctypes mirrors
+    import subprocess
+    from vhsd_gb300 import native
+    structs = {"runtime_info_v1": native.RuntimeInfo, "config_v1": native.RunConfig,
+               "result_v1": native.RunResult, "session_config_v1": native.SessionConfig,
+               "decode_result_v1": native.DecodeResult, "field_info_v1": native.FieldInfo}
+    src = tmp_path / "sizes.c"
+    src.write_text('#include <stdio.h>\n#include "vhsdecode_gb300.h"\nint main(void){\n' + "".join(
+        'printf("%%zu\\n", sizeof(vhsdecode_gb300_%s));\n' % k for k in structs) + "return 0;}\n")
+    exe = tmp_path / "sizes"
+    subprocess.check_call(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)])
+    sizes = [int(x) for x in subprocess.check_output([str(exe)]).split()]
+    for (name, cls), size in zip(structs.items(), sizes):
+        assert ctypes.sizeof(cls) == size, name
+
+
+def test_runtime_info_rejects_bad_struct_size(lib):
+    from vhsd_gb300 import native
+    info = native.RuntimeInfo()
+    info.struct_size = 12
+    st = lib.vhsdecode_gb300_get_runtime_info(0, ctypes.byref(info))
+    assert st in (native.STATUS_INVALID_ARGUMENT, native.STATUS_CUDA_UNAVAILABLE)
+    assert st == native.STATUS_INVALID_ARGUMENT
+
+
+@pytest.mark.skipif(HAVE_GPU, reason="checks the no-GPU status")
+def test_no_gpu_reports_cuda_unavailable(lib):
+    from vhsd_gb300 import native
+    with pytest.raises(native.BackendUnavailable):
+        native.runtime_info(0)
+    with pytest.raises(native.BackendUnavailable):
+        native.Session(native.PROFILE_PAL, 1 << 20)
+
+
+def test_null_pointer_status(lib):
+    from vhsd_gb300 import native
+    assert lib.vhsdecode_gb300_run(None, None) == native.STATUS_NULL_POINTER
+    assert b"null" in lib.vhsdecode_gb300_get_last_error()
+
+
+def test_run_rejects_unsupported_options(lib):
+    from vhsd_gb300 import native
+    cfg = native.RunConfig()
+    cfg.struct_size = ctypes.sizeof(cfg)
+    cfg.profile = native.PROFILE_PAL
+    cfg.sample_rate_mhz = 40.0
+    cfg.output_base_utf8 = b"/tmp/x"
+    cfg.input_sample_format = native.INPUT_FLOAT32
+    cfg.device_decimation_factor = 1
+    cfg.read_callback = native.READ_CB(lambda u, d, o, c: 0)
+    res = native.RunResult()
+    res.struct_size = ctypes.sizeof(res)
+    assert lib.vhsdecode_gb300_run(ctypes.byref(cfg), ctypes.byref(res)) == native.STATUS_INVALID_ARGUMENT
+    cfg.input_sample_format = native.INPUT_INT16
+    cfg.device_decimation_factor = 2
+    assert lib.vhsdecode_gb300_run(ctypes.byref(cfg), ctypes.byref(res)) == native.STATUS_INVALID_ARGUMENT
+    cfg.device_decimation_factor = 1
+    cfg.struct_size = 8
+    assert lib.vhsdecode_gb300_run(ctypes.byref(cfg), ctypes.byref(res)) == native.STATUS_INVALID_ARGUMENT
+
+
+@pytest.mark.parametrize("system", ["PAL", "NTSC"])
+def test_filter_design_matches_oracle(lib, system):
+    from vhsd_gb300 import native
+    from oracle import filters, formats
+    prof = native.PROFILE_PAL if system == "PAL" else native.PROFILE_NTSC
+    rv, v, s, env = native.design_filters(prof)
+    fl = filters.FilterSet(formats.get(system), 40e6)
+
+    def rel(a, b):
+        return np.max(np.abs(a - b)) / np.max(np.abs(b))
+
+    # the NTSC band-pass is evaluated from its 16th-order polynomial, as the reference does
+    assert rel(rv, fl.half("rf_video")) < 1e-6
+    assert rel(v, fl.half("video")) < 1e-10
+    assert rel(s, fl.half("video_lp05")) < 1e-10
+    np.testing.assert_allclose(env, [fl.env_b[0], fl.env_b[1], fl.env_a1], rtol=1e-15)
+
+
+@pytest.mark.parametrize("system", ["PAL", "NTSC"])
+def test_host_control_plane_matches_oracle(lib, system, request):
+    from vhsd_gb300 import native
+    from oracle import field, formats, sync
+    fields, ch = request.getfixturevalue("pal_oracle" if system == "PAL" else "ntsc_oracle")
+    prof = native.PROFILE_PAL if system == "PAL" else native.PROFILE_NTSC
+    sp = sync.SyncParams(formats.get(system), 40e6)
+    _, vlp, _, _ = ch
+    state = np.array([-1, 0], np.int32)
+    good = [f for f in fields if "error" not in f]
+    assert len(good) >= 3
+    for f in good:
+        s0 = f["span_start"]
+        _, slen = field.resolve_span(s0, field.read_length(sp))
+        r = native.field_sync(prof, f["pulses"], slen, state, ref=vlp[s0:s0 + slen])
+        assert r["first_field"] == f["first_field"]
+        assert r["line0"] == f["line0"]
+        assert r["first_hsync"] == f["first_hsync"]
+        assert r["mean_line"] == f["mean_line"]
+        assert r["next_offset"] == f["next_offset"]
+        assert len(r["locs"]) == sp.output_lines + 10
+
+
+def test_field_sync_rejects_empty_pulses(lib):
+    from vhsd_gb300 import native
+    state = np.array([-1, 0], np.int32)
+    with pytest.raises(native.NativeError):
+        native.field_sync(native.PROFILE_PAL, [], 1000000, state)

@@ -1,0 +1,153 @@
+"""Device parity against the CPU oracle, through the C ABI.
+
+Tolerances (stated once, used below):
+* demodulated / filtered video frequency: within 1 kHz;
+* line locations: within 0.01 sample;
+* uint16 TBC: |diff| <= 1 LSB on >= 99.9% of samples (FP32 fused path);
+  the FP64 plain path is held to the same bar;
+* field count, field order and dropout decisions identical.
+Integer / index work (pulses, angles, TBC arithmetic on identical inputs) is bit-exact.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+FREQ_TOL_HZ = 1000.0
+LINE_TOL = 0.01
+LSB_FRACTION = 0.999
+
+
+def test_device_atan2_bit_exact(gpu):
+    from vhsd_gb300 import native
+    from oracle import native as onative
+    rng = np.random.default_rng(7)
+    n = 1 << 16
+    re = (rng.standard_normal(n) * 10 ** rng.uniform(-3, 4, n)).astype(np.float32)
+    im = (rng.standard_normal(n) * 10 ** rng.uniform(-3, 4, n)).astype(np.float32)
+    special = np.array([0.0, -0.0, 1.0, -1.0, np.inf, -np.inf, np.nan, 1e-45, -1e-45, 3e38],
+                       np.float32)
+    re[:100] = np.resize(special, 100)
+    im[:100] = np.resize(special[::-1], 100)
+    a = native.vhs_angles(re, im)
+    b = onative.vhs_rust_angles(re, im)
+    assert a.view(np.uint32).tolist() == b.view(np.uint32).tolist()
+
+
+def test_device_pulses_match_state_machine(gpu):
+    from vhsd_gb300 import native
+    from oracle import native as onative
+    rng = np.random.default_rng(0x50414C)
+    specials = [np.nan, -np.inf, -1.0, 0.0, 1.0, np.inf]
+    for it in range(60):
+        n = int(rng.integers(1, 20000))
+        d = rng.random(n) * 20.0 - 10.0
+        mask = rng.integers(0, 20, n) == 0
+        d[mask] = np.array(specials)[rng.integers(0, len(specials), mask.sum())]
+        high = rng.random() * 12 - 6
+        mn = int(rng.integers(0, 12))
+        mx = int(rng.integers(mn, 64))
+        assert native.find_pulses(d, high, mn, mx) == onative.find_pulses(d, high, mn, mx)
+
+
+def test_device_tbc_bit_exact_against_oracle(gpu):
+    from vhsd_gb300 import native
+    from oracle import tbc
+    import json
+    import os
+    g = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "sinc_lut_rows.json")))
+    for c in g["cases"]:
+        src = np.arange(c["source_length"], dtype=np.float64)
+        locs = c["locations"]
+        nominal = max(1.0, float(np.median(np.diff(locs))))
+        want = tbc.resample_field(src, locs, c["first_line"], c["line_count"], c["outlen"], nominal, 0.0)
+        got = native.tbc_resample_lines(src, locs, c["first_line"], c["line_count"], c["outlen"])
+        assert got.tobytes() == want.tobytes(), c["name"]
+    # larger plan with wow smoothing and outlier factors
+    idx = np.arange(220000)
+    src = np.sin(idx * 0.0031) + np.cos(idx * 0.0007)
+    locs = 1000.25 + np.arange(101) * 2000.125 + 0.01 * np.arange(101) ** 2
+    locs[40] += 700.0
+    want = tbc.resample_field(src, locs, 3, 90, 1024, 2000.125, 1.5)
+    got = native.tbc_resample_lines(src, locs, 3, 90, 1024, 2000.125, 1.5)
+    # smoothing is evaluated in closed form on the device: equal to float rounding
+    assert np.max(np.abs(got - want)) <= 2 * np.max(np.abs(want)) * 2 ** -24
+
+
+def _session_decode(system, rf, precision):
+    from vhsd_gb300 import native
+    prof = native.PROFILE_PAL if system == "PAL" else native.PROFILE_NTSC
+    s = native.Session(prof, len(rf), precision=precision)
+    r = s.decode(rf)
+    return s, r
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp32_fused", "fp64_plain"])
+@pytest.mark.parametrize("system", ["PAL", "NTSC"])
+def test_stream_channels_match_oracle(gpu, system, precision, request):
+    rf, _ = request.getfixturevalue("pal_capture" if system == "PAL" else "ntsc_capture")
+    _, (video, vlp, env, _) = request.getfixturevalue("pal_oracle" if system == "PAL" else "ntsc_oracle")
+    from vhsd_gb300 import native
+    prof = native.PROFILE_PAL if system == "PAL" else native.PROFILE_NTSC
+    with native.Session(prof, len(rf), precision=precision) as s:
+        r = s.decode(rf, demod_only=True)
+        n = len(video)
+        assert r.stream_samples == n
+        v = s.stream(0, 0, n)
+        y = s.stream(1, 0, n)
+        e = s.stream(2, 0, n)
+    dv = np.abs(v - video)
+    dy = np.abs(y - vlp)
+    assert np.quantile(dv, 0.999) < FREQ_TOL_HZ, np.max(dv)
+    assert np.quantile(dy, 0.999) < FREQ_TOL_HZ, np.max(dy)
+    de = np.abs(e - env) / np.maximum(np.abs(env), 1.0)
+    assert np.quantile(de, 0.999) < 1e-3
+    if precision == 1:
+        assert np.max(dv) < 1.0 and np.max(dy) < 1.0
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp32_fused", "fp64_plain"])
+@pytest.mark.parametrize("system", ["PAL", "NTSC"])
+def test_fields_and_tbc_match_oracle(gpu, system, precision, request):
+    rf, _ = request.getfixturevalue("pal_capture" if system == "PAL" else "ntsc_capture")
+    fields, _ = request.getfixturevalue("pal_oracle" if system == "PAL" else "ntsc_oracle")
+    good = [f for f in fields if "error" not in f]
+    from vhsd_gb300 import native
+    prof = native.PROFILE_PAL if system == "PAL" else native.PROFILE_NTSC
+    with native.Session(prof, len(rf), precision=precision) as s:
+        r = s.decode(rf)
+        assert r.fields == len(good)
+        tb = s.tbc()
+        for i, f in enumerate(good):
+            info = s.field(i)
+            assert bool(info.is_first_field) == f["first_field"]
+            assert info.span_start == f["span_start"]
+            locs = s.lines(i)
+            assert np.max(np.abs(locs - f["locs"])) < LINE_TOL
+            d = np.abs(tb[i].astype(np.int64).ravel() - f["tbc"].astype(np.int64))
+            assert np.mean(d <= 1) >= LSB_FRACTION, (i, np.mean(d <= 1), d.max())
+            assert s.dropouts(i) == [tuple(x) for x in f["dropouts"]]
+
+
+def test_decode_is_deterministic(gpu, pal_capture):
+    from vhsd_gb300 import native
+    rf, _ = pal_capture
+    with native.Session(native.PROFILE_PAL, len(rf)) as s:
+        s.decode(rf)
+        a = s.tbc().copy()
+        s.decode(rf)
+        b = s.tbc()
+    assert a.tobytes() == b.tobytes()
+
+
+def test_device_input_pointer_path(gpu, pal_capture):
+    import torch
+    from vhsd_gb300 import native
+    rf, _ = pal_capture
+    d = torch.from_numpy(rf.copy()).cuda()
+    with native.Session(native.PROFILE_PAL, len(rf)) as s:
+        s.decode(rf)
+        host = s.tbc().copy()
+        s.decode(None, device_ptr=d.data_ptr(), count=len(rf))
+        dev = s.tbc()
+    assert host.tobytes() == dev.tobytes()

@@ -1,0 +1,1007 @@
+// C ABI and device session of the GB300 RF decode backend.
+//
+// Mirrors the bridge conventions of the reference's cuda-fast library
+// (src/VHSDecode.CudaFast.Native/src/vhsdecode_cuda_fast.cpp): strict
+// struct_size checks (:210-214, :249-254), a thread-local last error (:23-28),
+// every exception caught at the boundary (:367-377), cancellation polled
+// through a monotonic latch (src/cancellation_latch.h) and the callback.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#define VHSDECODE_GB300_EXPORTS 1
+#include "../../include/vhsdecode_gb300.h"
+#include "control.hpp"
+#include "filters.hpp"
+#include "formats.hpp"
+#include "kernels.h"
+
+namespace vhsd {
+template <typename T>
+cudaError_t launch_tbc_pw(const T*, int64_t, const TbcParams&, const double*, cudaStream_t);
+}
+
+using namespace vhsd;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+struct Failure : std::runtime_error {
+    int32_t status;
+    Failure(int32_t s, const std::string& m) : std::runtime_error(m), status(s) {}
+};
+
+int32_t fail(int32_t status, const std::string& msg) {
+    g_last_error = msg;
+    return status;
+}
+
+void ck(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) {
+        int32_t st = (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver ||
+                      e == cudaErrorInitializationError)
+                         ? VHSDECODE_GB300_STATUS_CUDA_UNAVAILABLE
+                         : VHSDECODE_GB300_STATUS_INTERNAL_ERROR;
+        throw Failure(st, std::string(what) + ": " + cudaGetErrorString(e));
+    }
+}
+
+template <typename F>
+int32_t guard(F&& f) {
+    try {
+        int32_t r = f();
+        if (r == VHSDECODE_GB300_STATUS_OK) g_last_error.clear();
+        return r;
+    } catch (const Failure& e) {
+        return fail(e.status, e.what());
+    } catch (const std::bad_alloc&) {
+        return fail(VHSDECODE_GB300_STATUS_INTERNAL_ERROR, "host allocation failed");
+    } catch (const std::exception& e) {
+        return fail(VHSDECODE_GB300_STATUS_INTERNAL_ERROR, e.what());
+    } catch (...) {
+        return fail(VHSDECODE_GB300_STATUS_INTERNAL_ERROR, "unknown native failure");
+    }
+}
+
+bool format_for(uint32_t profile, uint32_t speed, FormatParams& f) {
+    if (speed != VHSDECODE_GB300_TAPE_SPEED_SP) return false;
+    if (profile == VHSDECODE_GB300_PROFILE_PAL) { f = pal_vhs_sp(); return true; }
+    if (profile == VHSDECODE_GB300_PROFILE_NTSC) { f = ntsc_vhs_sp(); return true; }
+    return false;
+}
+
+// Kaiser-windowed sinc LUT, TbcLineResampler.BuildKaiserSincLookup (Core/Tbc/TbcLineResampler.cs:1297-1330).
+double bessel_i0(double x) {
+    double sum = 1.0, y = (x * x) / 4.0, term = 1.0;
+    for (int k = 1; k < 100; k++) {
+        term *= y / ((double)k * (double)k);
+        double next = sum + term;
+        if (next == sum) break;
+        sum = next;
+    }
+    return sum;
+}
+std::vector<float> build_sinc_lut() {
+    const int taps = 16, phases = 65536, half = 8;
+    const double beta = 5.0, pi = 3.14159265358979323846;
+    std::vector<float> lut((size_t)(phases + 1) * taps);
+    double i0b = bessel_i0(beta);
+    double w[16];
+    for (int p = 0; p < phases; p++) {
+        double phase = (double)p / phases, sum = 0.0;
+        for (int t = 0; t < taps; t++) {
+            double x = (double)((half - 1) - t) + phase;
+            double s = x == 0.0 ? 1.0 : std::sin(pi * x) / (pi * x);
+            double r = x / half;
+            double kw = (r < -1.0 || r > 1.0) ? 0.0 : bessel_i0(beta * std::sqrt(1.0 - r * r)) / i0b;
+            w[t] = s * kw;
+            sum += w[t];
+        }
+        for (int t = 0; t < taps; t++) lut[(size_t)p * taps + t] = (float)(w[t] / sum);
+    }
+    for (int t = 0; t < taps; t++) lut[(size_t)phases * taps + t] = lut[(size_t)(phases - 1) * taps + t];
+    return lut;
+}
+
+template <typename T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    void alloc(size_t count) {
+        release();
+        if (count == 0) return;
+        ck(cudaMalloc(&p, count * sizeof(T)), "cudaMalloc");
+        n = count;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    ~DevBuf() { release(); }
+};
+
+struct FieldRec {
+    FieldSync sync;
+    int64_t span_start;
+    int64_t span_len;
+    std::vector<double> refined;
+    std::vector<int32_t> drop;  // triplets
+};
+
+inline int64_t block_count(uint64_t n) {
+    return n < (uint64_t)kBlock ? 0 : (int64_t)((n - kBlock) / kStride + 1);
+}
+
+}  // namespace
+
+struct vhsdecode_gb300_session {
+    FormatParams fmt;
+    SyncParams sp;
+    FilterSpectra filt;
+    double fs = 40e6;
+    int precision = 0;
+    int device = 0;
+    uint64_t max_samples = 0;
+    int64_t max_blocks = 0;
+    int max_fields = 0;
+    int lines = 0;       // processed lines per field
+    int out_lines = 0;
+    int outlen = 0;
+    int num_sms = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[6] = {};
+    // device data
+    DevBuf<int16_t> rf;
+    DevBuf<float> v32, s32, e32;
+    DevBuf<double> v64, s64, e64;
+    DevBuf<float> rfv32;
+    DevBuf<float2> vid32, syn32, tw_hi, tw_lo;
+    DevBuf<double> rfv64;
+    DevBuf<double2> vid64, syn64;
+    DevBuf<float2> scratch;
+    DevBuf<float> scratch_raw;
+    DevBuf<int> repair;
+    DevBuf<double2> pwork;
+    DevBuf<double> pdwork;
+    DevBuf<float> pfwork;
+    DevBuf<int> pflag;
+    DevBuf<unsigned> pmask;
+    DevBuf<int64_t> pblk;
+    cudaGraphExec_t plain_graph = nullptr;
+    const int16_t* graph_rf = nullptr;   // input pointer baked into plain_graph
+    DevBuf<int64_t> pc_counts, pc_offsets, pc_events, pc_total;
+    int64_t pc_capacity = 0;
+    DevBuf<double> locs_in, locs_out;
+    DevBuf<uint8_t> fill_in, fill_out;
+    DevBuf<int64_t> span_start_d, span_len_d;
+    DevBuf<int> first_line_d, start_line_d, end_line_d, line_off_d;
+    DevBuf<float> lut;
+    DevBuf<double> pw, level_work;
+    DevBuf<uint16_t> tbc;
+    DevBuf<int64_t> drop_range, drop_events;
+    DevBuf<float> drop_mean, drop_partial;
+    DevBuf<int> drop_counts, drop_out_count, drop_status;
+    DevBuf<int32_t> drop_out;
+    int drop_cap = 1024, drop_out_cap = 4096;
+    int64_t span_len = 0;
+    // host results
+    std::vector<FieldRec> fields;
+    int64_t last_blocks = 0;
+    int last_repairs = 0;
+
+    bool fp32() const { return precision == VHSDECODE_GB300_PRECISION_FP32_FUSED; }
+};
+
+namespace {
+
+int64_t read_length(const SyncParams& sp) {
+    int64_t line = (int64_t)std::nearbyint(sp.line_period_us * sp.mhz);
+    int64_t base = sp.pal ? line * 400 : (line * 350 / 16384) * 16384;
+    return (base / kBlock + 2) * kBlock;
+}
+
+void resolve_span(int64_t intended, int64_t read_len, int64_t& s0, int64_t& slen) {
+    int64_t rl = std::max<int64_t>(0, intended - kCut);
+    int64_t a0 = (rl / kBlock) * kBlock;
+    int64_t a1 = a0 + read_len;
+    int64_t first = a0 / kStride, last = a1 / kStride;
+    s0 = first * kStride;
+    slen = (last - first + 1) * kStride;
+}
+
+void session_init(vhsdecode_gb300_session* s, const vhsdecode_gb300_session_config_v1& c) {
+    if (!format_for(c.profile, c.tape_speed, s->fmt))
+        throw Failure(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT,
+                      "unsupported profile / tape speed (PAL or NTSC, SP)");
+    if (!(c.sample_rate_mhz > 0.0) || std::fabs(c.sample_rate_mhz - 40.0) > 1e-9)
+        throw Failure(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "sample_rate_mhz must be 40");
+    if (c.precision > 1) throw Failure(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "unknown precision");
+    s->fs = c.sample_rate_mhz * 1e6;
+    s->precision = (int)c.precision;
+    s->device = c.device_id;
+    s->max_samples = c.max_samples;
+    s->sp = SyncParams::make(s->fmt, s->fs);
+    s->filt = design_filters(s->fmt, s->fs);
+    s->lines = s->sp.output_lines + 10;
+    s->out_lines = s->sp.output_lines;
+    s->outlen = s->fmt.outlinelen;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0)
+        throw Failure(VHSDECODE_GB300_STATUS_CUDA_UNAVAILABLE, "no CUDA device available");
+    if (c.device_id < 0 || c.device_id >= ndev)
+        throw Failure(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "device_id out of range");
+    ck(cudaSetDevice(c.device_id), "cudaSetDevice");
+    cudaDeviceProp prop{};
+    ck(cudaGetDeviceProperties(&prop, c.device_id), "cudaGetDeviceProperties");
+    s->num_sms = prop.multiProcessorCount;
+    ck(cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    s->stream = s->own_stream;
+    for (auto& ev : s->ev) ck(cudaEventCreate(&ev), "cudaEventCreate");
+    s->max_blocks = block_count(c.max_samples);
+    int64_t stream_cap = std::max<int64_t>(1, s->max_blocks) * kStride;
+    double field_samples = s->fs / (2.0 * s->fmt.fps);
+    s->max_fields = c.max_fields ? (int)c.max_fields
+                                 : (int)(stream_cap / field_samples) + 4;
+    s->rf.alloc(std::max<uint64_t>(c.max_samples, 16) + 8);
+    const int H = kHalf;
+    if (s->fp32()) {
+        s->v32.alloc(stream_cap); s->s32.alloc(stream_cap); s->e32.alloc(stream_cap);
+        std::vector<float> rv(H);
+        std::vector<float2> vv(H), sv(H);
+        for (int k = 0; k < H; k++) {
+            rv[k] = (float)s->filt.rf_video[k];
+            vv[k] = make_float2((float)s->filt.video[k].real(), (float)s->filt.video[k].imag());
+            sv[k] = make_float2((float)s->filt.sync[k].real(), (float)s->filt.sync[k].imag());
+        }
+        s->rfv32.alloc(H); s->vid32.alloc(H); s->syn32.alloc(H);
+        ck(cudaMemcpy(s->rfv32.p, rv.data(), H * sizeof(float), cudaMemcpyHostToDevice), "upload");
+        ck(cudaMemcpy(s->vid32.p, vv.data(), H * sizeof(float2), cudaMemcpyHostToDevice), "upload");
+        ck(cudaMemcpy(s->syn32.p, sv.data(), H * sizeof(float2), cudaMemcpyHostToDevice), "upload");
+        std::vector<float2> hi(256), lo(128);
+        const double pi = 3.14159265358979323846;
+        for (int h = 0; h < 256; h++) {
+            double a = -2.0 * pi * (h * 128.0) / 32768.0;
+            hi[h] = make_float2((float)std::cos(a), (float)std::sin(a));
+        }
+        for (int l = 0; l < 128; l++) {
+            double a = -2.0 * pi * l / 32768.0;
+            lo[l] = make_float2((float)std::cos(a), (float)std::sin(a));
+        }
+        s->tw_hi.alloc(256); s->tw_lo.alloc(128);
+        ck(cudaMemcpy(s->tw_hi.p, hi.data(), 256 * sizeof(float2), cudaMemcpyHostToDevice), "upload");
+        ck(cudaMemcpy(s->tw_lo.p, lo.data(), 128 * sizeof(float2), cudaMemcpyHostToDevice), "upload");
+        int clusters = s->num_sms / 2;
+        s->scratch.alloc((size_t)clusters * 2 * kBlock);
+        s->scratch_raw.alloc((size_t)clusters * kBlock);
+        s->repair.alloc(1);
+    } else {
+        s->v64.alloc(stream_cap); s->s64.alloc(stream_cap); s->e64.alloc(stream_cap);
+        std::vector<double2> vv(H), sv(H);
+        for (int k = 0; k < H; k++) {
+            vv[k] = make_double2(s->filt.video[k].real(), s->filt.video[k].imag());
+            sv[k] = make_double2(s->filt.sync[k].real(), s->filt.sync[k].imag());
+        }
+        s->rfv64.alloc(H); s->vid64.alloc(H); s->syn64.alloc(H);
+        ck(cudaMemcpy(s->rfv64.p, s->filt.rf_video.data(), H * sizeof(double), cudaMemcpyHostToDevice), "upload");
+        ck(cudaMemcpy(s->vid64.p, vv.data(), H * sizeof(double2), cudaMemcpyHostToDevice), "upload");
+        ck(cudaMemcpy(s->syn64.p, sv.data(), H * sizeof(double2), cudaMemcpyHostToDevice), "upload");
+        s->pwork.alloc(4 * (size_t)kBlock);
+        s->pdwork.alloc(3 * (size_t)kBlock);
+        s->pfwork.alloc(kBlock + 16);
+        s->pflag.alloc(4);
+        s->pmask.alloc(1024);
+        s->pblk.alloc(1);
+        ck(cudaMemset(s->pflag.p, 0, 4 * sizeof(int)), "memset");
+    }
+    int64_t nchunks = (stream_cap + kPulseChunk - 1) / kPulseChunk;
+    s->pc_counts.alloc(nchunks);
+    s->pc_offsets.alloc(nchunks);
+    s->pc_capacity = stream_cap / 64 + 4096;
+    s->pc_events.alloc(s->pc_capacity);
+    s->pc_total.alloc(1);
+    size_t fl = (size_t)s->max_fields * s->lines;
+    s->locs_in.alloc(fl); s->locs_out.alloc(fl);
+    s->fill_in.alloc(fl); s->fill_out.alloc(fl);
+    s->span_start_d.alloc(s->max_fields);
+    s->span_len_d.alloc(s->max_fields);
+    s->first_line_d.alloc(s->max_fields); s->start_line_d.alloc(s->max_fields);
+    s->end_line_d.alloc(s->max_fields); s->line_off_d.alloc(s->max_fields);
+    std::vector<float> lut = build_sinc_lut();
+    s->lut.alloc(lut.size());
+    ck(cudaMemcpy(s->lut.p, lut.data(), lut.size() * sizeof(float), cudaMemcpyHostToDevice), "upload");
+    double smoothing = s->fmt.frame_lines / 2.0;
+    double alpha = 1.0 / (smoothing * s->outlen);
+    std::vector<double> pw((size_t)s->outlen);
+    for (int k = 0; k < s->outlen; k++) pw[(size_t)k] = std::pow(1.0 - alpha, (double)(k + 1));
+    s->pw.alloc(pw.size());
+    ck(cudaMemcpy(s->pw.p, pw.data(), pw.size() * sizeof(double), cudaMemcpyHostToDevice), "upload");
+    s->level_work.alloc((size_t)s->max_fields * 1024);
+    s->tbc.alloc((size_t)s->max_fields * s->out_lines * s->outlen);
+    s->span_len = read_length(s->sp) + 2 * kStride;  // upper bound of a resolved span
+    int nch = dropout_chunks(s->span_len);
+    s->drop_range.alloc((size_t)s->max_fields * 2);
+    s->drop_mean.alloc(s->max_fields);
+    s->drop_partial.alloc((size_t)s->max_fields * nch);
+    s->drop_counts.alloc((size_t)s->max_fields * nch);
+    s->drop_events.alloc((size_t)s->max_fields * nch * s->drop_cap);
+    s->drop_out.alloc((size_t)s->max_fields * s->drop_out_cap * 3);
+    s->drop_out_count.alloc(s->max_fields);
+    s->drop_status.alloc(s->max_fields);
+}
+
+void session_free(vhsdecode_gb300_session* s) {
+    if (s->plain_graph) cudaGraphExecDestroy(s->plain_graph);
+    for (auto& ev : s->ev) if (ev) cudaEventDestroy(ev);
+    if (s->own_stream) cudaStreamDestroy(s->own_stream);
+}
+
+void run_demod(vhsdecode_gb300_session* s, const int16_t* rf_dev, int64_t nblocks) {
+    if (nblocks <= 0) return;
+    if (s->fp32()) {
+        FastDemodParams p{};
+        p.rf = rf_dev;
+        p.first_block = 0;
+        p.nblocks = nblocks;
+        p.rf_video = s->rfv32.p;
+        p.video = s->vid32.p;
+        p.sync = s->syn32.p;
+        p.tw_hi = s->tw_hi.p;
+        p.tw_lo = s->tw_lo.p;
+        p.fs = (float)s->fs;
+        p.diff_max = (float)((s->fmt.ire0 + s->fmt.hz_ire * 100.0) * 2.0);
+        p.dc = (float)s->fmt.ire0;
+        p.env_b0 = (float)s->filt.env_b0;
+        p.env_b1 = (float)s->filt.env_b1;
+        p.env_a1 = (float)s->filt.env_a1;
+        p.video_out = s->v32.p;
+        p.sync_out = s->s32.p;
+        p.env_out = s->e32.p;
+        p.scratch = s->scratch.p;
+        p.scratch_raw = s->scratch_raw.p;
+        p.repair_count = s->repair.p;
+        ck(cudaMemsetAsync(s->repair.p, 0, sizeof(int), s->stream), "memset");
+        ck(launch_demod_fp32(p, s->num_sms / 2, s->stream), "demod fp32 launch");
+    } else {
+        PlainDemodParams p{};
+        p.rf = rf_dev;
+        p.rf_video = s->rfv64.p;
+        p.video = s->vid64.p;
+        p.sync = s->syn64.p;
+        p.fs = s->fs;
+        p.diff_max = (s->fmt.ire0 + s->fmt.hz_ire * 100.0) * 2.0;
+        p.env_b0 = s->filt.env_b0;
+        p.env_b1 = s->filt.env_b1;
+        p.env_a1 = s->filt.env_a1;
+        p.video_out = s->v64.p;
+        p.sync_out = s->s64.p;
+        p.env_out = s->e64.p;
+        p.work = s->pwork.p;
+        p.dwork = s->pdwork.p;
+        p.fwork = s->pfwork.p;
+        p.flag = s->pflag.p;
+        p.mask = s->pmask.p;
+        p.blk = s->pblk.p;
+        // The capture lives in s->rf or a caller buffer; the graph bakes the
+        // pointer, so rebuild it when the input pointer changes.
+        if (!s->plain_graph || s->graph_rf != rf_dev) {
+            if (s->plain_graph) { cudaGraphExecDestroy(s->plain_graph); s->plain_graph = nullptr; }
+            cudaStream_t cs;
+            ck(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "stream");
+            cudaGraph_t g;
+            ck(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "capture");
+            cudaError_t le = launch_demod_fp64_block(p, cs);
+            cudaError_t ce = cudaStreamEndCapture(cs, &g);
+            cudaStreamDestroy(cs);
+            ck(le, "plain launch");
+            ck(ce, "end capture");
+            ck(cudaGraphInstantiate(&s->plain_graph, g, 0), "graph instantiate");
+            cudaGraphDestroy(g);
+            s->graph_rf = rf_dev;
+        }
+        int64_t zero = 0;
+        ck(cudaMemcpyAsync(s->pblk.p, &zero, sizeof(int64_t), cudaMemcpyHostToDevice, s->stream), "blk");
+        for (int64_t b = 0; b < nblocks; b++) ck(cudaGraphLaunch(s->plain_graph, s->stream), "graph launch");
+    }
+}
+
+template <typename T>
+void run_fields(vhsdecode_gb300_session* s, const T* video, const T* sync, const T* env,
+                int64_t stream_len, uint32_t max_fields, uint32_t& stop_reason, double& host_ms,
+                const std::atomic<bool>* cancel) {
+    const SyncParams& sp = s->sp;
+    double threshold = sp.ire_to_hz(sp.vsync_ire / 2.0);
+    ck(launch_pulse_events<T>(sync, stream_len, threshold, s->pc_counts.p, s->pc_offsets.p,
+                              s->pc_events.p, s->pc_capacity, s->pc_total.p, s->stream),
+       "pulse launch");
+    int64_t total = 0;
+    ck(cudaMemcpyAsync(&total, s->pc_total.p, sizeof(int64_t), cudaMemcpyDeviceToHost, s->stream), "d2h");
+    ck(cudaStreamSynchronize(s->stream), "sync");
+    if (total > s->pc_capacity)
+        throw Failure(VHSDECODE_GB300_STATUS_DECODE_ERROR, "sync pulse event capacity exceeded");
+    std::vector<int64_t> events((size_t)total);
+    if (total > 0)
+        ck(cudaMemcpy(events.data(), s->pc_events.p, (size_t)total * sizeof(int64_t),
+                      cudaMemcpyDeviceToHost), "d2h events");
+    auto t0 = std::chrono::steady_clock::now();
+    int64_t read_len = read_length(sp);
+    int64_t min_len = std::max<int64_t>(0, (int64_t)std::ceil(sp.usec(sp.eq_us) / 8.0));
+    int64_t max_len = std::max<int64_t>(1, (int64_t)(sp.nominal * 5.0));
+    FieldState st;
+    int64_t intended = 0;
+    s->fields.clear();
+    stop_reason = 0;
+    while (true) {
+        if (cancel && cancel->load()) throw Failure(VHSDECODE_GB300_STATUS_CANCELLED, "decode cancelled");
+        if ((int)s->fields.size() >= s->max_fields) { stop_reason = 1; break; }
+        if (max_fields && s->fields.size() >= max_fields) { stop_reason = 1; break; }
+        int64_t s0, slen;
+        resolve_span(intended, read_len, s0, slen);
+        if (s0 + slen > stream_len) break;
+        std::vector<Pulse> raw = span_pulses(events.data(), total, s0, slen, min_len, max_len);
+        RefFetch fetch = [&](int64_t start, int64_t len, std::vector<double>& out) {
+            std::vector<T> tmp((size_t)len);
+            ck(cudaMemcpy(tmp.data(), sync + s0 + start, (size_t)len * sizeof(T), cudaMemcpyDeviceToHost),
+               "rescue fetch");
+            out.assign(tmp.begin(), tmp.end());
+        };
+        FieldRec rec;
+        rec.sync = analyse_field(sp, raw, slen, st, fetch);
+        rec.span_start = s0;
+        rec.span_len = slen;
+        if (!rec.sync.ok) { stop_reason = 2; break; }
+        intended = s0 + std::max<int64_t>(1, (int64_t)round_away(rec.sync.next_offset));
+        s->fields.push_back(std::move(rec));
+    }
+    auto t1 = std::chrono::steady_clock::now();
+    host_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+    int nf = (int)s->fields.size();
+    if (nf == 0) return;
+    // per-field arrays
+    std::vector<double> locs((size_t)nf * s->lines);
+    std::vector<uint8_t> fill((size_t)nf * s->lines);
+    std::vector<int64_t> span((size_t)nf), slens((size_t)nf);
+    std::vector<int> fline(nf), sline(nf), eline(nf), loff(nf);
+    for (int f = 0; f < nf; f++) {
+        const FieldSync& fs = s->fields[(size_t)f].sync;
+        std::copy(fs.locs.begin(), fs.locs.end(), locs.begin() + (size_t)f * s->lines);
+        std::copy(fs.filled.begin(), fs.filled.end(), fill.begin() + (size_t)f * s->lines);
+        span[(size_t)f] = s->fields[(size_t)f].span_start;
+        slens[(size_t)f] = s->fields[(size_t)f].span_len;
+        fline[f] = sp.pal ? (fs.first_field ? 3 : 4) : 1;
+        loff[f] = sp.pal ? (fs.first_field ? 2 : 3) : 0;
+        sline[f] = loff[f] + 1;
+        eline[f] = std::min(s->lines - 1, sp.field_lines(fs.first_field) + sline[f] + 1);
+    }
+    cudaStream_t cs = s->stream;
+    ck(cudaMemcpyAsync(s->locs_in.p, locs.data(), locs.size() * sizeof(double), cudaMemcpyHostToDevice, cs), "h2d");
+    ck(cudaMemcpyAsync(s->fill_in.p, fill.data(), fill.size(), cudaMemcpyHostToDevice, cs), "h2d");
+    ck(cudaMemcpyAsync(s->span_start_d.p, span.data(), span.size() * sizeof(int64_t), cudaMemcpyHostToDevice, cs), "h2d");
+    ck(cudaMemcpyAsync(s->span_len_d.p, slens.data(), slens.size() * sizeof(int64_t), cudaMemcpyHostToDevice, cs), "h2d");
+    ck(cudaMemcpyAsync(s->first_line_d.p, fline.data(), nf * sizeof(int), cudaMemcpyHostToDevice, cs), "h2d");
+    ck(cudaMemcpyAsync(s->start_line_d.p, sline.data(), nf * sizeof(int), cudaMemcpyHostToDevice, cs), "h2d");
+    ck(cudaMemcpyAsync(s->end_line_d.p, eline.data(), nf * sizeof(int), cudaMemcpyHostToDevice, cs), "h2d");
+    ck(cudaMemcpyAsync(s->line_off_d.p, loff.data(), nf * sizeof(int), cudaMemcpyHostToDevice, cs), "h2d");
+    // the span-copies above read host vectors that stay alive until the sync below
+    HsyncParams hp{};
+    hp.nfields = nf;
+    hp.lines = s->lines;
+    hp.locs_in = s->locs_in.p;
+    hp.filled_in = s->fill_in.p;
+    hp.locs_out = s->locs_out.p;
+    hp.filled_out = s->fill_out.p;
+    hp.span_start = s->span_start_d.p;
+    hp.span_len = s->span_len_d.p;
+    hp.pal = sp.pal ? 1 : 0;
+    hp.threshold = threshold;
+    hp.one_us = std::max(1, (int)sp.mhz);
+    hp.normal_hsync = std::max(1, (int)sp.usec(sp.hsync_us));
+    hp.mhz32 = (double)(float)sp.mhz;
+    hp.ire0 = sp.ire0;
+    hp.hz_ire = sp.hz_ire;
+    hp.ntsc_shift = sp.pal ? 0.0 : ((117.25 / 360.0) / sp.fsc_mhz) * sp.mhz;
+    ck(launch_hsync_refine<T>(sync, stream_len, hp, cs), "hsync launch");
+    TbcParams tp{};
+    tp.nfields = nf;
+    tp.lines = s->lines;
+    tp.locs = s->locs_out.p;
+    tp.span_start = s->span_start_d.p;
+    tp.span_len = s->span_len_d.p;
+    tp.first_line = s->first_line_d.p;
+    tp.out_lines = s->out_lines;
+    tp.outlen = s->outlen;
+    tp.nominal = std::nearbyint(s->fmt.line_period_us * sp.mhz);
+    tp.smoothing = s->fmt.frame_lines / 2.0;
+    tp.lut = s->lut.p;
+    tp.ire0 = s->fmt.ire0;
+    tp.output_scale = output_scale(s->fmt);
+    tp.inv_hz_ire = 1.0 / s->fmt.hz_ire;
+    tp.offset = (s->fmt.output_zero + 0.5) - (s->fmt.vsync_ire * tp.output_scale);
+    tp.out_u16 = s->tbc.p;
+    tp.out_hz = nullptr;
+    tp.level_work = s->level_work.p;
+    ck(launch_tbc_pw<T>(video, stream_len, tp, s->pw.p, cs), "tbc launch");
+    DropoutParams dp{};
+    dp.nfields = nf;
+    dp.span_start = s->span_start_d.p;
+    dp.span_len = s->span_len_d.p;
+    dp.max_span_len = s->span_len;
+    dp.locs = s->locs_out.p;
+    dp.lines = s->lines;
+    dp.start_line = s->start_line_d.p;
+    dp.end_line = s->end_line_d.p;
+    dp.line_offset = s->line_off_d.p;
+    dp.outlen = s->outlen;
+    dp.range = s->drop_range.p;
+    dp.frac = 0.18f;
+    dp.hyst = 1.25;
+    dp.merge = 30;
+    dp.min_len = 10;
+    dp.mean_out = s->drop_mean.p;
+    dp.events = s->drop_events.p;
+    dp.cap = s->drop_cap;
+    dp.out = s->drop_out.p;
+    dp.out_cap = s->drop_out_cap;
+    dp.out_count = s->drop_out_count.p;
+    dp.status = s->drop_status.p;
+    ck(launch_dropouts_full<T>(env, stream_len, dp, s->drop_partial.p, s->drop_counts.p, cs),
+       "dropout launch");
+    std::vector<double> refined((size_t)nf * s->lines);
+    std::vector<int> dcount(nf), dstat(nf);
+    ck(cudaMemcpyAsync(refined.data(), s->locs_out.p, refined.size() * sizeof(double), cudaMemcpyDeviceToHost, cs), "d2h");
+    ck(cudaMemcpyAsync(dcount.data(), s->drop_out_count.p, nf * sizeof(int), cudaMemcpyDeviceToHost, cs), "d2h");
+    ck(cudaMemcpyAsync(dstat.data(), s->drop_status.p, nf * sizeof(int), cudaMemcpyDeviceToHost, cs), "d2h");
+    ck(cudaStreamSynchronize(cs), "sync");
+    for (int f = 0; f < nf; f++) {
+        FieldRec& r = s->fields[(size_t)f];
+        r.refined.assign(refined.begin() + (size_t)f * s->lines, refined.begin() + (size_t)(f + 1) * s->lines);
+        if (dstat[f] != 0)
+            throw Failure(VHSDECODE_GB300_STATUS_DECODE_ERROR, "dropout event capacity exceeded");
+        int c = std::min(dcount[f], s->drop_out_cap);
+        r.drop.resize((size_t)c * 3);
+        if (c > 0)
+            ck(cudaMemcpy(r.drop.data(), s->drop_out.p + (size_t)f * s->drop_out_cap * 3,
+                          (size_t)c * 3 * sizeof(int32_t), cudaMemcpyDeviceToHost), "d2h dropouts");
+    }
+}
+
+int32_t decode_impl(vhsdecode_gb300_session* s, const int16_t* rf, uint64_t n, uint32_t max_fields,
+                    uint32_t flags, vhsdecode_gb300_decode_result_v1* res,
+                    const std::atomic<bool>* cancel = nullptr) {
+    if (n > s->max_samples)
+        throw Failure(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "sample_count exceeds the session capacity");
+    ck(cudaSetDevice(s->device), "cudaSetDevice");
+    cudaStream_t cs = s->stream;
+    int64_t nblocks = block_count(n);
+    const int16_t* rf_dev = rf;
+    ck(cudaEventRecord(s->ev[0], cs), "event");
+    if (!(flags & VHSDECODE_GB300_DECODE_DEVICE_INPUT)) {
+        if (n > 0) ck(cudaMemcpyAsync(s->rf.p, rf, n * sizeof(int16_t), cudaMemcpyHostToDevice, cs), "h2d rf");
+        rf_dev = s->rf.p;
+    } else if (((uintptr_t)rf & 15u) != 0) {
+        throw Failure(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "device rf pointer must be 16-byte aligned");
+    }
+    ck(cudaEventRecord(s->ev[1], cs), "event");
+    run_demod(s, rf_dev, nblocks);
+    ck(cudaEventRecord(s->ev[2], cs), "event");
+    int64_t stream_len = nblocks * kStride;
+    uint32_t stop = 0;
+    double host_ms = 0.0;
+    s->fields.clear();
+    if (!(flags & VHSDECODE_GB300_DECODE_DEMOD_ONLY) && nblocks > 0) {
+        if (s->fp32()) run_fields<float>(s, s->v32.p, s->s32.p, s->e32.p, stream_len, max_fields, stop, host_ms, cancel);
+        else run_fields<double>(s, s->v64.p, s->s64.p, s->e64.p, stream_len, max_fields, stop, host_ms, cancel);
+    }
+    ck(cudaEventRecord(s->ev[3], cs), "event");
+    ck(cudaEventSynchronize(s->ev[3]), "sync");
+    int rep = 0;
+    if (s->fp32() && nblocks > 0)
+        ck(cudaMemcpy(&rep, s->repair.p, sizeof(int), cudaMemcpyDeviceToHost), "d2h");
+    s->last_blocks = nblocks;
+    s->last_repairs = rep;
+    if (res) {
+        float t_all = 0, t_dem = 0, t_fld = 0;
+        cudaEventElapsedTime(&t_all, s->ev[0], s->ev[3]);
+        cudaEventElapsedTime(&t_dem, s->ev[1], s->ev[2]);
+        cudaEventElapsedTime(&t_fld, s->ev[2], s->ev[3]);
+        res->fields = (uint32_t)s->fields.size();
+        res->output_line_length = (uint32_t)s->outlen;
+        res->output_field_lines = (uint32_t)s->out_lines;
+        res->blocks = (uint64_t)nblocks;
+        res->stream_samples = (uint64_t)stream_len;
+        res->repaired_blocks = (uint32_t)rep;
+        res->stop_reason = stop;
+        res->device_ms = t_all;
+        res->demod_ms = t_dem;
+        res->field_ms = t_fld;
+        res->host_ms = host_ms;
+    }
+    return VHSDECODE_GB300_STATUS_OK;
+}
+
+// RAII owner of a session for run().
+struct SessionHolder {
+    vhsdecode_gb300_session* s = nullptr;
+    ~SessionHolder() {
+        if (s) {
+            cudaSetDevice(s->device);
+            if (s->stream) cudaStreamSynchronize(s->stream);
+            session_free(s);
+            delete s;
+        }
+    }
+};
+
+bool file_exists(const std::string& path) {
+    FILE* f = std::fopen(path.c_str(), "rb");
+    if (f) { std::fclose(f); return true; }
+    return false;
+}
+
+void write_json(const std::string& path, const vhsdecode_gb300_session* s) {
+    FILE* f = std::fopen(path.c_str(), "wb");
+    if (!f) throw Failure(VHSDECODE_GB300_STATUS_OUTPUT_ERROR, "cannot open " + path);
+    const FormatParams& fm = s->fmt;
+    std::fprintf(f, "{\n  \"videoParameters\": {\"system\": \"%s\", \"fieldWidth\": %d, "
+                    "\"fieldHeight\": %d, \"sampleRate\": %.1f, \"numberOfSequentialFields\": %zu, "
+                    "\"isSourcePal\": %s, \"black16bIre\": %d, \"white16bIre\": %d},\n  \"fields\": [",
+                 fm.pal ? "PAL" : "NTSC", s->outlen, s->out_lines, fm.outfreq_mhz * 1e6, s->fields.size(),
+                 fm.pal ? "true" : "false",
+                 (int)std::lround(fm.output_zero + (0.0 - fm.vsync_ire) * output_scale(fm)),
+                 (int)std::lround(fm.output_zero + (100.0 - fm.vsync_ire) * output_scale(fm)));
+    for (size_t i = 0; i < s->fields.size(); i++) {
+        const FieldRec& r = s->fields[i];
+        long long file_loc = (long long)std::floor(r.span_start + r.sync.line0 + kCut);
+        std::fprintf(f, "%s\n    {\"seqNo\": %zu, \"isFirstField\": %s, \"fileLoc\": %lld",
+                     i ? "," : "", i + 1, r.sync.first_field ? "true" : "false", file_loc);
+        size_t nd = r.drop.size() / 3;
+        if (nd) {
+            std::fprintf(f, ", \"dropOuts\": {\"fieldLine\": [");
+            for (size_t k = 0; k < nd; k++) std::fprintf(f, "%s%d", k ? ", " : "", r.drop[3 * k]);
+            std::fprintf(f, "], \"startx\": [");
+            for (size_t k = 0; k < nd; k++) std::fprintf(f, "%s%d", k ? ", " : "", r.drop[3 * k + 1]);
+            std::fprintf(f, "], \"endx\": [");
+            for (size_t k = 0; k < nd; k++) std::fprintf(f, "%s%d", k ? ", " : "", r.drop[3 * k + 2]);
+            std::fprintf(f, "]}");
+        }
+        std::fprintf(f, "}");
+    }
+    std::fprintf(f, "\n  ]\n}\n");
+    if (std::fclose(f) != 0) throw Failure(VHSDECODE_GB300_STATUS_OUTPUT_ERROR, "cannot write " + path);
+}
+
+}  // namespace
+
+namespace vhsd {
+int32_t set_last_error(int32_t status, const char* msg) {
+    g_last_error = msg ? msg : "";
+    return status;
+}
+std::vector<float> sinc_lut_host() { return build_sinc_lut(); }
+}  // namespace vhsd
+
+extern "C" {
+
+VHSDECODE_GB300_API uint32_t VHSDECODE_GB300_CALL vhsdecode_gb300_get_abi_version(void) {
+    return VHSDECODE_GB300_ABI_VERSION;
+}
+
+VHSDECODE_GB300_API const char* VHSDECODE_GB300_CALL vhsdecode_gb300_get_last_error(void) {
+    return g_last_error.c_str();
+}
+
+VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_get_runtime_info(
+    int32_t device_id, vhsdecode_gb300_runtime_info_v1* info) {
+    return guard([&]() -> int32_t {
+        if (!info) return fail(VHSDECODE_GB300_STATUS_NULL_POINTER, "info is null");
+        if (info->struct_size != sizeof(vhsdecode_gb300_runtime_info_v1))
+            return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "runtime_info struct_size mismatch");
+        int n = 0;
+        if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0)
+            return fail(VHSDECODE_GB300_STATUS_CUDA_UNAVAILABLE, "no CUDA device available");
+        if (device_id < 0 || device_id >= n)
+            return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "device_id out of range");
+        cudaDeviceProp p{};
+        ck(cudaGetDeviceProperties(&p, device_id), "cudaGetDeviceProperties");
+        ck(cudaSetDevice(device_id), "cudaSetDevice");
+        size_t fr = 0, tot = 0;
+        ck(cudaMemGetInfo(&fr, &tot), "cudaMemGetInfo");
+        info->abi_version = VHSDECODE_GB300_ABI_VERSION;
+        info->device_id = device_id;
+        info->compute_major = p.major;
+        info->compute_minor = p.minor;
+        info->multiprocessor_count = p.multiProcessorCount;
+        info->total_vram_bytes = tot;
+        info->free_vram_bytes = fr;
+        std::snprintf(info->device_name, VHSDECODE_GB300_NAME_CAPACITY, "%s", p.name);
+        return VHSDECODE_GB300_STATUS_OK;
+    });
+}
+
+VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_run(
+    const vhsdecode_gb300_config_v1* config, vhsdecode_gb300_result_v1* result) {
+    return guard([&]() -> int32_t {
+        if (!config || !result) return fail(VHSDECODE_GB300_STATUS_NULL_POINTER, "null argument");
+        if (config->struct_size != sizeof(vhsdecode_gb300_config_v1))
+            return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "config struct_size mismatch");
+        if (result->struct_size != sizeof(vhsdecode_gb300_result_v1))
+            return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "result struct_size mismatch");
+        if (!config->read_callback) return fail(VHSDECODE_GB300_STATUS_NULL_POINTER, "read_callback is null");
+        if (!config->output_base_utf8 || !config->output_base_utf8[0])
+            return fail(VHSDECODE_GB300_STATUS_NULL_POINTER, "output_base_utf8 is null");
+        if (config->input_sample_format != VHSDECODE_GB300_INPUT_INT16)
+            return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "only int16 input is supported");
+        if (config->device_decimation_factor != 1)
+            return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "device_decimation_factor must be 1");
+        auto t0 = std::chrono::steady_clock::now();
+        std::string base = config->output_base_utf8;
+        std::string tbc_path = base + ".tbc", json_path = base + ".tbc.json";
+        if (!config->overwrite && (file_exists(tbc_path) || file_exists(json_path)))
+            return fail(VHSDECODE_GB300_STATUS_OUTPUT_ERROR, "output exists and overwrite is off");
+        auto cancelled = [&]() { return config->cancel_callback && config->cancel_callback(config->user_data) != 0; };
+        // pull the capture through the callback
+        std::vector<int16_t> rf;
+        const size_t chunk = (size_t)1 << 22;
+        uint64_t want = config->total_samples;
+        while (want == 0 || rf.size() < want) {
+            if (cancelled()) return fail(VHSDECODE_GB300_STATUS_CANCELLED, "decode cancelled");
+            size_t ask = chunk;
+            if (want) ask = (size_t)std::min<uint64_t>(chunk, want - rf.size());
+            size_t old = rf.size();
+            rf.resize(old + ask);
+            size_t got = config->read_callback(config->user_data, rf.data() + old, old, ask);
+            if (got > ask) return fail(VHSDECODE_GB300_STATUS_INPUT_ERROR, "read callback overran its buffer");
+            rf.resize(old + got);
+            if (got < ask) break;
+        }
+        if (rf.size() < (size_t)kBlock) return fail(VHSDECODE_GB300_STATUS_INPUT_ERROR, "input shorter than one block");
+        vhsdecode_gb300_session_config_v1 sc{};
+        sc.struct_size = sizeof(sc);
+        sc.profile = config->profile;
+        sc.tape_speed = config->tape_speed;
+        sc.device_id = config->device_id;
+        sc.sample_rate_mhz = config->sample_rate_mhz;
+        sc.max_samples = rf.size();
+        sc.precision = VHSDECODE_GB300_PRECISION_FP32_FUSED;
+        SessionHolder h;
+        h.s = new vhsdecode_gb300_session();
+        session_init(h.s, sc);
+        if (cancelled()) return fail(VHSDECODE_GB300_STATUS_CANCELLED, "decode cancelled");
+        vhsdecode_gb300_decode_result_v1 dr{};
+        dr.struct_size = sizeof(dr);
+        decode_impl(h.s, rf.data(), rf.size(), config->maximum_output_fields, 0, &dr);
+        if (cancelled()) return fail(VHSDECODE_GB300_STATUS_CANCELLED, "decode cancelled");
+        size_t per = (size_t)h.s->out_lines * h.s->outlen;
+        std::vector<uint16_t> tbc(per * h.s->fields.size());
+        if (!tbc.empty())
+            ck(cudaMemcpy(tbc.data(), h.s->tbc.p, tbc.size() * sizeof(uint16_t), cudaMemcpyDeviceToHost), "d2h tbc");
+        FILE* f = std::fopen(tbc_path.c_str(), "wb");
+        if (!f) return fail(VHSDECODE_GB300_STATUS_OUTPUT_ERROR, "cannot open " + tbc_path);
+        size_t wrote = tbc.empty() ? 0 : std::fwrite(tbc.data(), sizeof(uint16_t), tbc.size(), f);
+        int cerr = std::fclose(f);
+        if (wrote != tbc.size() || cerr != 0) return fail(VHSDECODE_GB300_STATUS_OUTPUT_ERROR, "cannot write " + tbc_path);
+        write_json(json_path, h.s);
+        result->fields_written = (uint32_t)h.s->fields.size();
+        result->output_line_length = (uint32_t)h.s->outlen;
+        result->output_field_lines = (uint32_t)h.s->out_lines;
+        result->elapsed_seconds =
+            std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        return VHSDECODE_GB300_STATUS_OK;
+    });
+}
+
+VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_session_create(
+    const vhsdecode_gb300_session_config_v1* config, vhsdecode_gb300_session** session) {
+    return guard([&]() -> int32_t {
+        if (!config || !session) return fail(VHSDECODE_GB300_STATUS_NULL_POINTER, "null argument");
+        *session = nullptr;
+        if (config->struct_size != sizeof(vhsdecode_gb300_session_config_v1))
+            return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "session_config struct_size mismatch");
+        std::unique_ptr<vhsdecode_gb300_session> s(new vhsdecode_gb300_session());
+        try {
+            session_init(s.get(), *config);
+        } catch (...) {
+            session_free(s.get());
+            throw;
+        }
+        *session = s.release();
+        return VHSDECODE_GB300_STATUS_OK;
+    });
+}
+
+VHSDECODE_GB300_API void VHSDECODE_GB300_CALL vhsdecode_gb300_session_destroy(vhsdecode_gb300_session* s) {
+    if (!s) return;
+    cudaSetDevice(s->device);
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    session_free(s);
+    delete s;
+}
+
+VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_session_set_stream(
+    vhsdecode_gb300_session* s, void* cuda_stream) {
+    return guard([&]() -> int32_t {
+        if (!s) return fail(VHSDECODE_GB300_STATUS_NULL_POINTER, "session is null");
+        s->stream = cuda_stream ? (cudaStream_t)cuda_stream : s->own_stream;
+        return VHSDECODE_GB300_STATUS_OK;
+    });
+}
+
+VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_session_decode(
+    vhsdecode_gb300_session* s, const int16_t* rf, uint64_t n, uint32_t max_fields, uint32_t flags,
+    vhsdecode_gb300_decode_result_v1* res) {
+    return guard([&]() -> int32_t {
+        if (!s || (!rf && n > 0)) return fail(VHSDECODE_GB300_STATUS_NULL_POINTER, "null argument");
+        if (res && res->struct_size != sizeof(vhsdecode_gb300_decode_result_v1))
+            return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "decode_result struct_size mismatch");
+        return decode_impl(s, rf, n, max_fields, flags, res);
+    });
+}
+
+VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_session_get_field(
+    vhsdecode_gb300_session* s, uint32_t index, vhsdecode_gb300_field_info_v1* info) {
+    return guard([&]() -> int32_t {
+        if (!s || !info) return fail(VHSDECODE_GB300_STATUS_NULL_POINTER, "null argument");
+        if (info->struct_size != sizeof(vhsdecode_gb300_field_info_v1))
+            return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "field_info struct_size mismatch");
+        if (index >= s->fields.size()) return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "field index out of range");
+        const FieldRec& r = s->fields[index];
+        info->is_first_field = r.sync.first_field ? 1 : 0;
+        info->span_start = r.span_start;
+        info->file_loc = (int64_t)std::floor(r.span_start + r.sync.line0 + kCut);
+        info->line0 = r.sync.line0;
+        info->first_hsync = r.sync.first_hsync;
+        info->mean_line_length = r.sync.mean_line;
+        info->next_field_offset = r.sync.next_offset;
+        info->line_count = (uint32_t)r.refined.size();
+        info->dropout_count = (uint32_t)(r.drop.size() / 3);
+        return VHSDECODE_GB300_STATUS_OK;
+    });
+}
+
+VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_session_copy_tbc(
+    vhsdecode_gb300_session* s, uint32_t first, uint32_t count, uint16_t* dst) {
+    return guard([&]() -> int32_t {
+        if (!s || (!dst && count)) return fail(VHSDECODE_GB300_STATUS_NULL_POINTER, "null argument");
+        if ((uint64_t)first + count > s->fields.size())
+            return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "field range out of range");
+        size_t per = (size_t)s->out_lines * s->outlen;
+        if (count)
+            ck(cudaMemcpyAsync(dst, s->tbc.p + (size_t)first * per, (size_t)count * per * sizeof(uint16_t),
+                               cudaMemcpyDeviceToHost, s->stream), "d2h tbc");
+        ck(cudaStreamSynchronize(s->stream), "sync");
+        return VHSDECODE_GB300_STATUS_OK;
+    });
+}
+
+VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_session_copy_lines(
+    vhsdecode_gb300_session* s, uint32_t field, double* dst, uint32_t cap) {
+    return guard([&]() -> int32_t {
+        if (!s || !dst) return fail(VHSDECODE_GB300_STATUS_NULL_POINTER, "null argument");
+        if (field >= s->fields.size()) return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "field index out of range");
+        const auto& r = s->fields[field].refined;
+        if (cap < r.size()) return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "capacity too small");
+        std::copy(r.begin(), r.end(), dst);
+        return VHSDECODE_GB300_STATUS_OK;
+    });
+}
+
+VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_session_copy_dropouts(
+    vhsdecode_gb300_session* s, uint32_t field, int32_t* line, int32_t* sx, int32_t* ex, uint32_t cap,
+    uint32_t* count) {
+    return guard([&]() -> int32_t {
+        if (!s || !count) return fail(VHSDECODE_GB300_STATUS_NULL_POINTER, "null argument");
+        if (field >= s->fields.size()) return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "field index out of range");
+        const auto& d = s->fields[field].drop;
+        uint32_t n = (uint32_t)(d.size() / 3);
+        *count = n;
+        if (n > cap) return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "capacity too small");
+        if (n && (!line || !sx || !ex)) return fail(VHSDECODE_GB300_STATUS_NULL_POINTER, "null output");
+        for (uint32_t i = 0; i < n; i++) { line[i] = d[3 * i]; sx[i] = d[3 * i + 1]; ex[i] = d[3 * i + 2]; }
+        return VHSDECODE_GB300_STATUS_OK;
+    });
+}
+
+VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_session_copy_stream(
+    vhsdecode_gb300_session* s, uint32_t channel, uint64_t start, uint64_t count, double* dst) {
+    return guard([&]() -> int32_t {
+        if (!s || (!dst && count)) return fail(VHSDECODE_GB300_STATUS_NULL_POINTER, "null argument");
+        if (channel > 2) return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "channel must be 0..2");
+        uint64_t len = (uint64_t)s->last_blocks * kStride;
+        if (start + count > len) return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "range beyond the stream");
+        ck(cudaStreamSynchronize(s->stream), "sync");
+        if (s->fp32()) {
+            const float* src = channel == 0 ? s->v32.p : channel == 1 ? s->s32.p : s->e32.p;
+            std::vector<float> tmp(count);
+            ck(cudaMemcpy(tmp.data(), src + start, count * sizeof(float), cudaMemcpyDeviceToHost), "d2h");
+            for (uint64_t i = 0; i < count; i++) dst[i] = tmp[i];
+        } else {
+            const double* src = channel == 0 ? s->v64.p : channel == 1 ? s->s64.p : s->e64.p;
+            ck(cudaMemcpy(dst, src + start, count * sizeof(double), cudaMemcpyDeviceToHost), "d2h");
+        }
+        return VHSDECODE_GB300_STATUS_OK;
+    });
+}
+
+VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_session_tbc_device(
+    vhsdecode_gb300_session* s, void** ptr, uint64_t* bytes) {
+    return guard([&]() -> int32_t {
+        if (!s || !ptr || !bytes) return fail(VHSDECODE_GB300_STATUS_NULL_POINTER, "null argument");
+        *ptr = s->tbc.p;
+        *bytes = (uint64_t)s->fields.size() * s->out_lines * s->outlen * sizeof(uint16_t);
+        return VHSDECODE_GB300_STATUS_OK;
+    });
+}
+
+VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_design_filters(
+    uint32_t profile, uint32_t speed, double mhz, double* rf_video, double* video, double* sync, double* env) {
+    return guard([&]() -> int32_t {
+        if (!rf_video || !video || !sync || !env) return fail(VHSDECODE_GB300_STATUS_NULL_POINTER, "null output");
+        FormatParams f;
+        if (!format_for(profile, speed, f)) return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "unsupported profile");
+        if (!(mhz > 0)) return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "sample rate must be positive");
+        FilterSpectra fs = design_filters(f, mhz * 1e6);
+        for (int k = 0; k < kHalf; k++) {
+            rf_video[k] = fs.rf_video[(size_t)k];
+            video[2 * k] = fs.video[(size_t)k].real();
+            video[2 * k + 1] = fs.video[(size_t)k].imag();
+            sync[2 * k] = fs.sync[(size_t)k].real();
+            sync[2 * k + 1] = fs.sync[(size_t)k].imag();
+        }
+        env[0] = fs.env_b0;
+        env[1] = fs.env_b1;
+        env[2] = fs.env_a1;
+        return VHSDECODE_GB300_STATUS_OK;
+    });
+}
+
+VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_field_sync(
+    uint32_t profile, double mhz, const int64_t* starts, const int64_t* lengths, uint64_t npulses,
+    int64_t span_len, const double* ref, int32_t* state, double* out, double* locs, uint32_t cap,
+    uint32_t* locs_count) {
+    return guard([&]() -> int32_t {
+        if ((!starts || !lengths) && npulses) return fail(VHSDECODE_GB300_STATUS_NULL_POINTER, "null pulses");
+        if (!state || !out || !locs_count) return fail(VHSDECODE_GB300_STATUS_NULL_POINTER, "null output");
+        FormatParams f;
+        if (!format_for(profile, 0, f)) return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "unsupported profile");
+        SyncParams sp = SyncParams::make(f, mhz * 1e6);
+        std::vector<Pulse> raw;
+        for (uint64_t i = 0; i < npulses; i++) raw.push_back({starts[i], lengths[i]});
+        FieldState st;
+        st.prev_first = state[0];
+        st.has_prev_hsync = state[1] != 0;
+        RefFetch fetch;
+        if (ref)
+            fetch = [&](int64_t s0, int64_t len, std::vector<double>& o) { o.assign(ref + s0, ref + s0 + len); };
+        FieldSync fs = analyse_field(sp, raw, span_len, st, fetch);
+        state[0] = st.prev_first;
+        state[1] = st.has_prev_hsync ? 1 : 0;
+        if (!fs.ok) return fail(VHSDECODE_GB300_STATUS_DECODE_ERROR, fs.error);
+        out[0] = fs.first_field ? 1.0 : 0.0;
+        out[1] = fs.line0;
+        out[2] = fs.first_hsync;
+        out[3] = fs.mean_line;
+        out[4] = fs.next_offset;
+        *locs_count = (uint32_t)fs.locs.size();
+        if (locs) {
+            if (cap < fs.locs.size()) return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "capacity too small");
+            std::copy(fs.locs.begin(), fs.locs.end(), locs);
+        }
+        return VHSDECODE_GB300_STATUS_OK;
+    });
+}
+
+}  // extern "C"

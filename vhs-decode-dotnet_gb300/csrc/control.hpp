@@ -1,0 +1,66 @@
+// Host-side field sync control plane: pulse timing and classification, mean
+// line length, field cadence, VBlank line-0 estimate, upstream line
+// locations and next-field offset.  Inputs are the device-extracted sync
+// pulses of one field span; everything here is scalar bookkeeping over a few
+// hundred pulses.
+#pragma once
+#include <cstdint>
+#include <functional>
+#include <string>
+#include <vector>
+
+#include "formats.hpp"
+
+namespace vhsd {
+
+struct Pulse { int64_t start, len; };
+enum PulseKind { kHSync = 0, kEq = 1, kVSync = 2, kEq2 = 3 };
+struct CPulse { int kind; int64_t start, len; bool in_order; };
+
+struct SyncParams {
+    bool pal;
+    double fs, mhz, nominal, line_period_us;
+    double hsync_us, eq_us, vsync_us;
+    int num_pulses;
+    double hsync_tol = 0.7, eq_tol = 0.9;
+    double ire0, hz_ire, vsync_ire;
+    int output_lines, outlinelen;
+    double fsc_mhz;
+    static SyncParams make(const FormatParams& f, double fs);
+    double usec(double us) const { return us * mhz; }
+    double ire_to_hz(double ire) const { return ire0 + hz_ire * ire; }
+    int field_lines(bool first) const {
+        int n = output_lines;
+        return pal ? (first ? n - 1 : n) : (first ? n : n - 1);
+    }
+};
+
+struct FieldState {
+    int prev_first = -1;   // -1 unknown, else 0/1
+    bool has_prev_hsync = false;
+};
+
+struct FieldSync {
+    bool ok = false;
+    std::string error;
+    bool first_field = false;
+    double line0 = 0, first_hsync = 0, mean_line = 0, next_offset = 0;
+    std::vector<double> locs;       // processed lines, span-relative
+    std::vector<uint8_t> filled;
+};
+
+// Reads `len` samples of the sync reference at span-relative `start`.
+using RefFetch = std::function<void(int64_t start, int64_t len, std::vector<double>& out)>;
+
+// Raw pulses of a span from the global edge events (2*pos + type, stream
+// coordinates): the state machine restarted at span_start as
+// PulseDetection.FindPulses would see it.
+std::vector<Pulse> span_pulses(const int64_t* events, int64_t nevents, int64_t span_start,
+                               int64_t span_len, int64_t min_len, int64_t max_len);
+
+FieldSync analyse_field(const SyncParams& sp, const std::vector<Pulse>& raw, int64_t span_len,
+                        FieldState& state, const RefFetch& fetch);
+
+double round_away(double x);
+
+}  // namespace vhsd

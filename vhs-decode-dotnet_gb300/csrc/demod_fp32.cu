@@ -1,0 +1,697 @@
+// Fused FP32 VHS block demodulator: one 32768-sample RF block per 2-CTA
+// thread-block cluster, every intermediate spectrum kept in the two CTAs'
+// shared memory and exchanged through distributed shared memory.
+//
+// Per block b (RF samples x[n] = rf[b*30720 + n], n < 32768) it computes what
+// the reference's exact VHS path computes per block
+// (Core/Dsp/RfDemodulator.cs:288-918, exact backend):
+//   X  = rfft(x);  Y = X * RfVideo                         (stage 1)
+//   z  = ifft(full(Y) * Hilbert)       analytic signal     (stage 2)
+//   d  = float polynomial-atan2 FM demod of z              (stage 3)
+//        + diff-demod spike repair when any d > limit      (repair path)
+//   env= |Re z| rolled by 4, 700 kHz first-order filtfilt  (envelope)
+//   D  = rfft(d - ire0)                                    (stage 4)
+//   video = irfft(D * Video) + ire0, sync = roll(irfft(D * VideoLowPass05), -32) + ire0
+//                                                          (stage 5)
+// and writes the kept samples [1024, 31744) of video, sync and envelope to the
+// stitched stream at stream index b*30720 + (n - 1024).
+//
+// Work split inside a cluster (rank 0 / rank 1):
+//   * the 16384-point packed complex FFT of a real block is split by
+//     decimation in frequency, rank 0 computing the even output bins and
+//     rank 1 the odd ones; the real-FFT post-processing pairs k with M-k,
+//     which have equal parity, so it stays local;
+//   * inverse transforms are split by decimation in time on the input bins
+//     (even bins on rank 0, odd bins on rank 1) and finished with one
+//     butterfly that reads the partner CTA's half through DSMEM;
+//   * the time-domain block is held as four 8192-sample chunks, chunks 0 and
+//     2 on rank 0, chunks 1 and 3 on rank 1.
+// Shared memory per CTA: 16384 complex floats (padded against bank
+// conflicts) plus twiddle tables; one CTA per SM.
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "fft_common.cuh"
+#include "vhs_math.cuh"
+#include "kernels.h"
+
+namespace cg = cooperative_groups;
+
+namespace vhsd {
+namespace fp32 {
+
+constexpr int N = 32768;      // RF block
+constexpr int M = 16384;      // packed complex length
+constexpr int Q = 8192;       // half of M, chunk length
+constexpr int T = 512;        // threads per CTA
+constexpr int S = 30720;      // block stride
+constexpr int CUT = 1024;
+constexpr int BUF = M + (M >> 4);  // padded buffer length in float2
+
+__device__ __forceinline__ int sx(int i) { return i + (i >> 4); }
+
+struct Tw {
+    float2 hi[256];  // exp(-2 pi i h*128/32768)
+    float2 lo[128];  // exp(-2 pi i l/32768)
+};
+
+// exp(-2 pi i k / 32768) for k in [0, 32768)
+__device__ __forceinline__ float2 w32k(const Tw& t, int k) {
+    return cmul(t.hi[(k >> 7) & 255], t.lo[k & 127]);
+}
+
+// One Stockham radix-R pass over `batch` transforms of length L stored
+// contiguously from buf index 0.  Each thread handles J butterflies.
+template <int R, int J, bool INV>
+__device__ __forceinline__ void pass(float2* buf, int L, int batch, int Ns, const Tw& tw, int tid) {
+    float2 v[J][R];
+    int dst[J];
+    bool act[J];
+    const int nbf = L / R;
+    const int step = 32768 / (Ns * R);
+#pragma unroll
+    for (int i = 0; i < J; i++) {
+        int g = tid + i * T;
+        act[i] = g < batch * nbf;
+        dst[i] = 0;
+        if (act[i]) {
+            int f = g / nbf;
+            int j = g - f * nbf;
+            int base = f * L;
+            int k = j & (Ns - 1);
+#pragma unroll
+            for (int r = 0; r < R; r++) v[i][r] = buf[sx(base + j + r * nbf)];
+            if (Ns > 1) {
+#pragma unroll
+                for (int r = 1; r < R; r++) {
+                    float2 w = w32k(tw, (k * r * step) & 32767);
+                    v[i][r] = INV ? cmulc(v[i][r], w) : cmul(v[i][r], w);
+                }
+            }
+            dft<R, INV>(v[i]);
+            dst[i] = base + (j - k) * R + k;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < J; i++) {
+        if (act[i]) {
+#pragma unroll
+            for (int r = 0; r < R; r++) buf[sx(dst[i] + r * Ns)] = v[i][r];
+        }
+    }
+    __syncthreads();
+}
+
+// 8192-point transform(s): radix 16 x 16 x 32.
+template <bool INV, int BATCH>
+__device__ __forceinline__ void fft8192(float2* buf, const Tw& tw, int tid) {
+    pass<16, BATCH, INV>(buf, Q, BATCH, 1, tw, tid);
+    pass<16, BATCH, INV>(buf, Q, BATCH, 16, tw, tid);
+    pass<32, (BATCH + 1) / 2, INV>(buf, Q, BATCH, 256, tw, tid);
+}
+
+// 16384-point transform: radix 16 x 32 x 32.
+template <bool INV>
+__device__ __forceinline__ void fft16384(float2* buf, const Tw& tw, int tid) {
+    pass<16, 2, INV>(buf, M, 1, 1, tw, tid);
+    pass<32, 1, INV>(buf, M, 1, 16, tw, tid);
+    pass<32, 1, INV>(buf, M, 1, 512, tw, tid);
+}
+
+
+struct Shared {
+    float2 buf[BUF];
+    Tw tw;
+    float2 nyq;          // Nyquist bin of the rank-0 half spectrum
+    float tail_theta[2];     // last angle of each local chunk
+    float tail_re[2][4];     // last four Re z of each local chunk
+    int flag;
+    int pad_;
+};
+
+// Half-spectrum post-processing of a real FFT computed as a packed complex
+// FFT: given C[k] and C[M-k] returns X[k] = (C[k] + C*[M-k])/2
+// - (i/2) W_N^k (C[k] - C*[M-k]).
+__device__ __forceinline__ float2 real_post(float2 ck, float2 cmk, float2 wk) {
+    float2 a = make_float2(0.5f * (ck.x + cmk.x), 0.5f * (ck.y - cmk.y));
+    float2 b = make_float2(0.5f * (ck.x - cmk.x), 0.5f * (ck.y + cmk.y));
+    // -i * W * b
+    float2 wb = cmul(wk, b);
+    return make_float2(a.x + wb.y, a.y - wb.x);
+}
+
+// Stage 1/4 post-processing: buf[0..8192) holds C at the rank's parity; write
+// X * g (g = per-bin real scale supplied by `scale`) back in place.  Rank 0
+// writes X[2q] at q (q < 8192) and X[16384] to nyq; rank 1 writes X[2q+1].
+template <typename ScaleFn>
+__device__ __forceinline__ void post_half(Shared& sh, int rank, int tid, ScaleFn scale) {
+    float2* buf = sh.buf;
+    if (rank == 0) {
+        for (int q = tid; q <= 4096; q += T) {
+            int q2 = 8192 - q;
+            float2 cq = buf[sx(q)];
+            float2 cq2 = (q == 0) ? cq : buf[sx(q2)];
+            if (q == 0) {
+                // X[0] = Re C0 + Im C0, X[M] = Re C0 - Im C0 (both real)
+                float x0 = cq.x + cq.y, xm = cq.x - cq.y;
+                buf[sx(0)] = scale(0, make_float2(x0, 0.0f));
+                sh.nyq = scale(M, make_float2(xm, 0.0f));
+            } else {
+                int k = 2 * q, k2 = 2 * q2;
+                float2 xk = real_post(cq, cq2, w32k(sh.tw, k));
+                float2 xk2 = real_post(cq2, cq, w32k(sh.tw, k2));
+                buf[sx(q)] = scale(k, xk);
+                if (q2 != q) buf[sx(q2)] = scale(k2, xk2);
+            }
+        }
+    } else {
+        for (int q = tid; q < 4096; q += T) {
+            int q2 = 8191 - q;
+            float2 cq = buf[sx(q)], cq2 = buf[sx(q2)];
+            int k = 2 * q + 1, k2 = 2 * q2 + 1;
+            float2 xk = real_post(cq, cq2, w32k(sh.tw, k));
+            float2 xk2 = real_post(cq2, cq, w32k(sh.tw, k2));
+            buf[sx(q)] = scale(k, xk);
+            buf[sx(q2)] = scale(k2, xk2);
+        }
+    }
+    __syncthreads();
+}
+
+// Sample index n held at local position i of `rank`.
+__device__ __forceinline__ int pos_to_n(int i, int rank) {
+    return ((2 * (i >> 13) + rank) << 13) | (i & 8191);
+}
+
+// Affine map composition helpers for the envelope scan.
+struct Aff { float a, b; };
+__device__ __forceinline__ Aff aff_then(Aff first, Aff second) {
+    // apply first, then second: s -> second.a*(first.a*s + first.b) + second.b
+    Aff r;
+    r.a = second.a * first.a;
+    r.b = fmaf(second.a, first.b, second.b);
+    return r;
+}
+
+__device__ __forceinline__ Aff warp_scan_incl(Aff v, int lane) {
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        float pa = __shfl_up_sync(0xffffffffu, v.a, o);
+        float pb = __shfl_up_sync(0xffffffffu, v.b, o);
+        if (lane >= o) v = aff_then(Aff{pa, pb}, v);
+    }
+    return v;
+}
+__device__ __forceinline__ Aff warp_scan_incl_rev(Aff v, int lane) {
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        float pa = __shfl_down_sync(0xffffffffu, v.a, o);
+        float pb = __shfl_down_sync(0xffffffffu, v.b, o);
+        if (lane + o < 32) v = aff_then(Aff{pa, pb}, v);
+    }
+    return v;
+}
+
+// Read raw (component y) or y-envelope (component y) at sample n from the
+// owning rank's buffer (local or remote through DSMEM).
+__device__ __forceinline__ float chunk_val(float2* local, float2* remote, int rank, int n) {
+    int ch = n >> 13;
+    int i = ((ch >> 1) << 13) | (n & 8191);
+    float2* b = ((ch & 1) == rank) ? local : remote;
+    return b[sx(i)].y;
+}
+
+}  // namespace fp32
+}  // namespace vhsd
+
+using namespace vhsd;
+using namespace vhsd::fp32;
+
+extern "C" __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(T, 1)
+vhsd_demod_fp32_kernel(FastDemodParams p) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Shared& sh = *reinterpret_cast<Shared*>(smem_raw);
+    cg::cluster_group cluster = cg::this_cluster();
+    const int rank = (int)cluster.block_rank();
+    const int tid = threadIdx.x;
+    const int lane = tid & 31, warp = tid >> 5;
+    float2* buf = sh.buf;
+    Shared* rsh = cluster.map_shared_rank(&sh, rank ^ 1);
+    float2* rbuf = rsh->buf;
+
+    for (int i = tid; i < 256; i += T) sh.tw.hi[i] = p.tw_hi[i];
+    for (int i = tid; i < 128; i += T) sh.tw.lo[i] = p.tw_lo[i];
+    __syncthreads();
+
+    const int cluster_id = blockIdx.x >> 1;
+    const int nclusters = gridDim.x >> 1;
+    const float inv_n = 1.0f / (float)N;
+    const float inv_m = 1.0f / (float)M;
+    const float freq = p.fs;
+
+    for (int64_t blk = cluster_id; blk < p.nblocks; blk += nclusters) {
+        const int16_t* x = p.rf + (blk + p.first_block) * (int64_t)S;
+        // ---------------- stage 1: RF forward FFT (packed, DIF split) -----
+        // thread loads 4 vectors of 8 int16 from each half
+#pragma unroll
+        for (int it = 0; it < 4; it++) {
+            int vi = tid + it * T;  // vector index in [0, 2048)
+            int4 va = __ldg(reinterpret_cast<const int4*>(x) + vi);
+            int4 vb = __ldg(reinterpret_cast<const int4*>(x + 16384) + vi);
+            const int16_t* ha = reinterpret_cast<const int16_t*>(&va);
+            const int16_t* hb = reinterpret_cast<const int16_t*>(&vb);
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                int pp = 4 * vi + e;
+                float2 ca = make_float2((float)ha[2 * e], (float)ha[2 * e + 1]);
+                float2 cb = make_float2((float)hb[2 * e], (float)hb[2 * e + 1]);
+                float2 r;
+                if (rank == 0) r = cadd(ca, cb);
+                else r = cmul(csub(ca, cb), w32k(sh.tw, 2 * pp));
+                buf[sx(pp)] = r;
+            }
+        }
+        __syncthreads();
+        fft8192<false, 1>(buf, sh.tw, tid);
+        // X * RfVideo * Hilbert / N  (Hilbert: 1 at 0 and N/2, 2 between)
+        post_half(sh, rank, tid, [&](int k, float2 v) {
+            float g = __ldg(p.rf_video + k) * ((k == 0 || k == M) ? inv_n : 2.0f * inv_n);
+            return make_float2(v.x * g, v.y * g);
+        });
+        // ---------------- stage 2: analytic inverse FFT -----------------
+        if (rank == 0) {
+            if (tid == 0) buf[sx(8192)] = sh.nyq;
+            for (int i = 8193 + tid; i < M; i += T) buf[sx(i)] = make_float2(0.f, 0.f);
+        } else {
+            for (int i = 8192 + tid; i < M; i += T) buf[sx(i)] = make_float2(0.f, 0.f);
+        }
+        __syncthreads();
+        fft16384<true>(buf, sh.tw, tid);
+        cluster.sync();
+        {
+            // z[n] = A[n] + W^-n B[n], z[n+16384] = A[n] - W^-n B[n]
+            float2 o1[16], o2[16];
+#pragma unroll
+            for (int t = 0; t < 16; t++) {
+                int nl = tid + t * T;                 // [0, 8192)
+                int n = nl + rank * 8192;             // [0, 16384)
+                float2 loc = buf[sx(n)];
+                float2 rem = rbuf[sx(n)];
+                float2 a = rank == 0 ? loc : rem;
+                float2 b = rank == 0 ? rem : loc;
+                float2 wb = cmulc(b, w32k(sh.tw, n));
+                float2 z1 = cadd(a, wb), z2 = csub(a, wb);
+                o1[t] = make_float2(vhs_atan2(z1.y, z1.x), z1.x);
+                o2[t] = make_float2(vhs_atan2(z2.y, z2.x), z2.x);
+            }
+            cluster.sync();
+#pragma unroll
+            for (int t = 0; t < 16; t++) {
+                int nl = tid + t * T;
+                buf[sx(nl)] = o1[t];          // chunk rank
+                buf[sx(8192 + nl)] = o2[t];   // chunk rank + 2
+            }
+        }
+        __syncthreads();
+        // ---------------- stage 3: demod, raw envelope, spike check ------
+        if (tid < 2) {
+            int i_last = tid * 8192 + 8191;
+            sh.tail_theta[tid] = buf[sx(i_last)].x;
+            for (int k = 0; k < 4; k++) sh.tail_re[tid][k] = buf[sx(i_last - 3 + k)].y;
+        }
+        cluster.sync();
+        bool spike = false;
+        {
+            float dv[32], rv[32];
+#pragma unroll
+            for (int t = 0; t < 32; t++) {
+                int i = tid + t * T;        // local position [0, 16384)
+                int n = pos_to_n(i, rank);
+                int il = i & 8191;
+                int lc = i >> 13;           // local chunk slot
+                int c = 2 * lc + rank;      // chunk of n
+                int plc = ((c + 3) & 3) >> 1;  // predecessor chunk (other rank) slot
+                float th = buf[sx(i)].x;
+                float thp = (il > 0) ? buf[sx(i - 1)].x : rsh->tail_theta[plc];
+                float d = (n == 0) ? 0.0f : vhs_freq_diff(th, thp, freq);
+                dv[t] = d;
+                if (n >= 20 && n < N - 20 && d > p.diff_max) spike = true;
+                float re = (il >= 4) ? buf[sx(i - 4)].y : rsh->tail_re[plc][il];
+                rv[t] = fabsf(re);
+            }
+            __syncthreads();
+#pragma unroll
+            for (int t = 0; t < 32; t++) buf[sx(tid + t * T)] = make_float2(dv[t], rv[t]);
+        }
+        int any = __syncthreads_or(spike ? 1 : 0);
+        if (tid == 0) sh.flag = any;
+        cluster.sync();
+        any = sh.flag | rsh->flag;
+        if (any) {
+            // Diff-demod repair (Core/Dsp/RfDemodulator.cs:966-1001, 2527-2582):
+            // rebuild the analytic signal into cluster scratch, demodulate its
+            // first difference, then replace spikes in ascending index order.
+            if (tid == 0 && rank == 0) atomicAdd(p.repair_count, 1);
+            float2* zs = p.scratch + (int64_t)cluster_id * (2 * N);
+            float* ds = reinterpret_cast<float*>(zs + N);
+            float* dds = ds + N;
+            float* raws = p.scratch_raw + (int64_t)cluster_id * N;
+#pragma unroll 4
+            for (int t = 0; t < 32; t++) {
+                int i = tid + t * T;
+                int n = pos_to_n(i, rank);
+                float2 v = buf[sx(i)];
+                ds[n] = v.x;
+                raws[n] = v.y;
+            }
+            __syncthreads();
+#pragma unroll
+            for (int it = 0; it < 4; it++) {
+                int vi = tid + it * T;
+                int4 va = __ldg(reinterpret_cast<const int4*>(x) + vi);
+                int4 vb = __ldg(reinterpret_cast<const int4*>(x + 16384) + vi);
+                const int16_t* ha = reinterpret_cast<const int16_t*>(&va);
+                const int16_t* hb = reinterpret_cast<const int16_t*>(&vb);
+#pragma unroll
+                for (int e = 0; e < 4; e++) {
+                    int pp = 4 * vi + e;
+                    float2 ca = make_float2((float)ha[2 * e], (float)ha[2 * e + 1]);
+                    float2 cb = make_float2((float)hb[2 * e], (float)hb[2 * e + 1]);
+                    buf[sx(pp)] = (rank == 0) ? cadd(ca, cb) : cmul(csub(ca, cb), w32k(sh.tw, 2 * pp));
+                }
+            }
+            __syncthreads();
+            fft8192<false, 1>(buf, sh.tw, tid);
+            post_half(sh, rank, tid, [&](int k, float2 v) {
+                float g = __ldg(p.rf_video + k) * ((k == 0 || k == M) ? inv_n : 2.0f * inv_n);
+                return make_float2(v.x * g, v.y * g);
+            });
+            if (rank == 0) {
+                if (tid == 0) buf[sx(8192)] = sh.nyq;
+                for (int i = 8193 + tid; i < M; i += T) buf[sx(i)] = make_float2(0.f, 0.f);
+            } else {
+                for (int i = 8192 + tid; i < M; i += T) buf[sx(i)] = make_float2(0.f, 0.f);
+            }
+            __syncthreads();
+            fft16384<true>(buf, sh.tw, tid);
+            cluster.sync();
+            for (int t = 0; t < 16; t++) {
+                int n = tid + t * T + rank * 8192;
+                float2 loc = buf[sx(n)];
+                float2 rem = rbuf[sx(n)];
+                float2 a = rank == 0 ? loc : rem;
+                float2 b = rank == 0 ? rem : loc;
+                float2 wb = cmulc(b, w32k(sh.tw, n));
+                zs[n] = cadd(a, wb);
+                zs[n + 16384] = csub(a, wb);
+            }
+            cluster.sync();
+            for (int t = 0; t < 32; t++) {
+                int n = pos_to_n(tid + t * T, rank);
+                float dd = 0.0f;
+                if (n >= 1) {
+                    float2 z0 = zs[n], zm1 = zs[n - 1];
+                    float2 dz = csub(z0, zm1);
+                    float th = vhs_atan2(dz.y, dz.x);
+                    float thp;
+                    if (n >= 2) {
+                        float2 dzp = csub(zm1, zs[n - 2]);
+                        thp = vhs_atan2(dzp.y, dzp.x);
+                    } else {
+                        thp = vhs_atan2(0.0f, 0.0f);
+                    }
+                    dd = vhs_freq_diff(th, thp, freq);
+                }
+                dds[n] = dd;
+            }
+            cluster.sync();
+            if (rank == 0) {
+                // spike mask from the demod before any replacement
+                unsigned* mask = reinterpret_cast<unsigned*>(buf);
+                for (int base = warp * 32; base < N; base += 32 * (T / 32)) {
+                    unsigned m = __ballot_sync(0xffffffffu, ds[base + lane] > p.diff_max);
+                    if (lane == 0) mask[base >> 5] = m;
+                }
+                __syncthreads();
+                if (warp == 0) {
+                    for (int word = 0; word < N / 32; word++) {
+                        unsigned m = mask[word];
+                        while (m) {
+                            int b = __ffs(m) - 1;
+                            m &= m - 1;
+                            int i0 = word * 32 + b;
+                            int st = max(i0 - 8, 0);
+                            int en = min(i0 + 30, N - 1);
+                            if (st >= en) continue;
+                            float mdd = -INFINITY, md = -INFINITY;
+                            for (int k = st + lane; k < en; k += 32) {
+                                mdd = fmaxf(mdd, dds[k]);
+                                md = fmaxf(md, ds[k]);
+                            }
+#pragma unroll
+                            for (int o = 16; o > 0; o >>= 1) {
+                                mdd = fmaxf(mdd, __shfl_xor_sync(0xffffffffu, mdd, o));
+                                md = fmaxf(md, __shfl_xor_sync(0xffffffffu, md, o));
+                            }
+                            if (mdd < md) {
+                                for (int k = st + lane; k < en; k += 32) ds[k] = dds[k];
+                            }
+                            __syncwarp();
+                        }
+                    }
+                }
+            }
+            cluster.sync();
+#pragma unroll 4
+            for (int t = 0; t < 32; t++) {
+                int i = tid + t * T;
+                int n = pos_to_n(i, rank);
+                buf[sx(i)] = make_float2(ds[n], raws[n]);
+            }
+            __syncthreads();
+        }
+        // ---------------- envelope: filtfilt with halo-started warp scans --
+        // warp w of this rank covers local positions [w*1024, w*1024+1024),
+        // i.e. samples n0 = chunk*8192 + (w & 7)*1024.
+        {
+            const int lc = warp >> 3;
+            const int c = 2 * lc + rank;
+            const int n0 = c * 8192 + (warp & 7) * 1024;
+            const float b0 = p.env_b0, b1 = p.env_b1, a1 = p.env_a1;
+            const float cc = -a1;
+            const float gk = b1 - a1 * b0;   // state input gain
+            float yv[32];
+            // forward: z1' = cc*z1 + gk*e ; y = b0*e + z1
+            float zin = 0.0f;
+            if (n0 >= 256) {
+                // halo of 256 samples: 8 per lane
+                float s = 0.0f;
+                Aff h{1.0f, 0.0f};
+                int hs = n0 - 256 + lane * 8;
+                float st = 0.0f;
+                for (int k = 0; k < 8; k++) {
+                    float e = chunk_val(buf, rbuf, rank, hs + k);
+                    st = fmaf(cc, st, gk * e);
+                }
+                h.a = 1.0f;
+                for (int k = 0; k < 8; k++) h.a *= cc;
+                h.b = st;
+                Aff inc = warp_scan_incl(h, lane);
+                zin = __shfl_sync(0xffffffffu, inc.b, 31);
+                (void)s;
+            }
+            {
+                int ms = n0 + lane * 32;
+                float st = 0.0f, pa = 1.0f;
+                for (int k = 0; k < 32; k++) {
+                    float e = chunk_val(buf, rbuf, rank, ms + k);
+                    st = fmaf(cc, st, gk * e);
+                    pa *= cc;
+                }
+                Aff loc{pa, st};
+                Aff inc = warp_scan_incl(loc, lane);
+                float prev_b = __shfl_up_sync(0xffffffffu, inc.b, 1);
+                float prev_a = __shfl_up_sync(0xffffffffu, inc.a, 1);
+                float z = lane == 0 ? zin : fmaf(prev_a, zin, prev_b);
+                for (int k = 0; k < 32; k++) {
+                    float e = chunk_val(buf, rbuf, rank, ms + k);
+                    float y = fmaf(b0, e, z);
+                    z = fmaf(cc, z, gk * e);
+                    yv[k] = y;
+                }
+            }
+            cluster.sync();
+            {
+                int ms = n0 + lane * 32;
+                for (int k = 0; k < 32; k++) {
+                    int n = ms + k;
+                    int i = (lc << 13) | (n & 8191);
+                    buf[sx(i)].y = yv[k];
+                }
+            }
+            cluster.sync();
+            // backward: w = b0*y + z1 ; z1' = cc*z1 + gk*y  (from high n to low n)
+            const int nend = n0 + 1024;
+            float zb = 0.0f;
+            if (nend + 256 <= N) {
+                int hs = nend + lane * 8;  // halo samples [nend, nend+256)
+                float st = 0.0f, pa = 1.0f;
+                for (int k = 7; k >= 0; k--) {
+                    float e = chunk_val(buf, rbuf, rank, hs + k);
+                    st = fmaf(cc, st, gk * e);
+                    pa *= cc;
+                }
+                Aff inc = warp_scan_incl_rev(Aff{pa, st}, lane);
+                zb = __shfl_sync(0xffffffffu, inc.b, 0);
+            }
+            {
+                int ms = n0 + lane * 32;
+                float st = 0.0f, pa = 1.0f;
+                for (int k = 31; k >= 0; k--) {
+                    st = fmaf(cc, st, gk * yv[k]);
+                    pa *= cc;
+                }
+                Aff inc = warp_scan_incl_rev(Aff{pa, st}, lane);
+                float nb = __shfl_down_sync(0xffffffffu, inc.b, 1);
+                float na = __shfl_down_sync(0xffffffffu, inc.a, 1);
+                float z = lane == 31 ? zb : fmaf(na, zb, nb);
+                float* envo = p.env_out + (blk + p.first_block) * (int64_t)S - CUT;
+                for (int k = 31; k >= 0; k--) {
+                    float y = yv[k];
+                    float w = fmaf(b0, y, z);
+                    z = fmaf(cc, z, gk * y);
+                    int n = ms + k;
+                    if (n >= CUT && n < CUT + S) envo[n] = w;
+                }
+            }
+        }
+        // ---------------- stage 4: forward FFT of (demod - ire0) -----------
+        {
+            float2 uo[8], vo[8];
+            int pidx[8];
+#pragma unroll
+            for (int t = 0; t < 8; t++) {
+                int pl = tid + t * T;              // [0, 4096)
+                int pp = pl + rank * 4096;         // p
+                pidx[t] = pp;
+                float d0 = buf[sx(2 * pl)].x - p.dc, d1 = buf[sx(2 * pl + 1)].x - p.dc;
+                float e0 = buf[sx(8192 + 2 * pl)].x - p.dc, e1 = buf[sx(8192 + 2 * pl + 1)].x - p.dc;
+                float2 ca = make_float2(d0, d1), cb = make_float2(e0, e1);
+                uo[t] = cadd(ca, cb);
+                vo[t] = cmul(csub(ca, cb), w32k(sh.tw, 2 * pp));
+            }
+            cluster.sync();
+#pragma unroll
+            for (int t = 0; t < 8; t++) {
+                int pp = pidx[t];
+                if (rank == 0) { buf[sx(pp)] = uo[t]; rbuf[sx(pp)] = vo[t]; }
+                else { rbuf[sx(pp)] = uo[t]; buf[sx(pp)] = vo[t]; }
+            }
+            cluster.sync();
+        }
+        fft8192<false, 1>(buf, sh.tw, tid);
+        post_half(sh, rank, tid, [&](int k, float2 v) { return v; });
+        // ---------------- stage 5: video and sync real inverse FFTs ---------
+        {
+            // F = X * H ; P[k] = (F[k] + F*[M-k])/2 + i (F[k] - F*[M-k]) W_N^-k / 2, scaled 1/M
+            const float sc = 0.5f * inv_m;
+            auto prep = [&](float2 fk, float2 fmk, int k) {
+                float2 a = make_float2(fk.x + fmk.x, fk.y - fmk.y);
+                float2 b = make_float2(fk.x - fmk.x, fk.y + fmk.y);
+                float2 bw = cmulc(b, w32k(sh.tw, k));
+                // a + i*bw
+                return make_float2(sc * (a.x - bw.y), sc * (a.y + bw.x));
+            };
+            if (rank == 0) {
+                for (int q = tid; q <= 4096; q += T) {
+                    int q2 = 8192 - q;
+                    int k = 2 * q, k2 = 2 * q2;
+                    float2 xk = buf[sx(q)];
+                    float2 xk2 = (q == 0) ? sh.nyq : buf[sx(q2)];
+                    if (q == 0) { xk.y = 0.f; xk2.y = 0.f; }
+                    float2 hv = __ldg(p.video + k), hv2 = __ldg(p.video + k2);
+                    float2 hs = __ldg(p.sync + k), hs2 = __ldg(p.sync + k2);
+                    float2 fv = cmul(xk, hv), fv2 = cmul(xk2, hv2);
+                    float2 fs = cmul(xk, hs), fs2 = cmul(xk2, hs2);
+                    if (q == 0) { fv.y = 0.f; fv2.y = 0.f; fs.y = 0.f; fs2.y = 0.f; }
+                    float2 pv = prep(fv, fv2, k), ps = prep(fs, fs2, k);
+                    buf[sx(q)] = pv;
+                    buf[sx(8192 + q)] = ps;
+                    if (q != 0 && q2 != q) {
+                        buf[sx(q2)] = prep(fv2, fv, k2);
+                        buf[sx(8192 + q2)] = prep(fs2, fs, k2);
+                    }
+                }
+            } else {
+                for (int q = tid; q < 4096; q += T) {
+                    int q2 = 8191 - q;
+                    int k = 2 * q + 1, k2 = 2 * q2 + 1;
+                    float2 xk = buf[sx(q)], xk2 = buf[sx(q2)];
+                    float2 hv = __ldg(p.video + k), hv2 = __ldg(p.video + k2);
+                    float2 hs = __ldg(p.sync + k), hs2 = __ldg(p.sync + k2);
+                    float2 fv = cmul(xk, hv), fv2 = cmul(xk2, hv2);
+                    float2 fs = cmul(xk, hs), fs2 = cmul(xk2, hs2);
+                    buf[sx(q)] = prep(fv, fv2, k);
+                    buf[sx(q2)] = prep(fv2, fv, k2);
+                    buf[sx(8192 + q)] = prep(fs, fs2, k);
+                    buf[sx(8192 + q2)] = prep(fs2, fs, k2);
+                }
+            }
+            __syncthreads();
+            fft8192<true, 2>(buf, sh.tw, tid);
+            cluster.sync();
+            float* vout = p.video_out + (blk + p.first_block) * (int64_t)S - CUT;
+            float* sout = p.sync_out + (blk + p.first_block) * (int64_t)S - CUT - 32;
+            const float dc = p.dc;
+#pragma unroll 2
+            for (int t = 0; t < 8; t++) {
+                int ml = tid + t * T;              // [0, 4096)
+                int m = ml + rank * 4096;          // [0, 8192)
+                float2 w = w32k(sh.tw, 2 * m);     // W_M^m = W_N^{2m}
+#pragma unroll
+                for (int sig = 0; sig < 2; sig++) {
+                    int off = sig * 8192;
+                    float2 loc = buf[sx(off + m)], rem = rbuf[sx(off + m)];
+                    float2 a = rank == 0 ? loc : rem;
+                    float2 b = rank == 0 ? rem : loc;
+                    float2 wb = cmulc(b, w);
+                    float2 p1 = cadd(a, wb), p2 = csub(a, wb);
+                    int n1 = 2 * m, n2 = 2 * m + 16384;
+                    if (sig == 0) {
+                        if (n1 >= CUT && n1 < CUT + S)
+                            *reinterpret_cast<float2*>(vout + n1) = make_float2(p1.x + dc, p1.y + dc);
+                        if (n2 >= CUT && n2 < CUT + S)
+                            *reinterpret_cast<float2*>(vout + n2) = make_float2(p2.x + dc, p2.y + dc);
+                    } else {
+                        if (n1 >= CUT + 32 && n1 < CUT + 32 + S)
+                            *reinterpret_cast<float2*>(sout + n1) = make_float2(p1.x + dc, p1.y + dc);
+                        if (n2 >= CUT + 32 && n2 < CUT + 32 + S)
+                            *reinterpret_cast<float2*>(sout + n2) = make_float2(p2.x + dc, p2.y + dc);
+                    }
+                }
+            }
+        }
+        cluster.sync();
+    }
+}
+
+namespace vhsd {
+
+size_t fp32_smem_bytes() { return sizeof(fp32::Shared); }
+
+cudaError_t launch_demod_fp32(const FastDemodParams& p, int num_clusters, cudaStream_t stream) {
+    size_t smem = sizeof(fp32::Shared);
+    cudaError_t e = cudaFuncSetAttribute(vhsd_demod_fp32_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    if (p.nblocks <= 0) return cudaSuccess;
+    int clusters = num_clusters;
+    if (clusters > p.nblocks) clusters = (int)p.nblocks;
+    if (clusters < 1) clusters = 1;
+    vhsd_demod_fp32_kernel<<<2 * clusters, fp32::T, smem, stream>>>(p);
+    return cudaGetLastError();
+}
+
+}  // namespace vhsd

@@ -1,0 +1,260 @@
+// Plain FP64 block demodulator: one 32768-sample block at a time, full-length
+// complex FFTs in global memory (Stockham radix-8, five passes), one kernel
+// per step.  It restates the same per-block math as the fused FP32 kernel
+// (Core/Dsp/RfDemodulator.cs:288-918) in binary64 and is the baseline the
+// fused path is measured against.  The session replays the per-block launch
+// sequence from a captured CUDA graph; the block index is read from device
+// memory so one graph serves every block.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "fft_common.cuh"
+#include "vhs_math.cuh"
+#include "kernels.h"
+
+namespace vhsd {
+namespace fp64 {
+
+constexpr int N = 32768;
+constexpr int H = N / 2;
+
+__device__ __forceinline__ double2 wN(int k, bool inv) {
+    double s, c;
+    sincospi(-2.0 * (double)k / (double)N, &s, &c);
+    return make_double2(c, inv ? -s : s);
+}
+
+// Stockham radix-8 pass: in -> out, L = N, Ns in {1, 8, 64, 512, 4096}.
+template <bool INV>
+__global__ void k_pass8(const double2* __restrict__ in, double2* __restrict__ out, int Ns) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int R = 8;
+    const int nbf = N / R;
+    if (j >= nbf) return;
+    int k = j & (Ns - 1);
+    double2 v[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) v[r] = in[j + r * nbf];
+    if (Ns > 1) {
+#pragma unroll
+        for (int r = 1; r < R; r++) {
+            double2 w = wN((k * r * (N / (Ns * R))) & (N - 1), INV);
+            v[r] = cmul(v[r], w);
+        }
+    }
+    dft<R, INV>(v);
+    int dst = (j - k) * R + k;
+#pragma unroll
+    for (int r = 0; r < R; r++) out[dst + r * Ns] = v[r];
+}
+
+// a -> b -> a ... five passes; result ends in `b`.
+template <bool INV>
+void fft(double2* a, double2* b, cudaStream_t s) {
+    int ns = 1;
+    double2* src = a;
+    double2* dst = b;
+    for (int pidx = 0; pidx < 5; pidx++) {
+        k_pass8<INV><<<(N / 8 + 255) / 256, 256, 0, s>>>(src, dst, ns);
+        ns *= 8;
+        double2* t = src; src = dst; dst = t;
+    }
+    // after 5 passes the data is in `src` (== b)
+}
+
+
+__global__ void k_load(const int16_t* rf, const int64_t* blk, double2* out) {
+    int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= N) return;
+    out[n] = make_double2((double)rf[blk[0] * kStride + n], 0.0);
+}
+
+// analytic spectrum: X * RfVideo * Hilbert / N  (bins > N/2 zero)
+__global__ void k_analytic_spec(const double2* X, const double* g, double2* Z) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= N) return;
+    double m;
+    if (k == 0 || k == H) m = g[k] / N;
+    else if (k < H) m = 2.0 * g[k] / N;
+    else m = 0.0;
+    Z[k] = make_double2(X[k].x * m, X[k].y * m);
+}
+
+// demod (float polynomial atan2 of the double analytic signal) + spike flag
+__global__ void k_demod(const double2* z, double* d, float fs, double diff_max, int* flag) {
+    int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= N) return;
+    double v = 0.0;
+    if (n > 0) {
+        float th = vhs_atan2((float)z[n].y, (float)z[n].x);
+        float tp = vhs_atan2((float)z[n - 1].y, (float)z[n - 1].x);
+        v = (double)vhs_freq_diff(th, tp, fs);
+    }
+    d[n] = v;
+    if (n >= 20 && n < N - 20 && v > diff_max) atomicOr(flag, 1);
+}
+
+// diff demod (analytic first difference), only when the block has spikes
+__global__ void k_diff_demod(const double2* z, double* dd, float fs, const int* flag) {
+    if (!flag[0]) return;
+    int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= N) return;
+    double v = 0.0;
+    if (n >= 1) {
+        double2 a = z[n], b = z[n - 1];
+        float th = vhs_atan2((float)(a.y - b.y), (float)(a.x - b.x));
+        float tp;
+        if (n >= 2) {
+            double2 c = z[n - 2];
+            tp = vhs_atan2((float)(b.y - c.y), (float)(b.x - c.x));
+        } else {
+            tp = vhs_atan2(0.0f, 0.0f);
+        }
+        v = (double)vhs_freq_diff(th, tp, fs);
+    }
+    dd[n] = v;
+}
+
+// ReplaceSpikes (Core/Dsp/RfDemodulator.cs:966-1001) on one warp, spike set
+// taken from the demod before replacement.
+__global__ void k_replace_spikes(double* d, const double* dd, double diff_max, int* flag,
+                                 unsigned* mask) {
+    if (!flag[0]) return;
+    int lane = threadIdx.x;
+    for (int base = 0; base < N; base += 32) {
+        unsigned m = __ballot_sync(0xffffffffu, d[base + lane] > diff_max);
+        if (lane == 0) mask[base >> 5] = m;
+    }
+    __syncwarp();
+    for (int word = 0; word < N / 32; word++) {
+        unsigned m = mask[word];
+        while (m) {
+            int b = __ffs(m) - 1;
+            m &= m - 1;
+            int i0 = word * 32 + b;
+            int st = max(i0 - 8, 0), en = min(i0 + 30, N - 1);
+            if (st >= en) continue;
+            double mdd = -INFINITY, md = -INFINITY;
+            for (int k = st + lane; k < en; k += 32) { mdd = fmax(mdd, dd[k]); md = fmax(md, d[k]); }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                mdd = fmax(mdd, __shfl_xor_sync(0xffffffffu, mdd, o));
+                md = fmax(md, __shfl_xor_sync(0xffffffffu, md, o));
+            }
+            if (mdd < md) for (int k = st + lane; k < en; k += 32) d[k] = dd[k];
+            __syncwarp();
+        }
+    }
+    if (lane == 0) flag[0] = 0;
+}
+
+// float32 envelope filtfilt, exactly sequential as the reference
+// (SosFilter.ApplyForwardBackwardFloat32, Core/Dsp/SosFilter.cs:300-540):
+// one thread per block; raw[n] = |float(Re z[n-4])|.
+__global__ void k_envelope(const double2* z, float* work, double* env, float b0, float b1, float a1) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int edge = 6;
+    float* ext = work;
+    float* raw = work + edge;
+    for (int n = 0; n < N; n++) raw[(n + 4) & (N - 1)] = fabsf((float)z[n].x);
+    float first = raw[0], last = raw[N - 1];
+    for (int i = 0; i < edge; i++) ext[i] = __fsub_rn(__fmul_rn(2.0f, first), raw[edge - i]);
+    for (int i = 0; i < edge; i++) ext[edge + N + i] = __fsub_rn(__fmul_rn(2.0f, last), raw[N - 2 - i]);
+    const int len = N + 2 * edge;
+    float b2 = 0.0f, a2 = 0.0f;
+    float ft = __fsub_rn(b1, __fmul_rn(a1, b0));
+    float st = __fsub_rn(b2, __fmul_rn(a2, b0));
+    float num = __fadd_rn(__fadd_rn(0.0f, ft), st);
+    float den = __fadd_rn(__fadd_rn(1.0f, a1), a2);
+    float zi0 = __fdiv_rn(num, den);
+    float zi1 = __fsub_rn(__fmul_rn(__fadd_rn(1.0f, a1), zi0), ft);
+    float z1 = __fmul_rn(zi0, ext[0]), z2 = __fmul_rn(zi1, ext[0]);
+    for (int s = 0; s < len; s++) {
+        float v = ext[s];
+        float f = __fadd_rn(__fmul_rn(b0, v), z1);
+        z1 = __fadd_rn(__fsub_rn(__fmul_rn(b1, v), __fmul_rn(a1, f)), z2);
+        z2 = __fsub_rn(__fmul_rn(b2, v), __fmul_rn(a2, f));
+        ext[s] = f;
+    }
+    z1 = __fmul_rn(zi0, ext[len - 1]);
+    z2 = __fmul_rn(zi1, ext[len - 1]);
+    for (int s = len - 1; s >= 0; s--) {
+        float v = ext[s];
+        float f = __fadd_rn(__fmul_rn(b0, v), z1);
+        z1 = __fadd_rn(__fsub_rn(__fmul_rn(b1, v), __fmul_rn(a1, f)), z2);
+        z2 = __fsub_rn(__fmul_rn(b2, v), __fmul_rn(a2, f));
+        ext[s] = f;
+    }
+    for (int n = 0; n < N; n++) env[n] = (double)ext[edge + n];
+}
+
+__global__ void k_real_to_complex(const double* d, double2* out) {
+    int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= N) return;
+    out[n] = make_double2(d[n], 0.0);
+}
+
+// Hermitian spectrum D * Hfilter for bins 0..N/2 (imaginary parts of the DC and
+// Nyquist bins dropped, as a c2r inverse does), mirrored above N/2, scaled 1/N.
+__global__ void k_filter_spec(const double2* D, const double2* h, double2* out) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= N) return;
+    int kk = k <= H ? k : N - k;
+    double2 v = cmul(D[kk], h[kk]);
+    if (kk == 0 || kk == H) v.y = 0.0;
+    if (k > H) v.y = -v.y;
+    out[k] = make_double2(v.x / N, v.y / N);
+}
+
+__global__ void k_store(const double2* x, const int64_t* blk, double* out, int shift) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= kStride) return;
+    int n = s + kCut + shift;
+    out[blk[0] * kStride + s] = x[n].x;
+}
+__global__ void k_store_real(const double* x, const int64_t* blk, double* out) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= kStride) return;
+    out[blk[0] * kStride + s] = x[s + kCut];
+}
+__global__ void k_next_block(int64_t* blk) { blk[0] += 1; }
+
+}  // namespace fp64
+
+// Work buffers: work = 4*N double2 (w0..w3), dwork = 4*N double (d, dd, env, scratch)
+cudaError_t launch_demod_fp64_block(const PlainDemodParams& p, cudaStream_t s) {
+    using namespace fp64;
+    const int B = 256, G = (N + B - 1) / B;
+    double2* w0 = p.work;
+    double2* w1 = p.work + N;
+    double2* w2 = p.work + 2 * N;
+    double2* w3 = p.work + 3 * N;
+    double* d = p.dwork;
+    double* dd = p.dwork + N;
+    double* env = p.dwork + 2 * N;
+    float* fscr = p.fwork;
+    int* flag = p.flag;
+    unsigned* mask = p.mask;
+    int64_t* blk = p.blk;
+    k_load<<<G, B, 0, s>>>(p.rf, blk, w0);
+    fft<false>(w0, w1, s);                         // X in w1
+    k_analytic_spec<<<G, B, 0, s>>>(w1, p.rf_video, w2);
+    fft<true>(w2, w3, s);                          // z in w3
+    k_demod<<<G, B, 0, s>>>(w3, d, (float)p.fs, p.diff_max, flag);
+    k_diff_demod<<<G, B, 0, s>>>(w3, dd, (float)p.fs, flag);
+    k_replace_spikes<<<1, 32, 0, s>>>(d, dd, p.diff_max, flag, mask);
+    k_envelope<<<1, 32, 0, s>>>(w3, fscr, env, (float)p.env_b0, (float)p.env_b1, (float)p.env_a1);
+    k_real_to_complex<<<G, B, 0, s>>>(d, w0);
+    fft<false>(w0, w1, s);                         // D in w1
+    k_filter_spec<<<G, B, 0, s>>>(w1, p.video, w2);
+    fft<true>(w2, w3, s);                          // video in w3
+    k_store<<<(kStride + B - 1) / B, B, 0, s>>>(w3, blk, p.video_out, 0);
+    k_filter_spec<<<G, B, 0, s>>>(w1, p.sync, w2);
+    fft<true>(w2, w0, s);                          // sync in w0
+    k_store<<<(kStride + B - 1) / B, B, 0, s>>>(w0, blk, p.sync_out, 32);
+    k_store_real<<<(kStride + B - 1) / B, B, 0, s>>>(env, blk, p.env_out);
+    k_next_block<<<1, 1, 0, s>>>(blk);
+    return cudaGetLastError();
+}
+
+}  // namespace vhsd

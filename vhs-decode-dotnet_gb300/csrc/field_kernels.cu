@@ -1,0 +1,744 @@
+// Field-level kernels of the VHS path: sync-pulse edge extraction, hsync edge
+// refinement, sinc TBC resampling to 4fSC uint16, envelope dropout runs.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "kernels.h"
+
+namespace vhsd {
+
+// ============================================================== pulses
+// PulseDetection.FindPulses (Core/Dsp/PulseDetection.cs:45-222) as edge
+// events over the whole stitched stream.  Event = 2*position + type with type
+// 0 for a pulse start (value <= high entered) and 1 for a pulse end (value >
+// high entered).  NaN keeps the state, as the reference's comparisons do.
+namespace {
+constexpr int kPT = 256;                      // threads per CTA
+constexpr int kPPer = kPulseChunk / kPT;      // samples per thread (16)
+
+template <typename T>
+__device__ __forceinline__ bool state_before(const T* ref, int64_t p0, double high) {
+    for (int64_t q = p0 - 1; q >= 0; q--) {
+        double v = (double)ref[q];
+        if (v <= high) return true;
+        if (v > high) return false;
+    }
+    return false;
+}
+
+template <typename T, bool WRITE>
+__global__ void k_pulse_pass(const T* __restrict__ ref, int64_t n, double high, int64_t* counts,
+                             const int64_t* offsets, int64_t* events, int64_t capacity) {
+    __shared__ int64_t warp_tot[kPT / 32];
+    const int64_t chunk = blockIdx.x;
+    const int64_t p0 = chunk * kPulseChunk + (int64_t)threadIdx.x * kPPer;
+    int cnt = 0;
+    bool in = false;
+    if (p0 < n) in = state_before(ref, p0, high);
+    bool st = in;
+    for (int k = 0; k < kPPer; k++) {
+        int64_t p = p0 + k;
+        if (p >= n) break;
+        double v = (double)ref[p];
+        if (st) { if (v > high) { st = false; cnt++; } }
+        else if (v <= high) { st = true; cnt++; }
+    }
+    // block exclusive scan of cnt
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    if (lane == 31) warp_tot[w] = incl;
+    __syncthreads();
+    int64_t wbase = 0, total = 0;
+    for (int i = 0; i < kPT / 32; i++) {
+        if (i < w) wbase += warp_tot[i];
+        total += warp_tot[i];
+    }
+    if (!WRITE) {
+        if (threadIdx.x == 0) counts[chunk] = total;
+        return;
+    }
+    int64_t off = offsets[chunk] + wbase + (incl - cnt);
+    st = in;
+    for (int k = 0; k < kPPer; k++) {
+        int64_t p = p0 + k;
+        if (p >= n) break;
+        double v = (double)ref[p];
+        if (st) {
+            if (v > high) {
+                st = false;
+                if (off < capacity) events[off] = 2 * p + 1;
+                off++;
+            }
+        } else if (v <= high) {
+            st = true;
+            if (off < capacity) events[off] = 2 * p;
+            off++;
+        }
+    }
+}
+
+// single-CTA exclusive scan of chunk counts
+__global__ void k_scan_counts(const int64_t* counts, int64_t nchunks, int64_t* offsets,
+                              int64_t* total) {
+    __shared__ int64_t carry;
+    __shared__ int64_t wsum[32];
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int64_t base = 0; base < nchunks; base += blockDim.x) {
+        int64_t i = base + threadIdx.x;
+        int64_t v = i < nchunks ? counts[i] : 0;
+        int64_t incl = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            int64_t t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        if (lane == 31) wsum[w] = incl;
+        __syncthreads();
+        int64_t wb = 0, tot = 0;
+        for (int k = 0; k < (int)(blockDim.x / 32); k++) {
+            if (k < w) wb += wsum[k];
+            tot += wsum[k];
+        }
+        if (i < nchunks) offsets[i] = carry + wb + incl - v;
+        __syncthreads();
+        if (threadIdx.x == 0) carry += tot;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) total[0] = carry;
+}
+}  // namespace
+
+template <typename T>
+cudaError_t launch_pulse_events(const T* ref, int64_t n, double high, int64_t* counts,
+                                int64_t* offsets, int64_t* events, int64_t capacity,
+                                int64_t* total, cudaStream_t s) {
+    int64_t nchunks = (n + kPulseChunk - 1) / kPulseChunk;
+    if (nchunks == 0) {
+        cudaMemsetAsync(total, 0, sizeof(int64_t), s);
+        return cudaGetLastError();
+    }
+    k_pulse_pass<T, false><<<(unsigned)nchunks, kPT, 0, s>>>(ref, n, high, counts, nullptr, nullptr, 0);
+    k_scan_counts<<<1, 1024, 0, s>>>(counts, nchunks, offsets, total);
+    k_pulse_pass<T, true><<<(unsigned)nchunks, kPT, 0, s>>>(ref, n, high, counts, offsets, events,
+                                                           capacity);
+    return cudaGetLastError();
+}
+template cudaError_t launch_pulse_events<float>(const float*, int64_t, double, int64_t*, int64_t*,
+                                                int64_t*, int64_t, int64_t*, cudaStream_t);
+template cudaError_t launch_pulse_events<double>(const double*, int64_t, double, int64_t*, int64_t*,
+                                                 int64_t*, int64_t, int64_t*, cudaStream_t);
+
+// ============================================================== hsync refine
+// RefineLineLocationsFromHSync, VHS branch with right-edge refinement
+// (Core/Decode/TbcFieldDecodePipeline.cs:4570-4679, 4807-5050) and
+// PulseDetection.CalculateZeroCrossing (Core/Dsp/PulseDetection.cs:17-40,
+// 224-275).  One warp per field; lines are processed in order because the
+// back-porch level carries from line to line.
+namespace {
+
+__device__ __forceinline__ double round_away(double x) {
+    return x >= 0.0 ? floor(x + 0.5) : -floor(-x + 0.5);
+}
+
+template <typename T>
+struct Span {
+    const T* d;
+    int64_t n;
+    __device__ double at(int64_t i) const { return (double)d[i]; }
+};
+
+// first crossing of `target` at/after `start` within count+1 samples; NaN if none
+template <typename T>
+__device__ double zero_crossing(const Span<T>& s, int64_t start, double target, int edge, int count,
+                                int lane) {
+    if (edge == 0) edge = s.at(start) < target ? 1 : -1;
+    int64_t end = min(s.n, start + (int64_t)count + 1);
+    int64_t len = end - start;
+    for (int64_t base = 1; base < len; base += 32) {
+        int64_t i = base + lane;
+        bool hit = false;
+        if (i < len) {
+            double a = s.at(start + i - 1), b = s.at(start + i);
+            hit = edge == 1 ? (a < target && b >= target) : (a > target && b <= target);
+        }
+        unsigned m = __ballot_sync(0xffffffffu, hit);
+        if (m) {
+            int64_t x = start + base + (__ffs(m) - 1);
+            double a = s.at(x - 1) - target;
+            double b = s.at(x) - target;
+            double y = (b - a) != 0.0 ? -a / (-a + b) : 0.0;
+            return (double)(x - 1) + y;
+        }
+    }
+    return nan("");
+}
+
+template <typename T>
+__device__ bool area_ok(const Span<T>& s, double crossing, int one_us, double end_us, double lo_hz,
+                        double hi_hz, int lane) {
+    int64_t st = (int64_t)round_away(crossing - 0.75 * one_us);
+    st = st < 0 ? 0 : (st > s.n ? s.n : st);
+    int64_t en = (int64_t)round_away(crossing + end_us * one_us);
+    en = en < st ? st : (en > s.n ? s.n : en);
+    if (en <= st) return false;
+    double mn = INFINITY, mx = -INFINITY;
+    for (int64_t i = st + lane; i < en; i += 32) {
+        double v = s.at(i);
+        mn = fmin(mn, v);
+        mx = fmax(mx, v);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+        mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    }
+    return mn >= lo_hz && mx <= hi_hz;
+}
+
+template <typename T>
+__device__ bool mean_range(const Span<T>& s, double start, double end, double* mean, int lane) {
+    int64_t st = (int64_t)round_away(start);
+    st = st < 0 ? 0 : (st > s.n ? s.n : st);
+    int64_t en = (int64_t)round_away(end);
+    en = en < st ? st : (en > s.n ? s.n : en);
+    if (en <= st) { *mean = 0.0; return false; }
+    double sum = 0.0;
+    for (int64_t i = st + lane; i < en; i += 32) sum += s.at(i);
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    *mean = sum / (double)(en - st);
+    return true;
+}
+
+template <typename T>
+__global__ void k_hsync(const T* stream, int64_t stream_len, HsyncParams p) {
+    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int lane = threadIdx.x & 31;
+    if (warp >= p.nfields) return;
+    int64_t s0 = p.span_start[warp];
+    Span<T> sp{stream + s0, min(p.span_len[warp], stream_len - s0)};
+    const double* in = p.locs_in + (int64_t)warp * p.lines;
+    const uint8_t* fin = p.filled_in + (int64_t)warp * p.lines;
+    double* out = p.locs_out + (int64_t)warp * p.lines;
+    uint8_t* fout = p.filled_out + (int64_t)warp * p.lines;
+    auto ire_hz = [&](double ire) { return p.ire0 + p.hz_ire * ire; };
+    const int one = p.one_us, normal = p.normal_hsync;
+    const int search = one * 2 > 1 ? one * 2 : 1;
+    double prev_porch = -1.0;
+    for (int line = 0; line < p.lines; line++) {
+        double loc = in[line];
+        bool filled = fin[line] != 0;
+        bool vsync_line = (line >= 3 && line <= 6) || (p.pal && line >= 1 && line <= 2);
+        if (vsync_line) {
+            if (lane == 0) { out[line] = loc - p.ntsc_shift; fout[line] = 1; }
+            continue;
+        }
+        double refined = loc;
+        uint8_t fo = filled;
+        if (!isfinite(loc)) {
+            if (lane == 0) { out[line] = loc - p.ntsc_shift; fout[line] = fo; }
+            continue;
+        }
+        int64_t ss = (int64_t)round_away(loc - one);
+        if (ss < 0 || ss >= sp.n - 1) {
+            if (lane == 0) { out[line] = loc - p.ntsc_shift; fout[line] = fo; }
+            continue;
+        }
+        int cnt = (int)min((int64_t)search, sp.n - ss - 1);
+        double crossing = zero_crossing(sp, ss, p.threshold, 0, cnt, lane);
+        double original = loc;
+        double right_ref = original;
+        if (crossing == crossing && !filled) {
+            // TryRefineLeftHSync
+            bool ok = false, preserve = false;
+            double rloc = crossing, porch = 0.0, sync_lv = 0.0;
+            if (area_ok(sp, crossing, one, 3.5, ire_hz(-65.0), ire_hz(110.0), lane) &&
+                mean_range(sp, crossing + one, crossing + 2.5 * one, &sync_lv, lane)) {
+                preserve = true;
+                bool have_porch = true;
+                if (prev_porch > 0.0) porch = prev_porch;
+                else have_porch = mean_range(sp, crossing - one, crossing - 0.5 * one, &porch, lane);
+                if (have_porch) {
+                    int c2 = (int)min((int64_t)400, sp.n - ss - 1);
+                    double rc = zero_crossing(sp, ss, (porch + sync_lv) / 2.0, 0, c2, lane);
+                    if (!(rc == rc) || fabs(rc - crossing) >= one / 2.0) {
+                        if (prev_porch > 0.0) {
+                            rc = zero_crossing(sp, ss, (prev_porch + sync_lv) / 2.0, 0, c2, lane);
+                            if (rc == rc && fabs(rc - crossing) < one / 2.0) {
+                                porch = prev_porch;
+                                ok = true;
+                                rloc = rc;
+                            }
+                        }
+                    } else {
+                        ok = true;
+                        rloc = rc;
+                    }
+                }
+            }
+            if (ok) {
+                refined = rloc;
+                right_ref = rloc;
+                fo = fin[line];
+                if (porch > 0.0) prev_porch = porch;
+            } else {
+                fo = 1;
+                refined = original;
+                if (preserve) right_ref = crossing;
+            }
+        } else {
+            fo = 1;
+            refined = original;
+        }
+        // TryRefineFromRightHSync
+        {
+            int64_t rs = ss + normal - one;
+            if (rs >= 0 && rs < sp.n - 1 && !(sp.at(rs) > p.threshold)) {
+                int rcnt = (int)min((int64_t)max(1, normal * 2), sp.n - rs - 1);
+                double rcx = zero_crossing(sp, rs, p.threshold, 1, rcnt, lane);
+                if (rcx == rcx) {
+                    double derived = rcx - normal;
+                    double sync_lv = 0.0, porch = 0.0;
+                    if (area_ok(sp, derived, one, 8.0, ire_hz(-65.0), ire_hz(30.0), lane) &&
+                        mean_range(sp, derived + one, derived + 2.5 * one, &sync_lv, lane) &&
+                        mean_range(sp, derived + normal + one, derived + normal + 2.0 * one, &porch,
+                                   lane)) {
+                        int c2 = (int)min((int64_t)400, sp.n - rs - 1);
+                        double rr = zero_crossing(sp, rs, (porch + sync_lv) / 2.0, 0, c2, lane);
+                        if (rr == rr && fabs(rr - rcx) < one / 2.0) {
+                            double cand = rcx - normal + 2.25 * (p.mhz32 / 40.0);
+                            if (fabs(cand - right_ref) < one * 2.0) {
+                                refined = cand;
+                                fo = 0;
+                                if (porch > 0.0) prev_porch = porch;
+                            }
+                        }
+                    }
+                }
+            }
+        }
+        if (lane == 0) { out[line] = refined - p.ntsc_shift; fout[line] = fo; }
+    }
+}
+}  // namespace
+
+template <typename T>
+cudaError_t launch_hsync_refine(const T* stream, int64_t stream_len, const HsyncParams& p,
+                                cudaStream_t s) {
+    if (p.nfields <= 0) return cudaSuccess;
+    int threads = 128;
+    int blocks = (p.nfields * 32 + threads - 1) / threads;
+    k_hsync<T><<<blocks, threads, 0, s>>>(stream, stream_len, p);
+    return cudaGetLastError();
+}
+template cudaError_t launch_hsync_refine<float>(const float*, int64_t, const HsyncParams&, cudaStream_t);
+template cudaError_t launch_hsync_refine<double>(const double*, int64_t, const HsyncParams&, cudaStream_t);
+
+// ============================================================== TBC
+// TbcLineResampler linear plan (Core/Tbc/TbcLineResampler.cs:732-805,
+// 818-878, 997-1011, 1480-1532), SampleSinc (:1167-1234) and
+// VideoOutputConverter.FastMathConversion (Core/Tbc/VideoOutputConverter.cs:9-40).
+namespace {
+
+// Per field: line factors, median / MAD outlier replacement, smoothing chain.
+// level_work per field: [2 * maxl] = (adjusted factor, value before the line)
+__global__ void k_tbc_levels(TbcParams p, const double* pw_outlen) {
+    __shared__ double fac[512];
+    __shared__ double srt[512];
+    const int f = blockIdx.x;
+    const int fl = p.first_line[f];
+    const int nl = fl + p.out_lines;          // lines covered by the plan incl. prefix
+    const double* loc = p.locs + (int64_t)f * p.lines;
+    const double inv = 1.0 / p.nominal;
+    for (int l = threadIdx.x; l < 512; l += blockDim.x) {
+        double v = INFINITY;
+        if (l < nl) {
+            int left = l < p.lines - 2 ? l : p.lines - 2;
+            v = __dsub_rn(__dmul_rn(loc[left + 1], inv), __dmul_rn(loc[left], inv));
+        }
+        fac[l] = v;
+        srt[l] = v;
+    }
+    __syncthreads();
+    // bitonic sort of srt[0..512)
+    for (int k = 2; k <= 512; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = threadIdx.x; i < 512; i += blockDim.x) {
+                int ixj = i ^ j;
+                if (ixj > i) {
+                    bool up = (i & k) == 0;
+                    double a = srt[i], b = srt[ixj];
+                    if ((a > b) == up) { srt[i] = b; srt[ixj] = a; }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    __shared__ double med_s, mad_s;
+    if (threadIdx.x == 0) {
+        med_s = (nl & 1) ? srt[nl / 2] : (srt[nl / 2 - 1] + srt[nl / 2]) / 2.0;
+    }
+    __syncthreads();
+    double med = med_s;
+    for (int l = threadIdx.x; l < 512; l += blockDim.x) srt[l] = l < nl ? fabs(fac[l] - med) : INFINITY;
+    __syncthreads();
+    for (int k = 2; k <= 512; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = threadIdx.x; i < 512; i += blockDim.x) {
+                int ixj = i ^ j;
+                if (ixj > i) {
+                    bool up = (i & k) == 0;
+                    double a = srt[i], b = srt[ixj];
+                    if ((a > b) == up) { srt[i] = b; srt[ixj] = a; }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    if (threadIdx.x == 0) {
+        mad_s = (nl & 1) ? srt[nl / 2] : (srt[nl / 2 - 1] + srt[nl / 2]) / 2.0;
+    }
+    __syncthreads();
+    double mad = mad_s;
+    double thr = mad > 0.0 ? 15.0 * mad : 0.001;
+    for (int l = threadIdx.x; l < nl; l += blockDim.x) {
+        double v = fac[l];
+        fac[l] = fabs(v - med) > thr ? med : v;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double* w = p.level_work + (int64_t)f * 1024;
+        double prev = fac[0];
+        double rN = pw_outlen ? pw_outlen[p.outlen - 1] : 1.0;  // (1-alpha)^outlen
+        for (int l = 0; l < nl; l++) {
+            double a = fac[l];
+            w[2 * l] = a;
+            w[2 * l + 1] = (l == 0) ? a : prev;
+            if (p.smoothing > 0.0 && l > 0) prev = a + rN * (prev - a);
+            else prev = a;
+        }
+    }
+}
+
+__device__ __forceinline__ int wrap_idx(int i, int len) {
+    if (i < 0) i += len;
+    return i < 0 ? 0 : (i > len - 1 ? len - 1 : i);
+}
+
+template <typename T>
+__device__ __forceinline__ double sample_sinc(const T* src, int64_t n, double position, const float* lut) {
+    if (!isfinite(position)) return 0.0;
+    const int taps = 16, phases = 65536;
+    float coord = __double2float_rn(position);
+    int ci = (int)coord;
+    float fraction = __fsub_rn(coord, (float)ci);
+    float pp = __fmul_rn(fraction, (float)phases);
+    int ps = (int)pp;
+    int pe = ps + 1;
+    float alpha = __fsub_rn(pp, (float)ps);
+    ps = wrap_idx(ps, phases + 1);
+    pe = wrap_idx(pe, phases + 1);
+    const float* ws = lut + (int64_t)ps * taps;
+    const float* we = lut + (int64_t)pe * taps;
+    int start = ci - (taps / 2 - 1);
+    bool interior = n >= taps && (uint32_t)start <= (uint32_t)(n - taps);
+    double r = 0.0;
+#pragma unroll
+    for (int t = 0; t < taps; t++) {
+        float sw = __ldg(ws + t);
+        float w = __fmaf_rn(alpha, __fsub_rn(__ldg(we + t), sw), sw);
+        int64_t idx = (int64_t)start + t;
+        if (!interior) {
+            if (idx < 0) idx += n;
+            idx = idx < 0 ? 0 : (idx > n - 1 ? n - 1 : idx);
+        }
+        float prod = __fmul_rn((float)src[idx], w);
+        r = __dadd_rn((double)prod, r);
+    }
+    return r;
+}
+
+template <typename T>
+__global__ void k_tbc(const T* stream, int64_t stream_len, TbcParams p, const double* pw) {
+    const int f = blockIdx.y;
+    const int ol = blockIdx.x;
+    const int fl = p.first_line[f];
+    const int line = fl + ol;
+    const double* loc = p.locs + (int64_t)f * p.lines;
+    const int64_t s0 = p.span_start[f];
+    const int64_t n = min(p.span_len[f], stream_len - s0);
+    const T* src = stream + s0;
+    const double nominal = p.nominal;
+    const double out_scale = __ddiv_rn(nominal, (double)p.outlen);
+    const double* w = p.level_work + (int64_t)f * 1024;
+    const double adj = w[2 * line], before = w[2 * line + 1];
+    const double ll = loc[line];
+    const double delta = __dsub_rn(loc[line + 1], ll);
+    for (int k = threadIdx.x; k < p.outlen; k += blockDim.x) {
+        int64_t idx = (int64_t)line * p.outlen + k;
+        double scaled = __dmul_rn((double)idx, out_scale);
+        double frac = __ddiv_rn(__dsub_rn(scaled, __dmul_rn((double)line, nominal)), nominal);
+        frac = frac < 0.0 ? 0.0 : (frac > 1.0 ? 1.0 : frac);
+        double pos = __dadd_rn(ll, __dmul_rn(delta, frac));
+        double la = adj;
+        if (p.smoothing > 0.0 && line > 0) la = adj + pw[k] * (before - adj);
+        double v = sample_sinc(src, n, pos, p.lut);
+        double outv = (double)__double2float_rn(__dmul_rn(v, la));
+        int64_t o = ((int64_t)f * p.out_lines + ol) * p.outlen + k;
+        if (p.out_hz) p.out_hz[o] = outv;
+        if (p.out_u16) {
+            double sd = __dmul_rn(p.output_scale, __dsub_rn(outv, p.ire0));
+            double val = __fma_rn(sd, p.inv_hz_ire, p.offset);
+            uint16_t u = val <= 0.0 ? 0 : (val >= 65535.0 ? 65535 : (uint16_t)val);
+            p.out_u16[o] = u;
+        }
+    }
+}
+}  // namespace
+
+// pw must hold (1-alpha)^(k+1) for k in [0, outlen) when smoothing > 0.
+template <typename T>
+cudaError_t launch_tbc_pw(const T* stream, int64_t stream_len, const TbcParams& p, const double* pw,
+                          cudaStream_t s) {
+    if (p.nfields <= 0) return cudaSuccess;
+    k_tbc_levels<<<p.nfields, 256, 0, s>>>(p, pw);
+    dim3 grid(p.out_lines, p.nfields);
+    k_tbc<T><<<grid, 256, 0, s>>>(stream, stream_len, p, pw);
+    return cudaGetLastError();
+}
+template cudaError_t launch_tbc_pw<float>(const float*, int64_t, const TbcParams&, const double*, cudaStream_t);
+template cudaError_t launch_tbc_pw<double>(const double*, int64_t, const TbcParams&, const double*, cudaStream_t);
+
+// ============================================================== dropouts
+// DetectTapeDropouts + RfDropoutDetector.FindDropouts + TbcDropoutMapper.MapTapeRfToTbc
+// (Core/Decode/TbcFieldDecodePipeline.cs:6593-6640; Core/Decode/TbcDropoutMapping.cs:52-107, 288-370).
+// threshold = float32 mean of the envelope over the field span * 0.18f; the
+// device emits ordered run boundaries of (env <= thr) and starts of
+// (env >= thr * hysteresis) per 16384-sample chunk, then one thread per field
+// runs the merge state machine over those events and maps the ranges to
+// (field line, start x, end x).
+namespace {
+constexpr int kDT = 256;
+constexpr int kDChunk = 16384;
+constexpr int kDPer = kDChunk / kDT;
+
+__global__ void k_drop_ranges(DropoutParams p, int64_t stream_len) {
+    int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= p.nfields) return;
+    int64_t n = min(p.span_len[f], stream_len - p.span_start[f]);
+    const double* loc = p.locs + (int64_t)f * p.lines;
+    int sl = p.start_line[f], el = p.end_line[f];
+    int64_t r0 = 0, r1 = 0;
+    if (sl >= 0 && el > sl && sl < p.lines) {
+        double a = floor(loc[sl]);
+        r0 = a < 0 ? 0 : (a > (double)n ? n : (int64_t)a);
+        double b = ceil(loc[el]);
+        r1 = b < (double)r0 ? r0 : (b > (double)n ? n : (int64_t)b);
+    }
+    p.range[2 * f] = r0;
+    p.range[2 * f + 1] = r1;
+}
+
+template <typename T>
+__global__ void k_env_partial(const T* stream, int64_t stream_len, DropoutParams p, float* partial,
+                              int nchunk) {
+    __shared__ float wsum[kDT / 32];
+    const int f = blockIdx.y, c = blockIdx.x;
+    const int64_t s0 = p.span_start[f];
+    const int64_t n = min(p.span_len[f], stream_len - s0);
+    float acc = 0.0f;
+    for (int k = 0; k < kDPer; k++) {
+        int64_t i = (int64_t)c * kDChunk + k * kDT + threadIdx.x;
+        if (i < n) acc += (float)stream[s0 + i];
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float t = 0.0f;
+        for (int i = 0; i < kDT / 32; i++) t += wsum[i];
+        partial[(int64_t)f * nchunk + c] = t;
+    }
+}
+
+__global__ void k_env_mean(DropoutParams p, const float* partial, int nchunk, int64_t stream_len) {
+    int f = blockIdx.x;
+    if (threadIdx.x != 0) return;
+    float t = 0.0f;
+    for (int c = 0; c < nchunk; c++) t += partial[(int64_t)f * nchunk + c];
+    int64_t n = min(p.span_len[f], stream_len - p.span_start[f]);
+    p.mean_out[f] = t / (float)n;
+}
+
+// event = 4*pos + type; type 0: (env <= down) run start, 1: run end, 2: (env >= up) start
+template <typename T>
+__global__ void k_drop_events(const T* stream, int64_t stream_len, DropoutParams p, int nchunk,
+                              int* chunk_counts) {
+    __shared__ int wtot[kDT / 32];
+    const int f = blockIdx.y, c = blockIdx.x;
+    const int64_t s0 = p.span_start[f];
+    const T* env = stream + s0;
+    const int64_t r0 = p.range[2 * f], r1 = p.range[2 * f + 1];
+    const float thrf = __fmul_rn(p.mean_out[f], p.frac);
+    const double down = (double)thrf, up = (double)thrf * p.hyst;
+    const int64_t b0 = r0 + (int64_t)c * kDChunk + (int64_t)threadIdx.x * kDPer;
+    auto flags = [&](int64_t i, bool& a, bool& b) {
+        if (i < r0 || i >= r1) { a = false; b = false; return; }
+        double v = (double)env[i];
+        a = v <= down;
+        b = v >= up;
+    };
+    int cnt = 0;
+    bool pa, pb;
+    flags(b0 - 1, pa, pb);
+    for (int k = 0; k < kDPer; k++) {
+        int64_t i = b0 + k;
+        if (i > r1) break;
+        bool a, b;
+        flags(i, a, b);
+        if (a != pa) cnt++;
+        if (b && !pb) cnt++;
+        pa = a; pb = b;
+    }
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int incl = cnt;
+    for (int o = 1; o < 32; o <<= 1) {
+        int t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    if (lane == 31) wtot[w] = incl;
+    __syncthreads();
+    int wb = 0, tot = 0;
+    for (int i = 0; i < kDT / 32; i++) { if (i < w) wb += wtot[i]; tot += wtot[i]; }
+    if (threadIdx.x == 0) chunk_counts[(int64_t)f * nchunk + c] = tot;
+    int off = wb + incl - cnt;
+    int64_t* ev = p.events + ((int64_t)f * nchunk + c) * p.cap;
+    flags(b0 - 1, pa, pb);
+    for (int k = 0; k < kDPer; k++) {
+        int64_t i = b0 + k;
+        if (i > r1) break;
+        bool a, b;
+        flags(i, a, b);
+        if (a != pa) { if (off < p.cap) ev[off] = 4 * i + (a ? 0 : 1); off++; }
+        if (b && !pb) { if (off < p.cap) ev[off] = 4 * i + 2; off++; }
+        pa = a; pb = b;
+    }
+}
+
+// One thread per field: merge state machine, minimum length, TBC mapping.
+__global__ void k_drop_finish(DropoutParams p, int nchunk, const int* chunk_counts) {
+    int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= p.nfields) return;
+    const int64_t r1 = p.range[2 * f + 1];
+    int32_t* out = p.out + (int64_t)f * p.out_cap * 3;
+    int nout = 0;
+    int status = 0;
+    const double* loc = p.locs + (int64_t)f * p.lines;
+    const int sl = p.start_line[f], el = p.end_line[f], off = p.line_offset[f];
+    // mapping state (MapTapeRfToTbc)
+    int li = sl;
+    double ls = 0.0, le = 0.0;
+    bool map_ok = sl >= 0 && el > sl && el < p.lines;
+    if (map_ok) { ls = loc[li]; le = loc[li + 1]; }
+    bool map_done = !map_ok;
+    auto emit = [&](int line, int sx, int ex) {
+        if (nout < p.out_cap) {
+            out[3 * nout] = line; out[3 * nout + 1] = sx; out[3 * nout + 2] = ex;
+        } else {
+            status = 1;
+        }
+        nout++;
+    };
+    auto map_range = [&](double ds, double de) {
+        if (map_done) return;
+        bool found = false;
+        int cur_line = 0, cur_sx = 0;
+        while (li < el) {
+            double ll = le - ls;
+            if ((ds >= ls || li == sl) && ds < le && ll > 0.0) {
+                int sx = (int)floor(((ds - ls) / ll) * p.outlen);
+                cur_line = li - off;
+                cur_sx = sx > 0 ? sx : 0;
+                found = true;
+                break;
+            }
+            li++;
+            if (li < el) { ls = loc[li]; le = loc[li + 1]; }
+        }
+        if (!found) { map_done = true; return; }
+        while (li < el) {
+            double ll = le - ls;
+            if (de < le && ll > 0.0) {
+                int ex = (int)ceil(((de - ls) / ll) * p.outlen);
+                emit(cur_line, cur_sx, ex < p.outlen ? ex : p.outlen);
+                break;
+            }
+            emit(cur_line, cur_sx, p.outlen);
+            li++;
+            if (li < el) {
+                ls = loc[li]; le = loc[li + 1];
+                cur_line = li - off;
+                cur_sx = 0;
+            }
+        }
+    };
+    bool have = false, open = false, pending = false;
+    int64_t start = 0, last_end = 0, cand = 0;
+    for (int c = 0; c < nchunk; c++) {
+        int cnt = chunk_counts[(int64_t)f * nchunk + c];
+        if (cnt > p.cap) { status = 2; cnt = p.cap; }
+        const int64_t* ev = p.events + ((int64_t)f * nchunk + c) * p.cap;
+        for (int e = 0; e < cnt; e++) {
+            int64_t pos = ev[e] >> 2;
+            int type = (int)(ev[e] & 3);
+            if (type == 0) {
+                if (!have) { start = pos; open = true; have = true; }
+                else if (!open) {
+                    int64_t c2 = last_end + p.merge + 1;
+                    cand = pos > c2 ? pos : c2;
+                    pending = true;
+                }
+            } else if (type == 1) {
+                if (pending) {
+                    if (cand < pos) { start = cand; open = true; }
+                    pending = false;
+                }
+            } else {
+                if (have && open) {
+                    open = false;
+                    last_end = pos;
+                    if (pos - start > p.min_len) map_range((double)start, (double)pos);
+                }
+            }
+        }
+    }
+    if (have && open && r1 - start > p.min_len) map_range((double)start, (double)r1);
+    p.out_count[f] = nout;
+    p.status[f] = status;
+}
+}  // namespace
+
+int dropout_chunks(int64_t span_len) { return (int)((span_len + kDChunk - 1) / kDChunk); }
+
+template <typename T>
+cudaError_t launch_dropouts_full(const T* stream, int64_t stream_len, const DropoutParams& p,
+                                 float* partial, int* chunk_counts, cudaStream_t s) {
+    if (p.nfields <= 0) return cudaSuccess;
+    int nchunk = dropout_chunks(p.max_span_len);
+    k_drop_ranges<<<(p.nfields + 127) / 128, 128, 0, s>>>(p, stream_len);
+    dim3 g(nchunk, p.nfields);
+    k_env_partial<T><<<g, kDT, 0, s>>>(stream, stream_len, p, partial, nchunk);
+    k_env_mean<<<p.nfields, 32, 0, s>>>(p, partial, nchunk, stream_len);
+    k_drop_events<T><<<g, kDT, 0, s>>>(stream, stream_len, p, nchunk, chunk_counts);
+    k_drop_finish<<<(p.nfields + 63) / 64, 64, 0, s>>>(p, nchunk, chunk_counts);
+    return cudaGetLastError();
+}
+template cudaError_t launch_dropouts_full<float>(const float*, int64_t, const DropoutParams&, float*, int*, cudaStream_t);
+template cudaError_t launch_dropouts_full<double>(const double*, int64_t, const DropoutParams&, float*, int*, cudaStream_t);
+
+}  // namespace vhsd

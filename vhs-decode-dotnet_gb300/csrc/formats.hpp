@@ -1,0 +1,81 @@
+// Format parameters for the supported tape formats.
+//
+// Values restate the frozen upstream parameter snapshot the reference embeds
+// (src/VHSDecode.Core/Formats/format-params.snapshot.json, cases PAL/VHS/sp and
+// NTSC/VHS/sp, read by Core/Formats/FormatCatalog.cs:46-112); only the keys the
+// RF -> TBC luma path reads are kept.
+#pragma once
+#include <cmath>
+#include <cstdint>
+
+namespace vhsd {
+
+struct FormatParams {
+    // system
+    bool pal;
+    double fps, ire0, hz_ire, vsync_ire, line_period_us;
+    double hsync_us, eq_us, vsync_us;
+    int num_pulses, outlinelen, frame_lines, output_zero;
+    double outfreq_mhz, fsc_mhz;
+    // RF video band-pass
+    double bpf_low, bpf_high;
+    int bpf_order;                // 0 = none (magnitude path), >0 Butterworth band-pass
+    double lpf_extra, hpf_extra;  // 0 = absent
+    int lpf_extra_order, hpf_extra_order;
+    double peak_freq, peak_gain, peak_bandwidth;
+    bool has_ramp;
+    double ramp_start, ramp_boost0, ramp_boost20;
+    bool ramp_double;
+    // video low-pass / de-emphasis
+    double video_lpf_freq;
+    int video_lpf_order;
+    bool video_lpf_supergauss;
+    double deemph_gain, deemph_mid, deemph_q;
+    double color_under;
+};
+
+inline FormatParams pal_vhs_sp() {
+    FormatParams f{};
+    f.pal = true;
+    f.fps = 25.0; f.ire0 = 4100000.0; f.hz_ire = 7000.0; f.vsync_ire = -42.857142857142854;
+    f.line_period_us = 64.0; f.hsync_us = 4.7; f.eq_us = 2.35; f.vsync_us = 27.3;
+    f.num_pulses = 5; f.outlinelen = 1135; f.frame_lines = 625; f.output_zero = 256;
+    f.outfreq_mhz = 17.734475; f.fsc_mhz = 4.43361875;
+    f.bpf_low = 1300000.0; f.bpf_high = 5780000.0; f.bpf_order = 0;
+    f.lpf_extra = 5910000.0; f.lpf_extra_order = 20;
+    f.hpf_extra = 1320000.0; f.hpf_extra_order = 12;
+    f.peak_freq = 4300000.0; f.peak_gain = 4.0; f.peak_bandwidth = 10000000.0;
+    f.has_ramp = true; f.ramp_start = 626953.0; f.ramp_boost0 = 0.0; f.ramp_boost20 = 1.0;
+    f.ramp_double = false;
+    f.video_lpf_freq = 3400000.0; f.video_lpf_order = 6; f.video_lpf_supergauss = false;
+    f.deemph_gain = 13.9794; f.deemph_mid = 273755.82; f.deemph_q = 0.462088186;
+    f.color_under = 626953.0;
+    return f;
+}
+
+inline FormatParams ntsc_vhs_sp() {
+    FormatParams f{};
+    f.pal = false;
+    f.fps = 29.970029970029973; f.ire0 = 3685714.2857142854; f.hz_ire = 7142.857142857143;
+    f.vsync_ire = -40.0; f.line_period_us = 63.55555555555555; f.hsync_us = 4.7; f.eq_us = 2.3;
+    f.vsync_us = 27.1; f.num_pulses = 6; f.outlinelen = 910; f.frame_lines = 525;
+    f.output_zero = 1024; f.outfreq_mhz = 14.318181818181818; f.fsc_mhz = 3.5795454545454546;
+    f.bpf_low = 500000.0; f.bpf_high = 6500000.0; f.bpf_order = 8;
+    f.lpf_extra = 6000000.0; f.lpf_extra_order = 25;
+    f.hpf_extra = 1200000.0; f.hpf_extra_order = 20;
+    f.peak_freq = 3900000.0; f.peak_gain = 4.0; f.peak_bandwidth = 10000000.0;
+    f.has_ramp = true; f.ramp_start = 629370.6293706294; f.ramp_boost0 = 0.0; f.ramp_boost20 = 1.0;
+    f.ramp_double = false;
+    f.video_lpf_freq = 6600000.0; f.video_lpf_order = 9; f.video_lpf_supergauss = true;
+    f.deemph_gain = 13.9794; f.deemph_mid = 273755.82; f.deemph_q = 0.462088186;
+    f.color_under = 629370.6293706294;
+    return f;
+}
+
+// VideoOutputConverter.ComputeOutputScale (Core/Tbc/VideoOutputConverter.cs:129-138)
+inline double output_scale(const FormatParams& f) {
+    double dividend = f.pal ? (double)(0xD300 - 0x0100) : (double)(0xC800 - 0x0400);
+    return dividend / (100.0 - f.vsync_ire);
+}
+
+}  // namespace vhsd

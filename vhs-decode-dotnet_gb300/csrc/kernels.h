@@ -1,0 +1,146 @@
+// Device-side entry points of the VHS RF decode path and their parameter
+// blocks.  All pointers are device pointers unless noted.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace vhsd {
+
+constexpr int kBlock = 32768;
+constexpr int kCut = 1024;
+constexpr int kStride = 30720;
+constexpr int kHalf = 16385;  // kBlock/2 + 1 spectrum bins
+
+// ---------------------------------------------------------------- FP32 fused
+struct FastDemodParams {
+    const int16_t* rf;         // capture, 16-byte aligned
+    int64_t first_block;       // first 32768-sample block to decode
+    int64_t nblocks;           // number of blocks
+    const float* rf_video;     // [kHalf] real RF band-pass gain
+    const float2* video;       // [kHalf] video LPF x de-emphasis
+    const float2* sync;        // [kHalf] video reference x 0.5 MHz FIR
+    const float2* tw_hi;       // [256] exp(-2 pi i h 128 / 32768)
+    const float2* tw_lo;       // [128] exp(-2 pi i l / 32768)
+    float fs;                  // sample rate (Hz)
+    float diff_max;            // diff-demod spike limit (Hz)
+    float dc;                  // subtracted before the demod FFT and added back
+    float env_b0, env_b1, env_a1;
+    float* video_out;          // stitched stream, stream index s = b*30720 + n - 1024
+    float* sync_out;
+    float* env_out;
+    float2* scratch;           // repair scratch: per cluster 2*32768 float2
+    float* scratch_raw;        // repair scratch: per cluster 32768 float
+    int* repair_count;         // counts blocks that took the spike-repair path
+};
+
+size_t fp32_smem_bytes();
+cudaError_t launch_demod_fp32(const FastDemodParams& p, int num_clusters, cudaStream_t stream);
+
+// ---------------------------------------------------------------- FP64 plain
+struct PlainDemodParams {
+    const int16_t* rf;
+    int64_t block;             // block index
+    const double* rf_video;    // [kHalf]
+    const double2* video;      // [kHalf]
+    const double2* sync;       // [kHalf]
+    double fs, diff_max;
+    double env_b0, env_b1, env_a1;
+    double* video_out;         // stitched stream (double)
+    double* sync_out;
+    double* env_out;
+    double2* work;             // per-block workspace: 4 * 32768 double2
+    double* dwork;             // per-block workspace: 3 * 32768 double
+    float* fwork;              // 32768 + 12 floats (envelope)
+    int* flag;                 // spike flag
+    unsigned* mask;            // 1024 words
+    int64_t* blk;              // device-resident block index, advanced per replay
+};
+cudaError_t launch_demod_fp64_block(const PlainDemodParams& p, cudaStream_t stream);
+
+// ---------------------------------------------------------------- pulses
+// Sync-pulse edge events of PulseDetection.FindPulses over a whole stitched
+// stream: starts (value <= high after > high) and ends (value > high after
+// <= high), NaN samples hold the state.  Two passes: count per chunk, then
+// ordered write.
+template <typename T>
+cudaError_t launch_pulse_events(const T* ref, int64_t n, double high, int64_t* counts,
+                                int64_t* offsets_scratch, int64_t* events, int64_t capacity,
+                                int64_t* total, cudaStream_t stream);
+constexpr int kPulseChunk = 4096;
+
+// ---------------------------------------------------------------- hsync refine
+struct HsyncParams {
+    int nfields;
+    int lines;                 // line locations per field
+    const double* locs_in;     // [nfields * lines] span-relative
+    const uint8_t* filled_in;  // [nfields * lines]
+    double* locs_out;
+    uint8_t* filled_out;
+    const int64_t* span_start; // [nfields] stream index of each field span
+    const int64_t* span_len;   // [nfields] span length
+    int pal;                   // PAL vsync-line rule
+    double threshold;          // sync threshold (Hz)
+    int one_us, normal_hsync;  // samples
+    double mhz32;              // (float)sample_rate_MHz
+    double ire0, hz_ire;
+    double ntsc_shift;         // subtracted after refinement (0 for PAL)
+};
+template <typename T>
+cudaError_t launch_hsync_refine(const T* sync_stream, int64_t stream_len, const HsyncParams& p,
+                                cudaStream_t stream);
+
+// ---------------------------------------------------------------- TBC
+struct TbcParams {
+    int nfields;
+    int lines;                  // line locations per field
+    const double* locs;         // [nfields * lines]
+    const int64_t* span_start;  // [nfields]
+    const int64_t* span_len;    // [nfields]
+    const int* first_line;      // [nfields] output first line
+    int out_lines;              // output lines per field
+    int outlen;                 // samples per output line
+    double nominal;             // nominal input line length (samples)
+    double smoothing;           // wow level-adjust smoothing (lines)
+    const float* lut;           // [(65536+1)*16] sinc LUT
+    double ire0, output_scale, inv_hz_ire, offset;  // uint16 conversion
+    uint16_t* out_u16;          // [nfields * out_lines * outlen] or null
+    double* out_hz;             // optional float output (values rounded to float)
+    double* level_work;         // [nfields * (max_first_line + out_lines)] line factors
+};
+// pw[k] = (1 - alpha)^(k+1), k < outlen, alpha = 1 / (smoothing * outlen)
+template <typename T>
+cudaError_t launch_tbc_pw(const T* video_stream, int64_t stream_len, const TbcParams& p,
+                          const double* pw, cudaStream_t stream);
+
+// ---------------------------------------------------------------- dropouts
+struct DropoutParams {
+    int nfields;
+    const int64_t* span_start;  // [nfields]
+    const int64_t* span_len;    // [nfields]
+    int64_t max_span_len;       // bound of span_len, sizes the per-chunk buffers
+    const double* locs;         // [nfields * lines] refined line locations
+    int lines;
+    const int* start_line;      // [nfields] lineOffset + 1
+    const int* end_line;        // [nfields]
+    const int* line_offset;     // [nfields]
+    int outlen;
+    int64_t* range;             // [nfields * 2] span-relative [start, end), written on device
+    float frac;                 // 0.18
+    double hyst;                // 1.25
+    int merge;                  // 30
+    int min_len;                // 10
+    float* mean_out;            // [nfields] float32 envelope mean over the span
+    int64_t* events;            // [nfields * nchunk * cap] 4*pos + type, per 16384-sample chunk
+    int cap;                    // events per chunk
+    int32_t* out;               // [nfields * out_cap * 3] (field line, start x, end x)
+    int out_cap;
+    int* out_count;             // [nfields]
+    int* status;                // [nfields] 0 ok, 1 output capacity, 2 event capacity
+};
+int dropout_chunks(int64_t span_len);
+// partial: [nfields * nchunk] floats; chunk_counts: [nfields * nchunk]
+template <typename T>
+cudaError_t launch_dropouts_full(const T* env_stream, int64_t stream_len, const DropoutParams& p,
+                                 float* partial, int* chunk_counts, cudaStream_t stream);
+
+}  // namespace vhsd
