@@ -66,7 +66,7 @@ def peaks():
 
 def profile_traffic_per_block():
     """DRAM bytes per block of the fused demodulator from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "demod_fp32_ntsc.md")
+    p = os.path.join(ROOT, "profiles", "demod_fp32_pal4.md")
     if not os.path.exists(p):
         return None
     for line in open(p):

@@ -13,6 +13,7 @@
 #include <cmath>
 #include <complex>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <new>
@@ -187,6 +188,8 @@ struct vhsdecode_gb300_session {
     int64_t pc_capacity = 0;
     DevBuf<double> locs_in, locs_out;
     DevBuf<uint8_t> fill_in, fill_out;
+    DevBuf<unsigned char> hsync_work;
+    DevBuf<int> hsync_misses;
     DevBuf<int64_t> span_start_d, span_len_d;
     DevBuf<int> first_line_d, start_line_d, end_line_d, line_off_d;
     DevBuf<float> lut;
@@ -317,6 +320,8 @@ void session_init(vhsdecode_gb300_session* s, const vhsdecode_gb300_session_conf
     size_t fl = (size_t)s->max_fields * s->lines;
     s->locs_in.alloc(fl); s->locs_out.alloc(fl);
     s->fill_in.alloc(fl); s->fill_out.alloc(fl);
+    s->hsync_work.alloc(hsync_work_bytes(s->max_fields, s->lines));
+    s->hsync_misses.alloc(1);
     s->span_start_d.alloc(s->max_fields);
     s->span_len_d.alloc(s->max_fields);
     s->first_line_d.alloc(s->max_fields); s->start_line_d.alloc(s->max_fields);
@@ -514,7 +519,14 @@ void run_fields(vhsdecode_gb300_session* s, const T* video, const T* sync, const
     hp.ire0 = sp.ire0;
     hp.hz_ire = sp.hz_ire;
     hp.ntsc_shift = sp.pal ? 0.0 : ((117.25 / 360.0) / sp.fsc_mhz) * sp.mhz;
+    hp.work = s->hsync_work.p;
+    hp.misses = nullptr;
+    const bool timing = std::getenv("VHSD_STAGE_TIMING") != nullptr;
+    cudaEvent_t st[4] = {};
+    if (timing) for (auto& e : st) ck(cudaEventCreate(&e), "event");
+    if (timing) ck(cudaEventRecord(st[0], cs), "event");
     ck(launch_hsync_refine<T>(sync, stream_len, hp, cs), "hsync launch");
+    if (timing) ck(cudaEventRecord(st[1], cs), "event");
     TbcParams tp{};
     tp.nfields = nf;
     tp.lines = s->lines;
@@ -535,6 +547,7 @@ void run_fields(vhsdecode_gb300_session* s, const T* video, const T* sync, const
     tp.out_hz = nullptr;
     tp.level_work = s->level_work.p;
     ck(launch_tbc_pw<T>(video, stream_len, tp, s->pw.p, cs), "tbc launch");
+    if (timing) ck(cudaEventRecord(st[2], cs), "event");
     DropoutParams dp{};
     dp.nfields = nf;
     dp.span_start = s->span_start_d.p;
@@ -560,6 +573,17 @@ void run_fields(vhsdecode_gb300_session* s, const T* video, const T* sync, const
     dp.status = s->drop_status.p;
     ck(launch_dropouts_full<T>(env, stream_len, dp, s->drop_partial.p, s->drop_counts.p, cs),
        "dropout launch");
+    if (timing) {
+        ck(cudaEventRecord(st[3], cs), "event");
+        ck(cudaEventSynchronize(st[3]), "sync");
+        float a = 0, b = 0, c = 0;
+        cudaEventElapsedTime(&a, st[0], st[1]);
+        cudaEventElapsedTime(&b, st[1], st[2]);
+        cudaEventElapsedTime(&c, st[2], st[3]);
+        std::fprintf(stderr, "[gb300 stage] fields=%d host_control=%.3f ms hsync=%.3f ms tbc=%.3f ms dropouts=%.3f ms\n",
+                     nf, host_ms, a, b, c);
+        for (auto& e : st) cudaEventDestroy(e);
+    }
     std::vector<double> refined((size_t)nf * s->lines);
     std::vector<int> dcount(nf), dstat(nf);
     ck(cudaMemcpyAsync(refined.data(), s->locs_out.p, refined.size() * sizeof(double), cudaMemcpyDeviceToHost, cs), "d2h");

@@ -215,115 +215,186 @@ __device__ bool mean_range(const Span<T>& s, double start, double end, double* m
     return true;
 }
 
+// Per-line quantities of the refinement that do not depend on the porch
+// level carried between lines (phase 1, one warp per line), the speculative
+// midpoint crossing for "carried porch = previous line's right-edge porch"
+// (phase 2), and the sequential carry over lines (phase 3, one warp per
+// field, which repeats a search only when the speculation missed).
+struct LineInfo {
+    double loc;      // input location
+    double crossing; // threshold crossing from round(loc - 1us), NaN if none
+    double sync;     // mean sync level after the crossing
+    double own_porch;
+    double rc_own;   // midpoint crossing with own porch, NaN if none
+    double rc_spec;  // midpoint crossing with the previous line's right porch, NaN if none
+    double r_porch;  // right-edge porch level (NaN if the right refinement is invalid)
+    double r_cand;   // right-edge candidate location
+    int64_t ss;      // search start
+    int flags;       // bit0 vsync line, bit1 usable (finite, ss in range), bit2 area+sync ok,
+                     // bit3 own porch valid, bit4 right candidate valid, bit5 filled in
+    int pad;
+};
+
 template <typename T>
-__global__ void k_hsync(const T* stream, int64_t stream_len, HsyncParams p) {
-    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    int lane = threadIdx.x & 31;
-    if (warp >= p.nfields) return;
-    int64_t s0 = p.span_start[warp];
-    Span<T> sp{stream + s0, min(p.span_len[warp], stream_len - s0)};
-    const double* in = p.locs_in + (int64_t)warp * p.lines;
-    const uint8_t* fin = p.filled_in + (int64_t)warp * p.lines;
-    double* out = p.locs_out + (int64_t)warp * p.lines;
-    uint8_t* fout = p.filled_out + (int64_t)warp * p.lines;
-    auto ire_hz = [&](double ire) { return p.ire0 + p.hz_ire * ire; };
+__global__ void k_hsync_lines(const T* stream, int64_t stream_len, HsyncParams p, LineInfo* info) {
+    const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (gw >= (int64_t)p.nfields * p.lines) return;
+    const int f = (int)(gw / p.lines), line = (int)(gw % p.lines);
+    const int64_t s0 = p.span_start[f];
+    Span<T> sp{stream + s0, min(p.span_len[f], stream_len - s0)};
+    const double loc = p.locs_in[gw];
     const int one = p.one_us, normal = p.normal_hsync;
     const int search = one * 2 > 1 ? one * 2 : 1;
-    double prev_porch = -1.0;
-    for (int line = 0; line < p.lines; line++) {
-        double loc = in[line];
-        bool filled = fin[line] != 0;
-        bool vsync_line = (line >= 3 && line <= 6) || (p.pal && line >= 1 && line <= 2);
-        if (vsync_line) {
-            if (lane == 0) { out[line] = loc - p.ntsc_shift; fout[line] = 1; }
-            continue;
-        }
-        double refined = loc;
-        uint8_t fo = filled;
-        if (!isfinite(loc)) {
-            if (lane == 0) { out[line] = loc - p.ntsc_shift; fout[line] = fo; }
-            continue;
-        }
-        int64_t ss = (int64_t)round_away(loc - one);
-        if (ss < 0 || ss >= sp.n - 1) {
-            if (lane == 0) { out[line] = loc - p.ntsc_shift; fout[line] = fo; }
-            continue;
-        }
+    auto ire_hz = [&](double ire) { return p.ire0 + p.hz_ire * ire; };
+    LineInfo li;
+    li.loc = loc;
+    li.crossing = li.sync = li.own_porch = li.rc_own = li.rc_spec = li.r_porch = li.r_cand = nan("");
+    li.ss = 0;
+    li.pad = 0;
+    int flags = p.filled_in[gw] ? 32 : 0;
+    bool vsync_line = (line >= 3 && line <= 6) || (p.pal && line >= 1 && line <= 2);
+    if (vsync_line) flags |= 1;
+    int64_t ss = isfinite(loc) ? (int64_t)round_away(loc - one) : -1;
+    if (!vsync_line && isfinite(loc) && ss >= 0 && ss < sp.n - 1) {
+        flags |= 2;
+        li.ss = ss;
         int cnt = (int)min((int64_t)search, sp.n - ss - 1);
         double crossing = zero_crossing(sp, ss, p.threshold, 0, cnt, lane);
-        double original = loc;
-        double right_ref = original;
-        if (crossing == crossing && !filled) {
-            // TryRefineLeftHSync
-            bool ok = false, preserve = false;
-            double rloc = crossing, porch = 0.0, sync_lv = 0.0;
+        li.crossing = crossing;
+        if (crossing == crossing) {
+            double sync_lv = 0.0, porch = 0.0;
             if (area_ok(sp, crossing, one, 3.5, ire_hz(-65.0), ire_hz(110.0), lane) &&
                 mean_range(sp, crossing + one, crossing + 2.5 * one, &sync_lv, lane)) {
-                preserve = true;
-                bool have_porch = true;
-                if (prev_porch > 0.0) porch = prev_porch;
-                else have_porch = mean_range(sp, crossing - one, crossing - 0.5 * one, &porch, lane);
-                if (have_porch) {
+                flags |= 4;
+                li.sync = sync_lv;
+                if (mean_range(sp, crossing - one, crossing - 0.5 * one, &porch, lane)) {
+                    flags |= 8;
+                    li.own_porch = porch;
                     int c2 = (int)min((int64_t)400, sp.n - ss - 1);
-                    double rc = zero_crossing(sp, ss, (porch + sync_lv) / 2.0, 0, c2, lane);
-                    if (!(rc == rc) || fabs(rc - crossing) >= one / 2.0) {
-                        if (prev_porch > 0.0) {
-                            rc = zero_crossing(sp, ss, (prev_porch + sync_lv) / 2.0, 0, c2, lane);
-                            if (rc == rc && fabs(rc - crossing) < one / 2.0) {
-                                porch = prev_porch;
-                                ok = true;
-                                rloc = rc;
-                            }
+                    li.rc_own = zero_crossing(sp, ss, (porch + sync_lv) / 2.0, 0, c2, lane);
+                }
+            }
+        }
+        // right edge (independent of the carried porch level)
+        int64_t rs = ss + normal - one;
+        if (rs >= 0 && rs < sp.n - 1 && !(sp.at(rs) > p.threshold)) {
+            int rcnt = (int)min((int64_t)max(1, normal * 2), sp.n - rs - 1);
+            double rcx = zero_crossing(sp, rs, p.threshold, 1, rcnt, lane);
+            if (rcx == rcx) {
+                double derived = rcx - normal;
+                double sync_lv = 0.0, porch = 0.0;
+                if (area_ok(sp, derived, one, 8.0, ire_hz(-65.0), ire_hz(30.0), lane) &&
+                    mean_range(sp, derived + one, derived + 2.5 * one, &sync_lv, lane) &&
+                    mean_range(sp, derived + normal + one, derived + normal + 2.0 * one, &porch, lane)) {
+                    int c2 = (int)min((int64_t)400, sp.n - rs - 1);
+                    double rr = zero_crossing(sp, rs, (porch + sync_lv) / 2.0, 0, c2, lane);
+                    if (rr == rr && fabs(rr - rcx) < one / 2.0) {
+                        flags |= 16;
+                        li.r_porch = porch;
+                        li.r_cand = rcx - normal + 2.25 * (p.mhz32 / 40.0);
+                    }
+                }
+            }
+        }
+    }
+    li.flags = flags;
+    if (lane == 0) info[gw] = li;
+}
+
+template <typename T>
+__global__ void k_hsync_spec(const T* stream, int64_t stream_len, HsyncParams p, LineInfo* info) {
+    const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (gw >= (int64_t)p.nfields * p.lines) return;
+    const int line = (int)(gw % p.lines);
+    if (line == 0) return;
+    LineInfo& li = info[gw];
+    const LineInfo& prev = info[gw - 1];
+    if (!(li.flags & 4) || !(prev.flags & 16) || !(prev.r_porch > 0.0)) return;
+    const int f = (int)(gw / p.lines);
+    const int64_t s0 = p.span_start[f];
+    Span<T> sp{stream + s0, min(p.span_len[f], stream_len - s0)};
+    int c2 = (int)min((int64_t)400, sp.n - li.ss - 1);
+    double rc = zero_crossing(sp, li.ss, (prev.r_porch + li.sync) / 2.0, 0, c2, lane);
+    if (lane == 0) li.rc_spec = rc;
+}
+
+template <typename T>
+__global__ void k_hsync_chain(const T* stream, int64_t stream_len, HsyncParams p, const LineInfo* info,
+                              int* misses) {
+    const int f = blockIdx.x;
+    const int lane = threadIdx.x;
+    const int64_t s0 = p.span_start[f];
+    Span<T> sp{stream + s0, min(p.span_len[f], stream_len - s0)};
+    const LineInfo* fi = info + (int64_t)f * p.lines;
+    const int one = p.one_us;
+    double pp = -1.0;
+    double prev_r = nan("");
+    int miss = 0;
+    for (int line = 0; line < p.lines; line++) {
+        const LineInfo li = fi[line];
+        double out = li.loc;
+        uint8_t fo = (li.flags & 32) ? 1 : 0;
+        const bool filled = (li.flags & 32) != 0;
+        if (li.flags & 1) {
+            fo = 1;
+        } else if (li.flags & 2) {
+            double right_ref = li.loc;
+            double refined = li.loc;
+            if (li.crossing == li.crossing && !filled) {
+                bool ok = false, preserve = false;
+                double rloc = 0.0, porch = 0.0;
+                if (li.flags & 4) {
+                    preserve = true;
+                    double rc = nan("");
+                    bool have = true;
+                    if (pp > 0.0) {
+                        porch = pp;
+                        if (pp == prev_r) {
+                            rc = li.rc_spec;
+                        } else {
+                            miss++;
+                            int c2 = (int)min((int64_t)400, sp.n - li.ss - 1);
+                            rc = zero_crossing(sp, li.ss, (pp + li.sync) / 2.0, 0, c2, lane);
                         }
+                    } else if (li.flags & 8) {
+                        porch = li.own_porch;
+                        rc = li.rc_own;
                     } else {
+                        have = false;
+                    }
+                    if (have && rc == rc && fabs(rc - li.crossing) < one / 2.0) {
                         ok = true;
                         rloc = rc;
                     }
                 }
-            }
-            if (ok) {
-                refined = rloc;
-                right_ref = rloc;
-                fo = fin[line];
-                if (porch > 0.0) prev_porch = porch;
+                if (ok) {
+                    refined = rloc;
+                    right_ref = rloc;
+                    fo = filled ? 1 : 0;
+                    if (porch > 0.0) pp = porch;
+                } else {
+                    fo = 1;
+                    if (preserve) right_ref = li.crossing;
+                }
             } else {
                 fo = 1;
-                refined = original;
-                if (preserve) right_ref = crossing;
             }
-        } else {
-            fo = 1;
-            refined = original;
-        }
-        // TryRefineFromRightHSync
-        {
-            int64_t rs = ss + normal - one;
-            if (rs >= 0 && rs < sp.n - 1 && !(sp.at(rs) > p.threshold)) {
-                int rcnt = (int)min((int64_t)max(1, normal * 2), sp.n - rs - 1);
-                double rcx = zero_crossing(sp, rs, p.threshold, 1, rcnt, lane);
-                if (rcx == rcx) {
-                    double derived = rcx - normal;
-                    double sync_lv = 0.0, porch = 0.0;
-                    if (area_ok(sp, derived, one, 8.0, ire_hz(-65.0), ire_hz(30.0), lane) &&
-                        mean_range(sp, derived + one, derived + 2.5 * one, &sync_lv, lane) &&
-                        mean_range(sp, derived + normal + one, derived + normal + 2.0 * one, &porch,
-                                   lane)) {
-                        int c2 = (int)min((int64_t)400, sp.n - rs - 1);
-                        double rr = zero_crossing(sp, rs, (porch + sync_lv) / 2.0, 0, c2, lane);
-                        if (rr == rr && fabs(rr - rcx) < one / 2.0) {
-                            double cand = rcx - normal + 2.25 * (p.mhz32 / 40.0);
-                            if (fabs(cand - right_ref) < one * 2.0) {
-                                refined = cand;
-                                fo = 0;
-                                if (porch > 0.0) prev_porch = porch;
-                            }
-                        }
-                    }
-                }
+            if ((li.flags & 16) && fabs(li.r_cand - right_ref) < one * 2.0) {
+                refined = li.r_cand;
+                fo = 0;
+                if (li.r_porch > 0.0) pp = li.r_porch;
             }
+            out = refined;
         }
-        if (lane == 0) { out[line] = refined - p.ntsc_shift; fout[line] = fo; }
+        prev_r = (li.flags & 16) ? li.r_porch : nan("");
+        if (lane == 0) {
+            p.locs_out[(int64_t)f * p.lines + line] = out - p.ntsc_shift;
+            p.filled_out[(int64_t)f * p.lines + line] = fo;
+        }
     }
+    if (lane == 0 && misses) atomicAdd(misses, miss);
 }
 }  // namespace
 
@@ -331,11 +402,16 @@ template <typename T>
 cudaError_t launch_hsync_refine(const T* stream, int64_t stream_len, const HsyncParams& p,
                                 cudaStream_t s) {
     if (p.nfields <= 0) return cudaSuccess;
-    int threads = 128;
-    int blocks = (p.nfields * 32 + threads - 1) / threads;
-    k_hsync<T><<<blocks, threads, 0, s>>>(stream, stream_len, p);
+    const int64_t warps = (int64_t)p.nfields * p.lines;
+    const int threads = 256;
+    const unsigned blocks = (unsigned)((warps * 32 + threads - 1) / threads);
+    LineInfo* info = reinterpret_cast<LineInfo*>(p.work);
+    k_hsync_lines<T><<<blocks, threads, 0, s>>>(stream, stream_len, p, info);
+    k_hsync_spec<T><<<blocks, threads, 0, s>>>(stream, stream_len, p, info);
+    k_hsync_chain<T><<<p.nfields, 32, 0, s>>>(stream, stream_len, p, info, p.misses);
     return cudaGetLastError();
 }
+size_t hsync_work_bytes(int nfields, int lines) { return (size_t)nfields * lines * sizeof(LineInfo); }
 template cudaError_t launch_hsync_refine<float>(const float*, int64_t, const HsyncParams&, cudaStream_t);
 template cudaError_t launch_hsync_refine<double>(const double*, int64_t, const HsyncParams&, cudaStream_t);
 

@@ -84,7 +84,10 @@ struct HsyncParams {
     double mhz32;              // (float)sample_rate_MHz
     double ire0, hz_ire;
     double ntsc_shift;         // subtracted after refinement (0 for PAL)
+    void* work;                // hsync_work_bytes(nfields, lines) of per-line scratch
+    int* misses;               // optional: counts carried-porch speculation misses
 };
+size_t hsync_work_bytes(int nfields, int lines);
 template <typename T>
 cudaError_t launch_hsync_refine(const T* sync_stream, int64_t stream_len, const HsyncParams& p,
                                 cudaStream_t stream);
