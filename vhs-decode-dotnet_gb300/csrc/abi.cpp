@@ -522,11 +522,11 @@ void run_fields(vhsdecode_gb300_session* s, const T* video, const T* sync, const
     hp.work = s->hsync_work.p;
     hp.misses = nullptr;
     const bool timing = std::getenv("VHSD_STAGE_TIMING") != nullptr;
-    cudaEvent_t st[4] = {};
-    if (timing) for (auto& e : st) ck(cudaEventCreate(&e), "event");
-    if (timing) ck(cudaEventRecord(st[0], cs), "event");
+    cudaEvent_t sev[4] = {};
+    if (timing) for (auto& e : sev) ck(cudaEventCreate(&e), "event");
+    if (timing) ck(cudaEventRecord(sev[0], cs), "event");
     ck(launch_hsync_refine<T>(sync, stream_len, hp, cs), "hsync launch");
-    if (timing) ck(cudaEventRecord(st[1], cs), "event");
+    if (timing) ck(cudaEventRecord(sev[1], cs), "event");
     TbcParams tp{};
     tp.nfields = nf;
     tp.lines = s->lines;
@@ -547,7 +547,7 @@ void run_fields(vhsdecode_gb300_session* s, const T* video, const T* sync, const
     tp.out_hz = nullptr;
     tp.level_work = s->level_work.p;
     ck(launch_tbc_pw<T>(video, stream_len, tp, s->pw.p, cs), "tbc launch");
-    if (timing) ck(cudaEventRecord(st[2], cs), "event");
+    if (timing) ck(cudaEventRecord(sev[2], cs), "event");
     DropoutParams dp{};
     dp.nfields = nf;
     dp.span_start = s->span_start_d.p;
@@ -574,15 +574,15 @@ void run_fields(vhsdecode_gb300_session* s, const T* video, const T* sync, const
     ck(launch_dropouts_full<T>(env, stream_len, dp, s->drop_partial.p, s->drop_counts.p, cs),
        "dropout launch");
     if (timing) {
-        ck(cudaEventRecord(st[3], cs), "event");
-        ck(cudaEventSynchronize(st[3]), "sync");
+        ck(cudaEventRecord(sev[3], cs), "event");
+        ck(cudaEventSynchronize(sev[3]), "sync");
         float a = 0, b = 0, c = 0;
-        cudaEventElapsedTime(&a, st[0], st[1]);
-        cudaEventElapsedTime(&b, st[1], st[2]);
-        cudaEventElapsedTime(&c, st[2], st[3]);
+        cudaEventElapsedTime(&a, sev[0], sev[1]);
+        cudaEventElapsedTime(&b, sev[1], sev[2]);
+        cudaEventElapsedTime(&c, sev[2], sev[3]);
         std::fprintf(stderr, "[gb300 stage] fields=%d host_control=%.3f ms hsync=%.3f ms tbc=%.3f ms dropouts=%.3f ms\n",
                      nf, host_ms, a, b, c);
-        for (auto& e : st) cudaEventDestroy(e);
+        for (auto& e : sev) cudaEventDestroy(e);
     }
     std::vector<double> refined((size_t)nf * s->lines);
     std::vector<int> dcount(nf), dstat(nf);
