@@ -189,6 +189,9 @@ struct vhsdecode_gb300_session {
     DevBuf<double> locs_in, locs_out;
     DevBuf<uint8_t> fill_in, fill_out;
     DevBuf<unsigned char> hsync_work;
+    DevBuf<unsigned char> gather;       // rescue segments of the sync reference
+    DevBuf<int64_t> gather_meta;
+    size_t gather_cap = 0;
     DevBuf<int> hsync_misses;
     DevBuf<int64_t> span_start_d, span_len_d;
     DevBuf<int> first_line_d, start_line_d, end_line_d, line_off_d;
@@ -443,6 +446,58 @@ void run_fields(vhsdecode_gb300_session* s, const T* video, const T* sync, const
         ck(cudaMemcpy(events.data(), s->pc_events.p, (size_t)total * sizeof(int64_t),
                       cudaMemcpyDeviceToHost), "d2h events");
     auto t0 = std::chrono::steady_clock::now();
+    // Long-hsync rescue (SyncAnalyzer.TryRescueLongHSync) reads the sync
+    // reference inside pulses longer than the hsync window.  Gather every
+    // such pulse of the stream on the device in one pass and copy it back
+    // once; a request outside the gathered set falls back to a direct copy.
+    std::vector<int64_t> seg_start, seg_off;
+    std::vector<int32_t> seg_len;
+    std::vector<T> seg_data;
+    int fallback_fetches = 0;
+    {
+        std::vector<Pulse> all = span_pulses(events.data(), total, 0, stream_len, 0, INT64_MAX);
+        std::vector<double> hl;
+        double lo = sp.usec(sp.hsync_us - 1.75), hi = sp.usec(sp.hsync_us + 2.0);
+        for (const Pulse& p : all) if ((double)p.len >= lo && (double)p.len <= hi) hl.push_back((double)p.len);
+        if (!hl.empty()) {
+            std::nth_element(hl.begin(), hl.begin() + hl.size() / 2, hl.end());
+            double h1 = hl[hl.size() / 2] + sp.usec(sp.hsync_tol);
+            double cmin = h1 - 8.0, cmax = 3.0 * (h1 + 8.0);
+            int64_t off = 0;
+            for (const Pulse& p : all) {
+                if ((double)p.len >= cmin && (double)p.len <= cmax) {
+                    seg_start.push_back(p.start);
+                    seg_len.push_back((int32_t)p.len);
+                    seg_off.push_back(off);
+                    off += p.len;
+                }
+            }
+            if (off > 0) {
+                if ((size_t)off > s->gather_cap) {
+                    s->gather.alloc((size_t)off * sizeof(double));
+                    s->gather_meta.alloc(seg_start.size() * 3);
+                    s->gather_cap = (size_t)off;
+                } else if (seg_start.size() * 3 > s->gather_meta.n) {
+                    s->gather_meta.alloc(seg_start.size() * 3);
+                }
+                std::vector<int64_t> meta(seg_start.size() * 3);
+                for (size_t k = 0; k < seg_start.size(); k++) {
+                    meta[3 * k] = seg_start[k];
+                    meta[3 * k + 1] = seg_len[k];
+                    meta[3 * k + 2] = seg_off[k];
+                }
+                if (meta.size() > s->gather_meta.n) s->gather_meta.alloc(meta.size());
+                ck(cudaMemcpy(s->gather_meta.p, meta.data(), meta.size() * sizeof(int64_t),
+                              cudaMemcpyHostToDevice), "h2d");
+                ck(launch_gather<T>(sync, reinterpret_cast<T*>(s->gather.p), s->gather_meta.p,
+                                    (int)seg_start.size(), s->stream), "gather launch");
+                seg_data.resize((size_t)off);
+                ck(cudaMemcpyAsync(seg_data.data(), s->gather.p, (size_t)off * sizeof(T),
+                                   cudaMemcpyDeviceToHost, s->stream), "d2h");
+                ck(cudaStreamSynchronize(s->stream), "sync");
+            }
+        }
+    }
     int64_t read_len = read_length(sp);
     int64_t min_len = std::max<int64_t>(0, (int64_t)std::ceil(sp.usec(sp.eq_us) / 8.0));
     int64_t max_len = std::max<int64_t>(1, (int64_t)(sp.nominal * 5.0));
@@ -459,8 +514,19 @@ void run_fields(vhsdecode_gb300_session* s, const T* video, const T* sync, const
         if (s0 + slen > stream_len) break;
         std::vector<Pulse> raw = span_pulses(events.data(), total, s0, slen, min_len, max_len);
         RefFetch fetch = [&](int64_t start, int64_t len, std::vector<double>& out) {
+            int64_t gs = s0 + start;
+            auto it = std::upper_bound(seg_start.begin(), seg_start.end(), gs);
+            if (it != seg_start.begin()) {
+                size_t k = (size_t)(it - seg_start.begin()) - 1;
+                if (gs + len <= seg_start[k] + seg_len[k]) {
+                    const T* base = seg_data.data() + seg_off[k] + (gs - seg_start[k]);
+                    out.assign(base, base + len);
+                    return;
+                }
+            }
+            fallback_fetches++;
             std::vector<T> tmp((size_t)len);
-            ck(cudaMemcpy(tmp.data(), sync + s0 + start, (size_t)len * sizeof(T), cudaMemcpyDeviceToHost),
+            ck(cudaMemcpy(tmp.data(), sync + gs, (size_t)len * sizeof(T), cudaMemcpyDeviceToHost),
                "rescue fetch");
             out.assign(tmp.begin(), tmp.end());
         };
@@ -580,8 +646,9 @@ void run_fields(vhsdecode_gb300_session* s, const T* video, const T* sync, const
         cudaEventElapsedTime(&a, sev[0], sev[1]);
         cudaEventElapsedTime(&b, sev[1], sev[2]);
         cudaEventElapsedTime(&c, sev[2], sev[3]);
-        std::fprintf(stderr, "[gb300 stage] fields=%d host_control=%.3f ms hsync=%.3f ms tbc=%.3f ms dropouts=%.3f ms\n",
-                     nf, host_ms, a, b, c);
+        std::fprintf(stderr, "[gb300 stage] fields=%d host_control=%.3f ms hsync=%.3f ms tbc=%.3f ms "
+                     "dropouts=%.3f ms rescue_segments=%zu fallback_fetches=%d\n",
+                     nf, host_ms, a, b, c, seg_start.size(), fallback_fetches);
         for (auto& e : sev) cudaEventDestroy(e);
     }
     std::vector<double> refined((size_t)nf * s->lines);

@@ -327,7 +327,15 @@ __global__ void k_hsync_chain(const T* stream, int64_t stream_len, HsyncParams p
     const int lane = threadIdx.x;
     const int64_t s0 = p.span_start[f];
     Span<T> sp{stream + s0, min(p.span_len[f], stream_len - s0)};
-    const LineInfo* fi = info + (int64_t)f * p.lines;
+    extern __shared__ __align__(16) unsigned char chain_smem[];
+    LineInfo* fi = reinterpret_cast<LineInfo*>(chain_smem);
+    {
+        const int4* g = reinterpret_cast<const int4*>(info + (int64_t)f * p.lines);
+        int4* d = reinterpret_cast<int4*>(fi);
+        const int words = (int)(p.lines * sizeof(LineInfo) / sizeof(int4));
+        for (int i = lane; i < words; i += 32) d[i] = g[i];
+        __syncwarp();
+    }
     const int one = p.one_us;
     double pp = -1.0;
     double prev_r = nan("");
@@ -408,7 +416,8 @@ cudaError_t launch_hsync_refine(const T* stream, int64_t stream_len, const Hsync
     LineInfo* info = reinterpret_cast<LineInfo*>(p.work);
     k_hsync_lines<T><<<blocks, threads, 0, s>>>(stream, stream_len, p, info);
     k_hsync_spec<T><<<blocks, threads, 0, s>>>(stream, stream_len, p, info);
-    k_hsync_chain<T><<<p.nfields, 32, 0, s>>>(stream, stream_len, p, info, p.misses);
+    k_hsync_chain<T><<<p.nfields, 32, p.lines * sizeof(LineInfo), s>>>(stream, stream_len, p, info,
+                                                                       p.misses);
     return cudaGetLastError();
 }
 size_t hsync_work_bytes(int nfields, int lines) { return (size_t)nfields * lines * sizeof(LineInfo); }
@@ -575,16 +584,96 @@ __global__ void k_tbc(const T* stream, int64_t stream_len, TbcParams p, const do
         }
     }
 }
+// Float-float accumulation of the 16 float products: TwoSum keeps the running
+// sum to about 48 bits, so the result equals the reference's binary64 sum up
+// to its last bits and the float32 output rounds the same way except with a
+// probability of about 2^-24 per sample.  Positions and the level adjust use
+// the per-line linear form pos(k) = A + k B of the same linear plan.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+__global__ void k_tbc_fast(const float* stream, int64_t stream_len, TbcParams p, const double* pw) {
+    const int f = blockIdx.y;
+    const int ol = blockIdx.x;
+    const int fl = p.first_line[f];
+    const int line = fl + ol;
+    const double* loc = p.locs + (int64_t)f * p.lines;
+    const int64_t s0 = p.span_start[f];
+    const int64_t n = min(p.span_len[f], stream_len - s0);
+    const float* src = stream + s0;
+    const double nominal = p.nominal;
+    const double out_scale = nominal / (double)p.outlen;
+    const double* w = p.level_work + (int64_t)f * 1024;
+    const double adj = w[2 * line], dlev = w[2 * line + 1] - adj;
+    const double ll = loc[line];
+    const double delta = loc[line + 1] - ll;
+    const double a_line = ll + delta * (((double)line * p.outlen * out_scale - (double)line * nominal) / nominal);
+    const double b_line = delta * out_scale / nominal;
+    const bool smooth = p.smoothing > 0.0 && line > 0;
+    const float4* lut4 = reinterpret_cast<const float4*>(p.lut);
+    for (int k = threadIdx.x; k < p.outlen; k += blockDim.x) {
+        float coord = __double2float_rn(fma((double)k, b_line, a_line));
+        int ci = (int)coord;
+        float fraction = __fsub_rn(coord, (float)ci);
+        float pp = __fmul_rn(fraction, 65536.0f);
+        int ps = (int)pp;
+        int pe = ps + 1;
+        float alpha = __fsub_rn(pp, (float)ps);
+        ps = wrap_idx(ps, 65537);
+        pe = wrap_idx(pe, 65537);
+        int start = ci - 7;
+        bool interior = n >= 16 && (uint32_t)start <= (uint32_t)(n - 16);
+        float hi = 0.0f, lo = 0.0f;
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            float4 ws = __ldg(lut4 + (int64_t)ps * 4 + q);
+            float4 we = __ldg(lut4 + (int64_t)pe * 4 + q);
+            float wsv[4] = {ws.x, ws.y, ws.z, ws.w};
+            float wev[4] = {we.x, we.y, we.z, we.w};
+#pragma unroll
+            for (int r = 0; r < 4; r++) {
+                int t = 4 * q + r;
+                float wt = __fmaf_rn(alpha, __fsub_rn(wev[r], wsv[r]), wsv[r]);
+                int64_t idx = (int64_t)start + t;
+                if (!interior) {
+                    if (idx < 0) idx += n;
+                    idx = idx < 0 ? 0 : (idx > n - 1 ? n - 1 : idx);
+                }
+                float prod = __fmul_rn(__ldg(src + idx), wt);
+                float s, e;
+                two_sum(hi, prod, s, e);
+                hi = s;
+                lo = __fadd_rn(lo, e);
+            }
+        }
+        double v = (double)hi + (double)lo;
+        double la = smooth ? fma(pw[k], dlev, adj) : adj;
+        float outf = __double2float_rn(v * la);
+        int64_t o = ((int64_t)f * p.out_lines + ol) * p.outlen + k;
+        double sd = p.output_scale * ((double)outf - p.ire0);
+        double val = fma(sd, p.inv_hz_ire, p.offset);
+        p.out_u16[o] = val <= 0.0 ? 0 : (val >= 65535.0 ? 65535 : (uint16_t)val);
+    }
+}
 }  // namespace
 
 // pw must hold (1-alpha)^(k+1) for k in [0, outlen) when smoothing > 0.
+// Float streams render with float-float accumulation when only uint16 output
+// is asked for; double streams and float-value outputs use binary64 as the
+// reference does.
 template <typename T>
 cudaError_t launch_tbc_pw(const T* stream, int64_t stream_len, const TbcParams& p, const double* pw,
                           cudaStream_t s) {
     if (p.nfields <= 0) return cudaSuccess;
     k_tbc_levels<<<p.nfields, 256, 0, s>>>(p, pw);
     dim3 grid(p.out_lines, p.nfields);
-    k_tbc<T><<<grid, 256, 0, s>>>(stream, stream_len, p, pw);
+    if (sizeof(T) == sizeof(float) && p.out_u16 && !p.out_hz)
+        k_tbc_fast<<<grid, 256, 0, s>>>(reinterpret_cast<const float*>(stream), stream_len, p, pw);
+    else
+        k_tbc<T><<<grid, 256, 0, s>>>(stream, stream_len, p, pw);
     return cudaGetLastError();
 }
 template cudaError_t launch_tbc_pw<float>(const float*, int64_t, const TbcParams&, const double*, cudaStream_t);
@@ -817,4 +906,25 @@ cudaError_t launch_dropouts_full(const T* stream, int64_t stream_len, const Drop
 template cudaError_t launch_dropouts_full<float>(const float*, int64_t, const DropoutParams&, float*, int*, cudaStream_t);
 template cudaError_t launch_dropouts_full<double>(const double*, int64_t, const DropoutParams&, float*, int*, cudaStream_t);
 
+}  // namespace vhsd
+
+namespace vhsd {
+// Copies segments meta[3k] .. meta[3k]+meta[3k+1] of `src` to dst + meta[3k+2].
+namespace {
+template <typename T>
+__global__ void k_gather(const T* src, T* dst, const int64_t* meta, int nseg) {
+    int k = blockIdx.x;
+    if (k >= nseg) return;
+    int64_t s = meta[3 * k], len = meta[3 * k + 1], off = meta[3 * k + 2];
+    for (int64_t i = threadIdx.x; i < len; i += blockDim.x) dst[off + i] = src[s + i];
+}
+}  // namespace
+template <typename T>
+cudaError_t launch_gather(const T* src, T* dst, const int64_t* meta, int nseg, cudaStream_t s) {
+    if (nseg <= 0) return cudaSuccess;
+    k_gather<T><<<nseg, 128, 0, s>>>(src, dst, meta, nseg);
+    return cudaGetLastError();
+}
+template cudaError_t launch_gather<float>(const float*, float*, const int64_t*, int, cudaStream_t);
+template cudaError_t launch_gather<double>(const double*, double*, const int64_t*, int, cudaStream_t);
 }  // namespace vhsd

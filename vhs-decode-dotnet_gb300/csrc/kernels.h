@@ -147,3 +147,8 @@ cudaError_t launch_dropouts_full(const T* env_stream, int64_t stream_len, const 
                                  float* partial, int* chunk_counts, cudaStream_t stream);
 
 }  // namespace vhsd
+
+namespace vhsd {
+template <typename T>
+cudaError_t launch_gather(const T* src, T* dst, const int64_t* meta, int nseg, cudaStream_t stream);
+}  // namespace vhsd
