@@ -195,7 +195,8 @@ struct vhsdecode_gb300_session {
     DevBuf<int> hsync_misses;
     DevBuf<int64_t> span_start_d, span_len_d;
     DevBuf<int> first_line_d, start_line_d, end_line_d, line_off_d;
-    DevBuf<float> lut;
+    DevBuf<float> lut, lut_pair;
+    DevBuf<float2> pw_ff;
     DevBuf<double> pw, level_work;
     DevBuf<uint16_t> tbc;
     DevBuf<int64_t> drop_range, drop_events;
@@ -314,9 +315,9 @@ void session_init(vhsdecode_gb300_session* s, const vhsdecode_gb300_session_conf
         s->pblk.alloc(1);
         ck(cudaMemset(s->pflag.p, 0, 4 * sizeof(int)), "memset");
     }
-    int64_t nchunks = (stream_cap + kPulseChunk - 1) / kPulseChunk;
-    s->pc_counts.alloc(nchunks);
-    s->pc_offsets.alloc(nchunks);
+    int64_t pslots = pulse_count_slots(stream_cap);
+    s->pc_counts.alloc(pslots);
+    s->pc_offsets.alloc(pslots);
     s->pc_capacity = stream_cap / 64 + 4096;
     s->pc_events.alloc(s->pc_capacity);
     s->pc_total.alloc(1);
@@ -332,12 +333,31 @@ void session_init(vhsdecode_gb300_session* s, const vhsdecode_gb300_session_conf
     std::vector<float> lut = build_sinc_lut();
     s->lut.alloc(lut.size());
     ck(cudaMemcpy(s->lut.p, lut.data(), lut.size() * sizeof(float), cudaMemcpyHostToDevice), "upload");
+    {
+        // rows p and p+1 side by side: one 128-byte line per interpolated tap set
+        std::vector<float> pair((size_t)65536 * 32);
+        for (size_t r = 0; r < 65536; r++)
+            for (int t = 0; t < 16; t++) {
+                pair[r * 32 + t] = lut[r * 16 + t];
+                pair[r * 32 + 16 + t] = lut[(r + 1) * 16 + t];
+            }
+        s->lut_pair.alloc(pair.size());
+        ck(cudaMemcpy(s->lut_pair.p, pair.data(), pair.size() * sizeof(float), cudaMemcpyHostToDevice),
+           "upload");
+    }
     double smoothing = s->fmt.frame_lines / 2.0;
     double alpha = 1.0 / (smoothing * s->outlen);
     std::vector<double> pw((size_t)s->outlen);
     for (int k = 0; k < s->outlen; k++) pw[(size_t)k] = std::pow(1.0 - alpha, (double)(k + 1));
     s->pw.alloc(pw.size());
     ck(cudaMemcpy(s->pw.p, pw.data(), pw.size() * sizeof(double), cudaMemcpyHostToDevice), "upload");
+    std::vector<float2> pwf(pw.size());
+    for (size_t k = 0; k < pw.size(); k++) {
+        float hi = (float)pw[k];
+        pwf[k] = make_float2(hi, (float)(pw[k] - (double)hi));
+    }
+    s->pw_ff.alloc(pwf.size());
+    ck(cudaMemcpy(s->pw_ff.p, pwf.data(), pwf.size() * sizeof(float2), cudaMemcpyHostToDevice), "upload");
     s->level_work.alloc((size_t)s->max_fields * 1024);
     s->tbc.alloc((size_t)s->max_fields * s->out_lines * s->outlen);
     s->span_len = read_length(s->sp) + 2 * kStride;  // upper bound of a resolved span
@@ -605,6 +625,8 @@ void run_fields(vhsdecode_gb300_session* s, const T* video, const T* sync, const
     tp.nominal = std::nearbyint(s->fmt.line_period_us * sp.mhz);
     tp.smoothing = s->fmt.frame_lines / 2.0;
     tp.lut = s->lut.p;
+    tp.lut_pair = s->lut_pair.p;
+    tp.pw_ff = s->pw_ff.p;
     tp.ire0 = s->fmt.ire0;
     tp.output_scale = output_scale(s->fmt);
     tp.inv_hz_ire = 1.0 / s->fmt.hz_ire;

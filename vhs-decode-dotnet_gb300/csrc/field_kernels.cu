@@ -14,74 +14,90 @@ namespace vhsd {
 // 0 for a pulse start (value <= high entered) and 1 for a pulse end (value >
 // high entered).  NaN keeps the state, as the reference's comparisons do.
 namespace {
-constexpr int kPT = 256;                      // threads per CTA
-constexpr int kPPer = kPulseChunk / kPT;      // samples per thread (16)
+constexpr int kPWarpSamples = 1024;           // contiguous samples per warp
+constexpr int kPT = kPulseChunk / kPWarpSamples * 32;  // threads per CTA (4 warps)
+
+// Exact comparison threshold: for a float sample v and a double h,
+// v <= h  <=>  v <= hf  with hf the largest float not above h.
+template <typename T>
+struct Cmp {
+    T h;
+};
+template <typename T>
+__host__ __device__ inline Cmp<T> make_cmp(double high);
+template <>
+__host__ __device__ inline Cmp<double> make_cmp<double>(double high) { return {high}; }
+template <>
+__host__ __device__ inline Cmp<float> make_cmp<float>(double high) {
+    float f = (float)high;
+    if ((double)f > high) f = nextafterf(f, -INFINITY);
+    return {f};
+}
 
 template <typename T>
-__device__ __forceinline__ bool state_before(const T* ref, int64_t p0, double high) {
+__device__ __forceinline__ bool state_before(const T* ref, int64_t p0, T h) {
     for (int64_t q = p0 - 1; q >= 0; q--) {
-        double v = (double)ref[q];
-        if (v <= high) return true;
-        if (v > high) return false;
+        T v = ref[q];
+        if (v <= h) return true;
+        if (v > h) return false;
     }
     return false;
 }
 
+// Edge bits of 32 consecutive samples given the state before the first one.
+// NaN samples (and samples past the end) keep the state.
+__device__ __forceinline__ unsigned edge_bits(unsigned cond, unsigned hold, unsigned& st) {
+    if (hold == 0u) {
+        unsigned prev = (cond << 1) | st;
+        st = cond >> 31;
+        return cond ^ prev;
+    }
+    unsigned s = st, edges = 0u;
+    for (int b = 0; b < 32; b++) {
+        if ((hold >> b) & 1u) continue;
+        unsigned c = (cond >> b) & 1u;
+        if (c != s) edges |= 1u << b;
+        s = c;
+    }
+    st = s;
+    return edges;
+}
+
 template <typename T, bool WRITE>
-__global__ void k_pulse_pass(const T* __restrict__ ref, int64_t n, double high, int64_t* counts,
+__global__ void k_pulse_pass(const T* __restrict__ ref, int64_t n, Cmp<T> cmp, int64_t* counts,
                              const int64_t* offsets, int64_t* events, int64_t capacity) {
-    __shared__ int64_t warp_tot[kPT / 32];
-    const int64_t chunk = blockIdx.x;
-    const int64_t p0 = chunk * kPulseChunk + (int64_t)threadIdx.x * kPPer;
-    int cnt = 0;
-    bool in = false;
-    if (p0 < n) in = state_before(ref, p0, high);
-    bool st = in;
-    for (int k = 0; k < kPPer; k++) {
-        int64_t p = p0 + k;
-        if (p >= n) break;
-        double v = (double)ref[p];
-        if (st) { if (v > high) { st = false; cnt++; } }
-        else if (v <= high) { st = true; cnt++; }
-    }
-    // block exclusive scan of cnt
-    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    int incl = cnt;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        int t = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += t;
-    }
-    if (lane == 31) warp_tot[w] = incl;
-    __syncthreads();
-    int64_t wbase = 0, total = 0;
-    for (int i = 0; i < kPT / 32; i++) {
-        if (i < w) wbase += warp_tot[i];
-        total += warp_tot[i];
-    }
-    if (!WRITE) {
-        if (threadIdx.x == 0) counts[chunk] = total;
+    const int lane = threadIdx.x & 31;
+    const int64_t wg = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t start = wg * kPWarpSamples;
+    if (start >= n) {
+        if (!WRITE && lane == 0) counts[wg] = 0;
         return;
     }
-    int64_t off = offsets[chunk] + wbase + (incl - cnt);
-    st = in;
-    for (int k = 0; k < kPPer; k++) {
-        int64_t p = p0 + k;
-        if (p >= n) break;
-        double v = (double)ref[p];
-        if (st) {
-            if (v > high) {
-                st = false;
-                if (off < capacity) events[off] = 2 * p + 1;
-                off++;
-            }
-        } else if (v <= high) {
-            st = true;
-            if (off < capacity) events[off] = 2 * p;
-            off++;
+    unsigned st = 0u;
+    if (lane == 0) st = state_before(ref, start, cmp.h) ? 1u : 0u;
+    st = __shfl_sync(0xffffffffu, st, 0);
+    int64_t off = WRITE ? offsets[wg] : 0;
+    int64_t cnt = 0;
+    for (int it = 0; it < kPWarpSamples / 32; it++) {
+        int64_t p = start + it * 32 + lane;
+        bool inb = p < n;
+        T v = inb ? ref[p] : (T)0;
+        bool hold = !inb || !(v == v);
+        bool c = inb && (v <= cmp.h);
+        unsigned cm = __ballot_sync(0xffffffffu, c);
+        unsigned hm = __ballot_sync(0xffffffffu, hold);
+        unsigned e = edge_bits(cm, hm, st);
+        if (WRITE && ((e >> lane) & 1u)) {
+            int64_t o = off + __popc(e & ((1u << lane) - 1u));
+            if (o < capacity) events[o] = 2 * p + (c ? 0 : 1);
         }
+        int pc = __popc(e);
+        off += pc;
+        cnt += pc;
     }
+    if (!WRITE && lane == 0) counts[wg] = cnt;
 }
+
 
 // single-CTA exclusive scan of chunk counts
 __global__ void k_scan_counts(const int64_t* counts, int64_t nchunks, int64_t* offsets,
@@ -124,9 +140,11 @@ cudaError_t launch_pulse_events(const T* ref, int64_t n, double high, int64_t* c
         cudaMemsetAsync(total, 0, sizeof(int64_t), s);
         return cudaGetLastError();
     }
-    k_pulse_pass<T, false><<<(unsigned)nchunks, kPT, 0, s>>>(ref, n, high, counts, nullptr, nullptr, 0);
-    k_scan_counts<<<1, 1024, 0, s>>>(counts, nchunks, offsets, total);
-    k_pulse_pass<T, true><<<(unsigned)nchunks, kPT, 0, s>>>(ref, n, high, counts, offsets, events,
+    Cmp<T> cmp = make_cmp<T>(high);
+    int64_t slots = pulse_count_slots(n);
+    k_pulse_pass<T, false><<<(unsigned)nchunks, kPT, 0, s>>>(ref, n, cmp, counts, nullptr, nullptr, 0);
+    k_scan_counts<<<1, 1024, 0, s>>>(counts, slots, offsets, total);
+    k_pulse_pass<T, true><<<(unsigned)nchunks, kPT, 0, s>>>(ref, n, cmp, counts, offsets, events,
                                                            capacity);
     return cudaGetLastError();
 }
@@ -584,38 +602,88 @@ __global__ void k_tbc(const T* stream, int64_t stream_len, TbcParams p, const do
         }
     }
 }
-// Float-float accumulation of the 16 float products: TwoSum keeps the running
-// sum to about 48 bits, so the result equals the reference's binary64 sum up
-// to its last bits and the float32 output rounds the same way except with a
-// probability of about 2^-24 per sample.  Positions and the level adjust use
-// the per-line linear form pos(k) = A + k B of the same linear plan.
+// Float-only rendering of a float stream to uint16.  Every quantity the
+// reference keeps in binary64 is carried as an unevaluated float pair
+// (hi + lo, about 48 significant bits): the line's linear position plan
+// pos(k) = A + k B, the smoothed level factor, the sum of the 16 float
+// products (TwoSum) and the uint16 conversion, whose floor is taken on the
+// exact pair.  Results equal the binary64 ones except where a value lies
+// within about 2^-46 (relative) of a float rounding boundary or of an integer.
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
     s = __fadd_rn(a, b);
     float bb = __fsub_rn(s, a);
     e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
 }
+__device__ __forceinline__ void quick_two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    e = __fsub_rn(b, __fsub_rn(s, a));
+}
+__device__ __forceinline__ float2 split_double(double d) {
+    float hi = __double2float_rn(d);
+    return make_float2(hi, __double2float_rn(d - (double)hi));
+}
+// (ah + al) * (bh + bl) as a pair
+__device__ __forceinline__ float2 ff_mul(float ah, float al, float bh, float bl) {
+    float m = __fmul_rn(ah, bh);
+    float e = __fmaf_rn(ah, bh, -m);
+    e = __fmaf_rn(ah, bl, e);
+    e = __fmaf_rn(al, bh, e);
+    float s, t;
+    quick_two_sum(m, e, s, t);
+    return make_float2(s, t);
+}
+// (ah + al) + (bh + bl) as a pair
+__device__ __forceinline__ float2 ff_add(float ah, float al, float bh, float bl) {
+    float s, e;
+    two_sum(ah, bh, s, e);
+    e = __fadd_rn(e, __fadd_rn(al, bl));
+    float h, t;
+    quick_two_sum(s, e, h, t);
+    return make_float2(h, t);
+}
 
-__global__ void k_tbc_fast(const float* stream, int64_t stream_len, TbcParams p, const double* pw) {
+struct TbcLineConsts {
+    float2 a, b;        // position plan A, B
+    float2 adj, dlev;   // level factor and (value before the line - factor)
+    float2 ire0, k;     // conversion: (outf - ire0) * k + off
+    float2 off;
+    int smooth;
+};
+
+__global__ void __launch_bounds__(256) k_tbc_fast(const float* stream, int64_t stream_len, TbcParams p) {
+    __shared__ TbcLineConsts c;
     const int f = blockIdx.y;
     const int ol = blockIdx.x;
-    const int fl = p.first_line[f];
-    const int line = fl + ol;
-    const double* loc = p.locs + (int64_t)f * p.lines;
+    const int line = p.first_line[f] + ol;
     const int64_t s0 = p.span_start[f];
     const int64_t n = min(p.span_len[f], stream_len - s0);
     const float* src = stream + s0;
-    const double nominal = p.nominal;
-    const double out_scale = nominal / (double)p.outlen;
-    const double* w = p.level_work + (int64_t)f * 1024;
-    const double adj = w[2 * line], dlev = w[2 * line + 1] - adj;
-    const double ll = loc[line];
-    const double delta = loc[line + 1] - ll;
-    const double a_line = ll + delta * (((double)line * p.outlen * out_scale - (double)line * nominal) / nominal);
-    const double b_line = delta * out_scale / nominal;
-    const bool smooth = p.smoothing > 0.0 && line > 0;
+    if (threadIdx.x == 0) {
+        const double* loc = p.locs + (int64_t)f * p.lines;
+        const double nominal = p.nominal;
+        const double out_scale = nominal / (double)p.outlen;
+        const double* w = p.level_work + (int64_t)f * 1024;
+        const double adj = w[2 * line];
+        const double ll = loc[line];
+        const double delta = loc[line + 1] - ll;
+        c.a = split_double(ll + delta * (((double)line * p.outlen * out_scale - (double)line * nominal) / nominal));
+        c.b = split_double(delta * out_scale / nominal);
+        c.adj = split_double(adj);
+        c.dlev = split_double(w[2 * line + 1] - adj);
+        c.ire0 = split_double(p.ire0);
+        c.k = split_double(p.output_scale * p.inv_hz_ire);
+        c.off = split_double(p.offset);
+        c.smooth = p.smoothing > 0.0 && line > 0;
+    }
+    __syncthreads();
     const float4* lut4 = reinterpret_cast<const float4*>(p.lut);
+    const float4* pair4 = reinterpret_cast<const float4*>(p.lut_pair);
+    uint16_t* out = p.out_u16 + ((int64_t)f * p.out_lines + ol) * p.outlen;
     for (int k = threadIdx.x; k < p.outlen; k += blockDim.x) {
-        float coord = __double2float_rn(fma((double)k, b_line, a_line));
+        const float kf = (float)k;
+        float2 kb = ff_mul(kf, 0.0f, c.b.x, c.b.y);
+        float2 pos = ff_add(c.a.x, c.a.y, kb.x, kb.y);
+        float coord = __fadd_rn(pos.x, pos.y);
         int ci = (int)coord;
         float fraction = __fsub_rn(coord, (float)ci);
         float pp = __fmul_rn(fraction, 65536.0f);
@@ -624,13 +692,22 @@ __global__ void k_tbc_fast(const float* stream, int64_t stream_len, TbcParams p,
         float alpha = __fsub_rn(pp, (float)ps);
         ps = wrap_idx(ps, 65537);
         pe = wrap_idx(pe, 65537);
+        const float4* rs;
+        const float4* re;
+        if (pe == ps + 1 && pair4) {
+            rs = pair4 + (int64_t)ps * 8;
+            re = rs + 4;
+        } else {
+            rs = lut4 + (int64_t)ps * 4;
+            re = lut4 + (int64_t)pe * 4;
+        }
         int start = ci - 7;
         bool interior = n >= 16 && (uint32_t)start <= (uint32_t)(n - 16);
         float hi = 0.0f, lo = 0.0f;
 #pragma unroll
         for (int q = 0; q < 4; q++) {
-            float4 ws = __ldg(lut4 + (int64_t)ps * 4 + q);
-            float4 we = __ldg(lut4 + (int64_t)pe * 4 + q);
+            float4 ws = __ldg(rs + q);
+            float4 we = __ldg(re + q);
             float wsv[4] = {ws.x, ws.y, ws.z, ws.w};
             float wev[4] = {we.x, we.y, we.z, we.w};
 #pragma unroll
@@ -649,13 +726,32 @@ __global__ void k_tbc_fast(const float* stream, int64_t stream_len, TbcParams p,
                 lo = __fadd_rn(lo, e);
             }
         }
-        double v = (double)hi + (double)lo;
-        double la = smooth ? fma(pw[k], dlev, adj) : adj;
-        float outf = __double2float_rn(v * la);
-        int64_t o = ((int64_t)f * p.out_lines + ol) * p.outlen + k;
-        double sd = p.output_scale * ((double)outf - p.ire0);
-        double val = fma(sd, p.inv_hz_ire, p.offset);
-        p.out_u16[o] = val <= 0.0 ? 0 : (val >= 65535.0 ? 65535 : (uint16_t)val);
+        float2 la = c.adj;
+        if (c.smooth) {
+            float2 pw = p.pw_ff[k];
+            float2 t = ff_mul(pw.x, pw.y, c.dlev.x, c.dlev.y);
+            la = ff_add(c.adj.x, c.adj.y, t.x, t.y);
+        }
+        float2 v = ff_mul(hi, lo, la.x, la.y);
+        float outf = __fadd_rn(v.x, v.y);
+        if (!isfinite(outf)) {
+            out[k] = outf > 0.0f ? 65535 : 0;
+            continue;
+        }
+        // val = (outf - ire0) * k + off, floor taken on the pair
+        float2 d = ff_add(outf, 0.0f, -c.ire0.x, -c.ire0.y);
+        float2 sk = ff_mul(d.x, d.y, c.k.x, c.k.y);
+        float2 val = ff_add(sk.x, sk.y, c.off.x, c.off.y);
+        uint16_t u;
+        if (!(fabsf(val.x) < 1.0e6f)) {
+            u = val.x > 0.0f ? 65535 : 0;   // infinite, huge or NaN (NaN converts to 0)
+        } else {
+            float fl = floorf(val.x);
+            float r = __fadd_rn(__fsub_rn(val.x, fl), val.y);
+            int F = (int)fl + (r < 0.0f ? -1 : (r >= 1.0f ? 1 : 0));
+            u = (uint16_t)(F < 0 ? 0 : (F > 65535 ? 65535 : F));
+        }
+        out[k] = u;
     }
 }
 }  // namespace
@@ -670,8 +766,8 @@ cudaError_t launch_tbc_pw(const T* stream, int64_t stream_len, const TbcParams& 
     if (p.nfields <= 0) return cudaSuccess;
     k_tbc_levels<<<p.nfields, 256, 0, s>>>(p, pw);
     dim3 grid(p.out_lines, p.nfields);
-    if (sizeof(T) == sizeof(float) && p.out_u16 && !p.out_hz)
-        k_tbc_fast<<<grid, 256, 0, s>>>(reinterpret_cast<const float*>(stream), stream_len, p, pw);
+    if (sizeof(T) == sizeof(float) && p.out_u16 && !p.out_hz && (p.smoothing <= 0.0 || p.pw_ff))
+        k_tbc_fast<<<grid, 256, 0, s>>>(reinterpret_cast<const float*>(stream), stream_len, p);
     else
         k_tbc<T><<<grid, 256, 0, s>>>(stream, stream_len, p, pw);
     return cudaGetLastError();
@@ -740,70 +836,141 @@ __global__ void k_env_mean(DropoutParams p, const float* partial, int nchunk, in
     p.mean_out[f] = t / (float)n;
 }
 
-// event = 4*pos + type; type 0: (env <= down) run start, 1: run end, 2: (env >= up) start
+// Exact float forms of the two dropout comparisons: for a float sample v,
+// v <= (double)down  <=>  v <= dn  and  v >= up  <=>  v >= upf  with upf the
+// smallest float not below up.
 template <typename T>
-__global__ void k_drop_events(const T* stream, int64_t stream_len, DropoutParams p, int nchunk,
-                              int* chunk_counts) {
+struct DropThr {
+    T down, up;
+};
+__device__ inline DropThr<double> make_drop_thr(float thrf, double hyst, double*) {
+    return {(double)thrf, (double)thrf * hyst};
+}
+__device__ inline DropThr<float> make_drop_thr(float thrf, double hyst, float*) {
+    double up = (double)thrf * hyst;
+    float u = (float)up;
+    if ((double)u < up) u = nextafterf(u, INFINITY);
+    return {thrf, u};
+}
+
+constexpr int kDWarp = kDChunk / (kDT / 32);   // 2048 samples per warp
+constexpr int kDIter = kDWarp / 32;
+
+// event = 4*pos + type; type 0: (env <= down) run start, 1: run end, 2: (env >= up) start.
+// Each warp scans a contiguous 2048-sample slice with ballots, keeps the
+// per-iteration masks in shared memory, and writes its events in order after a
+// CTA scan of the warp counts.
+template <typename T>
+__global__ void __launch_bounds__(kDT) k_drop_events(const T* stream, int64_t stream_len,
+                                                     DropoutParams p, int nchunk, int* chunk_counts) {
     __shared__ int wtot[kDT / 32];
+    __shared__ unsigned masks[kDT / 32][kDIter][3];
     const int f = blockIdx.y, c = blockIdx.x;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int64_t s0 = p.span_start[f];
     const T* env = stream + s0;
     const int64_t r0 = p.range[2 * f], r1 = p.range[2 * f + 1];
-    const float thrf = __fmul_rn(p.mean_out[f], p.frac);
-    const double down = (double)thrf, up = (double)thrf * p.hyst;
-    const int64_t b0 = r0 + (int64_t)c * kDChunk + (int64_t)threadIdx.x * kDPer;
+    const DropThr<T> th = make_drop_thr(__fmul_rn(p.mean_out[f], p.frac), p.hyst, (T*)nullptr);
+    const int64_t base = r0 + (int64_t)c * kDChunk + (int64_t)w * kDWarp;
     auto flags = [&](int64_t i, bool& a, bool& b) {
         if (i < r0 || i >= r1) { a = false; b = false; return; }
-        double v = (double)env[i];
-        a = v <= down;
-        b = v >= up;
+        T v = env[i];
+        a = v <= th.down;
+        b = v >= th.up;
     };
-    int cnt = 0;
     bool pa, pb;
-    flags(b0 - 1, pa, pb);
-    for (int k = 0; k < kDPer; k++) {
-        int64_t i = b0 + k;
-        if (i > r1) break;
+    flags(base - 1, pa, pb);
+    unsigned sa = pa ? 1u : 0u, sb = pb ? 1u : 0u;
+    int cnt = 0, iters = 0;
+    for (int it = 0; it < kDIter; it++) {
+        int64_t i0 = base + it * 32;
+        if (i0 > r1) break;
         bool a, b;
-        flags(i, a, b);
-        if (a != pa) cnt++;
-        if (b && !pb) cnt++;
-        pa = a; pb = b;
+        flags(i0 + lane, a, b);
+        unsigned A = __ballot_sync(0xffffffffu, a), B = __ballot_sync(0xffffffffu, b);
+        unsigned ea = A ^ ((A << 1) | sa);
+        unsigned eb = B & ~((B << 1) | sb);
+        sa = A >> 31;
+        sb = B >> 31;
+        if (lane == 0) { masks[w][it][0] = ea; masks[w][it][1] = A & ea; masks[w][it][2] = eb; }
+        cnt += __popc(ea) + __popc(eb);
+        iters = it + 1;
     }
-    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    int incl = cnt;
-    for (int o = 1; o < 32; o <<= 1) {
-        int t = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += t;
-    }
-    if (lane == 31) wtot[w] = incl;
+    if (lane == 0) wtot[w] = cnt;
     __syncthreads();
     int wb = 0, tot = 0;
     for (int i = 0; i < kDT / 32; i++) { if (i < w) wb += wtot[i]; tot += wtot[i]; }
     if (threadIdx.x == 0) chunk_counts[(int64_t)f * nchunk + c] = tot;
-    int off = wb + incl - cnt;
+    if (cnt == 0) return;
     int64_t* ev = p.events + ((int64_t)f * nchunk + c) * p.cap;
-    flags(b0 - 1, pa, pb);
-    for (int k = 0; k < kDPer; k++) {
-        int64_t i = b0 + k;
-        if (i > r1) break;
-        bool a, b;
-        flags(i, a, b);
-        if (a != pa) { if (off < p.cap) ev[off] = 4 * i + (a ? 0 : 1); off++; }
-        if (b && !pb) { if (off < p.cap) ev[off] = 4 * i + 2; off++; }
-        pa = a; pb = b;
+    int off = wb;
+    const unsigned lt = (1u << lane) - 1u;
+    for (int it = 0; it < iters; it++) {
+        unsigned ea = masks[w][it][0], ta = masks[w][it][1], eb = masks[w][it][2];
+        if ((ea | eb) == 0u) continue;
+        unsigned bit = 1u << lane;
+        int pre = __popc(ea & lt) + __popc(eb & lt);
+        int64_t i = base + it * 32 + lane;
+        int o = off + pre;
+        if (ea & bit) { if (o < p.cap) ev[o] = 4 * i + ((ta & bit) ? 0 : 1); o++; }
+        if (eb & bit) { if (o < p.cap) ev[o] = 4 * i + 2; }
+        off += __popc(ea) + __popc(eb);
     }
 }
 
-// One thread per field: merge state machine, minimum length, TBC mapping.
+constexpr int kDropSmemEvents = 4096;
+
+size_t drop_finish_smem(int lines, int nchunk) {
+    return (size_t)lines * sizeof(double) + kDropSmemEvents * sizeof(int64_t) +
+           (size_t)(nchunk + 1) * sizeof(int);
+}
+
+// One CTA per field.  The field's line locations, chunk offsets and (when they
+// fit) its events are staged in shared memory; thread 0 then runs the merge
+// state machine, the minimum length rule and the TBC mapping.
 __global__ void k_drop_finish(DropoutParams p, int nchunk, const int* chunk_counts) {
-    int f = blockIdx.x * blockDim.x + threadIdx.x;
-    if (f >= p.nfields) return;
+    extern __shared__ __align__(16) unsigned char dsm[];
+    double* sloc = reinterpret_cast<double*>(dsm);
+    int64_t* sev = reinterpret_cast<int64_t*>(sloc + p.lines);
+    int* soff = reinterpret_cast<int*>(sev + kDropSmemEvents);
+    __shared__ int s_status;
+    const int f = blockIdx.x;
+    const int lane = threadIdx.x & 31;
+    const double* gloc = p.locs + (int64_t)f * p.lines;
+    for (int i = threadIdx.x; i < p.lines; i += blockDim.x) sloc[i] = gloc[i];
+    if (threadIdx.x < 32) {
+        int carry = 0, st = 0;
+        for (int c0 = 0; c0 < nchunk; c0 += 32) {
+            int c = c0 + lane;
+            int v = c < nchunk ? chunk_counts[(int64_t)f * nchunk + c] : 0;
+            if (v > p.cap) { v = p.cap; st = 2; }
+            int incl = v;
+            for (int o = 1; o < 32; o <<= 1) {
+                int t = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += t;
+            }
+            if (c < nchunk) soff[c] = carry + incl - v;
+            carry += __shfl_sync(0xffffffffu, incl, 31);
+        }
+        st = __reduce_max_sync(0xffffffffu, st);
+        if (lane == 0) { soff[nchunk] = carry; s_status = st; }
+    }
+    __syncthreads();
+    const bool fits = soff[nchunk] <= kDropSmemEvents;
+    if (fits) {
+        for (int c = 0; c < nchunk; c++) {
+            int cnt = soff[c + 1] - soff[c];
+            const int64_t* ev = p.events + ((int64_t)f * nchunk + c) * p.cap;
+            for (int e = threadIdx.x; e < cnt; e += blockDim.x) sev[soff[c] + e] = ev[e];
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
     const int64_t r1 = p.range[2 * f + 1];
     int32_t* out = p.out + (int64_t)f * p.out_cap * 3;
     int nout = 0;
-    int status = 0;
-    const double* loc = p.locs + (int64_t)f * p.lines;
+    int status = s_status;
+    const double* loc = sloc;
     const int sl = p.start_line[f], el = p.end_line[f], off = p.line_offset[f];
     // mapping state (MapTapeRfToTbc)
     int li = sl;
@@ -855,9 +1022,8 @@ __global__ void k_drop_finish(DropoutParams p, int nchunk, const int* chunk_coun
     bool have = false, open = false, pending = false;
     int64_t start = 0, last_end = 0, cand = 0;
     for (int c = 0; c < nchunk; c++) {
-        int cnt = chunk_counts[(int64_t)f * nchunk + c];
-        if (cnt > p.cap) { status = 2; cnt = p.cap; }
-        const int64_t* ev = p.events + ((int64_t)f * nchunk + c) * p.cap;
+        int cnt = soff[c + 1] - soff[c];
+        const int64_t* ev = fits ? sev + soff[c] : p.events + ((int64_t)f * nchunk + c) * p.cap;
         for (int e = 0; e < cnt; e++) {
             int64_t pos = ev[e] >> 2;
             int type = (int)(ev[e] & 3);
@@ -900,7 +1066,13 @@ cudaError_t launch_dropouts_full(const T* stream, int64_t stream_len, const Drop
     k_env_partial<T><<<g, kDT, 0, s>>>(stream, stream_len, p, partial, nchunk);
     k_env_mean<<<p.nfields, 32, 0, s>>>(p, partial, nchunk, stream_len);
     k_drop_events<T><<<g, kDT, 0, s>>>(stream, stream_len, p, nchunk, chunk_counts);
-    k_drop_finish<<<(p.nfields + 63) / 64, 64, 0, s>>>(p, nchunk, chunk_counts);
+    size_t smem = drop_finish_smem(p.lines, nchunk);
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(k_drop_finish, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    k_drop_finish<<<p.nfields, 128, smem, s>>>(p, nchunk, chunk_counts);
     return cudaGetLastError();
 }
 template cudaError_t launch_dropouts_full<float>(const float*, int64_t, const DropoutParams&, float*, int*, cudaStream_t);

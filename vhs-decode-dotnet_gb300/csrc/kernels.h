@@ -60,13 +60,15 @@ cudaError_t launch_demod_fp64_block(const PlainDemodParams& p, cudaStream_t stre
 // ---------------------------------------------------------------- pulses
 // Sync-pulse edge events of PulseDetection.FindPulses over a whole stitched
 // stream: starts (value <= high after > high) and ends (value > high after
-// <= high), NaN samples hold the state.  Two passes: count per chunk, then
-// ordered write.
+// <= high), NaN samples hold the state.  Two passes: count per warp slice of
+// 1024 samples, then ordered write.  counts / offsets_scratch hold
+// pulse_count_slots(n) entries.
+constexpr int kPulseChunk = 4096;
+inline int64_t pulse_count_slots(int64_t n) { return (n + kPulseChunk - 1) / kPulseChunk * 4; }
 template <typename T>
 cudaError_t launch_pulse_events(const T* ref, int64_t n, double high, int64_t* counts,
                                 int64_t* offsets_scratch, int64_t* events, int64_t capacity,
                                 int64_t* total, cudaStream_t stream);
-constexpr int kPulseChunk = 4096;
 
 // ---------------------------------------------------------------- hsync refine
 struct HsyncParams {
@@ -105,6 +107,8 @@ struct TbcParams {
     double nominal;             // nominal input line length (samples)
     double smoothing;           // wow level-adjust smoothing (lines)
     const float* lut;           // [(65536+1)*16] sinc LUT
+    const float* lut_pair;      // optional [65536][32]: rows p and p+1 side by side
+    const float2* pw_ff;        // optional [outlen] pw as (hi, lo) float pairs
     double ire0, output_scale, inv_hz_ire, offset;  // uint16 conversion
     uint16_t* out_u16;          // [nfields * out_lines * outlen] or null
     double* out_hz;             // optional float output (values rounded to float)

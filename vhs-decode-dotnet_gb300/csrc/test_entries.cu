@@ -91,11 +91,11 @@ VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_find_pulses(
     *count = 0;
     if (n == 0) return set_last_error(VHSDECODE_GB300_STATUS_OK, "");
     Scoped sc;
-    int64_t nchunks = ((int64_t)n + kPulseChunk - 1) / kPulseChunk;
+    int64_t pslots = pulse_count_slots((int64_t)n);
     int64_t capacity = (int64_t)n + 16;
     double* dref = sc.alloc<double>(n);
-    int64_t* dcounts = sc.alloc<int64_t>(nchunks);
-    int64_t* doffs = sc.alloc<int64_t>(nchunks);
+    int64_t* dcounts = sc.alloc<int64_t>(pslots);
+    int64_t* doffs = sc.alloc<int64_t>(pslots);
     int64_t* dev = sc.alloc<int64_t>(capacity);
     int64_t* dtot = sc.alloc<int64_t>(1);
     if (!dref || !dcounts || !doffs || !dev || !dtot)
