@@ -275,6 +275,20 @@ VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_find_pulses(
 VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_vhs_angles(
     const float* real, const float* imaginary, uint64_t n, float* angles);
 
+/* Sync-pulse edge events over `length` float samples already on the device,
+ * with no device memory allocated by the call.  No counterpart in the
+ * reference: it serves callers that may not allocate while decoding (a thread
+ * capturing CUDA graphs, a real-time loop, a fixed memory budget).
+ * events[i] = 2 * position + (0 for a pulse start, 1 for a pulse end), in
+ * order; *total receives the full count (entries past `capacity` are not
+ * written).  `stream` is a cudaStream_t (NULL = legacy default stream).
+ * Limit: length <= 16777216 samples, else INVALID_ARGUMENT.  The first call on
+ * a device sets up its fixed scratch: make it before capturing a stream.
+ * Calls on one device share that scratch and must not overlap. */
+VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_pulse_events_noalloc(
+    const float* sync, int64_t length, double high, int64_t* events, int64_t capacity,
+    int64_t* total, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -44,6 +44,7 @@ EXPORTS = [
     "vhsdecode_gb300_session_tbc_device", "vhsdecode_gb300_design_filters",
     "vhsdecode_gb300_field_sync", "vhsdecode_gb300_tbc_resample_lines",
     "vhsdecode_gb300_find_pulses", "vhsdecode_gb300_vhs_angles",
+    "vhsdecode_gb300_pulse_events_noalloc",
 ]
 
 
@@ -159,6 +160,8 @@ def load(path: str = LIB_PATH):
                                               ctypes.c_int64, _vp, _vp, ctypes.c_uint64,
                                               _P(ctypes.c_uint64)]
     L.vhsdecode_gb300_vhs_angles.argtypes = [_vp, _vp, ctypes.c_uint64, _vp]
+    L.vhsdecode_gb300_pulse_events_noalloc.argtypes = [_vp, ctypes.c_int64, ctypes.c_double, _vp,
+                                                       ctypes.c_int64, _vp, _vp]
     for name in EXPORTS:
         if not hasattr(L, name):
             raise NativeError(STATUS_INTERNAL_ERROR, "missing export " + name)
