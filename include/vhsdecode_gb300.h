@@ -2,11 +2,11 @@
  * vhsdecode_gb300 -- C ABI of the GB300 (sm_103a) RF decode backend.
  *
  * Drop-in for the reference's native `cuda-fast` boundary
- * (src/VHSDecode.CudaFast.Native/include/vhsdecode_cuda_fast.h:130-309 in
+ * (src/VHSDecode.CudaFast.Native/include/vhsdecode_cuda_fast.h:26-174 in
  * vhs-decode-dotnet): same status codes, enums, callback shapes, versioned
  * structs that start with `struct_size`, a thread-local last error and a
  * whole-run entry point.  The managed side binds it through P/Invoke exactly
- * as Core/Dsp/CudaFast/CudaFastNativeRuntime.cs:491-621 binds the cuda-fast
+ * as Core/Dsp/CudaFast/CudaFastNativeRuntime.cs:131-185 binds the cuda-fast
  * library (NativeLibrary.Load + GetExport, ABI version check).
  *
  * Beyond the run() handoff it exposes a session API that keeps a capture and
@@ -41,7 +41,7 @@
 extern "C" {
 #endif
 
-/* Status codes: values of vhsdecode_cuda_fast_status (vhsdecode_cuda_fast.h:155-165). */
+/* Status codes: values of vhsdecode_cuda_fast_status (vhsdecode_cuda_fast.h:26-36). */
 typedef enum vhsdecode_gb300_status {
     VHSDECODE_GB300_STATUS_OK = 0,
     VHSDECODE_GB300_STATUS_NULL_POINTER = -20000,
@@ -54,21 +54,21 @@ typedef enum vhsdecode_gb300_status {
     VHSDECODE_GB300_STATUS_INTERNAL_ERROR = -20007
 } vhsdecode_gb300_status;
 
-/* vhsdecode_cuda_fast_profile (vhsdecode_cuda_fast.h:167-171); PAL_M is rejected. */
+/* vhsdecode_cuda_fast_profile (vhsdecode_cuda_fast.h:38-42); PAL_M is rejected. */
 typedef enum vhsdecode_gb300_profile {
     VHSDECODE_GB300_PROFILE_NTSC = 0,
     VHSDECODE_GB300_PROFILE_PAL = 1,
     VHSDECODE_GB300_PROFILE_PAL_M = 2
 } vhsdecode_gb300_profile;
 
-/* vhsdecode_cuda_fast_tape_speed (:173-177); only SP parameters are built in. */
+/* vhsdecode_cuda_fast_tape_speed (:44-48); only SP parameters are built in. */
 typedef enum vhsdecode_gb300_tape_speed {
     VHSDECODE_GB300_TAPE_SPEED_SP = 0,
     VHSDECODE_GB300_TAPE_SPEED_LP = 1,
     VHSDECODE_GB300_TAPE_SPEED_EP = 2
 } vhsdecode_gb300_tape_speed;
 
-/* vhsdecode_cuda_fast_input_sample_format (:179-182); run() accepts INT16. */
+/* vhsdecode_cuda_fast_input_sample_format (:50-53); run() accepts INT16. */
 typedef enum vhsdecode_gb300_input_sample_format {
     VHSDECODE_GB300_INPUT_FLOAT32 = 0,
     VHSDECODE_GB300_INPUT_INT16 = 1
@@ -80,7 +80,7 @@ typedef enum vhsdecode_gb300_precision {
     VHSDECODE_GB300_PRECISION_FP64_PLAIN = 1  /* one block at a time, FP64 throughout */
 } vhsdecode_gb300_precision;
 
-/* Callbacks: shapes of vhsdecode_cuda_fast_read_callback / cancel_callback (:184-192).
+/* Callbacks: shapes of vhsdecode_cuda_fast_read_callback / cancel_callback (:55-62).
  * read: copy up to sample_count int16 samples starting at sample_offset into
  * destination and return the count; a short count means end of input, 0 means
  * end of input or failure. cancel: return nonzero to cancel. */
@@ -88,7 +88,7 @@ typedef size_t (VHSDECODE_GB300_CALL *vhsdecode_gb300_read_callback)(
     void* user_data, void* destination, uint64_t sample_offset, size_t sample_count);
 typedef int32_t (VHSDECODE_GB300_CALL *vhsdecode_gb300_cancel_callback)(void* user_data);
 
-/* vhsdecode_cuda_fast_runtime_info_v1 (:200-210). */
+/* vhsdecode_cuda_fast_runtime_info_v1 (:71-81). */
 typedef struct vhsdecode_gb300_runtime_info_v1 {
     uint32_t struct_size;
     uint32_t abi_version;
@@ -101,7 +101,7 @@ typedef struct vhsdecode_gb300_runtime_info_v1 {
     char device_name[VHSDECODE_GB300_NAME_CAPACITY];
 } vhsdecode_gb300_runtime_info_v1;
 
-/* vhsdecode_cuda_fast_config_v1 (:212-227), same fields and order. */
+/* vhsdecode_cuda_fast_config_v1 (:83-98), same fields and order. */
 typedef struct vhsdecode_gb300_config_v1 {
     uint32_t struct_size;
     uint32_t profile;
@@ -119,7 +119,7 @@ typedef struct vhsdecode_gb300_config_v1 {
     void* user_data;
 } vhsdecode_gb300_config_v1;
 
-/* vhsdecode_cuda_fast_result_v1 (:229-235). */
+/* vhsdecode_cuda_fast_result_v1 (:100-106). */
 typedef struct vhsdecode_gb300_result_v1 {
     uint32_t struct_size;
     uint32_t fields_written;
@@ -176,30 +176,30 @@ typedef struct vhsdecode_gb300_field_info_v1 {
 
 /* ---- reference-shaped entry points ---------------------------------- */
 
-/* vhsdecode_cuda_fast_get_abi_version (:274-275) */
+/* vhsdecode_cuda_fast_get_abi_version (:145-146) */
 VHSDECODE_GB300_API uint32_t VHSDECODE_GB300_CALL vhsdecode_gb300_get_abi_version(void);
 
-/* vhsdecode_cuda_fast_get_runtime_info (:277-280) */
+/* vhsdecode_cuda_fast_get_runtime_info (:148-151) */
 VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_get_runtime_info(
     int32_t device_id, vhsdecode_gb300_runtime_info_v1* info);
 
-/* vhsdecode_cuda_fast_run (:282-285): whole-run handoff.  Pulls int16 RF through
+/* vhsdecode_cuda_fast_run (:153-156): whole-run handoff.  Pulls int16 RF through
  * read_callback, decodes every field and writes <base>.tbc (uint16 LE luma,
  * outlinelen x (frame_lines/2+1) per field) and <base>.tbc.json. */
 VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_run(
     const vhsdecode_gb300_config_v1* config, vhsdecode_gb300_result_v1* result);
 
-/* vhsdecode_cuda_fast_get_last_error (:302-303), thread-local message. */
+/* vhsdecode_cuda_fast_get_last_error (:173-174), thread-local message. */
 VHSDECODE_GB300_API const char* VHSDECODE_GB300_CALL vhsdecode_gb300_get_last_error(void);
 
 /* ---- session API ------------------------------------------------------ */
 
-/* Replaces the preview context of vhsdecode_cuda_fast_preview_create (:287-290):
+/* Replaces the preview context of vhsdecode_cuda_fast_preview_create (:158-161):
  * a persistent device context for repeated windows. */
 VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_session_create(
     const vhsdecode_gb300_session_config_v1* config, vhsdecode_gb300_session** session);
 
-/* vhsdecode_cuda_fast_preview_destroy (:297-299) */
+/* vhsdecode_cuda_fast_preview_destroy (:169-171) */
 VHSDECODE_GB300_API void VHSDECODE_GB300_CALL vhsdecode_gb300_session_destroy(
     vhsdecode_gb300_session* session);
 
