@@ -271,6 +271,12 @@ VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_find_pulses(
     int64_t maximum_length, int64_t* starts, int64_t* lengths, uint64_t capacity,
     uint64_t* count);
 
+/* Device FM demodulation of n float pairs (PortedMath.UnwrapHilbertVhsRustApproximation,
+ * Core/Dsp/PortedMath.cs:70-230, 519-551): out[0] = 0, out[i] = wrapped angle
+ * difference of samples i and i-1 scaled to Hz at sample_rate_hz. */
+VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_vhs_demod(
+    const float* real, const float* imaginary, uint64_t n, double sample_rate_hz, float* out);
+
 /* Device polynomial atan2 (the FM demodulator's angle) for n float pairs. */
 VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_vhs_angles(
     const float* real, const float* imaginary, uint64_t n, float* angles);

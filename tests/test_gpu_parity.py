@@ -38,6 +38,28 @@ def test_device_atan2_bit_exact(gpu):
     assert a[~nan].view(np.uint32).tolist() == b[~nan].view(np.uint32).tolist()
 
 
+def test_device_fm_demod_bit_exact(gpu):
+    from vhsd_gb300 import native
+    from oracle import native as onative
+    rng = np.random.default_rng(11)
+    n = 1 << 16
+    # phases stepping by up to +-pi with equal, opposite and near-boundary angles
+    ph = np.cumsum(rng.uniform(-np.pi, np.pi, n))
+    ph[1000:1010] = ph[999]
+    ph[2000:2010] = np.pi * np.array([1, -1] * 5)
+    amp = 10 ** rng.uniform(-40, 4, n)
+    re = (amp * np.cos(ph)).astype(np.float32)
+    im = (amp * np.sin(ph)).astype(np.float32)
+    im[3000:3010] = np.array([0.0, -0.0] * 5, np.float32)
+    re[3000:3010] = np.array([1.0, 1.0, -1.0, -1.0, 1e-45, -1e-45, 2.0, 3.0, -2.0, -3.0], np.float32)
+    re[4000:4010] = np.float32(np.nan)
+    a = native.vhs_demod(re, im, 40e6)
+    b = onative.vhs_rust_demod(re.astype(np.float64), im.astype(np.float64), 40e6).astype(np.float32)
+    nan = np.isnan(b)
+    assert np.array_equal(np.isnan(a), nan)
+    assert a[~nan].view(np.uint32).tolist() == b[~nan].view(np.uint32).tolist()
+
+
 def test_device_pulses_match_state_machine(gpu):
     from vhsd_gb300 import native
     from oracle import native as onative

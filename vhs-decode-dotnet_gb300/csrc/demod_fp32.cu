@@ -54,6 +54,7 @@ __device__ __forceinline__ int sx(int i) { return i + (i >> 4); }
 struct Tw {
     float2 hi[256];  // exp(-2 pi i h*128/32768)
     float2 lo[128];  // exp(-2 pi i l/32768)
+    float2 lo8[16];  // lo[8 b]: conflict-free W^(8 v) for consecutive v
 };
 
 // exp(-2 pi i k / 32768) for k in [0, 32768)
@@ -63,6 +64,10 @@ __device__ __forceinline__ float2 w32k(const Tw& t, int k) {
 
 // One Stockham radix-R pass over `batch` transforms of length L stored
 // contiguously from buf index 0.  Each thread handles J butterflies.
+// Twiddles W^(k r step), r = 8a + b: W^(8a k step) is read from the tables
+// (a < R/8), W^(b k step) for b < 8 is built by repeated multiplication with
+// W^(k step), so a butterfly does R/8 table reads instead of R-1 and no
+// strided (bank-conflicting) table pattern remains.
 template <int R, int J, bool INV>
 __device__ __forceinline__ void pass(float2* buf, int L, int batch, int Ns, const Tw& tw, int tid) {
     float2 v[J][R];
@@ -83,10 +88,26 @@ __device__ __forceinline__ void pass(float2* buf, int L, int batch, int Ns, cons
 #pragma unroll
             for (int r = 0; r < R; r++) v[i][r] = buf[sx(base + j + r * nbf)];
             if (Ns > 1) {
+                float2 wb[8];
+                wb[0] = make_float2(1.0f, 0.0f);
+                wb[1] = w32k(tw, (k * step) & 32767);
+                if (INV) wb[1].y = -wb[1].y;
 #pragma unroll
-                for (int r = 1; r < R; r++) {
-                    float2 w = w32k(tw, (k * r * step) & 32767);
-                    v[i][r] = INV ? cmulc(v[i][r], w) : cmul(v[i][r], w);
+                for (int b = 2; b < 8; b++) wb[b] = cmul(wb[b - 1], wb[1]);
+#pragma unroll
+                for (int a = 0; a < R / 8; a++) {
+                    float2 wa = make_float2(1.0f, 0.0f);
+                    if (a > 0) {
+                        wa = w32k(tw, (8 * a * k * step) & 32767);
+                        if (INV) wa.y = -wa.y;
+                    }
+#pragma unroll
+                    for (int b = 0; b < 8; b++) {
+                        int r = 8 * a + b;
+                        if (r == 0) continue;
+                        float2 w = (a == 0) ? wb[b] : (b == 0 ? wa : cmul(wa, wb[b]));
+                        v[i][r] = cmul(v[i][r], w);
+                    }
                 }
             }
             dft<R, INV>(v[i]);
@@ -223,6 +244,32 @@ __device__ __forceinline__ float chunk_val(float2* local, float2* remote, int ra
     return b[sx(i)].y;
 }
 
+// One RF block into this rank's packed DIF input: rank 0 gets a + b, rank 1
+// (a - b) W^(2p), p in [0, 8192), where a / b are the complex pairs of the
+// block's first / second half.  W^(2p) = W^(8v) W^(2e) for p = 4v + e.
+__device__ __forceinline__ void load_rf(float2* buf, const int16_t* x, int rank, const Tw& tw, int tid) {
+#pragma unroll
+    for (int it = 0; it < 4; it++) {
+        int vi = tid + it * T;  // vector index in [0, 2048)
+        int4 va = __ldg(reinterpret_cast<const int4*>(x) + vi);
+        int4 vb = __ldg(reinterpret_cast<const int4*>(x + 16384) + vi);
+        const int16_t* ha = reinterpret_cast<const int16_t*>(&va);
+        const int16_t* hb = reinterpret_cast<const int16_t*>(&vb);
+        float2 w8 = make_float2(1.0f, 0.0f);
+        if (rank) w8 = cmul(tw.hi[vi >> 4], tw.lo8[vi & 15]);
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            int pp = 4 * vi + e;
+            float2 ca = make_float2((float)ha[2 * e], (float)ha[2 * e + 1]);
+            float2 cb = make_float2((float)hb[2 * e], (float)hb[2 * e + 1]);
+            float2 r;
+            if (rank == 0) r = cadd(ca, cb);
+            else r = cmul(csub(ca, cb), e == 0 ? w8 : cmul(w8, tw.lo[2 * e]));
+            buf[sx(pp)] = r;
+        }
+    }
+}
+
 }  // namespace fp32
 }  // namespace vhsd
 
@@ -243,6 +290,7 @@ vhsd_demod_fp32_kernel(FastDemodParams p) {
 
     for (int i = tid; i < 256; i += T) sh.tw.hi[i] = p.tw_hi[i];
     for (int i = tid; i < 128; i += T) sh.tw.lo[i] = p.tw_lo[i];
+    for (int i = tid; i < 16; i += T) sh.tw.lo8[i] = p.tw_lo[8 * i];
     __syncthreads();
 
     const int cluster_id = blockIdx.x >> 1;
@@ -254,25 +302,7 @@ vhsd_demod_fp32_kernel(FastDemodParams p) {
     for (int64_t blk = cluster_id; blk < p.nblocks; blk += nclusters) {
         const int16_t* x = p.rf + (blk + p.first_block) * (int64_t)S;
         // ---------------- stage 1: RF forward FFT (packed, DIF split) -----
-        // thread loads 4 vectors of 8 int16 from each half
-#pragma unroll
-        for (int it = 0; it < 4; it++) {
-            int vi = tid + it * T;  // vector index in [0, 2048)
-            int4 va = __ldg(reinterpret_cast<const int4*>(x) + vi);
-            int4 vb = __ldg(reinterpret_cast<const int4*>(x + 16384) + vi);
-            const int16_t* ha = reinterpret_cast<const int16_t*>(&va);
-            const int16_t* hb = reinterpret_cast<const int16_t*>(&vb);
-#pragma unroll
-            for (int e = 0; e < 4; e++) {
-                int pp = 4 * vi + e;
-                float2 ca = make_float2((float)ha[2 * e], (float)ha[2 * e + 1]);
-                float2 cb = make_float2((float)hb[2 * e], (float)hb[2 * e + 1]);
-                float2 r;
-                if (rank == 0) r = cadd(ca, cb);
-                else r = cmul(csub(ca, cb), w32k(sh.tw, 2 * pp));
-                buf[sx(pp)] = r;
-            }
-        }
+        load_rf(buf, x, rank, sh.tw, tid);
         __syncthreads();
         fft8192<false, 1>(buf, sh.tw, tid);
         // X * RfVideo * Hilbert / N  (Hilbert: 1 at 0 and N/2, 2 between)
@@ -367,21 +397,7 @@ vhsd_demod_fp32_kernel(FastDemodParams p) {
                 raws[n] = v.y;
             }
             __syncthreads();
-#pragma unroll
-            for (int it = 0; it < 4; it++) {
-                int vi = tid + it * T;
-                int4 va = __ldg(reinterpret_cast<const int4*>(x) + vi);
-                int4 vb = __ldg(reinterpret_cast<const int4*>(x + 16384) + vi);
-                const int16_t* ha = reinterpret_cast<const int16_t*>(&va);
-                const int16_t* hb = reinterpret_cast<const int16_t*>(&vb);
-#pragma unroll
-                for (int e = 0; e < 4; e++) {
-                    int pp = 4 * vi + e;
-                    float2 ca = make_float2((float)ha[2 * e], (float)ha[2 * e + 1]);
-                    float2 cb = make_float2((float)hb[2 * e], (float)hb[2 * e + 1]);
-                    buf[sx(pp)] = (rank == 0) ? cadd(ca, cb) : cmul(csub(ca, cb), w32k(sh.tw, 2 * pp));
-                }
-            }
+            load_rf(buf, x, rank, sh.tw, tid);
             __syncthreads();
             fft8192<false, 1>(buf, sh.tw, tid);
             post_half(sh, rank, tid, [&](int k, float2 v) {
@@ -473,8 +489,11 @@ vhsd_demod_fp32_kernel(FastDemodParams p) {
             __syncthreads();
         }
         // ---------------- envelope: filtfilt with halo-started warp scans --
-        // warp w of this rank covers local positions [w*1024, w*1024+1024),
-        // i.e. samples n0 = chunk*8192 + (w & 7)*1024.
+        // Warp w of this rank covers samples [n0, n0 + 1024) as four rows of
+        // 256; in each row lane l runs the recurrence over its 8 consecutive
+        // samples and a warp affine scan joins the lanes.  The state entering
+        // the warp's range comes from a 256-sample halo started at zero (the
+        // filter's memory c^256 is below 1e-12).
         {
             const int lc = warp >> 3;
             const int c = 2 * lc + rank;
@@ -482,88 +501,91 @@ vhsd_demod_fp32_kernel(FastDemodParams p) {
             const float b0 = p.env_b0, b1 = p.env_b1, a1 = p.env_a1;
             const float cc = -a1;
             const float gk = b1 - a1 * b0;   // state input gain
+            float c8 = cc;
+#pragma unroll
+            for (int k = 1; k < 8; k++) c8 *= cc;
+            const float* lbuf = reinterpret_cast<const float*>(buf);
+            auto local_y = [&](int n) { return lbuf[2 * sx((lc << 13) | (n & 8191)) + 1]; };
             float yv[32];
             // forward: z1' = cc*z1 + gk*e ; y = b0*e + z1
-            float zin = 0.0f;
+            float carry = 0.0f;
             if (n0 >= 256) {
-                // halo of 256 samples: 8 per lane
-                float s = 0.0f;
-                Aff h{1.0f, 0.0f};
                 int hs = n0 - 256 + lane * 8;
                 float st = 0.0f;
-                for (int k = 0; k < 8; k++) {
-                    float e = chunk_val(buf, rbuf, rank, hs + k);
-                    st = fmaf(cc, st, gk * e);
-                }
-                h.a = 1.0f;
-                for (int k = 0; k < 8; k++) h.a *= cc;
-                h.b = st;
-                Aff inc = warp_scan_incl(h, lane);
-                zin = __shfl_sync(0xffffffffu, inc.b, 31);
-                (void)s;
+#pragma unroll
+                for (int k = 0; k < 8; k++) st = fmaf(cc, st, gk * chunk_val(buf, rbuf, rank, hs + k));
+                Aff inc = warp_scan_incl(Aff{c8, st}, lane);
+                carry = __shfl_sync(0xffffffffu, inc.b, 31);
             }
-            {
-                int ms = n0 + lane * 32;
-                float st = 0.0f, pa = 1.0f;
-                for (int k = 0; k < 32; k++) {
-                    float e = chunk_val(buf, rbuf, rank, ms + k);
-                    st = fmaf(cc, st, gk * e);
-                    pa *= cc;
+#pragma unroll
+            for (int row = 0; row < 4; row++) {
+                int ms = n0 + row * 256 + lane * 8;
+                float ev[8];
+                float st = 0.0f;
+#pragma unroll
+                for (int k = 0; k < 8; k++) {
+                    ev[k] = local_y(ms + k);
+                    st = fmaf(cc, st, gk * ev[k]);
                 }
-                Aff loc{pa, st};
-                Aff inc = warp_scan_incl(loc, lane);
-                float prev_b = __shfl_up_sync(0xffffffffu, inc.b, 1);
-                float prev_a = __shfl_up_sync(0xffffffffu, inc.a, 1);
-                float z = lane == 0 ? zin : fmaf(prev_a, zin, prev_b);
-                for (int k = 0; k < 32; k++) {
-                    float e = chunk_val(buf, rbuf, rank, ms + k);
-                    float y = fmaf(b0, e, z);
-                    z = fmaf(cc, z, gk * e);
-                    yv[k] = y;
+                Aff inc = warp_scan_incl(Aff{c8, st}, lane);
+                float pb = __shfl_up_sync(0xffffffffu, inc.b, 1);
+                float pa = __shfl_up_sync(0xffffffffu, inc.a, 1);
+                float z = lane == 0 ? carry : fmaf(pa, carry, pb);
+#pragma unroll
+                for (int k = 0; k < 8; k++) {
+                    yv[row * 8 + k] = fmaf(b0, ev[k], z);
+                    z = fmaf(cc, z, gk * ev[k]);
                 }
+                carry = __shfl_sync(0xffffffffu, z, 31);
             }
             cluster.sync();
             {
-                int ms = n0 + lane * 32;
-                for (int k = 0; k < 32; k++) {
-                    int n = ms + k;
-                    int i = (lc << 13) | (n & 8191);
-                    buf[sx(i)].y = yv[k];
+                float* wbuf = reinterpret_cast<float*>(buf);
+#pragma unroll
+                for (int row = 0; row < 4; row++) {
+#pragma unroll
+                    for (int k = 0; k < 8; k++) {
+                        int n = n0 + row * 256 + lane * 8 + k;
+                        wbuf[2 * sx((lc << 13) | (n & 8191)) + 1] = yv[row * 8 + k];
+                    }
                 }
             }
             cluster.sync();
             // backward: w = b0*y + z1 ; z1' = cc*z1 + gk*y  (from high n to low n)
             const int nend = n0 + 1024;
-            float zb = 0.0f;
+            carry = 0.0f;
             if (nend + 256 <= N) {
                 int hs = nend + lane * 8;  // halo samples [nend, nend+256)
-                float st = 0.0f, pa = 1.0f;
-                for (int k = 7; k >= 0; k--) {
-                    float e = chunk_val(buf, rbuf, rank, hs + k);
-                    st = fmaf(cc, st, gk * e);
-                    pa *= cc;
-                }
-                Aff inc = warp_scan_incl_rev(Aff{pa, st}, lane);
-                zb = __shfl_sync(0xffffffffu, inc.b, 0);
+                float st = 0.0f;
+#pragma unroll
+                for (int k = 7; k >= 0; k--) st = fmaf(cc, st, gk * chunk_val(buf, rbuf, rank, hs + k));
+                Aff inc = warp_scan_incl_rev(Aff{c8, st}, lane);
+                carry = __shfl_sync(0xffffffffu, inc.b, 0);
             }
-            {
-                int ms = n0 + lane * 32;
-                float st = 0.0f, pa = 1.0f;
-                for (int k = 31; k >= 0; k--) {
-                    st = fmaf(cc, st, gk * yv[k]);
-                    pa *= cc;
-                }
-                Aff inc = warp_scan_incl_rev(Aff{pa, st}, lane);
+            float* envo = p.env_out + (blk + p.first_block) * (int64_t)S - CUT;
+#pragma unroll
+            for (int row = 3; row >= 0; row--) {
+                int ms = n0 + row * 256 + lane * 8;
+                float st = 0.0f;
+#pragma unroll
+                for (int k = 7; k >= 0; k--) st = fmaf(cc, st, gk * yv[row * 8 + k]);
+                Aff inc = warp_scan_incl_rev(Aff{c8, st}, lane);
                 float nb = __shfl_down_sync(0xffffffffu, inc.b, 1);
                 float na = __shfl_down_sync(0xffffffffu, inc.a, 1);
-                float z = lane == 31 ? zb : fmaf(na, zb, nb);
-                float* envo = p.env_out + (blk + p.first_block) * (int64_t)S - CUT;
-                for (int k = 31; k >= 0; k--) {
-                    float y = yv[k];
-                    float w = fmaf(b0, y, z);
+                float z = lane == 31 ? carry : fmaf(na, carry, nb);
+                float wv[8];
+#pragma unroll
+                for (int k = 7; k >= 0; k--) {
+                    float y = yv[row * 8 + k];
+                    wv[k] = fmaf(b0, y, z);
                     z = fmaf(cc, z, gk * y);
-                    int n = ms + k;
-                    if (n >= CUT && n < CUT + S) envo[n] = w;
+                }
+                carry = __shfl_sync(0xffffffffu, z, 0);
+                int rs = n0 + row * 256;   // rows lie wholly inside or outside the kept range
+                if (rs >= CUT && rs < CUT + S) {
+                    float4* o = reinterpret_cast<float4*>(envo + ms);
+                    o[0] = make_float4(wv[0], wv[1], wv[2], wv[3]);
+                    o[1] = make_float4(wv[4], wv[5], wv[6], wv[7]);
                 }
             }
         }

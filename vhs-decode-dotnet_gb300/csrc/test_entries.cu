@@ -25,6 +25,13 @@ using namespace vhsd;
 
 namespace {
 
+__global__ void k_demod(const float* re, const float* im, int64_t n, float freq, float* out) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (i == 0) { out[0] = 0.0f; return; }
+    out[i] = vhs_freq_diff(vhs_atan2(im[i], re[i]), vhs_atan2(im[i - 1], re[i - 1]), freq);
+}
+
 __global__ void k_angles(const float* re, const float* im, int64_t n, float* out) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) out[i] = vhs_atan2(im[i], re[i]);
@@ -78,6 +85,24 @@ VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_vhs_angles(
     CUDA_OR_RETURN(cudaMemcpy(dre, re, n * sizeof(float), cudaMemcpyHostToDevice), "h2d");
     CUDA_OR_RETURN(cudaMemcpy(dim, im, n * sizeof(float), cudaMemcpyHostToDevice), "h2d");
     k_angles<<<(unsigned)((n + 255) / 256), 256>>>(dre, dim, (int64_t)n, dout);
+    CUDA_OR_RETURN(cudaGetLastError(), "launch");
+    CUDA_OR_RETURN(cudaMemcpy(out, dout, n * sizeof(float), cudaMemcpyDeviceToHost), "d2h");
+    return set_last_error(VHSDECODE_GB300_STATUS_OK, "");
+}
+
+VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_vhs_demod(
+    const float* re, const float* im, uint64_t n, double sample_rate_hz, float* out) {
+    if ((!re || !im || !out) && n) return set_last_error(VHSDECODE_GB300_STATUS_NULL_POINTER, "null argument");
+    if (!have_device()) return set_last_error(VHSDECODE_GB300_STATUS_CUDA_UNAVAILABLE, "no CUDA device available");
+    if (n == 0) return set_last_error(VHSDECODE_GB300_STATUS_OK, "");
+    Scoped sc;
+    float* dre = sc.alloc<float>(n);
+    float* dim = sc.alloc<float>(n);
+    float* dout = sc.alloc<float>(n);
+    if (!dre || !dim || !dout) return set_last_error(VHSDECODE_GB300_STATUS_INTERNAL_ERROR, "cudaMalloc failed");
+    CUDA_OR_RETURN(cudaMemcpy(dre, re, n * sizeof(float), cudaMemcpyHostToDevice), "h2d");
+    CUDA_OR_RETURN(cudaMemcpy(dim, im, n * sizeof(float), cudaMemcpyHostToDevice), "h2d");
+    k_demod<<<(unsigned)((n + 255) / 256), 256>>>(dre, dim, (int64_t)n, (float)sample_rate_hz, dout);
     CUDA_OR_RETURN(cudaGetLastError(), "launch");
     CUDA_OR_RETURN(cudaMemcpy(out, dout, n * sizeof(float), cudaMemcpyDeviceToHost), "d2h");
     return set_last_error(VHSDECODE_GB300_STATUS_OK, "");

@@ -31,10 +31,19 @@ __device__ __forceinline__ float vhs_atan2(float y, float x) {
 }
 
 // PortedMath.VhsRustFrequencyDifference (Core/Dsp/PortedMath.cs:546-551).
+// floor(d / tau) is taken without the division where its value is certain:
+// +0 for 0 < d < tau and -1 for -tau <= d < -1e-30 (the rounded quotient of a
+// float d in those ranges stays inside [0, 1) resp. [-1, 0) and away from
+// zero); anything else (signed zeros, NaN, tiny negatives whose quotient
+// rounds to -0, |d| >= tau) takes the exact division.
 __device__ __forceinline__ float vhs_freq_diff(float cur, float prev, float freq) {
     const float tau = 6.28318548f;
     float d = __fsub_rn(cur, prev);
-    d = __fsub_rn(d, __fmul_rn(floorf(__fdiv_rn(d, tau)), tau));
+    float q;
+    if (d > 0.0f && d < tau) q = 0.0f;
+    else if (d < -1.0e-30f && d >= -tau) q = -1.0f;
+    else q = floorf(__fdiv_rn(d, tau));
+    d = __fsub_rn(d, __fmul_rn(q, tau));
     return __fdiv_rn(__fmul_rn(d, freq), tau);
 }
 

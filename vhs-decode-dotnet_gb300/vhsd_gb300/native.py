@@ -44,7 +44,7 @@ EXPORTS = [
     "vhsdecode_gb300_session_tbc_device", "vhsdecode_gb300_design_filters",
     "vhsdecode_gb300_field_sync", "vhsdecode_gb300_tbc_resample_lines",
     "vhsdecode_gb300_find_pulses", "vhsdecode_gb300_vhs_angles",
-    "vhsdecode_gb300_pulse_events_noalloc",
+    "vhsdecode_gb300_pulse_events_noalloc", "vhsdecode_gb300_vhs_demod",
 ]
 
 
@@ -160,6 +160,7 @@ def load(path: str = LIB_PATH):
                                               ctypes.c_int64, _vp, _vp, ctypes.c_uint64,
                                               _P(ctypes.c_uint64)]
     L.vhsdecode_gb300_vhs_angles.argtypes = [_vp, _vp, ctypes.c_uint64, _vp]
+    L.vhsdecode_gb300_vhs_demod.argtypes = [_vp, _vp, ctypes.c_uint64, ctypes.c_double, _vp]
     L.vhsdecode_gb300_pulse_events_noalloc.argtypes = [_vp, ctypes.c_int64, ctypes.c_double, _vp,
                                                        ctypes.c_int64, _vp, _vp]
     for name in EXPORTS:
@@ -251,6 +252,14 @@ def vhs_angles(re, im):
     im = np.ascontiguousarray(im, np.float32)
     out = np.zeros(len(re), np.float32)
     check(load().vhsdecode_gb300_vhs_angles(_ptr(re), _ptr(im), len(re), _ptr(out)))
+    return out
+
+
+def vhs_demod(re, im, fs):
+    re = np.ascontiguousarray(re, np.float32)
+    im = np.ascontiguousarray(im, np.float32)
+    out = np.zeros(len(re), np.float32)
+    check(load().vhsdecode_gb300_vhs_demod(_ptr(re), _ptr(im), len(re), float(fs), _ptr(out)))
     return out
 
 
