@@ -34,7 +34,7 @@
 #  define VHSDECODE_GB300_CALL
 #endif
 
-#define VHSDECODE_GB300_ABI_VERSION 0x00010000u
+#define VHSDECODE_GB300_ABI_VERSION 0x00010001u
 #define VHSDECODE_GB300_NAME_CAPACITY 128u
 
 #ifdef __cplusplus
@@ -159,6 +159,8 @@ typedef struct vhsdecode_gb300_decode_result_v1 {
     double demod_ms;            /* block demodulator kernel time */
     double field_ms;            /* pulses + hsync + TBC + dropout kernels */
     double host_ms;             /* host control plane */
+    uint32_t kernel_launches;   /* device kernels this decode launched */
+    uint32_t segments;          /* pipeline segments of the demod (1 for the plain path) */
 } vhsdecode_gb300_decode_result_v1;
 
 typedef struct vhsdecode_gb300_field_info_v1 {

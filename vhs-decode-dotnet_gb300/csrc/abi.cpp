@@ -15,6 +15,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <memory>
 #include <new>
 #include <stdexcept>
@@ -142,6 +143,9 @@ struct FieldRec {
     std::vector<int32_t> drop;  // triplets
 };
 
+constexpr int64_t kFirstSegBlocks = 40;   // about 1.2 M stream samples
+constexpr int64_t kSegBlocks = 128;        // about 3.9 M stream samples
+
 inline int64_t block_count(uint64_t n) {
     return n < (uint64_t)kBlock ? 0 : (int64_t)((n - kBlock) / kStride + 1);
 }
@@ -185,13 +189,27 @@ struct vhsdecode_gb300_session {
     cudaGraphExec_t plain_graph = nullptr;
     const int16_t* graph_rf = nullptr;   // input pointer baked into plain_graph
     DevBuf<int64_t> pc_counts, pc_offsets, pc_events, pc_total;
+    DevBuf<int64_t> pc_counts_alt, pc_offsets_alt;   // scan scratch of odd segments
     int64_t pc_capacity = 0;
     DevBuf<double> locs_in, locs_out;
     DevBuf<uint8_t> fill_in, fill_out;
     DevBuf<unsigned char> hsync_work;
-    DevBuf<unsigned char> gather;       // rescue segments of the sync reference
-    DevBuf<int64_t> gather_meta;
-    size_t gather_cap = 0;
+    // pipelined FP32 decode: per-segment pulse events, pinned host copies
+    cudaStream_t aux_stream = nullptr;   // rescue fetches while the session stream is busy
+    cudaStream_t copy_stream = nullptr;  // RF copies ahead of the demod
+    cudaStream_t d2h_stream = nullptr;   // pulse events back to the host behind the demod
+    cudaStream_t alt_stream = nullptr;   // odd segments, so a segment's straggler blocks overlap the next one
+    cudaEvent_t alt_start = nullptr, alt_end = nullptr;
+    std::vector<cudaEvent_t> seg_done, seg_copied, seg_pulsed, seg_dem;
+    int nseg_max = 0;
+    int64_t seg_cap = 0;                 // pulse events per segment
+    DevBuf<int64_t> seg_events, seg_total;
+    int64_t* h_events = nullptr;         // pinned [nseg_max * seg_cap]
+    int64_t* h_totals = nullptr;         // pinned [nseg_max]
+    int rescue_fetches = 0;
+    uint32_t launches = 0;               // kernels started by the current decode
+    double enqueue_ms = 0.0;             // host time to queue the pipelined demod
+    uint32_t segments = 0;
     DevBuf<int> hsync_misses;
     DevBuf<int64_t> span_start_d, span_len_d;
     DevBuf<int> first_line_d, start_line_d, end_line_d, line_off_d;
@@ -257,6 +275,7 @@ void session_init(vhsdecode_gb300_session* s, const vhsdecode_gb300_session_conf
     ck(cudaGetDeviceProperties(&prop, c.device_id), "cudaGetDeviceProperties");
     s->num_sms = prop.multiProcessorCount;
     ck(cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    ck(cudaStreamCreateWithFlags(&s->aux_stream, cudaStreamNonBlocking), "cudaStreamCreate");
     s->stream = s->own_stream;
     for (auto& ev : s->ev) ck(cudaEventCreate(&ev), "cudaEventCreate");
     s->max_blocks = block_count(c.max_samples);
@@ -293,9 +312,33 @@ void session_init(vhsdecode_gb300_session* s, const vhsdecode_gb300_session_conf
         ck(cudaMemcpy(s->tw_hi.p, hi.data(), 256 * sizeof(float2), cudaMemcpyHostToDevice), "upload");
         ck(cudaMemcpy(s->tw_lo.p, lo.data(), 128 * sizeof(float2), cudaMemcpyHostToDevice), "upload");
         int clusters = s->num_sms / 2;
-        s->scratch.alloc((size_t)clusters * 2 * kBlock);
-        s->scratch_raw.alloc((size_t)clusters * kBlock);
+        // two halves: segments on the two compute streams may run at once
+        s->scratch.alloc((size_t)2 * clusters * 2 * kBlock);
+        s->scratch_raw.alloc((size_t)2 * clusters * kBlock);
         s->repair.alloc(1);
+        s->nseg_max = (int)((std::max<int64_t>(0, s->max_blocks - kFirstSegBlocks) + kSegBlocks - 1) / kSegBlocks) + 1;
+        s->seg_cap = kSegBlocks * kStride / 64 + 4096;
+        s->seg_events.alloc((size_t)s->nseg_max * s->seg_cap);
+        s->pc_counts_alt.alloc(pulse_count_slots(kSegBlocks * kStride));
+        s->pc_offsets_alt.alloc(pulse_count_slots(kSegBlocks * kStride));
+        s->seg_total.alloc((size_t)s->nseg_max);
+        ck(cudaHostAlloc((void**)&s->h_events, (size_t)s->nseg_max * s->seg_cap * sizeof(int64_t),
+                         cudaHostAllocDefault), "cudaHostAlloc");
+        ck(cudaHostAlloc((void**)&s->h_totals, (size_t)s->nseg_max * sizeof(int64_t), cudaHostAllocDefault),
+           "cudaHostAlloc");
+        s->seg_done.resize((size_t)s->nseg_max);
+        s->seg_copied.resize((size_t)s->nseg_max);
+        s->seg_pulsed.resize((size_t)s->nseg_max);
+        s->seg_dem.resize((size_t)s->nseg_max * 2);
+        for (auto& e : s->seg_done) ck(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
+        for (auto& e : s->seg_copied) ck(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
+        for (auto& e : s->seg_pulsed) ck(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
+        for (auto& e : s->seg_dem) ck(cudaEventCreate(&e), "cudaEventCreate");
+        ck(cudaStreamCreateWithFlags(&s->copy_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        ck(cudaStreamCreateWithFlags(&s->d2h_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        ck(cudaStreamCreateWithFlags(&s->alt_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        ck(cudaEventCreateWithFlags(&s->alt_start, cudaEventDisableTiming), "cudaEventCreate");
+        ck(cudaEventCreateWithFlags(&s->alt_end, cudaEventDisableTiming), "cudaEventCreate");
     } else {
         s->v64.alloc(stream_cap); s->s64.alloc(stream_cap); s->e64.alloc(stream_cap);
         std::vector<double2> vv(H), sv(H);
@@ -375,33 +418,49 @@ void session_init(vhsdecode_gb300_session* s, const vhsdecode_gb300_session_conf
 void session_free(vhsdecode_gb300_session* s) {
     if (s->plain_graph) cudaGraphExecDestroy(s->plain_graph);
     for (auto& ev : s->ev) if (ev) cudaEventDestroy(ev);
+    for (auto* v : {&s->seg_done, &s->seg_copied, &s->seg_pulsed, &s->seg_dem})
+        for (auto& ev : *v) if (ev) cudaEventDestroy(ev);
+    if (s->h_events) cudaFreeHost(s->h_events);
+    if (s->h_totals) cudaFreeHost(s->h_totals);
+    if (s->copy_stream) cudaStreamDestroy(s->copy_stream);
+    if (s->d2h_stream) cudaStreamDestroy(s->d2h_stream);
+    if (s->alt_stream) cudaStreamDestroy(s->alt_stream);
+    if (s->alt_start) cudaEventDestroy(s->alt_start);
+    if (s->alt_end) cudaEventDestroy(s->alt_end);
+    if (s->aux_stream) cudaStreamDestroy(s->aux_stream);
     if (s->own_stream) cudaStreamDestroy(s->own_stream);
+}
+
+FastDemodParams fp32_params(vhsdecode_gb300_session* s, const int16_t* rf_dev) {
+    FastDemodParams p{};
+    p.rf = rf_dev;
+    p.first_block = 0;
+    p.nblocks = 0;
+    p.rf_video = s->rfv32.p;
+    p.video = s->vid32.p;
+    p.sync = s->syn32.p;
+    p.tw_hi = s->tw_hi.p;
+    p.tw_lo = s->tw_lo.p;
+    p.fs = (float)s->fs;
+    p.diff_max = (float)((s->fmt.ire0 + s->fmt.hz_ire * 100.0) * 2.0);
+    p.dc = (float)s->fmt.ire0;
+    p.env_b0 = (float)s->filt.env_b0;
+    p.env_b1 = (float)s->filt.env_b1;
+    p.env_a1 = (float)s->filt.env_a1;
+    p.video_out = s->v32.p;
+    p.sync_out = s->s32.p;
+    p.env_out = s->e32.p;
+    p.scratch = s->scratch.p;
+    p.scratch_raw = s->scratch_raw.p;
+    p.repair_count = s->repair.p;
+    return p;
 }
 
 void run_demod(vhsdecode_gb300_session* s, const int16_t* rf_dev, int64_t nblocks) {
     if (nblocks <= 0) return;
     if (s->fp32()) {
-        FastDemodParams p{};
-        p.rf = rf_dev;
-        p.first_block = 0;
+        FastDemodParams p = fp32_params(s, rf_dev);
         p.nblocks = nblocks;
-        p.rf_video = s->rfv32.p;
-        p.video = s->vid32.p;
-        p.sync = s->syn32.p;
-        p.tw_hi = s->tw_hi.p;
-        p.tw_lo = s->tw_lo.p;
-        p.fs = (float)s->fs;
-        p.diff_max = (float)((s->fmt.ire0 + s->fmt.hz_ire * 100.0) * 2.0);
-        p.dc = (float)s->fmt.ire0;
-        p.env_b0 = (float)s->filt.env_b0;
-        p.env_b1 = (float)s->filt.env_b1;
-        p.env_a1 = (float)s->filt.env_a1;
-        p.video_out = s->v32.p;
-        p.sync_out = s->s32.p;
-        p.env_out = s->e32.p;
-        p.scratch = s->scratch.p;
-        p.scratch_raw = s->scratch_raw.p;
-        p.repair_count = s->repair.p;
         ck(cudaMemsetAsync(s->repair.p, 0, sizeof(int), s->stream), "memset");
         ck(launch_demod_fp32(p, s->num_sms / 2, s->stream), "demod fp32 launch");
     } else {
@@ -447,84 +506,31 @@ void run_demod(vhsdecode_gb300_session* s, const int16_t* rf_dev, int64_t nblock
     }
 }
 
+// Pulse events of the stitched stream in stream order.  upto(pos) returns once
+// every event before stream position pos is in `events` (the pipelined decode
+// waits there for the segment that finalises pos).
+struct EventFeed {
+    std::vector<int64_t> events;
+    std::function<void(int64_t)> upto;
+};
+
+// TbcFieldSequenceDecodeEngine order (Core/Decode/TbcFieldSequenceDecodeEngine.cs:442-560):
+// resolve the next field span, take its pulses, run the control plane, step by
+// the next-field offset.  The long-hsync rescue reads the sync reference of a
+// finished span on the auxiliary stream, so it never waits behind queued work.
 template <typename T>
-void run_fields(vhsdecode_gb300_session* s, const T* video, const T* sync, const T* env,
-                int64_t stream_len, uint32_t max_fields, uint32_t& stop_reason, double& host_ms,
-                const std::atomic<bool>* cancel) {
+void host_field_loop(vhsdecode_gb300_session* s, const T* sync, int64_t stream_len, uint32_t max_fields,
+                     EventFeed& feed, uint32_t& stop_reason, const std::atomic<bool>* cancel) {
     const SyncParams& sp = s->sp;
-    double threshold = sp.ire_to_hz(sp.vsync_ire / 2.0);
-    ck(launch_pulse_events<T>(sync, stream_len, threshold, s->pc_counts.p, s->pc_offsets.p,
-                              s->pc_events.p, s->pc_capacity, s->pc_total.p, s->stream),
-       "pulse launch");
-    int64_t total = 0;
-    ck(cudaMemcpyAsync(&total, s->pc_total.p, sizeof(int64_t), cudaMemcpyDeviceToHost, s->stream), "d2h");
-    ck(cudaStreamSynchronize(s->stream), "sync");
-    if (total > s->pc_capacity)
-        throw Failure(VHSDECODE_GB300_STATUS_DECODE_ERROR, "sync pulse event capacity exceeded");
-    std::vector<int64_t> events((size_t)total);
-    if (total > 0)
-        ck(cudaMemcpy(events.data(), s->pc_events.p, (size_t)total * sizeof(int64_t),
-                      cudaMemcpyDeviceToHost), "d2h events");
-    auto t0 = std::chrono::steady_clock::now();
-    // Long-hsync rescue (SyncAnalyzer.TryRescueLongHSync) reads the sync
-    // reference inside pulses longer than the hsync window.  Gather every
-    // such pulse of the stream on the device in one pass and copy it back
-    // once; a request outside the gathered set falls back to a direct copy.
-    std::vector<int64_t> seg_start, seg_off;
-    std::vector<int32_t> seg_len;
-    std::vector<T> seg_data;
-    int fallback_fetches = 0;
-    {
-        std::vector<Pulse> all = span_pulses(events.data(), total, 0, stream_len, 0, INT64_MAX);
-        std::vector<double> hl;
-        double lo = sp.usec(sp.hsync_us - 1.75), hi = sp.usec(sp.hsync_us + 2.0);
-        for (const Pulse& p : all) if ((double)p.len >= lo && (double)p.len <= hi) hl.push_back((double)p.len);
-        if (!hl.empty()) {
-            std::nth_element(hl.begin(), hl.begin() + hl.size() / 2, hl.end());
-            double h1 = hl[hl.size() / 2] + sp.usec(sp.hsync_tol);
-            double cmin = h1 - 8.0, cmax = 3.0 * (h1 + 8.0);
-            int64_t off = 0;
-            for (const Pulse& p : all) {
-                if ((double)p.len >= cmin && (double)p.len <= cmax) {
-                    seg_start.push_back(p.start);
-                    seg_len.push_back((int32_t)p.len);
-                    seg_off.push_back(off);
-                    off += p.len;
-                }
-            }
-            if (off > 0) {
-                if ((size_t)off > s->gather_cap) {
-                    s->gather.alloc((size_t)off * sizeof(double));
-                    s->gather_meta.alloc(seg_start.size() * 3);
-                    s->gather_cap = (size_t)off;
-                } else if (seg_start.size() * 3 > s->gather_meta.n) {
-                    s->gather_meta.alloc(seg_start.size() * 3);
-                }
-                std::vector<int64_t> meta(seg_start.size() * 3);
-                for (size_t k = 0; k < seg_start.size(); k++) {
-                    meta[3 * k] = seg_start[k];
-                    meta[3 * k + 1] = seg_len[k];
-                    meta[3 * k + 2] = seg_off[k];
-                }
-                if (meta.size() > s->gather_meta.n) s->gather_meta.alloc(meta.size());
-                ck(cudaMemcpy(s->gather_meta.p, meta.data(), meta.size() * sizeof(int64_t),
-                              cudaMemcpyHostToDevice), "h2d");
-                ck(launch_gather<T>(sync, reinterpret_cast<T*>(s->gather.p), s->gather_meta.p,
-                                    (int)seg_start.size(), s->stream), "gather launch");
-                seg_data.resize((size_t)off);
-                ck(cudaMemcpyAsync(seg_data.data(), s->gather.p, (size_t)off * sizeof(T),
-                                   cudaMemcpyDeviceToHost, s->stream), "d2h");
-                ck(cudaStreamSynchronize(s->stream), "sync");
-            }
-        }
-    }
     int64_t read_len = read_length(sp);
     int64_t min_len = std::max<int64_t>(0, (int64_t)std::ceil(sp.usec(sp.eq_us) / 8.0));
     int64_t max_len = std::max<int64_t>(1, (int64_t)(sp.nominal * 5.0));
     FieldState st;
     int64_t intended = 0;
     s->fields.clear();
+    s->rescue_fetches = 0;
     stop_reason = 0;
+    std::vector<T> tmp;
     while (true) {
         if (cancel && cancel->load()) throw Failure(VHSDECODE_GB300_STATUS_CANCELLED, "decode cancelled");
         if ((int)s->fields.size() >= s->max_fields) { stop_reason = 1; break; }
@@ -532,23 +538,16 @@ void run_fields(vhsdecode_gb300_session* s, const T* video, const T* sync, const
         int64_t s0, slen;
         resolve_span(intended, read_len, s0, slen);
         if (s0 + slen > stream_len) break;
-        std::vector<Pulse> raw = span_pulses(events.data(), total, s0, slen, min_len, max_len);
+        feed.upto(s0 + slen);
+        std::vector<Pulse> raw = span_pulses(feed.events.data(), (int64_t)feed.events.size(), s0, slen,
+                                             min_len, max_len);
         RefFetch fetch = [&](int64_t start, int64_t len, std::vector<double>& out) {
-            int64_t gs = s0 + start;
-            auto it = std::upper_bound(seg_start.begin(), seg_start.end(), gs);
-            if (it != seg_start.begin()) {
-                size_t k = (size_t)(it - seg_start.begin()) - 1;
-                if (gs + len <= seg_start[k] + seg_len[k]) {
-                    const T* base = seg_data.data() + seg_off[k] + (gs - seg_start[k]);
-                    out.assign(base, base + len);
-                    return;
-                }
-            }
-            fallback_fetches++;
-            std::vector<T> tmp((size_t)len);
-            ck(cudaMemcpy(tmp.data(), sync + gs, (size_t)len * sizeof(T), cudaMemcpyDeviceToHost),
-               "rescue fetch");
+            tmp.resize((size_t)len);
+            ck(cudaMemcpyAsync(tmp.data(), sync + s0 + start, (size_t)len * sizeof(T),
+                               cudaMemcpyDeviceToHost, s->aux_stream), "rescue fetch");
+            ck(cudaStreamSynchronize(s->aux_stream), "rescue fetch");
             out.assign(tmp.begin(), tmp.end());
+            s->rescue_fetches++;
         };
         FieldRec rec;
         rec.sync = analyse_field(sp, raw, slen, st, fetch);
@@ -558,11 +557,16 @@ void run_fields(vhsdecode_gb300_session* s, const T* video, const T* sync, const
         intended = s0 + std::max<int64_t>(1, (int64_t)round_away(rec.sync.next_offset));
         s->fields.push_back(std::move(rec));
     }
-    auto t1 = std::chrono::steady_clock::now();
-    host_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+}
+
+// Device field stage for the analysed fields: hsync refinement, TBC, dropouts,
+// then the refined line locations and dropout lists back to the host.
+template <typename T>
+void field_stage(vhsdecode_gb300_session* s, const T* video, const T* sync, const T* env,
+                 int64_t stream_len) {
+    const SyncParams& sp = s->sp;
     int nf = (int)s->fields.size();
     if (nf == 0) return;
-    // per-field arrays
     std::vector<double> locs((size_t)nf * s->lines);
     std::vector<uint8_t> fill((size_t)nf * s->lines);
     std::vector<int64_t> span((size_t)nf), slens((size_t)nf);
@@ -587,7 +591,7 @@ void run_fields(vhsdecode_gb300_session* s, const T* video, const T* sync, const
     ck(cudaMemcpyAsync(s->start_line_d.p, sline.data(), nf * sizeof(int), cudaMemcpyHostToDevice, cs), "h2d");
     ck(cudaMemcpyAsync(s->end_line_d.p, eline.data(), nf * sizeof(int), cudaMemcpyHostToDevice, cs), "h2d");
     ck(cudaMemcpyAsync(s->line_off_d.p, loff.data(), nf * sizeof(int), cudaMemcpyHostToDevice, cs), "h2d");
-    // the span-copies above read host vectors that stay alive until the sync below
+    // the copies above read host vectors that stay alive until the sync below
     HsyncParams hp{};
     hp.nfields = nf;
     hp.lines = s->lines;
@@ -598,7 +602,7 @@ void run_fields(vhsdecode_gb300_session* s, const T* video, const T* sync, const
     hp.span_start = s->span_start_d.p;
     hp.span_len = s->span_len_d.p;
     hp.pal = sp.pal ? 1 : 0;
-    hp.threshold = threshold;
+    hp.threshold = sp.ire_to_hz(sp.vsync_ire / 2.0);
     hp.one_us = std::max(1, (int)sp.mhz);
     hp.normal_hsync = std::max(1, (int)sp.usec(sp.hsync_us));
     hp.mhz32 = (double)(float)sp.mhz;
@@ -612,6 +616,7 @@ void run_fields(vhsdecode_gb300_session* s, const T* video, const T* sync, const
     if (timing) for (auto& e : sev) ck(cudaEventCreate(&e), "event");
     if (timing) ck(cudaEventRecord(sev[0], cs), "event");
     ck(launch_hsync_refine<T>(sync, stream_len, hp, cs), "hsync launch");
+    s->launches += kHsyncKernels;
     if (timing) ck(cudaEventRecord(sev[1], cs), "event");
     TbcParams tp{};
     tp.nfields = nf;
@@ -635,6 +640,7 @@ void run_fields(vhsdecode_gb300_session* s, const T* video, const T* sync, const
     tp.out_hz = nullptr;
     tp.level_work = s->level_work.p;
     ck(launch_tbc_pw<T>(video, stream_len, tp, s->pw.p, cs), "tbc launch");
+    s->launches += kTbcKernels;
     if (timing) ck(cudaEventRecord(sev[2], cs), "event");
     DropoutParams dp{};
     dp.nfields = nf;
@@ -661,6 +667,7 @@ void run_fields(vhsdecode_gb300_session* s, const T* video, const T* sync, const
     dp.status = s->drop_status.p;
     ck(launch_dropouts_full<T>(env, stream_len, dp, s->drop_partial.p, s->drop_counts.p, cs),
        "dropout launch");
+    s->launches += kDropoutKernels;
     if (timing) {
         ck(cudaEventRecord(sev[3], cs), "event");
         ck(cudaEventSynchronize(sev[3]), "sync");
@@ -668,9 +675,9 @@ void run_fields(vhsdecode_gb300_session* s, const T* video, const T* sync, const
         cudaEventElapsedTime(&a, sev[0], sev[1]);
         cudaEventElapsedTime(&b, sev[1], sev[2]);
         cudaEventElapsedTime(&c, sev[2], sev[3]);
-        std::fprintf(stderr, "[gb300 stage] fields=%d host_control=%.3f ms hsync=%.3f ms tbc=%.3f ms "
-                     "dropouts=%.3f ms rescue_segments=%zu fallback_fetches=%d\n",
-                     nf, host_ms, a, b, c, seg_start.size(), fallback_fetches);
+        std::fprintf(stderr, "[gb300 stage] fields=%d hsync=%.3f ms tbc=%.3f ms dropouts=%.3f ms "
+                     "rescue_fetches=%d enqueue=%.3f ms segments=%u\n", nf, a, b, c, s->rescue_fetches,
+                     s->enqueue_ms, s->segments);
         for (auto& e : sev) cudaEventDestroy(e);
     }
     std::vector<double> refined((size_t)nf * s->lines);
@@ -687,9 +694,170 @@ void run_fields(vhsdecode_gb300_session* s, const T* video, const T* sync, const
         int c = std::min(dcount[f], s->drop_out_cap);
         r.drop.resize((size_t)c * 3);
         if (c > 0)
-            ck(cudaMemcpy(r.drop.data(), s->drop_out.p + (size_t)f * s->drop_out_cap * 3,
-                          (size_t)c * 3 * sizeof(int32_t), cudaMemcpyDeviceToHost), "d2h dropouts");
+            ck(cudaMemcpyAsync(r.drop.data(), s->drop_out.p + (size_t)f * s->drop_out_cap * 3,
+                               (size_t)c * 3 * sizeof(int32_t), cudaMemcpyDeviceToHost, cs), "d2h dropouts");
     }
+    ck(cudaStreamSynchronize(cs), "sync");
+}
+
+// Segment boundaries (in blocks) of the pipelined decode: a short first
+// segment so the control plane can start early, then kSegBlocks each.
+std::vector<int64_t> segment_bounds(int64_t nblocks) {
+    std::vector<int64_t> b{0};
+    int64_t e = std::min<int64_t>(nblocks, kFirstSegBlocks);
+    while (b.back() < nblocks) {
+        b.push_back(e);
+        e = std::min<int64_t>(nblocks, e + kSegBlocks);
+    }
+    return b;
+}
+
+// FP32 decode, pipelined: the capture is demodulated in segments; after each
+// segment the device writes that segment's pulse events and copies them to
+// pinned host memory, so the host control plane analyses the fields of
+// finished segments while later segments are still being demodulated.  With
+// host input the RF of each segment is copied on a separate stream ahead of
+// its demod.  Results are identical to a single pass: demod blocks are
+// independent and the ranged pulse scan carries its state across segments.
+void decode_fp32_pipelined(vhsdecode_gb300_session* s, const int16_t* rf, uint64_t n, bool host_input,
+                           bool demod_only, uint32_t max_fields, uint32_t& stop, double& host_ms,
+                           float& demod_ms, const std::atomic<bool>* cancel) {
+    cudaStream_t cs = s->stream;
+    int64_t nblocks = block_count(n);
+    int64_t stream_len = nblocks * kStride;
+    // with no field work to overlap, the demod runs as one launch
+    std::vector<int64_t> bounds = demod_only ? std::vector<int64_t>{0, nblocks} : segment_bounds(nblocks);
+    if (nblocks == 0) bounds.assign(1, 0);
+    int nseg = (int)bounds.size() - 1;
+    s->segments = (uint32_t)nseg;
+    if (nseg > s->nseg_max) throw Failure(VHSDECODE_GB300_STATUS_INTERNAL_ERROR, "segment table too small");
+    const int16_t* rf_dev = host_input ? s->rf.p : rf;
+    FastDemodParams p = fp32_params(s, rf_dev);
+    ck(cudaMemsetAsync(s->repair.p, 0, sizeof(int), cs), "memset");
+    const double threshold = s->sp.ire_to_hz(s->sp.vsync_ire / 2.0);
+    // even segments run on the session stream, odd ones on alt_stream; the
+    // pulse scan of segment k reads the sync reference up to its end and the
+    // state before it, so it waits for the demod of segments k-1 and k
+    ck(cudaEventRecord(s->alt_start, cs), "event");
+    ck(cudaStreamWaitEvent(s->alt_stream, s->alt_start, 0), "wait");
+    int64_t copied = 0;
+    auto tq0 = std::chrono::steady_clock::now();
+    for (int k = 0; k < nseg; k++) {
+        int64_t b0 = bounds[(size_t)k], b1 = bounds[(size_t)k + 1];
+        cudaStream_t ks = (k & 1) ? s->alt_stream : cs;
+        if (host_input) {
+            int64_t c1 = std::min<int64_t>((int64_t)n, (b1 - 1) * kStride + kBlock);
+            if (c1 > copied) {
+                ck(cudaMemcpyAsync(s->rf.p + copied, rf + copied, (size_t)(c1 - copied) * sizeof(int16_t),
+                                   cudaMemcpyHostToDevice, s->copy_stream), "h2d rf");
+                copied = c1;
+            }
+            ck(cudaEventRecord(s->seg_copied[(size_t)k], s->copy_stream), "event");
+            ck(cudaStreamWaitEvent(ks, s->seg_copied[(size_t)k], 0), "wait");
+        }
+        p.first_block = b0;
+        p.nblocks = b1 - b0;
+        const size_t half = (size_t)(s->num_sms / 2) * kBlock;
+        p.scratch = s->scratch.p + (k & 1) * 2 * half;
+        p.scratch_raw = s->scratch_raw.p + (k & 1) * half;
+        ck(cudaEventRecord(s->seg_dem[(size_t)(2 * k)], ks), "event");
+        ck(launch_demod_fp32(p, s->num_sms / 2, ks), "demod fp32 launch");
+        ck(cudaEventRecord(s->seg_dem[(size_t)(2 * k + 1)], ks), "event");
+        s->launches += 1;
+        if (!demod_only) {
+            // the scan needs the previous segment's samples (state before b0)
+            if (k > 0) ck(cudaStreamWaitEvent(ks, s->seg_dem[(size_t)(2 * k - 1)], 0), "wait");
+            int64_t* ev = s->seg_events.p + (size_t)k * s->seg_cap;
+            int64_t* cnt = (k & 1) ? s->pc_counts_alt.p : s->pc_counts.p;
+            int64_t* off = (k & 1) ? s->pc_offsets_alt.p : s->pc_offsets.p;
+            ck(launch_pulse_events_range<float>(s->s32.p, b0 * kStride, b1 * kStride, threshold, cnt, off, ev,
+                                                s->seg_cap, s->seg_total.p + k, ks),
+               "pulse launch");
+            s->launches += kPulseKernels;
+            ck(cudaEventRecord(s->seg_pulsed[(size_t)k], ks), "event");
+            ck(cudaStreamWaitEvent(s->d2h_stream, s->seg_pulsed[(size_t)k], 0), "wait");
+            ck(cudaMemcpyAsync(s->h_totals + k, s->seg_total.p + k, sizeof(int64_t), cudaMemcpyDeviceToHost,
+                               s->d2h_stream), "d2h");
+            ck(cudaMemcpyAsync(s->h_events + (size_t)k * s->seg_cap, ev, (size_t)s->seg_cap * sizeof(int64_t),
+                               cudaMemcpyDeviceToHost, s->d2h_stream), "d2h events");
+            ck(cudaEventRecord(s->seg_done[(size_t)k], s->d2h_stream), "event");
+        }
+    }
+    // the session stream continues only after the odd segments
+    ck(cudaEventRecord(s->alt_end, s->alt_stream), "event");
+    ck(cudaStreamWaitEvent(cs, s->alt_end, 0), "wait");
+    s->enqueue_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tq0).count();
+    if (!demod_only && nblocks > 0) {
+        auto t0 = std::chrono::steady_clock::now();
+        EventFeed feed;
+        int kdone = 0;
+        int64_t ready = 0;
+        feed.upto = [&](int64_t pos) {
+            while (ready < pos && kdone < nseg) {
+                ck(cudaEventSynchronize(s->seg_done[(size_t)kdone]), "segment wait");
+                int64_t cnt = s->h_totals[kdone];
+                if (cnt > s->seg_cap)
+                    throw Failure(VHSDECODE_GB300_STATUS_DECODE_ERROR, "sync pulse event capacity exceeded");
+                const int64_t* e = s->h_events + (size_t)kdone * s->seg_cap;
+                feed.events.insert(feed.events.end(), e, e + cnt);
+                ready = bounds[(size_t)kdone + 1] * kStride;
+                kdone++;
+            }
+        };
+        host_field_loop<float>(s, s->s32.p, stream_len, max_fields, feed, stop, cancel);
+        host_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        ck(cudaEventRecord(s->ev[2], cs), "event");
+        field_stage<float>(s, s->v32.p, s->s32.p, s->e32.p, stream_len);
+    } else {
+        ck(cudaEventRecord(s->ev[2], cs), "event");
+    }
+    ck(cudaStreamSynchronize(s->d2h_stream), "sync");
+    ck(cudaEventSynchronize(s->seg_dem[(size_t)(2 * std::max(0, nseg - 1) + 1)]), "sync");
+    demod_ms = 0.0f;
+    for (int k = 0; k < nseg; k++) {
+        float t = 0.0f;
+        ck(cudaEventElapsedTime(&t, s->seg_dem[(size_t)(2 * k)], s->seg_dem[(size_t)(2 * k + 1)]), "elapsed");
+        demod_ms += t;
+    }
+}
+
+// FP64 plain decode: whole capture, one block per graph replay, then the
+// whole-stream pulse scan, the control plane and the field stage in order.
+void decode_plain(vhsdecode_gb300_session* s, const int16_t* rf_dev, uint64_t n, bool demod_only,
+                  uint32_t max_fields, uint32_t& stop, double& host_ms, float& demod_ms,
+                  const std::atomic<bool>* cancel) {
+    cudaStream_t cs = s->stream;
+    int64_t nblocks = block_count(n);
+    int64_t stream_len = nblocks * kStride;
+    ck(cudaEventRecord(s->ev[1], cs), "event");
+    run_demod(s, rf_dev, nblocks);
+    s->launches += (uint32_t)(nblocks * kPlainBlockKernels);
+    s->segments = 1;
+    ck(cudaEventRecord(s->ev[2], cs), "event");
+    if (!demod_only && nblocks > 0) {
+        const double threshold = s->sp.ire_to_hz(s->sp.vsync_ire / 2.0);
+        ck(launch_pulse_events<double>(s->s64.p, stream_len, threshold, s->pc_counts.p, s->pc_offsets.p,
+                                       s->pc_events.p, s->pc_capacity, s->pc_total.p, cs), "pulse launch");
+        s->launches += kPulseKernels;
+        int64_t total = 0;
+        ck(cudaMemcpyAsync(&total, s->pc_total.p, sizeof(int64_t), cudaMemcpyDeviceToHost, cs), "d2h");
+        ck(cudaStreamSynchronize(cs), "sync");
+        if (total > s->pc_capacity)
+            throw Failure(VHSDECODE_GB300_STATUS_DECODE_ERROR, "sync pulse event capacity exceeded");
+        EventFeed feed;
+        feed.events.resize((size_t)total);
+        if (total > 0)
+            ck(cudaMemcpyAsync(feed.events.data(), s->pc_events.p, (size_t)total * sizeof(int64_t),
+                               cudaMemcpyDeviceToHost, cs), "d2h events");
+        ck(cudaStreamSynchronize(cs), "sync");
+        feed.upto = [](int64_t) {};
+        auto t0 = std::chrono::steady_clock::now();
+        host_field_loop<double>(s, s->s64.p, stream_len, max_fields, feed, stop, cancel);
+        host_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        field_stage<double>(s, s->v64.p, s->s64.p, s->e64.p, stream_len);
+    }
+    ck(cudaEventSynchronize(s->ev[2]), "sync");
+    ck(cudaEventElapsedTime(&demod_ms, s->ev[1], s->ev[2]), "elapsed");
 }
 
 int32_t decode_impl(vhsdecode_gb300_session* s, const int16_t* rf, uint64_t n, uint32_t max_fields,
@@ -699,25 +867,29 @@ int32_t decode_impl(vhsdecode_gb300_session* s, const int16_t* rf, uint64_t n, u
         throw Failure(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "sample_count exceeds the session capacity");
     ck(cudaSetDevice(s->device), "cudaSetDevice");
     cudaStream_t cs = s->stream;
-    int64_t nblocks = block_count(n);
-    const int16_t* rf_dev = rf;
-    ck(cudaEventRecord(s->ev[0], cs), "event");
-    if (!(flags & VHSDECODE_GB300_DECODE_DEVICE_INPUT)) {
-        if (n > 0) ck(cudaMemcpyAsync(s->rf.p, rf, n * sizeof(int16_t), cudaMemcpyHostToDevice, cs), "h2d rf");
-        rf_dev = s->rf.p;
-    } else if (((uintptr_t)rf & 15u) != 0) {
+    const bool host_input = !(flags & VHSDECODE_GB300_DECODE_DEVICE_INPUT);
+    const bool demod_only = (flags & VHSDECODE_GB300_DECODE_DEMOD_ONLY) != 0;
+    if (!host_input && ((uintptr_t)rf & 15u) != 0)
         throw Failure(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "device rf pointer must be 16-byte aligned");
-    }
-    ck(cudaEventRecord(s->ev[1], cs), "event");
-    run_demod(s, rf_dev, nblocks);
-    ck(cudaEventRecord(s->ev[2], cs), "event");
-    int64_t stream_len = nblocks * kStride;
+    int64_t nblocks = block_count(n);
     uint32_t stop = 0;
     double host_ms = 0.0;
+    float demod_ms = 0.0f;
     s->fields.clear();
-    if (!(flags & VHSDECODE_GB300_DECODE_DEMOD_ONLY) && nblocks > 0) {
-        if (s->fp32()) run_fields<float>(s, s->v32.p, s->s32.p, s->e32.p, stream_len, max_fields, stop, host_ms, cancel);
-        else run_fields<double>(s, s->v64.p, s->s64.p, s->e64.p, stream_len, max_fields, stop, host_ms, cancel);
+    s->launches = 0;
+    s->segments = 0;
+    ck(cudaEventRecord(s->ev[0], cs), "event");
+    if (s->fp32()) {
+        // the copy stream must not start before earlier work on the session stream
+        if (host_input) ck(cudaStreamWaitEvent(s->copy_stream, s->ev[0], 0), "wait");
+        decode_fp32_pipelined(s, rf, n, host_input, demod_only, max_fields, stop, host_ms, demod_ms, cancel);
+    } else {
+        const int16_t* rf_dev = rf;
+        if (host_input) {
+            if (n > 0) ck(cudaMemcpyAsync(s->rf.p, rf, n * sizeof(int16_t), cudaMemcpyHostToDevice, cs), "h2d rf");
+            rf_dev = s->rf.p;
+        }
+        decode_plain(s, rf_dev, n, demod_only, max_fields, stop, host_ms, demod_ms, cancel);
     }
     ck(cudaEventRecord(s->ev[3], cs), "event");
     ck(cudaEventSynchronize(s->ev[3]), "sync");
@@ -727,21 +899,22 @@ int32_t decode_impl(vhsdecode_gb300_session* s, const int16_t* rf, uint64_t n, u
     s->last_blocks = nblocks;
     s->last_repairs = rep;
     if (res) {
-        float t_all = 0, t_dem = 0, t_fld = 0;
+        float t_all = 0, t_fld = 0;
         cudaEventElapsedTime(&t_all, s->ev[0], s->ev[3]);
-        cudaEventElapsedTime(&t_dem, s->ev[1], s->ev[2]);
         cudaEventElapsedTime(&t_fld, s->ev[2], s->ev[3]);
         res->fields = (uint32_t)s->fields.size();
         res->output_line_length = (uint32_t)s->outlen;
         res->output_field_lines = (uint32_t)s->out_lines;
         res->blocks = (uint64_t)nblocks;
-        res->stream_samples = (uint64_t)stream_len;
+        res->stream_samples = (uint64_t)(nblocks * kStride);
         res->repaired_blocks = (uint32_t)rep;
         res->stop_reason = stop;
         res->device_ms = t_all;
-        res->demod_ms = t_dem;
+        res->demod_ms = demod_ms;
         res->field_ms = t_fld;
         res->host_ms = host_ms;
+        res->kernel_launches = s->launches;
+        res->segments = s->segments;
     }
     return VHSDECODE_GB300_STATUS_OK;
 }

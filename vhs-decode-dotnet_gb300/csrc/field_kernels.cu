@@ -64,11 +64,12 @@ __device__ __forceinline__ unsigned edge_bits(unsigned cond, unsigned hold, unsi
 }
 
 template <typename T, bool WRITE>
-__global__ void k_pulse_pass(const T* __restrict__ ref, int64_t n, Cmp<T> cmp, int64_t* counts,
-                             const int64_t* offsets, int64_t* events, int64_t capacity) {
+__global__ void k_pulse_pass(const T* __restrict__ ref, int64_t begin, int64_t n, Cmp<T> cmp,
+                             int64_t* counts, const int64_t* offsets, int64_t* events,
+                             int64_t capacity) {
     const int lane = threadIdx.x & 31;
     const int64_t wg = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int64_t start = wg * kPWarpSamples;
+    const int64_t start = begin + wg * kPWarpSamples;
     if (start >= n) {
         if (!WRITE && lane == 0) counts[wg] = 0;
         return;
@@ -132,26 +133,38 @@ __global__ void k_scan_counts(const int64_t* counts, int64_t nchunks, int64_t* o
 }  // namespace
 
 template <typename T>
-cudaError_t launch_pulse_events(const T* ref, int64_t n, double high, int64_t* counts,
-                                int64_t* offsets, int64_t* events, int64_t capacity,
-                                int64_t* total, cudaStream_t s) {
-    int64_t nchunks = (n + kPulseChunk - 1) / kPulseChunk;
+cudaError_t launch_pulse_events_range(const T* ref, int64_t begin, int64_t end, double high,
+                                      int64_t* counts, int64_t* offsets, int64_t* events,
+                                      int64_t capacity, int64_t* total, cudaStream_t s) {
+    int64_t len = end > begin ? end - begin : 0;
+    int64_t nchunks = (len + kPulseChunk - 1) / kPulseChunk;
     if (nchunks == 0) {
         cudaMemsetAsync(total, 0, sizeof(int64_t), s);
         return cudaGetLastError();
     }
     Cmp<T> cmp = make_cmp<T>(high);
-    int64_t slots = pulse_count_slots(n);
-    k_pulse_pass<T, false><<<(unsigned)nchunks, kPT, 0, s>>>(ref, n, cmp, counts, nullptr, nullptr, 0);
+    int64_t slots = pulse_count_slots(len);
+    k_pulse_pass<T, false><<<(unsigned)nchunks, kPT, 0, s>>>(ref, begin, end, cmp, counts, nullptr,
+                                                            nullptr, 0);
     k_scan_counts<<<1, 1024, 0, s>>>(counts, slots, offsets, total);
-    k_pulse_pass<T, true><<<(unsigned)nchunks, kPT, 0, s>>>(ref, n, cmp, counts, offsets, events,
-                                                           capacity);
+    k_pulse_pass<T, true><<<(unsigned)nchunks, kPT, 0, s>>>(ref, begin, end, cmp, counts, offsets,
+                                                           events, capacity);
     return cudaGetLastError();
+}
+template <typename T>
+cudaError_t launch_pulse_events(const T* ref, int64_t n, double high, int64_t* counts,
+                                int64_t* offsets, int64_t* events, int64_t capacity,
+                                int64_t* total, cudaStream_t s) {
+    return launch_pulse_events_range<T>(ref, 0, n, high, counts, offsets, events, capacity, total, s);
 }
 template cudaError_t launch_pulse_events<float>(const float*, int64_t, double, int64_t*, int64_t*,
                                                 int64_t*, int64_t, int64_t*, cudaStream_t);
 template cudaError_t launch_pulse_events<double>(const double*, int64_t, double, int64_t*, int64_t*,
                                                  int64_t*, int64_t, int64_t*, cudaStream_t);
+template cudaError_t launch_pulse_events_range<float>(const float*, int64_t, int64_t, double, int64_t*,
+                                                      int64_t*, int64_t*, int64_t, int64_t*, cudaStream_t);
+template cudaError_t launch_pulse_events_range<double>(const double*, int64_t, int64_t, double, int64_t*,
+                                                       int64_t*, int64_t*, int64_t, int64_t*, cudaStream_t);
 
 // ============================================================== hsync refine
 // RefineLineLocationsFromHSync, VHS branch with right-edge refinement
@@ -1078,25 +1091,4 @@ cudaError_t launch_dropouts_full(const T* stream, int64_t stream_len, const Drop
 template cudaError_t launch_dropouts_full<float>(const float*, int64_t, const DropoutParams&, float*, int*, cudaStream_t);
 template cudaError_t launch_dropouts_full<double>(const double*, int64_t, const DropoutParams&, float*, int*, cudaStream_t);
 
-}  // namespace vhsd
-
-namespace vhsd {
-// Copies segments meta[3k] .. meta[3k]+meta[3k+1] of `src` to dst + meta[3k+2].
-namespace {
-template <typename T>
-__global__ void k_gather(const T* src, T* dst, const int64_t* meta, int nseg) {
-    int k = blockIdx.x;
-    if (k >= nseg) return;
-    int64_t s = meta[3 * k], len = meta[3 * k + 1], off = meta[3 * k + 2];
-    for (int64_t i = threadIdx.x; i < len; i += blockDim.x) dst[off + i] = src[s + i];
-}
-}  // namespace
-template <typename T>
-cudaError_t launch_gather(const T* src, T* dst, const int64_t* meta, int nseg, cudaStream_t s) {
-    if (nseg <= 0) return cudaSuccess;
-    k_gather<T><<<nseg, 128, 0, s>>>(src, dst, meta, nseg);
-    return cudaGetLastError();
-}
-template cudaError_t launch_gather<float>(const float*, float*, const int64_t*, int, cudaStream_t);
-template cudaError_t launch_gather<double>(const double*, double*, const int64_t*, int, cudaStream_t);
 }  // namespace vhsd

@@ -56,6 +56,7 @@ struct PlainDemodParams {
     int64_t* blk;              // device-resident block index, advanced per replay
 };
 cudaError_t launch_demod_fp64_block(const PlainDemodParams& p, cudaStream_t stream);
+constexpr int kPlainBlockKernels = 38;  // kernels in one plain-path block (13 + 5 FFTs x 5 passes)
 
 // ---------------------------------------------------------------- pulses
 // Sync-pulse edge events of PulseDetection.FindPulses over a whole stitched
@@ -64,11 +65,19 @@ cudaError_t launch_demod_fp64_block(const PlainDemodParams& p, cudaStream_t stre
 // 1024 samples, then ordered write.  counts / offsets_scratch hold
 // pulse_count_slots(n) entries.
 constexpr int kPulseChunk = 4096;
+constexpr int kPulseKernels = 3;      // kernels one launch_pulse_events* call starts
 inline int64_t pulse_count_slots(int64_t n) { return (n + kPulseChunk - 1) / kPulseChunk * 4; }
 template <typename T>
 cudaError_t launch_pulse_events(const T* ref, int64_t n, double high, int64_t* counts,
                                 int64_t* offsets_scratch, int64_t* events, int64_t capacity,
                                 int64_t* total, cudaStream_t stream);
+// Same over stream positions [begin, end) of `ref`; the state entering `begin`
+// is taken from the samples before it, so consecutive ranges give exactly the
+// events of one pass over their union.  Scratch holds pulse_count_slots(end - begin).
+template <typename T>
+cudaError_t launch_pulse_events_range(const T* ref, int64_t begin, int64_t end, double high,
+                                      int64_t* counts, int64_t* offsets_scratch, int64_t* events,
+                                      int64_t capacity, int64_t* total, cudaStream_t stream);
 
 // ---------------------------------------------------------------- hsync refine
 struct HsyncParams {
@@ -90,6 +99,7 @@ struct HsyncParams {
     int* misses;               // optional: counts carried-porch speculation misses
 };
 size_t hsync_work_bytes(int nfields, int lines);
+constexpr int kHsyncKernels = 3;
 template <typename T>
 cudaError_t launch_hsync_refine(const T* sync_stream, int64_t stream_len, const HsyncParams& p,
                                 cudaStream_t stream);
@@ -114,6 +124,7 @@ struct TbcParams {
     double* out_hz;             // optional float output (values rounded to float)
     double* level_work;         // [nfields * (max_first_line + out_lines)] line factors
 };
+constexpr int kTbcKernels = 2;
 // pw[k] = (1 - alpha)^(k+1), k < outlen, alpha = 1 / (smoothing * outlen)
 template <typename T>
 cudaError_t launch_tbc_pw(const T* video_stream, int64_t stream_len, const TbcParams& p,
@@ -145,14 +156,10 @@ struct DropoutParams {
     int* status;                // [nfields] 0 ok, 1 output capacity, 2 event capacity
 };
 int dropout_chunks(int64_t span_len);
+constexpr int kDropoutKernels = 5;
 // partial: [nfields * nchunk] floats; chunk_counts: [nfields * nchunk]
 template <typename T>
 cudaError_t launch_dropouts_full(const T* env_stream, int64_t stream_len, const DropoutParams& p,
                                  float* partial, int* chunk_counts, cudaStream_t stream);
 
-}  // namespace vhsd
-
-namespace vhsd {
-template <typename T>
-cudaError_t launch_gather(const T* src, T* dst, const int64_t* meta, int nseg, cudaStream_t stream);
 }  // namespace vhsd

@@ -13,7 +13,7 @@ import os
 
 import numpy as np
 
-ABI_VERSION = 0x00010000
+ABI_VERSION = 0x00010001
 STATUS_OK = 0
 STATUS_NULL_POINTER = -20000
 STATUS_INVALID_ARGUMENT = -20001
@@ -104,7 +104,8 @@ class DecodeResult(ctypes.Structure):
                 ("blocks", ctypes.c_uint64), ("stream_samples", ctypes.c_uint64),
                 ("repaired_blocks", ctypes.c_uint32), ("stop_reason", ctypes.c_uint32),
                 ("device_ms", ctypes.c_double), ("demod_ms", ctypes.c_double),
-                ("field_ms", ctypes.c_double), ("host_ms", ctypes.c_double)]
+                ("field_ms", ctypes.c_double), ("host_ms", ctypes.c_double),
+                ("kernel_launches", ctypes.c_uint32), ("segments", ctypes.c_uint32)]
 
 
 class FieldInfo(ctypes.Structure):
