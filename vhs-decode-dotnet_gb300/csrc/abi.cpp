@@ -209,6 +209,11 @@ struct vhsdecode_gb300_session {
     int rescue_fetches = 0;
     uint32_t launches = 0;               // kernels started by the current decode
     double enqueue_ms = 0.0;             // host time to queue the pipelined demod
+    cudaStream_t field_stream = nullptr; // field batches, concurrent with later demod segments
+    cudaEvent_t field_end = nullptr;
+    bool stage_timing = false;           // VHSD_STAGE_TIMING set: per-stage kernel times to stderr
+    cudaEvent_t stage_ev[4] = {};
+    float stage_ms[3] = {};
     uint32_t segments = 0;
     DevBuf<int> hsync_misses;
     DevBuf<int64_t> span_start_d, span_len_d;
@@ -276,6 +281,10 @@ void session_init(vhsdecode_gb300_session* s, const vhsdecode_gb300_session_conf
     s->num_sms = prop.multiProcessorCount;
     ck(cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking), "cudaStreamCreate");
     ck(cudaStreamCreateWithFlags(&s->aux_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    ck(cudaStreamCreateWithFlags(&s->field_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    ck(cudaEventCreateWithFlags(&s->field_end, cudaEventDisableTiming), "cudaEventCreate");
+    for (auto& e : s->stage_ev) ck(cudaEventCreate(&e), "cudaEventCreate");
+    s->stage_timing = std::getenv("VHSD_STAGE_TIMING") != nullptr;
     s->stream = s->own_stream;
     for (auto& ev : s->ev) ck(cudaEventCreate(&ev), "cudaEventCreate");
     s->max_blocks = block_count(c.max_samples);
@@ -428,6 +437,9 @@ void session_free(vhsdecode_gb300_session* s) {
     if (s->alt_start) cudaEventDestroy(s->alt_start);
     if (s->alt_end) cudaEventDestroy(s->alt_end);
     if (s->aux_stream) cudaStreamDestroy(s->aux_stream);
+    if (s->field_stream) cudaStreamDestroy(s->field_stream);
+    if (s->field_end) cudaEventDestroy(s->field_end);
+    for (auto& e : s->stage_ev) if (e) cudaEventDestroy(e);
     if (s->own_stream) cudaStreamDestroy(s->own_stream);
 }
 
@@ -520,7 +532,8 @@ struct EventFeed {
 // finished span on the auxiliary stream, so it never waits behind queued work.
 template <typename T>
 void host_field_loop(vhsdecode_gb300_session* s, const T* sync, int64_t stream_len, uint32_t max_fields,
-                     EventFeed& feed, uint32_t& stop_reason, const std::atomic<bool>* cancel) {
+                     EventFeed& feed, uint32_t& stop_reason, const std::atomic<bool>* cancel,
+                     const std::function<void(int)>& on_field = nullptr) {
     const SyncParams& sp = s->sp;
     int64_t read_len = read_length(sp);
     int64_t min_len = std::max<int64_t>(0, (int64_t)std::ceil(sp.usec(sp.eq_us) / 8.0));
@@ -556,51 +569,53 @@ void host_field_loop(vhsdecode_gb300_session* s, const T* sync, int64_t stream_l
         if (!rec.sync.ok) { stop_reason = 2; break; }
         intended = s0 + std::max<int64_t>(1, (int64_t)round_away(rec.sync.next_offset));
         s->fields.push_back(std::move(rec));
+        if (on_field) on_field((int)s->fields.size());
     }
 }
 
-// Device field stage for the analysed fields: hsync refinement, TBC, dropouts,
-// then the refined line locations and dropout lists back to the host.
+// Device field stage for fields [f0, f1) of s->fields: hsync refinement, TBC
+// and dropouts, queued on `fs` (every per-field array is offset by f0).  The
+// host must already have seen the demod of those fields' spans complete.
 template <typename T>
-void field_stage(vhsdecode_gb300_session* s, const T* video, const T* sync, const T* env,
-                 int64_t stream_len) {
+void launch_field_batch(vhsdecode_gb300_session* s, int f0, int f1, const T* video, const T* sync,
+                        const T* env, int64_t stream_len, cudaStream_t fs) {
     const SyncParams& sp = s->sp;
-    int nf = (int)s->fields.size();
-    if (nf == 0) return;
-    std::vector<double> locs((size_t)nf * s->lines);
-    std::vector<uint8_t> fill((size_t)nf * s->lines);
+    const int nf = f1 - f0;
+    if (nf <= 0) return;
+    const size_t L = (size_t)s->lines;
+    std::vector<double> locs((size_t)nf * L);
+    std::vector<uint8_t> fill((size_t)nf * L);
     std::vector<int64_t> span((size_t)nf), slens((size_t)nf);
     std::vector<int> fline(nf), sline(nf), eline(nf), loff(nf);
-    for (int f = 0; f < nf; f++) {
-        const FieldSync& fs = s->fields[(size_t)f].sync;
-        std::copy(fs.locs.begin(), fs.locs.end(), locs.begin() + (size_t)f * s->lines);
-        std::copy(fs.filled.begin(), fs.filled.end(), fill.begin() + (size_t)f * s->lines);
-        span[(size_t)f] = s->fields[(size_t)f].span_start;
-        slens[(size_t)f] = s->fields[(size_t)f].span_len;
-        fline[f] = sp.pal ? (fs.first_field ? 3 : 4) : 1;
-        loff[f] = sp.pal ? (fs.first_field ? 2 : 3) : 0;
-        sline[f] = loff[f] + 1;
-        eline[f] = std::min(s->lines - 1, sp.field_lines(fs.first_field) + sline[f] + 1);
+    for (int i = 0; i < nf; i++) {
+        const FieldSync& fsy = s->fields[(size_t)(f0 + i)].sync;
+        std::copy(fsy.locs.begin(), fsy.locs.end(), locs.begin() + (size_t)i * L);
+        std::copy(fsy.filled.begin(), fsy.filled.end(), fill.begin() + (size_t)i * L);
+        span[(size_t)i] = s->fields[(size_t)(f0 + i)].span_start;
+        slens[(size_t)i] = s->fields[(size_t)(f0 + i)].span_len;
+        fline[i] = sp.pal ? (fsy.first_field ? 3 : 4) : 1;
+        loff[i] = sp.pal ? (fsy.first_field ? 2 : 3) : 0;
+        sline[i] = loff[i] + 1;
+        eline[i] = std::min(s->lines - 1, sp.field_lines(fsy.first_field) + sline[i] + 1);
     }
-    cudaStream_t cs = s->stream;
-    ck(cudaMemcpyAsync(s->locs_in.p, locs.data(), locs.size() * sizeof(double), cudaMemcpyHostToDevice, cs), "h2d");
-    ck(cudaMemcpyAsync(s->fill_in.p, fill.data(), fill.size(), cudaMemcpyHostToDevice, cs), "h2d");
-    ck(cudaMemcpyAsync(s->span_start_d.p, span.data(), span.size() * sizeof(int64_t), cudaMemcpyHostToDevice, cs), "h2d");
-    ck(cudaMemcpyAsync(s->span_len_d.p, slens.data(), slens.size() * sizeof(int64_t), cudaMemcpyHostToDevice, cs), "h2d");
-    ck(cudaMemcpyAsync(s->first_line_d.p, fline.data(), nf * sizeof(int), cudaMemcpyHostToDevice, cs), "h2d");
-    ck(cudaMemcpyAsync(s->start_line_d.p, sline.data(), nf * sizeof(int), cudaMemcpyHostToDevice, cs), "h2d");
-    ck(cudaMemcpyAsync(s->end_line_d.p, eline.data(), nf * sizeof(int), cudaMemcpyHostToDevice, cs), "h2d");
-    ck(cudaMemcpyAsync(s->line_off_d.p, loff.data(), nf * sizeof(int), cudaMemcpyHostToDevice, cs), "h2d");
-    // the copies above read host vectors that stay alive until the sync below
+    // pageable sources: each copy has been staged by the time the call returns
+    ck(cudaMemcpyAsync(s->locs_in.p + f0 * L, locs.data(), locs.size() * sizeof(double), cudaMemcpyHostToDevice, fs), "h2d");
+    ck(cudaMemcpyAsync(s->fill_in.p + f0 * L, fill.data(), fill.size(), cudaMemcpyHostToDevice, fs), "h2d");
+    ck(cudaMemcpyAsync(s->span_start_d.p + f0, span.data(), nf * sizeof(int64_t), cudaMemcpyHostToDevice, fs), "h2d");
+    ck(cudaMemcpyAsync(s->span_len_d.p + f0, slens.data(), nf * sizeof(int64_t), cudaMemcpyHostToDevice, fs), "h2d");
+    ck(cudaMemcpyAsync(s->first_line_d.p + f0, fline.data(), nf * sizeof(int), cudaMemcpyHostToDevice, fs), "h2d");
+    ck(cudaMemcpyAsync(s->start_line_d.p + f0, sline.data(), nf * sizeof(int), cudaMemcpyHostToDevice, fs), "h2d");
+    ck(cudaMemcpyAsync(s->end_line_d.p + f0, eline.data(), nf * sizeof(int), cudaMemcpyHostToDevice, fs), "h2d");
+    ck(cudaMemcpyAsync(s->line_off_d.p + f0, loff.data(), nf * sizeof(int), cudaMemcpyHostToDevice, fs), "h2d");
     HsyncParams hp{};
     hp.nfields = nf;
     hp.lines = s->lines;
-    hp.locs_in = s->locs_in.p;
-    hp.filled_in = s->fill_in.p;
-    hp.locs_out = s->locs_out.p;
-    hp.filled_out = s->fill_out.p;
-    hp.span_start = s->span_start_d.p;
-    hp.span_len = s->span_len_d.p;
+    hp.locs_in = s->locs_in.p + f0 * L;
+    hp.filled_in = s->fill_in.p + f0 * L;
+    hp.locs_out = s->locs_out.p + f0 * L;
+    hp.filled_out = s->fill_out.p + f0 * L;
+    hp.span_start = s->span_start_d.p + f0;
+    hp.span_len = s->span_len_d.p + f0;
     hp.pal = sp.pal ? 1 : 0;
     hp.threshold = sp.ire_to_hz(sp.vsync_ire / 2.0);
     hp.one_us = std::max(1, (int)sp.mhz);
@@ -609,22 +624,20 @@ void field_stage(vhsdecode_gb300_session* s, const T* video, const T* sync, cons
     hp.ire0 = sp.ire0;
     hp.hz_ire = sp.hz_ire;
     hp.ntsc_shift = sp.pal ? 0.0 : ((117.25 / 360.0) / sp.fsc_mhz) * sp.mhz;
-    hp.work = s->hsync_work.p;
+    hp.work = s->hsync_work.p + hsync_work_bytes(f0, s->lines);
     hp.misses = nullptr;
-    const bool timing = std::getenv("VHSD_STAGE_TIMING") != nullptr;
-    cudaEvent_t sev[4] = {};
-    if (timing) for (auto& e : sev) ck(cudaEventCreate(&e), "event");
-    if (timing) ck(cudaEventRecord(sev[0], cs), "event");
-    ck(launch_hsync_refine<T>(sync, stream_len, hp, cs), "hsync launch");
+    const bool timing = s->stage_timing;
+    if (timing) ck(cudaEventRecord(s->stage_ev[0], fs), "event");
+    ck(launch_hsync_refine<T>(sync, stream_len, hp, fs), "hsync launch");
     s->launches += kHsyncKernels;
-    if (timing) ck(cudaEventRecord(sev[1], cs), "event");
+    if (timing) ck(cudaEventRecord(s->stage_ev[1], fs), "event");
     TbcParams tp{};
     tp.nfields = nf;
     tp.lines = s->lines;
-    tp.locs = s->locs_out.p;
-    tp.span_start = s->span_start_d.p;
-    tp.span_len = s->span_len_d.p;
-    tp.first_line = s->first_line_d.p;
+    tp.locs = s->locs_out.p + f0 * L;
+    tp.span_start = s->span_start_d.p + f0;
+    tp.span_len = s->span_len_d.p + f0;
+    tp.first_line = s->first_line_d.p + f0;
     tp.out_lines = s->out_lines;
     tp.outlen = s->outlen;
     tp.nominal = std::nearbyint(s->fmt.line_period_us * sp.mhz);
@@ -636,56 +649,61 @@ void field_stage(vhsdecode_gb300_session* s, const T* video, const T* sync, cons
     tp.output_scale = output_scale(s->fmt);
     tp.inv_hz_ire = 1.0 / s->fmt.hz_ire;
     tp.offset = (s->fmt.output_zero + 0.5) - (s->fmt.vsync_ire * tp.output_scale);
-    tp.out_u16 = s->tbc.p;
+    tp.out_u16 = s->tbc.p + (size_t)f0 * s->out_lines * s->outlen;
     tp.out_hz = nullptr;
-    tp.level_work = s->level_work.p;
-    ck(launch_tbc_pw<T>(video, stream_len, tp, s->pw.p, cs), "tbc launch");
+    tp.level_work = s->level_work.p + (size_t)f0 * 1024;
+    ck(launch_tbc_pw<T>(video, stream_len, tp, s->pw.p, fs), "tbc launch");
     s->launches += kTbcKernels;
-    if (timing) ck(cudaEventRecord(sev[2], cs), "event");
+    if (timing) ck(cudaEventRecord(s->stage_ev[2], fs), "event");
+    const int nch = dropout_chunks(s->span_len);
     DropoutParams dp{};
     dp.nfields = nf;
-    dp.span_start = s->span_start_d.p;
-    dp.span_len = s->span_len_d.p;
+    dp.span_start = s->span_start_d.p + f0;
+    dp.span_len = s->span_len_d.p + f0;
     dp.max_span_len = s->span_len;
-    dp.locs = s->locs_out.p;
+    dp.locs = s->locs_out.p + f0 * L;
     dp.lines = s->lines;
-    dp.start_line = s->start_line_d.p;
-    dp.end_line = s->end_line_d.p;
-    dp.line_offset = s->line_off_d.p;
+    dp.start_line = s->start_line_d.p + f0;
+    dp.end_line = s->end_line_d.p + f0;
+    dp.line_offset = s->line_off_d.p + f0;
     dp.outlen = s->outlen;
-    dp.range = s->drop_range.p;
+    dp.range = s->drop_range.p + 2 * (size_t)f0;
     dp.frac = 0.18f;
     dp.hyst = 1.25;
     dp.merge = 30;
     dp.min_len = 10;
-    dp.mean_out = s->drop_mean.p;
-    dp.events = s->drop_events.p;
+    dp.mean_out = s->drop_mean.p + f0;
+    dp.events = s->drop_events.p + (size_t)f0 * nch * s->drop_cap;
     dp.cap = s->drop_cap;
-    dp.out = s->drop_out.p;
+    dp.out = s->drop_out.p + (size_t)f0 * s->drop_out_cap * 3;
     dp.out_cap = s->drop_out_cap;
-    dp.out_count = s->drop_out_count.p;
-    dp.status = s->drop_status.p;
-    ck(launch_dropouts_full<T>(env, stream_len, dp, s->drop_partial.p, s->drop_counts.p, cs),
-       "dropout launch");
+    dp.out_count = s->drop_out_count.p + f0;
+    dp.status = s->drop_status.p + f0;
+    ck(launch_dropouts_full<T>(env, stream_len, dp, s->drop_partial.p + (size_t)f0 * nch,
+                               s->drop_counts.p + (size_t)f0 * nch, fs), "dropout launch");
     s->launches += kDropoutKernels;
     if (timing) {
-        ck(cudaEventRecord(sev[3], cs), "event");
-        ck(cudaEventSynchronize(sev[3]), "sync");
+        ck(cudaEventRecord(s->stage_ev[3], fs), "event");
+        ck(cudaEventSynchronize(s->stage_ev[3]), "sync");
         float a = 0, b = 0, c = 0;
-        cudaEventElapsedTime(&a, sev[0], sev[1]);
-        cudaEventElapsedTime(&b, sev[1], sev[2]);
-        cudaEventElapsedTime(&c, sev[2], sev[3]);
-        std::fprintf(stderr, "[gb300 stage] fields=%d hsync=%.3f ms tbc=%.3f ms dropouts=%.3f ms "
-                     "rescue_fetches=%d enqueue=%.3f ms segments=%u\n", nf, a, b, c, s->rescue_fetches,
-                     s->enqueue_ms, s->segments);
-        for (auto& e : sev) cudaEventDestroy(e);
+        cudaEventElapsedTime(&a, s->stage_ev[0], s->stage_ev[1]);
+        cudaEventElapsedTime(&b, s->stage_ev[1], s->stage_ev[2]);
+        cudaEventElapsedTime(&c, s->stage_ev[2], s->stage_ev[3]);
+        s->stage_ms[0] += a; s->stage_ms[1] += b; s->stage_ms[2] += c;
     }
+}
+
+// Refined line locations and dropout lists of every field back to the host
+// once `fs` has finished the field stage.
+void collect_field_results(vhsdecode_gb300_session* s, cudaStream_t fs) {
+    int nf = (int)s->fields.size();
+    if (nf == 0) return;
     std::vector<double> refined((size_t)nf * s->lines);
     std::vector<int> dcount(nf), dstat(nf);
-    ck(cudaMemcpyAsync(refined.data(), s->locs_out.p, refined.size() * sizeof(double), cudaMemcpyDeviceToHost, cs), "d2h");
-    ck(cudaMemcpyAsync(dcount.data(), s->drop_out_count.p, nf * sizeof(int), cudaMemcpyDeviceToHost, cs), "d2h");
-    ck(cudaMemcpyAsync(dstat.data(), s->drop_status.p, nf * sizeof(int), cudaMemcpyDeviceToHost, cs), "d2h");
-    ck(cudaStreamSynchronize(cs), "sync");
+    ck(cudaMemcpyAsync(refined.data(), s->locs_out.p, refined.size() * sizeof(double), cudaMemcpyDeviceToHost, fs), "d2h");
+    ck(cudaMemcpyAsync(dcount.data(), s->drop_out_count.p, nf * sizeof(int), cudaMemcpyDeviceToHost, fs), "d2h");
+    ck(cudaMemcpyAsync(dstat.data(), s->drop_status.p, nf * sizeof(int), cudaMemcpyDeviceToHost, fs), "d2h");
+    ck(cudaStreamSynchronize(fs), "sync");
     for (int f = 0; f < nf; f++) {
         FieldRec& r = s->fields[(size_t)f];
         r.refined.assign(refined.begin() + (size_t)f * s->lines, refined.begin() + (size_t)(f + 1) * s->lines);
@@ -695,9 +713,13 @@ void field_stage(vhsdecode_gb300_session* s, const T* video, const T* sync, cons
         r.drop.resize((size_t)c * 3);
         if (c > 0)
             ck(cudaMemcpyAsync(r.drop.data(), s->drop_out.p + (size_t)f * s->drop_out_cap * 3,
-                               (size_t)c * 3 * sizeof(int32_t), cudaMemcpyDeviceToHost, cs), "d2h dropouts");
+                               (size_t)c * 3 * sizeof(int32_t), cudaMemcpyDeviceToHost, fs), "d2h dropouts");
     }
-    ck(cudaStreamSynchronize(cs), "sync");
+    ck(cudaStreamSynchronize(fs), "sync");
+    if (s->stage_timing)
+        std::fprintf(stderr, "[gb300 stage] fields=%d hsync=%.3f ms tbc=%.3f ms dropouts=%.3f ms "
+                     "rescue_fetches=%d enqueue=%.3f ms segments=%u\n", nf, s->stage_ms[0], s->stage_ms[1],
+                     s->stage_ms[2], s->rescue_fetches, s->enqueue_ms, s->segments);
 }
 
 // Segment boundaries (in blocks) of the pipelined decode: a short first
@@ -804,10 +826,16 @@ void decode_fp32_pipelined(vhsdecode_gb300_session* s, const int16_t* rf, uint64
                 kdone++;
             }
         };
+        // The field kernels are latency bound per field (the hsync chain walks
+        // a field's lines in order), so they run as one batch over all fields.
         host_field_loop<float>(s, s->s32.p, stream_len, max_fields, feed, stop, cancel);
         host_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
         ck(cudaEventRecord(s->ev[2], cs), "event");
-        field_stage<float>(s, s->v32.p, s->s32.p, s->e32.p, stream_len);
+        launch_field_batch<float>(s, 0, (int)s->fields.size(), s->v32.p, s->s32.p, s->e32.p,
+                                  stream_len, s->field_stream);
+        collect_field_results(s, s->field_stream);
+        ck(cudaEventRecord(s->field_end, s->field_stream), "event");
+        ck(cudaStreamWaitEvent(cs, s->field_end, 0), "wait");
     } else {
         ck(cudaEventRecord(s->ev[2], cs), "event");
     }
@@ -854,7 +882,8 @@ void decode_plain(vhsdecode_gb300_session* s, const int16_t* rf_dev, uint64_t n,
         auto t0 = std::chrono::steady_clock::now();
         host_field_loop<double>(s, s->s64.p, stream_len, max_fields, feed, stop, cancel);
         host_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-        field_stage<double>(s, s->v64.p, s->s64.p, s->e64.p, stream_len);
+        launch_field_batch<double>(s, 0, (int)s->fields.size(), s->v64.p, s->s64.p, s->e64.p, stream_len, cs);
+        collect_field_results(s, cs);
     }
     ck(cudaEventSynchronize(s->ev[2]), "sync");
     ck(cudaEventElapsedTime(&demod_ms, s->ev[1], s->ev[2]), "elapsed");
@@ -878,6 +907,7 @@ int32_t decode_impl(vhsdecode_gb300_session* s, const int16_t* rf, uint64_t n, u
     s->fields.clear();
     s->launches = 0;
     s->segments = 0;
+    s->stage_ms[0] = s->stage_ms[1] = s->stage_ms[2] = 0.0f;
     ck(cudaEventRecord(s->ev[0], cs), "event");
     if (s->fp32()) {
         // the copy stream must not start before earlier work on the session stream

@@ -185,26 +185,43 @@ struct Span {
     __device__ double at(int64_t i) const { return (double)d[i]; }
 };
 
+// Exact sample-vs-threshold tests in the stream's own type.  For a float
+// sample v and a double t: v < t <=> v < hi and v > t <=> v > lo, with hi the
+// smallest float >= t and lo the largest float <= t (NaN compares false either way).
+template <typename T>
+struct Thr {
+    T lo, hi;
+};
+__device__ __forceinline__ Thr<double> make_thr(double t, const double*) { return {t, t}; }
+__device__ __forceinline__ Thr<float> make_thr(double t, const float*) {
+    float f = __double2float_rn(t);
+    float lo = f, hi = f;
+    if ((double)f > t) lo = nextafterf(f, -INFINITY);
+    if ((double)f < t) hi = nextafterf(f, INFINITY);
+    return {lo, hi};
+}
+
 // first crossing of `target` at/after `start` within count+1 samples; NaN if none
 template <typename T>
 __device__ double zero_crossing(const Span<T>& s, int64_t start, double target, int edge, int count,
                                 int lane) {
-    if (edge == 0) edge = s.at(start) < target ? 1 : -1;
+    const Thr<T> th = make_thr(target, (const T*)nullptr);
+    if (edge == 0) edge = s.d[start] < th.hi ? 1 : -1;
     int64_t end = min(s.n, start + (int64_t)count + 1);
     int64_t len = end - start;
     for (int64_t base = 1; base < len; base += 32) {
         int64_t i = base + lane;
+        T b = i < len ? s.d[start + i] : (T)0;
+        T a = __shfl_up_sync(0xffffffffu, b, 1);
+        if (lane == 0) a = s.d[start + base - 1];
         bool hit = false;
-        if (i < len) {
-            double a = s.at(start + i - 1), b = s.at(start + i);
-            hit = edge == 1 ? (a < target && b >= target) : (a > target && b <= target);
-        }
+        if (i < len) hit = edge == 1 ? (a < th.hi && b >= th.hi) : (a > th.lo && b <= th.lo);
         unsigned m = __ballot_sync(0xffffffffu, hit);
         if (m) {
             int64_t x = start + base + (__ffs(m) - 1);
-            double a = s.at(x - 1) - target;
-            double b = s.at(x) - target;
-            double y = (b - a) != 0.0 ? -a / (-a + b) : 0.0;
+            double av = s.at(x - 1) - target;
+            double bv = s.at(x) - target;
+            double y = (bv - av) != 0.0 ? -av / (-av + bv) : 0.0;
             return (double)(x - 1) + y;
         }
     }
@@ -219,9 +236,9 @@ __device__ bool area_ok(const Span<T>& s, double crossing, int one_us, double en
     int64_t en = (int64_t)round_away(crossing + end_us * one_us);
     en = en < st ? st : (en > s.n ? s.n : en);
     if (en <= st) return false;
-    double mn = INFINITY, mx = -INFINITY;
+    T mn = (T)INFINITY, mx = (T)-INFINITY;
     for (int64_t i = st + lane; i < en; i += 32) {
-        double v = s.at(i);
+        T v = s.d[i];
         mn = fmin(mn, v);
         mx = fmax(mx, v);
     }
@@ -229,7 +246,17 @@ __device__ bool area_ok(const Span<T>& s, double crossing, int one_us, double en
         mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
         mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     }
-    return mn >= lo_hz && mx <= hi_hz;
+    return (double)mn >= lo_hz && (double)mx <= hi_hz;
+}
+
+// Lane partial sums: float streams accumulate as float pairs (TwoSum), which
+// is exact to about 2^-48 relative; the lanes combine in double.
+__device__ __forceinline__ void acc_add(double& acc, float& lo, double v) { acc += v; (void)lo; }
+__device__ __forceinline__ void acc_add(float& acc, float& lo, float v) {
+    float s = __fadd_rn(acc, v);
+    float bb = __fsub_rn(s, acc);
+    lo = __fadd_rn(lo, __fadd_rn(__fsub_rn(acc, __fsub_rn(s, bb)), __fsub_rn(v, bb)));
+    acc = s;
 }
 
 template <typename T>
@@ -239,8 +266,10 @@ __device__ bool mean_range(const Span<T>& s, double start, double end, double* m
     int64_t en = (int64_t)round_away(end);
     en = en < st ? st : (en > s.n ? s.n : en);
     if (en <= st) { *mean = 0.0; return false; }
-    double sum = 0.0;
-    for (int64_t i = st + lane; i < en; i += 32) sum += s.at(i);
+    T acc = (T)0;
+    float lo = 0.0f;
+    for (int64_t i = st + lane; i < en; i += 32) acc_add(acc, lo, s.d[i]);
+    double sum = (double)acc + (double)lo;
     for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
     *mean = sum / (double)(en - st);
     return true;
