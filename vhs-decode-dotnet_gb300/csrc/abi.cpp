@@ -135,6 +135,16 @@ struct DevBuf {
     ~DevBuf() { release(); }
 };
 
+// Identity of a captured pipeline graph: the graph bakes these in.
+struct PipeKey {
+    const void* rf = nullptr;
+    uint64_t n = 0;
+    bool host_input = false, demod_only = false;
+    bool operator==(const PipeKey& o) const {
+        return rf == o.rf && n == o.n && host_input == o.host_input && demod_only == o.demod_only;
+    }
+};
+
 struct FieldRec {
     FieldSync sync;
     int64_t span_start;
@@ -199,8 +209,11 @@ struct vhsdecode_gb300_session {
     cudaStream_t copy_stream = nullptr;  // RF copies ahead of the demod
     cudaStream_t d2h_stream = nullptr;   // pulse events back to the host behind the demod
     cudaStream_t alt_stream = nullptr;   // odd segments, so a segment's straggler blocks overlap the next one
-    cudaEvent_t alt_start = nullptr, alt_end = nullptr;
-    std::vector<cudaEvent_t> seg_done, seg_copied, seg_pulsed, seg_dem;
+    cudaStream_t cap_stream = nullptr;   // origin of the pipeline graph capture
+    cudaEvent_t alt_start = nullptr, alt_end = nullptr, copy_end = nullptr, d2h_end = nullptr;
+    cudaGraphExec_t pipe_exec = nullptr; // captured segment pipeline
+    PipeKey pipe_key{};
+    std::vector<cudaEvent_t> seg_done, seg_copied, seg_pulsed, seg_dem, seg_demod_end;
     int nseg_max = 0;
     int64_t seg_cap = 0;                 // pulse events per segment
     DevBuf<int64_t> seg_events, seg_total;
@@ -339,6 +352,8 @@ void session_init(vhsdecode_gb300_session* s, const vhsdecode_gb300_session_conf
         s->seg_copied.resize((size_t)s->nseg_max);
         s->seg_pulsed.resize((size_t)s->nseg_max);
         s->seg_dem.resize((size_t)s->nseg_max * 2);
+        s->seg_demod_end.resize((size_t)s->nseg_max);
+        for (auto& e : s->seg_demod_end) ck(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
         for (auto& e : s->seg_done) ck(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
         for (auto& e : s->seg_copied) ck(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
         for (auto& e : s->seg_pulsed) ck(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
@@ -348,6 +363,9 @@ void session_init(vhsdecode_gb300_session* s, const vhsdecode_gb300_session_conf
         ck(cudaStreamCreateWithFlags(&s->alt_stream, cudaStreamNonBlocking), "cudaStreamCreate");
         ck(cudaEventCreateWithFlags(&s->alt_start, cudaEventDisableTiming), "cudaEventCreate");
         ck(cudaEventCreateWithFlags(&s->alt_end, cudaEventDisableTiming), "cudaEventCreate");
+        ck(cudaEventCreateWithFlags(&s->copy_end, cudaEventDisableTiming), "cudaEventCreate");
+        ck(cudaEventCreateWithFlags(&s->d2h_end, cudaEventDisableTiming), "cudaEventCreate");
+        ck(cudaStreamCreateWithFlags(&s->cap_stream, cudaStreamNonBlocking), "cudaStreamCreate");
     } else {
         s->v64.alloc(stream_cap); s->s64.alloc(stream_cap); s->e64.alloc(stream_cap);
         std::vector<double2> vv(H), sv(H);
@@ -427,7 +445,7 @@ void session_init(vhsdecode_gb300_session* s, const vhsdecode_gb300_session_conf
 void session_free(vhsdecode_gb300_session* s) {
     if (s->plain_graph) cudaGraphExecDestroy(s->plain_graph);
     for (auto& ev : s->ev) if (ev) cudaEventDestroy(ev);
-    for (auto* v : {&s->seg_done, &s->seg_copied, &s->seg_pulsed, &s->seg_dem})
+    for (auto* v : {&s->seg_done, &s->seg_copied, &s->seg_pulsed, &s->seg_dem, &s->seg_demod_end})
         for (auto& ev : *v) if (ev) cudaEventDestroy(ev);
     if (s->h_events) cudaFreeHost(s->h_events);
     if (s->h_totals) cudaFreeHost(s->h_totals);
@@ -436,6 +454,10 @@ void session_free(vhsdecode_gb300_session* s) {
     if (s->alt_stream) cudaStreamDestroy(s->alt_stream);
     if (s->alt_start) cudaEventDestroy(s->alt_start);
     if (s->alt_end) cudaEventDestroy(s->alt_end);
+    if (s->copy_end) cudaEventDestroy(s->copy_end);
+    if (s->d2h_end) cudaEventDestroy(s->d2h_end);
+    if (s->pipe_exec) cudaGraphExecDestroy(s->pipe_exec);
+    if (s->cap_stream) cudaStreamDestroy(s->cap_stream);
     if (s->aux_stream) cudaStreamDestroy(s->aux_stream);
     if (s->field_stream) cudaStreamDestroy(s->field_stream);
     if (s->field_end) cudaEventDestroy(s->field_end);
@@ -704,18 +726,27 @@ void collect_field_results(vhsdecode_gb300_session* s, cudaStream_t fs) {
     ck(cudaMemcpyAsync(dcount.data(), s->drop_out_count.p, nf * sizeof(int), cudaMemcpyDeviceToHost, fs), "d2h");
     ck(cudaMemcpyAsync(dstat.data(), s->drop_status.p, nf * sizeof(int), cudaMemcpyDeviceToHost, fs), "d2h");
     ck(cudaStreamSynchronize(fs), "sync");
+    int maxc = 0;
+    for (int f = 0; f < nf; f++) {
+        if (dstat[f] != 0)
+            throw Failure(VHSDECODE_GB300_STATUS_DECODE_ERROR, "dropout event capacity exceeded");
+        maxc = std::max(maxc, std::min(dcount[f], s->drop_out_cap));
+    }
+    // one strided copy of the first maxc triplets of every field
+    std::vector<int32_t> drops((size_t)nf * maxc * 3);
+    if (maxc > 0) {
+        ck(cudaMemcpy2DAsync(drops.data(), (size_t)maxc * 3 * sizeof(int32_t), s->drop_out.p,
+                             (size_t)s->drop_out_cap * 3 * sizeof(int32_t), (size_t)maxc * 3 * sizeof(int32_t),
+                             (size_t)nf, cudaMemcpyDeviceToHost, fs), "d2h dropouts");
+        ck(cudaStreamSynchronize(fs), "sync");
+    }
     for (int f = 0; f < nf; f++) {
         FieldRec& r = s->fields[(size_t)f];
         r.refined.assign(refined.begin() + (size_t)f * s->lines, refined.begin() + (size_t)(f + 1) * s->lines);
-        if (dstat[f] != 0)
-            throw Failure(VHSDECODE_GB300_STATUS_DECODE_ERROR, "dropout event capacity exceeded");
         int c = std::min(dcount[f], s->drop_out_cap);
-        r.drop.resize((size_t)c * 3);
-        if (c > 0)
-            ck(cudaMemcpyAsync(r.drop.data(), s->drop_out.p + (size_t)f * s->drop_out_cap * 3,
-                               (size_t)c * 3 * sizeof(int32_t), cudaMemcpyDeviceToHost, fs), "d2h dropouts");
+        const int32_t* src = drops.data() + (size_t)f * maxc * 3;
+        r.drop.assign(src, src + (size_t)c * 3);
     }
-    ck(cudaStreamSynchronize(fs), "sync");
     if (s->stage_timing)
         std::fprintf(stderr, "[gb300 stage] fields=%d hsync=%.3f ms tbc=%.3f ms dropouts=%.3f ms "
                      "rescue_fetches=%d enqueue=%.3f ms segments=%u\n", nf, s->stage_ms[0], s->stage_ms[1],
@@ -741,6 +772,89 @@ std::vector<int64_t> segment_bounds(int64_t nblocks) {
 // host input the RF of each segment is copied on a separate stream ahead of
 // its demod.  Results are identical to a single pass: demod blocks are
 // independent and the ranged pulse scan carries its state across segments.
+// Queues the segment pipeline from `root`: RF copies on copy_stream, demod and
+// pulse scans alternating between root and alt_stream, event copies on
+// d2h_stream; every side stream joins back into root at the end.  When
+// `capturing`, the events the host waits on or times (seg_done, seg_dem) are
+// recorded as external graph nodes.
+void enqueue_pipeline(vhsdecode_gb300_session* s, const int16_t* rf, uint64_t n, bool host_input,
+                      bool demod_only, const std::vector<int64_t>& bounds, cudaStream_t root, bool capturing) {
+    auto rec = [&](cudaEvent_t e, cudaStream_t st, bool external) {
+        if (capturing && external) ck(cudaEventRecordWithFlags(e, st, cudaEventRecordExternal), "event");
+        else ck(cudaEventRecord(e, st), "event");
+    };
+    const int nseg = (int)bounds.size() - 1;
+    const int16_t* rf_dev = host_input ? s->rf.p : rf;
+    FastDemodParams p = fp32_params(s, rf_dev);
+    const double threshold = s->sp.ire_to_hz(s->sp.vsync_ire / 2.0);
+    ck(cudaMemsetAsync(s->repair.p, 0, sizeof(int), root), "memset");
+    rec(s->alt_start, root, false);
+    ck(cudaStreamWaitEvent(s->alt_stream, s->alt_start, 0), "wait");
+    ck(cudaStreamWaitEvent(s->copy_stream, s->alt_start, 0), "wait");
+    ck(cudaStreamWaitEvent(s->d2h_stream, s->alt_start, 0), "wait");
+    int64_t copied = 0;
+    for (int k = 0; k < nseg; k++) {
+        int64_t b0 = bounds[(size_t)k], b1 = bounds[(size_t)k + 1];
+        cudaStream_t ks = (k & 1) ? s->alt_stream : root;
+        if (host_input) {
+            int64_t c1 = std::min<int64_t>((int64_t)n, (b1 - 1) * kStride + kBlock);
+            if (c1 > copied) {
+                ck(cudaMemcpyAsync(s->rf.p + copied, rf + copied, (size_t)(c1 - copied) * sizeof(int16_t),
+                                   cudaMemcpyHostToDevice, s->copy_stream), "h2d rf");
+                copied = c1;
+            }
+            rec(s->seg_copied[(size_t)k], s->copy_stream, false);
+            ck(cudaStreamWaitEvent(ks, s->seg_copied[(size_t)k], 0), "wait");
+        }
+        p.first_block = b0;
+        p.nblocks = b1 - b0;
+        const size_t half = (size_t)(s->num_sms / 2) * kBlock;
+        p.scratch = s->scratch.p + (k & 1) * 2 * half;
+        p.scratch_raw = s->scratch_raw.p + (k & 1) * half;
+        rec(s->seg_dem[(size_t)(2 * k)], ks, true);
+        ck(launch_demod_fp32(p, s->num_sms / 2, ks), "demod fp32 launch");
+        rec(s->seg_dem[(size_t)(2 * k + 1)], ks, true);
+        rec(s->seg_demod_end[(size_t)k], ks, false);   // dependency edge (the timing record above is external)
+        if (!demod_only) {
+            // the scan needs the previous segment's samples (state before b0)
+            if (k > 0) ck(cudaStreamWaitEvent(ks, s->seg_demod_end[(size_t)k - 1], 0), "wait");
+            int64_t* ev = s->seg_events.p + (size_t)k * s->seg_cap;
+            int64_t* cnt = (k & 1) ? s->pc_counts_alt.p : s->pc_counts.p;
+            int64_t* off = (k & 1) ? s->pc_offsets_alt.p : s->pc_offsets.p;
+            ck(launch_pulse_events_range<float>(s->s32.p, b0 * kStride, b1 * kStride, threshold, cnt, off, ev,
+                                                s->seg_cap, s->seg_total.p + k, ks), "pulse launch");
+            rec(s->seg_pulsed[(size_t)k], ks, false);
+            ck(cudaStreamWaitEvent(s->d2h_stream, s->seg_pulsed[(size_t)k], 0), "wait");
+            ck(cudaMemcpyAsync(s->h_totals + k, s->seg_total.p + k, sizeof(int64_t), cudaMemcpyDeviceToHost,
+                               s->d2h_stream), "d2h");
+            ck(cudaMemcpyAsync(s->h_events + (size_t)k * s->seg_cap, ev, (size_t)s->seg_cap * sizeof(int64_t),
+                               cudaMemcpyDeviceToHost, s->d2h_stream), "d2h events");
+            rec(s->seg_done[(size_t)k], s->d2h_stream, true);
+        }
+    }
+    // join the side streams back into root
+    for (cudaStream_t side : {s->alt_stream, s->copy_stream, s->d2h_stream}) {
+        cudaEvent_t j = side == s->alt_stream ? s->alt_end : (side == s->copy_stream ? s->copy_end : s->d2h_end);
+        rec(j, side, false);
+        ck(cudaStreamWaitEvent(root, j, 0), "wait");
+    }
+}
+
+// Kernels the pipeline queues for `bounds` (demod + pulse scans).
+uint32_t pipeline_launches(const std::vector<int64_t>& bounds, bool demod_only) {
+    uint32_t nseg = (uint32_t)(bounds.size() - 1);
+    return nseg * (1u + (demod_only ? 0u : (uint32_t)kPulseKernels));
+}
+
+// FP32 decode, pipelined: the capture is demodulated in segments; after each
+// segment the device writes that segment's pulse events and copies them to
+// pinned host memory, so the host control plane analyses the fields of
+// finished segments while later segments are still being demodulated.  With
+// host input the RF of each segment is copied on a separate stream ahead of
+// its demod.  Results are identical to a single pass: demod blocks are
+// independent and the ranged pulse scan carries its state across segments.
+// With device input or pinned host input the queued work is captured once as
+// a CUDA graph (keyed by the input pointer, length and mode) and replayed.
 void decode_fp32_pipelined(vhsdecode_gb300_session* s, const int16_t* rf, uint64_t n, bool host_input,
                            bool demod_only, uint32_t max_fields, uint32_t& stop, double& host_ms,
                            float& demod_ms, const std::atomic<bool>* cancel) {
@@ -753,61 +867,40 @@ void decode_fp32_pipelined(vhsdecode_gb300_session* s, const int16_t* rf, uint64
     int nseg = (int)bounds.size() - 1;
     s->segments = (uint32_t)nseg;
     if (nseg > s->nseg_max) throw Failure(VHSDECODE_GB300_STATUS_INTERNAL_ERROR, "segment table too small");
-    const int16_t* rf_dev = host_input ? s->rf.p : rf;
-    FastDemodParams p = fp32_params(s, rf_dev);
-    ck(cudaMemsetAsync(s->repair.p, 0, sizeof(int), cs), "memset");
-    const double threshold = s->sp.ire_to_hz(s->sp.vsync_ire / 2.0);
-    // even segments run on the session stream, odd ones on alt_stream; the
-    // pulse scan of segment k reads the sync reference up to its end and the
-    // state before it, so it waits for the demod of segments k-1 and k
-    ck(cudaEventRecord(s->alt_start, cs), "event");
-    ck(cudaStreamWaitEvent(s->alt_stream, s->alt_start, 0), "wait");
-    int64_t copied = 0;
     auto tq0 = std::chrono::steady_clock::now();
-    for (int k = 0; k < nseg; k++) {
-        int64_t b0 = bounds[(size_t)k], b1 = bounds[(size_t)k + 1];
-        cudaStream_t ks = (k & 1) ? s->alt_stream : cs;
-        if (host_input) {
-            int64_t c1 = std::min<int64_t>((int64_t)n, (b1 - 1) * kStride + kBlock);
-            if (c1 > copied) {
-                ck(cudaMemcpyAsync(s->rf.p + copied, rf + copied, (size_t)(c1 - copied) * sizeof(int16_t),
-                                   cudaMemcpyHostToDevice, s->copy_stream), "h2d rf");
-                copied = c1;
-            }
-            ck(cudaEventRecord(s->seg_copied[(size_t)k], s->copy_stream), "event");
-            ck(cudaStreamWaitEvent(ks, s->seg_copied[(size_t)k], 0), "wait");
-        }
-        p.first_block = b0;
-        p.nblocks = b1 - b0;
-        const size_t half = (size_t)(s->num_sms / 2) * kBlock;
-        p.scratch = s->scratch.p + (k & 1) * 2 * half;
-        p.scratch_raw = s->scratch_raw.p + (k & 1) * half;
-        ck(cudaEventRecord(s->seg_dem[(size_t)(2 * k)], ks), "event");
-        ck(launch_demod_fp32(p, s->num_sms / 2, ks), "demod fp32 launch");
-        ck(cudaEventRecord(s->seg_dem[(size_t)(2 * k + 1)], ks), "event");
-        s->launches += 1;
-        if (!demod_only) {
-            // the scan needs the previous segment's samples (state before b0)
-            if (k > 0) ck(cudaStreamWaitEvent(ks, s->seg_dem[(size_t)(2 * k - 1)], 0), "wait");
-            int64_t* ev = s->seg_events.p + (size_t)k * s->seg_cap;
-            int64_t* cnt = (k & 1) ? s->pc_counts_alt.p : s->pc_counts.p;
-            int64_t* off = (k & 1) ? s->pc_offsets_alt.p : s->pc_offsets.p;
-            ck(launch_pulse_events_range<float>(s->s32.p, b0 * kStride, b1 * kStride, threshold, cnt, off, ev,
-                                                s->seg_cap, s->seg_total.p + k, ks),
-               "pulse launch");
-            s->launches += kPulseKernels;
-            ck(cudaEventRecord(s->seg_pulsed[(size_t)k], ks), "event");
-            ck(cudaStreamWaitEvent(s->d2h_stream, s->seg_pulsed[(size_t)k], 0), "wait");
-            ck(cudaMemcpyAsync(s->h_totals + k, s->seg_total.p + k, sizeof(int64_t), cudaMemcpyDeviceToHost,
-                               s->d2h_stream), "d2h");
-            ck(cudaMemcpyAsync(s->h_events + (size_t)k * s->seg_cap, ev, (size_t)s->seg_cap * sizeof(int64_t),
-                               cudaMemcpyDeviceToHost, s->d2h_stream), "d2h events");
-            ck(cudaEventRecord(s->seg_done[(size_t)k], s->d2h_stream), "event");
-        }
+    bool graphable = !host_input;
+    if (host_input && n > 0) {
+        cudaPointerAttributes attr{};
+        graphable = cudaPointerGetAttributes(&attr, rf) == cudaSuccess && attr.type == cudaMemoryTypeHost;
+        cudaGetLastError();
     }
-    // the session stream continues only after the odd segments
-    ck(cudaEventRecord(s->alt_end, s->alt_stream), "event");
-    ck(cudaStreamWaitEvent(cs, s->alt_end, 0), "wait");
+    if (graphable && nseg > 0) {
+        PipeKey key{rf, n, host_input, demod_only};
+        if (!s->pipe_exec || !(s->pipe_key == key)) {
+            if (s->pipe_exec) { cudaGraphExecDestroy(s->pipe_exec); s->pipe_exec = nullptr; }
+            FastDemodParams p0 = fp32_params(s, s->rf.p);
+            ck(launch_demod_fp32(p0, s->num_sms / 2, s->cap_stream), "demod attribute");  // nblocks 0: sets attributes only
+            ck(cudaStreamBeginCapture(s->cap_stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+            cudaGraph_t g = nullptr;
+            try {
+                enqueue_pipeline(s, rf, n, host_input, demod_only, bounds, s->cap_stream, true);
+            } catch (...) {
+                cudaStreamEndCapture(s->cap_stream, &g);
+                if (g) cudaGraphDestroy(g);
+                cudaGetLastError();
+                throw;
+            }
+            ck(cudaStreamEndCapture(s->cap_stream, &g), "end capture");
+            cudaError_t ie = cudaGraphInstantiate(&s->pipe_exec, g, 0);
+            cudaGraphDestroy(g);
+            ck(ie, "graph instantiate");
+            s->pipe_key = key;
+        }
+        ck(cudaGraphLaunch(s->pipe_exec, cs), "graph launch");
+    } else {
+        enqueue_pipeline(s, rf, n, host_input, demod_only, bounds, cs, false);
+    }
+    s->launches += pipeline_launches(bounds, demod_only);
     s->enqueue_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tq0).count();
     if (!demod_only && nblocks > 0) {
         auto t0 = std::chrono::steady_clock::now();
@@ -910,8 +1003,6 @@ int32_t decode_impl(vhsdecode_gb300_session* s, const int16_t* rf, uint64_t n, u
     s->stage_ms[0] = s->stage_ms[1] = s->stage_ms[2] = 0.0f;
     ck(cudaEventRecord(s->ev[0], cs), "event");
     if (s->fp32()) {
-        // the copy stream must not start before earlier work on the session stream
-        if (host_input) ck(cudaStreamWaitEvent(s->copy_stream, s->ev[0], 0), "wait");
         decode_fp32_pipelined(s, rf, n, host_input, demod_only, max_fields, stop, host_ms, demod_ms, cancel);
     } else {
         const int16_t* rf_dev = rf;

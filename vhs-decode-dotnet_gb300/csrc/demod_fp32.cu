@@ -29,6 +29,7 @@
 // Shared memory per CTA: 16384 complex floats (padded against bank
 // conflicts) plus twiddle tables; one CTA per SM.
 #include <cooperative_groups.h>
+#include <atomic>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -703,11 +704,20 @@ namespace vhsd {
 
 size_t fp32_smem_bytes() { return sizeof(fp32::Shared); }
 
+// The shared-memory attribute is set once per device (the first call on a
+// device must not be inside a stream capture).
 cudaError_t launch_demod_fp32(const FastDemodParams& p, int num_clusters, cudaStream_t stream) {
+    static std::atomic<uint64_t> attr_set{0};
     size_t smem = sizeof(fp32::Shared);
-    cudaError_t e = cudaFuncSetAttribute(vhsd_demod_fp32_kernel,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
+    const uint64_t bit = dev < 64 ? (uint64_t)1 << dev : 0;
+    if (!bit || !(attr_set.load() & bit)) {
+        e = cudaFuncSetAttribute(vhsd_demod_fp32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        attr_set.fetch_or(bit);
+    }
     if (p.nblocks <= 0) return cudaSuccess;
     int clusters = num_clusters;
     if (clusters > p.nblocks) clusters = (int)p.nblocks;
