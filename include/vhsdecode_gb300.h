@@ -154,7 +154,7 @@ typedef struct vhsdecode_gb300_decode_result_v1 {
     uint64_t blocks;            /* 32768-sample blocks demodulated */
     uint64_t stream_samples;    /* stitched stream length = blocks * 30720 */
     uint32_t repaired_blocks;   /* blocks that took the diff-demod spike repair */
-    uint32_t stop_reason;       /* 0 end of data, 1 max fields, 2 field error */
+    uint32_t stop_reason;       /* 0 end of data, 1 max fields (failed fields are skipped past) */
     double device_ms;           /* stream time of the whole decode */
     double demod_ms;            /* block demodulator kernel time */
     double field_ms;            /* pulses + hsync + TBC + dropout kernels */
@@ -282,6 +282,71 @@ VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_vhs_demod(
 /* Device polynomial atan2 (the FM demodulator's angle) for n float pairs. */
 VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_vhs_angles(
     const float* real, const float* imaginary, uint64_t n, float* angles);
+
+/* ---------------------------------------------------------------- serving
+ * Window server: continuous batching of decode windows from many client
+ * streams on one GPU.  Replaces the single-window preview context of
+ * vhsdecode_cuda_fast_preview_create / _decode_window (:158-171), which
+ * serialises windows behind a mutex: here `workers` windows decode at once,
+ * each on a device slot of its format, admitted while the slots' device
+ * memory stays inside the budget.  Windows of one stream_id decode in
+ * submission order and carry the stream's sync history (field parity, hsync
+ * history, next-field continuation) unless `seek` is set.  `samples` and
+ * `tbc_out` must stay valid until the window's result has been returned by
+ * vhsdecode_gb300_server_wait. */
+typedef struct vhsdecode_gb300_server vhsdecode_gb300_server;
+
+typedef struct vhsdecode_gb300_server_config_v1 {
+    uint32_t struct_size;
+    int32_t device_id;
+    uint32_t workers;               /* windows decoded at once (0 = 4) */
+    uint32_t reserved;
+    uint64_t max_window_samples;    /* longest window accepted; sizes every slot */
+    uint64_t memory_budget_bytes;   /* device memory for slots (0 = 80 % of free memory) */
+} vhsdecode_gb300_server_config_v1;
+
+typedef struct vhsdecode_gb300_window_v1 {
+    uint32_t struct_size;
+    uint32_t stream_id;             /* client stream; its windows decode in order */
+    uint32_t profile;               /* vhsdecode_gb300_profile */
+    uint32_t tape_speed;
+    double sample_rate_mhz;
+    const int16_t* samples;         /* host RF samples of the window */
+    uint64_t sample_count;
+    uint64_t source_offset;         /* stream position of samples[0] */
+    uint32_t seek;                  /* 1: discontinuity, start without the stream's history */
+    uint32_t max_fields;            /* 0 = as many as fit */
+    uint16_t* tbc_out;              /* host destination for the fields' TBC, or NULL */
+    uint64_t tbc_capacity;          /* uint16 elements at tbc_out */
+} vhsdecode_gb300_window_v1;
+
+typedef struct vhsdecode_gb300_window_result_v1 {
+    uint32_t struct_size;
+    int32_t status;                 /* vhsdecode_gb300_status of this window */
+    uint32_t stream_id;
+    uint32_t fields;
+    uint32_t first_field_is_first;  /* parity of the window's first field */
+    uint32_t continued;             /* 1 when the stream's sync history was used */
+    uint64_t ticket;
+    uint64_t sample_count;
+    uint64_t next_source_offset;    /* a window starting at or before this continues the stream;
+                                       starting exactly here (on the stream's 983040-sample grid)
+                                       reproduces a whole-stream decode bit for bit */
+    double queue_ms;                /* submit to start of decode */
+    double decode_ms;
+    double latency_ms;              /* submit to result */
+} vhsdecode_gb300_window_result_v1;
+
+VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_server_create(
+    const vhsdecode_gb300_server_config_v1* config, vhsdecode_gb300_server** server);
+/* Queues a window; returns at once with its ticket. */
+VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_server_submit(
+    vhsdecode_gb300_server* server, const vhsdecode_gb300_window_v1* window, uint64_t* ticket);
+/* Blocks until the window is done; returns its status (result->status). */
+VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_server_wait(
+    vhsdecode_gb300_server* server, uint64_t ticket, vhsdecode_gb300_window_result_v1* result);
+/* Finishes the windows being decoded, cancels queued ones, frees the slots. */
+VHSDECODE_GB300_API void VHSDECODE_GB300_CALL vhsdecode_gb300_server_destroy(vhsdecode_gb300_server* server);
 
 /* Sync-pulse edge events over `length` float samples already on the device,
  * with no device memory allocated by the call.  No counterpart in the

@@ -19,7 +19,15 @@ from .filters import FilterSet
 
 
 class FieldError(Exception):
-    pass
+    """A field that could not be decoded, with the reference's recovery step
+    (BuildRecoveryException / ThrowIfInsufficientFieldData,
+    Core/Decode/TbcFieldDecodePipeline.cs:1150-1166, 5636-5650, 5936-6007; the engine
+    loop Core/Decode/TbcFieldSequenceDecodeEngine.cs:804-847): the engine moves its
+    read position on by ``offset`` samples and tries again."""
+
+    def __init__(self, msg, offset):
+        super().__init__(msg)
+        self.offset = int(offset)   # C# (long) cast: truncation
 
 
 def read_length(sp):
@@ -44,6 +52,7 @@ class FieldState:
     def __init__(self):
         self.prev_first = None
         self.has_prev_hsync = False
+        self.pulses_seen = False   # _vhsPulseSearchInitialized
 
 
 def _single_estimate(fe, le, has_prev):
@@ -73,7 +82,9 @@ def decode_field(sp, fmt, video, vlp, env, state, want_tbc=True):
     threshold = sp.ire_to_hz(sp.vsync_ire / 2.0)
     raw = sync.find_raw_pulses(sp, vlp, threshold)
     if not raw:
-        raise FieldError("no sync pulses")
+        # NoFirstHSync once pulses have been seen, else NoSyncPulses
+        raise FieldError("no sync pulses", sp.nominal * 100.0 if state.pulses_seen else sp.fs / 10.0)
+    state.pulses_seen = True
     timing = sync.estimate_timing(sp, raw)
     classified = sync.classify_pulses(sp, raw, timing)
     refined, _ = sync.refine_pulses(sp, raw, timing, vlp, 10.0 * sp.hz_ire)
@@ -83,19 +94,19 @@ def decode_field(sp, fmt, video, vlp, env, state, want_tbc=True):
     field_lines = sp.field_lines()[0 if first_field else 1]
     g1 = sync.find_first_group(refined, None, 9)
     if g1 is None:
-        raise FieldError("no vblank")
+        raise FieldError("no vblank", sp.nominal * 100.0)
     g2 = sync.find_first_group(refined, g1["eq1"] + (field_lines - 2.0) * mll, 9)
     fe, le, comb = sync.estimate_line0_from_groups(sp, classified, g1, g2, mll, first_field, field_lines)
     pick = comb if comb is not None else _single_estimate(fe, le, state.has_prev_hsync)
     if pick is None:
-        raise FieldError("no line 0")
+        raise FieldError("no line 0", sp.nominal * 100.0)
     line0 = pick["line0"]
     fh = pick["first_hsync"]
     state.has_prev_hsync = True
     processed = sp.output_lines + 10
     last_line = ((len(video) - line0) / mll) - 1.0
     if last_line < processed:
-        raise FieldError("insufficient data")
+        raise FieldError("insufficient data", max(line0 - mll * 20.0, sp.nominal))
     fh_line = sync.first_hsync_line(sp, first_field)
     locs, filled = sync.build_upstream_line_locations(refined, float(math.trunc(fh)), int(fh_line),
                                                       mll, processed)
@@ -191,8 +202,9 @@ def decode_capture(rf, fmt, fs=40e6, max_fields=None, want_tbc=True, channels=No
         try:
             f = decode_field(sp, fmt, video[sl], vlp[sl], env[sl], state, want_tbc)
         except FieldError as exc:
-            fields.append({"error": str(exc), "span_start": s0})
-            break
+            fields.append({"error": str(exc), "span_start": s0, "recovery": exc.offset})
+            intended = max(0, intended + exc.offset)
+            continue
         f["span_start"] = s0
         fields.append(f)
         intended = s0 + max(1, int(sync.round_away(f["next_offset"])))

@@ -34,7 +34,9 @@ def test_struct_sizes_match_c_layout(lib, tmp_path):
     from vhsd_gb300 import native
     structs = {"runtime_info_v1": native.RuntimeInfo, "config_v1": native.RunConfig,
                "result_v1": native.RunResult, "session_config_v1": native.SessionConfig,
-               "decode_result_v1": native.DecodeResult, "field_info_v1": native.FieldInfo}
+               "decode_result_v1": native.DecodeResult, "field_info_v1": native.FieldInfo,
+               "server_config_v1": native.ServerConfig, "window_v1": native.Window,
+               "window_result_v1": native.WindowResult}
     src = tmp_path / "sizes.c"
     src.write_text('#include <stdio.h>\n#include "vhsdecode_gb300.h"\nint main(void){\n' + "".join(
         'printf("%%zu\\n", sizeof(vhsdecode_gb300_%s));\n' % k for k in structs) + "return 0;}\n")
@@ -136,3 +138,14 @@ def test_field_sync_rejects_empty_pulses(lib):
     state = np.array([-1, 0], np.int32)
     with pytest.raises(native.NativeError):
         native.field_sync(native.PROFILE_PAL, [], 1000000, state)
+
+
+@pytest.mark.skipif(HAVE_GPU, reason="checks the no-GPU status")
+def test_server_create_without_gpu_reports_unavailable(lib):
+    from vhsd_gb300 import native
+    cfg = native.ServerConfig(ctypes.sizeof(native.ServerConfig), 0, 2, 0, 1 << 22, 0)
+    h = ctypes.c_void_p()
+    st = lib.vhsdecode_gb300_server_create(ctypes.byref(cfg), ctypes.byref(h))
+    assert st == native.STATUS_CUDA_UNAVAILABLE
+    bad = native.ServerConfig(8, 0, 2, 0, 1 << 22, 0)
+    assert lib.vhsdecode_gb300_server_create(ctypes.byref(bad), ctypes.byref(h)) == native.STATUS_INVALID_ARGUMENT

@@ -195,3 +195,28 @@ def test_pinned_input_graph_replay_matches(gpu, ntsc_capture):
             assert s.tbc().tobytes() == want.tobytes()
             assert all(np.array_equal(s.lines(i), locs[i]) for i in range(r.fields))
         assert r.segments >= 1 and r.kernel_launches > 0
+
+
+def test_field_recovery_matches_oracle(gpu, pal_capture):
+    # a capture that starts mid-field: the first attempt fails and the engine
+    # moves on by the reference's recovery step, then decodes the next fields
+    from oracle import field, formats
+    from vhsd_gb300 import native
+    rf, _ = pal_capture
+    x = np.ascontiguousarray(rf[1115360:])
+    fields, _ = field.decode_capture(x, formats.get("PAL"))
+    assert any("error" in f for f in fields)
+    good = [f for f in fields if "error" not in f]
+    assert good
+    with native.Session(native.PROFILE_PAL, len(x)) as s:
+        r = s.decode(x)
+        assert r.fields == len(good)
+        tb = s.tbc()
+        for i, f in enumerate(good):
+            info = s.field(i)
+            assert info.span_start == f["span_start"]
+            assert bool(info.is_first_field) == f["first_field"]
+            assert np.max(np.abs(s.lines(i) - f["locs"])) < LINE_TOL
+            d = np.abs(tb[i].astype(np.int64).ravel() - f["tbc"].astype(np.int64))
+            assert np.mean(d <= 1) >= LSB_FRACTION
+            assert s.dropouts(i) == [tuple(y) for y in f["dropouts"]]

@@ -28,6 +28,7 @@
 #include "filters.hpp"
 #include "formats.hpp"
 #include "kernels.h"
+#include "session.hpp"
 
 namespace vhsd {
 template <typename T>
@@ -35,47 +36,15 @@ cudaError_t launch_tbc_pw(const T*, int64_t, const TbcParams&, const double*, cu
 }
 
 using namespace vhsd;
+using namespace vhsd::detail;
+
+namespace vhsd {
+namespace detail {
+thread_local std::string g_last_error;
+}  // namespace detail
+}  // namespace vhsd
 
 namespace {
-
-thread_local std::string g_last_error;
-
-struct Failure : std::runtime_error {
-    int32_t status;
-    Failure(int32_t s, const std::string& m) : std::runtime_error(m), status(s) {}
-};
-
-int32_t fail(int32_t status, const std::string& msg) {
-    g_last_error = msg;
-    return status;
-}
-
-void ck(cudaError_t e, const char* what) {
-    if (e != cudaSuccess) {
-        int32_t st = (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver ||
-                      e == cudaErrorInitializationError)
-                         ? VHSDECODE_GB300_STATUS_CUDA_UNAVAILABLE
-                         : VHSDECODE_GB300_STATUS_INTERNAL_ERROR;
-        throw Failure(st, std::string(what) + ": " + cudaGetErrorString(e));
-    }
-}
-
-template <typename F>
-int32_t guard(F&& f) {
-    try {
-        int32_t r = f();
-        if (r == VHSDECODE_GB300_STATUS_OK) g_last_error.clear();
-        return r;
-    } catch (const Failure& e) {
-        return fail(e.status, e.what());
-    } catch (const std::bad_alloc&) {
-        return fail(VHSDECODE_GB300_STATUS_INTERNAL_ERROR, "host allocation failed");
-    } catch (const std::exception& e) {
-        return fail(VHSDECODE_GB300_STATUS_INTERNAL_ERROR, e.what());
-    } catch (...) {
-        return fail(VHSDECODE_GB300_STATUS_INTERNAL_ERROR, "unknown native failure");
-    }
-}
 
 bool format_for(uint32_t profile, uint32_t speed, FormatParams& f) {
     if (speed != VHSDECODE_GB300_TAPE_SPEED_SP) return false;
@@ -117,139 +86,10 @@ std::vector<float> build_sinc_lut() {
     return lut;
 }
 
-template <typename T>
-struct DevBuf {
-    T* p = nullptr;
-    size_t n = 0;
-    void alloc(size_t count) {
-        release();
-        if (count == 0) return;
-        ck(cudaMalloc(&p, count * sizeof(T)), "cudaMalloc");
-        n = count;
-    }
-    void release() {
-        if (p) cudaFree(p);
-        p = nullptr;
-        n = 0;
-    }
-    ~DevBuf() { release(); }
-};
-
-// Identity of a captured pipeline graph: the graph bakes these in.
-struct PipeKey {
-    const void* rf = nullptr;
-    uint64_t n = 0;
-    bool host_input = false, demod_only = false;
-    bool operator==(const PipeKey& o) const {
-        return rf == o.rf && n == o.n && host_input == o.host_input && demod_only == o.demod_only;
-    }
-};
-
-struct FieldRec {
-    FieldSync sync;
-    int64_t span_start;
-    int64_t span_len;
-    std::vector<double> refined;
-    std::vector<int32_t> drop;  // triplets
-};
-
-constexpr int64_t kFirstSegBlocks = 40;   // about 1.2 M stream samples
-constexpr int64_t kSegBlocks = 128;        // about 3.9 M stream samples
-
-inline int64_t block_count(uint64_t n) {
-    return n < (uint64_t)kBlock ? 0 : (int64_t)((n - kBlock) / kStride + 1);
-}
-
 }  // namespace
 
-struct vhsdecode_gb300_session {
-    FormatParams fmt;
-    SyncParams sp;
-    FilterSpectra filt;
-    double fs = 40e6;
-    int precision = 0;
-    int device = 0;
-    uint64_t max_samples = 0;
-    int64_t max_blocks = 0;
-    int max_fields = 0;
-    int lines = 0;       // processed lines per field
-    int out_lines = 0;
-    int outlen = 0;
-    int num_sms = 0;
-    cudaStream_t own_stream = nullptr;
-    cudaStream_t stream = nullptr;
-    cudaEvent_t ev[6] = {};
-    // device data
-    DevBuf<int16_t> rf;
-    DevBuf<float> v32, s32, e32;
-    DevBuf<double> v64, s64, e64;
-    DevBuf<float> rfv32;
-    DevBuf<float2> vid32, syn32, tw_hi, tw_lo;
-    DevBuf<double> rfv64;
-    DevBuf<double2> vid64, syn64;
-    DevBuf<float2> scratch;
-    DevBuf<float> scratch_raw;
-    DevBuf<int> repair;
-    DevBuf<double2> pwork;
-    DevBuf<double> pdwork;
-    DevBuf<float> pfwork;
-    DevBuf<int> pflag;
-    DevBuf<unsigned> pmask;
-    DevBuf<int64_t> pblk;
-    cudaGraphExec_t plain_graph = nullptr;
-    const int16_t* graph_rf = nullptr;   // input pointer baked into plain_graph
-    DevBuf<int64_t> pc_counts, pc_offsets, pc_events, pc_total;
-    DevBuf<int64_t> pc_counts_alt, pc_offsets_alt;   // scan scratch of odd segments
-    int64_t pc_capacity = 0;
-    DevBuf<double> locs_in, locs_out;
-    DevBuf<uint8_t> fill_in, fill_out;
-    DevBuf<unsigned char> hsync_work;
-    // pipelined FP32 decode: per-segment pulse events, pinned host copies
-    cudaStream_t aux_stream = nullptr;   // rescue fetches while the session stream is busy
-    cudaStream_t copy_stream = nullptr;  // RF copies ahead of the demod
-    cudaStream_t d2h_stream = nullptr;   // pulse events back to the host behind the demod
-    cudaStream_t alt_stream = nullptr;   // odd segments, so a segment's straggler blocks overlap the next one
-    cudaStream_t cap_stream = nullptr;   // origin of the pipeline graph capture
-    cudaEvent_t alt_start = nullptr, alt_end = nullptr, copy_end = nullptr, d2h_end = nullptr;
-    cudaGraphExec_t pipe_exec = nullptr; // captured segment pipeline
-    PipeKey pipe_key{};
-    std::vector<cudaEvent_t> seg_done, seg_copied, seg_pulsed, seg_dem, seg_demod_end;
-    int nseg_max = 0;
-    int64_t seg_cap = 0;                 // pulse events per segment
-    DevBuf<int64_t> seg_events, seg_total;
-    int64_t* h_events = nullptr;         // pinned [nseg_max * seg_cap]
-    int64_t* h_totals = nullptr;         // pinned [nseg_max]
-    int rescue_fetches = 0;
-    uint32_t launches = 0;               // kernels started by the current decode
-    double enqueue_ms = 0.0;             // host time to queue the pipelined demod
-    cudaStream_t field_stream = nullptr; // field batches, concurrent with later demod segments
-    cudaEvent_t field_end = nullptr;
-    bool stage_timing = false;           // VHSD_STAGE_TIMING set: per-stage kernel times to stderr
-    cudaEvent_t stage_ev[4] = {};
-    float stage_ms[3] = {};
-    uint32_t segments = 0;
-    DevBuf<int> hsync_misses;
-    DevBuf<int64_t> span_start_d, span_len_d;
-    DevBuf<int> first_line_d, start_line_d, end_line_d, line_off_d;
-    DevBuf<float> lut, lut_pair;
-    DevBuf<float2> pw_ff;
-    DevBuf<double> pw, level_work;
-    DevBuf<uint16_t> tbc;
-    DevBuf<int64_t> drop_range, drop_events;
-    DevBuf<float> drop_mean, drop_partial;
-    DevBuf<int> drop_counts, drop_out_count, drop_status;
-    DevBuf<int32_t> drop_out;
-    int drop_cap = 1024, drop_out_cap = 4096;
-    int64_t span_len = 0;
-    // host results
-    std::vector<FieldRec> fields;
-    int64_t last_blocks = 0;
-    int last_repairs = 0;
-
-    bool fp32() const { return precision == VHSDECODE_GB300_PRECISION_FP32_FUSED; }
-};
-
-namespace {
+namespace vhsd {
+namespace detail {
 
 int64_t read_length(const SyncParams& sp) {
     int64_t line = (int64_t)std::nearbyint(sp.line_period_us * sp.mhz);
@@ -270,8 +110,8 @@ void session_init(vhsdecode_gb300_session* s, const vhsdecode_gb300_session_conf
     if (!format_for(c.profile, c.tape_speed, s->fmt))
         throw Failure(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT,
                       "unsupported profile / tape speed (PAL or NTSC, SP)");
-    if (!(c.sample_rate_mhz > 0.0) || std::fabs(c.sample_rate_mhz - 40.0) > 1e-9)
-        throw Failure(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "sample_rate_mhz must be 40");
+    if (!(c.sample_rate_mhz >= 10.0 && c.sample_rate_mhz <= 100.0))
+        throw Failure(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "sample_rate_mhz must be within 10..100");
     if (c.precision > 1) throw Failure(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "unknown precision");
     s->fs = c.sample_rate_mhz * 1e6;
     s->precision = (int)c.precision;
@@ -555,15 +395,16 @@ struct EventFeed {
 template <typename T>
 void host_field_loop(vhsdecode_gb300_session* s, const T* sync, int64_t stream_len, uint32_t max_fields,
                      EventFeed& feed, uint32_t& stop_reason, const std::atomic<bool>* cancel,
-                     const std::function<void(int)>& on_field = nullptr) {
+                     DecodeCarry* carry) {
     const SyncParams& sp = s->sp;
     int64_t read_len = read_length(sp);
     int64_t min_len = std::max<int64_t>(0, (int64_t)std::ceil(sp.usec(sp.eq_us) / 8.0));
     int64_t max_len = std::max<int64_t>(1, (int64_t)(sp.nominal * 5.0));
-    FieldState st;
-    int64_t intended = 0;
+    FieldState st = carry ? carry->state : FieldState{};
+    int64_t intended = carry ? std::max<int64_t>(0, carry->start) : 0;
     s->fields.clear();
     s->rescue_fetches = 0;
+    s->recoveries = 0;
     stop_reason = 0;
     std::vector<T> tmp;
     while (true) {
@@ -588,10 +429,18 @@ void host_field_loop(vhsdecode_gb300_session* s, const T* sync, int64_t stream_l
         rec.sync = analyse_field(sp, raw, slen, st, fetch);
         rec.span_start = s0;
         rec.span_len = slen;
-        if (!rec.sync.ok) { stop_reason = 2; break; }
+        if (!rec.sync.ok) {
+            // the reference engine moves on and tries again (TbcFieldSequenceDecodeEngine.cs:804-847)
+            intended = std::max<int64_t>(0, intended + rec.sync.recover_offset);
+            s->recoveries++;
+            continue;
+        }
         intended = s0 + std::max<int64_t>(1, (int64_t)round_away(rec.sync.next_offset));
         s->fields.push_back(std::move(rec));
-        if (on_field) on_field((int)s->fields.size());
+    }
+    if (carry) {
+        carry->state = st;
+        carry->next = intended;
     }
 }
 
@@ -857,7 +706,7 @@ uint32_t pipeline_launches(const std::vector<int64_t>& bounds, bool demod_only) 
 // a CUDA graph (keyed by the input pointer, length and mode) and replayed.
 void decode_fp32_pipelined(vhsdecode_gb300_session* s, const int16_t* rf, uint64_t n, bool host_input,
                            bool demod_only, uint32_t max_fields, uint32_t& stop, double& host_ms,
-                           float& demod_ms, const std::atomic<bool>* cancel) {
+                           float& demod_ms, const std::atomic<bool>* cancel, DecodeCarry* carry) {
     cudaStream_t cs = s->stream;
     int64_t nblocks = block_count(n);
     int64_t stream_len = nblocks * kStride;
@@ -874,6 +723,7 @@ void decode_fp32_pipelined(vhsdecode_gb300_session* s, const int16_t* rf, uint64
         graphable = cudaPointerGetAttributes(&attr, rf) == cudaSuccess && attr.type == cudaMemoryTypeHost;
         cudaGetLastError();
     }
+    if (carry && carry->no_graph) graphable = false;
     if (graphable && nseg > 0) {
         PipeKey key{rf, n, host_input, demod_only};
         if (!s->pipe_exec || !(s->pipe_key == key)) {
@@ -921,7 +771,7 @@ void decode_fp32_pipelined(vhsdecode_gb300_session* s, const int16_t* rf, uint64
         };
         // The field kernels are latency bound per field (the hsync chain walks
         // a field's lines in order), so they run as one batch over all fields.
-        host_field_loop<float>(s, s->s32.p, stream_len, max_fields, feed, stop, cancel);
+        host_field_loop<float>(s, s->s32.p, stream_len, max_fields, feed, stop, cancel, carry);
         host_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
         ck(cudaEventRecord(s->ev[2], cs), "event");
         launch_field_batch<float>(s, 0, (int)s->fields.size(), s->v32.p, s->s32.p, s->e32.p,
@@ -946,7 +796,7 @@ void decode_fp32_pipelined(vhsdecode_gb300_session* s, const int16_t* rf, uint64
 // whole-stream pulse scan, the control plane and the field stage in order.
 void decode_plain(vhsdecode_gb300_session* s, const int16_t* rf_dev, uint64_t n, bool demod_only,
                   uint32_t max_fields, uint32_t& stop, double& host_ms, float& demod_ms,
-                  const std::atomic<bool>* cancel) {
+                  const std::atomic<bool>* cancel, DecodeCarry* carry) {
     cudaStream_t cs = s->stream;
     int64_t nblocks = block_count(n);
     int64_t stream_len = nblocks * kStride;
@@ -973,7 +823,7 @@ void decode_plain(vhsdecode_gb300_session* s, const int16_t* rf_dev, uint64_t n,
         ck(cudaStreamSynchronize(cs), "sync");
         feed.upto = [](int64_t) {};
         auto t0 = std::chrono::steady_clock::now();
-        host_field_loop<double>(s, s->s64.p, stream_len, max_fields, feed, stop, cancel);
+        host_field_loop<double>(s, s->s64.p, stream_len, max_fields, feed, stop, cancel, carry);
         host_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
         launch_field_batch<double>(s, 0, (int)s->fields.size(), s->v64.p, s->s64.p, s->e64.p, stream_len, cs);
         collect_field_results(s, cs);
@@ -984,7 +834,7 @@ void decode_plain(vhsdecode_gb300_session* s, const int16_t* rf_dev, uint64_t n,
 
 int32_t decode_impl(vhsdecode_gb300_session* s, const int16_t* rf, uint64_t n, uint32_t max_fields,
                     uint32_t flags, vhsdecode_gb300_decode_result_v1* res,
-                    const std::atomic<bool>* cancel = nullptr) {
+                    const std::atomic<bool>* cancel, DecodeCarry* carry) {
     if (n > s->max_samples)
         throw Failure(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "sample_count exceeds the session capacity");
     ck(cudaSetDevice(s->device), "cudaSetDevice");
@@ -1003,14 +853,15 @@ int32_t decode_impl(vhsdecode_gb300_session* s, const int16_t* rf, uint64_t n, u
     s->stage_ms[0] = s->stage_ms[1] = s->stage_ms[2] = 0.0f;
     ck(cudaEventRecord(s->ev[0], cs), "event");
     if (s->fp32()) {
-        decode_fp32_pipelined(s, rf, n, host_input, demod_only, max_fields, stop, host_ms, demod_ms, cancel);
+        decode_fp32_pipelined(s, rf, n, host_input, demod_only, max_fields, stop, host_ms, demod_ms, cancel,
+                              carry);
     } else {
         const int16_t* rf_dev = rf;
         if (host_input) {
             if (n > 0) ck(cudaMemcpyAsync(s->rf.p, rf, n * sizeof(int16_t), cudaMemcpyHostToDevice, cs), "h2d rf");
             rf_dev = s->rf.p;
         }
-        decode_plain(s, rf_dev, n, demod_only, max_fields, stop, host_ms, demod_ms, cancel);
+        decode_plain(s, rf_dev, n, demod_only, max_fields, stop, host_ms, demod_ms, cancel, carry);
     }
     ck(cudaEventRecord(s->ev[3], cs), "event");
     ck(cudaEventSynchronize(s->ev[3]), "sync");
@@ -1091,7 +942,8 @@ void write_json(const std::string& path, const vhsdecode_gb300_session* s) {
     if (std::fclose(f) != 0) throw Failure(VHSDECODE_GB300_STATUS_OUTPUT_ERROR, "cannot write " + path);
 }
 
-}  // namespace
+}  // namespace detail
+}  // namespace vhsd
 
 namespace vhsd {
 int32_t set_last_error(int32_t status, const char* msg) {

@@ -406,7 +406,16 @@ bool resolve_cadence(const SyncParams& sp, const std::vector<CPulse>& p, double 
 FieldSync analyse_field(const SyncParams& sp, const std::vector<Pulse>& raw, int64_t span_len,
                         FieldState& state, const RefFetch& fetch) {
     FieldSync out;
-    if (raw.empty()) { out.error = "no sync pulses"; return out; }
+    // recovery steps of BuildRecoveryException / ThrowIfInsufficientFieldData
+    // (Core/Decode/TbcFieldDecodePipeline.cs:1150-1166, 5636-5650, 5936-6007)
+    auto fail = [&](const char* why, double offset) {
+        out.error = why;
+        out.recover_offset = (int64_t)offset;
+        return out;
+    };
+    if (raw.empty())
+        return fail("no sync pulses", state.pulses_seen ? sp.nominal * 100.0 : sp.fs / 10.0);
+    state.pulses_seen = true;
     Timing t = estimate_timing(sp, raw);
     std::vector<CPulse> classified = classify_pulses(sp, raw, t);
     std::vector<CPulse> refined = refine_pulses(sp, raw, t, span_len, fetch, 10.0 * sp.hz_ire);
@@ -415,7 +424,7 @@ FieldSync analyse_field(const SyncParams& sp, const std::vector<Pulse>& raw, int
     state.prev_first = first ? 1 : 0;
     int field_lines = sp.field_lines(first);
     auto g1 = find_first_group(refined, std::nullopt, 9);
-    if (!g1) { out.error = "no vblank"; return out; }
+    if (!g1) return fail("no vblank", sp.nominal * 100.0);
     auto g2 = find_first_group(refined, g1->eq1 + (field_lines - 2.0) * mll, 9);
     Bound b = boundaries(sp.pal, first);
     double section = sp.num_pulses / 2.0;
@@ -445,11 +454,12 @@ FieldSync analyse_field(const SyncParams& sp, const std::vector<Pulse>& raw, int
         else if (le) pick = le;
         else pick = fe;
     }
-    if (!pick) { out.error = "no line 0"; return out; }
+    if (!pick) return fail("no line 0", sp.nominal * 100.0);
     state.has_prev_hsync = true;
     int processed = sp.output_lines + 10;
     double last_line = (((double)span_len - pick->line0) / mll) - 1.0;
-    if (last_line < processed) { out.error = "insufficient data"; return out; }
+    if (last_line < processed)
+        return fail("insufficient data", std::max(pick->line0 - mll * 20.0, sp.nominal));
     // BuildUpstreamLineLocations (SyncAnalysis.cs:551-614)
     std::vector<double> pl;
     for (const CPulse& p : refined) pl.push_back((double)p.start);

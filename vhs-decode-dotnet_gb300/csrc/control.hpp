@@ -38,11 +38,15 @@ struct SyncParams {
 struct FieldState {
     int prev_first = -1;   // -1 unknown, else 0/1
     bool has_prev_hsync = false;
+    bool pulses_seen = false;   // a span with raw pulses was analysed (_vhsPulseSearchInitialized)
 };
 
 struct FieldSync {
     bool ok = false;
     std::string error;
+    // when !ok: samples the engine advances its read position before retrying
+    // (TbcFieldDecodeRecoveryException.SuggestedOffsetSamples, C# long truncation)
+    int64_t recover_offset = 0;
     bool first_field = false;
     double line0 = 0, first_hsync = 0, mean_line = 0, next_offset = 0;
     std::vector<double> locs;       // processed lines, span-relative

@@ -1,0 +1,223 @@
+// Internal state of a decode session and the helpers shared by the C ABI
+// translation units (abi.cpp, server.cpp).  Not part of the public interface.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <atomic>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/vhsdecode_gb300.h"
+#include "control.hpp"
+#include "filters.hpp"
+#include "formats.hpp"
+#include "kernels.h"
+
+namespace vhsd {
+namespace detail {
+
+extern thread_local std::string g_last_error;
+
+struct Failure : std::runtime_error {
+    int32_t status;
+    Failure(int32_t s, const std::string& m) : std::runtime_error(m), status(s) {}
+};
+
+inline int32_t fail(int32_t status, const std::string& msg) {
+    g_last_error = msg;
+    return status;
+}
+
+inline void ck(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) {
+        int32_t st = (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver ||
+                      e == cudaErrorInitializationError)
+                         ? VHSDECODE_GB300_STATUS_CUDA_UNAVAILABLE
+                         : VHSDECODE_GB300_STATUS_INTERNAL_ERROR;
+        throw Failure(st, std::string(what) + ": " + cudaGetErrorString(e));
+    }
+}
+
+template <typename F>
+int32_t guard(F&& f) {
+    try {
+        int32_t r = f();
+        if (r == VHSDECODE_GB300_STATUS_OK) g_last_error.clear();
+        return r;
+    } catch (const Failure& e) {
+        return fail(e.status, e.what());
+    } catch (const std::bad_alloc&) {
+        return fail(VHSDECODE_GB300_STATUS_INTERNAL_ERROR, "host allocation failed");
+    } catch (const std::exception& e) {
+        return fail(VHSDECODE_GB300_STATUS_INTERNAL_ERROR, e.what());
+    } catch (...) {
+        return fail(VHSDECODE_GB300_STATUS_INTERNAL_ERROR, "unknown native failure");
+    }
+}
+
+template <typename T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    void alloc(size_t count) {
+        release();
+        if (count == 0) return;
+        ck(cudaMalloc(&p, count * sizeof(T)), "cudaMalloc");
+        n = count;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    ~DevBuf() { release(); }
+};
+
+// Identity of a captured pipeline graph: the graph bakes these in.
+struct PipeKey {
+    const void* rf = nullptr;
+    uint64_t n = 0;
+    bool host_input = false, demod_only = false;
+    bool operator==(const PipeKey& o) const {
+        return rf == o.rf && n == o.n && host_input == o.host_input && demod_only == o.demod_only;
+    }
+};
+
+struct FieldRec {
+    FieldSync sync;
+    int64_t span_start;
+    int64_t span_len;
+    std::vector<double> refined;
+    std::vector<int32_t> drop;  // triplets
+};
+
+constexpr int64_t kFirstSegBlocks = 40;   // about 1.2 M stream samples
+constexpr int64_t kSegBlocks = 128;        // about 3.9 M stream samples
+
+inline int64_t block_count(uint64_t n) {
+    return n < (uint64_t)kBlock ? 0 : (int64_t)((n - kBlock) / kStride + 1);
+}
+
+}  // namespace detail
+}  // namespace vhsd
+
+using vhsd::detail::DevBuf;
+using vhsd::detail::PipeKey;
+using vhsd::detail::FieldRec;
+using vhsd::FormatParams;
+using vhsd::SyncParams;
+using vhsd::FilterSpectra;
+using vhsd::kBlock;
+using vhsd::kStride;
+
+struct vhsdecode_gb300_session {
+    FormatParams fmt;
+    SyncParams sp;
+    FilterSpectra filt;
+    double fs = 40e6;
+    int precision = 0;
+    int device = 0;
+    uint64_t max_samples = 0;
+    int64_t max_blocks = 0;
+    int max_fields = 0;
+    int lines = 0;       // processed lines per field
+    int out_lines = 0;
+    int outlen = 0;
+    int num_sms = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[6] = {};
+    // device data
+    DevBuf<int16_t> rf;
+    DevBuf<float> v32, s32, e32;
+    DevBuf<double> v64, s64, e64;
+    DevBuf<float> rfv32;
+    DevBuf<float2> vid32, syn32, tw_hi, tw_lo;
+    DevBuf<double> rfv64;
+    DevBuf<double2> vid64, syn64;
+    DevBuf<float2> scratch;
+    DevBuf<float> scratch_raw;
+    DevBuf<int> repair;
+    DevBuf<double2> pwork;
+    DevBuf<double> pdwork;
+    DevBuf<float> pfwork;
+    DevBuf<int> pflag;
+    DevBuf<unsigned> pmask;
+    DevBuf<int64_t> pblk;
+    cudaGraphExec_t plain_graph = nullptr;
+    const int16_t* graph_rf = nullptr;   // input pointer baked into plain_graph
+    DevBuf<int64_t> pc_counts, pc_offsets, pc_events, pc_total;
+    DevBuf<int64_t> pc_counts_alt, pc_offsets_alt;   // scan scratch of odd segments
+    int64_t pc_capacity = 0;
+    DevBuf<double> locs_in, locs_out;
+    DevBuf<uint8_t> fill_in, fill_out;
+    DevBuf<unsigned char> hsync_work;
+    // pipelined FP32 decode: per-segment pulse events, pinned host copies
+    cudaStream_t aux_stream = nullptr;   // rescue fetches while the session stream is busy
+    cudaStream_t copy_stream = nullptr;  // RF copies ahead of the demod
+    cudaStream_t d2h_stream = nullptr;   // pulse events back to the host behind the demod
+    cudaStream_t alt_stream = nullptr;   // odd segments, so a segment's straggler blocks overlap the next one
+    cudaStream_t cap_stream = nullptr;   // origin of the pipeline graph capture
+    cudaEvent_t alt_start = nullptr, alt_end = nullptr, copy_end = nullptr, d2h_end = nullptr;
+    cudaGraphExec_t pipe_exec = nullptr; // captured segment pipeline
+    PipeKey pipe_key{};
+    std::vector<cudaEvent_t> seg_done, seg_copied, seg_pulsed, seg_dem, seg_demod_end;
+    int nseg_max = 0;
+    int64_t seg_cap = 0;                 // pulse events per segment
+    DevBuf<int64_t> seg_events, seg_total;
+    int64_t* h_events = nullptr;         // pinned [nseg_max * seg_cap]
+    int64_t* h_totals = nullptr;         // pinned [nseg_max]
+    int rescue_fetches = 0;
+    int recoveries = 0;                  // field attempts that failed and were skipped past
+    uint32_t launches = 0;               // kernels started by the current decode
+    double enqueue_ms = 0.0;             // host time to queue the pipelined demod
+    cudaStream_t field_stream = nullptr; // field batches, concurrent with later demod segments
+    cudaEvent_t field_end = nullptr;
+    bool stage_timing = false;           // VHSD_STAGE_TIMING set: per-stage kernel times to stderr
+    cudaEvent_t stage_ev[4] = {};
+    float stage_ms[3] = {};
+    uint32_t segments = 0;
+    DevBuf<int> hsync_misses;
+    DevBuf<int64_t> span_start_d, span_len_d;
+    DevBuf<int> first_line_d, start_line_d, end_line_d, line_off_d;
+    DevBuf<float> lut, lut_pair;
+    DevBuf<float2> pw_ff;
+    DevBuf<double> pw, level_work;
+    DevBuf<uint16_t> tbc;
+    DevBuf<int64_t> drop_range, drop_events;
+    DevBuf<float> drop_mean, drop_partial;
+    DevBuf<int> drop_counts, drop_out_count, drop_status;
+    DevBuf<int32_t> drop_out;
+    int drop_cap = 1024, drop_out_cap = 4096;
+    int64_t span_len = 0;
+    // host results
+    std::vector<FieldRec> fields;
+    int64_t last_blocks = 0;
+    int last_repairs = 0;
+
+    bool fp32() const { return precision == VHSDECODE_GB300_PRECISION_FP32_FUSED; }
+};
+
+namespace vhsd {
+namespace detail {
+
+// Decode options beyond the public flags: the server carries a stream's sync
+// history from one window to the next and starts at its continuation point.
+struct DecodeCarry {
+    FieldState state;          // field parity / hsync history
+    int64_t start = 0;         // stitched-stream index where the first field span is resolved
+    int64_t next = 0;          // out: continuation point of the next field (stitched-stream index)
+    bool no_graph = false;     // queue the pipeline directly (inputs change every call)
+};
+
+void session_init(vhsdecode_gb300_session* s, const vhsdecode_gb300_session_config_v1& c);
+void session_free(vhsdecode_gb300_session* s);
+int32_t decode_impl(vhsdecode_gb300_session* s, const int16_t* rf, uint64_t n, uint32_t max_fields,
+                    uint32_t flags, vhsdecode_gb300_decode_result_v1* res,
+                    const std::atomic<bool>* cancel = nullptr, DecodeCarry* carry = nullptr);
+
+}  // namespace detail
+}  // namespace vhsd

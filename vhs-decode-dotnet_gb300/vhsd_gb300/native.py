@@ -45,6 +45,8 @@ EXPORTS = [
     "vhsdecode_gb300_field_sync", "vhsdecode_gb300_tbc_resample_lines",
     "vhsdecode_gb300_find_pulses", "vhsdecode_gb300_vhs_angles",
     "vhsdecode_gb300_pulse_events_noalloc", "vhsdecode_gb300_vhs_demod",
+    "vhsdecode_gb300_server_create", "vhsdecode_gb300_server_submit", "vhsdecode_gb300_server_wait",
+    "vhsdecode_gb300_server_destroy",
 ]
 
 
@@ -116,6 +118,30 @@ class FieldInfo(ctypes.Structure):
                 ("line_count", ctypes.c_uint32), ("dropout_count", ctypes.c_uint32)]
 
 
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("struct_size", ctypes.c_uint32), ("device_id", ctypes.c_int32),
+                ("workers", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+                ("max_window_samples", ctypes.c_uint64), ("memory_budget_bytes", ctypes.c_uint64)]
+
+
+class Window(ctypes.Structure):
+    _fields_ = [("struct_size", ctypes.c_uint32), ("stream_id", ctypes.c_uint32),
+                ("profile", ctypes.c_uint32), ("tape_speed", ctypes.c_uint32),
+                ("sample_rate_mhz", ctypes.c_double), ("samples", ctypes.c_void_p),
+                ("sample_count", ctypes.c_uint64), ("source_offset", ctypes.c_uint64),
+                ("seek", ctypes.c_uint32), ("max_fields", ctypes.c_uint32),
+                ("tbc_out", ctypes.c_void_p), ("tbc_capacity", ctypes.c_uint64)]
+
+
+class WindowResult(ctypes.Structure):
+    _fields_ = [("struct_size", ctypes.c_uint32), ("status", ctypes.c_int32),
+                ("stream_id", ctypes.c_uint32), ("fields", ctypes.c_uint32),
+                ("first_field_is_first", ctypes.c_uint32), ("continued", ctypes.c_uint32),
+                ("ticket", ctypes.c_uint64), ("sample_count", ctypes.c_uint64),
+                ("next_source_offset", ctypes.c_uint64), ("queue_ms", ctypes.c_double),
+                ("decode_ms", ctypes.c_double), ("latency_ms", ctypes.c_double)]
+
+
 _lib = None
 _P = ctypes.POINTER
 _vp = ctypes.c_void_p
@@ -162,6 +188,11 @@ def load(path: str = LIB_PATH):
                                               _P(ctypes.c_uint64)]
     L.vhsdecode_gb300_vhs_angles.argtypes = [_vp, _vp, ctypes.c_uint64, _vp]
     L.vhsdecode_gb300_vhs_demod.argtypes = [_vp, _vp, ctypes.c_uint64, ctypes.c_double, _vp]
+    L.vhsdecode_gb300_server_create.argtypes = [_P(ServerConfig), _P(_vp)]
+    L.vhsdecode_gb300_server_submit.argtypes = [_vp, _P(Window), _P(ctypes.c_uint64)]
+    L.vhsdecode_gb300_server_wait.argtypes = [_vp, ctypes.c_uint64, _P(WindowResult)]
+    L.vhsdecode_gb300_server_destroy.argtypes = [_vp]
+    L.vhsdecode_gb300_server_destroy.restype = None
     L.vhsdecode_gb300_pulse_events_noalloc.argtypes = [_vp, ctypes.c_int64, ctypes.c_double, _vp,
                                                        ctypes.c_int64, _vp, _vp]
     for name in EXPORTS:
@@ -367,3 +398,56 @@ class Session:
         b = ctypes.c_uint64()
         check(load().vhsdecode_gb300_session_tbc_device(self._h, ctypes.byref(p), ctypes.byref(b)))
         return p.value, b.value
+
+
+class Server:
+    """Window server (serving API of include/vhsdecode_gb300.h): windows of many
+    client streams decoded concurrently on one GPU, in order per stream."""
+
+    def __init__(self, max_window_samples, workers=4, memory_budget=0, device=0):
+        L = load()
+        cfg = ServerConfig(ctypes.sizeof(ServerConfig), device, workers, 0, int(max_window_samples),
+                           int(memory_budget))
+        h = _vp()
+        check(L.vhsdecode_gb300_server_create(ctypes.byref(cfg), ctypes.byref(h)))
+        self._h = h
+        self._keep = {}
+
+    def submit(self, stream_id, profile, rf, source_offset=0, seek=False, max_fields=0, tbc_out=None,
+               sample_rate_mhz=40.0, tape_speed=TAPE_SP):
+        """Queue a window (``rf``: int16 host array, kept alive until ``wait``); returns a ticket."""
+        rf = np.ascontiguousarray(rf, np.int16)
+        w = Window(ctypes.sizeof(Window), stream_id, profile, tape_speed, float(sample_rate_mhz),
+                   rf.ctypes.data, len(rf), int(source_offset), 1 if seek else 0, int(max_fields),
+                   tbc_out.ctypes.data if tbc_out is not None else None,
+                   tbc_out.size if tbc_out is not None else 0)
+        t = ctypes.c_uint64(0)
+        check(load().vhsdecode_gb300_server_submit(self._h, ctypes.byref(w), ctypes.byref(t)))
+        self._keep[t.value] = (rf, tbc_out)
+        return t.value
+
+    def wait(self, ticket):
+        """Block until the window is done; returns its WindowResult (raises on a failed window)."""
+        r = WindowResult()
+        r.struct_size = ctypes.sizeof(WindowResult)
+        st = load().vhsdecode_gb300_server_wait(self._h, ticket, ctypes.byref(r))
+        self._keep.pop(ticket, None)
+        check(st)
+        return r
+
+    def close(self):
+        if self._h:
+            load().vhsdecode_gb300_server_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
