@@ -68,3 +68,18 @@ def ntsc_oracle(ntsc_capture):
     rf, _ = ntsc_capture
     fields, ch = field.decode_capture(rf, formats.get("NTSC"))
     return fields, ch
+
+
+@pytest.fixture(scope="session")
+def ntsc20_capture():
+    from vhsd_gb300 import synth
+    rf, info = synth.generate(synth.config("ntsc_small", fs=20e6))
+    return rf, info
+
+
+@pytest.fixture(scope="session")
+def ntsc20_oracle(ntsc20_capture):
+    from oracle import field, formats
+    rf, _ = ntsc20_capture
+    fields, ch = field.decode_capture(rf, formats.get("NTSC"), fs=20e6)
+    return fields, ch

@@ -220,3 +220,27 @@ def test_field_recovery_matches_oracle(gpu, pal_capture):
             d = np.abs(tb[i].astype(np.int64).ravel() - f["tbc"].astype(np.int64))
             assert np.mean(d <= 1) >= LSB_FRACTION
             assert s.dropouts(i) == [tuple(y) for y in f["dropouts"]]
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp32_fused", "fp64_plain"])
+def test_20msps_fields_match_oracle(gpu, precision, ntsc20_capture, ntsc20_oracle):
+    # NTSC VHS sampled at 20 MSPS (the serving mix's 20 MSPS streams)
+    from vhsd_gb300 import native
+    rf, _ = ntsc20_capture
+    fields, (video, _, _, _) = ntsc20_oracle
+    good = [f for f in fields if "error" not in f]
+    with native.Session(native.PROFILE_NTSC, len(rf), precision=precision, sample_rate_mhz=20.0) as s:
+        r = s.decode(rf, demod_only=True)
+        v = s.stream(0, 0, len(video))
+        assert np.quantile(np.abs(v - video), 0.999) < FREQ_TOL_HZ
+        r = s.decode(rf)
+        assert r.fields == len(good)
+        tb = s.tbc()
+        for i, f in enumerate(good):
+            info = s.field(i)
+            assert bool(info.is_first_field) == f["first_field"]
+            assert info.span_start == f["span_start"]
+            assert np.max(np.abs(s.lines(i) - f["locs"])) < LINE_TOL
+            d = np.abs(tb[i].astype(np.int64).ravel() - f["tbc"].astype(np.int64))
+            assert np.mean(d <= 1) >= LSB_FRACTION
+            assert s.dropouts(i) == [tuple(x) for x in f["dropouts"]]
