@@ -306,6 +306,9 @@ def run_ours(args, world, rank, local):
         cpu = {"value": round(msps, 3), "unit": "MSPS", "cores": procs, "kind": "port",
                "sample": "whole workload capture (%d samples, %.1f s): oracle restatement, block "
                          "demod over %d spawn processes + sequential field path" % (n, dt, procs)}
+    serving = None
+    if rank == 0 and world == 1 and not args.skip_serve:
+        serving = run_serving(args, local)
     if rank == 0:
         line = {"metric": METRIC, "value": round(value, 3), "unit": "MSPS", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
@@ -327,12 +330,125 @@ def run_ours(args, world, rank, local):
                              "algorithmic_bytes": int(DEMOD_BYTES_PER_BLOCK * nblocks)},
                 "cpu_baseline": cpu,
                 "plain_fp64": plain,
+                "serving": serving,
                 "gpu_launches": int(launches),
                 "clocks": clk,
                 "stage_ms": {"demod": round(avg_demod, 4), "field_kernels_and_host": round(r.field_ms, 4),
                              "host_control": round(r.host_ms, 4)}}
         print(json.dumps(line))
     sess.close()
+
+
+# Serving mix of 2-s windows (share, profile, MSPS, label).  The PAL S-VHS and
+# NTSC LaserDisc shares are decoded as PAL VHS / NTSC VHS windows of the same
+# sample rate and length (their demod branches are not built), so the offered
+# sample load is the mix's own: 200 windows/s x 68 M samples = 13.6 GSPS.
+SERVE_MIX = [(0.40, "PAL", 40.0, "pal_vhs_40"), (0.30, "NTSC", 20.0, "ntsc_vhs_20"),
+             (0.15, "PAL", 40.0, "pal_svhs_40 as pal_vhs_40"), (0.15, "NTSC", 40.0, "ntsc_ld_40 as ntsc_vhs_40")]
+SERVE_TILE_FIELDS = 8
+
+
+def serve_source(system, mhz, seconds):
+    """Seeded synthetic capture of `seconds`, built by repeating an 8-field
+    synthetic recording (the joins are FM phase jumps, decoded like head
+    switches).  Cached in /tmp."""
+    from vhsd_gb300 import synth
+    cache = os.path.join("/tmp", "vhsd_serve_%s_%d_%d.npy" % (system, int(mhz), SERVE_TILE_FIELDS))
+    if os.path.exists(cache):
+        tile = np.load(cache)
+    else:
+        cfg = synth.config("pal4" if system == "PAL" else "ntsc_small", fields=SERVE_TILE_FIELDS,
+                           fs=mhz * 1e6, seed=31 if system == "PAL" else 32)
+        tile, _ = synth.generate(cfg)
+        try:
+            np.save(cache, tile)
+        except OSError:
+            pass
+    n = int(seconds * mhz * 1e6)
+    return np.resize(tile, n)
+
+
+def run_serving(args, local):
+    """Poisson arrivals of 2-s windows over 32 client streams into the window
+    server; returns latency percentiles and aggregate RF MSPS."""
+    import torch
+    from vhsd_gb300 import native
+    rng = np.random.default_rng(2024)
+    win_s, rate, nstreams, dur = 2.0, float(args.serve_rate), 32, float(args.serve_seconds)
+    src_s = 6.0
+    sources = {}
+    for share, system, mhz, label in SERVE_MIX:
+        key = (system, mhz)
+        if key not in sources:
+            host = serve_source(system, mhz, src_s)
+            sources[key] = torch.from_numpy(host).pin_memory().numpy()
+    # streams: formats by the mix shares
+    counts = [int(round(share * nstreams)) for share, _, _, _ in SERVE_MIX]
+    counts[0] += nstreams - sum(counts)
+    streams = []
+    for (share, system, mhz, label), c in zip(SERVE_MIX, counts):
+        for _ in range(c):
+            streams.append({"system": system, "mhz": mhz, "label": label, "offset": None, "left": 0})
+    max_win = int(win_s * 40e6)
+    prof = {"PAL": native.PROFILE_PAL, "NTSC": native.PROFILE_NTSC}
+    per_field = {"PAL": 313 * 1135, "NTSC": 263 * 910}
+    outs = {sysn: [torch.empty(130 * per_field[sysn], dtype=torch.int16).pin_memory().numpy().view(np.uint16)
+                   for _ in range(8)] for sysn in ("PAL", "NTSC")}
+    sv = native.Server(max_win, workers=args.serve_workers, device=local)
+
+    def window(st):
+        src = sources[(st["system"], st["mhz"])]
+        n = int(win_s * st["mhz"] * 1e6)
+        seek = st["offset"] is None or st["left"] <= 0 or st["offset"] + 2 * n > len(src)
+        if seek:
+            st["offset"] = int(rng.integers(0, len(src) - n))
+            st["left"] = int(rng.integers(1, 11))   # windows until the next seek
+        else:
+            st["offset"] += n - int(0.12 * st["mhz"] * 1e6)   # 0.12 s preroll overlap
+        st["left"] -= 1
+        return src[st["offset"]:st["offset"] + n], st["offset"], seek
+
+    # warm-up: `workers` windows of every format at once, so each worker has a
+    # slot of each format before the timed arrivals start
+    warm = []
+    for key in sources:
+        st0 = next(x for x in streams if (x["system"], x["mhz"]) == key)
+        for i in range(args.serve_workers):
+            x, off, seek = window(dict(st0))
+            warm.append(sv.submit(1000 + len(warm), prof[st0["system"]], x, off, seek=True,
+                                  sample_rate_mhz=st0["mhz"], tbc_out=outs[st0["system"]][i % 8]))
+    for t in warm:
+        sv.wait(t)
+    # arrivals
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, size=int(rate * dur * 1.5) + 10))
+    arrivals = arrivals[arrivals < dur]
+    tickets = []
+    t0 = time.perf_counter()
+    samples = 0
+    for k, ta in enumerate(arrivals):
+        now = time.perf_counter() - t0
+        if ta > now:
+            time.sleep(ta - now)
+        si = int(rng.integers(0, nstreams))
+        st = streams[si]
+        x, off, seek = window(st)
+        samples += len(x)
+        tickets.append(sv.submit(si, prof[st["system"]], x, off, seek=seek, sample_rate_mhz=st["mhz"],
+                                 tbc_out=outs[st["system"]][k % 8]))
+    res = [sv.wait(t) for t in tickets]
+    t_end = time.perf_counter() - t0
+    sv.close()
+    lat = np.array([r.latency_ms for r in res])
+    ok = sum(1 for r in res if r.status == 0)
+    return {"windows": len(res), "ok": ok, "offered_windows_per_s": rate, "streams": nstreams,
+            "window_s": win_s, "workers": args.serve_workers, "seconds": round(t_end, 3),
+            "p50_ms": round(float(np.percentile(lat, 50)), 2), "p99_ms": round(float(np.percentile(lat, 99)), 2),
+            "mean_queue_ms": round(float(np.mean([r.queue_ms for r in res])), 2),
+            "msps": round(samples / t_end / 1e6, 1),
+            "offered_msps": round(samples / dur / 1e6, 1),
+            "fields": int(sum(r.fields for r in res)),
+            "mix": [m[3] for m in SERVE_MIX],
+            "data": "synthetic, 8-field recordings repeated to 6 s per format; TBC copied to pinned host"}
 
 
 def main():
@@ -344,6 +460,10 @@ def main():
     ap.add_argument("--workload", default="ntsc60", choices=sorted(WORKLOADS))
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-plain", action="store_true")
+    ap.add_argument("--skip-serve", action="store_true")
+    ap.add_argument("--serve-rate", type=float, default=200.0, help="window arrivals per second")
+    ap.add_argument("--serve-seconds", type=float, default=3.0)
+    ap.add_argument("--serve-workers", type=int, default=8)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -240,7 +240,7 @@ void session_init(vhsdecode_gb300_session* s, const vhsdecode_gb300_session_conf
     s->span_len_d.alloc(s->max_fields);
     s->first_line_d.alloc(s->max_fields); s->start_line_d.alloc(s->max_fields);
     s->end_line_d.alloc(s->max_fields); s->line_off_d.alloc(s->max_fields);
-    std::vector<float> lut = build_sinc_lut();
+    static const std::vector<float> lut = build_sinc_lut();   // built once per process
     s->lut.alloc(lut.size());
     ck(cudaMemcpy(s->lut.p, lut.data(), lut.size() * sizeof(float), cudaMemcpyHostToDevice), "upload");
     {
