@@ -148,44 +148,87 @@ __global__ void k_replace_spikes(double* d, const double* dd, double diff_max, i
     if (lane == 0) flag[0] = 0;
 }
 
-// float32 envelope filtfilt, exactly sequential as the reference
-// (SosFilter.ApplyForwardBackwardFloat32, Core/Dsp/SosFilter.cs:300-540):
-// one thread per block; raw[n] = |float(Re z[n-4])|.
-__global__ void k_envelope(const double2* z, float* work, double* env, float b0, float b1, float a1) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    const int edge = 6;
-    float* ext = work;
-    float* raw = work + edge;
-    for (int n = 0; n < N; n++) raw[(n + 4) & (N - 1)] = fabsf((float)z[n].x);
-    float first = raw[0], last = raw[N - 1];
-    for (int i = 0; i < edge; i++) ext[i] = __fsub_rn(__fmul_rn(2.0f, first), raw[edge - i]);
-    for (int i = 0; i < edge; i++) ext[edge + N + i] = __fsub_rn(__fmul_rn(2.0f, last), raw[N - 2 - i]);
-    const int len = N + 2 * edge;
-    float b2 = 0.0f, a2 = 0.0f;
-    float ft = __fsub_rn(b1, __fmul_rn(a1, b0));
-    float st = __fsub_rn(b2, __fmul_rn(a2, b0));
-    float num = __fadd_rn(__fadd_rn(0.0f, ft), st);
-    float den = __fadd_rn(__fadd_rn(1.0f, a1), a2);
-    float zi0 = __fdiv_rn(num, den);
-    float zi1 = __fsub_rn(__fmul_rn(__fadd_rn(1.0f, a1), zi0), ft);
-    float z1 = __fmul_rn(zi0, ext[0]), z2 = __fmul_rn(zi1, ext[0]);
-    for (int s = 0; s < len; s++) {
-        float v = ext[s];
-        float f = __fadd_rn(__fmul_rn(b0, v), z1);
-        z1 = __fadd_rn(__fsub_rn(__fmul_rn(b1, v), __fmul_rn(a1, f)), z2);
-        z2 = __fsub_rn(__fmul_rn(b2, v), __fmul_rn(a2, f));
-        ext[s] = f;
+// float32 envelope filtfilt (SosFilter.ApplyForwardBackwardFloat32,
+// Core/Dsp/SosFilter.cs:300-540) of raw[n] = |float(Re z[n-4])| (circular
+// roll by 4), in float32 like the reference, as a parallel scan: one CTA of
+// 32 warps, warp w covers samples [1024 w, 1024 w + 1024) as four rows of 256
+// (8 consecutive samples per lane, lanes joined by an affine warp scan).  The
+// state entering a warp's range comes from a 256-sample halo started at zero
+// (the first-order filter's memory c^256 is below 1e-12); at the block edges
+// the recursion starts from zero instead of the reference's padded
+// steady-state start, which only touches samples the overlap-save cut drops.
+struct EnvAff { float a, b; };
+__device__ __forceinline__ EnvAff env_then(EnvAff first, EnvAff second) {
+    return EnvAff{second.a * first.a, fmaf(second.a, first.b, second.b)};
+}
+__device__ __forceinline__ EnvAff env_scan(EnvAff v, int lane) {
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        float pa = __shfl_up_sync(0xffffffffu, v.a, o), pb = __shfl_up_sync(0xffffffffu, v.b, o);
+        if (lane >= o) v = env_then(EnvAff{pa, pb}, v);
     }
-    z1 = __fmul_rn(zi0, ext[len - 1]);
-    z2 = __fmul_rn(zi1, ext[len - 1]);
-    for (int s = len - 1; s >= 0; s--) {
-        float v = ext[s];
-        float f = __fadd_rn(__fmul_rn(b0, v), z1);
-        z1 = __fadd_rn(__fsub_rn(__fmul_rn(b1, v), __fmul_rn(a1, f)), z2);
-        z2 = __fsub_rn(__fmul_rn(b2, v), __fmul_rn(a2, f));
-        ext[s] = f;
+    return v;
+}
+__device__ __forceinline__ EnvAff env_scan_rev(EnvAff v, int lane) {
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        float pa = __shfl_down_sync(0xffffffffu, v.a, o), pb = __shfl_down_sync(0xffffffffu, v.b, o);
+        if (lane + o < 32) v = env_then(EnvAff{pa, pb}, v);
     }
-    for (int n = 0; n < N; n++) env[n] = (double)ext[edge + n];
+    return v;
+}
+
+__global__ void __launch_bounds__(1024) k_envelope(const double2* z, float* work, double* env, float b0,
+                                                   float b1, float a1) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int n0 = warp * 1024;
+    const float cc = -a1, gk = b1 - a1 * b0;
+    float c8 = cc;
+#pragma unroll
+    for (int k = 1; k < 8; k++) c8 *= cc;
+    auto raw = [&](int n) { return fabsf((float)z[(n - 4) & (N - 1)].x); };
+    float yv[32];
+    float carry = 0.0f;
+    if (n0 >= 256) {
+        float st = 0.0f;
+        for (int k = 0; k < 8; k++) st = fmaf(cc, st, gk * raw(n0 - 256 + lane * 8 + k));
+        EnvAff inc = env_scan(EnvAff{c8, st}, lane);
+        carry = __shfl_sync(0xffffffffu, inc.b, 31);
+    }
+    for (int row = 0; row < 4; row++) {
+        int ms = n0 + row * 256 + lane * 8;
+        float ev[8], st = 0.0f;
+        for (int k = 0; k < 8; k++) { ev[k] = raw(ms + k); st = fmaf(cc, st, gk * ev[k]); }
+        EnvAff inc = env_scan(EnvAff{c8, st}, lane);
+        float pb = __shfl_up_sync(0xffffffffu, inc.b, 1), pa = __shfl_up_sync(0xffffffffu, inc.a, 1);
+        float zz = lane == 0 ? carry : fmaf(pa, carry, pb);
+        for (int k = 0; k < 8; k++) { yv[row * 8 + k] = fmaf(b0, ev[k], zz); zz = fmaf(cc, zz, gk * ev[k]); }
+        carry = __shfl_sync(0xffffffffu, zz, 31);
+        for (int k = 0; k < 8; k++) work[ms + k] = yv[row * 8 + k];
+    }
+    __syncthreads();
+    const int nend = n0 + 1024;
+    carry = 0.0f;
+    if (nend + 256 <= N) {
+        float st = 0.0f;
+        for (int k = 7; k >= 0; k--) st = fmaf(cc, st, gk * work[nend + lane * 8 + k]);
+        EnvAff inc = env_scan_rev(EnvAff{c8, st}, lane);
+        carry = __shfl_sync(0xffffffffu, inc.b, 0);
+    }
+    for (int row = 3; row >= 0; row--) {
+        int ms = n0 + row * 256 + lane * 8;
+        float st = 0.0f;
+        for (int k = 7; k >= 0; k--) st = fmaf(cc, st, gk * yv[row * 8 + k]);
+        EnvAff inc = env_scan_rev(EnvAff{c8, st}, lane);
+        float nb = __shfl_down_sync(0xffffffffu, inc.b, 1), na = __shfl_down_sync(0xffffffffu, inc.a, 1);
+        float zz = lane == 31 ? carry : fmaf(na, carry, nb);
+        for (int k = 7; k >= 0; k--) {
+            float y = yv[row * 8 + k];
+            env[ms + k] = (double)fmaf(b0, y, zz);
+            zz = fmaf(cc, zz, gk * y);
+        }
+        carry = __shfl_sync(0xffffffffu, zz, 0);
+    }
 }
 
 __global__ void k_real_to_complex(const double* d, double2* out) {
@@ -243,7 +286,7 @@ cudaError_t launch_demod_fp64_block(const PlainDemodParams& p, cudaStream_t s) {
     k_demod<<<G, B, 0, s>>>(w3, d, (float)p.fs, p.diff_max, flag);
     k_diff_demod<<<G, B, 0, s>>>(w3, dd, (float)p.fs, flag);
     k_replace_spikes<<<1, 32, 0, s>>>(d, dd, p.diff_max, flag, mask);
-    k_envelope<<<1, 32, 0, s>>>(w3, fscr, env, (float)p.env_b0, (float)p.env_b1, (float)p.env_a1);
+    k_envelope<<<1, 1024, 0, s>>>(w3, fscr, env, (float)p.env_b0, (float)p.env_b1, (float)p.env_a1);
     k_real_to_complex<<<G, B, 0, s>>>(d, w0);
     fft<false>(w0, w1, s);                         // D in w1
     k_filter_spec<<<G, B, 0, s>>>(w1, p.video, w2);
