@@ -66,7 +66,7 @@ def peaks():
 
 def profile_traffic_per_block():
     """DRAM bytes per block of the fused demodulator from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "demod_fp32_pal4.md")
+    p = os.path.join(ROOT, "profiles", "demod_fp32_ntsc60.md")
     if not os.path.exists(p):
         return None
     for line in open(p):
@@ -451,6 +451,27 @@ def run_serving(args, local):
             "data": "synthetic, 8-field recordings repeated to 6 s per format; TBC copied to pinned host"}
 
 
+def run_profile_demod(args, local):
+    """Demod-only decodes of the workload (one fused demodulator launch each),
+    for kernel captures: warm-up, then --steps decodes; prints the kernel times."""
+    import torch
+    from vhsd_gb300 import native
+    desc, system = WORKLOADS[args.workload]
+    prof = native.PROFILE_PAL if system == "PAL" else native.PROFILE_NTSC
+    rf = workload(args.workload)
+    sess = native.Session(prof, len(rf), device=local)
+    d_rf = torch.from_numpy(rf).to("cuda")
+    for _ in range(args.warmup):
+        sess.decode(None, device_ptr=d_rf.data_ptr(), count=len(rf), demod_only=True)
+    ms = []
+    for _ in range(args.steps):
+        r = sess.decode(None, device_ptr=d_rf.data_ptr(), count=len(rf), demod_only=True)
+        ms.append(r.demod_ms)
+    torch.cuda.synchronize()
+    print(json.dumps({"workload": args.workload, "blocks": int(r.blocks), "demod_ms": ms}))
+    sess.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -464,11 +485,15 @@ def main():
     ap.add_argument("--serve-rate", type=float, default=200.0, help="window arrivals per second")
     ap.add_argument("--serve-seconds", type=float, default=3.0)
     ap.add_argument("--serve-workers", type=int, default=8)
+    ap.add_argument("--profile-demod", action="store_true",
+                    help="only demod-only decodes of the workload (for kernel captures)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     world, rank, local = dist_init(args)
-    if args.impl == "reference":
+    if args.profile_demod:
+        run_profile_demod(args, local)
+    elif args.impl == "reference":
         run_reference(args, world, rank)
     else:
         run_ours(args, world, rank, local)
