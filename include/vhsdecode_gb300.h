@@ -279,6 +279,13 @@ VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_find_pulses(
 VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_vhs_demod(
     const float* real, const float* imaginary, uint64_t n, double sample_rate_hz, float* out);
 
+/* Device ReplaceSpikes (RfDemodulator.ReplaceSpikes, Core/Dsp/RfDemodulator.cs:966-1001)
+ * in the block demodulator's parallel form, in place on `demod` (n a multiple of
+ * 32, at most 2^20): windows [i-8, i+30) around demod > max_value take `diffed`
+ * where max(diffed) < max(demod). */
+VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_replace_spikes(
+    float* demod, const float* diffed, uint64_t n, float max_value);
+
 /* Device polynomial atan2 (the FM demodulator's angle) for n float pairs. */
 VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_vhs_angles(
     const float* real, const float* imaginary, uint64_t n, float* angles);

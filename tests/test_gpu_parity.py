@@ -60,6 +60,24 @@ def test_device_fm_demod_bit_exact(gpu):
     assert a[~nan].view(np.uint32).tolist() == b[~nan].view(np.uint32).tolist()
 
 
+def test_parallel_replace_spikes_matches_sequential(gpu):
+    # dense, overlapping spike windows where the order of replacements matters
+    from vhsd_gb300 import native
+    from oracle import demod as odemod
+    rng = np.random.default_rng(99)
+    for it in range(40):
+        n = 32 * int(rng.integers(1, 300))
+        d = rng.normal(0.0, 1.0, n).astype(np.float32)
+        f = rng.normal(0.0, 1.0, n).astype(np.float32)
+        dens = rng.choice([0.002, 0.02, 0.1, 0.5])
+        hit = rng.random(n) < dens
+        d[hit] = rng.uniform(3.0, 9.0, hit.sum()).astype(np.float32)
+        f[rng.random(n) < dens] += np.float32(rng.uniform(0, 8))
+        want = odemod.replace_spikes(d.astype(np.float64), f.astype(np.float64), 2.5).astype(np.float32)
+        got = native.replace_spikes(d, f, 2.5)
+        assert got.tobytes() == want.tobytes(), (it, n, dens)
+
+
 def test_device_pulses_match_state_machine(gpu):
     from vhsd_gb300 import native
     from oracle import native as onative

@@ -176,7 +176,6 @@ void session_init(vhsdecode_gb300_session* s, const vhsdecode_gb300_session_conf
         int clusters = s->num_sms / 2;
         // two halves: segments on the two compute streams may run at once
         s->scratch.alloc((size_t)2 * clusters * 2 * kBlock);
-        s->scratch_raw.alloc((size_t)2 * clusters * kBlock);
         s->repair.alloc(1);
         s->nseg_max = (int)((std::max<int64_t>(0, s->max_blocks - kFirstSegBlocks) + kSegBlocks - 1) / kSegBlocks) + 1;
         s->seg_cap = kSegBlocks * kStride / 64 + 4096;
@@ -325,7 +324,6 @@ FastDemodParams fp32_params(vhsdecode_gb300_session* s, const int16_t* rf_dev) {
     p.sync_out = s->s32.p;
     p.env_out = s->e32.p;
     p.scratch = s->scratch.p;
-    p.scratch_raw = s->scratch_raw.p;
     p.repair_count = s->repair.p;
     return p;
 }
@@ -659,7 +657,6 @@ void enqueue_pipeline(vhsdecode_gb300_session* s, const int16_t* rf, uint64_t n,
         p.nblocks = b1 - b0;
         const size_t half = (size_t)(s->num_sms / 2) * kBlock;
         p.scratch = s->scratch.p + (k & 1) * 2 * half;
-        p.scratch_raw = s->scratch_raw.p + (k & 1) * half;
         rec(s->seg_dem[(size_t)(2 * k)], ks, true);
         ck(launch_demod_fp32(p, s->num_sms / 2, ks), "demod fp32 launch");
         rec(s->seg_dem[(size_t)(2 * k + 1)], ks, true);

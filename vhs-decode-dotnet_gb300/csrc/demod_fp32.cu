@@ -30,10 +30,12 @@
 // conflicts) plus twiddle tables; one CTA per SM.
 #include <cooperative_groups.h>
 #include <atomic>
+#include <climits>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
 #include "fft_common.cuh"
+#include "spikes.cuh"
 #include "vhs_math.cuh"
 #include "kernels.h"
 
@@ -145,8 +147,11 @@ __device__ __forceinline__ void fft16384(float2* buf, const Tw& tw, int tid) {
 
 struct Shared {
     float2 buf[BUF];
+    float theta[M];          // stage 3: angle, then demod, of each local sample
+    unsigned repl[N / 32];   // spike windows chosen for replacement (repair path)
     Tw tw;
-    float2 nyq;          // Nyquist bin of the rank-0 half spectrum
+    float2 nyq;              // Nyquist bin of the rank-0 half spectrum
+    float2 tail_z[2][2];     // last two analytic samples of each local chunk
     float tail_theta[2];     // last angle of each local chunk
     float tail_re[2][4];     // last four Re z of each local chunk
     int flag;
@@ -322,7 +327,9 @@ vhsd_demod_fp32_kernel(FastDemodParams p) {
         fft16384<true>(buf, sh.tw, tid);
         cluster.sync();
         {
-            // z[n] = A[n] + W^-n B[n], z[n+16384] = A[n] - W^-n B[n]
+            // z[n] = A[n] + W^-n B[n], z[n+16384] = A[n] - W^-n B[n]; the
+            // analytic signal stays in buf (chunk rank at local 0..8191,
+            // chunk rank + 2 at 8192..16383) until the demod is final
             float2 o1[16], o2[16];
 #pragma unroll
             for (int t = 0; t < 16; t++) {
@@ -333,9 +340,8 @@ vhsd_demod_fp32_kernel(FastDemodParams p) {
                 float2 a = rank == 0 ? loc : rem;
                 float2 b = rank == 0 ? rem : loc;
                 float2 wb = cmulc(b, w32k(sh.tw, n));
-                float2 z1 = cadd(a, wb), z2 = csub(a, wb);
-                o1[t] = make_float2(vhs_atan2(z1.y, z1.x), z1.x);
-                o2[t] = make_float2(vhs_atan2(z2.y, z2.x), z2.x);
+                o1[t] = cadd(a, wb);
+                o2[t] = csub(a, wb);
             }
             cluster.sync();
 #pragma unroll
@@ -346,95 +352,92 @@ vhsd_demod_fp32_kernel(FastDemodParams p) {
             }
         }
         __syncthreads();
-        // ---------------- stage 3: demod, raw envelope, spike check ------
+        // ---------------- stage 3: angles, demod, spike check -------------
+#pragma unroll 4
+        for (int t = 0; t < 32; t++) {
+            int i = tid + t * T;
+            float2 z = buf[sx(i)];
+            sh.theta[i] = vhs_atan2(z.y, z.x);
+        }
+        __syncthreads();
         if (tid < 2) {
             int i_last = tid * 8192 + 8191;
-            sh.tail_theta[tid] = buf[sx(i_last)].x;
-            for (int k = 0; k < 4; k++) sh.tail_re[tid][k] = buf[sx(i_last - 3 + k)].y;
+            sh.tail_theta[tid] = sh.theta[i_last];
+            for (int k = 0; k < 4; k++) sh.tail_re[tid][k] = buf[sx(i_last - 3 + k)].x;
+            sh.tail_z[tid][0] = buf[sx(i_last - 1)];
+            sh.tail_z[tid][1] = buf[sx(i_last)];
         }
         cluster.sync();
         bool spike = false;
         {
-            float dv[32], rv[32];
+            float dv[32];
 #pragma unroll
             for (int t = 0; t < 32; t++) {
                 int i = tid + t * T;        // local position [0, 16384)
                 int n = pos_to_n(i, rank);
                 int il = i & 8191;
-                int lc = i >> 13;           // local chunk slot
-                int c = 2 * lc + rank;      // chunk of n
+                int c = 2 * (i >> 13) + rank;  // chunk of n
                 int plc = ((c + 3) & 3) >> 1;  // predecessor chunk (other rank) slot
-                float th = buf[sx(i)].x;
-                float thp = (il > 0) ? buf[sx(i - 1)].x : rsh->tail_theta[plc];
+                float th = sh.theta[i];
+                float thp = (il > 0) ? sh.theta[i - 1] : rsh->tail_theta[plc];
                 float d = (n == 0) ? 0.0f : vhs_freq_diff(th, thp, freq);
                 dv[t] = d;
                 if (n >= 20 && n < N - 20 && d > p.diff_max) spike = true;
-                float re = (il >= 4) ? buf[sx(i - 4)].y : rsh->tail_re[plc][il];
-                rv[t] = fabsf(re);
             }
             __syncthreads();
 #pragma unroll
-            for (int t = 0; t < 32; t++) buf[sx(tid + t * T)] = make_float2(dv[t], rv[t]);
+            for (int t = 0; t < 32; t++) sh.theta[tid + t * T] = dv[t];   // theta now holds the demod
         }
         int any = __syncthreads_or(spike ? 1 : 0);
         if (tid == 0) sh.flag = any;
         cluster.sync();
         any = sh.flag | rsh->flag;
         if (any) {
-            // Diff-demod repair (Core/Dsp/RfDemodulator.cs:966-1001, 2527-2582):
-            // rebuild the analytic signal into cluster scratch, demodulate its
-            // first difference, then replace spikes in ascending index order.
+            // Diff-demod repair (Core/Dsp/RfDemodulator.cs:966-1001, 2527-2582)
+            // with the analytic signal still in buf: demod and spike mask to
+            // cluster scratch, the diff-demod only around spikes, then
+            // ReplaceSpikes in parallel (spikes.cuh) on rank 0.
             if (tid == 0 && rank == 0) atomicAdd(p.repair_count, 1);
-            float2* zs = p.scratch + (int64_t)cluster_id * (2 * N);
-            float* ds = reinterpret_cast<float*>(zs + N);
+            float* ds = reinterpret_cast<float*>(p.scratch + (int64_t)cluster_id * (2 * N));
             float* dds = ds + N;
-            float* raws = p.scratch_raw + (int64_t)cluster_id * N;
+            unsigned* maskg = reinterpret_cast<unsigned*>(dds + N);
+            int* cposg = reinterpret_cast<int*>(maskg + N / 32);
 #pragma unroll 4
             for (int t = 0; t < 32; t++) {
                 int i = tid + t * T;
                 int n = pos_to_n(i, rank);
-                float2 v = buf[sx(i)];
-                ds[n] = v.x;
-                raws[n] = v.y;
-            }
-            __syncthreads();
-            load_rf(buf, x, rank, sh.tw, tid);
-            __syncthreads();
-            fft8192<false, 1>(buf, sh.tw, tid);
-            post_half(sh, rank, tid, [&](int k, float2 v) {
-                float g = __ldg(p.rf_video + k) * ((k == 0 || k == M) ? inv_n : 2.0f * inv_n);
-                return make_float2(v.x * g, v.y * g);
-            });
-            if (rank == 0) {
-                if (tid == 0) buf[sx(8192)] = sh.nyq;
-                for (int i = 8193 + tid; i < M; i += T) buf[sx(i)] = make_float2(0.f, 0.f);
-            } else {
-                for (int i = 8192 + tid; i < M; i += T) buf[sx(i)] = make_float2(0.f, 0.f);
-            }
-            __syncthreads();
-            fft16384<true>(buf, sh.tw, tid);
-            cluster.sync();
-            for (int t = 0; t < 16; t++) {
-                int n = tid + t * T + rank * 8192;
-                float2 loc = buf[sx(n)];
-                float2 rem = rbuf[sx(n)];
-                float2 a = rank == 0 ? loc : rem;
-                float2 b = rank == 0 ? rem : loc;
-                float2 wb = cmulc(b, w32k(sh.tw, n));
-                zs[n] = cadd(a, wb);
-                zs[n + 16384] = csub(a, wb);
+                float d = sh.theta[i];
+                ds[n] = d;
+                unsigned m = __ballot_sync(0xffffffffu, d > p.diff_max);   // 32 consecutive n
+                if (lane == 0) maskg[n >> 5] = m;
             }
             cluster.sync();
+            // diff-demod, only where some window can reach (a spike in [n-29, n+8])
+#pragma unroll 2
             for (int t = 0; t < 32; t++) {
-                int n = pos_to_n(tid + t * T, rank);
+                int i = tid + t * T;
+                int n = pos_to_n(i, rank);
+                int a0 = max(n - 29, 0), a1 = min(n + 8, N - 1);
+                bool need = false;
+                for (int w = a0 >> 5; w <= (a1 >> 5); w++) {
+                    int lo = max(a0 - w * 32, 0), hi = min(a1 - w * 32, 31);
+                    unsigned sel = (hi == 31 ? 0xffffffffu : ((2u << hi) - 1u)) & ~((1u << lo) - 1u);
+                    need = need || (maskg[w] & sel) != 0u;
+                }
+                if (!need) continue;
                 float dd = 0.0f;
                 if (n >= 1) {
-                    float2 z0 = zs[n], zm1 = zs[n - 1];
-                    float2 dz = csub(z0, zm1);
+                    int il = i & 8191;
+                    int c = 2 * (i >> 13) + rank;
+                    int plc = ((c + 3) & 3) >> 1;
+                    float2 z0 = buf[sx(i)];
+                    float2 z1 = il >= 1 ? buf[sx(i - 1)] : rsh->tail_z[plc][1];
+                    float2 dz = csub(z0, z1);
                     float th = vhs_atan2(dz.y, dz.x);
                     float thp;
                     if (n >= 2) {
-                        float2 dzp = csub(zm1, zs[n - 2]);
+                        float2 z2 = il >= 2 ? buf[sx(i - 2)] : rsh->tail_z[plc][il == 1 ? 1 : 0];
+                        float2 dzp = csub(z1, z2);
                         thp = vhs_atan2(dzp.y, dzp.x);
                     } else {
                         thp = vhs_atan2(0.0f, 0.0f);
@@ -445,50 +448,38 @@ vhsd_demod_fp32_kernel(FastDemodParams p) {
             }
             cluster.sync();
             if (rank == 0) {
-                // spike mask from the demod before any replacement
-                unsigned* mask = reinterpret_cast<unsigned*>(buf);
-                for (int base = warp * 32; base < N; base += 32 * (T / 32)) {
-                    unsigned m = __ballot_sync(0xffffffffu, ds[base + lane] > p.diff_max);
-                    if (lane == 0) mask[base >> 5] = m;
-                }
+                spike_thresholds(ds, dds, maskg, cposg, N, tid, T);
                 __syncthreads();
-                if (warp == 0) {
-                    for (int word = 0; word < N / 32; word++) {
-                        unsigned m = mask[word];
-                        while (m) {
-                            int b = __ffs(m) - 1;
-                            m &= m - 1;
-                            int i0 = word * 32 + b;
-                            int st = max(i0 - 8, 0);
-                            int en = min(i0 + 30, N - 1);
-                            if (st >= en) continue;
-                            float mdd = -INFINITY, md = -INFINITY;
-                            for (int k = st + lane; k < en; k += 32) {
-                                mdd = fmaxf(mdd, dds[k]);
-                                md = fmaxf(md, ds[k]);
-                            }
-#pragma unroll
-                            for (int o = 16; o > 0; o >>= 1) {
-                                mdd = fmaxf(mdd, __shfl_xor_sync(0xffffffffu, mdd, o));
-                                md = fmaxf(md, __shfl_xor_sync(0xffffffffu, md, o));
-                            }
-                            if (mdd < md) {
-                                for (int k = st + lane; k < en; k += 32) ds[k] = dds[k];
-                            }
-                            __syncwarp();
-                        }
-                    }
-                }
+                if (warp == 0) spike_walk(maskg, cposg, sh.repl, N, lane);
+                __syncthreads();
+                spike_apply(ds, dds, sh.repl, N, tid, T);
             }
             cluster.sync();
 #pragma unroll 4
             for (int t = 0; t < 32; t++) {
                 int i = tid + t * T;
-                int n = pos_to_n(i, rank);
-                buf[sx(i)] = make_float2(ds[n], raws[n]);
+                sh.theta[i] = ds[pos_to_n(i, rank)];
             }
             __syncthreads();
         }
+        // buf <- (demod, raw envelope |Re z[n-4]|)
+        {
+            float dv[32], rv[32];
+#pragma unroll
+            for (int t = 0; t < 32; t++) {
+                int i = tid + t * T;
+                int il = i & 8191;
+                int c = 2 * (i >> 13) + rank;
+                int plc = ((c + 3) & 3) >> 1;
+                dv[t] = sh.theta[i];
+                float re = (il >= 4) ? buf[sx(i - 4)].x : rsh->tail_re[plc][il];
+                rv[t] = fabsf(re);
+            }
+            __syncthreads();
+#pragma unroll
+            for (int t = 0; t < 32; t++) buf[sx(tid + t * T)] = make_float2(dv[t], rv[t]);
+        }
+        cluster.sync();   // the envelope halos read the partner's buf
         // ---------------- envelope: filtfilt with halo-started warp scans --
         // Warp w of this rank covers samples [n0, n0 + 1024) as four rows of
         // 256; in each row lane l runs the recurrence over its 8 consecutive

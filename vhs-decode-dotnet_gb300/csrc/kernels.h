@@ -28,8 +28,7 @@ struct FastDemodParams {
     float* video_out;          // stitched stream, stream index s = b*30720 + n - 1024
     float* sync_out;
     float* env_out;
-    float2* scratch;           // repair scratch: per cluster 2*32768 float2
-    float* scratch_raw;        // repair scratch: per cluster 32768 float
+    float2* scratch;           // repair scratch: per cluster 2*32768 float2 (demod, diff-demod, spike mask, thresholds)
     int* repair_count;         // counts blocks that took the spike-repair path
 };
 

@@ -139,7 +139,6 @@ struct vhsdecode_gb300_session {
     DevBuf<double> rfv64;
     DevBuf<double2> vid64, syn64;
     DevBuf<float2> scratch;
-    DevBuf<float> scratch_raw;
     DevBuf<int> repair;
     DevBuf<double2> pwork;
     DevBuf<double> pdwork;

@@ -12,6 +12,7 @@
 #include "control.hpp"
 #include "kernels.h"
 #include "vhs_math.cuh"
+#include "spikes.cuh"
 
 namespace vhsd {
 template <typename T>
@@ -30,6 +31,24 @@ __global__ void k_demod(const float* re, const float* im, int64_t n, float freq,
     if (i >= n) return;
     if (i == 0) { out[0] = 0.0f; return; }
     out[i] = vhs_freq_diff(vhs_atan2(im[i], re[i]), vhs_atan2(im[i - 1], re[i - 1]), freq);
+}
+
+// ReplaceSpikes of a whole array on one CTA with the block demodulator's
+// parallel form; n a multiple of 32.
+__global__ void k_replace_spikes_test(float* demod, const float* diffed, unsigned* mask, int* cpos, int n,
+                                      float max_value) {
+    extern __shared__ unsigned repl[];
+    const int lane = threadIdx.x & 31;
+    for (int base = (threadIdx.x >> 5) * 32; base < n; base += blockDim.x) {
+        unsigned m = __ballot_sync(0xffffffffu, demod[base + lane] > max_value);
+        if (lane == 0) mask[base >> 5] = m;
+    }
+    __syncthreads();
+    spike_thresholds(demod, diffed, mask, cpos, n, threadIdx.x, blockDim.x);
+    __syncthreads();
+    if (threadIdx.x < 32) spike_walk(mask, cpos, repl, n, lane);
+    __syncthreads();
+    spike_apply(demod, diffed, repl, n, threadIdx.x, blockDim.x);
 }
 
 __global__ void k_angles(const float* re, const float* im, int64_t n, float* out) {
@@ -105,6 +124,27 @@ VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_vhs_demod(
     k_demod<<<(unsigned)((n + 255) / 256), 256>>>(dre, dim, (int64_t)n, (float)sample_rate_hz, dout);
     CUDA_OR_RETURN(cudaGetLastError(), "launch");
     CUDA_OR_RETURN(cudaMemcpy(out, dout, n * sizeof(float), cudaMemcpyDeviceToHost), "d2h");
+    return set_last_error(VHSDECODE_GB300_STATUS_OK, "");
+}
+
+VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_replace_spikes(
+    float* demod, const float* diffed, uint64_t n, float max_value) {
+    if ((!demod || !diffed) && n) return set_last_error(VHSDECODE_GB300_STATUS_NULL_POINTER, "null argument");
+    if (n % 32 != 0 || n > (1u << 20))
+        return set_last_error(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "n must be a multiple of 32, at most 2^20");
+    if (!have_device()) return set_last_error(VHSDECODE_GB300_STATUS_CUDA_UNAVAILABLE, "no CUDA device available");
+    if (n == 0) return set_last_error(VHSDECODE_GB300_STATUS_OK, "");
+    Scoped sc;
+    float* dd = sc.alloc<float>(n);
+    float* df = sc.alloc<float>(n);
+    unsigned* dm = sc.alloc<unsigned>(n / 32);
+    int* dc = sc.alloc<int>(n);
+    if (!dd || !df || !dm || !dc) return set_last_error(VHSDECODE_GB300_STATUS_INTERNAL_ERROR, "cudaMalloc failed");
+    CUDA_OR_RETURN(cudaMemcpy(dd, demod, n * sizeof(float), cudaMemcpyHostToDevice), "h2d");
+    CUDA_OR_RETURN(cudaMemcpy(df, diffed, n * sizeof(float), cudaMemcpyHostToDevice), "h2d");
+    k_replace_spikes_test<<<1, 512, (n / 32) * sizeof(unsigned)>>>(dd, df, dm, dc, (int)n, max_value);
+    CUDA_OR_RETURN(cudaGetLastError(), "launch");
+    CUDA_OR_RETURN(cudaMemcpy(demod, dd, n * sizeof(float), cudaMemcpyDeviceToHost), "d2h");
     return set_last_error(VHSDECODE_GB300_STATUS_OK, "");
 }
 

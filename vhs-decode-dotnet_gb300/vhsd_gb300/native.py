@@ -46,7 +46,7 @@ EXPORTS = [
     "vhsdecode_gb300_find_pulses", "vhsdecode_gb300_vhs_angles",
     "vhsdecode_gb300_pulse_events_noalloc", "vhsdecode_gb300_vhs_demod",
     "vhsdecode_gb300_server_create", "vhsdecode_gb300_server_submit", "vhsdecode_gb300_server_wait",
-    "vhsdecode_gb300_server_destroy",
+    "vhsdecode_gb300_server_destroy", "vhsdecode_gb300_replace_spikes",
 ]
 
 
@@ -188,6 +188,7 @@ def load(path: str = LIB_PATH):
                                               _P(ctypes.c_uint64)]
     L.vhsdecode_gb300_vhs_angles.argtypes = [_vp, _vp, ctypes.c_uint64, _vp]
     L.vhsdecode_gb300_vhs_demod.argtypes = [_vp, _vp, ctypes.c_uint64, ctypes.c_double, _vp]
+    L.vhsdecode_gb300_replace_spikes.argtypes = [_vp, _vp, ctypes.c_uint64, ctypes.c_float]
     L.vhsdecode_gb300_server_create.argtypes = [_P(ServerConfig), _P(_vp)]
     L.vhsdecode_gb300_server_submit.argtypes = [_vp, _P(Window), _P(ctypes.c_uint64)]
     L.vhsdecode_gb300_server_wait.argtypes = [_vp, ctypes.c_uint64, _P(WindowResult)]
@@ -293,6 +294,13 @@ def vhs_demod(re, im, fs):
     out = np.zeros(len(re), np.float32)
     check(load().vhsdecode_gb300_vhs_demod(_ptr(re), _ptr(im), len(re), float(fs), _ptr(out)))
     return out
+
+
+def replace_spikes(demod, diffed, max_value):
+    d = np.ascontiguousarray(demod, np.float32).copy()
+    f = np.ascontiguousarray(diffed, np.float32)
+    check(load().vhsdecode_gb300_replace_spikes(_ptr(d), _ptr(f), len(d), float(max_value)))
+    return d
 
 
 class Session:
