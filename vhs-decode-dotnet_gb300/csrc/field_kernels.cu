@@ -79,22 +79,32 @@ __global__ void k_pulse_pass(const T* __restrict__ ref, int64_t begin, int64_t n
     st = __shfl_sync(0xffffffffu, st, 0);
     int64_t off = WRITE ? offsets[wg] : 0;
     int64_t cnt = 0;
-    for (int it = 0; it < kPWarpSamples / 32; it++) {
-        int64_t p = start + it * 32 + lane;
-        bool inb = p < n;
-        T v = inb ? ref[p] : (T)0;
-        bool hold = !inb || !(v == v);
-        bool c = inb && (v <= cmp.h);
-        unsigned cm = __ballot_sync(0xffffffffu, c);
-        unsigned hm = __ballot_sync(0xffffffffu, hold);
-        unsigned e = edge_bits(cm, hm, st);
-        if (WRITE && ((e >> lane) & 1u)) {
-            int64_t o = off + __popc(e & ((1u << lane) - 1u));
-            if (o < capacity) events[o] = 2 * p + (c ? 0 : 1);
+    // eight loads in flight per lane, then the ballots in order
+    for (int it0 = 0; it0 < kPWarpSamples / 32; it0 += 8) {
+        T vv[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            int64_t p = start + (it0 + j) * 32 + lane;
+            vv[j] = p < n ? ref[p] : (T)0;
         }
-        int pc = __popc(e);
-        off += pc;
-        cnt += pc;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            int64_t p = start + (it0 + j) * 32 + lane;
+            bool inb = p < n;
+            T v = vv[j];
+            bool hold = !inb || !(v == v);
+            bool c = inb && (v <= cmp.h);
+            unsigned cm = __ballot_sync(0xffffffffu, c);
+            unsigned hm = __ballot_sync(0xffffffffu, hold);
+            unsigned e = edge_bits(cm, hm, st);
+            if (WRITE && ((e >> lane) & 1u)) {
+                int64_t o = off + __popc(e & ((1u << lane) - 1u));
+                if (o < capacity) events[o] = 2 * p + (c ? 0 : 1);
+            }
+            int pc = __popc(e);
+            off += pc;
+            cnt += pc;
+        }
     }
     if (!WRITE && lane == 0) counts[wg] = cnt;
 }
@@ -721,8 +731,17 @@ __global__ void __launch_bounds__(256) k_tbc_fast(const float* stream, int64_t s
     const float4* lut4 = reinterpret_cast<const float4*>(p.lut);
     const float4* pair4 = reinterpret_cast<const float4*>(p.lut_pair);
     uint16_t* out = p.out_u16 + ((int64_t)f * p.out_lines + ol) * p.outlen;
-    for (int k = threadIdx.x; k < p.outlen; k += blockDim.x) {
-        const float kf = (float)k;
+    // Each lane owns one output sample (position, level and conversion done
+    // once); the 16-tap sums are gathered cooperatively: in round r the quad
+    // q of lanes works on the sample of lane 8 r + q, lane `sub` reading taps
+    // 4 sub .. 4 sub + 3, so a sample's 128-byte row pair is read by one
+    // quad in two coalesced accesses instead of eight scattered ones.
+    const int lane = threadIdx.x & 31;
+    const int q = lane >> 2, sub = lane & 3;
+    for (int k0 = 0; k0 < p.outlen; k0 += blockDim.x) {
+        const int k = k0 + threadIdx.x;
+        const bool valid = k < p.outlen;
+        const float kf = (float)(valid ? k : 0);
         float2 kb = ff_mul(kf, 0.0f, c.b.x, c.b.y);
         float2 pos = ff_add(c.a.x, c.a.y, kb.x, kb.y);
         float coord = __fadd_rn(pos.x, pos.y);
@@ -734,30 +753,34 @@ __global__ void __launch_bounds__(256) k_tbc_fast(const float* stream, int64_t s
         float alpha = __fsub_rn(pp, (float)ps);
         ps = wrap_idx(ps, 65537);
         pe = wrap_idx(pe, 65537);
-        const float4* rs;
-        const float4* re;
-        if (pe == ps + 1 && pair4) {
-            rs = pair4 + (int64_t)ps * 8;
-            re = rs + 4;
-        } else {
-            rs = lut4 + (int64_t)ps * 4;
-            re = lut4 + (int64_t)pe * 4;
-        }
-        int start = ci - 7;
-        bool interior = n >= 16 && (uint32_t)start <= (uint32_t)(n - 16);
-        float hi = 0.0f, lo = 0.0f;
+        const int start = ci - 7;
+        const int interior = (n >= 16 && (uint32_t)start <= (uint32_t)(n - 16)) ? 1 : 0;
+        float hi_own = 0.0f, lo_own = 0.0f;
 #pragma unroll
-        for (int q = 0; q < 4; q++) {
-            float4 ws = __ldg(rs + q);
-            float4 we = __ldg(re + q);
-            float wsv[4] = {ws.x, ws.y, ws.z, ws.w};
-            float wev[4] = {we.x, we.y, we.z, we.w};
+        for (int rnd = 0; rnd < 4; rnd++) {
+            const int owner = rnd * 8 + q;
+            const int ps_o = __shfl_sync(0xffffffffu, ps, owner);
+            const int pe_o = __shfl_sync(0xffffffffu, pe, owner);
+            const int st_o = __shfl_sync(0xffffffffu, start, owner);
+            const float al_o = __shfl_sync(0xffffffffu, alpha, owner);
+            const int in_o = __shfl_sync(0xffffffffu, interior, owner);
+            float4 ws, we;
+            if (pe_o == ps_o + 1 && pair4) {
+                const float4* rs = pair4 + (int64_t)ps_o * 8;
+                ws = __ldg(rs + sub);
+                we = __ldg(rs + 4 + sub);
+            } else {
+                ws = __ldg(lut4 + (int64_t)ps_o * 4 + sub);
+                we = __ldg(lut4 + (int64_t)pe_o * 4 + sub);
+            }
+            const float wsv[4] = {ws.x, ws.y, ws.z, ws.w};
+            const float wev[4] = {we.x, we.y, we.z, we.w};
+            float hi = 0.0f, lo = 0.0f;
 #pragma unroll
             for (int r = 0; r < 4; r++) {
-                int t = 4 * q + r;
-                float wt = __fmaf_rn(alpha, __fsub_rn(wev[r], wsv[r]), wsv[r]);
-                int64_t idx = (int64_t)start + t;
-                if (!interior) {
+                float wt = __fmaf_rn(al_o, __fsub_rn(wev[r], wsv[r]), wsv[r]);
+                int64_t idx = (int64_t)st_o + 4 * sub + r;
+                if (!in_o) {
                     if (idx < 0) idx += n;
                     idx = idx < 0 ? 0 : (idx > n - 1 ? n - 1 : idx);
                 }
@@ -767,14 +790,27 @@ __global__ void __launch_bounds__(256) k_tbc_fast(const float* stream, int64_t s
                 hi = s;
                 lo = __fadd_rn(lo, e);
             }
+#pragma unroll
+            for (int o = 1; o < 4; o <<= 1) {
+                float oh = __shfl_xor_sync(0xffffffffu, hi, o);
+                float olo = __shfl_xor_sync(0xffffffffu, lo, o);
+                float2 t = ff_add(hi, lo, oh, olo);
+                hi = t.x;
+                lo = t.y;
+            }
+            // the owners of this round (lanes 8 rnd .. 8 rnd + 7) take their sums
+            const float rh = __shfl_sync(0xffffffffu, hi, 4 * (lane & 7));
+            const float rl = __shfl_sync(0xffffffffu, lo, 4 * (lane & 7));
+            if ((lane >> 3) == rnd) { hi_own = rh; lo_own = rl; }
         }
+        if (!valid) continue;
         float2 la = c.adj;
         if (c.smooth) {
             float2 pw = p.pw_ff[k];
             float2 t = ff_mul(pw.x, pw.y, c.dlev.x, c.dlev.y);
             la = ff_add(c.adj.x, c.adj.y, t.x, t.y);
         }
-        float2 v = ff_mul(hi, lo, la.x, la.y);
+        float2 v = ff_mul(hi_own, lo_own, la.x, la.y);
         float outf = __fadd_rn(v.x, v.y);
         if (!isfinite(outf)) {
             out[k] = outf > 0.0f ? 65535 : 0;
@@ -924,19 +960,30 @@ __global__ void __launch_bounds__(kDT) k_drop_events(const T* stream, int64_t st
     flags(base - 1, pa, pb);
     unsigned sa = pa ? 1u : 0u, sb = pb ? 1u : 0u;
     int cnt = 0, iters = 0;
-    for (int it = 0; it < kDIter; it++) {
-        int64_t i0 = base + it * 32;
-        if (i0 > r1) break;
-        bool a, b;
-        flags(i0 + lane, a, b);
-        unsigned A = __ballot_sync(0xffffffffu, a), B = __ballot_sync(0xffffffffu, b);
-        unsigned ea = A ^ ((A << 1) | sa);
-        unsigned eb = B & ~((B << 1) | sb);
-        sa = A >> 31;
-        sb = B >> 31;
-        if (lane == 0) { masks[w][it][0] = ea; masks[w][it][1] = A & ea; masks[w][it][2] = eb; }
-        cnt += __popc(ea) + __popc(eb);
-        iters = it + 1;
+    // eight loads in flight per lane, then the ballots in order
+    for (int it0 = 0; it0 < kDIter; it0 += 8) {
+        if (base + it0 * 32 > r1) break;
+        T v[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            int64_t i = base + (it0 + j) * 32 + lane;
+            v[j] = (i >= r0 && i < r1) ? env[i] : (T)0;
+        }
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            int it = it0 + j;
+            int64_t i = base + it * 32 + lane;
+            bool in = i >= r0 && i < r1;
+            bool a = in && v[j] <= th.down, b = in && v[j] >= th.up;
+            unsigned A = __ballot_sync(0xffffffffu, a), B = __ballot_sync(0xffffffffu, b);
+            unsigned ea = A ^ ((A << 1) | sa);
+            unsigned eb = B & ~((B << 1) | sb);
+            sa = A >> 31;
+            sb = B >> 31;
+            if (lane == 0) { masks[w][it][0] = ea; masks[w][it][1] = A & ea; masks[w][it][2] = eb; }
+            cnt += __popc(ea) + __popc(eb);
+        }
+        iters = it0 + 8;
     }
     if (lane == 0) wtot[w] = cnt;
     __syncthreads();
