@@ -305,89 +305,338 @@ struct LineInfo {
     int pad;
 };
 
+// Cooperative warp primitives for the line stage: the warp works on one
+// line's samples at a time (parameters broadcast from the line's lane); the
+// binary64 arithmetic of all 32 lines then runs lane-parallel, one line per
+// lane, so no FP64 instruction is repeated across lanes.
+
+// index of the first crossing of `th` in (start, min(n, start + count + 1)), -1 if none
 template <typename T>
-__global__ void k_hsync_lines(const T* stream, int64_t stream_len, HsyncParams p, LineInfo* info) {
-    const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (gw >= (int64_t)p.nfields * p.lines) return;
-    const int f = (int)(gw / p.lines), line = (int)(gw % p.lines);
-    const int64_t s0 = p.span_start[f];
-    Span<T> sp{stream + s0, min(p.span_len[f], stream_len - s0)};
-    const double loc = p.locs_in[gw];
-    const int one = p.one_us, normal = p.normal_hsync;
-    const int search = one * 2 > 1 ? one * 2 : 1;
-    auto ire_hz = [&](double ire) { return p.ire0 + p.hz_ire * ire; };
-    LineInfo li;
-    li.loc = loc;
-    li.crossing = li.sync = li.own_porch = li.rc_own = li.rc_spec = li.r_porch = li.r_cand = nan("");
-    li.ss = 0;
-    li.pad = 0;
-    int flags = p.filled_in[gw] ? 32 : 0;
-    bool vsync_line = (line >= 3 && line <= 6) || (p.pal && line >= 1 && line <= 2);
-    if (vsync_line) flags |= 1;
-    int64_t ss = isfinite(loc) ? (int64_t)round_away(loc - one) : -1;
-    if (!vsync_line && isfinite(loc) && ss >= 0 && ss < sp.n - 1) {
-        flags |= 2;
-        li.ss = ss;
-        int cnt = (int)min((int64_t)search, sp.n - ss - 1);
-        double crossing = zero_crossing(sp, ss, p.threshold, 0, cnt, lane);
-        li.crossing = crossing;
-        if (crossing == crossing) {
-            double sync_lv = 0.0, porch = 0.0;
-            if (area_ok(sp, crossing, one, 3.5, ire_hz(-65.0), ire_hz(110.0), lane) &&
-                mean_range(sp, crossing + one, crossing + 2.5 * one, &sync_lv, lane)) {
-                flags |= 4;
-                li.sync = sync_lv;
-                if (mean_range(sp, crossing - one, crossing - 0.5 * one, &porch, lane)) {
-                    flags |= 8;
-                    li.own_porch = porch;
-                    int c2 = (int)min((int64_t)400, sp.n - ss - 1);
-                    li.rc_own = zero_crossing(sp, ss, (porch + sync_lv) / 2.0, 0, c2, lane);
-                }
-            }
-        }
-        // right edge (independent of the carried porch level)
-        int64_t rs = ss + normal - one;
-        if (rs >= 0 && rs < sp.n - 1 && !(sp.at(rs) > p.threshold)) {
-            int rcnt = (int)min((int64_t)max(1, normal * 2), sp.n - rs - 1);
-            double rcx = zero_crossing(sp, rs, p.threshold, 1, rcnt, lane);
-            if (rcx == rcx) {
-                double derived = rcx - normal;
-                double sync_lv = 0.0, porch = 0.0;
-                if (area_ok(sp, derived, one, 8.0, ire_hz(-65.0), ire_hz(30.0), lane) &&
-                    mean_range(sp, derived + one, derived + 2.5 * one, &sync_lv, lane) &&
-                    mean_range(sp, derived + normal + one, derived + normal + 2.0 * one, &porch, lane)) {
-                    int c2 = (int)min((int64_t)400, sp.n - rs - 1);
-                    double rr = zero_crossing(sp, rs, (porch + sync_lv) / 2.0, 0, c2, lane);
-                    if (rr == rr && fabs(rr - rcx) < one / 2.0) {
-                        flags |= 16;
-                        li.r_porch = porch;
-                        li.r_cand = rcx - normal + 2.25 * (p.mhz32 / 40.0);
-                    }
-                }
-            }
-        }
+__device__ int64_t coop_first_crossing(const T* d, int64_t n, int64_t start, Thr<T> th, int edge, int count,
+                                       int lane) {
+    if (edge == 0) edge = d[start] < th.hi ? 1 : -1;
+    int64_t end = min(n, start + (int64_t)count + 1);
+    int64_t len = end - start;
+    for (int64_t base = 1; base < len; base += 32) {
+        int64_t i = base + lane;
+        T b = i < len ? d[start + i] : (T)0;
+        T a = __shfl_up_sync(0xffffffffu, b, 1);
+        if (lane == 0) a = d[start + base - 1];
+        bool hit = false;
+        if (i < len) hit = edge == 1 ? (a < th.hi && b >= th.hi) : (a > th.lo && b <= th.lo);
+        unsigned m = __ballot_sync(0xffffffffu, hit);
+        if (m) return start + base + (__ffs(m) - 1);
     }
-    li.flags = flags;
-    if (lane == 0) info[gw] = li;
+    return -1;
+}
+
+// PulseDetection.CalculateZeroCrossing's interpolation at a found crossing x
+template <typename T>
+__device__ __forceinline__ double crossing_at(const T* d, int64_t x, double target) {
+    double a = (double)d[x - 1] - target;
+    double b = (double)d[x] - target;
+    double y = (b - a) != 0.0 ? -a / (-a + b) : 0.0;
+    return (double)(x - 1) + y;
 }
 
 template <typename T>
-__global__ void k_hsync_spec(const T* stream, int64_t stream_len, HsyncParams p, LineInfo* info) {
-    const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (gw >= (int64_t)p.nfields * p.lines) return;
-    const int line = (int)(gw % p.lines);
-    if (line == 0) return;
-    LineInfo& li = info[gw];
-    const LineInfo& prev = info[gw - 1];
-    if (!(li.flags & 4) || !(prev.flags & 16) || !(prev.r_porch > 0.0)) return;
-    const int f = (int)(gw / p.lines);
-    const int64_t s0 = p.span_start[f];
-    Span<T> sp{stream + s0, min(p.span_len[f], stream_len - s0)};
-    int c2 = (int)min((int64_t)400, sp.n - li.ss - 1);
-    double rc = zero_crossing(sp, li.ss, (prev.r_porch + li.sync) / 2.0, 0, c2, lane);
-    if (lane == 0) li.rc_spec = rc;
+__device__ void coop_minmax(const T* d, int64_t st, int64_t en, T& mn, T& mx, int lane) {
+    mn = (T)INFINITY;
+    mx = (T)-INFINITY;
+    for (int64_t i = st + lane; i < en; i += 32) {
+        T v = d[i];
+        mn = fmin(mn, v);
+        mx = fmax(mx, v);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+        mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    }
+}
+
+__device__ __forceinline__ void pair_add(float& hi, float& lo, float oh, float ol) {
+    float s = __fadd_rn(hi, oh);
+    float bb = __fsub_rn(s, hi);
+    float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(oh, bb));
+    e = __fadd_rn(e, __fadd_rn(lo, ol));
+    hi = __fadd_rn(s, e);
+    lo = __fsub_rn(e, __fsub_rn(hi, s));
+}
+__device__ __forceinline__ double coop_total(const float* d, int64_t st, int64_t en, int lane) {
+    float hi = 0.0f, lo = 0.0f;
+    for (int64_t i = st + lane; i < en; i += 32) pair_add(hi, lo, d[i], 0.0f);
+    for (int o = 16; o > 0; o >>= 1)
+        pair_add(hi, lo, __shfl_xor_sync(0xffffffffu, hi, o), __shfl_xor_sync(0xffffffffu, lo, o));
+    return (double)hi + (double)lo;
+}
+__device__ __forceinline__ double coop_total(const double* d, int64_t st, int64_t en, int lane) {
+    double acc = 0.0;
+    for (int64_t i = st + lane; i < en; i += 32) acc += d[i];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    return acc;
+}
+
+// [round(start), round(end)) clipped to [0, n]
+__device__ __forceinline__ void range_of(double start, double end, int64_t n, int64_t& st, int64_t& en) {
+    st = (int64_t)round_away(start);
+    st = st < 0 ? 0 : (st > n ? n : st);
+    en = (int64_t)round_away(end);
+    en = en < st ? st : (en > n ? n : en);
+}
+
+// Per-line state of the line stage, shared between the line's search warp
+// and the lane of warp 0 that does the line's binary64 arithmetic.
+struct LineWork {
+    int64_t s0, n, ss, rs;
+    int64_t x[4];            // crossings found: threshold, own midpoint, right edge, right midpoint
+    int64_t r[12];           // ranges: area, sync, porch (left); area, sync, porch (right)
+    double sum[4];           // left sync, left porch, right sync, right porch
+    float mn[2], mx[2];      // area extrema (left, right), float streams
+    double mnd[2], mxd[2];   // area extrema, double streams
+    float tlo[2], thi[2];    // midpoint thresholds (own, right), float form
+    double tlod[2], thid[2];
+    int cnt[4];
+    int want;                // bit k: search / reduction k requested
+};
+
+template <typename T>
+__device__ __forceinline__ void store_extrema(LineWork& w, int k, T mn, T mx);
+template <>
+__device__ __forceinline__ void store_extrema<float>(LineWork& w, int k, float mn, float mx) { w.mn[k] = mn; w.mx[k] = mx; }
+template <>
+__device__ __forceinline__ void store_extrema<double>(LineWork& w, int k, double mn, double mx) { w.mnd[k] = mn; w.mxd[k] = mx; }
+__device__ __forceinline__ double ext_min(const LineWork& w, int k, const float*) { return (double)w.mn[k]; }
+__device__ __forceinline__ double ext_max(const LineWork& w, int k, const float*) { return (double)w.mx[k]; }
+__device__ __forceinline__ double ext_min(const LineWork& w, int k, const double*) { return w.mnd[k]; }
+__device__ __forceinline__ double ext_max(const LineWork& w, int k, const double*) { return w.mxd[k]; }
+__device__ __forceinline__ void store_thr(LineWork& w, int k, Thr<float> t) { w.tlo[k] = t.lo; w.thi[k] = t.hi; }
+__device__ __forceinline__ void store_thr(LineWork& w, int k, Thr<double> t) { w.tlod[k] = t.lo; w.thid[k] = t.hi; }
+__device__ __forceinline__ Thr<float> load_thr(const LineWork& w, int k, const float*) { return {w.tlo[k], w.thi[k]}; }
+__device__ __forceinline__ Thr<double> load_thr(const LineWork& w, int k, const double*) { return {w.tlod[k], w.thid[k]}; }
+
+// 32 lines per CTA of 32 warps: warp w runs the sample searches and
+// reductions of line w (the 32 lines proceed concurrently); warp 0 runs the
+// binary64 arithmetic of all 32 lines lane-parallel between the phases.
+// Per line: threshold crossing from round(loc - 1 us), area and level checks,
+// own-porch midpoint crossing, and the right-edge candidate -- the per-line
+// part of RefineLineLocationsFromHSync.
+template <typename T>
+__global__ void __launch_bounds__(1024) k_hsync_lines(const T* stream, int64_t stream_len, HsyncParams p,
+                                                      LineInfo* info) {
+    __shared__ LineWork lw[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t total = (int64_t)p.nfields * p.lines;
+    const int one = p.one_us, normal = p.normal_hsync;
+    const int search = one * 2 > 1 ? one * 2 : 1;
+    auto ire_hz = [&](double ire) { return p.ire0 + p.hz_ire * ire; };
+    const Thr<T> th0 = make_thr(p.threshold, (const T*)nullptr);
+    // warp 0, lane l <-> line g = 32 blockIdx + l
+    const int64_t g = (int64_t)blockIdx.x * 32 + lane;
+    const bool have = g < total;
+    LineInfo li;
+    double crossing = NAN, rcx = NAN, target_own = 0.0, target_r = 0.0, r_porch = 0.0;
+    int flags = 0;
+    bool usable = false;
+    if (warp == 0) {
+        const int f = have ? (int)(g / p.lines) : 0;
+        const int line = have ? (int)(g % p.lines) : 0;
+        const int64_t s0 = have ? p.span_start[f] : 0;
+        const int64_t n = have ? min(p.span_len[f], stream_len - s0) : 0;
+        const double loc = have ? p.locs_in[g] : (double)NAN;
+        li.loc = loc;
+        li.crossing = li.sync = li.own_porch = li.rc_own = li.rc_spec = li.r_porch = li.r_cand = nan("");
+        li.ss = 0;
+        li.pad = 0;
+        flags = (have && p.filled_in[g]) ? 32 : 0;
+        const bool vsync_line = (line >= 3 && line <= 6) || (p.pal && line >= 1 && line <= 2);
+        if (vsync_line) flags |= 1;
+        const int64_t ss = isfinite(loc) ? (int64_t)round_away(loc - one) : -1;
+        usable = have && !vsync_line && isfinite(loc) && ss >= 0 && ss < n - 1;
+        LineWork& w = lw[lane];
+        w.s0 = s0; w.n = n; w.ss = ss; w.want = 0;
+        w.x[0] = w.x[1] = w.x[2] = w.x[3] = -1;
+        if (usable) {
+            flags |= 2;
+            li.ss = ss;
+            w.cnt[0] = (int)min((int64_t)search, n - ss - 1);
+            w.want |= 1;
+            const int64_t rs = ss + normal - one;
+            w.rs = rs;
+            if (rs >= 0 && rs < n - 1 && !((double)stream[s0 + rs] > p.threshold)) {
+                w.cnt[2] = (int)min((int64_t)max(1, normal * 2), n - rs - 1);
+                w.want |= 4;
+            }
+        }
+    }
+    __syncthreads();
+    // phase A: threshold crossings (left, from ss; right edge, rising, from rs)
+    {
+        const LineWork& w = lw[warp];
+        const T* d = stream + w.s0;
+        if (w.want & 1) {
+            int64_t r = coop_first_crossing(d, w.n, w.ss, th0, 0, w.cnt[0], lane);
+            if (lane == 0) lw[warp].x[0] = r;
+        }
+        if (w.want & 4) {
+            int64_t r = coop_first_crossing(d, w.n, w.rs, th0, 1, w.cnt[2], lane);
+            if (lane == 0) lw[warp].x[2] = r;
+        }
+    }
+    __syncthreads();
+    // warp 0: interpolate, derive the level ranges
+    if (warp == 0) {
+        LineWork& w = lw[lane];
+        const T* d = stream + w.s0;
+        w.want &= ~(1 | 4);
+        if (usable) {
+            crossing = w.x[0] >= 0 ? crossing_at(d, w.x[0], p.threshold) : (double)NAN;
+            li.crossing = crossing;
+            if (crossing == crossing) {
+                range_of(crossing - 0.75 * one, crossing + 3.5 * one, w.n, w.r[0], w.r[1]);
+                range_of(crossing + one, crossing + 2.5 * one, w.n, w.r[2], w.r[3]);
+                range_of(crossing - one, crossing - 0.5 * one, w.n, w.r[4], w.r[5]);
+                w.want |= 16;
+            }
+            rcx = w.x[2] >= 0 ? crossing_at(d, w.x[2], p.threshold) : (double)NAN;
+            if (rcx == rcx) {
+                const double derived = rcx - normal;
+                range_of(derived - 0.75 * one, derived + 8.0 * one, w.n, w.r[6], w.r[7]);
+                range_of(derived + one, derived + 2.5 * one, w.n, w.r[8], w.r[9]);
+                range_of(derived + normal + one, derived + normal + 2.0 * one, w.n, w.r[10], w.r[11]);
+                w.want |= 32;
+            }
+        }
+    }
+    __syncthreads();
+    // phase B: area extrema and level sums
+    {
+        const LineWork& w = lw[warp];
+        const T* d = stream + w.s0;
+        for (int side = 0; side < 2; side++) {
+            if (!(w.want & (16 << side))) continue;
+            const int64_t* r = w.r + 6 * side;
+            T mn, mx;
+            coop_minmax(d, r[0], r[1], mn, mx, lane);
+            double s1 = coop_total(d, r[2], r[3], lane);
+            double s2 = coop_total(d, r[4], r[5], lane);
+            if (lane == 0) {
+                store_extrema<T>(lw[warp], side, mn, mx);
+                lw[warp].sum[2 * side] = s1;
+                lw[warp].sum[2 * side + 1] = s2;
+            }
+        }
+    }
+    __syncthreads();
+    // warp 0: level checks, midpoint thresholds
+    if (warp == 0) {
+        LineWork& w = lw[lane];
+        const T* tp = nullptr;
+        if (w.want & 16) {
+            if (w.r[1] > w.r[0] && ext_min(w, 0, tp) >= ire_hz(-65.0) && ext_max(w, 0, tp) <= ire_hz(110.0) &&
+                w.r[3] > w.r[2]) {
+                const double sync_lv = w.sum[0] / (double)(w.r[3] - w.r[2]);
+                flags |= 4;
+                li.sync = sync_lv;
+                if (w.r[5] > w.r[4]) {
+                    const double porch = w.sum[1] / (double)(w.r[5] - w.r[4]);
+                    flags |= 8;
+                    li.own_porch = porch;
+                    target_own = (porch + sync_lv) / 2.0;
+                    store_thr(w, 0, make_thr(target_own, tp));
+                    w.cnt[1] = (int)min((int64_t)400, w.n - w.ss - 1);
+                    w.want |= 2;
+                }
+            }
+        }
+        if (w.want & 32) {
+            if (w.r[7] > w.r[6] && ext_min(w, 1, tp) >= ire_hz(-65.0) && ext_max(w, 1, tp) <= ire_hz(30.0) &&
+                w.r[9] > w.r[8] && w.r[11] > w.r[10]) {
+                const double r_sync = w.sum[2] / (double)(w.r[9] - w.r[8]);
+                r_porch = w.sum[3] / (double)(w.r[11] - w.r[10]);
+                target_r = (r_porch + r_sync) / 2.0;
+                store_thr(w, 1, make_thr(target_r, tp));
+                w.cnt[3] = (int)min((int64_t)400, w.n - w.rs - 1);
+                w.want |= 8;
+            }
+        }
+    }
+    __syncthreads();
+    // phase C: midpoint crossings (own porch from ss; right edge from rs)
+    {
+        const LineWork& w = lw[warp];
+        const T* d = stream + w.s0;
+        if (w.want & 2) {
+            int64_t r = coop_first_crossing(d, w.n, w.ss, load_thr(w, 0, (const T*)nullptr), 0, w.cnt[1], lane);
+            if (lane == 0) lw[warp].x[1] = r;
+        }
+        if (w.want & 8) {
+            int64_t r = coop_first_crossing(d, w.n, w.rs, load_thr(w, 1, (const T*)nullptr), 0, w.cnt[3], lane);
+            if (lane == 0) lw[warp].x[3] = r;
+        }
+    }
+    __syncthreads();
+    if (warp == 0) {
+        const LineWork& w = lw[lane];
+        const T* d = stream + w.s0;
+        if (w.want & 2) li.rc_own = w.x[1] >= 0 ? crossing_at(d, w.x[1], target_own) : (double)NAN;
+        if (w.want & 8) {
+            const double rr = w.x[3] >= 0 ? crossing_at(d, w.x[3], target_r) : (double)NAN;
+            if (rr == rr && fabs(rr - rcx) < one / 2.0) {
+                flags |= 16;
+                li.r_porch = r_porch;
+                li.r_cand = rcx - normal + 2.25 * (p.mhz32 / 40.0);
+            }
+        }
+        li.flags = flags;
+        if (have) info[g] = li;
+    }
+}
+
+// Speculative midpoint crossing for "carried porch = previous line's
+// right-edge porch": 32 lines per CTA, warp w searches line w.
+template <typename T>
+__global__ void __launch_bounds__(1024) k_hsync_spec(const T* stream, int64_t stream_len, HsyncParams p,
+                                                     LineInfo* info) {
+    __shared__ LineWork lw[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t total = (int64_t)p.nfields * p.lines;
+    const int64_t g = (int64_t)blockIdx.x * 32 + lane;
+    double target = 0.0;
+    if (warp == 0) {
+        LineWork& w = lw[lane];
+        w.want = 0;
+        w.x[0] = -1;
+        const bool have = g < total;
+        const int f = have ? (int)(g / p.lines) : 0;
+        const int line = have ? (int)(g % p.lines) : 0;
+        w.s0 = have ? p.span_start[f] : 0;
+        w.n = have ? min(p.span_len[f], stream_len - w.s0) : 0;
+        if (have && line > 0) {
+            const LineInfo& li = info[g];
+            const LineInfo& prev = info[g - 1];
+            if ((li.flags & 4) && (prev.flags & 16) && prev.r_porch > 0.0) {
+                target = (prev.r_porch + li.sync) / 2.0;
+                w.ss = li.ss;
+                store_thr(w, 0, make_thr(target, (const T*)nullptr));
+                w.cnt[0] = (int)min((int64_t)400, w.n - w.ss - 1);
+                w.want = 1;
+            }
+        }
+    }
+    __syncthreads();
+    {
+        const LineWork& w = lw[warp];
+        if (w.want) {
+            int64_t r = coop_first_crossing(stream + w.s0, w.n, w.ss, load_thr(w, 0, (const T*)nullptr), 0,
+                                            w.cnt[0], lane);
+            if (lane == 0) lw[warp].x[0] = r;
+        }
+    }
+    __syncthreads();
+    if (warp == 0 && lw[lane].want) {
+        const LineWork& w = lw[lane];
+        info[g].rc_spec = w.x[0] >= 0 ? crossing_at(stream + w.s0, w.x[0], target) : (double)NAN;
+    }
 }
 
 template <typename T>
@@ -480,9 +729,9 @@ template <typename T>
 cudaError_t launch_hsync_refine(const T* stream, int64_t stream_len, const HsyncParams& p,
                                 cudaStream_t s) {
     if (p.nfields <= 0) return cudaSuccess;
-    const int64_t warps = (int64_t)p.nfields * p.lines;
-    const int threads = 256;
-    const unsigned blocks = (unsigned)((warps * 32 + threads - 1) / threads);
+    const int64_t lines = (int64_t)p.nfields * p.lines;   // 32 lines per CTA of 32 warps
+    const int threads = 1024;
+    const unsigned blocks = (unsigned)((lines + 31) / 32);
     LineInfo* info = reinterpret_cast<LineInfo*>(p.work);
     k_hsync_lines<T><<<blocks, threads, 0, s>>>(stream, stream_len, p, info);
     k_hsync_spec<T><<<blocks, threads, 0, s>>>(stream, stream_len, p, info);
