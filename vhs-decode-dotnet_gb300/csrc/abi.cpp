@@ -495,6 +495,10 @@ void launch_field_batch(vhsdecode_gb300_session* s, int f0, int f1, const T* vid
     hp.ntsc_shift = sp.pal ? 0.0 : ((117.25 / 360.0) / sp.fsc_mhz) * sp.mhz;
     hp.work = s->hsync_work.p + hsync_work_bytes(f0, s->lines);
     hp.misses = nullptr;
+    if (s->stage_timing) {
+        ck(cudaMemsetAsync(s->hsync_misses.p, 0, sizeof(int), fs), "memset");
+        hp.misses = s->hsync_misses.p;
+    }
     const bool timing = s->stage_timing;
     if (timing) ck(cudaEventRecord(s->stage_ev[0], fs), "event");
     ck(launch_hsync_refine<T>(sync, stream_len, hp, fs), "hsync launch");
@@ -594,10 +598,13 @@ void collect_field_results(vhsdecode_gb300_session* s, cudaStream_t fs) {
         const int32_t* src = drops.data() + (size_t)f * maxc * 3;
         r.drop.assign(src, src + (size_t)c * 3);
     }
-    if (s->stage_timing)
+    if (s->stage_timing) {
+        int miss = 0;
+        ck(cudaMemcpy(&miss, s->hsync_misses.p, sizeof(int), cudaMemcpyDeviceToHost), "d2h");
         std::fprintf(stderr, "[gb300 stage] fields=%d hsync=%.3f ms tbc=%.3f ms dropouts=%.3f ms "
-                     "rescue_fetches=%d enqueue=%.3f ms segments=%u\n", nf, s->stage_ms[0], s->stage_ms[1],
-                     s->stage_ms[2], s->rescue_fetches, s->enqueue_ms, s->segments);
+                     "rescue_fetches=%d enqueue=%.3f ms segments=%u porch_misses=%d\n", nf, s->stage_ms[0],
+                     s->stage_ms[1], s->stage_ms[2], s->rescue_fetches, s->enqueue_ms, s->segments, miss);
+    }
 }
 
 // Segment boundaries (in blocks) of the pipelined decode: a short first

@@ -213,29 +213,18 @@ __device__ __forceinline__ Thr<float> make_thr(double t, const float*) {
 
 // first crossing of `target` at/after `start` within count+1 samples; NaN if none
 template <typename T>
+__device__ int64_t coop_first_crossing(const T* d, int64_t n, int64_t start, Thr<T> th, int edge, int count,
+                                       int lane);
+template <typename T>
 __device__ double zero_crossing(const Span<T>& s, int64_t start, double target, int edge, int count,
                                 int lane) {
     const Thr<T> th = make_thr(target, (const T*)nullptr);
-    if (edge == 0) edge = s.d[start] < th.hi ? 1 : -1;
-    int64_t end = min(s.n, start + (int64_t)count + 1);
-    int64_t len = end - start;
-    for (int64_t base = 1; base < len; base += 32) {
-        int64_t i = base + lane;
-        T b = i < len ? s.d[start + i] : (T)0;
-        T a = __shfl_up_sync(0xffffffffu, b, 1);
-        if (lane == 0) a = s.d[start + base - 1];
-        bool hit = false;
-        if (i < len) hit = edge == 1 ? (a < th.hi && b >= th.hi) : (a > th.lo && b <= th.lo);
-        unsigned m = __ballot_sync(0xffffffffu, hit);
-        if (m) {
-            int64_t x = start + base + (__ffs(m) - 1);
-            double av = s.at(x - 1) - target;
-            double bv = s.at(x) - target;
-            double y = (bv - av) != 0.0 ? -av / (-av + bv) : 0.0;
-            return (double)(x - 1) + y;
-        }
-    }
-    return nan("");
+    int64_t x = coop_first_crossing(s.d, s.n, start, th, edge, count, lane);
+    if (x < 0) return nan("");
+    double a = s.at(x - 1) - target;
+    double b = s.at(x) - target;
+    double y = (b - a) != 0.0 ? -a / (-a + b) : 0.0;
+    return (double)(x - 1) + y;
 }
 
 template <typename T>
@@ -302,8 +291,20 @@ struct LineInfo {
     int64_t ss;      // search start
     int flags;       // bit0 vsync line, bit1 usable (finite, ss in range), bit2 area+sync ok,
                      // bit3 own porch valid, bit4 right candidate valid, bit5 filled in
-    int pad;
+    int pre;         // comparisons precomputed for the chain (kPre* bits)
 };
+
+// LineInfo::pre bits: the chain's binary64 comparisons that do not depend on
+// the carried porch, evaluated lane-parallel by the line and spec kernels.
+constexpr int kPreCross = 1;       // crossing is a number
+constexpr int kPreOwnOk = 2;       // rc_own is a number and within 1/2 us of the crossing
+constexpr int kPreSpecOk = 4;      // rc_spec is a number and within 1/2 us of the crossing
+constexpr int kPreNearOwn = 8;     // right candidate within 2 us of rc_own
+constexpr int kPreNearSpec = 16;   // ... of rc_spec
+constexpr int kPreNearCross = 32;  // ... of the crossing
+constexpr int kPreNearLoc = 64;    // ... of the input location
+constexpr int kPreOwnPos = 128;    // own porch > 0
+constexpr int kPreRPos = 256;      // right porch > 0
 
 // Cooperative warp primitives for the line stage: the warp works on one
 // line's samples at a time (parameters broadcast from the line's lane); the
@@ -311,21 +312,33 @@ struct LineInfo {
 // lane, so no FP64 instruction is repeated across lanes.
 
 // index of the first crossing of `th` in (start, min(n, start + count + 1)), -1 if none
+// (128 samples per step: four chunks of 32 are loaded before any is tested)
 template <typename T>
 __device__ int64_t coop_first_crossing(const T* d, int64_t n, int64_t start, Thr<T> th, int edge, int count,
                                        int lane) {
     if (edge == 0) edge = d[start] < th.hi ? 1 : -1;
     int64_t end = min(n, start + (int64_t)count + 1);
     int64_t len = end - start;
-    for (int64_t base = 1; base < len; base += 32) {
-        int64_t i = base + lane;
-        T b = i < len ? d[start + i] : (T)0;
-        T a = __shfl_up_sync(0xffffffffu, b, 1);
-        if (lane == 0) a = d[start + base - 1];
-        bool hit = false;
-        if (i < len) hit = edge == 1 ? (a < th.hi && b >= th.hi) : (a > th.lo && b <= th.lo);
-        unsigned m = __ballot_sync(0xffffffffu, hit);
-        if (m) return start + base + (__ffs(m) - 1);
+    for (int64_t base0 = 1; base0 < len; base0 += 128) {
+        T bv[4], av[4];
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            int64_t i = base0 + 32 * c + lane;
+            bv[c] = i < len ? d[start + i] : (T)0;
+            av[c] = (lane == 0 && base0 + 32 * c < len) ? d[start + base0 + 32 * c - 1] : (T)0;
+        }
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            int64_t base = base0 + 32 * c;
+            int64_t i = base + lane;
+            T b = bv[c];
+            T a = __shfl_up_sync(0xffffffffu, b, 1);
+            if (lane == 0) a = av[c];
+            bool hit = false;
+            if (i < len) hit = edge == 1 ? (a < th.hi && b >= th.hi) : (a > th.lo && b <= th.lo);
+            unsigned m = __ballot_sync(0xffffffffu, hit);
+            if (m) return start + base + (__ffs(m) - 1);
+        }
     }
     return -1;
 }
@@ -446,7 +459,7 @@ __global__ void __launch_bounds__(1024) k_hsync_lines(const T* stream, int64_t s
         li.loc = loc;
         li.crossing = li.sync = li.own_porch = li.rc_own = li.rc_spec = li.r_porch = li.r_cand = nan("");
         li.ss = 0;
-        li.pad = 0;
+        li.pre = 0;
         flags = (have && p.filled_in[g]) ? 32 : 0;
         const bool vsync_line = (line >= 3 && line <= 6) || (p.pal && line >= 1 && line <= 2);
         if (vsync_line) flags |= 1;
@@ -588,6 +601,18 @@ __global__ void __launch_bounds__(1024) k_hsync_lines(const T* stream, int64_t s
             }
         }
         li.flags = flags;
+        int pre = 0;
+        const double half = one / 2.0, two = one * 2.0;
+        if (li.crossing == li.crossing) pre |= kPreCross;
+        if (li.rc_own == li.rc_own && fabs(li.rc_own - li.crossing) < half) pre |= kPreOwnOk;
+        if (li.own_porch > 0.0) pre |= kPreOwnPos;
+        if (flags & 16) {
+            if (fabs(li.r_cand - li.rc_own) < two) pre |= kPreNearOwn;
+            if (fabs(li.r_cand - li.crossing) < two) pre |= kPreNearCross;
+            if (fabs(li.r_cand - li.loc) < two) pre |= kPreNearLoc;
+            if (li.r_porch > 0.0) pre |= kPreRPos;
+        }
+        li.pre = pre;
         if (have) info[g] = li;
     }
 }
@@ -635,7 +660,14 @@ __global__ void __launch_bounds__(1024) k_hsync_spec(const T* stream, int64_t st
     __syncthreads();
     if (warp == 0 && lw[lane].want) {
         const LineWork& w = lw[lane];
-        info[g].rc_spec = w.x[0] >= 0 ? crossing_at(stream + w.s0, w.x[0], target) : (double)NAN;
+        LineInfo& li = info[g];
+        const double rc = w.x[0] >= 0 ? crossing_at(stream + w.s0, w.x[0], target) : (double)NAN;
+        li.rc_spec = rc;
+        int pre = li.pre;
+        const int one = p.one_us;
+        if (rc == rc && fabs(rc - li.crossing) < one / 2.0) pre |= kPreSpecOk;
+        if ((li.flags & 16) && fabs(li.r_cand - rc) < one * 2.0) pre |= kPreNearSpec;
+        li.pre = pre;
     }
 }
 
@@ -655,67 +687,85 @@ __global__ void k_hsync_chain(const T* stream, int64_t stream_len, HsyncParams p
         for (int i = lane; i < words; i += 32) d[i] = g[i];
         __syncwarp();
     }
+    // The carry walk: every comparison that does not involve the carried
+    // porch level was precomputed (LineInfo::pre); the carried level enters
+    // only through "is it bit-identical to the previous line's right porch"
+    // (then the speculative crossing rc_spec applies) and, on a miss, a new
+    // midpoint search.  The carried level is positive once set, so its
+    // "> 0" test is a flag.
     const int one = p.one_us;
     double pp = -1.0;
-    double prev_r = nan("");
+    bool pp_set = false;
+    long long prev_r_bits = -1;    // bits of the previous line's right porch, -1 when none
     int miss = 0;
+    enum { kRefLoc, kRefCross, kRefOwn, kRefSpec, kRefMiss };
     for (int line = 0; line < p.lines; line++) {
-        const LineInfo li = fi[line];
+        const LineInfo& li = fi[line];
+        const int flags = li.flags, pre = li.pre;
         double out = li.loc;
-        uint8_t fo = (li.flags & 32) ? 1 : 0;
-        const bool filled = (li.flags & 32) != 0;
-        if (li.flags & 1) {
+        uint8_t fo = (flags & 32) ? 1 : 0;
+        const bool filled = (flags & 32) != 0;
+        if (flags & 1) {
             fo = 1;
-        } else if (li.flags & 2) {
-            double right_ref = li.loc;
-            double refined = li.loc;
-            if (li.crossing == li.crossing && !filled) {
-                bool ok = false, preserve = false;
-                double rloc = 0.0, porch = 0.0;
-                if (li.flags & 4) {
+        } else if (flags & 2) {
+            int ref = kRefLoc;
+            double refined = li.loc, rc_miss = 0.0;
+            if ((pre & kPreCross) && !filled) {
+                bool ok = false, preserve = false, porch_pos = false;
+                double porch = 0.0;
+                int kind = kRefLoc;
+                if (flags & 4) {
                     preserve = true;
-                    double rc = nan("");
-                    bool have = true;
-                    if (pp > 0.0) {
+                    if (pp_set) {
                         porch = pp;
-                        if (pp == prev_r) {
-                            rc = li.rc_spec;
+                        porch_pos = true;
+                        if (__double_as_longlong(pp) == prev_r_bits) {
+                            ok = (pre & kPreSpecOk) != 0;
+                            kind = kRefSpec;
                         } else {
                             miss++;
                             int c2 = (int)min((int64_t)400, sp.n - li.ss - 1);
-                            rc = zero_crossing(sp, li.ss, (pp + li.sync) / 2.0, 0, c2, lane);
+                            rc_miss = zero_crossing(sp, li.ss, (pp + li.sync) / 2.0, 0, c2, lane);
+                            ok = rc_miss == rc_miss && fabs(rc_miss - li.crossing) < one / 2.0;
+                            kind = kRefMiss;
                         }
-                    } else if (li.flags & 8) {
+                    } else if (flags & 8) {
                         porch = li.own_porch;
-                        rc = li.rc_own;
-                    } else {
-                        have = false;
-                    }
-                    if (have && rc == rc && fabs(rc - li.crossing) < one / 2.0) {
-                        ok = true;
-                        rloc = rc;
+                        porch_pos = (pre & kPreOwnPos) != 0;
+                        ok = (pre & kPreOwnOk) != 0;
+                        kind = kRefOwn;
                     }
                 }
                 if (ok) {
-                    refined = rloc;
-                    right_ref = rloc;
+                    refined = kind == kRefSpec ? li.rc_spec : (kind == kRefOwn ? li.rc_own : rc_miss);
+                    ref = kind;
                     fo = filled ? 1 : 0;
-                    if (porch > 0.0) pp = porch;
+                    if (porch_pos) { pp = porch; pp_set = true; }
                 } else {
                     fo = 1;
-                    if (preserve) right_ref = li.crossing;
+                    if (preserve) ref = kRefCross;
                 }
             } else {
                 fo = 1;
             }
-            if ((li.flags & 16) && fabs(li.r_cand - right_ref) < one * 2.0) {
-                refined = li.r_cand;
-                fo = 0;
-                if (li.r_porch > 0.0) pp = li.r_porch;
+            if (flags & 16) {
+                bool near;
+                switch (ref) {
+                    case kRefCross: near = (pre & kPreNearCross) != 0; break;
+                    case kRefOwn: near = (pre & kPreNearOwn) != 0; break;
+                    case kRefSpec: near = (pre & kPreNearSpec) != 0; break;
+                    case kRefMiss: near = fabs(li.r_cand - rc_miss) < one * 2.0; break;
+                    default: near = (pre & kPreNearLoc) != 0; break;
+                }
+                if (near) {
+                    refined = li.r_cand;
+                    fo = 0;
+                    if (pre & kPreRPos) { pp = li.r_porch; pp_set = true; }
+                }
             }
             out = refined;
         }
-        prev_r = (li.flags & 16) ? li.r_porch : nan("");
+        prev_r_bits = (flags & 16) && li.r_porch == li.r_porch ? __double_as_longlong(li.r_porch) : -1;
         if (lane == 0) {
             p.locs_out[(int64_t)f * p.lines + line] = out - p.ntsc_shift;
             p.filled_out[(int64_t)f * p.lines + line] = fo;
