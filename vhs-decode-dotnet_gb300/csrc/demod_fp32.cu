@@ -342,6 +342,8 @@ vhsd_demod_fp32_kernel(FastDemodParams p) {
                 float2 wb = cmulc(b, w32k(sh.tw, n));
                 o1[t] = cadd(a, wb);
                 o2[t] = csub(a, wb);
+                sh.theta[nl] = vhs_atan2(o1[t].y, o1[t].x);
+                sh.theta[8192 + nl] = vhs_atan2(o2[t].y, o2[t].x);
             }
             cluster.sync();
 #pragma unroll
@@ -352,14 +354,7 @@ vhsd_demod_fp32_kernel(FastDemodParams p) {
             }
         }
         __syncthreads();
-        // ---------------- stage 3: angles, demod, spike check -------------
-#pragma unroll 4
-        for (int t = 0; t < 32; t++) {
-            int i = tid + t * T;
-            float2 z = buf[sx(i)];
-            sh.theta[i] = vhs_atan2(z.y, z.x);
-        }
-        __syncthreads();
+        // ---------------- stage 3: demod, spike check ----------------------
         if (tid < 2) {
             int i_last = tid * 8192 + 8191;
             sh.tail_theta[tid] = sh.theta[i_last];
