@@ -484,7 +484,7 @@ def main():
     ap.add_argument("--skip-serve", action="store_true")
     ap.add_argument("--serve-rate", type=float, default=200.0, help="window arrivals per second")
     ap.add_argument("--serve-seconds", type=float, default=3.0)
-    ap.add_argument("--serve-workers", type=int, default=8)
+    ap.add_argument("--serve-workers", type=int, default=4)
     ap.add_argument("--profile-demod", action="store_true",
                     help="only demod-only decodes of the workload (for kernel captures)")
     args = ap.parse_args()
