@@ -34,8 +34,10 @@ for _p in (ROOT, PKG):
 
 METRIC = "RF MSPS demod+TBC on 1 GB300"
 WORKLOADS = {
-    "ntsc60": ("NTSC VHS SP, 60 fields, 40 MSPS int16, 200 dropouts, 38 dB SNR", "NTSC"),
-    "pal4": ("PAL VHS SP, 4 fields, 40 MSPS int16, 40 dB SNR", "PAL"),
+    "ntsc60": ("NTSC VHS SP, 60 fields, 40 MSPS int16, 200 dropouts, 38 dB SNR", "NTSC", "VHS"),
+    "pal4": ("PAL VHS SP, 4 fields, 40 MSPS int16, 40 dB SNR", "PAL", "VHS"),
+    "svhs100": ("PAL S-VHS SP, 100 fields, 40 MSPS int16, 42 dB SNR, +/-0.5 % wobble at 15 Hz, "
+                "+/-2-sample head-switch jumps per field (sub-deemphasis on)", "PAL", "SVHS"),
 }
 BLOCK, STRIDE = 32768, 30720
 # algorithmic bytes of the fused demodulator per 32768-sample block:
@@ -64,9 +66,9 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def profile_traffic_per_block():
+def profile_traffic_per_block(workload="ntsc60"):
     """DRAM bytes per block of the fused demodulator from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "demod_fp32_ntsc60.md")
+    p = os.path.join(ROOT, "profiles", "demod_fp32_%s.md" % workload)
     if not os.path.exists(p):
         return None
     for line in open(p):
@@ -148,10 +150,10 @@ def make_pool(procs):
     return mp.get_context("spawn").Pool(procs)
 
 
-def cpu_oracle_msps(rf, system, procs, pool=None):
+def cpu_oracle_msps(rf, system, procs, pool=None, tape="VHS"):
     """Oracle decode of the capture: block demod over a spawn pool, field path sequential."""
     from oracle import demod, field, formats
-    fmt = formats.get(system)
+    fmt = formats.get(system, tape)
     nblocks = demod.block_count(len(rf))
     own = pool is None
     if own:
@@ -160,7 +162,7 @@ def cpu_oracle_msps(rf, system, procs, pool=None):
     chunks = np.array_split(np.arange(nblocks), procs * 4)
     try:
         parts = pool.map(_oracle_demod_part,
-                         [(rf[int(c[0]) * STRIDE: (int(c[-1]) * STRIDE + BLOCK)], system, len(c))
+                         [(rf[int(c[0]) * STRIDE: (int(c[-1]) * STRIDE + BLOCK)], system, tape, len(c))
                           for c in chunks if len(c)])
     finally:
         if own:
@@ -177,14 +179,14 @@ _FILTERS = {}
 
 
 def _oracle_demod_part(args):
-    rf, system, nb = args
+    rf, system, tape, nb = args
     from oracle import demod, formats
     from oracle.filters import FilterSet
-    fmt = formats.get(system)
-    if system not in _FILTERS:
-        _FILTERS[system] = FilterSet(fmt, 40e6)
+    fmt = formats.get(system, tape)
+    if (system, tape) not in _FILTERS:
+        _FILTERS[(system, tape)] = FilterSet(fmt, 40e6)
     dmax = (fmt["sys"]["ire0"] + fmt["sys"]["hz_ire"] * 100.0) * 2.0
-    v, l, e, _ = demod.demod_stream(rf, _FILTERS[system], 40e6, dmax, 0, nb)
+    v, l, e, _ = demod.demod_stream(rf, _FILTERS[(system, tape)], 40e6, dmax, 0, nb)
     return v, l, e
 
 
@@ -192,14 +194,14 @@ def run_reference(args, world, rank):
     if rank != 0:
         return
     rf = workload(args.workload)
-    desc, system = WORKLOADS[args.workload]
+    desc, system, tape = WORKLOADS[args.workload]
     procs = os.cpu_count() or 1
     pool = make_pool(procs)
     for _ in range(args.warmup):
-        cpu_oracle_msps(rf[: 4 * 1048576], system, procs, pool)
+        cpu_oracle_msps(rf[: 4 * 1048576], system, procs, pool, tape)
     times = []
     for _ in range(args.steps):
-        msps, dt, nf = cpu_oracle_msps(rf, system, procs, pool)
+        msps, dt, nf = cpu_oracle_msps(rf, system, procs, pool, tape)
         times.append(dt)
     pool.close()
     avg = sum(times) / len(times)
@@ -221,11 +223,12 @@ def run_ours(args, world, rank, local):
     import torch
     from vhsd_gb300 import native
     torch.cuda.set_device(local)
-    desc, system = WORKLOADS[args.workload]
+    desc, system, tape = WORKLOADS[args.workload]
     prof = native.PROFILE_PAL if system == "PAL" else native.PROFILE_NTSC
+    tfmt = native.FORMAT_SVHS if tape == "SVHS" else native.FORMAT_VHS
     rf = workload(args.workload)
     n = len(rf)
-    sess = native.Session(prof, n, precision=native.PRECISION_FP32_FUSED, device=local)
+    sess = native.Session(prof, n, precision=native.PRECISION_FP32_FUSED, device=local, tape_format=tfmt)
     stream = torch.cuda.current_stream()
     sess.set_stream(stream.cuda_stream)
     d_rf = torch.from_numpy(rf).to("cuda")
@@ -278,11 +281,11 @@ def run_ours(args, world, rank, local):
     peak, peak_kind = peaks()
     avg_demod = sum(demod_ms) / len(demod_ms)
     achieved = DEMOD_BYTES_PER_BLOCK * nblocks / (avg_demod / 1e3) / 1e9
-    tpb = profile_traffic_per_block()
+    tpb = profile_traffic_per_block(args.workload)
     # plain FP64 baseline (one block at a time) on the same capture, one step
     plain = None
     if not args.skip_plain:
-        ps = native.Session(prof, n, precision=native.PRECISION_FP64_PLAIN, device=local)
+        ps = native.Session(prof, n, precision=native.PRECISION_FP64_PLAIN, device=local, tape_format=tfmt)
         ps.set_stream(stream.cuda_stream)
         ps.decode(None, device_ptr=d_rf.data_ptr(), count=n)
         torch.cuda.synchronize()
@@ -300,8 +303,8 @@ def run_ours(args, world, rank, local):
     if rank == 0 and world == 1 and not args.skip_cpu:
         procs = os.cpu_count() or 1
         pool = make_pool(procs)
-        cpu_oracle_msps(rf[: 4 * 1048576], system, procs, pool)
-        msps, dt, nf = cpu_oracle_msps(rf, system, procs, pool)
+        cpu_oracle_msps(rf[: 4 * 1048576], system, procs, pool, tape)
+        msps, dt, nf = cpu_oracle_msps(rf, system, procs, pool, tape)
         pool.close()
         cpu = {"value": round(msps, 3), "unit": "MSPS", "cores": procs, "kind": "port",
                "sample": "whole workload capture (%d samples, %.1f s): oracle restatement, block "
@@ -339,26 +342,28 @@ def run_ours(args, world, rank, local):
     sess.close()
 
 
-# Serving mix of 2-s windows (share, profile, MSPS, label).  The PAL S-VHS and
-# NTSC LaserDisc shares are decoded as PAL VHS / NTSC VHS windows of the same
-# sample rate and length (their demod branches are not built), so the offered
-# sample load is the mix's own: 200 windows/s x 68 M samples = 13.6 GSPS.
-SERVE_MIX = [(0.40, "PAL", 40.0, "pal_vhs_40"), (0.30, "NTSC", 20.0, "ntsc_vhs_20"),
-             (0.15, "PAL", 40.0, "pal_svhs_40 as pal_vhs_40"), (0.15, "NTSC", 40.0, "ntsc_ld_40 as ntsc_vhs_40")]
+# Serving mix of 2-s windows (share, profile, tape format, MSPS, label).  The
+# NTSC LaserDisc share is decoded as NTSC VHS windows of the same sample rate
+# and length (the LaserDisc demod branch is not built), so the offered sample
+# load is the mix's own: 200 windows/s x 68 M samples = 13.6 GSPS.
+SERVE_MIX = [(0.40, "PAL", "VHS", 40.0, "pal_vhs_40"), (0.30, "NTSC", "VHS", 20.0, "ntsc_vhs_20"),
+             (0.15, "PAL", "SVHS", 40.0, "pal_svhs_40"),
+             (0.15, "NTSC", "VHS", 40.0, "ntsc_ld_40 as ntsc_vhs_40")]
 SERVE_TILE_FIELDS = 8
 
 
-def serve_source(system, mhz, seconds):
+def serve_source(system, tape, mhz, seconds):
     """Seeded synthetic capture of `seconds`, built by repeating an 8-field
     synthetic recording (the joins are FM phase jumps, decoded like head
     switches).  Cached in /tmp."""
     from vhsd_gb300 import synth
-    cache = os.path.join("/tmp", "vhsd_serve_%s_%d_%d.npy" % (system, int(mhz), SERVE_TILE_FIELDS))
+    cache = os.path.join("/tmp", "vhsd_serve_%s_%s_%d_%d.npy" % (system, tape, int(mhz), SERVE_TILE_FIELDS))
     if os.path.exists(cache):
         tile = np.load(cache)
     else:
-        cfg = synth.config("pal4" if system == "PAL" else "ntsc_small", fields=SERVE_TILE_FIELDS,
-                           fs=mhz * 1e6, seed=31 if system == "PAL" else 32)
+        name = "svhs_small" if tape == "SVHS" else ("pal4" if system == "PAL" else "ntsc_small")
+        cfg = synth.config(name, fields=SERVE_TILE_FIELDS, fs=mhz * 1e6,
+                           seed=(33 if tape == "SVHS" else 31) if system == "PAL" else 32)
         tile, _ = synth.generate(cfg)
         try:
             np.save(cache, tile)
@@ -377,27 +382,29 @@ def run_serving(args, local):
     win_s, rate, nstreams, dur = 2.0, float(args.serve_rate), 32, float(args.serve_seconds)
     src_s = 6.0
     sources = {}
-    for share, system, mhz, label in SERVE_MIX:
-        key = (system, mhz)
+    for share, system, tape, mhz, label in SERVE_MIX:
+        key = (system, tape, mhz)
         if key not in sources:
-            host = serve_source(system, mhz, src_s)
+            host = serve_source(system, tape, mhz, src_s)
             sources[key] = torch.from_numpy(host).pin_memory().numpy()
     # streams: formats by the mix shares
-    counts = [int(round(share * nstreams)) for share, _, _, _ in SERVE_MIX]
+    counts = [int(round(m[0] * nstreams)) for m in SERVE_MIX]
     counts[0] += nstreams - sum(counts)
     streams = []
-    for (share, system, mhz, label), c in zip(SERVE_MIX, counts):
+    for (share, system, tape, mhz, label), c in zip(SERVE_MIX, counts):
         for _ in range(c):
-            streams.append({"system": system, "mhz": mhz, "label": label, "offset": None, "left": 0})
+            streams.append({"system": system, "tape": tape, "mhz": mhz, "label": label, "offset": None,
+                            "left": 0})
     max_win = int(win_s * 40e6)
     prof = {"PAL": native.PROFILE_PAL, "NTSC": native.PROFILE_NTSC}
+    tfmt = {"VHS": native.FORMAT_VHS, "SVHS": native.FORMAT_SVHS}
     per_field = {"PAL": 313 * 1135, "NTSC": 263 * 910}
     outs = {sysn: [torch.empty(130 * per_field[sysn], dtype=torch.int16).pin_memory().numpy().view(np.uint16)
                    for _ in range(8)] for sysn in ("PAL", "NTSC")}
     sv = native.Server(max_win, workers=args.serve_workers, device=local)
 
     def window(st):
-        src = sources[(st["system"], st["mhz"])]
+        src = sources[(st["system"], st["tape"], st["mhz"])]
         n = int(win_s * st["mhz"] * 1e6)
         seek = st["offset"] is None or st["left"] <= 0 or st["offset"] + 2 * n > len(src)
         if seek:
@@ -412,11 +419,12 @@ def run_serving(args, local):
     # slot of each format before the timed arrivals start
     warm = []
     for key in sources:
-        st0 = next(x for x in streams if (x["system"], x["mhz"]) == key)
+        st0 = next(x for x in streams if (x["system"], x["tape"], x["mhz"]) == key)
         for i in range(args.serve_workers):
             x, off, seek = window(dict(st0))
             warm.append(sv.submit(1000 + len(warm), prof[st0["system"]], x, off, seek=True,
-                                  sample_rate_mhz=st0["mhz"], tbc_out=outs[st0["system"]][i % 8]))
+                                  sample_rate_mhz=st0["mhz"], tbc_out=outs[st0["system"]][i % 8],
+                                  tape_format=tfmt[st0["tape"]]))
     for t in warm:
         sv.wait(t)
     # arrivals
@@ -434,7 +442,7 @@ def run_serving(args, local):
         x, off, seek = window(st)
         samples += len(x)
         tickets.append(sv.submit(si, prof[st["system"]], x, off, seek=seek, sample_rate_mhz=st["mhz"],
-                                 tbc_out=outs[st["system"]][k % 8]))
+                                 tbc_out=outs[st["system"]][k % 8], tape_format=tfmt[st["tape"]]))
     res = [sv.wait(t) for t in tickets]
     t_end = time.perf_counter() - t0
     sv.close()
@@ -447,7 +455,7 @@ def run_serving(args, local):
             "msps": round(samples / t_end / 1e6, 1),
             "offered_msps": round(samples / dur / 1e6, 1),
             "fields": int(sum(r.fields for r in res)),
-            "mix": [m[3] for m in SERVE_MIX],
+            "mix": [m[4] for m in SERVE_MIX],
             "data": "synthetic, 8-field recordings repeated to 6 s per format; TBC copied to pinned host"}
 
 
@@ -456,10 +464,11 @@ def run_profile_demod(args, local):
     for kernel captures: warm-up, then --steps decodes; prints the kernel times."""
     import torch
     from vhsd_gb300 import native
-    desc, system = WORKLOADS[args.workload]
+    desc, system, tape = WORKLOADS[args.workload]
     prof = native.PROFILE_PAL if system == "PAL" else native.PROFILE_NTSC
     rf = workload(args.workload)
-    sess = native.Session(prof, len(rf), device=local)
+    sess = native.Session(prof, len(rf), device=local,
+                          tape_format=native.FORMAT_SVHS if tape == "SVHS" else native.FORMAT_VHS)
     d_rf = torch.from_numpy(rf).to("cuda")
     for _ in range(args.warmup):
         sess.decode(None, device_ptr=d_rf.data_ptr(), count=len(rf), demod_only=True)

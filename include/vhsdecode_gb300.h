@@ -34,7 +34,7 @@
 #  define VHSDECODE_GB300_CALL
 #endif
 
-#define VHSDECODE_GB300_ABI_VERSION 0x00010001u
+#define VHSDECODE_GB300_ABI_VERSION 0x00010002u
 #define VHSDECODE_GB300_NAME_CAPACITY 128u
 
 #ifdef __cplusplus
@@ -67,6 +67,14 @@ typedef enum vhsdecode_gb300_tape_speed {
     VHSDECODE_GB300_TAPE_SPEED_LP = 1,
     VHSDECODE_GB300_TAPE_SPEED_EP = 2
 } vhsdecode_gb300_tape_speed;
+
+/* Tape format: the reference's --tape_format values VHS and SVHS (format
+ * parameter snapshot cases <system>/VHS/sp and <system>/SVHS/sp).  The
+ * reference's cuda-fast ABI has no such field (it decodes VHS only). */
+typedef enum vhsdecode_gb300_tape_format {
+    VHSDECODE_GB300_TAPE_FORMAT_VHS = 0,
+    VHSDECODE_GB300_TAPE_FORMAT_SVHS = 1
+} vhsdecode_gb300_tape_format;
 
 /* vhsdecode_cuda_fast_input_sample_format (:50-53); run() accepts INT16. */
 typedef enum vhsdecode_gb300_input_sample_format {
@@ -119,6 +127,27 @@ typedef struct vhsdecode_gb300_config_v1 {
     void* user_data;
 } vhsdecode_gb300_config_v1;
 
+/* config_v1 followed by the tape format.  run() takes either struct, told
+ * apart by struct_size (config_v1 decodes VHS). */
+typedef struct vhsdecode_gb300_config_v2 {
+    uint32_t struct_size;
+    uint32_t profile;
+    uint32_t tape_speed;
+    int32_t device_id;
+    double sample_rate_mhz;
+    uint64_t total_samples;
+    const char* output_base_utf8;
+    int32_t overwrite;
+    uint32_t input_sample_format;
+    uint32_t maximum_output_fields;
+    uint32_t device_decimation_factor;
+    vhsdecode_gb300_read_callback read_callback;
+    vhsdecode_gb300_cancel_callback cancel_callback;
+    void* user_data;
+    uint32_t tape_format;       /* vhsdecode_gb300_tape_format */
+    uint32_t reserved;
+} vhsdecode_gb300_config_v2;
+
 /* vhsdecode_cuda_fast_result_v1 (:100-106). */
 typedef struct vhsdecode_gb300_result_v1 {
     uint32_t struct_size;
@@ -140,6 +169,8 @@ typedef struct vhsdecode_gb300_session_config_v1 {
     uint64_t max_samples;       /* capacity of one capture / window */
     uint32_t precision;         /* vhsdecode_gb300_precision */
     uint32_t max_fields;        /* 0 = derived from max_samples */
+    uint32_t tape_format;       /* vhsdecode_gb300_tape_format */
+    uint32_t reserved;
 } vhsdecode_gb300_session_config_v1;
 
 /* flags for vhsdecode_gb300_session_decode */
@@ -187,7 +218,8 @@ VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_get_runtime_inf
 
 /* vhsdecode_cuda_fast_run (:153-156): whole-run handoff.  Pulls int16 RF through
  * read_callback, decodes every field and writes <base>.tbc (uint16 LE luma,
- * outlinelen x (frame_lines/2+1) per field) and <base>.tbc.json. */
+ * outlinelen x (frame_lines/2+1) per field) and <base>.tbc.json.  `config`
+ * may point to a vhsdecode_gb300_config_v2 (struct_size tells). */
 VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_run(
     const vhsdecode_gb300_config_v1* config, vhsdecode_gb300_result_v1* result);
 
@@ -243,11 +275,14 @@ VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_session_tbc_dev
 
 /* ---- stage-level entry points (tests) ------------------------------ */
 
-/* Filter spectra (bins 0..16384) for a profile at a sample rate; host only.
- * video / sync are interleaved (re, im). env receives b0, b1, a1. */
+/* Filter spectra (bins 0..16384) for a format at a sample rate; host only.
+ * video / sync / sub_high are interleaved (re, im); sub_high (may be NULL)
+ * receives Video x the sub-deemphasis high-pass, zeros for formats without
+ * sub-deemphasis.  env receives the envelope low-pass b0, b1, a1 and, from
+ * env[3], the sub-deemphasis amplitude low-pass b0, b1, a1 (zeros without). */
 VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_design_filters(
-    uint32_t profile, uint32_t tape_speed, double sample_rate_mhz, double* rf_video,
-    double* video, double* sync, double* env);
+    uint32_t profile, uint32_t tape_speed, uint32_t tape_format, double sample_rate_mhz,
+    double* rf_video, double* video, double* sync, double* sub_high, double* env);
 
 /* Host control plane on given raw pulses of one span; host only.
  * state[0] = previous first-field flag (-1 unknown), state[1] = has previous
@@ -325,6 +360,8 @@ typedef struct vhsdecode_gb300_window_v1 {
     uint32_t max_fields;            /* 0 = as many as fit */
     uint16_t* tbc_out;              /* host destination for the fields' TBC, or NULL */
     uint64_t tbc_capacity;          /* uint16 elements at tbc_out */
+    uint32_t tape_format;           /* vhsdecode_gb300_tape_format */
+    uint32_t reserved;
 } vhsdecode_gb300_window_v1;
 
 typedef struct vhsdecode_gb300_window_result_v1 {

@@ -13,7 +13,9 @@ Restates the managed ``exact`` VHS real-FFT path of
 * diff-demod spike repair (RfDemodulator.cs:2527-2582, 966-1001);
 * float32 envelope filtfilt (RfDemodulator.cs:1755-1839);
 * demod real FFT x Video / x VideoLowPass05, real inverses, roll -32
-  (RfDemodulator.cs:792-885).
+  (RfDemodulator.cs:792-885);
+* S-VHS sub-deemphasis of the video (``ApplySubDeemphasisRealCore``,
+  RfDemodulator.cs:2852-2990, 3144-3220).
 
 Stitching follows ``RfBlockStreamDecoder.ReadCore`` / ``CopyTrimmedWindow``
 (Core/Decode/RfBlockStreamDecoder.cs:418-560, 1586-1610): block b reads RF
@@ -44,6 +46,32 @@ def replace_spikes(demod, diffed, max_value, replace_start=8, replace_end=30):
     return demod
 
 
+def sub_deemphasis(video, video_spec, filters):
+    """``ApplySubDeemphasisRealCore`` (Core/Dsp/RfDemodulator.cs:2852-2990)."""
+    n = len(video)
+    o = filters.sub
+    high = np.fft.irfft(video_spec * filters.sub_highpass[: n // 2 + 1], n)
+    # BuildAnalyticMagnitudeWithWorkspace (RfDemodulator.cs:3181-3220)
+    spec = np.fft.fft(high)
+    spec[1:n // 2] *= 2.0
+    spec[n // 2 + 1:] = 0.0
+    amp = np.abs(np.fft.ifft(spec))   # numpy's magnitude, as NumpyComplexMagnitude (:3222-3244)
+    amp = amp / (o["deviation"] / 2.0)
+    amp = native.filtfilt1_f64(amp, filters.sub_amp_b[0], filters.sub_amp_b[1], filters.sub_amp_a1)
+    amp = np.maximum(0.0, amp)
+    if o["scale1"] is not None:
+        amp = amp * o["scale1"]
+    amp = np.power(amp, o["exp"])
+    if o["scale2"] is not None:
+        amp = amp * o["scale2"]
+    rate = o["logistic_rate"]
+    if rate is not None and rate > 0.0:
+        mid = o["logistic_mid"] if o["logistic_mid"] is not None else 0.0
+        amp = amp * (1.0 / (1.0 + np.exp(-rate * (amp - mid))))
+    static = o["static"] if o["static"] is not None else 0.0
+    return video - ((high * (1.0 - amp)) + high * static)
+
+
 def demod_block(x, filters, fs, diff_max, return_debug=False):
     """Demodulate one RF block; returns (video, video_lowpass, envelope, weak, debug)."""
     x = np.asarray(x, np.float64)
@@ -68,7 +96,10 @@ def demod_block(x, filters, fs, diff_max, return_debug=False):
     envelope = native.vhs_envelope(filtered_real, filters.env_b[0], filters.env_b[1], filters.env_a1)
     weak = bool(np.any(envelope == 0.0))
     dspec = np.fft.rfft(demod)
-    video = np.fft.irfft(dspec * filters.video[:h], n)
+    vspec = dspec * filters.video[:h]
+    video = np.fft.irfft(vspec, n)
+    if getattr(filters, "sub", None) is not None:
+        video = sub_deemphasis(video, vspec, filters)
     vlp = np.fft.irfft(dspec * filters.video_lp05[:h], n)
     vlp = np.roll(vlp, -filters.video_lp05_offset)
     dbg = None

@@ -7,11 +7,15 @@ response (``scipy.signal.freqz(..., worN=N, whole=True)`` semantics, as
 the real-FFT path only reads bins 0..N/2.
 """
 import math
+import os
 
 import numpy as np
 import scipy.signal as sps
 
 from . import formats
+
+DATA = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                    "vhs-decode-dotnet_gb300", "data")
 
 
 def _freqz_ba(b, a, n):
@@ -113,6 +117,44 @@ def deemphasis_ba(fs, gain_db, mid_hz, q):
     return a, b
 
 
+def custom_luma_table(filename, fs, n):
+    """``DecodeFilterSetBuilder.TryLoadCustomFilter`` (Core/Dsp/DecodeFilterSet.cs:1658-1714):
+    the resource ``<filename>-<(int)fs>.txt`` (bins 0..N/2, mirrored conjugate above),
+    or None when the reference has no table for this rate.  The tables are the
+    reference's resources converted to binary64 pairs (pinned by SHA-256 in
+    tests/golden/format_params.json)."""
+    path = os.path.join(DATA, "%s-%d.f64" % (filename, int(fs)))
+    if not os.path.exists(path):
+        return None
+    half = np.fromfile(path, "<f8").reshape(-1, 2)
+    half = half[:, 0] + 1j * half[:, 1]
+    if len(half) != n // 2 + 1:
+        return None
+    out = np.zeros(n, complex)
+    out[: len(half)] = half
+    i = np.arange(1, len(half) - 1)
+    out[n - i] = np.conj(half[i])
+    return out
+
+
+def apply_custom_video_filters(video, rf, fs, n):
+    """``ApplyCustomVideoFilters`` (Core/Dsp/DecodeFilterSet.cs:1560-1609); shelves are
+    designed with fs/2 as their rate argument, as the reference passes them."""
+    for flt in rf.get("video_custom_luma_filters") or []:
+        kind = flt["type"]
+        resp = None
+        if kind == "file":
+            resp = custom_luma_table(flt["filename"], fs, n)
+        elif kind == "highshelf":
+            b, a = high_shelf(flt["midfreq"], flt["gain"], fs / 2.0, flt["q"])
+            resp = _freqz_ba(b, a, n)
+        elif kind == "lowshelf":
+            raise NotImplementedError("low shelf custom luma filters")
+        if resp is not None and len(resp) == len(video):
+            video = video * resp
+    return video
+
+
 def firwin_lowpass_hamming(numtaps, cutoff):
     """``FirWinLowPass`` (Core/Dsp/DecodeFilterSet.cs:1346-1375) == scipy.signal.firwin."""
     return sps.firwin(numtaps, cutoff, window="hamming")
@@ -169,7 +211,8 @@ class FilterSet:
         # De-emphasis shelf (DecodeFilterSet.cs:1104-1152).
         db, da = deemphasis_ba(fs, rf["deemph_gain"], rf["deemph_mid"], rf["deemph_q"])
         deemp = _freqz_ba(db, da, n)
-        self.video = vlp * deemp                       # BuildVideo: LPF x de-emphasis
+        # BuildVideo (DecodeFilterSet.cs:1063-1091): LPF x de-emphasis x custom luma filters
+        self.video = apply_custom_video_filters(vlp * deemp, rf, fs, n)
         video_ref = vlp * deemp                        # BuildVideoReference
         if 500_000.0 >= nyq:
             self.video_lp05 = video_ref
@@ -183,6 +226,20 @@ class FilterSet:
         norm = 1.0 / (1.0 + k)
         self.env_b = (k * norm, k * norm)
         self.env_a1 = (k - 1.0) * norm
+        # Sub-deemphasis (RfDemodulator.cs:2852-2990, 3101-3142): first-order Butterworth
+        # high-pass (band-pass when nonlinear_bandpass_upper is set) and amplitude low-pass.
+        self.sub = formats.sub_deemphasis(fmt)
+        if self.sub is not None:
+            o = self.sub
+            if o["bandpass_upper"] is not None:
+                raise NotImplementedError("sub-deemphasis band-pass")
+            kh = math.tan(math.pi * (o["highpass"] / nyq) / 2.0)
+            nh = 1.0 / (1.0 + kh)
+            self.sub_highpass = _freqz_ba([nh, -nh, 0.0], [1.0, (kh - 1.0) * nh, 0.0], n)
+            ka = math.tan(math.pi * (o["amp_lpf"] / nyq) / 2.0)
+            na = 1.0 / (1.0 + ka)
+            self.sub_amp_b = (ka * na, ka * na)
+            self.sub_amp_a1 = (ka - 1.0) * na
 
     def half(self, name):
         return getattr(self, name)[: self.n // 2 + 1]

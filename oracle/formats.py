@@ -2,7 +2,8 @@
 
 The values restate the frozen upstream snapshot the reference embeds
 (``src/VHSDecode.Core/Formats/format-params.snapshot.json``, cases
-``PAL/VHS/sp`` and ``NTSC/VHS/sp``; read through ``FormatCatalog.cs:46-112``).
+``PAL/VHS/sp``, ``NTSC/VHS/sp``, ``PAL/SVHS/sp`` and ``NTSC/SVHS/sp``; read
+through ``FormatCatalog.cs:46-112``).
 Only the keys the RF -> TBC luma path reads are kept.  ``tests/golden/
 format_params.json`` (written by ``tests/golden/make_golden.py`` from the
 reference snapshot) pins this table.
@@ -63,11 +64,62 @@ NTSC_VHS_SP = {
     },
 }
 
-FORMATS = {("PAL", "VHS", "sp"): PAL_VHS_SP, ("NTSC", "VHS", "sp"): NTSC_VHS_SP}
+_SVHS_RF = {
+    "video_bpf_low": 2000000.0, "video_bpf_high": 8980000.0,
+    "video_bpf_order": None, "video_bpf_supergauss": False,
+    "video_lpf_extra": 9100000.0, "video_lpf_extra_order": 25,
+    "video_hpf_extra": 1300000.0, "video_hpf_extra_order": 20,
+    "video_rf_peak_freq": 6200000.0, "video_rf_peak_gain": 4.0,
+    "video_rf_peak_bandwidth": 16000000.0,
+    "boost_rf_linear_0": 1.0, "boost_rf_linear_20": 4.0,
+    "video_lpf_freq": 7500000.0, "video_lpf_order": 6, "video_lpf_supergauss": True,
+    "video_custom_luma_filters": [
+        {"type": "file", "filename": "svhs-sp-linear-subdeemphasis"},
+        {"type": "highshelf", "midfreq": 2000000.0, "gain": 4.0, "q": 0.4967045}],
+    "use_sub_deemphasis": True,
+    "nonlinear_highpass_freq": 320000.0, "nonlinear_amp_lpf_freq": 590000.0,
+    "nonlinear_exp_scaling": 0.23, "nonlinear_scaling_1": None, "nonlinear_scaling_2": 0.72,
+    "nonlinear_logistic_mid": 0.2, "nonlinear_logistic_rate": 14.0,
+}
+
+
+def _svhs(base, ire0, hz_ire):
+    fmt = {"system": base["system"], "tape_format": "SVHS", "tape_speed": "sp",
+           "sys": dict(base["sys"], ire0=ire0, hz_ire=hz_ire), "rf": dict(base["rf"])}
+    fmt["rf"].update(_SVHS_RF)
+    return fmt
+
+
+PAL_SVHS_SP = _svhs(PAL_VHS_SP, 5880000.0, 11200.0)
+NTSC_SVHS_SP = _svhs(NTSC_VHS_SP, 5857142.857142857, 11428.57142857143)
+
+FORMATS = {("PAL", "VHS", "sp"): PAL_VHS_SP, ("NTSC", "VHS", "sp"): NTSC_VHS_SP,
+           ("PAL", "SVHS", "sp"): PAL_SVHS_SP, ("NTSC", "SVHS", "sp"): NTSC_SVHS_SP}
 
 
 def get(system: str, tape_format: str = "VHS", speed: str = "sp") -> dict:
     return FORMATS[(system.upper(), tape_format.upper(), speed.lower())]
+
+
+def sub_deemphasis(fmt: dict):
+    """``DecodeSession.BuildSubDeemphasisOptions`` (Core/Decode/DecodeSession.cs:1250-1278),
+    or None when the format does not use sub-deemphasis."""
+    rf, sy = fmt["rf"], fmt["sys"]
+    if not rf.get("use_sub_deemphasis"):
+        return None
+    dev = sy.get("nonlinear_deviation")
+    if dev is None:
+        dev = sy["hz_ire"] * (100.0 + -sy["vsync_ire"])
+    return {"highpass": rf["nonlinear_highpass_freq"],
+            "bandpass_upper": rf.get("nonlinear_bandpass_upper"),
+            "order": rf.get("nonlinear_bandpass_order") or 1,
+            "amp_lpf": rf.get("nonlinear_amp_lpf_freq") or 700000.0,
+            "deviation": dev,
+            "exp": rf.get("nonlinear_exp_scaling") if rf.get("nonlinear_exp_scaling") is not None else 0.25,
+            "scale1": rf.get("nonlinear_scaling_1"), "scale2": rf.get("nonlinear_scaling_2"),
+            "logistic_mid": rf.get("nonlinear_logistic_mid"),
+            "logistic_rate": rf.get("nonlinear_logistic_rate"),
+            "static": rf.get("nonlinear_static_factor")}
 
 
 def output_scale(fmt: dict) -> float:

@@ -37,6 +37,8 @@ def lib():
         L.oracle_vhs_rust_angles.argtypes = [_fp, _fp, ctypes.c_int64, _fp]
         L.oracle_vhs_envelope.argtypes = [_dp, ctypes.c_int64, ctypes.c_double, ctypes.c_double,
                                           ctypes.c_double, _dp, _fp]
+        L.oracle_filtfilt1_f64.argtypes = [_dp, ctypes.c_int64, ctypes.c_double, ctypes.c_double,
+                                           ctypes.c_double, _dp, _dp]
         L.oracle_find_pulses.argtypes = [_dp, ctypes.c_int64, ctypes.c_double, ctypes.c_int64,
                                          ctypes.c_int64, _i64p, _i64p, ctypes.c_int64]
         L.oracle_find_pulses.restype = ctypes.c_int64
@@ -79,6 +81,14 @@ def vhs_envelope(filtered, b0, b1, a1):
     work = np.empty(len(filtered) + 12, np.float32)
     lib().oracle_vhs_envelope(ptr(filtered, _dp), len(filtered), b0, b1, a1, ptr(out, _dp),
                               ptr(work, _fp))
+    return out
+
+
+def filtfilt1_f64(x, b0, b1, a1):
+    x = np.ascontiguousarray(x, np.float64)
+    out = np.empty_like(x)
+    work = np.empty(len(x) + 12)
+    lib().oracle_filtfilt1_f64(ptr(x, _dp), len(x), b0, b1, a1, ptr(out, _dp), ptr(work, _dp))
     return out
 
 

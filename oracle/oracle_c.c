@@ -123,6 +123,50 @@ void oracle_vhs_envelope(const double *filtered, int64_t n, double b0d, double b
 }
 
 /*
+ * SosFilter.ApplyForwardBackward (Core/Dsp/SosFilter.cs:178-232, 281-298,
+ * 540-570, 972-1001) for one first-order section (b0, b1, 0; 1, a1, 0), in
+ * binary64: odd extension of 6 samples, steady-state zi scaled by the first /
+ * last extended value, direct form II transposed forward then backward.
+ * `work` must hold n + 12 doubles.  Used for the sub-deemphasis amplitude.
+ */
+void oracle_filtfilt1_f64(const double *x, int64_t n, double b0, double b1, double a1,
+                          double *out, double *work)
+{
+    const int edge = 6;
+    double *ext = work;
+    double first = x[0], last = x[n - 1];
+    for (int i = 0; i < edge; i++) ext[i] = (2.0 * first) - x[edge - i];
+    for (int64_t i = 0; i < n; i++) ext[edge + i] = x[i];
+    for (int i = 0; i < edge; i++) ext[edge + n + i] = (2.0 * last) - x[n - 2 - i];
+    int64_t len = n + 2 * edge;
+    double b2 = 0.0, a2 = 0.0;
+    double first_term = b1 - (a1 * b0);
+    double second_term = b2 - (a2 * b0);
+    double num = (0.0 + first_term) + second_term;
+    double den = (1.0 + a1) + a2;
+    double zi0 = num / den;
+    double zi1 = ((1.0 + a1) * zi0) - first_term;
+    double z1 = zi0 * ext[0], z2 = zi1 * ext[0];
+    for (int64_t s = 0; s < len; s++) {
+        double v = ext[s];
+        double f = (b0 * v) + z1;
+        z1 = (b1 * v) - (a1 * f) + z2;
+        z2 = (b2 * v) - (a2 * f);
+        ext[s] = f;
+    }
+    z1 = zi0 * ext[len - 1];
+    z2 = zi1 * ext[len - 1];
+    for (int64_t s = len - 1; s >= 0; s--) {
+        double v = ext[s];
+        double f = (b0 * v) + z1;
+        z1 = (b1 * v) - (a1 * f) + z2;
+        z2 = (b2 * v) - (a2 * f);
+        ext[s] = f;
+    }
+    for (int64_t i = 0; i < n; i++) out[i] = ext[edge + i];
+}
+
+/*
  * PulseDetection.FindPulsesScalar (Core/Dsp/PulseDetection.cs:186-222).
  * Returns the pulse count (capped at `cap`, the true count is still returned).
  */

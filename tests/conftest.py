@@ -83,3 +83,33 @@ def ntsc20_oracle(ntsc20_capture):
     rf, _ = ntsc20_capture
     fields, ch = field.decode_capture(rf, formats.get("NTSC"), fs=20e6)
     return fields, ch
+
+
+@pytest.fixture(scope="session")
+def svhs_capture():
+    from vhsd_gb300 import synth
+    rf, info = synth.generate(synth.config("svhs_small"))
+    return rf, info
+
+
+@pytest.fixture(scope="session")
+def svhs_oracle(svhs_capture):
+    from oracle import field, formats
+    rf, _ = svhs_capture
+    fields, ch = field.decode_capture(rf, formats.get("PAL", "SVHS"))
+    return fields, ch
+
+
+@pytest.fixture(scope="session")
+def svhs_ntsc_capture():
+    from vhsd_gb300 import synth
+    rf, info = synth.generate(synth.config("svhs_ntsc_small"))
+    return rf, info
+
+
+@pytest.fixture(scope="session")
+def svhs_ntsc_oracle(svhs_ntsc_capture):
+    from oracle import field, formats
+    rf, _ = svhs_ntsc_capture
+    fields, ch = field.decode_capture(rf, formats.get("NTSC", "SVHS"))
+    return fields, ch

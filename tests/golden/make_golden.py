@@ -6,7 +6,10 @@ test time.
 
 * format_params.json: the keys of the frozen upstream parameter snapshot
   (src/VHSDecode.Core/Formats/format-params.snapshot.json) that the RF -> TBC
-  luma path reads, for the PAL/VHS/sp and NTSC/VHS/sp cases.
+  luma path reads, for the PAL/VHS/sp, NTSC/VHS/sp, PAL/SVHS/sp and
+  NTSC/SVHS/sp cases, and the SHA-256 of the S-VHS custom luma tables
+  (src/VHSDecode.Core/Formats/custom/*.txt) converted as
+  vhs-decode-dotnet_gb300/data/make_tables.py converts them.
 * sinc_lut_rows.json: the rows of the reference's 65537 x 16 sinc LUT
   (src/VHSDecode.Core/Tbc/Resources/sinc_lut.npz) that the three
   platform-independent SHA-256 tests of tests/VHSDecode.Tests/
@@ -30,7 +33,12 @@ RF_KEYS = ["video_bpf_low", "video_bpf_high", "video_bpf_order", "video_bpf_supe
            "video_rf_peak_freq", "video_rf_peak_gain", "video_rf_peak_bandwidth",
            "boost_rf_linear_0", "boost_rf_linear_20", "start_rf_linear", "boost_rf_linear_double",
            "video_lpf_freq", "video_lpf_order", "video_lpf_supergauss", "deemph_gain",
-           "deemph_mid", "deemph_q", "color_under_carrier"]
+           "deemph_mid", "deemph_q", "color_under_carrier", "video_custom_luma_filters",
+           "use_sub_deemphasis", "nonlinear_highpass_freq", "nonlinear_bandpass_upper",
+           "nonlinear_bandpass_order", "nonlinear_amp_lpf_freq", "nonlinear_exp_scaling",
+           "nonlinear_scaling_1", "nonlinear_scaling_2", "nonlinear_logistic_mid",
+           "nonlinear_logistic_rate", "nonlinear_static_factor"]
+SYS_KEYS_SUB = ["nonlinear_deviation"]
 
 # (name, source length, locations, first line, line count, outlen, expected SHA-256)
 HASH_CASES = [
@@ -63,9 +71,20 @@ def main():
     out = {}
     for c in snap["cases"]:
         key = (c["system"], c["tape_format"], c["tape_speed"])
-        if key in (("PAL", "VHS", "sp"), ("NTSC", "VHS", "sp")):
-            out["/".join(key)] = {"sys": {k: c["sysparams"].get(k) for k in SYS_KEYS},
+        if key in (("PAL", "VHS", "sp"), ("NTSC", "VHS", "sp"), ("PAL", "SVHS", "sp"),
+                   ("NTSC", "SVHS", "sp")):
+            out["/".join(key)] = {"sys": {k: c["sysparams"].get(k) for k in SYS_KEYS + SYS_KEYS_SUB},
                                   "rf": {k: c["rfparams"].get(k) for k in RF_KEYS}}
+    import hashlib
+    import struct
+    tables = {}
+    for rate in (40000000, 17734475):
+        txt = open(os.path.join(REF, "src/VHSDecode.Core/Formats/custom",
+                                "svhs-sp-linear-subdeemphasis-%d.txt" % rate)).read()
+        vals = [complex(x.strip()) for x in txt.splitlines() if x.strip()]
+        blob = b"".join(struct.pack("<dd", v.real, v.imag) for v in vals)
+        tables["svhs-sp-linear-subdeemphasis-%d" % rate] = hashlib.sha256(blob).hexdigest()
+    out["custom_luma_tables_sha256"] = tables
     with open(os.path.join(HERE, "format_params.json"), "w") as f:
         json.dump(out, f, indent=1, sort_keys=True)
 

@@ -33,6 +33,7 @@ def test_struct_sizes_match_c_layout(lib, tmp_path):
     import subprocess
     from vhsd_gb300 import native
     structs = {"runtime_info_v1": native.RuntimeInfo, "config_v1": native.RunConfig,
+               "config_v2": native.RunConfigV2,
                "result_v1": native.RunResult, "session_config_v1": native.SessionConfig,
                "decode_result_v1": native.DecodeResult, "field_info_v1": native.FieldInfo,
                "server_config_v1": native.ServerConfig, "window_v1": native.Window,
@@ -92,13 +93,15 @@ def test_run_rejects_unsupported_options(lib):
     assert lib.vhsdecode_gb300_run(ctypes.byref(cfg), ctypes.byref(res)) == native.STATUS_INVALID_ARGUMENT
 
 
-@pytest.mark.parametrize("system", ["PAL", "NTSC"])
-def test_filter_design_matches_oracle(lib, system):
+@pytest.mark.parametrize("system,tape", [("PAL", "VHS"), ("NTSC", "VHS"), ("PAL", "SVHS"),
+                                         ("NTSC", "SVHS")])
+def test_filter_design_matches_oracle(lib, system, tape):
     from vhsd_gb300 import native
     from oracle import filters, formats
     prof = native.PROFILE_PAL if system == "PAL" else native.PROFILE_NTSC
-    rv, v, s, env = native.design_filters(prof)
-    fl = filters.FilterSet(formats.get(system), 40e6)
+    fmt_id = native.FORMAT_SVHS if tape == "SVHS" else native.FORMAT_VHS
+    rv, v, s, env, sub_high, sub_env = native.design_filters(prof, tape_format=fmt_id, sub=True)
+    fl = filters.FilterSet(formats.get(system, tape), 40e6)
 
     def rel(a, b):
         return np.max(np.abs(a - b)) / np.max(np.abs(b))
@@ -108,6 +111,23 @@ def test_filter_design_matches_oracle(lib, system):
     assert rel(v, fl.half("video")) < 1e-10
     assert rel(s, fl.half("video_lp05")) < 1e-10
     np.testing.assert_allclose(env, [fl.env_b[0], fl.env_b[1], fl.env_a1], rtol=1e-15)
+    if tape == "SVHS":
+        # Video carries the measured S-VHS luma table and the 2 MHz high shelf
+        assert rel(sub_high, (fl.video * fl.sub_highpass)[:16385]) < 1e-10
+        np.testing.assert_allclose(sub_env, [fl.sub_amp_b[0], fl.sub_amp_b[1], fl.sub_amp_a1],
+                                   rtol=1e-15)
+    else:
+        assert not np.any(sub_high) and not np.any(sub_env)
+
+
+def test_svhs_custom_luma_table_only_at_tabulated_rates(lib):
+    # the reference skips the file filter at rates without a resource table
+    from vhsd_gb300 import native
+    from oracle import filters, formats
+    fl = filters.FilterSet(formats.get("PAL", "SVHS"), 28e6)
+    _, v, _, _ = native.design_filters(native.PROFILE_PAL, 28.0, tape_format=native.FORMAT_SVHS)
+    assert np.max(np.abs(v - fl.half("video"))) / np.max(np.abs(fl.half("video"))) < 1e-10
+    assert filters.custom_luma_table("svhs-sp-linear-subdeemphasis", 28e6, 32768) is None
 
 
 @pytest.mark.parametrize("system", ["PAL", "NTSC"])

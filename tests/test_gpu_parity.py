@@ -262,3 +262,64 @@ def test_20msps_fields_match_oracle(gpu, precision, ntsc20_capture, ntsc20_oracl
             d = np.abs(tb[i].astype(np.int64).ravel() - f["tbc"].astype(np.int64))
             assert np.mean(d <= 1) >= LSB_FRACTION
             assert s.dropouts(i) == [tuple(x) for x in f["dropouts"]]
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp32_fused", "fp64_plain"])
+@pytest.mark.parametrize("system", ["PAL", "NTSC"])
+def test_svhs_matches_oracle(gpu, system, precision, request):
+    # S-VHS: custom luma filters and the nonlinear sub-deemphasis on the video,
+    # +/-0.5 % timebase wobble and +/-2-sample head-switch jumps in the capture
+    from vhsd_gb300 import native
+    cap, orc = ("svhs_capture", "svhs_oracle") if system == "PAL" else ("svhs_ntsc_capture",
+                                                                         "svhs_ntsc_oracle")
+    rf, _ = request.getfixturevalue(cap)
+    fields, (video, vlp, env, _) = request.getfixturevalue(orc)
+    good = [f for f in fields if "error" not in f]
+    assert len(good) >= 3
+    prof = native.PROFILE_PAL if system == "PAL" else native.PROFILE_NTSC
+    with native.Session(prof, len(rf), precision=precision, tape_format=native.FORMAT_SVHS) as s:
+        r = s.decode(rf, demod_only=True)
+        n = len(video)
+        assert r.stream_samples == n
+        v = s.stream(0, 0, n)
+        y = s.stream(1, 0, n)
+        e = s.stream(2, 0, n)
+        dv = np.abs(v - video)
+        dy = np.abs(y - vlp)
+        assert np.quantile(dv, 0.999) < FREQ_TOL_HZ, np.max(dv)
+        assert np.quantile(dy, 0.999) < FREQ_TOL_HZ, np.max(dy)
+        de = np.abs(e - env) / np.maximum(np.abs(env), 1.0)
+        assert np.quantile(de, 0.999) < 1e-3
+        if precision == 1:
+            assert np.max(dv) < 1.0 and np.max(dy) < 1.0
+        r = s.decode(rf)
+        assert r.fields == len(good)
+        tb = s.tbc()
+        for i, f in enumerate(good):
+            info = s.field(i)
+            assert bool(info.is_first_field) == f["first_field"]
+            assert info.span_start == f["span_start"]
+            assert np.max(np.abs(s.lines(i) - f["locs"])) < LINE_TOL
+            d = np.abs(tb[i].astype(np.int64).ravel() - f["tbc"].astype(np.int64))
+            assert np.mean(d <= 1) >= LSB_FRACTION, (i, np.mean(d <= 1), d.max())
+            assert s.dropouts(i) == [tuple(x) for x in f["dropouts"]]
+
+
+def test_svhs_sub_deemphasis_changes_the_video(gpu, svhs_capture):
+    # the same capture decoded as VHS-filtered S-VHS levels without the
+    # sub-deemphasis branch differs: the correction is really applied
+    from vhsd_gb300 import native
+    from oracle import demod, filters, formats
+    rf, _ = svhs_capture
+    fmt = formats.get("PAL", "SVHS")
+    fl = filters.FilterSet(fmt, 40e6)
+    x = rf[10 * 30720:10 * 30720 + 32768].astype(np.float64)
+    v_sub, _, _, _, _ = demod.demod_block(x, fl, 40e6, None)
+    fl.sub = None
+    v_lin, _, _, _, _ = demod.demod_block(x, fl, 40e6, None)
+    with native.Session(native.PROFILE_PAL, len(rf), tape_format=native.FORMAT_SVHS) as s:
+        s.decode(rf, demod_only=True)
+        got = s.stream(0, 10 * 30720, 30720)
+    keep = slice(1024, 1024 + 30720)
+    assert np.quantile(np.abs(got - v_sub[keep]), 0.999) < FREQ_TOL_HZ
+    assert np.quantile(np.abs(v_sub[keep] - v_lin[keep]), 0.9) > 10 * FREQ_TOL_HZ

@@ -19,21 +19,25 @@ def _windows(rf, n, length):
 
 
 def _run(server, jobs, per_field):
-    """jobs: (stream, profile, offset, samples, max_fields); all submitted before any wait."""
+    """jobs: (stream, profile, offset, samples, max_fields[, tape format]); all submitted
+    before any wait."""
     outs, tickets = [], []
-    for stream, prof, off, x, mf in jobs:
+    for job in jobs:
+        stream, prof, off, x, mf = job[:5]
+        tape = job[5] if len(job) > 5 else 0
         out = np.zeros(mf * per_field[prof], np.uint16)
         tickets.append(server.submit(stream, prof, x, source_offset=off, seek=True, max_fields=mf,
-                                     tbc_out=out))
+                                     tbc_out=out, tape_format=tape))
         outs.append(out)
     res = [server.wait(t) for t in tickets]
     return res, outs
 
 
-def test_window_alone_equals_in_mix(gpu, pal_capture, ntsc_capture):
+def test_window_alone_equals_in_mix(gpu, pal_capture, ntsc_capture, svhs_capture):
     from vhsd_gb300 import native
     pal, _ = pal_capture
     ntsc, _ = ntsc_capture
+    svhs, _ = svhs_capture
     per_field = {native.PROFILE_PAL: 313 * 1135, native.PROFILE_NTSC: 263 * 910}
     length = 1_400_000
     jobs = []
@@ -41,6 +45,8 @@ def test_window_alone_equals_in_mix(gpu, pal_capture, ntsc_capture):
         jobs.append((k, native.PROFILE_PAL, off, x, 2))
     for k, (off, x) in enumerate(_windows(ntsc, 3, length)):
         jobs.append((10 + k, native.PROFILE_NTSC, off, x, 2))
+    for k, (off, x) in enumerate(_windows(svhs, 2, length)):
+        jobs.append((20 + k, native.PROFILE_PAL, off, x, 2, native.FORMAT_SVHS))
     with native.Server(length, workers=1) as sv:
         alone = []
         for j in jobs:

@@ -120,12 +120,28 @@ def test_replace_spikes_known_answers():
 
 def test_format_table_matches_snapshot():
     g = json.load(open(os.path.join(GOLDEN, "format_params.json")))
-    for key, fmt in (("PAL/VHS/sp", formats.PAL_VHS_SP), ("NTSC/VHS/sp", formats.NTSC_VHS_SP)):
+    for key, fmt in (("PAL/VHS/sp", formats.PAL_VHS_SP), ("NTSC/VHS/sp", formats.NTSC_VHS_SP),
+                     ("PAL/SVHS/sp", formats.PAL_SVHS_SP), ("NTSC/SVHS/sp", formats.NTSC_SVHS_SP)):
+        sub = bool(g[key]["rf"].get("use_sub_deemphasis"))
         for k, v in g[key]["sys"].items():
-            assert fmt["sys"][k] == v, (key, k)
+            assert fmt["sys"].get(k) == v, (key, k)
         for k, v in g[key]["rf"].items():
+            if k.startswith("nonlinear_") and not sub:
+                continue   # read only by the sub-deemphasis (and the off-by-default nldeemp)
             mine = fmt["rf"].get(k)
             assert (mine or None) == (v or None) or mine == v, (key, k, mine, v)
+        assert (formats.sub_deemphasis(fmt) is not None) == sub
+
+
+def test_custom_luma_tables_match_reference_resources():
+    # the shipped binary tables are the reference's text resources value for value
+    import hashlib
+    g = json.load(open(os.path.join(GOLDEN, "format_params.json")))["custom_luma_tables_sha256"]
+    data = os.path.join(os.path.dirname(GOLDEN), "..", "vhs-decode-dotnet_gb300", "data")
+    for name, digest in g.items():
+        blob = open(os.path.join(data, name + ".f64"), "rb").read()
+        assert len(blob) == 16385 * 16
+        assert hashlib.sha256(blob).hexdigest() == digest, name
 
 
 def test_vhs_demod_recovers_constant_frequency():

@@ -46,10 +46,12 @@ thread_local std::string g_last_error;
 
 namespace {
 
-bool format_for(uint32_t profile, uint32_t speed, FormatParams& f) {
+bool format_for(uint32_t profile, uint32_t speed, uint32_t tape_format, FormatParams& f) {
     if (speed != VHSDECODE_GB300_TAPE_SPEED_SP) return false;
-    if (profile == VHSDECODE_GB300_PROFILE_PAL) { f = pal_vhs_sp(); return true; }
-    if (profile == VHSDECODE_GB300_PROFILE_NTSC) { f = ntsc_vhs_sp(); return true; }
+    const bool pal = profile == VHSDECODE_GB300_PROFILE_PAL, ntsc = profile == VHSDECODE_GB300_PROFILE_NTSC;
+    if (!pal && !ntsc) return false;
+    if (tape_format == VHSDECODE_GB300_TAPE_FORMAT_VHS) { f = pal ? pal_vhs_sp() : ntsc_vhs_sp(); return true; }
+    if (tape_format == VHSDECODE_GB300_TAPE_FORMAT_SVHS) { f = pal ? pal_svhs_sp() : ntsc_svhs_sp(); return true; }
     return false;
 }
 
@@ -107,9 +109,9 @@ void resolve_span(int64_t intended, int64_t read_len, int64_t& s0, int64_t& slen
 }
 
 void session_init(vhsdecode_gb300_session* s, const vhsdecode_gb300_session_config_v1& c) {
-    if (!format_for(c.profile, c.tape_speed, s->fmt))
+    if (!format_for(c.profile, c.tape_speed, c.tape_format, s->fmt))
         throw Failure(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT,
-                      "unsupported profile / tape speed (PAL or NTSC, SP)");
+                      "unsupported profile / tape speed / tape format (PAL or NTSC, SP, VHS or SVHS)");
     if (!(c.sample_rate_mhz >= 10.0 && c.sample_rate_mhz <= 100.0))
         throw Failure(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "sample_rate_mhz must be within 10..100");
     if (c.precision > 1) throw Failure(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "unknown precision");
@@ -118,7 +120,11 @@ void session_init(vhsdecode_gb300_session* s, const vhsdecode_gb300_session_conf
     s->device = c.device_id;
     s->max_samples = c.max_samples;
     s->sp = SyncParams::make(s->fmt, s->fs);
-    s->filt = design_filters(s->fmt, s->fs);
+    try {
+        s->filt = design_filters(s->fmt, s->fs);
+    } catch (const std::runtime_error& e) {
+        throw Failure(VHSDECODE_GB300_STATUS_INTERNAL_ERROR, e.what());
+    }
     s->lines = s->sp.output_lines + 10;
     s->out_lines = s->sp.output_lines;
     s->outlen = s->fmt.outlinelen;
@@ -160,6 +166,13 @@ void session_init(vhsdecode_gb300_session* s, const vhsdecode_gb300_session_conf
         ck(cudaMemcpy(s->rfv32.p, rv.data(), H * sizeof(float), cudaMemcpyHostToDevice), "upload");
         ck(cudaMemcpy(s->vid32.p, vv.data(), H * sizeof(float2), cudaMemcpyHostToDevice), "upload");
         ck(cudaMemcpy(s->syn32.p, sv.data(), H * sizeof(float2), cudaMemcpyHostToDevice), "upload");
+        if (!s->filt.sub_high.empty()) {
+            std::vector<float2> hv(H);
+            for (int k = 0; k < H; k++)
+                hv[k] = make_float2((float)s->filt.sub_high[k].real(), (float)s->filt.sub_high[k].imag());
+            s->sub32.alloc(H);
+            ck(cudaMemcpy(s->sub32.p, hv.data(), H * sizeof(float2), cudaMemcpyHostToDevice), "upload");
+        }
         std::vector<float2> hi(256), lo(128);
         const double pi = 3.14159265358979323846;
         for (int h = 0; h < 256; h++) {
@@ -216,6 +229,13 @@ void session_init(vhsdecode_gb300_session* s, const vhsdecode_gb300_session_conf
         ck(cudaMemcpy(s->rfv64.p, s->filt.rf_video.data(), H * sizeof(double), cudaMemcpyHostToDevice), "upload");
         ck(cudaMemcpy(s->vid64.p, vv.data(), H * sizeof(double2), cudaMemcpyHostToDevice), "upload");
         ck(cudaMemcpy(s->syn64.p, sv.data(), H * sizeof(double2), cudaMemcpyHostToDevice), "upload");
+        if (!s->filt.sub_high.empty()) {
+            std::vector<double2> hv(H);
+            for (int k = 0; k < H; k++)
+                hv[k] = make_double2(s->filt.sub_high[k].real(), s->filt.sub_high[k].imag());
+            s->sub64.alloc(H);
+            ck(cudaMemcpy(s->sub64.p, hv.data(), H * sizeof(double2), cudaMemcpyHostToDevice), "upload");
+        }
         s->pwork.alloc(4 * (size_t)kBlock);
         s->pdwork.alloc(3 * (size_t)kBlock);
         s->pfwork.alloc(kBlock + 16);
@@ -304,6 +324,22 @@ void session_free(vhsdecode_gb300_session* s) {
     if (s->own_stream) cudaStreamDestroy(s->own_stream);
 }
 
+template <typename T, typename T2>
+SubDeemphT<T, T2> sub_params(const FormatParams& f, const FilterSpectra& filt) {
+    SubDeemphT<T, T2> d{};
+    d.inv_half_dev = (T)(1.0 / (f.sub_deviation / 2.0));
+    d.b0 = (T)filt.sub_b0;
+    d.b1 = (T)filt.sub_b1;
+    d.a1 = (T)filt.sub_a1;
+    d.exponent = (T)f.sub_exp;
+    d.scale1 = std::isnan(f.sub_scale1) ? (T)1 : (T)f.sub_scale1;
+    d.scale2 = std::isnan(f.sub_scale2) ? (T)1 : (T)f.sub_scale2;
+    d.logistic_mid = std::isnan(f.sub_logistic_mid) ? (T)0 : (T)f.sub_logistic_mid;
+    d.logistic_rate = std::isnan(f.sub_logistic_rate) ? (T)0 : (T)f.sub_logistic_rate;
+    d.static_factor = (T)f.sub_static;
+    return d;
+}
+
 FastDemodParams fp32_params(vhsdecode_gb300_session* s, const int16_t* rf_dev) {
     FastDemodParams p{};
     p.rf = rf_dev;
@@ -325,6 +361,10 @@ FastDemodParams fp32_params(vhsdecode_gb300_session* s, const int16_t* rf_dev) {
     p.env_out = s->e32.p;
     p.scratch = s->scratch.p;
     p.repair_count = s->repair.p;
+    if (s->sub32.p) {
+        p.sub = sub_params<float, float2>(s->fmt, s->filt);
+        p.sub.high = s->sub32.p;
+    }
     return p;
 }
 
@@ -355,6 +395,10 @@ void run_demod(vhsdecode_gb300_session* s, const int16_t* rf_dev, int64_t nblock
         p.flag = s->pflag.p;
         p.mask = s->pmask.p;
         p.blk = s->pblk.p;
+        if (s->sub64.p) {
+            p.sub = sub_params<double, double2>(s->fmt, s->filt);
+            p.sub.high = s->sub64.p;
+        }
         // The capture lives in s->rf or a caller buffer; the graph bakes the
         // pointer, so rebuild it when the input pointer changes.
         if (!s->plain_graph || s->graph_rf != rf_dev) {
@@ -806,7 +850,7 @@ void decode_plain(vhsdecode_gb300_session* s, const int16_t* rf_dev, uint64_t n,
     int64_t stream_len = nblocks * kStride;
     ck(cudaEventRecord(s->ev[1], cs), "event");
     run_demod(s, rf_dev, nblocks);
-    s->launches += (uint32_t)(nblocks * kPlainBlockKernels);
+    s->launches += (uint32_t)(nblocks * (kPlainBlockKernels + (s->sub64.p ? kPlainSubKernels : 0)));
     s->segments = 1;
     ck(cudaEventRecord(s->ev[2], cs), "event");
     if (!demod_only && nblocks > 0) {
@@ -999,8 +1043,13 @@ VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_run(
     const vhsdecode_gb300_config_v1* config, vhsdecode_gb300_result_v1* result) {
     return guard([&]() -> int32_t {
         if (!config || !result) return fail(VHSDECODE_GB300_STATUS_NULL_POINTER, "null argument");
-        if (config->struct_size != sizeof(vhsdecode_gb300_config_v1))
+        if (config->struct_size != sizeof(vhsdecode_gb300_config_v1) &&
+            config->struct_size != sizeof(vhsdecode_gb300_config_v2))
             return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "config struct_size mismatch");
+        const uint32_t tape_format =
+            config->struct_size == sizeof(vhsdecode_gb300_config_v2)
+                ? reinterpret_cast<const vhsdecode_gb300_config_v2*>(config)->tape_format
+                : (uint32_t)VHSDECODE_GB300_TAPE_FORMAT_VHS;
         if (result->struct_size != sizeof(vhsdecode_gb300_result_v1))
             return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "result struct_size mismatch");
         if (!config->read_callback) return fail(VHSDECODE_GB300_STATUS_NULL_POINTER, "read_callback is null");
@@ -1036,6 +1085,7 @@ VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_run(
         sc.struct_size = sizeof(sc);
         sc.profile = config->profile;
         sc.tape_speed = config->tape_speed;
+        sc.tape_format = tape_format;
         sc.device_id = config->device_id;
         sc.sample_rate_mhz = config->sample_rate_mhz;
         sc.max_samples = rf.size();
@@ -1210,13 +1260,30 @@ VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_session_tbc_dev
 }
 
 VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_design_filters(
-    uint32_t profile, uint32_t speed, double mhz, double* rf_video, double* video, double* sync, double* env) {
+    uint32_t profile, uint32_t speed, uint32_t tape_format, double mhz, double* rf_video, double* video,
+    double* sync, double* sub_high, double* env) {
     return guard([&]() -> int32_t {
         if (!rf_video || !video || !sync || !env) return fail(VHSDECODE_GB300_STATUS_NULL_POINTER, "null output");
         FormatParams f;
-        if (!format_for(profile, speed, f)) return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "unsupported profile");
+        if (!format_for(profile, speed, tape_format, f))
+            return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "unsupported profile");
         if (!(mhz > 0)) return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "sample rate must be positive");
-        FilterSpectra fs = design_filters(f, mhz * 1e6);
+        FilterSpectra fs;
+        try {
+            fs = design_filters(f, mhz * 1e6);
+        } catch (const std::runtime_error& e) {
+            return fail(VHSDECODE_GB300_STATUS_INTERNAL_ERROR, e.what());
+        }
+        if (sub_high) {
+            for (int k = 0; k < kHalf; k++) {
+                std::complex<double> v = fs.sub_high.empty() ? std::complex<double>() : fs.sub_high[(size_t)k];
+                sub_high[2 * k] = v.real();
+                sub_high[2 * k + 1] = v.imag();
+            }
+        }
+        env[3] = fs.sub_b0;
+        env[4] = fs.sub_b1;
+        env[5] = fs.sub_a1;
         for (int k = 0; k < kHalf; k++) {
             rf_video[k] = fs.rf_video[(size_t)k];
             video[2 * k] = fs.video[(size_t)k].real();
@@ -1239,7 +1306,8 @@ VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_field_sync(
         if ((!starts || !lengths) && npulses) return fail(VHSDECODE_GB300_STATUS_NULL_POINTER, "null pulses");
         if (!state || !out || !locs_count) return fail(VHSDECODE_GB300_STATUS_NULL_POINTER, "null output");
         FormatParams f;
-        if (!format_for(profile, 0, f)) return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "unsupported profile");
+        if (!format_for(profile, 0, VHSDECODE_GB300_TAPE_FORMAT_VHS, f))
+            return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "unsupported profile");
         SyncParams sp = SyncParams::make(f, mhz * 1e6);
         std::vector<Pulse> raw;
         for (uint64_t i = 0; i < npulses; i++) raw.push_back({starts[i], lengths[i]});

@@ -13,6 +13,9 @@
 //   D  = rfft(d - ire0)                                    (stage 4)
 //   video = irfft(D * Video) + ire0, sync = roll(irfft(D * VideoLowPass05), -32) + ire0
 //                                                          (stage 5)
+//   S-VHS sub-deemphasis: a = ifft(one-sided D * Video * HighPass) (the
+//   analytic signal of the high part), amp = |a| low-passed forward and
+//   backward, video -= Re a * (1 - map(amp))                (stage 6)
 // and writes the kept samples [1024, 31744) of video, sync and envelope to the
 // stitched stream at stream index b*30720 + (n - 1024).
 //
@@ -250,6 +253,119 @@ __device__ __forceinline__ float chunk_val(float2* local, float2* remote, int ra
     return b[sx(i)].y;
 }
 
+// First-order low-pass filtfilt (the one-section case of
+// SosFilter.ApplyForwardBackward / ApplyForwardBackwardFloat32,
+// Core/Dsp/SosFilter.cs:178-340) of component y of the block held in buf.
+// Warp w of this rank covers samples [n0, n0 + 1024) as four rows of 256; in
+// each row lane l runs the recurrence over its 8 consecutive samples and a warp
+// affine scan joins the lanes.  The state entering the warp's range comes from
+// a 256-sample halo started at zero (for the 590 / 700 kHz filters at 40 MSPS
+// the memory c^256 is below 1e-10); at the block edges the recursion starts
+// from zero instead of the padded steady-state start, which only moves samples
+// the overlap-save cut drops.  Component y is overwritten by the forward pass.
+// emit(row_start, ms, wv) receives the final values wv[0..8) of samples
+// ms..ms+7, rows in descending order.  Called by every thread of both CTAs.
+template <typename Emit>
+__device__ __forceinline__ void filtfilt_rows(float2* buf, float2* rbuf, int rank, int warp, int lane,
+                                              float b0, float b1, float a1, cg::cluster_group& cluster,
+                                              Emit emit) {
+    const int lc = warp >> 3;
+    const int c = 2 * lc + rank;
+    const int n0 = c * 8192 + (warp & 7) * 1024;
+    const float cc = -a1;
+    const float gk = b1 - a1 * b0;   // state input gain
+    float c8 = cc;
+#pragma unroll
+    for (int k = 1; k < 8; k++) c8 *= cc;
+    const float* lbuf = reinterpret_cast<const float*>(buf);
+    auto local_y = [&](int n) { return lbuf[2 * sx((lc << 13) | (n & 8191)) + 1]; };
+    float yv[32];
+    // forward: z1' = cc*z1 + gk*e ; y = b0*e + z1
+    float carry = 0.0f;
+    if (n0 >= 256) {
+        int hs = n0 - 256 + lane * 8;
+        float st = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 8; k++) st = fmaf(cc, st, gk * chunk_val(buf, rbuf, rank, hs + k));
+        Aff inc = warp_scan_incl(Aff{c8, st}, lane);
+        carry = __shfl_sync(0xffffffffu, inc.b, 31);
+    }
+#pragma unroll
+    for (int row = 0; row < 4; row++) {
+        int ms = n0 + row * 256 + lane * 8;
+        float ev[8];
+        float st = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            ev[k] = local_y(ms + k);
+            st = fmaf(cc, st, gk * ev[k]);
+        }
+        Aff inc = warp_scan_incl(Aff{c8, st}, lane);
+        float pb = __shfl_up_sync(0xffffffffu, inc.b, 1);
+        float pa = __shfl_up_sync(0xffffffffu, inc.a, 1);
+        float z = lane == 0 ? carry : fmaf(pa, carry, pb);
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            yv[row * 8 + k] = fmaf(b0, ev[k], z);
+            z = fmaf(cc, z, gk * ev[k]);
+        }
+        carry = __shfl_sync(0xffffffffu, z, 31);
+    }
+    cluster.sync();
+    {
+        float* wbuf = reinterpret_cast<float*>(buf);
+#pragma unroll
+        for (int row = 0; row < 4; row++) {
+#pragma unroll
+            for (int k = 0; k < 8; k++) {
+                int n = n0 + row * 256 + lane * 8 + k;
+                wbuf[2 * sx((lc << 13) | (n & 8191)) + 1] = yv[row * 8 + k];
+            }
+        }
+    }
+    cluster.sync();
+    // backward: w = b0*y + z1 ; z1' = cc*z1 + gk*y  (from high n to low n)
+    const int nend = n0 + 1024;
+    carry = 0.0f;
+    if (nend + 256 <= N) {
+        int hs = nend + lane * 8;  // halo samples [nend, nend+256)
+        float st = 0.0f;
+#pragma unroll
+        for (int k = 7; k >= 0; k--) st = fmaf(cc, st, gk * chunk_val(buf, rbuf, rank, hs + k));
+        Aff inc = warp_scan_incl_rev(Aff{c8, st}, lane);
+        carry = __shfl_sync(0xffffffffu, inc.b, 0);
+    }
+#pragma unroll
+    for (int row = 3; row >= 0; row--) {
+        int ms = n0 + row * 256 + lane * 8;
+        float st = 0.0f;
+#pragma unroll
+        for (int k = 7; k >= 0; k--) st = fmaf(cc, st, gk * yv[row * 8 + k]);
+        Aff inc = warp_scan_incl_rev(Aff{c8, st}, lane);
+        float nb = __shfl_down_sync(0xffffffffu, inc.b, 1);
+        float na = __shfl_down_sync(0xffffffffu, inc.a, 1);
+        float z = lane == 31 ? carry : fmaf(na, carry, nb);
+        float wv[8];
+#pragma unroll
+        for (int k = 7; k >= 0; k--) {
+            float y = yv[row * 8 + k];
+            wv[k] = fmaf(b0, y, z);
+            z = fmaf(cc, z, gk * y);
+        }
+        carry = __shfl_sync(0xffffffffu, z, 0);
+        emit(n0 + row * 256, ms, wv);
+    }
+}
+
+// Nonlinear gain of the low-passed sub-deemphasis amplitude
+// (Core/Dsp/RfDemodulator.cs:2963-2981).
+__device__ __forceinline__ float sub_gain(float amp, const SubDeemph& s) {
+    amp = fmaxf(0.0f, amp) * s.scale1;
+    amp = powf(amp, s.exponent) * s.scale2;
+    if (s.logistic_rate > 0.0f) amp *= 1.0f / (1.0f + expf(-s.logistic_rate * (amp - s.logistic_mid)));
+    return amp;
+}
+
 // One RF block into this rank's packed DIF input: rank 0 gets a + b, rank 1
 // (a - b) W^(2p), p in [0, 8192), where a / b are the complex pairs of the
 // block's first / second half.  W^(2p) = W^(8v) W^(2e) for p = 4v + e.
@@ -475,106 +591,18 @@ vhsd_demod_fp32_kernel(FastDemodParams p) {
             for (int t = 0; t < 32; t++) buf[sx(tid + t * T)] = make_float2(dv[t], rv[t]);
         }
         cluster.sync();   // the envelope halos read the partner's buf
-        // ---------------- envelope: filtfilt with halo-started warp scans --
-        // Warp w of this rank covers samples [n0, n0 + 1024) as four rows of
-        // 256; in each row lane l runs the recurrence over its 8 consecutive
-        // samples and a warp affine scan joins the lanes.  The state entering
-        // the warp's range comes from a 256-sample halo started at zero (the
-        // filter's memory c^256 is below 1e-12).
+        // ---------------- envelope: 700 kHz filtfilt of |Re z[n-4]| ----------
         {
-            const int lc = warp >> 3;
-            const int c = 2 * lc + rank;
-            const int n0 = c * 8192 + (warp & 7) * 1024;
-            const float b0 = p.env_b0, b1 = p.env_b1, a1 = p.env_a1;
-            const float cc = -a1;
-            const float gk = b1 - a1 * b0;   // state input gain
-            float c8 = cc;
-#pragma unroll
-            for (int k = 1; k < 8; k++) c8 *= cc;
-            const float* lbuf = reinterpret_cast<const float*>(buf);
-            auto local_y = [&](int n) { return lbuf[2 * sx((lc << 13) | (n & 8191)) + 1]; };
-            float yv[32];
-            // forward: z1' = cc*z1 + gk*e ; y = b0*e + z1
-            float carry = 0.0f;
-            if (n0 >= 256) {
-                int hs = n0 - 256 + lane * 8;
-                float st = 0.0f;
-#pragma unroll
-                for (int k = 0; k < 8; k++) st = fmaf(cc, st, gk * chunk_val(buf, rbuf, rank, hs + k));
-                Aff inc = warp_scan_incl(Aff{c8, st}, lane);
-                carry = __shfl_sync(0xffffffffu, inc.b, 31);
-            }
-#pragma unroll
-            for (int row = 0; row < 4; row++) {
-                int ms = n0 + row * 256 + lane * 8;
-                float ev[8];
-                float st = 0.0f;
-#pragma unroll
-                for (int k = 0; k < 8; k++) {
-                    ev[k] = local_y(ms + k);
-                    st = fmaf(cc, st, gk * ev[k]);
-                }
-                Aff inc = warp_scan_incl(Aff{c8, st}, lane);
-                float pb = __shfl_up_sync(0xffffffffu, inc.b, 1);
-                float pa = __shfl_up_sync(0xffffffffu, inc.a, 1);
-                float z = lane == 0 ? carry : fmaf(pa, carry, pb);
-#pragma unroll
-                for (int k = 0; k < 8; k++) {
-                    yv[row * 8 + k] = fmaf(b0, ev[k], z);
-                    z = fmaf(cc, z, gk * ev[k]);
-                }
-                carry = __shfl_sync(0xffffffffu, z, 31);
-            }
-            cluster.sync();
-            {
-                float* wbuf = reinterpret_cast<float*>(buf);
-#pragma unroll
-                for (int row = 0; row < 4; row++) {
-#pragma unroll
-                    for (int k = 0; k < 8; k++) {
-                        int n = n0 + row * 256 + lane * 8 + k;
-                        wbuf[2 * sx((lc << 13) | (n & 8191)) + 1] = yv[row * 8 + k];
-                    }
-                }
-            }
-            cluster.sync();
-            // backward: w = b0*y + z1 ; z1' = cc*z1 + gk*y  (from high n to low n)
-            const int nend = n0 + 1024;
-            carry = 0.0f;
-            if (nend + 256 <= N) {
-                int hs = nend + lane * 8;  // halo samples [nend, nend+256)
-                float st = 0.0f;
-#pragma unroll
-                for (int k = 7; k >= 0; k--) st = fmaf(cc, st, gk * chunk_val(buf, rbuf, rank, hs + k));
-                Aff inc = warp_scan_incl_rev(Aff{c8, st}, lane);
-                carry = __shfl_sync(0xffffffffu, inc.b, 0);
-            }
             float* envo = p.env_out + (blk + p.first_block) * (int64_t)S - CUT;
-#pragma unroll
-            for (int row = 3; row >= 0; row--) {
-                int ms = n0 + row * 256 + lane * 8;
-                float st = 0.0f;
-#pragma unroll
-                for (int k = 7; k >= 0; k--) st = fmaf(cc, st, gk * yv[row * 8 + k]);
-                Aff inc = warp_scan_incl_rev(Aff{c8, st}, lane);
-                float nb = __shfl_down_sync(0xffffffffu, inc.b, 1);
-                float na = __shfl_down_sync(0xffffffffu, inc.a, 1);
-                float z = lane == 31 ? carry : fmaf(na, carry, nb);
-                float wv[8];
-#pragma unroll
-                for (int k = 7; k >= 0; k--) {
-                    float y = yv[row * 8 + k];
-                    wv[k] = fmaf(b0, y, z);
-                    z = fmaf(cc, z, gk * y);
-                }
-                carry = __shfl_sync(0xffffffffu, z, 0);
-                int rs = n0 + row * 256;   // rows lie wholly inside or outside the kept range
-                if (rs >= CUT && rs < CUT + S) {
-                    float4* o = reinterpret_cast<float4*>(envo + ms);
-                    o[0] = make_float4(wv[0], wv[1], wv[2], wv[3]);
-                    o[1] = make_float4(wv[4], wv[5], wv[6], wv[7]);
-                }
-            }
+            filtfilt_rows(buf, rbuf, rank, warp, lane, p.env_b0, p.env_b1, p.env_a1, cluster,
+                          [&](int rs, int ms, const float* wv) {
+                              // rows lie wholly inside or outside the kept range
+                              if (rs >= CUT && rs < CUT + S) {
+                                  float4* o = reinterpret_cast<float4*>(envo + ms);
+                                  o[0] = make_float4(wv[0], wv[1], wv[2], wv[3]);
+                                  o[1] = make_float4(wv[4], wv[5], wv[6], wv[7]);
+                              }
+                          });
         }
         // ---------------- stage 4: forward FFT of (demod - ire0) -----------
         {
@@ -602,6 +630,12 @@ vhsd_demod_fp32_kernel(FastDemodParams p) {
         }
         fft8192<false, 1>(buf, sh.tw, tid);
         post_half(sh, rank, tid, [&](int k, float2 v) { return v; });
+        const bool sub = p.sub.high != nullptr;
+        float2* xs = reinterpret_cast<float2*>(sh.theta);   // D kept for stage 6
+        if (sub) {
+            for (int q = tid; q < 8192; q += T) xs[q] = buf[sx(q)];
+            __syncthreads();   // stage 5 rewrites these bins in place
+        }
         // ---------------- stage 5: video and sync real inverse FFTs ---------
         {
             // F = X * H ; P[k] = (F[k] + F*[M-k])/2 + i (F[k] - F*[M-k]) W_N^-k / 2, scaled 1/M
@@ -681,6 +715,79 @@ vhsd_demod_fp32_kernel(FastDemodParams p) {
                     }
                 }
             }
+        }
+        if (sub) {
+            // ---------------- stage 6: S-VHS sub-deemphasis -------------------
+            // A[k] = D[k] Video[k] HighPass[k] (x2 for 0 < k < N/2, real part
+            // at 0 and N/2, zero above): ifft(A) is the analytic signal of
+            // high = irfft(D Video HighPass), whose real part is `high` and
+            // whose modulus is the reference's analytic magnitude
+            // (BuildAnalyticMagnitudeWithWorkspace, RfDemodulator.cs:3181-3220).
+            // The video written above is corrected in place: every sample a
+            // rank stores lies in its own two chunks.
+            cluster.sync();   // the partner has finished reading this buf
+            const float s2 = 2.0f * inv_n;
+            for (int q = tid; q < 8192; q += T) {
+                int k = 2 * q + rank;
+                float2 v = cmul(xs[q], __ldg(p.sub.high + k));
+                buf[sx(q)] = (k == 0) ? make_float2(v.x * inv_n, 0.0f) : make_float2(v.x * s2, v.y * s2);
+            }
+            if (rank == 0) {
+                if (tid == 0) {
+                    float2 v = cmul(sh.nyq, __ldg(p.sub.high + M));
+                    buf[sx(8192)] = make_float2(v.x * inv_n, 0.0f);
+                }
+                for (int i = 8193 + tid; i < M; i += T) buf[sx(i)] = make_float2(0.f, 0.f);
+            } else {
+                for (int i = 8192 + tid; i < M; i += T) buf[sx(i)] = make_float2(0.f, 0.f);
+            }
+            __syncthreads();
+            fft16384<true>(buf, sh.tw, tid);
+            cluster.sync();
+            {
+                // (high, |a| * 2 / deviation) in the time layout of the envelope
+                float2 o1[16], o2[16];
+#pragma unroll
+                for (int t = 0; t < 16; t++) {
+                    int nl = tid + t * T;
+                    int n = nl + rank * 8192;
+                    float2 loc = buf[sx(n)];
+                    float2 rem = rbuf[sx(n)];
+                    float2 a = rank == 0 ? loc : rem;
+                    float2 b = rank == 0 ? rem : loc;
+                    float2 wb = cmulc(b, w32k(sh.tw, n));
+                    float2 z1 = cadd(a, wb), z2 = csub(a, wb);
+                    o1[t] = make_float2(z1.x, hypotf(z1.x, z1.y) * p.sub.inv_half_dev);
+                    o2[t] = make_float2(z2.x, hypotf(z2.x, z2.y) * p.sub.inv_half_dev);
+                }
+                cluster.sync();
+#pragma unroll
+                for (int t = 0; t < 16; t++) {
+                    int nl = tid + t * T;
+                    buf[sx(nl)] = o1[t];
+                    buf[sx(8192 + nl)] = o2[t];
+                }
+            }
+            cluster.sync();
+            float* vfix = p.video_out + (blk + p.first_block) * (int64_t)S - CUT;
+            const float stat = p.sub.static_factor;
+            filtfilt_rows(buf, rbuf, rank, warp, lane, p.sub.b0, p.sub.b1, p.sub.a1, cluster,
+                          [&](int rs, int ms, const float* wv) {
+                              if (rs >= CUT && rs < CUT + S) {
+                                  float4* o = reinterpret_cast<float4*>(vfix + ms);
+                                  float4 va = o[0], vb = o[1];
+                                  float vv[8] = {va.x, va.y, va.z, va.w, vb.x, vb.y, vb.z, vb.w};
+                                  const int base = ((ms >> 14) << 13) | (ms & 8191);   // local index of ms
+#pragma unroll
+                                  for (int k = 0; k < 8; k++) {
+                                      float h = buf[sx(base + k)].x;
+                                      float g = sub_gain(wv[k], p.sub);
+                                      vv[k] -= h * (1.0f - g) + h * stat;
+                                  }
+                                  o[0] = make_float4(vv[0], vv[1], vv[2], vv[3]);
+                                  o[1] = make_float4(vv[4], vv[5], vv[6], vv[7]);
+                              }
+                          });
         }
         cluster.sync();
     }

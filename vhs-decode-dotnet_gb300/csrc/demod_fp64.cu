@@ -231,6 +231,133 @@ __global__ void __launch_bounds__(1024) k_envelope(const double2* z, float* work
     }
 }
 
+// Sub-deemphasis (ApplySubDeemphasisRealCore, Core/Dsp/RfDemodulator.cs:2852-2990),
+// step 1: one-sided spectrum whose inverse is the analytic signal of
+// high = irfft(D Video HighPass): x2 for 0 < k < N/2, real part at 0 and N/2
+// (what a c2r inverse keeps), zero above; scaled 1/N.
+__global__ void k_sub_spec(const double2* D, const double2* g, double2* A) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= N) return;
+    double2 v = make_double2(0.0, 0.0);
+    if (k <= H) {
+        v = cmul(D[k], g[k]);
+        if (k == 0 || k == H) v = make_double2(v.x / N, 0.0);
+        else v = make_double2(2.0 * v.x / N, 2.0 * v.y / N);
+    }
+    A[k] = v;
+}
+
+struct Aff64 { double a, b; };
+__device__ __forceinline__ Aff64 aff64_then(Aff64 first, Aff64 second) {
+    return Aff64{second.a * first.a, fma(second.a, first.b, second.b)};
+}
+__device__ __forceinline__ Aff64 aff64_scan(Aff64 v, int lane) {
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        double pa = __shfl_up_sync(0xffffffffu, v.a, o), pb = __shfl_up_sync(0xffffffffu, v.b, o);
+        if (lane >= o) v = aff64_then(Aff64{pa, pb}, v);
+    }
+    return v;
+}
+__device__ __forceinline__ Aff64 aff64_scan_rev(Aff64 v, int lane) {
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        double pa = __shfl_down_sync(0xffffffffu, v.a, o), pb = __shfl_down_sync(0xffffffffu, v.b, o);
+        if (lane + o < 32) v = aff64_then(Aff64{pa, pb}, v);
+    }
+    return v;
+}
+
+__device__ __forceinline__ double sub_gain64(double amp, const SubDeemph64& s) {
+    amp = fmax(0.0, amp) * s.scale1;
+    amp = pow(amp, s.exponent) * s.scale2;
+    if (s.logistic_rate > 0.0) amp *= 1.0 / (1.0 + exp(-s.logistic_rate * (amp - s.logistic_mid)));
+    return amp;
+}
+
+// Step 2: amp[n] = |a[n]| * 2 / deviation.
+__global__ void k_sub_mag(const double2* a, double* amp, SubDeemph64 sub) {
+    int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= N) return;
+    amp[n] = hypot(a[n].x, a[n].y) * sub.inv_half_dev;
+}
+
+// Steps 3-4: first-order low-pass filtfilt of amp in binary64, one warp (one
+// CTA) per 1024-sample range, 32 ranges per block: the range is four rows of
+// 256 (8 consecutive samples per lane) joined by affine warp scans, and the
+// state entering it comes from the 1024 samples before it (after it, backward)
+// started at zero, where the filter's memory c^1024 is below 1e-40; at the
+// block edges the recursion starts from zero instead of the padded
+// steady-state start, which only moves samples the overlap-save cut drops.
+// Forward: amp -> fwd.  Backward: fwd -> out.
+template <bool BACKWARD>
+__global__ void __launch_bounds__(32) k_sub_filt(const double* in, double* out, SubDeemph64 sub) {
+    const int lane = threadIdx.x;
+    const int n0 = blockIdx.x * 1024;
+    const double cc = -sub.a1, gk = sub.b1 - sub.a1 * sub.b0, b0 = sub.b0;
+    double c8 = cc;
+#pragma unroll
+    for (int k = 1; k < 8; k++) c8 *= cc;
+    double carry = 0.0;
+    if (!BACKWARD) {
+        if (n0 >= 1024) {
+            for (int hr = 0; hr < 4; hr++) {
+                int ms = n0 - 1024 + hr * 256 + lane * 8;
+                double ev[8], st = 0.0;
+                for (int k = 0; k < 8; k++) { ev[k] = in[ms + k]; st = fma(cc, st, gk * ev[k]); }
+                Aff64 inc = aff64_scan(Aff64{c8, st}, lane);
+                double pb = __shfl_up_sync(0xffffffffu, inc.b, 1), pa = __shfl_up_sync(0xffffffffu, inc.a, 1);
+                double z = lane == 0 ? carry : fma(pa, carry, pb);
+                for (int k = 0; k < 8; k++) z = fma(cc, z, gk * ev[k]);
+                carry = __shfl_sync(0xffffffffu, z, 31);
+            }
+        }
+        for (int row = 0; row < 4; row++) {
+            int ms = n0 + row * 256 + lane * 8;
+            double ev[8], st = 0.0;
+            for (int k = 0; k < 8; k++) { ev[k] = in[ms + k]; st = fma(cc, st, gk * ev[k]); }
+            Aff64 inc = aff64_scan(Aff64{c8, st}, lane);
+            double pb = __shfl_up_sync(0xffffffffu, inc.b, 1), pa = __shfl_up_sync(0xffffffffu, inc.a, 1);
+            double z = lane == 0 ? carry : fma(pa, carry, pb);
+            for (int k = 0; k < 8; k++) { out[ms + k] = fma(b0, ev[k], z); z = fma(cc, z, gk * ev[k]); }
+            carry = __shfl_sync(0xffffffffu, z, 31);
+        }
+    } else {
+        const int nend = n0 + 1024;
+        if (nend + 1024 <= N) {
+            for (int hr = 3; hr >= 0; hr--) {
+                int ms = nend + hr * 256 + lane * 8;
+                double ev[8], st = 0.0;
+                for (int k = 7; k >= 0; k--) { ev[k] = in[ms + k]; st = fma(cc, st, gk * ev[k]); }
+                Aff64 inc = aff64_scan_rev(Aff64{c8, st}, lane);
+                double nb = __shfl_down_sync(0xffffffffu, inc.b, 1), na = __shfl_down_sync(0xffffffffu, inc.a, 1);
+                double z = lane == 31 ? carry : fma(na, carry, nb);
+                for (int k = 7; k >= 0; k--) z = fma(cc, z, gk * ev[k]);
+                carry = __shfl_sync(0xffffffffu, z, 0);
+            }
+        }
+        for (int row = 3; row >= 0; row--) {
+            int ms = n0 + row * 256 + lane * 8;
+            double ev[8], st = 0.0;
+            for (int k = 7; k >= 0; k--) { ev[k] = in[ms + k]; st = fma(cc, st, gk * ev[k]); }
+            Aff64 inc = aff64_scan_rev(Aff64{c8, st}, lane);
+            double nb = __shfl_down_sync(0xffffffffu, inc.b, 1), na = __shfl_down_sync(0xffffffffu, inc.a, 1);
+            double z = lane == 31 ? carry : fma(na, carry, nb);
+            for (int k = 7; k >= 0; k--) { out[ms + k] = fma(b0, ev[k], z); z = fma(cc, z, gk * ev[k]); }
+            carry = __shfl_sync(0xffffffffu, z, 0);
+        }
+    }
+}
+
+// Step 5, elementwise: video[n] -= Re a[n] (1 - map(amp[n])) + Re a[n] static_factor.
+__global__ void k_sub_apply(const double2* a, const double* amp, double2* video, SubDeemph64 sub) {
+    int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= N) return;
+    double h = a[n].x;
+    double g = sub_gain64(amp[n], sub);
+    video[n].x -= h * (1.0 - g) + h * sub.static_factor;
+}
+
 __global__ void k_real_to_complex(const double* d, double2* out) {
     int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= N) return;
@@ -291,6 +418,14 @@ cudaError_t launch_demod_fp64_block(const PlainDemodParams& p, cudaStream_t s) {
     fft<false>(w0, w1, s);                         // D in w1
     k_filter_spec<<<G, B, 0, s>>>(w1, p.video, w2);
     fft<true>(w2, w3, s);                          // video in w3
+    if (p.sub.high) {
+        k_sub_spec<<<G, B, 0, s>>>(w1, p.sub.high, w2);
+        fft<true>(w2, w0, s);                      // analytic high part in w0
+        k_sub_mag<<<G, B, 0, s>>>(w0, dd, p.sub);
+        k_sub_filt<false><<<N / 1024, 32, 0, s>>>(dd, d, p.sub);
+        k_sub_filt<true><<<N / 1024, 32, 0, s>>>(d, dd, p.sub);
+        k_sub_apply<<<G, B, 0, s>>>(w0, dd, w3, p.sub);
+    }
     k_store<<<(kStride + B - 1) / B, B, 0, s>>>(w3, blk, p.video_out, 0);
     k_filter_spec<<<G, B, 0, s>>>(w1, p.sync, w2);
     fft<true>(w2, w0, s);                          // sync in w0

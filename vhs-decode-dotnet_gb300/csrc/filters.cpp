@@ -11,13 +11,24 @@
 //             complex de-emphasis shelf.
 //   VideoLowPass05 (:1093-1102, :1248-1263): Video reference x 65-tap Hamming
 //             FIR at 0.5 MHz.
+//   Custom luma filters (:1560-1609, S-VHS): Video x measured response table
+//             x high shelf designed with sampleRate/2 as its rate argument.
+//   Sub-deemphasis high-pass (RfDemodulator.cs:3101-3142): first-order
+//             Butterworth SOS at nonlinear_highpass_freq; amplitude low-pass
+//             first-order Butterworth at nonlinear_amp_lpf_freq
+//             (IirFilterDesign.cs:1078-1114).
 // Butterworth low/high-pass magnitudes use the bilinear closed form
 // |H|^2 = 1 / (1 + (tan(w/2) / tan(wc/2))^(+-2N)); the band-pass keeps the
 // transfer-function (polynomial) evaluation the reference uses.
 #include "filters.hpp"
 
+#include <dlfcn.h>
+
 #include <cmath>
 #include <complex>
+#include <cstdio>
+#include <stdexcept>
+#include <string>
 #include <vector>
 
 namespace vhsd {
@@ -129,6 +140,34 @@ static void peaking(double norm_freq, double gain_db, double bw_oct, std::vector
     a = {1.0, d1 / d0, d2 / d0};
 }
 
+// Folder of the data files: ../data relative to the folder of this library.
+static std::string data_dir() {
+    Dl_info info{};
+    if (dladdr(reinterpret_cast<void*>(&data_dir), &info) && info.dli_fname) {
+        std::string so(info.dli_fname);
+        size_t slash = so.rfind('/');
+        std::string dir = slash == std::string::npos ? std::string(".") : so.substr(0, slash);
+        return dir + "/../data";
+    }
+    return "data";
+}
+
+bool load_custom_luma(double fs, std::vector<cd>& half) {
+    const long rate = (long)fs;   // (int)sampleRateHz in the resource name
+    if (rate != 40000000L && rate != 17734475L) return false;   // the reference ships these two
+    std::string path = data_dir() + "/svhs-sp-linear-subdeemphasis-" + std::to_string(rate) + ".f64";
+    FILE* fp = std::fopen(path.c_str(), "rb");
+    if (!fp) throw std::runtime_error("custom luma filter table missing: " + path);
+    const int H = 32768 / 2 + 1;
+    std::vector<double> raw((size_t)2 * H);
+    size_t got = std::fread(raw.data(), sizeof(double), raw.size(), fp);
+    std::fclose(fp);
+    if (got != raw.size()) throw std::runtime_error("custom luma filter table truncated: " + path);
+    half.resize((size_t)H);
+    for (int k = 0; k < H; k++) half[(size_t)k] = cd(raw[(size_t)2 * k], raw[(size_t)2 * k + 1]);
+    return true;
+}
+
 static double sinc(double x) {
     if (std::fabs(x) < 1e-12) return 1.0;
     double s = kPi * x;
@@ -178,6 +217,18 @@ FilterSpectra design_filters(const FormatParams& f, double fs) {
     std::vector<double> db, da;
     high_shelf(f.deemph_mid, f.deemph_gain, fs, f.deemph_q, db, da);  // inverse used below
     std::vector<double> fir = firwin_lowpass_hamming(65, 0.5 / (nyq / 1e6));
+    std::vector<cd> custom;
+    const bool has_custom = f.custom_luma_table && load_custom_luma(fs, custom);
+    std::vector<double> shb, sha;
+    if (f.shelf_mid > 0) high_shelf(f.shelf_mid, f.shelf_gain, fs / 2.0, f.shelf_q, shb, sha);
+    std::vector<double> hpb, hpa;
+    if (f.sub_deemph) {
+        double k = std::tan(kPi * (f.sub_hp_freq / nyq) / 2.0);
+        double norm = 1.0 / (1.0 + k);
+        hpb = {norm, -norm, 0.0};
+        hpa = {1.0, (k - 1.0) * norm, 0.0};
+        out.sub_high.assign(H, cd(0.0, 0.0));
+    }
     const double wc_lpx = kPi * f.lpf_extra / nyq, wc_hpx = kPi * f.hpf_extra / nyq;
     const double wc_v = kPi * f.video_lpf_freq / nyq;
     for (int k = 0; k < H; k++) {
@@ -206,7 +257,11 @@ FilterSpectra design_filters(const FormatParams& f, double fs) {
         }
         cd deemph = freq_resp(da, db, w);  // de-emphasis = 1 / high shelf
         cd v = vlp * deemph;
-        out.video[(size_t)k] = v;
+        cd vid = v;
+        if (has_custom) vid *= custom[(size_t)k];
+        if (f.shelf_mid > 0) vid *= freq_resp(shb, sha, w);
+        out.video[(size_t)k] = vid;
+        if (f.sub_deemph) out.sub_high[(size_t)k] = vid * freq_resp(hpb, hpa, w);
         cd firr(0.0, 0.0);
         for (int n = 0; n < 65; n++) firr += fir[(size_t)n] * std::polar(1.0, -w * n);
         out.sync[(size_t)k] = v * firr;
@@ -216,6 +271,13 @@ FilterSpectra design_filters(const FormatParams& f, double fs) {
     out.env_b0 = kk * norm;
     out.env_b1 = kk * norm;
     out.env_a1 = (kk - 1.0) * norm;
+    if (f.sub_deemph) {
+        double ka = std::tan(kPi * (f.sub_amp_lpf / nyq) / 2.0);
+        double na = 1.0 / (1.0 + ka);
+        out.sub_b0 = ka * na;
+        out.sub_b1 = ka * na;
+        out.sub_a1 = (ka - 1.0) * na;
+    }
     return out;
 }
 

@@ -1,9 +1,10 @@
 // Format parameters for the supported tape formats.
 //
 // Values restate the frozen upstream parameter snapshot the reference embeds
-// (src/VHSDecode.Core/Formats/format-params.snapshot.json, cases PAL/VHS/sp and
-// NTSC/VHS/sp, read by Core/Formats/FormatCatalog.cs:46-112); only the keys the
-// RF -> TBC luma path reads are kept.
+// (src/VHSDecode.Core/Formats/format-params.snapshot.json, cases PAL/VHS/sp,
+// NTSC/VHS/sp, PAL/SVHS/sp and NTSC/SVHS/sp, read by
+// Core/Formats/FormatCatalog.cs:46-112); only the keys the RF -> TBC luma path
+// reads are kept.
 #pragma once
 #include <cmath>
 #include <cstdint>
@@ -32,6 +33,20 @@ struct FormatParams {
     bool video_lpf_supergauss;
     double deemph_gain, deemph_mid, deemph_q;
     double color_under;
+    // video_custom_luma_filters (DecodeFilterSet.cs:1560-1609): the measured
+    // "svhs-sp-linear-subdeemphasis" response (used where a table exists for
+    // the sample rate) and a high shelf designed at half the sample rate
+    bool custom_luma_table;
+    double shelf_mid, shelf_gain, shelf_q;   // shelf_mid 0 = none
+    // sub-deemphasis (DecodeSession.cs:1250-1278, RfDemodulator.cs:2852-2990)
+    bool sub_deemph;
+    double sub_hp_freq;                      // first-order Butterworth high-pass
+    double sub_amp_lpf;                      // first-order Butterworth amplitude low-pass
+    double sub_deviation;                    // hz_ire * (100 - vsync_ire)
+    double sub_exp;                          // nonlinear_exp_scaling
+    double sub_scale1, sub_scale2;           // NaN = absent
+    double sub_logistic_mid, sub_logistic_rate;  // rate NaN or <= 0 = absent
+    double sub_static;                       // nonlinear_static_factor (absent = 0)
 };
 
 inline FormatParams pal_vhs_sp() {
@@ -69,6 +84,44 @@ inline FormatParams ntsc_vhs_sp() {
     f.video_lpf_freq = 6600000.0; f.video_lpf_order = 9; f.video_lpf_supergauss = true;
     f.deemph_gain = 13.9794; f.deemph_mid = 273755.82; f.deemph_q = 0.462088186;
     f.color_under = 629370.6293706294;
+    return f;
+}
+
+// S-VHS keeps its system's sync/TBC parameters and changes the FM levels,
+// the RF and video filters and adds the custom luma filters and
+// sub-deemphasis (snapshot cases PAL/SVHS/sp, NTSC/SVHS/sp).
+inline void svhs_common(FormatParams& f) {
+    f.lpf_extra = 9100000.0; f.lpf_extra_order = 25;
+    f.hpf_extra = 1300000.0; f.hpf_extra_order = 20;
+    f.bpf_low = 2000000.0; f.bpf_high = 8980000.0; f.bpf_order = 0;
+    f.peak_freq = 6200000.0; f.peak_gain = 4.0; f.peak_bandwidth = 16000000.0;
+    f.ramp_boost0 = 1.0; f.ramp_boost20 = 4.0;
+    f.video_lpf_freq = 7500000.0; f.video_lpf_order = 6; f.video_lpf_supergauss = true;
+    f.custom_luma_table = true;
+    f.shelf_mid = 2000000.0; f.shelf_gain = 4.0; f.shelf_q = 0.4967045;
+    f.sub_deemph = true;
+    f.sub_hp_freq = 320000.0;
+    f.sub_amp_lpf = 590000.0;
+    f.sub_deviation = f.hz_ire * (100.0 + -f.vsync_ire);
+    f.sub_exp = 0.23;
+    f.sub_scale1 = NAN;
+    f.sub_scale2 = 0.72;
+    f.sub_logistic_mid = 0.2;
+    f.sub_logistic_rate = 14.0;
+    f.sub_static = 0.0;
+}
+
+inline FormatParams pal_svhs_sp() {
+    FormatParams f = pal_vhs_sp();
+    f.ire0 = 5880000.0; f.hz_ire = 11200.0;
+    svhs_common(f);
+    return f;
+}
+
+inline FormatParams ntsc_svhs_sp() {
+    FormatParams f = ntsc_vhs_sp();
+    f.ire0 = 5857142.857142857; f.hz_ire = 11428.57142857143;
+    svhs_common(f);
     return f;
 }
 

@@ -12,6 +12,22 @@ constexpr int kStride = 30720;
 constexpr int kHalf = 16385;  // kBlock/2 + 1 spectrum bins
 
 // ---------------------------------------------------------------- FP32 fused
+// Sub-deemphasis of ApplySubDeemphasisRealCore (Core/Dsp/RfDemodulator.cs:2852-2990):
+// high = irfft(D x Video x HighPass); amp = |analytic(high)| * 2 / deviation,
+// first-order low-pass filtfilt, then max(0), x scale1, ^exponent, x scale2,
+// x logistic; video -= high * (1 - amp) + high * static_factor.
+template <typename T, typename T2>
+struct SubDeemphT {
+    const T2* high;            // [kHalf] Video x high-pass, nullptr = off
+    T inv_half_dev;            // 2 / deviation
+    T b0, b1, a1;              // amplitude low-pass
+    T exponent, scale1, scale2;   // absent scales are 1
+    T logistic_mid, logistic_rate;  // rate <= 0: no logistic factor
+    T static_factor;
+};
+using SubDeemph = SubDeemphT<float, float2>;
+using SubDeemph64 = SubDeemphT<double, double2>;
+
 struct FastDemodParams {
     const int16_t* rf;         // capture, 16-byte aligned
     int64_t first_block;       // first 32768-sample block to decode
@@ -30,6 +46,7 @@ struct FastDemodParams {
     float* env_out;
     float2* scratch;           // repair scratch: per cluster 2*32768 float2 (demod, diff-demod, spike mask, thresholds)
     int* repair_count;         // counts blocks that took the spike-repair path
+    SubDeemph sub;             // sub-deemphasis (sub.high == nullptr: off)
 };
 
 size_t fp32_smem_bytes();
@@ -53,9 +70,11 @@ struct PlainDemodParams {
     int* flag;                 // spike flag
     unsigned* mask;            // 1024 words
     int64_t* blk;              // device-resident block index, advanced per replay
+    SubDeemph64 sub;           // sub-deemphasis (sub.high == nullptr: off)
 };
 cudaError_t launch_demod_fp64_block(const PlainDemodParams& p, cudaStream_t stream);
 constexpr int kPlainBlockKernels = 38;  // kernels in one plain-path block (13 + 5 FFTs x 5 passes)
+constexpr int kPlainSubKernels = 10;    // added by sub-deemphasis (5 + 1 FFT x 5 passes)
 
 // ---------------------------------------------------------------- pulses
 // Sync-pulse edge events of PulseDetection.FindPulses over a whole stitched

@@ -6,7 +6,7 @@
 // that arrive while others are on the GPU are admitted as soon as a worker
 // and device memory are free and their kernels overlap on the device.
 //
-// Slots are created on demand for a (profile, tape speed, sample rate) and
+// Slots are created on demand for a (profile, tape speed, tape format, sample rate) and
 // kept; a new slot is admitted only while the device-memory footprint of all
 // slots stays inside the server's budget, otherwise an idle slot of another
 // format is released or the window waits in the queue.  Windows of one
@@ -44,7 +44,7 @@ double ms_between(Clock::time_point a, Clock::time_point b) {
 
 struct Slot {
     vhsdecode_gb300_session* s = nullptr;
-    uint32_t profile = 0, speed = 0;
+    uint32_t profile = 0, speed = 0, tape_format = 0;
     double mhz = 0.0;
     size_t bytes = 0;
     bool busy = false;
@@ -84,7 +84,8 @@ struct vhsdecode_gb300_server {
 namespace {
 
 bool same_format(const Slot& sl, const vhsdecode_gb300_window_v1& w) {
-    return sl.profile == w.profile && sl.speed == w.tape_speed && sl.mhz == w.sample_rate_mhz;
+    return sl.profile == w.profile && sl.speed == w.tape_speed && sl.tape_format == w.tape_format &&
+           sl.mhz == w.sample_rate_mhz;
 }
 
 // Device footprint of one slot, measured when the first slot of a format is
@@ -136,6 +137,7 @@ bool pick(vhsdecode_gb300_server* sv, Request& out, Slot*& slot, std::vector<Slo
             found = new Slot;
             found->profile = it->w.profile;
             found->speed = it->w.tape_speed;
+            found->tape_format = it->w.tape_format;
             found->mhz = it->w.sample_rate_mhz;
             found->bytes = need;   // reserved now, corrected after creation
             sv->used += need;
@@ -156,6 +158,7 @@ void create_slot(vhsdecode_gb300_server* sv, Slot* sl) {
     c.struct_size = sizeof(c);
     c.profile = sl->profile;
     c.tape_speed = sl->speed;
+    c.tape_format = sl->tape_format;
     c.device_id = sv->cfg.device_id;
     c.sample_rate_mhz = sl->mhz;
     c.max_samples = sv->cfg.max_window_samples;
@@ -279,8 +282,9 @@ void worker_main(vhsdecode_gb300_server* sv) {
 
 bool supported(const vhsdecode_gb300_window_v1& w) {
     return (w.profile == VHSDECODE_GB300_PROFILE_PAL || w.profile == VHSDECODE_GB300_PROFILE_NTSC) &&
-           w.tape_speed == VHSDECODE_GB300_TAPE_SPEED_SP && w.sample_rate_mhz >= 10.0 &&
-           w.sample_rate_mhz <= 100.0;
+           w.tape_speed == VHSDECODE_GB300_TAPE_SPEED_SP &&
+           (w.tape_format == VHSDECODE_GB300_TAPE_FORMAT_VHS || w.tape_format == VHSDECODE_GB300_TAPE_FORMAT_SVHS) &&
+           w.sample_rate_mhz >= 10.0 && w.sample_rate_mhz <= 100.0;
 }
 
 }  // namespace

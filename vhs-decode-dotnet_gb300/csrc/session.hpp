@@ -135,9 +135,9 @@ struct vhsdecode_gb300_session {
     DevBuf<float> v32, s32, e32;
     DevBuf<double> v64, s64, e64;
     DevBuf<float> rfv32;
-    DevBuf<float2> vid32, syn32, tw_hi, tw_lo;
+    DevBuf<float2> vid32, syn32, sub32, tw_hi, tw_lo;
     DevBuf<double> rfv64;
-    DevBuf<double2> vid64, syn64;
+    DevBuf<double2> vid64, syn64, sub64;
     DevBuf<float2> scratch;
     DevBuf<int> repair;
     DevBuf<double2> pwork;

@@ -13,7 +13,7 @@ import os
 
 import numpy as np
 
-ABI_VERSION = 0x00010001
+ABI_VERSION = 0x00010002
 STATUS_OK = 0
 STATUS_NULL_POINTER = -20000
 STATUS_INVALID_ARGUMENT = -20001
@@ -26,6 +26,7 @@ STATUS_INTERNAL_ERROR = -20007
 
 PROFILE_NTSC, PROFILE_PAL, PROFILE_PAL_M = 0, 1, 2
 TAPE_SP, TAPE_LP, TAPE_EP = 0, 1, 2
+FORMAT_VHS, FORMAT_SVHS = 0, 1
 INPUT_FLOAT32, INPUT_INT16 = 0, 1
 PRECISION_FP32_FUSED, PRECISION_FP64_PLAIN = 0, 1
 DECODE_DEVICE_INPUT = 0x1
@@ -87,6 +88,11 @@ class RunConfig(ctypes.Structure):
                 ("cancel_callback", CANCEL_CB), ("user_data", ctypes.c_void_p)]
 
 
+class RunConfigV2(ctypes.Structure):
+    """config_v1 followed by the tape format (vhsdecode_gb300_config_v2)."""
+    _fields_ = RunConfig._fields_ + [("tape_format", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
 class RunResult(ctypes.Structure):
     _fields_ = [("struct_size", ctypes.c_uint32), ("fields_written", ctypes.c_uint32),
                 ("output_line_length", ctypes.c_uint32), ("output_field_lines", ctypes.c_uint32),
@@ -97,7 +103,8 @@ class SessionConfig(ctypes.Structure):
     _fields_ = [("struct_size", ctypes.c_uint32), ("profile", ctypes.c_uint32),
                 ("tape_speed", ctypes.c_uint32), ("device_id", ctypes.c_int32),
                 ("sample_rate_mhz", ctypes.c_double), ("max_samples", ctypes.c_uint64),
-                ("precision", ctypes.c_uint32), ("max_fields", ctypes.c_uint32)]
+                ("precision", ctypes.c_uint32), ("max_fields", ctypes.c_uint32),
+                ("tape_format", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
 
 
 class DecodeResult(ctypes.Structure):
@@ -130,7 +137,8 @@ class Window(ctypes.Structure):
                 ("sample_rate_mhz", ctypes.c_double), ("samples", ctypes.c_void_p),
                 ("sample_count", ctypes.c_uint64), ("source_offset", ctypes.c_uint64),
                 ("seek", ctypes.c_uint32), ("max_fields", ctypes.c_uint32),
-                ("tbc_out", ctypes.c_void_p), ("tbc_capacity", ctypes.c_uint64)]
+                ("tbc_out", ctypes.c_void_p), ("tbc_capacity", ctypes.c_uint64),
+                ("tape_format", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
 
 
 class WindowResult(ctypes.Structure):
@@ -174,8 +182,8 @@ def load(path: str = LIB_PATH):
     L.vhsdecode_gb300_session_copy_stream.argtypes = [_vp, ctypes.c_uint32, ctypes.c_uint64,
                                                       ctypes.c_uint64, _vp]
     L.vhsdecode_gb300_session_tbc_device.argtypes = [_vp, _P(_vp), _P(ctypes.c_uint64)]
-    L.vhsdecode_gb300_design_filters.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_double,
-                                                 _vp, _vp, _vp, _vp]
+    L.vhsdecode_gb300_design_filters.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                                 ctypes.c_double, _vp, _vp, _vp, _vp, _vp]
     L.vhsdecode_gb300_field_sync.argtypes = [ctypes.c_uint32, ctypes.c_double, _vp, _vp,
                                              ctypes.c_uint64, ctypes.c_int64, _vp, _vp, _vp, _vp,
                                              ctypes.c_uint32, _P(ctypes.c_uint32)]
@@ -227,15 +235,21 @@ def runtime_info(device=0):
     return info
 
 
-def design_filters(profile, sample_rate_mhz=40.0, tape_speed=TAPE_SP):
+def design_filters(profile, sample_rate_mhz=40.0, tape_speed=TAPE_SP, tape_format=FORMAT_VHS,
+                   sub=False):
+    """(rf_video, video, sync, env b0/b1/a1); with ``sub`` also (sub_high, sub b0/b1/a1)."""
     n = 16385
     rv = np.zeros(n)
     v = np.zeros(2 * n)
     s = np.zeros(2 * n)
-    env = np.zeros(3)
-    check(load().vhsdecode_gb300_design_filters(profile, tape_speed, sample_rate_mhz, _ptr(rv),
-                                                _ptr(v), _ptr(s), _ptr(env)))
-    return rv, v[0::2] + 1j * v[1::2], s[0::2] + 1j * s[1::2], env
+    h = np.zeros(2 * n)
+    env = np.zeros(6)
+    check(load().vhsdecode_gb300_design_filters(profile, tape_speed, tape_format, sample_rate_mhz,
+                                                _ptr(rv), _ptr(v), _ptr(s), _ptr(h), _ptr(env)))
+    out = (rv, v[0::2] + 1j * v[1::2], s[0::2] + 1j * s[1::2], env[:3])
+    if sub:
+        out = out + (h[0::2] + 1j * h[1::2], env[3:])
+    return out
 
 
 def field_sync(profile, pulses, span_len, state, ref=None, sample_rate_mhz=40.0):
@@ -307,12 +321,13 @@ class Session:
     """Device-resident decode context (session API of include/vhsdecode_gb300.h)."""
 
     def __init__(self, profile, max_samples, precision=PRECISION_FP32_FUSED, device=0,
-                 sample_rate_mhz=40.0, max_fields=0):
+                 sample_rate_mhz=40.0, max_fields=0, tape_format=FORMAT_VHS):
         L = load()
         cfg = SessionConfig()
         cfg.struct_size = ctypes.sizeof(SessionConfig)
         cfg.profile = profile
         cfg.tape_speed = TAPE_SP
+        cfg.tape_format = tape_format
         cfg.device_id = device
         cfg.sample_rate_mhz = sample_rate_mhz
         cfg.max_samples = int(max_samples)
@@ -422,13 +437,13 @@ class Server:
         self._keep = {}
 
     def submit(self, stream_id, profile, rf, source_offset=0, seek=False, max_fields=0, tbc_out=None,
-               sample_rate_mhz=40.0, tape_speed=TAPE_SP):
+               sample_rate_mhz=40.0, tape_speed=TAPE_SP, tape_format=FORMAT_VHS):
         """Queue a window (``rf``: int16 host array, kept alive until ``wait``); returns a ticket."""
         rf = np.ascontiguousarray(rf, np.int16)
         w = Window(ctypes.sizeof(Window), stream_id, profile, tape_speed, float(sample_rate_mhz),
                    rf.ctypes.data, len(rf), int(source_offset), 1 if seek else 0, int(max_fields),
                    tbc_out.ctypes.data if tbc_out is not None else None,
-                   tbc_out.size if tbc_out is not None else 0)
+                   tbc_out.size if tbc_out is not None else 0, int(tape_format), 0)
         t = ctypes.c_uint64(0)
         check(load().vhsdecode_gb300_server_submit(self._h, ctypes.byref(w), ctypes.byref(t)))
         self._keep[t.value] = (rf, tbc_out)

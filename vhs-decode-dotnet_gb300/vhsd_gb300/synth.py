@@ -57,6 +57,22 @@ def ntsc_vhs(**kw):
     return SynthConfig(**base)
 
 
+def pal_svhs(**kw):
+    """PAL S-VHS SP: sync tip 5.4 MHz, peak white 7.0 MHz.  The pre-emphasis is
+    the linear shelf only (the decoder's sub-deemphasis is a nonlinear
+    refinement on top of it)."""
+    base = dict(ire0=5880000.0, hz_ire=11200.0)
+    base.update(kw)
+    return SynthConfig(**base)
+
+
+def ntsc_svhs(**kw):
+    base = dict(system="NTSC", ire0=5857142.857142857, hz_ire=11428.57142857143,
+                vsync_ire=-40.0, chroma_hz=629370.6293706294)
+    base.update(kw)
+    return SynthConfig(**base)
+
+
 def _geometry(system):
     if system == "PAL":
         return dict(lines=625, line_us=64.0, hsync_us=4.7, eq_us=2.35, vsync_us=27.3,
@@ -247,7 +263,9 @@ def _high_shelf(center_hz, gain_db, fs, q):
 
 
 def config(name: str, **overrides):
-    """Named workloads: 'pal4' (PAL VHS 4 fields), 'ntsc60' (NTSC VHS 60 fields, dropouts)."""
+    """Named workloads: 'pal4' (PAL VHS 4 fields), 'ntsc60' (NTSC VHS 60 fields, dropouts),
+    'svhs100' (PAL S-VHS 100 fields, 42 dB SNR, +/-0.5 % timebase wobble at 15 Hz,
+    +/-2-sample head-switch jumps every field) and small parity cases."""
     if name == "pal4":
         c = pal_vhs(fields=4, seed=11, snr_db=40.0)
     elif name == "ntsc60":
@@ -257,6 +275,15 @@ def config(name: str, **overrides):
         c = pal_vhs(fields=3, seed=5, snr_db=40.0)
     elif name == "ntsc_small":
         c = ntsc_vhs(fields=3, seed=6, snr_db=38.0, dropouts=8)
+    elif name == "svhs100":
+        c = pal_svhs(fields=100, seed=33, snr_db=42.0, wobble_frac=0.005, wobble_hz=15.0,
+                     headswitch_samples=2.0, patterns=("bars", "ramp", "noise", "noise"))
+    elif name == "svhs_small":
+        c = pal_svhs(fields=4, seed=7, snr_db=42.0, wobble_frac=0.005, wobble_hz=15.0,
+                     headswitch_samples=2.0)
+    elif name == "svhs_ntsc_small":
+        c = ntsc_svhs(fields=3, seed=8, snr_db=42.0, dropouts=6, wobble_frac=0.005,
+                      headswitch_samples=2.0)
     else:
         raise KeyError(name)
     for k, v in overrides.items():
