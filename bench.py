@@ -320,6 +320,7 @@ def run_ours(args, world, rank, local):
                 "config": {"workload": args.workload, "description": desc, "samples": int(n),
                            "blocks": nblocks, "fields": int(fields),
                            "precision": "fp32 fused demod, fp64 sync/TBC",
+                           "fft_plan": int(r.fft_plan),
                            "l2": "inputs and streams larger than L2 (no flush)",
                            "parallelism": "replicas" if world > 1 else "single"},
                 "e2e": {"value": round(e2e_value, 3), "unit": "MSPS",

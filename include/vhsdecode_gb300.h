@@ -192,6 +192,8 @@ typedef struct vhsdecode_gb300_decode_result_v1 {
     double host_ms;             /* host control plane */
     uint32_t kernel_launches;   /* device kernels this decode launched */
     uint32_t segments;          /* pipeline segments of the demod (1 for the plain path) */
+    uint32_t fft_plan;          /* radix plans the fused demodulator used (tuned per device) */
+    uint32_t reserved;
 } vhsdecode_gb300_decode_result_v1;
 
 typedef struct vhsdecode_gb300_field_info_v1 {

@@ -169,3 +169,12 @@ def test_server_create_without_gpu_reports_unavailable(lib):
     assert st == native.STATUS_CUDA_UNAVAILABLE
     bad = native.ServerConfig(8, 0, 2, 0, 1 << 22, 0)
     assert lib.vhsdecode_gb300_server_create(ctypes.byref(bad), ctypes.byref(h)) == native.STATUS_INVALID_ARGUMENT
+
+
+def test_unsupported_formats_are_rejected(lib):
+    # format validation precedes any device work, so this holds with or without a GPU
+    from vhsd_gb300 import native
+    for prof, tape in ((native.PROFILE_PAL_M, native.FORMAT_VHS), (native.PROFILE_PAL, 7)):
+        with pytest.raises(native.NativeError) as ei:
+            native.Session(prof, 1 << 20, tape_format=tape)
+        assert ei.value.status == native.STATUS_INVALID_ARGUMENT

@@ -323,3 +323,22 @@ def test_svhs_sub_deemphasis_changes_the_video(gpu, svhs_capture):
     keep = slice(1024, 1024 + 30720)
     assert np.quantile(np.abs(got - v_sub[keep]), 0.999) < FREQ_TOL_HZ
     assert np.quantile(np.abs(v_sub[keep] - v_lin[keep]), 0.9) > 10 * FREQ_TOL_HZ
+
+
+@pytest.mark.parametrize("plan", [0, 1, 4, 5])
+def test_every_fft_radix_plan_matches_oracle(gpu, plan, pal_capture, pal_oracle, monkeypatch):
+    # the autotuner may pick any radix plan: each must meet the stage tolerances
+    from vhsd_gb300 import native
+    rf, _ = pal_capture
+    _, (video, vlp, env, _) = pal_oracle
+    monkeypatch.setenv("VHSD_FFT_PLAN", str(plan))
+    with native.Session(native.PROFILE_PAL, len(rf)) as s:
+        r = s.decode(rf, demod_only=True)
+        assert r.fft_plan == plan
+        n = len(video)
+        v = s.stream(0, 0, n)
+        y = s.stream(1, 0, n)
+        e = s.stream(2, 0, n)
+    assert np.quantile(np.abs(v - video), 0.999) < FREQ_TOL_HZ
+    assert np.quantile(np.abs(y - vlp), 0.999) < FREQ_TOL_HZ
+    assert np.quantile(np.abs(e - env) / np.maximum(np.abs(env), 1.0), 0.999) < 1e-3

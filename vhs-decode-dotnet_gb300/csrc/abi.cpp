@@ -17,6 +17,7 @@
 #include <cstring>
 #include <functional>
 #include <memory>
+#include <mutex>
 #include <new>
 #include <stdexcept>
 #include <string>
@@ -107,6 +108,9 @@ void resolve_span(int64_t intended, int64_t read_len, int64_t& s0, int64_t& slen
     s0 = first * kStride;
     slen = (last - first + 1) * kStride;
 }
+
+FastDemodParams fp32_params(vhsdecode_gb300_session* s, const int16_t* rf_dev);
+int tuned_fft_plan(vhsdecode_gb300_session* s, FastDemodParams base);
 
 void session_init(vhsdecode_gb300_session* s, const vhsdecode_gb300_session_config_v1& c) {
     if (!format_for(c.profile, c.tape_speed, c.tape_format, s->fmt))
@@ -218,6 +222,7 @@ void session_init(vhsdecode_gb300_session* s, const vhsdecode_gb300_session_conf
         ck(cudaEventCreateWithFlags(&s->copy_end, cudaEventDisableTiming), "cudaEventCreate");
         ck(cudaEventCreateWithFlags(&s->d2h_end, cudaEventDisableTiming), "cudaEventCreate");
         ck(cudaStreamCreateWithFlags(&s->cap_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        s->fft_plan = tuned_fft_plan(s, fp32_params(s, nullptr));
     } else {
         s->v64.alloc(stream_cap); s->s64.alloc(stream_cap); s->e64.alloc(stream_cap);
         std::vector<double2> vv(H), sv(H);
@@ -340,6 +345,84 @@ SubDeemphT<T, T2> sub_params(const FormatParams& f, const FilterSpectra& filt) {
     return d;
 }
 
+// FFT radix plan autotuner.  The fused demodulator is compiled for the
+// kFftPlans radix plans of its 8192- and 16384-point transforms (same results
+// up to float rounding).  The first FP32 session on a device times each on a
+// synthetic FM carrier block set (four launches of 4 blocks per cluster each,
+// after one warm-up) and keeps the fastest for the process; plan 0 is kept
+// unless another is at least 2 % faster, so that outputs do not flip between
+// runs on timing noise.  VHSD_FFT_PLAN=<n> fixes the plan (one of kFftPlans)
+// and VHSD_TUNE_LOG=1 prints the timings.  Must run outside stream capture
+// (session creation is).
+int tuned_fft_plan(vhsdecode_gb300_session* s, FastDemodParams base) {
+    static std::mutex m;
+    static int plans[64];
+    static bool done[64] = {};
+    if (const char* env = std::getenv("VHSD_FFT_PLAN")) {
+        int v = std::atoi(env);
+        for (int plan : kFftPlans)
+            if (plan == v) return v;
+    }
+    std::lock_guard<std::mutex> lk(m);
+    const int dev = s->device;
+    if (dev >= 0 && dev < 64 && done[dev]) return plans[dev];
+    const int clusters = s->num_sms / 2;
+    const int64_t nb = 4 * (int64_t)clusters;
+    const int64_t n = nb * kStride + (kBlock - kStride);
+    std::vector<int16_t> host((size_t)n);
+    const double f = s->fmt.ire0 + 50.0 * s->fmt.hz_ire;
+    uint32_t lcg = 12345u;
+    double ph = 0.0;
+    for (int64_t i = 0; i < n; i++) {
+        lcg = lcg * 1664525u + 1013904223u;
+        ph += 2.0 * 3.14159265358979323846 * (f + 300000.0 * std::sin(i * 1e-4)) / s->fs;
+        host[(size_t)i] = (int16_t)std::lrint(8000.0 * std::cos(ph) + (double)((lcg >> 24) & 63) - 32.0);
+    }
+    DevBuf<int16_t> rf;
+    DevBuf<float> v, y, e;
+    rf.alloc((size_t)n + 8);
+    v.alloc((size_t)nb * kStride);
+    y.alloc((size_t)nb * kStride);
+    e.alloc((size_t)nb * kStride);
+    ck(cudaMemcpy(rf.p, host.data(), (size_t)n * sizeof(int16_t), cudaMemcpyHostToDevice), "tune upload");
+    cudaStream_t st;
+    ck(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "cudaStreamCreate");
+    cudaEvent_t e0, e1;
+    ck(cudaEventCreate(&e0), "cudaEventCreate");
+    ck(cudaEventCreate(&e1), "cudaEventCreate");
+    FastDemodParams p = base;
+    p.rf = rf.p;
+    p.first_block = 0;
+    p.nblocks = nb;
+    p.video_out = v.p;
+    p.sync_out = y.p;
+    p.env_out = e.p;
+    const bool log = std::getenv("VHSD_TUNE_LOG") != nullptr;
+    int best = 0;
+    float best_ms = 0.0f, plan0_ms = 0.0f;
+    for (int plan : kFftPlans) {
+        p.fft_plan = plan;
+        const int a = plan & 3, b = (plan >> 2) & 3;
+        ck(launch_demod_fp32(p, clusters, st), "tune launch");
+        ck(cudaEventRecord(e0, st), "event");
+        for (int r = 0; r < 4; r++) ck(launch_demod_fp32(p, clusters, st), "tune launch");
+        ck(cudaEventRecord(e1, st), "event");
+        ck(cudaEventSynchronize(e1), "event sync");
+        float ms = 0.0f;
+        ck(cudaEventElapsedTime(&ms, e0, e1), "event time");
+        if (log) std::fprintf(stderr, "vhsd fft plan %d (8192:%d 16384:%d): %.4f ms\n", p.fft_plan, a, b, ms / 4);
+        if (p.fft_plan == 0) plan0_ms = ms;
+        if (p.fft_plan == 0 || ms < best_ms) { best = p.fft_plan; best_ms = ms; }
+    }
+    if (best != 0 && best_ms > 0.98f * plan0_ms) best = 0;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaStreamDestroy(st);
+    if (log) std::fprintf(stderr, "vhsd fft plan chosen: %d\n", best);
+    if (dev >= 0 && dev < 64) { plans[dev] = best; done[dev] = true; }
+    return best;
+}
+
 FastDemodParams fp32_params(vhsdecode_gb300_session* s, const int16_t* rf_dev) {
     FastDemodParams p{};
     p.rf = rf_dev;
@@ -365,6 +448,7 @@ FastDemodParams fp32_params(vhsdecode_gb300_session* s, const int16_t* rf_dev) {
         p.sub = sub_params<float, float2>(s->fmt, s->filt);
         p.sub.high = s->sub32.p;
     }
+    p.fft_plan = s->fft_plan;
     return p;
 }
 
@@ -935,6 +1019,7 @@ int32_t decode_impl(vhsdecode_gb300_session* s, const int16_t* rf, uint64_t n, u
         res->host_ms = host_ms;
         res->kernel_launches = s->launches;
         res->segments = s->segments;
+        res->fft_plan = (uint32_t)s->fft_plan;
     }
     return VHSDECODE_GB300_STATUS_OK;
 }

@@ -131,26 +131,51 @@ __device__ __forceinline__ void pass(float2* buf, int L, int batch, int Ns, cons
     __syncthreads();
 }
 
+// Butterflies per thread of a radix-R pass over `batch` transforms of length L.
+__host__ __device__ constexpr int pass_j(int L, int R, int batch) { return (batch * (L / R) + T - 1) / T; }
+
 // The transforms are called, not inlined: each is used at two call sites, and
 // one shared copy keeps the kernel's code small enough that instruction fetch
-// stops stalling the warps (measured 11 % faster per block).
-//
-// 8192-point transform(s): radix 16 x 16 x 32.
-template <bool INV, int BATCH>
-__device__ __noinline__ void fft8192(float2* buf, const Tw& tw, int tid) {
-    pass<16, BATCH, INV>(buf, Q, BATCH, 1, tw, tid);
-    pass<16, BATCH, INV>(buf, Q, BATCH, 16, tw, tid);
-    pass<32, (BATCH + 1) / 2, INV>(buf, Q, BATCH, 256, tw, tid);
+// stops stalling the warps (measured 11 % faster per block).  Each length has
+// several three-pass radix plans; the kernel is compiled for the plans in
+// kFftPlans (kernels.h), and the host times those once per device and launches
+// the fastest (a plan selected at run time inside one kernel cost 2 %, an
+// indirect call 20 %).
+template <bool INV, int BATCH, int R1, int R2, int R3>
+__device__ __noinline__ void fft8192p(float2* buf, const Tw& tw, int tid) {
+    static_assert(R1 * R2 * R3 == Q, "radix plan");
+    pass<R1, pass_j(Q, R1, BATCH), INV>(buf, Q, BATCH, 1, tw, tid);
+    pass<R2, pass_j(Q, R2, BATCH), INV>(buf, Q, BATCH, R1, tw, tid);
+    pass<R3, pass_j(Q, R3, BATCH), INV>(buf, Q, BATCH, R1 * R2, tw, tid);
 }
 
-// 16384-point transform: radix 16 x 32 x 32.
-template <bool INV>
-__device__ __noinline__ void fft16384(float2* buf, const Tw& tw, int tid) {
-    pass<16, 2, INV>(buf, M, 1, 1, tw, tid);
-    pass<32, 1, INV>(buf, M, 1, 16, tw, tid);
-    pass<32, 1, INV>(buf, M, 1, 512, tw, tid);
+template <bool INV, int R1, int R2, int R3>
+__device__ __noinline__ void fft16384p(float2* buf, const Tw& tw, int tid) {
+    static_assert(R1 * R2 * R3 == M, "radix plan");
+    pass<R1, pass_j(M, R1, 1), INV>(buf, M, 1, 1, tw, tid);
+    pass<R2, pass_j(M, R2, 1), INV>(buf, M, 1, R1, tw, tid);
+    pass<R3, pass_j(M, R3, 1), INV>(buf, M, 1, R1 * R2, tw, tid);
 }
 
+// 8192-point transform(s) of plan PLAN (bits 0-1): 16x16x32, 32x16x16,
+// 16x32x16 or 8x32x32.
+template <bool INV, int BATCH, int PLAN>
+__device__ __forceinline__ void fft8192(float2* buf, const Tw& tw, int tid) {
+    constexpr int a = PLAN & 3;
+    if constexpr (a == 1) fft8192p<INV, BATCH, 32, 16, 16>(buf, tw, tid);
+    else if constexpr (a == 2) fft8192p<INV, BATCH, 16, 32, 16>(buf, tw, tid);
+    else if constexpr (a == 3) fft8192p<INV, BATCH, 8, 32, 32>(buf, tw, tid);
+    else fft8192p<INV, BATCH, 16, 16, 32>(buf, tw, tid);
+}
+
+// 16384-point transform of plan PLAN (bits 2-3): 16x32x32, 32x32x16 or 32x16x32.
+template <bool INV, int PLAN>
+__device__ __forceinline__ void fft16384(float2* buf, const Tw& tw, int tid) {
+    constexpr int b = (PLAN >> 2) & 3;
+    if constexpr (b == 1) fft16384p<INV, 32, 32, 16>(buf, tw, tid);
+    else if constexpr (b == 2) fft16384p<INV, 32, 16, 32>(buf, tw, tid);
+    else fft16384p<INV, 16, 32, 32>(buf, tw, tid);
+}
 
 struct Shared {
     float2 buf[BUF];
@@ -177,16 +202,10 @@ __device__ __forceinline__ float2 real_post(float2 ck, float2 cmk, float2 wk) {
 }
 
 // Stage 1/4 post-processing: buf[0..8192) holds C at the rank's parity; write
-// X * g back in place, g = gain[k] * (k == 0 || k == M ? g0 : 2 g0) when
-// `gain` is given (the RF band-pass with the Hilbert weights), else 1.  Rank 0
+// X * g (g = per-bin real scale supplied by `scale`) back in place.  Rank 0
 // writes X[2q] at q (q < 8192) and X[16384] to nyq; rank 1 writes X[2q+1].
-// Called (not inlined) from both stages, for code size.
-__device__ __noinline__ void post_half(Shared& sh, int rank, int tid, const float* __restrict__ gain, float g0) {
-    auto scale = [&](int k, float2 v) {
-        if (gain == nullptr) return v;
-        float g = __ldg(gain + k) * ((k == 0 || k == M) ? g0 : 2.0f * g0);
-        return make_float2(v.x * g, v.y * g);
-    };
+template <typename ScaleFn>
+__device__ __forceinline__ void post_half(Shared& sh, int rank, int tid, ScaleFn scale) {
     float2* buf = sh.buf;
     if (rank == 0) {
         for (int q = tid; q <= 4096; q += T) {
@@ -491,7 +510,8 @@ __device__ __noinline__ void repair_block(Shared& sh, Shared* rsh, const FastDem
 using namespace vhsd;
 using namespace vhsd::fp32;
 
-extern "C" __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(T, 1)
+template <int PLAN>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(T, 1)
 vhsd_demod_fp32_kernel(FastDemodParams p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Shared& sh = *reinterpret_cast<Shared*>(smem_raw);
@@ -519,9 +539,12 @@ vhsd_demod_fp32_kernel(FastDemodParams p) {
         // ---------------- stage 1: RF forward FFT (packed, DIF split) -----
         load_rf(buf, x, rank, sh.tw, tid);
         __syncthreads();
-        fft8192<false, 1>(buf, sh.tw, tid);
+        fft8192<false, 1, PLAN>(buf, sh.tw, tid);
         // X * RfVideo * Hilbert / N  (Hilbert: 1 at 0 and N/2, 2 between)
-        post_half(sh, rank, tid, p.rf_video, inv_n);
+        post_half(sh, rank, tid, [&](int k, float2 v) {
+            float g = __ldg(p.rf_video + k) * ((k == 0 || k == M) ? inv_n : 2.0f * inv_n);
+            return make_float2(v.x * g, v.y * g);
+        });
         // ---------------- stage 2: analytic inverse FFT -----------------
         if (rank == 0) {
             if (tid == 0) buf[sx(8192)] = sh.nyq;
@@ -530,7 +553,7 @@ vhsd_demod_fp32_kernel(FastDemodParams p) {
             for (int i = 8192 + tid; i < M; i += T) buf[sx(i)] = make_float2(0.f, 0.f);
         }
         __syncthreads();
-        fft16384<true>(buf, sh.tw, tid);
+        fft16384<true, PLAN>(buf, sh.tw, tid);
         cluster.sync();
         {
             // z[n] = A[n] + W^-n B[n], z[n+16384] = A[n] - W^-n B[n]; the
@@ -649,8 +672,8 @@ vhsd_demod_fp32_kernel(FastDemodParams p) {
             }
             cluster.sync();
         }
-        fft8192<false, 1>(buf, sh.tw, tid);
-        post_half(sh, rank, tid, nullptr, 1.0f);
+        fft8192<false, 1, PLAN>(buf, sh.tw, tid);
+        post_half(sh, rank, tid, [&](int k, float2 v) { return v; });
         const bool sub = p.sub.high != nullptr;
         float2* xs = reinterpret_cast<float2*>(sh.theta);   // D kept for stage 6
         if (sub) {
@@ -704,7 +727,7 @@ vhsd_demod_fp32_kernel(FastDemodParams p) {
                 }
             }
             __syncthreads();
-            fft8192<true, 2>(buf, sh.tw, tid);
+            fft8192<true, 2, PLAN>(buf, sh.tw, tid);
             cluster.sync();
             float* vout = p.video_out + (blk + p.first_block) * (int64_t)S - CUT;
             float* sout = p.sync_out + (blk + p.first_block) * (int64_t)S - CUT - 32;
@@ -763,7 +786,7 @@ vhsd_demod_fp32_kernel(FastDemodParams p) {
                 for (int i = 8192 + tid; i < M; i += T) buf[sx(i)] = make_float2(0.f, 0.f);
             }
             __syncthreads();
-            fft16384<true>(buf, sh.tw, tid);
+            fft16384<true, PLAN>(buf, sh.tw, tid);
             cluster.sync();
             {
                 // (high, |a| * 2 / deviation) in the time layout of the envelope
@@ -818,26 +841,39 @@ namespace vhsd {
 
 size_t fp32_smem_bytes() { return sizeof(fp32::Shared); }
 
-// The shared-memory attribute is set once per device (the first call on a
-// device must not be inside a stream capture).
-cudaError_t launch_demod_fp32(const FastDemodParams& p, int num_clusters, cudaStream_t stream) {
+template <int PLAN>
+static cudaError_t launch_plan(const FastDemodParams& p, int clusters, cudaStream_t stream, int dev) {
     static std::atomic<uint64_t> attr_set{0};
     size_t smem = sizeof(fp32::Shared);
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return e;
     const uint64_t bit = dev < 64 ? (uint64_t)1 << dev : 0;
     if (!bit || !(attr_set.load() & bit)) {
-        e = cudaFuncSetAttribute(vhsd_demod_fp32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t e = cudaFuncSetAttribute(vhsd_demod_fp32_kernel<PLAN>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         attr_set.fetch_or(bit);
     }
     if (p.nblocks <= 0) return cudaSuccess;
-    int clusters = num_clusters;
-    if (clusters > p.nblocks) clusters = (int)p.nblocks;
-    if (clusters < 1) clusters = 1;
-    vhsd_demod_fp32_kernel<<<2 * clusters, fp32::T, smem, stream>>>(p);
+    vhsd_demod_fp32_kernel<PLAN><<<2 * clusters, fp32::T, smem, stream>>>(p);
     return cudaGetLastError();
+}
+
+// The shared-memory attribute is set once per device and plan (the first call
+// on a device must not be inside a stream capture).
+cudaError_t launch_demod_fp32(const FastDemodParams& p, int num_clusters, cudaStream_t stream) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    int clusters = num_clusters;
+    if (p.nblocks > 0 && clusters > p.nblocks) clusters = (int)p.nblocks;
+    if (clusters < 1) clusters = 1;
+    static_assert(kFftPlanCount == 4, "plan list");
+    switch (p.fft_plan) {
+    case kFftPlans[0]: return launch_plan<kFftPlans[0]>(p, clusters, stream, dev);
+    case kFftPlans[1]: return launch_plan<kFftPlans[1]>(p, clusters, stream, dev);
+    case kFftPlans[2]: return launch_plan<kFftPlans[2]>(p, clusters, stream, dev);
+    case kFftPlans[3]: return launch_plan<kFftPlans[3]>(p, clusters, stream, dev);
+    default: return cudaErrorInvalidValue;
+    }
 }
 
 }  // namespace vhsd

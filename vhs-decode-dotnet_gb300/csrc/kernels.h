@@ -47,7 +47,14 @@ struct FastDemodParams {
     float2* scratch;           // repair scratch: per cluster 2*32768 float2 (demod, diff-demod, spike mask, thresholds)
     int* repair_count;         // counts blocks that took the spike-repair path
     SubDeemph sub;             // sub-deemphasis (sub.high == nullptr: off)
+    int fft_plan;              // radix plans: bits 0-1 the 8192-point, bits 2-3 the 16384-point transform
 };
+// Radix plans the fused kernel is compiled for (8192-point plan | 16384-point
+// plan << 2): 16x16x32 | 16x32x32, 32x16x16 | 16x32x32, 16x16x32 | 32x32x16,
+// 32x16x16 | 32x32x16.  The other plans of the transforms (16x32x16, 8x32x32;
+// 32x16x32) measured 1-30 % slower on GB300.
+constexpr int kFftPlanCount = 4;
+constexpr int kFftPlans[kFftPlanCount] = {0, 1, 4, 5};
 
 size_t fp32_smem_bytes();
 cudaError_t launch_demod_fp32(const FastDemodParams& p, int num_clusters, cudaStream_t stream);

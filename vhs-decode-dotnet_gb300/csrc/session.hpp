@@ -127,6 +127,7 @@ struct vhsdecode_gb300_session {
     int out_lines = 0;
     int outlen = 0;
     int num_sms = 0;
+    int fft_plan = 0;    // radix plans of the fused demodulator (tuned per device)
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[6] = {};

@@ -114,7 +114,8 @@ class DecodeResult(ctypes.Structure):
                 ("repaired_blocks", ctypes.c_uint32), ("stop_reason", ctypes.c_uint32),
                 ("device_ms", ctypes.c_double), ("demod_ms", ctypes.c_double),
                 ("field_ms", ctypes.c_double), ("host_ms", ctypes.c_double),
-                ("kernel_launches", ctypes.c_uint32), ("segments", ctypes.c_uint32)]
+                ("kernel_launches", ctypes.c_uint32), ("segments", ctypes.c_uint32),
+                ("fft_plan", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
 
 
 class FieldInfo(ctypes.Structure):
