@@ -21,6 +21,7 @@
 #include <new>
 #include <stdexcept>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #define VHSDECODE_GB300_EXPORTS 1
@@ -293,6 +294,7 @@ void session_init(vhsdecode_gb300_session* s, const vhsdecode_gb300_session_conf
     s->pw_ff.alloc(pwf.size());
     ck(cudaMemcpy(s->pw_ff.p, pwf.data(), pwf.size() * sizeof(float2), cudaMemcpyHostToDevice), "upload");
     s->level_work.alloc((size_t)s->max_fields * 1024);
+    s->tbc_consts.alloc((size_t)s->max_fields * s->out_lines * kTbcLineConstsBytes);
     s->tbc.alloc((size_t)s->max_fields * s->out_lines * s->outlen);
     s->span_len = read_length(s->sp) + 2 * kStride;  // upper bound of a resolved span
     int nch = dropout_chunks(s->span_len);
@@ -653,8 +655,11 @@ void launch_field_batch(vhsdecode_gb300_session* s, int f0, int f1, const T* vid
     tp.out_u16 = s->tbc.p + (size_t)f0 * s->out_lines * s->outlen;
     tp.out_hz = nullptr;
     tp.level_work = s->level_work.p + (size_t)f0 * 1024;
+    tp.line_consts = std::is_same<T, float>::value
+                         ? s->tbc_consts.p + (size_t)f0 * s->out_lines * kTbcLineConstsBytes
+                         : nullptr;
     ck(launch_tbc_pw<T>(video, stream_len, tp, s->pw.p, fs), "tbc launch");
-    s->launches += kTbcKernels;
+    s->launches += tp.line_consts ? kTbcFastKernels : kTbcKernels;
     if (timing) ck(cudaEventRecord(s->stage_ev[2], fs), "event");
     const int nch = dropout_chunks(s->span_len);
     DropoutParams dp{};

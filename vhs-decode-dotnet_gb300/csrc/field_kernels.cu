@@ -1001,32 +1001,45 @@ struct TbcLineConsts {
     int smooth;
 };
 
+static_assert(sizeof(TbcLineConsts) <= kTbcLineConstsBytes, "line constants slot");
+
+// The binary64 per-line plan of k_tbc_fast, one thread per output line of
+// every field (lane-parallel, so no CTA of the sinc kernel waits on a serial
+// FP64 preamble): position plan a + b k (TbcLineResampler's linear plan),
+// the line's level factor and the uint16 conversion, each split to a float pair.
+__global__ void k_tbc_consts(TbcParams p) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (int64_t)p.nfields * p.out_lines) return;
+    const int f = (int)(t / p.out_lines);
+    const int ol = (int)(t - (int64_t)f * p.out_lines);
+    const int line = p.first_line[f] + ol;
+    const double* loc = p.locs + (int64_t)f * p.lines;
+    const double nominal = p.nominal;
+    const double out_scale = nominal / (double)p.outlen;
+    const double* w = p.level_work + (int64_t)f * 1024;
+    const double adj = w[2 * line];
+    const double ll = loc[line];
+    const double delta = loc[line + 1] - ll;
+    TbcLineConsts c;
+    c.a = split_double(ll + delta * (((double)line * p.outlen * out_scale - (double)line * nominal) / nominal));
+    c.b = split_double(delta * out_scale / nominal);
+    c.adj = split_double(adj);
+    c.dlev = split_double(w[2 * line + 1] - adj);
+    c.ire0 = split_double(p.ire0);
+    c.k = split_double(p.output_scale * p.inv_hz_ire);
+    c.off = split_double(p.offset);
+    c.smooth = p.smoothing > 0.0 && line > 0;
+    reinterpret_cast<TbcLineConsts*>(p.line_consts + t * kTbcLineConstsBytes)[0] = c;
+}
+
 __global__ void __launch_bounds__(256) k_tbc_fast(const float* stream, int64_t stream_len, TbcParams p) {
-    __shared__ TbcLineConsts c;
     const int f = blockIdx.y;
     const int ol = blockIdx.x;
-    const int line = p.first_line[f] + ol;
     const int64_t s0 = p.span_start[f];
     const int64_t n = min(p.span_len[f], stream_len - s0);
     const float* src = stream + s0;
-    if (threadIdx.x == 0) {
-        const double* loc = p.locs + (int64_t)f * p.lines;
-        const double nominal = p.nominal;
-        const double out_scale = nominal / (double)p.outlen;
-        const double* w = p.level_work + (int64_t)f * 1024;
-        const double adj = w[2 * line];
-        const double ll = loc[line];
-        const double delta = loc[line + 1] - ll;
-        c.a = split_double(ll + delta * (((double)line * p.outlen * out_scale - (double)line * nominal) / nominal));
-        c.b = split_double(delta * out_scale / nominal);
-        c.adj = split_double(adj);
-        c.dlev = split_double(w[2 * line + 1] - adj);
-        c.ire0 = split_double(p.ire0);
-        c.k = split_double(p.output_scale * p.inv_hz_ire);
-        c.off = split_double(p.offset);
-        c.smooth = p.smoothing > 0.0 && line > 0;
-    }
-    __syncthreads();
+    const TbcLineConsts& c = *reinterpret_cast<const TbcLineConsts*>(
+        p.line_consts + ((int64_t)f * p.out_lines + ol) * kTbcLineConstsBytes);
     const float4* lut4 = reinterpret_cast<const float4*>(p.lut);
     const float4* pair4 = reinterpret_cast<const float4*>(p.lut_pair);
     uint16_t* out = p.out_u16 + ((int64_t)f * p.out_lines + ol) * p.outlen;
@@ -1143,10 +1156,14 @@ cudaError_t launch_tbc_pw(const T* stream, int64_t stream_len, const TbcParams& 
     if (p.nfields <= 0) return cudaSuccess;
     k_tbc_levels<<<p.nfields, 256, 0, s>>>(p, pw);
     dim3 grid(p.out_lines, p.nfields);
-    if (sizeof(T) == sizeof(float) && p.out_u16 && !p.out_hz && (p.smoothing <= 0.0 || p.pw_ff))
+    if (sizeof(T) == sizeof(float) && p.out_u16 && !p.out_hz && (p.smoothing <= 0.0 || p.pw_ff) &&
+        p.line_consts) {
+        const int64_t nl = (int64_t)p.nfields * p.out_lines;
+        k_tbc_consts<<<(unsigned)((nl + 127) / 128), 128, 0, s>>>(p);
         k_tbc_fast<<<grid, 256, 0, s>>>(reinterpret_cast<const float*>(stream), stream_len, p);
-    else
+    } else {
         k_tbc<T><<<grid, 256, 0, s>>>(stream, stream_len, p, pw);
+    }
     return cudaGetLastError();
 }
 template cudaError_t launch_tbc_pw<float>(const float*, int64_t, const TbcParams&, const double*, cudaStream_t);

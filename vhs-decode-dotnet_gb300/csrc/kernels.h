@@ -148,8 +148,12 @@ struct TbcParams {
     uint16_t* out_u16;          // [nfields * out_lines * outlen] or null
     double* out_hz;             // optional float output (values rounded to float)
     double* level_work;         // [nfields * (max_first_line + out_lines)] line factors
+    unsigned char* line_consts; // [nfields * out_lines * kTbcLineConstsBytes] float-pair line plans
+                                // of the fast float kernel (null: binary64 kernel)
 };
-constexpr int kTbcKernels = 2;
+constexpr int kTbcLineConstsBytes = 64;
+constexpr int kTbcKernels = 2;      // levels + sinc (binary64 kernel)
+constexpr int kTbcFastKernels = 3;  // levels + line plans + sinc (float kernel)
 // pw[k] = (1 - alpha)^(k+1), k < outlen, alpha = 1 / (smoothing * outlen)
 template <typename T>
 cudaError_t launch_tbc_pw(const T* video_stream, int64_t stream_len, const TbcParams& p,

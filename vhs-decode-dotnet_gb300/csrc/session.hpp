@@ -186,6 +186,7 @@ struct vhsdecode_gb300_session {
     DevBuf<float> lut, lut_pair;
     DevBuf<float2> pw_ff;
     DevBuf<double> pw, level_work;
+    DevBuf<unsigned char> tbc_consts;   // float-pair line plans of the fast TBC kernel
     DevBuf<uint16_t> tbc;
     DevBuf<int64_t> drop_range, drop_events;
     DevBuf<float> drop_mean, drop_partial;
