@@ -63,83 +63,108 @@ __device__ __forceinline__ unsigned edge_bits(unsigned cond, unsigned hold, unsi
     return edges;
 }
 
+// Two passes over a stream range, 1024 samples per warp, kPT threads per CTA.
+// Pass 0 counts each warp's edge events (counts[warp]) and each CTA's sum; the
+// CTA that finishes last (a ticket taken after a fence, so every other CTA's
+// sum is visible to it) scans the CTA sums into exclusive CTA offsets and the
+// total.  No CTA waits on another.  Pass 1 recounts nothing: a warp's offset
+// is its CTA's offset plus the counts of the warps before it in the CTA, and
+// it writes its events in order.  offsets layout: [0] ticket (zeroed before
+// pass 0), [1, 1 + nchunks) CTA offsets, [1 + nchunks, 1 + 2 nchunks) CTA sums.
 template <typename T, bool WRITE>
-__global__ void k_pulse_pass(const T* __restrict__ ref, int64_t begin, int64_t n, Cmp<T> cmp,
-                             int64_t* counts, const int64_t* offsets, int64_t* events,
-                             int64_t capacity) {
-    const int lane = threadIdx.x & 31;
+__global__ void __launch_bounds__(kPT) k_pulse_pass(const T* __restrict__ ref, int64_t begin, int64_t n,
+                                                    Cmp<T> cmp, int64_t* counts, int64_t* offsets,
+                                                    int64_t* events, int64_t capacity, int64_t* total,
+                                                    int64_t nchunks) {
+    constexpr int kWarps = kPT / 32;
+    __shared__ int64_t wcnt[kWarps];
+    __shared__ bool last;
+    const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
     const int64_t wg = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t start = begin + wg * kPWarpSamples;
-    if (start >= n) {
-        if (!WRITE && lane == 0) counts[wg] = 0;
-        return;
-    }
-    unsigned st = 0u;
-    if (lane == 0) st = state_before(ref, start, cmp.h) ? 1u : 0u;
-    st = __shfl_sync(0xffffffffu, st, 0);
-    int64_t off = WRITE ? offsets[wg] : 0;
     int64_t cnt = 0;
-    // eight loads in flight per lane, then the ballots in order
-    for (int it0 = 0; it0 < kPWarpSamples / 32; it0 += 8) {
-        T vv[8];
-#pragma unroll
-        for (int j = 0; j < 8; j++) {
-            int64_t p = start + (it0 + j) * 32 + lane;
-            vv[j] = p < n ? ref[p] : (T)0;
+    if (start < n) {
+        unsigned st = 0u;
+        if (lane == 0) st = state_before(ref, start, cmp.h) ? 1u : 0u;
+        st = __shfl_sync(0xffffffffu, st, 0);
+        int64_t off = 0;
+        if (WRITE) {
+            off = offsets[1 + blockIdx.x];
+            for (int k = 0; k < wl; k++) off += counts[(int64_t)blockIdx.x * kWarps + k];
         }
+        // eight loads in flight per lane, then the ballots in order
+        for (int it0 = 0; it0 < kPWarpSamples / 32; it0 += 8) {
+            T vv[8];
 #pragma unroll
-        for (int j = 0; j < 8; j++) {
-            int64_t p = start + (it0 + j) * 32 + lane;
-            bool inb = p < n;
-            T v = vv[j];
-            bool hold = !inb || !(v == v);
-            bool c = inb && (v <= cmp.h);
-            unsigned cm = __ballot_sync(0xffffffffu, c);
-            unsigned hm = __ballot_sync(0xffffffffu, hold);
-            unsigned e = edge_bits(cm, hm, st);
-            if (WRITE && ((e >> lane) & 1u)) {
-                int64_t o = off + __popc(e & ((1u << lane) - 1u));
-                if (o < capacity) events[o] = 2 * p + (c ? 0 : 1);
+            for (int j = 0; j < 8; j++) {
+                int64_t p = start + (it0 + j) * 32 + lane;
+                vv[j] = p < n ? ref[p] : (T)0;
             }
-            int pc = __popc(e);
-            off += pc;
-            cnt += pc;
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                int64_t p = start + (it0 + j) * 32 + lane;
+                bool inb = p < n;
+                T v = vv[j];
+                bool hold = !inb || !(v == v);
+                bool c = inb && (v <= cmp.h);
+                unsigned cm = __ballot_sync(0xffffffffu, c);
+                unsigned hm = __ballot_sync(0xffffffffu, hold);
+                unsigned e = edge_bits(cm, hm, st);
+                if (WRITE && ((e >> lane) & 1u)) {
+                    int64_t o = off + __popc(e & ((1u << lane) - 1u));
+                    if (o < capacity) events[o] = 2 * p + (c ? 0 : 1);
+                }
+                int pc = __popc(e);
+                off += pc;
+                cnt += pc;
+            }
         }
     }
-    if (!WRITE && lane == 0) counts[wg] = cnt;
-}
-
-
-// single-CTA exclusive scan of chunk counts
-__global__ void k_scan_counts(const int64_t* counts, int64_t nchunks, int64_t* offsets,
-                              int64_t* total) {
+    if (WRITE) return;
+    if (lane == 0) {
+        counts[wg] = cnt;
+        wcnt[wl] = cnt;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int64_t sum = 0;
+        for (int k = 0; k < kWarps; k++) sum += wcnt[k];
+        offsets[1 + nchunks + blockIdx.x] = sum;
+        __threadfence();
+        unsigned long long t = atomicAdd(reinterpret_cast<unsigned long long*>(offsets), 1ull);
+        last = t == (unsigned long long)(nchunks - 1);
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    // exclusive scan of the CTA sums (read from L2: other CTAs wrote them)
+    __shared__ int64_t wsum[kWarps];
     __shared__ int64_t carry;
-    __shared__ int64_t wsum[32];
     if (threadIdx.x == 0) carry = 0;
     __syncthreads();
-    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    for (int64_t base = 0; base < nchunks; base += blockDim.x) {
+    for (int64_t base = 0; base < nchunks; base += kPT) {
         int64_t i = base + threadIdx.x;
-        int64_t v = i < nchunks ? counts[i] : 0;
+        int64_t v = i < nchunks ? __ldcg(offsets + 1 + nchunks + i) : 0;
         int64_t incl = v;
         for (int o = 1; o < 32; o <<= 1) {
             int64_t t = __shfl_up_sync(0xffffffffu, incl, o);
             if (lane >= o) incl += t;
         }
-        if (lane == 31) wsum[w] = incl;
+        if (lane == 31) wsum[wl] = incl;
         __syncthreads();
         int64_t wb = 0, tot = 0;
-        for (int k = 0; k < (int)(blockDim.x / 32); k++) {
-            if (k < w) wb += wsum[k];
+        for (int k = 0; k < kWarps; k++) {
+            if (k < wl) wb += wsum[k];
             tot += wsum[k];
         }
-        if (i < nchunks) offsets[i] = carry + wb + incl - v;
+        if (i < nchunks) offsets[1 + i] = carry + wb + incl - v;
         __syncthreads();
         if (threadIdx.x == 0) carry += tot;
         __syncthreads();
     }
     if (threadIdx.x == 0) total[0] = carry;
 }
+
 }  // namespace
 
 template <typename T>
@@ -153,12 +178,12 @@ cudaError_t launch_pulse_events_range(const T* ref, int64_t begin, int64_t end, 
         return cudaGetLastError();
     }
     Cmp<T> cmp = make_cmp<T>(high);
-    int64_t slots = pulse_count_slots(len);
-    k_pulse_pass<T, false><<<(unsigned)nchunks, kPT, 0, s>>>(ref, begin, end, cmp, counts, nullptr,
-                                                            nullptr, 0);
-    k_scan_counts<<<1, 1024, 0, s>>>(counts, slots, offsets, total);
+    cudaError_t e = cudaMemsetAsync(offsets, 0, sizeof(int64_t), s);   // the last-CTA ticket
+    if (e != cudaSuccess) return e;
+    k_pulse_pass<T, false><<<(unsigned)nchunks, kPT, 0, s>>>(ref, begin, end, cmp, counts, offsets,
+                                                            nullptr, 0, total, nchunks);
     k_pulse_pass<T, true><<<(unsigned)nchunks, kPT, 0, s>>>(ref, begin, end, cmp, counts, offsets,
-                                                           events, capacity);
+                                                           events, capacity, total, nchunks);
     return cudaGetLastError();
 }
 template <typename T>
@@ -671,107 +696,171 @@ __global__ void __launch_bounds__(1024) k_hsync_spec(const T* stream, int64_t st
     }
 }
 
+// Carried state of the chain: the porch level carried from line to line
+// (RefineLineLocationsFromHSync's previous porch), whether it is set, and the
+// bits of the previous line's right porch (-1 when none).
+struct ChainState {
+    double pp;
+    long long prev_r_bits;
+    int pp_set;
+    int miss;
+};
+
+__device__ __forceinline__ bool same_state(const ChainState& a, const ChainState& b) {
+    return __double_as_longlong(a.pp) == __double_as_longlong(b.pp) && a.pp_set == b.pp_set &&
+           a.prev_r_bits == b.prev_r_bits;
+}
+
+// One line of the carry walk (called by all 32 lanes of a warp: a porch miss
+// runs a cooperative crossing search).  Every comparison that does not involve
+// the carried porch level was precomputed (LineInfo::pre); the carried level
+// enters only through "is it bit-identical to the previous line's right porch"
+// (then the speculative crossing rc_spec applies) and, on a miss, a new
+// midpoint search.  The carried level is positive once set, so its "> 0" test
+// is a flag.
 template <typename T>
-__global__ void k_hsync_chain(const T* stream, int64_t stream_len, HsyncParams p, const LineInfo* info,
-                              int* misses) {
+__device__ __forceinline__ void chain_step(const LineInfo& li, ChainState& cs, const Span<T>& sp, int one,
+                                           int lane, double& out, uint8_t& fo_out) {
+    enum { kRefLoc, kRefCross, kRefOwn, kRefSpec, kRefMiss };
+    const int flags = li.flags, pre = li.pre;
+    out = li.loc;
+    uint8_t fo = (flags & 32) ? 1 : 0;
+    const bool filled = (flags & 32) != 0;
+    if (flags & 1) {
+        fo = 1;
+    } else if (flags & 2) {
+        int ref = kRefLoc;
+        double refined = li.loc, rc_miss = 0.0;
+        if ((pre & kPreCross) && !filled) {
+            bool ok = false, preserve = false, porch_pos = false;
+            double porch = 0.0;
+            int kind = kRefLoc;
+            if (flags & 4) {
+                preserve = true;
+                if (cs.pp_set) {
+                    porch = cs.pp;
+                    porch_pos = true;
+                    if (__double_as_longlong(cs.pp) == cs.prev_r_bits) {
+                        ok = (pre & kPreSpecOk) != 0;
+                        kind = kRefSpec;
+                    } else {
+                        cs.miss++;
+                        int c2 = (int)min((int64_t)400, sp.n - li.ss - 1);
+                        rc_miss = zero_crossing(sp, li.ss, (cs.pp + li.sync) / 2.0, 0, c2, lane);
+                        ok = rc_miss == rc_miss && fabs(rc_miss - li.crossing) < one / 2.0;
+                        kind = kRefMiss;
+                    }
+                } else if (flags & 8) {
+                    porch = li.own_porch;
+                    porch_pos = (pre & kPreOwnPos) != 0;
+                    ok = (pre & kPreOwnOk) != 0;
+                    kind = kRefOwn;
+                }
+            }
+            if (ok) {
+                refined = kind == kRefSpec ? li.rc_spec : (kind == kRefOwn ? li.rc_own : rc_miss);
+                ref = kind;
+                fo = filled ? 1 : 0;
+                if (porch_pos) { cs.pp = porch; cs.pp_set = 1; }
+            } else {
+                fo = 1;
+                if (preserve) ref = kRefCross;
+            }
+        } else {
+            fo = 1;
+        }
+        if (flags & 16) {
+            bool near;
+            switch (ref) {
+                case kRefCross: near = (pre & kPreNearCross) != 0; break;
+                case kRefOwn: near = (pre & kPreNearOwn) != 0; break;
+                case kRefSpec: near = (pre & kPreNearSpec) != 0; break;
+                case kRefMiss: near = fabs(li.r_cand - rc_miss) < one * 2.0; break;
+                default: near = (pre & kPreNearLoc) != 0; break;
+            }
+            if (near) {
+                refined = li.r_cand;
+                fo = 0;
+                if (pre & kPreRPos) { cs.pp = li.r_porch; cs.pp_set = 1; }
+            }
+        }
+        out = refined;
+    }
+    cs.prev_r_bits = (flags & 16) && li.r_porch == li.r_porch ? __double_as_longlong(li.r_porch) : -1;
+    fo_out = fo;
+}
+
+// The walk over a field's lines, split into kChainWarps segments walked at
+// once, one warp each.  A segment's entering state is guessed by walking the
+// kChainWarm lines before it from the initial state (a right-edge refinement
+// resets the carried state, so the guess is almost always exact); afterwards
+// warp 0 compares each guess with the state the previous segment actually
+// left and re-walks the segments whose guess differed, in order.  The result
+// is the sequential walk's, bit for bit.
+constexpr int kChainWarps = 8;
+constexpr int kChainWarm = 12;
+
+template <typename T>
+__global__ void __launch_bounds__(32 * kChainWarps) k_hsync_chain(const T* stream, int64_t stream_len,
+                                                                   HsyncParams p, const LineInfo* info,
+                                                                   int* misses) {
     const int f = blockIdx.x;
-    const int lane = threadIdx.x;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int64_t s0 = p.span_start[f];
     Span<T> sp{stream + s0, min(p.span_len[f], stream_len - s0)};
     extern __shared__ __align__(16) unsigned char chain_smem[];
     LineInfo* fi = reinterpret_cast<LineInfo*>(chain_smem);
+    __shared__ ChainState entry[kChainWarps], leave[kChainWarps];
     {
         const int4* g = reinterpret_cast<const int4*>(info + (int64_t)f * p.lines);
         int4* d = reinterpret_cast<int4*>(fi);
         const int words = (int)(p.lines * sizeof(LineInfo) / sizeof(int4));
-        for (int i = lane; i < words; i += 32) d[i] = g[i];
-        __syncwarp();
+        for (int i = threadIdx.x; i < words; i += blockDim.x) d[i] = g[i];
     }
-    // The carry walk: every comparison that does not involve the carried
-    // porch level was precomputed (LineInfo::pre); the carried level enters
-    // only through "is it bit-identical to the previous line's right porch"
-    // (then the speculative crossing rc_spec applies) and, on a miss, a new
-    // midpoint search.  The carried level is positive once set, so its
-    // "> 0" test is a flag.
+    __syncthreads();
     const int one = p.one_us;
-    double pp = -1.0;
-    bool pp_set = false;
-    long long prev_r_bits = -1;    // bits of the previous line's right porch, -1 when none
-    int miss = 0;
-    enum { kRefLoc, kRefCross, kRefOwn, kRefSpec, kRefMiss };
-    for (int line = 0; line < p.lines; line++) {
-        const LineInfo& li = fi[line];
-        const int flags = li.flags, pre = li.pre;
-        double out = li.loc;
-        uint8_t fo = (flags & 32) ? 1 : 0;
-        const bool filled = (flags & 32) != 0;
-        if (flags & 1) {
-            fo = 1;
-        } else if (flags & 2) {
-            int ref = kRefLoc;
-            double refined = li.loc, rc_miss = 0.0;
-            if ((pre & kPreCross) && !filled) {
-                bool ok = false, preserve = false, porch_pos = false;
-                double porch = 0.0;
-                int kind = kRefLoc;
-                if (flags & 4) {
-                    preserve = true;
-                    if (pp_set) {
-                        porch = pp;
-                        porch_pos = true;
-                        if (__double_as_longlong(pp) == prev_r_bits) {
-                            ok = (pre & kPreSpecOk) != 0;
-                            kind = kRefSpec;
-                        } else {
-                            miss++;
-                            int c2 = (int)min((int64_t)400, sp.n - li.ss - 1);
-                            rc_miss = zero_crossing(sp, li.ss, (pp + li.sync) / 2.0, 0, c2, lane);
-                            ok = rc_miss == rc_miss && fabs(rc_miss - li.crossing) < one / 2.0;
-                            kind = kRefMiss;
-                        }
-                    } else if (flags & 8) {
-                        porch = li.own_porch;
-                        porch_pos = (pre & kPreOwnPos) != 0;
-                        ok = (pre & kPreOwnOk) != 0;
-                        kind = kRefOwn;
-                    }
-                }
-                if (ok) {
-                    refined = kind == kRefSpec ? li.rc_spec : (kind == kRefOwn ? li.rc_own : rc_miss);
-                    ref = kind;
-                    fo = filled ? 1 : 0;
-                    if (porch_pos) { pp = porch; pp_set = true; }
-                } else {
-                    fo = 1;
-                    if (preserve) ref = kRefCross;
-                }
-            } else {
-                fo = 1;
+    const int seg = (p.lines + kChainWarps - 1) / kChainWarps;
+    double* locs = p.locs_out + (int64_t)f * p.lines;
+    uint8_t* filled = p.filled_out + (int64_t)f * p.lines;
+    auto walk = [&](ChainState& cs, int l0, int l1) {
+        for (int line = l0; line < l1; line++) {
+            double out;
+            uint8_t fo;
+            chain_step(fi[line], cs, sp, one, lane, out, fo);
+            if (lane == 0) {
+                locs[line] = out - p.ntsc_shift;
+                filled[line] = fo;
             }
-            if (flags & 16) {
-                bool near;
-                switch (ref) {
-                    case kRefCross: near = (pre & kPreNearCross) != 0; break;
-                    case kRefOwn: near = (pre & kPreNearOwn) != 0; break;
-                    case kRefSpec: near = (pre & kPreNearSpec) != 0; break;
-                    case kRefMiss: near = fabs(li.r_cand - rc_miss) < one * 2.0; break;
-                    default: near = (pre & kPreNearLoc) != 0; break;
-                }
-                if (near) {
-                    refined = li.r_cand;
-                    fo = 0;
-                    if (pre & kPreRPos) { pp = li.r_porch; pp_set = true; }
-                }
-            }
-            out = refined;
         }
-        prev_r_bits = (flags & 16) && li.r_porch == li.r_porch ? __double_as_longlong(li.r_porch) : -1;
-        if (lane == 0) {
-            p.locs_out[(int64_t)f * p.lines + line] = out - p.ntsc_shift;
-            p.filled_out[(int64_t)f * p.lines + line] = fo;
-        }
+    };
+    const int l0 = min(w * seg, p.lines), l1 = min(l0 + seg, p.lines);
+    ChainState cs{-1.0, -1, 0, 0};
+    for (int line = max(0, l0 - kChainWarm); line < l0; line++) {
+        double out;
+        uint8_t fo;
+        chain_step(fi[line], cs, sp, one, lane, out, fo);
     }
-    if (lane == 0 && misses) atomicAdd(misses, miss);
+    cs.miss = 0;
+    if (lane == 0) entry[w] = cs;
+    walk(cs, l0, l1);
+    if (lane == 0) leave[w] = cs;
+    __syncthreads();
+    if (w != 0) return;
+    ChainState prev = leave[0];
+    int total = prev.miss;
+    for (int k = 1; k < kChainWarps; k++) {
+        const int a = min(k * seg, p.lines), b = min(a + seg, p.lines);
+        if (same_state(entry[k], prev)) {
+            prev = leave[k];
+        } else {
+            ChainState c = prev;
+            c.miss = 0;
+            walk(c, a, b);
+            prev = c;
+        }
+        total += prev.miss;
+    }
+    if (lane == 0 && misses) atomicAdd(misses, total);
 }
 }  // namespace
 
@@ -785,8 +874,8 @@ cudaError_t launch_hsync_refine(const T* stream, int64_t stream_len, const Hsync
     LineInfo* info = reinterpret_cast<LineInfo*>(p.work);
     k_hsync_lines<T><<<blocks, threads, 0, s>>>(stream, stream_len, p, info);
     k_hsync_spec<T><<<blocks, threads, 0, s>>>(stream, stream_len, p, info);
-    k_hsync_chain<T><<<p.nfields, 32, p.lines * sizeof(LineInfo), s>>>(stream, stream_len, p, info,
-                                                                       p.misses);
+    k_hsync_chain<T><<<p.nfields, 32 * kChainWarps, p.lines * sizeof(LineInfo), s>>>(stream, stream_len, p,
+                                                                                     info, p.misses);
     return cudaGetLastError();
 }
 size_t hsync_work_bytes(int nfields, int lines) { return (size_t)nfields * lines * sizeof(LineInfo); }

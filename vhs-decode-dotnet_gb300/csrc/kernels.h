@@ -90,7 +90,7 @@ constexpr int kPlainSubKernels = 10;    // added by sub-deemphasis (5 + 1 FFT x 
 // 1024 samples, then ordered write.  counts / offsets_scratch hold
 // pulse_count_slots(n) entries.
 constexpr int kPulseChunk = 4096;
-constexpr int kPulseKernels = 3;      // kernels one launch_pulse_events* call starts
+constexpr int kPulseKernels = 2;      // kernels one launch_pulse_events* call starts (plus a memset)
 inline int64_t pulse_count_slots(int64_t n) { return (n + kPulseChunk - 1) / kPulseChunk * 4; }
 template <typename T>
 cudaError_t launch_pulse_events(const T* ref, int64_t n, double high, int64_t* counts,
