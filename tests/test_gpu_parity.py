@@ -144,6 +144,7 @@ def test_stream_channels_match_oracle(gpu, system, precision, request):
     dy = np.abs(y - vlp)
     assert np.quantile(dv, 0.999) < FREQ_TOL_HZ, np.max(dv)
     assert np.quantile(dy, 0.999) < FREQ_TOL_HZ, np.max(dy)
+    assert np.median(dv) < 2.0 and np.median(dy) < 2.0, (np.median(dv), np.median(dy))
     de = np.abs(e - env) / np.maximum(np.abs(env), 1.0)
     assert np.quantile(de, 0.999) < 1e-3
     if precision == 1:
@@ -288,6 +289,8 @@ def test_svhs_matches_oracle(gpu, system, precision, request):
         dy = np.abs(y - vlp)
         assert np.quantile(dv, 0.999) < FREQ_TOL_HZ, np.max(dv)
         assert np.quantile(dy, 0.999) < FREQ_TOL_HZ, np.max(dy)
+        # no systematic offset (FP32 rounding alone is well under 2 Hz)
+        assert np.median(dv) < 2.0 and np.median(dy) < 2.0, (np.median(dv), np.median(dy))
         de = np.abs(e - env) / np.maximum(np.abs(env), 1.0)
         assert np.quantile(de, 0.999) < 1e-3
         if precision == 1:

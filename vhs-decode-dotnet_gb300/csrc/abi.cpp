@@ -438,6 +438,10 @@ FastDemodParams fp32_params(vhsdecode_gb300_session* s, const int16_t* rf_dev) {
     p.fs = (float)s->fs;
     p.diff_max = (float)((s->fmt.ire0 + s->fmt.hz_ire * 100.0) * 2.0);
     p.dc = (float)s->fmt.ire0;
+    // the DC gain of Video is not exactly 1 for S-VHS (its measured luma table
+    // starts at 1.0000019): 5.88 MHz x 1.9e-6 would be an 11 Hz offset
+    p.dc_video = (float)((double)p.dc * s->filt.video[0].real());
+    p.dc_sync = (float)((double)p.dc * s->filt.sync[0].real());
     p.env_b0 = (float)s->filt.env_b0;
     p.env_b1 = (float)s->filt.env_b1;
     p.env_a1 = (float)s->filt.env_a1;

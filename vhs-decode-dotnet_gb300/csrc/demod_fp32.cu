@@ -11,7 +11,8 @@
 //        + diff-demod spike repair when any d > limit      (repair path)
 //   env= |Re z| rolled by 4, 700 kHz first-order filtfilt  (envelope)
 //   D  = rfft(d - ire0)                                    (stage 4)
-//   video = irfft(D * Video) + ire0, sync = roll(irfft(D * VideoLowPass05), -32) + ire0
+//   video = irfft(D * Video) + ire0 Video[0], sync = roll(irfft(D * VideoLowPass05), -32)
+//           + ire0 VideoLowPass05[0]
 //                                                          (stage 5)
 //   S-VHS sub-deemphasis: a = ifft(one-sided D * Video * HighPass) (the
 //   analytic signal of the high part), amp = |a| low-passed forward and
@@ -731,7 +732,8 @@ vhsd_demod_fp32_kernel(FastDemodParams p) {
             cluster.sync();
             float* vout = p.video_out + (blk + p.first_block) * (int64_t)S - CUT;
             float* sout = p.sync_out + (blk + p.first_block) * (int64_t)S - CUT - 32;
-            const float dc = p.dc;
+            // the removed DC returns through each filter's DC gain
+            const float dcv = p.dc_video, dcs = p.dc_sync;
 #pragma unroll 2
             for (int t = 0; t < 8; t++) {
                 int ml = tid + t * T;              // [0, 4096)
@@ -748,14 +750,14 @@ vhsd_demod_fp32_kernel(FastDemodParams p) {
                     int n1 = 2 * m, n2 = 2 * m + 16384;
                     if (sig == 0) {
                         if (n1 >= CUT && n1 < CUT + S)
-                            *reinterpret_cast<float2*>(vout + n1) = make_float2(p1.x + dc, p1.y + dc);
+                            *reinterpret_cast<float2*>(vout + n1) = make_float2(p1.x + dcv, p1.y + dcv);
                         if (n2 >= CUT && n2 < CUT + S)
-                            *reinterpret_cast<float2*>(vout + n2) = make_float2(p2.x + dc, p2.y + dc);
+                            *reinterpret_cast<float2*>(vout + n2) = make_float2(p2.x + dcv, p2.y + dcv);
                     } else {
                         if (n1 >= CUT + 32 && n1 < CUT + 32 + S)
-                            *reinterpret_cast<float2*>(sout + n1) = make_float2(p1.x + dc, p1.y + dc);
+                            *reinterpret_cast<float2*>(sout + n1) = make_float2(p1.x + dcs, p1.y + dcs);
                         if (n2 >= CUT + 32 && n2 < CUT + 32 + S)
-                            *reinterpret_cast<float2*>(sout + n2) = make_float2(p2.x + dc, p2.y + dc);
+                            *reinterpret_cast<float2*>(sout + n2) = make_float2(p2.x + dcs, p2.y + dcs);
                     }
                 }
             }

@@ -39,7 +39,8 @@ struct FastDemodParams {
     const float2* tw_lo;       // [128] exp(-2 pi i l / 32768)
     float fs;                  // sample rate (Hz)
     float diff_max;            // diff-demod spike limit (Hz)
-    float dc;                  // subtracted before the demod FFT and added back
+    float dc;                  // subtracted before the demod FFT (ire0) ...
+    float dc_video, dc_sync;   // ... and added back as ire0 x the filters' DC gains
     float env_b0, env_b1, env_a1;
     float* video_out;          // stitched stream, stream index s = b*30720 + n - 1024
     float* sync_out;
