@@ -400,15 +400,16 @@ __device__ __forceinline__ float sub_gain(float amp, const SubDeemph& s) {
     return amp;
 }
 
-// One RF block into this rank's packed DIF input: rank 0 gets a + b, rank 1
+// One RF block (read from the prefetch copy in shared memory) into this
+// rank's packed DIF input: rank 0 gets a + b, rank 1
 // (a - b) W^(2p), p in [0, 8192), where a / b are the complex pairs of the
 // block's first / second half.  W^(2p) = W^(8v) W^(2e) for p = 4v + e.
 __device__ __forceinline__ void load_rf(float2* buf, const int16_t* x, int rank, const Tw& tw, int tid) {
 #pragma unroll
     for (int it = 0; it < 4; it++) {
         int vi = tid + it * T;  // vector index in [0, 2048)
-        int4 va = __ldg(reinterpret_cast<const int4*>(x) + vi);
-        int4 vb = __ldg(reinterpret_cast<const int4*>(x + 16384) + vi);
+        int4 va = reinterpret_cast<const int4*>(x)[vi];
+        int4 vb = reinterpret_cast<const int4*>(x + 16384)[vi];
         const int16_t* ha = reinterpret_cast<const int16_t*>(&va);
         const int16_t* hb = reinterpret_cast<const int16_t*>(&vb);
         float2 w8 = make_float2(1.0f, 0.0f);
@@ -505,6 +506,21 @@ __device__ __noinline__ void repair_block(Shared& sh, Shared* rsh, const FastDem
     __syncthreads();
 }
 
+// Next block's RF (32768 int16 = 64 KB, both halves) into `dst` with
+// asynchronous 16-byte copies (8 per thread), overlapping the current block's
+// later stages; prefetch_wait() + a barrier make it visible.
+__device__ __forceinline__ void prefetch_rf(void* dst, const int16_t* x, int tid) {
+    const char* src = reinterpret_cast<const char*>(x);
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        const int off = (tid + i * T) * 16;
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d + off), "l"(src + off) : "memory");
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+__device__ __forceinline__ void prefetch_wait() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
 }  // namespace fp32
 }  // namespace vhsd
 
@@ -535,10 +551,18 @@ vhsd_demod_fp32_kernel(FastDemodParams p) {
     const float inv_m = 1.0f / (float)M;
     const float freq = p.fs;
 
+    // the RF of each block is prefetched into sh.theta (free from the demod's
+    // last read until the next block's angles) while the previous block
+    // finishes
+    const int16_t* rf_smem = reinterpret_cast<const int16_t*>(sh.theta);
+    if (cluster_id < p.nblocks) prefetch_rf(sh.theta, p.rf + (cluster_id + p.first_block) * (int64_t)S, tid);
     for (int64_t blk = cluster_id; blk < p.nblocks; blk += nclusters) {
-        const int16_t* x = p.rf + (blk + p.first_block) * (int64_t)S;
+        const bool has_next = blk + nclusters < p.nblocks;
+        const int16_t* x_next = p.rf + (blk + nclusters + p.first_block) * (int64_t)S;
         // ---------------- stage 1: RF forward FFT (packed, DIF split) -----
-        load_rf(buf, x, rank, sh.tw, tid);
+        prefetch_wait();
+        __syncthreads();
+        load_rf(buf, rf_smem, rank, sh.tw, tid);
         __syncthreads();
         fft8192<false, 1, PLAN>(buf, sh.tw, tid);
         // X * RfVideo * Hilbert / N  (Hilbert: 1 at 0 and N/2, 2 between)
@@ -649,6 +673,7 @@ vhsd_demod_fp32_kernel(FastDemodParams p) {
                               }
                           });
         }
+        if (has_next && p.sub.high == nullptr) prefetch_rf(sh.theta, x_next, tid);
         // ---------------- stage 4: forward FFT of (demod - ire0) -----------
         {
             float2 uo[8], vo[8];
@@ -788,6 +813,7 @@ vhsd_demod_fp32_kernel(FastDemodParams p) {
                 for (int i = 8192 + tid; i < M; i += T) buf[sx(i)] = make_float2(0.f, 0.f);
             }
             __syncthreads();
+            if (has_next) prefetch_rf(sh.theta, x_next, tid);   // the saved spectrum is consumed
             fft16384<true, PLAN>(buf, sh.tw, tid);
             cluster.sync();
             {
