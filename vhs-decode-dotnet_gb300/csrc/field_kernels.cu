@@ -1121,7 +1121,9 @@ __global__ void k_tbc_consts(TbcParams p) {
     reinterpret_cast<TbcLineConsts*>(p.line_consts + t * kTbcLineConstsBytes)[0] = c;
 }
 
-__global__ void __launch_bounds__(256) k_tbc_fast(const float* stream, int64_t stream_len, TbcParams p) {
+constexpr int kTbcFastMaxThreads = 384;
+__global__ void __launch_bounds__(kTbcFastMaxThreads) k_tbc_fast(const float* stream, int64_t stream_len,
+                                                                 TbcParams p) {
     const int f = blockIdx.y;
     const int ol = blockIdx.x;
     const int64_t s0 = p.span_start[f];
@@ -1249,7 +1251,11 @@ cudaError_t launch_tbc_pw(const T* stream, int64_t stream_len, const TbcParams& 
         p.line_consts) {
         const int64_t nl = (int64_t)p.nfields * p.out_lines;
         k_tbc_consts<<<(unsigned)((nl + 127) / 128), 128, 0, s>>>(p);
-        k_tbc_fast<<<grid, 256, 0, s>>>(reinterpret_cast<const float*>(stream), stream_len, p);
+        // a line in the fewest passes of at most 384 lanes, with the fewest idle
+        // lanes in the last pass (NTSC 910 samples: 3 x 320, PAL 1135: 3 x 384)
+        const int passes = (p.outlen + kTbcFastMaxThreads - 1) / kTbcFastMaxThreads;
+        const int threads = ((p.outlen + passes - 1) / passes + 31) / 32 * 32;
+        k_tbc_fast<<<grid, threads, 0, s>>>(reinterpret_cast<const float*>(stream), stream_len, p);
     } else {
         k_tbc<T><<<grid, 256, 0, s>>>(stream, stream_len, p, pw);
     }
