@@ -20,11 +20,25 @@ namespace vhsd {
 
 double round_away(double x) { return x >= 0 ? std::floor(x + 0.5) : -std::floor(-x + 0.5); }
 
+// numpy median: the middle element, or the mean of the two middle ones
+// (selection instead of a full sort; same values).
 static double median(std::vector<double> v) {
-    std::sort(v.begin(), v.end());
     size_t n = v.size();
     if (n == 0) return NAN;
-    return (n & 1) ? v[n / 2] : (v[n / 2 - 1] + v[n / 2]) / 2.0;
+    auto mid = v.begin() + (ptrdiff_t)(n / 2);
+    std::nth_element(v.begin(), mid, v.end());
+    if (n & 1) return *mid;
+    double lo = *std::max_element(v.begin(), mid);
+    return (lo + *mid) / 2.0;
+}
+
+static RatioBounds ratio_bounds(double n, double lo, double hi) {
+    RatioBounds b;
+    b.lo = (int64_t)std::floor(lo * n) - 4;
+    while ((double)b.lo / n < lo) b.lo++;
+    b.hi = (int64_t)std::ceil(hi * n) + 4;
+    while ((double)b.hi / n > hi) b.hi--;
+    return b;
 }
 
 SyncParams SyncParams::make(const FormatParams& f, double fs) {
@@ -44,12 +58,17 @@ SyncParams SyncParams::make(const FormatParams& f, double fs) {
     s.output_lines = f.frame_lines / 2 + 1;
     s.outlinelen = f.outlinelen;
     s.fsc_mhz = f.fsc_mhz;
+    s.half_line = ratio_bounds(s.nominal, 0.4, 0.6);
+    s.line = ratio_bounds(s.nominal, 0.9, 1.1);
+    s.mixed = ratio_bounds(s.nominal, 0.4, 1.1);
+    s.mean_line = ratio_bounds(s.nominal, 0.95, 1.05);
     return s;
 }
 
 std::vector<Pulse> span_pulses(const int64_t* ev, int64_t nev, int64_t s0, int64_t slen,
                                int64_t min_len, int64_t max_len) {
     std::vector<Pulse> out;
+    out.reserve(512);
     int64_t s1 = s0 + slen;
     const int64_t* lo = std::lower_bound(ev, ev + nev, 2 * s0);
     int64_t cur = -1;
@@ -71,13 +90,32 @@ std::vector<Pulse> span_pulses(const int64_t* ev, int64_t nev, int64_t s0, int64
 
 namespace {
 
-struct Timing { double h0, h1, e0, e1, v0, v1; };
-
 bool in_range(double v, double lo, double hi) { return v >= lo && v <= hi; }
+
+// The integer lengths L with lo <= L <= hi (empty for NaN bounds), so pulse
+// length tests compare integers, with the same outcome as the double test.
+struct LenRange {
+    int64_t lo = 1, hi = 0;
+    bool has(int64_t v) const { return v >= lo && v <= hi; }
+};
+LenRange len_range(double lo, double hi) {
+    LenRange r;
+    if (lo == lo && hi == hi) {
+        r.lo = (int64_t)std::ceil(lo);
+        r.hi = (int64_t)std::floor(hi);
+    }
+    return r;
+}
+
+struct Timing {
+    double h0, h1, e0, e1, v0, v1;
+    LenRange hs, eq, vs, long_hs;   // [h0,h1], [e0,e1], [v0,v1], [h1, 3 h1]
+};
 
 Timing estimate_timing(const SyncParams& sp, const std::vector<Pulse>& raw) {
     double lo = sp.usec(sp.hsync_us - 1.75), hi = sp.usec(sp.hsync_us + 2.0);
     std::vector<double> lens;
+    lens.reserve(raw.size());
     for (const Pulse& p : raw) if (in_range((double)p.len, lo, hi)) lens.push_back((double)p.len);
     double med = lens.empty() ? sp.hsync_us : median(lens);
     double off = med - sp.usec(sp.hsync_us);
@@ -88,27 +126,32 @@ Timing estimate_timing(const SyncParams& sp, const std::vector<Pulse>& raw) {
     t.e1 = sp.usec(sp.eq_us + sp.eq_tol) + off;
     t.v0 = sp.usec(sp.vsync_us * 0.5) + off;
     t.v1 = sp.usec(sp.vsync_us + 1.0) + off;
+    t.hs = len_range(t.h0, t.h1);
+    t.eq = len_range(t.e0, t.e1);
+    t.vs = len_range(t.v0, t.v1);
+    t.long_hs = len_range(t.h1, t.h1 * 3.0);
     return t;
 }
 
 int classify(const Timing& t, int64_t len) {
-    double l = (double)len;
-    if (in_range(l, t.h0, t.h1)) return kHSync;
-    if (in_range(l, t.e0, t.e1)) return kEq;
-    if (in_range(l, t.v0, t.v1)) return kVSync;
+    if (t.hs.has(len)) return kHSync;
+    if (t.eq.has(len)) return kEq;
+    if (t.vs.has(len)) return kVSync;
     return -1;
 }
 
+// (start - prev.start) / nominal within [0.4, 0.6] between two non-hsync
+// pulses, [0.9, 1.1] between two hsyncs, else [0.4, 1.1]
 bool quality(const SyncParams& sp, const CPulse& prev, int kind, int64_t start) {
-    double lo, hi;
-    if (prev.kind != kHSync && kind != kHSync) { lo = 0.4; hi = 0.6; }
-    else if (prev.kind == kHSync && kind == kHSync) { lo = 0.9; hi = 1.1; }
-    else { lo = 0.4; hi = 1.1; }
-    return in_range((double)(start - prev.start) / sp.nominal, lo, hi);
+    const int64_t d = start - prev.start;
+    if (prev.kind != kHSync && kind != kHSync) return sp.half_line.contains(d);
+    if (prev.kind == kHSync && kind == kHSync) return sp.line.contains(d);
+    return sp.mixed.contains(d);
 }
 
 std::vector<CPulse> classify_pulses(const SyncParams& sp, const std::vector<Pulse>& raw, const Timing& t) {
     std::vector<CPulse> out;
+    out.reserve(raw.size());
     for (const Pulse& p : raw) {
         int k = classify(t, p.len);
         if (k < 0) continue;
@@ -143,6 +186,7 @@ std::vector<Pulse> find_pulses_host(const std::vector<double>& d, double high, i
 int read_vblank(const SyncParams& sp, const std::vector<Pulse>& pulses, const Timing& t, int start,
                 int end, std::vector<CPulse>& dest) {
     std::vector<CPulse> valid;
+    valid.reserve((size_t)std::max(0, end - start));
     int state = -1;
     double state_end = 0.0;
     bool has_len = false;
@@ -195,20 +239,20 @@ std::vector<CPulse> refine_pulses(const SyncParams& sp, const std::vector<Pulse>
                                   int64_t span_len, const RefFetch& fetch, double rescue_step) {
     std::vector<Pulse> work = raw;
     std::vector<CPulse> dest;
+    dest.reserve(raw.size() + 32);
     size_t i = 0;
     int64_t mn = std::max<int64_t>(0, (int64_t)std::ceil(sp.usec(sp.eq_us) / 8.0));
     int64_t mx = std::max<int64_t>(1, (int64_t)(sp.nominal * 5.0));
     int rescues = 0;
     while (i < work.size()) {
         const Pulse p = work[i];
-        double l = (double)p.len;
-        if (in_range(l, t.h0, t.h1)) {
+        if (t.hs.has(p.len)) {
             bool ok = !dest.empty() && quality(sp, dest.back(), kHSync, p.start);
             dest.push_back({kHSync, p.start, p.len, ok});
             i++;
             continue;
         }
-        if (fetch && rescue_step > 0.0 && in_range(l, t.h1, t.h1 * 3.0) && rescues < 100000) {
+        if (fetch && rescue_step > 0.0 && t.long_hs.has(p.len) && rescues < 100000) {
             int64_t st = std::min(std::max<int64_t>(p.start, 0), span_len);
             int64_t en = std::min(std::max<int64_t>(p.start + p.len, st), span_len);
             std::optional<Pulse> r;
@@ -226,7 +270,7 @@ std::vector<CPulse> refine_pulses(const SyncParams& sp, const std::vector<Pulse>
             i++;
             continue;
         }
-        bool can = i > 2 && in_range(l, t.e0, t.e1) && !dest.empty() && dest.back().kind == kHSync;
+        bool can = i > 2 && t.eq.has(p.len) && !dest.empty() && dest.back().kind == kHSync;
         if (!can) { i++; continue; }
         int cnt = read_vblank(sp, work, t, (int)i - 2, (int)std::min(work.size(), i + 24), dest);
         if (cnt == 0) { i++; continue; }
@@ -253,8 +297,8 @@ double mean_line_length(const SyncParams& sp, const std::vector<CPulse>& v) {
     double sum = 0.0;
     int cnt = 0;
     for (int i = run_start + 1; i < run_start + run_len; i++) {
-        double ll = (double)(v[(size_t)i].start - v[(size_t)i - 1].start);
-        if (in_range(ll / sp.nominal, 0.95, 1.05)) { sum += ll; cnt++; }
+        const int64_t d = v[(size_t)i].start - v[(size_t)i - 1].start;
+        if (sp.mean_line.contains(d)) { sum += (double)d; cnt++; }
     }
     return cnt > 0 ? sum / cnt : sp.nominal;
 }
@@ -462,8 +506,9 @@ FieldSync analyse_field(const SyncParams& sp, const std::vector<Pulse>& raw, int
         return fail("insufficient data", std::max(pick->line0 - mll * 20.0, sp.nominal));
     // BuildUpstreamLineLocations (SyncAnalysis.cs:551-614)
     std::vector<double> pl;
+    pl.reserve(refined.size());
     for (const CPulse& p : refined) pl.push_back((double)p.start);
-    std::sort(pl.begin(), pl.end());
+    if (!std::is_sorted(pl.begin(), pl.end())) std::sort(pl.begin(), pl.end());
     double ref_pulse = std::trunc(pick->first_hsync);
     int ref_line = (int)pick->fh_line;
     out.locs.assign((size_t)processed, 0.0);

@@ -17,6 +17,14 @@ struct Pulse { int64_t start, len; };
 enum PulseKind { kHSync = 0, kEq = 1, kVSync = 2, kEq2 = 3 };
 struct CPulse { int kind; int64_t start, len; bool in_order; };
 
+// The integers d with lo <= RN(d / n) <= hi, as [lo, hi] (RN(d / n) is
+// monotone in d, so the set is an interval): ratio tests of sample distances
+// without a division, bit-exact to the divided form.
+struct RatioBounds {
+    int64_t lo, hi;
+    bool contains(int64_t d) const { return d >= lo && d <= hi; }
+};
+
 struct SyncParams {
     bool pal;
     double fs, mhz, nominal, line_period_us;
@@ -26,6 +34,8 @@ struct SyncParams {
     double ire0, hz_ire, vsync_ire;
     int output_lines, outlinelen;
     double fsc_mhz;
+    // pulse spacing / nominal line in [0.4, 0.6], [0.9, 1.1], [0.4, 1.1], [0.95, 1.05]
+    RatioBounds half_line, line, mixed, mean_line;
     static SyncParams make(const FormatParams& f, double fs);
     double usec(double us) const { return us * mhz; }
     double ire_to_hz(double ire) const { return ire0 + hz_ire * ire; }

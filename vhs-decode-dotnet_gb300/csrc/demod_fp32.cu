@@ -30,8 +30,10 @@
 //     butterfly that reads the partner CTA's half through DSMEM;
 //   * the time-domain block is held as four 8192-sample chunks, chunks 0 and
 //     2 on rank 0, chunks 1 and 3 on rank 1.
-// Shared memory per CTA: 16384 complex floats (padded against bank
-// conflicts) plus twiddle tables; one CTA per SM.
+// Shared memory per CTA (212 KB, one CTA per SM): 16384 complex floats
+// (padded against bank conflicts), a 16384-float buffer that holds the angles,
+// then the demod, then (S-VHS) the kept spectrum, and in between the next
+// block's RF prefetch; plus twiddle tables.
 #include <cooperative_groups.h>
 #include <atomic>
 #include <climits>
