@@ -160,6 +160,8 @@ void session_init(vhsdecode_gb300_session* s, const vhsdecode_gb300_session_conf
     const int H = kHalf;
     if (s->fp32()) {
         s->v32.alloc(stream_cap); s->s32.alloc(stream_cap); s->e32.alloc(stream_cap);
+        s->sync_cond.alloc((size_t)stream_cap / 32 + 1);
+        s->sync_hold.alloc((size_t)stream_cap / 32 + 1);
         std::vector<float> rv(H);
         std::vector<float2> vv(H), sv(H);
         for (int k = 0; k < H; k++) {
@@ -396,6 +398,8 @@ int tuned_fft_plan(vhsdecode_gb300_session* s, FastDemodParams base) {
     p.rf = rf.p;
     p.first_block = 0;
     p.nblocks = nb;
+    p.sync_cond = nullptr;   // the tuning blocks are not the session's stream
+    p.sync_hold = nullptr;
     p.video_out = v.p;
     p.sync_out = y.p;
     p.env_out = e.p;
@@ -455,6 +459,9 @@ FastDemodParams fp32_params(vhsdecode_gb300_session* s, const int16_t* rf_dev) {
         p.sub.high = s->sub32.p;
     }
     p.fft_plan = s->fft_plan;
+    p.sync_cond = s->sync_cond.p;
+    p.sync_hold = s->sync_hold.p;
+    p.sync_thr = pulse_float_threshold(s->sp.ire_to_hz(s->sp.vsync_ire / 2.0));
     return p;
 }
 
@@ -777,7 +784,6 @@ void enqueue_pipeline(vhsdecode_gb300_session* s, const int16_t* rf, uint64_t n,
     const int nseg = (int)bounds.size() - 1;
     const int16_t* rf_dev = host_input ? s->rf.p : rf;
     FastDemodParams p = fp32_params(s, rf_dev);
-    const double threshold = s->sp.ire_to_hz(s->sp.vsync_ire / 2.0);
     ck(cudaMemsetAsync(s->repair.p, 0, sizeof(int), root), "memset");
     rec(s->alt_start, root, false);
     ck(cudaStreamWaitEvent(s->alt_stream, s->alt_start, 0), "wait");
@@ -811,8 +817,9 @@ void enqueue_pipeline(vhsdecode_gb300_session* s, const int16_t* rf, uint64_t n,
             int64_t* ev = s->seg_events.p + (size_t)k * s->seg_cap;
             int64_t* cnt = (k & 1) ? s->pc_counts_alt.p : s->pc_counts.p;
             int64_t* off = (k & 1) ? s->pc_offsets_alt.p : s->pc_offsets.p;
-            ck(launch_pulse_events_range<float>(s->s32.p, b0 * kStride, b1 * kStride, threshold, cnt, off, ev,
-                                                s->seg_cap, s->seg_total.p + k, ks), "pulse launch");
+            // from the pulse-scan bits the demod wrote with the sync stream
+            ck(launch_pulse_bits_range(s->sync_cond.p, s->sync_hold.p, b0 * kStride, b1 * kStride, cnt, off, ev,
+                                       s->seg_cap, s->seg_total.p + k, ks), "pulse launch");
             rec(s->seg_pulsed[(size_t)k], ks, false);
             ck(cudaStreamWaitEvent(s->d2h_stream, s->seg_pulsed[(size_t)k], 0), "wait");
             ck(cudaMemcpyAsync(s->h_totals + k, s->seg_total.p + k, sizeof(int64_t), cudaMemcpyDeviceToHost,

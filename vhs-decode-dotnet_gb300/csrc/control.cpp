@@ -156,7 +156,7 @@ std::vector<CPulse> classify_pulses(const SyncParams& sp, const std::vector<Puls
         int k = classify(t, p.len);
         if (k < 0) continue;
         bool ok = !out.empty() && quality(sp, out.back(), k, p.start);
-        out.push_back({k, p.start, p.len, ok});
+        out.push_back({p.start, p.len, k, ok});
     }
     return out;
 }
@@ -224,7 +224,7 @@ int read_vblank(const SyncParams& sp, const std::vector<Pulse>& pulses, const Ti
         }
         if (acc >= 0) {
             bool ok = !valid.empty() && quality(sp, valid.back(), acc, p.start);
-            valid.push_back({acc, p.start, p.len, ok});
+            valid.push_back({p.start, p.len, acc, ok});
             state = acc;
         }
         if (done) {
@@ -248,7 +248,7 @@ std::vector<CPulse> refine_pulses(const SyncParams& sp, const std::vector<Pulse>
         const Pulse p = work[i];
         if (t.hs.has(p.len)) {
             bool ok = !dest.empty() && quality(sp, dest.back(), kHSync, p.start);
-            dest.push_back({kHSync, p.start, p.len, ok});
+            dest.push_back({p.start, p.len, kHSync, ok});
             i++;
             continue;
         }
@@ -380,10 +380,18 @@ std::optional<Est> finalize(const std::vector<CPulse>& pulses, const Acc& acc, d
     double fh = round_away((acc.loc_sum + acc.off_sum) / acc.count);
     double off = 0.0;
     int cnt = 0;
+    const double inv = 1.0 / mll;
     for (const CPulse& p : pulses) {
         if (p.kind != kHSync || !p.in_order) continue;
-        double line = (((double)p.start - fh) / mll) + fh_line;
-        int rl = (int)round_away(line);
+        // round_away(((start - fh) / mll) + fh_line): a pulse sits near a
+        // whole line, so the product with 1/mll (a few ulp off the quotient)
+        // rounds the same unless it lands near a half-line, where the exact
+        // division decides
+        double approx = (((double)p.start - fh) * inv) + fh_line;
+        double nearest = round_away(approx);
+        int rl = (int)(std::fabs(approx - nearest) < 0.49
+                           ? nearest
+                           : round_away((((double)p.start - fh) / mll) + fh_line));
         if (rl > field_lines) break;
         if (rl >= fh_line) {
             off += fh + mll * (rl - fh_line) - (double)p.start;

@@ -15,7 +15,7 @@ namespace vhsd {
 
 struct Pulse { int64_t start, len; };
 enum PulseKind { kHSync = 0, kEq = 1, kVSync = 2, kEq2 = 3 };
-struct CPulse { int kind; int64_t start, len; bool in_order; };
+struct CPulse { int64_t start, len; int kind; bool in_order; };
 
 // The integers d with lo <= RN(d / n) <= hi, as [lo, hi] (RN(d / n) is
 // monotone in d, so the set is an interval): ratio tests of sample distances

@@ -508,6 +508,40 @@ __device__ __noinline__ void repair_block(Shared& sh, Shared* rsh, const FastDem
     __syncthreads();
 }
 
+// Bits 0..15 of x to the even bit positions of the result.
+__device__ __forceinline__ unsigned spread16(unsigned x) {
+    x &= 0xffffu;
+    x = (x | (x << 8)) & 0x00ff00ffu;
+    x = (x | (x << 4)) & 0x0f0f0f0fu;
+    x = (x | (x << 2)) & 0x33333333u;
+    x = (x | (x << 1)) & 0x55555555u;
+    return x;
+}
+
+// Pulse-scan bits of the sync reference samples base + 2 lane and base +
+// 2 lane + 1 (q.x, q.y) held by the 32 lanes of a warp: condition (v <= the
+// exact float threshold of the pulse scan) and hold (NaN) words for stream
+// samples [sbase + base, sbase + base + 64), written where the word lies in
+// the kept range.  Called by all 32 lanes.
+__device__ __forceinline__ void sync_bits(float2 q, int base, int64_t sbase, const FastDemodParams& p,
+                                          int lane) {
+    const unsigned ce = __ballot_sync(0xffffffffu, q.x <= p.sync_thr);
+    const unsigned co = __ballot_sync(0xffffffffu, q.y <= p.sync_thr);
+    const unsigned he = __ballot_sync(0xffffffffu, q.x != q.x);
+    const unsigned ho = __ballot_sync(0xffffffffu, q.y != q.y);
+    if (lane < 2) {
+        const int n = base + 32 * lane;   // first block sample of this lane's word
+        if (n >= CUT + 32 && n + 32 <= CUT + 32 + S) {
+            const int sh = 16 * lane;
+            const unsigned c = spread16(ce >> sh) | (spread16(co >> sh) << 1);
+            const unsigned h = spread16(he >> sh) | (spread16(ho >> sh) << 1);
+            const int64_t w = (sbase + n) >> 5;
+            p.sync_cond[w] = c;
+            p.sync_hold[w] = h;
+        }
+    }
+}
+
 // Next block's RF (32768 int16 = 64 KB, both halves) into `dst` with
 // asynchronous 16-byte copies (8 per thread), overlapping the current block's
 // later stages; prefetch_wait() + a barrier make it visible.
@@ -781,10 +815,18 @@ vhsd_demod_fp32_kernel(FastDemodParams p) {
                         if (n2 >= CUT && n2 < CUT + S)
                             *reinterpret_cast<float2*>(vout + n2) = make_float2(p2.x + dcv, p2.y + dcv);
                     } else {
-                        if (n1 >= CUT + 32 && n1 < CUT + 32 + S)
-                            *reinterpret_cast<float2*>(sout + n1) = make_float2(p1.x + dcs, p1.y + dcs);
-                        if (n2 >= CUT + 32 && n2 < CUT + 32 + S)
-                            *reinterpret_cast<float2*>(sout + n2) = make_float2(p2.x + dcs, p2.y + dcs);
+                        const float2 q1 = make_float2(p1.x + dcs, p1.y + dcs);
+                        const float2 q2 = make_float2(p2.x + dcs, p2.y + dcs);
+                        if (n1 >= CUT + 32 && n1 < CUT + 32 + S) *reinterpret_cast<float2*>(sout + n1) = q1;
+                        if (n2 >= CUT + 32 && n2 < CUT + 32 + S) *reinterpret_cast<float2*>(sout + n2) = q2;
+                        if (p.sync_cond) {
+                            // the pulse scan's inputs as bits: v <= threshold and
+                            // NaN, for the warp's 64 consecutive samples of each half
+                            const int64_t sbase = (blk + p.first_block) * (int64_t)S - CUT - 32;
+                            const int base1 = 2 * (m - lane);
+                            sync_bits(q1, base1, sbase, p, lane);
+                            sync_bits(q2, base1 + 16384, sbase, p, lane);
+                        }
                     }
                 }
             }

@@ -71,56 +71,16 @@ __device__ __forceinline__ unsigned edge_bits(unsigned cond, unsigned hold, unsi
 // is its CTA's offset plus the counts of the warps before it in the CTA, and
 // it writes its events in order.  offsets layout: [0] ticket (zeroed before
 // pass 0), [1, 1 + nchunks) CTA offsets, [1 + nchunks, 1 + 2 nchunks) CTA sums.
-template <typename T, bool WRITE>
-__global__ void __launch_bounds__(kPT) k_pulse_pass(const T* __restrict__ ref, int64_t begin, int64_t n,
-                                                    Cmp<T> cmp, int64_t* counts, int64_t* offsets,
-                                                    int64_t* events, int64_t capacity, int64_t* total,
-                                                    int64_t nchunks) {
+// Pass-0 tail shared by the float and the bit scans: each warp's count to
+// counts[warp], the CTA's sum to offsets[1 + nchunks + CTA]; the CTA that
+// takes the last ticket scans the CTA sums into offsets[1 .. 1 + nchunks) and
+// the total.  Called by every thread of the CTA (cnt valid on lane 0).
+__device__ __forceinline__ void finish_counts(int64_t cnt, int64_t wg, int64_t* counts, int64_t* offsets,
+                                              int64_t* total, int64_t nchunks) {
     constexpr int kWarps = kPT / 32;
     __shared__ int64_t wcnt[kWarps];
     __shared__ bool last;
     const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
-    const int64_t wg = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int64_t start = begin + wg * kPWarpSamples;
-    int64_t cnt = 0;
-    if (start < n) {
-        unsigned st = 0u;
-        if (lane == 0) st = state_before(ref, start, cmp.h) ? 1u : 0u;
-        st = __shfl_sync(0xffffffffu, st, 0);
-        int64_t off = 0;
-        if (WRITE) {
-            off = offsets[1 + blockIdx.x];
-            for (int k = 0; k < wl; k++) off += counts[(int64_t)blockIdx.x * kWarps + k];
-        }
-        // eight loads in flight per lane, then the ballots in order
-        for (int it0 = 0; it0 < kPWarpSamples / 32; it0 += 8) {
-            T vv[8];
-#pragma unroll
-            for (int j = 0; j < 8; j++) {
-                int64_t p = start + (it0 + j) * 32 + lane;
-                vv[j] = p < n ? ref[p] : (T)0;
-            }
-#pragma unroll
-            for (int j = 0; j < 8; j++) {
-                int64_t p = start + (it0 + j) * 32 + lane;
-                bool inb = p < n;
-                T v = vv[j];
-                bool hold = !inb || !(v == v);
-                bool c = inb && (v <= cmp.h);
-                unsigned cm = __ballot_sync(0xffffffffu, c);
-                unsigned hm = __ballot_sync(0xffffffffu, hold);
-                unsigned e = edge_bits(cm, hm, st);
-                if (WRITE && ((e >> lane) & 1u)) {
-                    int64_t o = off + __popc(e & ((1u << lane) - 1u));
-                    if (o < capacity) events[o] = 2 * p + (c ? 0 : 1);
-                }
-                int pc = __popc(e);
-                off += pc;
-                cnt += pc;
-            }
-        }
-    }
-    if (WRITE) return;
     if (lane == 0) {
         counts[wg] = cnt;
         wcnt[wl] = cnt;
@@ -165,7 +125,148 @@ __global__ void __launch_bounds__(kPT) k_pulse_pass(const T* __restrict__ ref, i
     if (threadIdx.x == 0) total[0] = carry;
 }
 
+template <typename T, bool WRITE>
+__global__ void __launch_bounds__(kPT) k_pulse_pass(const T* __restrict__ ref, int64_t begin, int64_t n,
+                                                    Cmp<T> cmp, int64_t* counts, int64_t* offsets,
+                                                    int64_t* events, int64_t capacity, int64_t* total,
+                                                    int64_t nchunks) {
+    constexpr int kWarps = kPT / 32;
+    const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
+    const int64_t wg = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t start = begin + wg * kPWarpSamples;
+    int64_t cnt = 0;
+    if (start < n) {
+        unsigned st = 0u;
+        if (lane == 0) st = state_before(ref, start, cmp.h) ? 1u : 0u;
+        st = __shfl_sync(0xffffffffu, st, 0);
+        int64_t off = 0;
+        if (WRITE) {
+            off = offsets[1 + blockIdx.x];
+            for (int k = 0; k < wl; k++) off += counts[(int64_t)blockIdx.x * kWarps + k];
+        }
+        // eight loads in flight per lane, then the ballots in order
+        for (int it0 = 0; it0 < kPWarpSamples / 32; it0 += 8) {
+            T vv[8];
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                int64_t p = start + (it0 + j) * 32 + lane;
+                vv[j] = p < n ? ref[p] : (T)0;
+            }
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                int64_t p = start + (it0 + j) * 32 + lane;
+                bool inb = p < n;
+                T v = vv[j];
+                bool hold = !inb || !(v == v);
+                bool c = inb && (v <= cmp.h);
+                unsigned cm = __ballot_sync(0xffffffffu, c);
+                unsigned hm = __ballot_sync(0xffffffffu, hold);
+                unsigned e = edge_bits(cm, hm, st);
+                if (WRITE && ((e >> lane) & 1u)) {
+                    int64_t o = off + __popc(e & ((1u << lane) - 1u));
+                    if (o < capacity) events[o] = 2 * p + (c ? 0 : 1);
+                }
+                int pc = __popc(e);
+                off += pc;
+                cnt += pc;
+            }
+        }
+    }
+    if (WRITE) return;
+    finish_counts(cnt, wg, counts, offsets, total, nchunks);
+}
+
+// The same two passes over the pulse-scan bits the fused demodulator writes
+// (cond: v <= threshold, hold: NaN; 32 stream samples per word, [begin, n)
+// word-aligned): a warp's 32 lanes take its 32 words; the state entering each
+// word is that of the last non-NaN sample before it (the warp's entering state
+// from the words before `start`, walked back like state_before), found with a
+// ballot of the words holding a non-NaN sample.
+__device__ __forceinline__ bool bits_state_before(const unsigned* cond, const unsigned* hold, int64_t p0) {
+    for (int64_t w = (p0 >> 5) - 1; w >= 0; w--) {
+        const unsigned h = hold[w];
+        if (h != 0xffffffffu) {
+            const int b = 31 - __clz(~h);
+            return (cond[w] >> b) & 1u;
+        }
+    }
+    return false;
+}
+
+template <bool WRITE>
+__global__ void __launch_bounds__(kPT) k_pulse_bits(const unsigned* __restrict__ cond,
+                                                    const unsigned* __restrict__ hold, int64_t begin, int64_t n,
+                                                    int64_t* counts, int64_t* offsets, int64_t* events,
+                                                    int64_t capacity, int64_t* total, int64_t nchunks) {
+    constexpr int kWarps = kPT / 32;
+    const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
+    const int64_t wg = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t start = begin + wg * kPWarpSamples;
+    int64_t cnt = 0;
+    if (start < n) {
+        unsigned st0 = 0u;
+        if (lane == 0) st0 = bits_state_before(cond, hold, start) ? 1u : 0u;
+        st0 = __shfl_sync(0xffffffffu, st0, 0);
+        const int64_t p0 = start + 32 * lane;   // first sample of this lane's word
+        const bool inb = p0 < n;
+        const unsigned c = inb ? cond[p0 >> 5] : 0u;
+        const unsigned h = inb ? hold[p0 >> 5] : 0xffffffffu;
+        const bool has = h != 0xffffffffu;
+        const unsigned last = has ? (c >> (31 - __clz(~h))) & 1u : 0u;
+        const unsigned hm = __ballot_sync(0xffffffffu, has);
+        const unsigned before = hm & ((1u << lane) - 1u);
+        const int src = before ? 31 - __clz(before) : 0;
+        const unsigned from = __shfl_sync(0xffffffffu, last, src);
+        unsigned st = before ? from : st0;
+        const unsigned e = edge_bits(c, h, st);
+        const int pc = __popc(e);
+        int incl = pc;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        cnt = __shfl_sync(0xffffffffu, incl, 31);
+        if (WRITE) {
+            int64_t off = offsets[1 + blockIdx.x];
+            for (int k = 0; k < wl; k++) off += counts[(int64_t)blockIdx.x * kWarps + k];
+            off += incl - pc;
+            unsigned m = e;
+            while (m) {
+                const int b = __ffs(m) - 1;
+                m &= m - 1;
+                const int64_t p = p0 + b;
+                if (off < capacity) events[off] = 2 * p + (((c >> b) & 1u) ? 0 : 1);
+                off++;
+            }
+        }
+    }
+    if (WRITE) return;
+    finish_counts(cnt, wg, counts, offsets, total, nchunks);
+}
+
 }  // namespace
+
+float pulse_float_threshold(double high) { return make_cmp<float>(high).h; }
+
+cudaError_t launch_pulse_bits_range(const unsigned* cond, const unsigned* hold, int64_t begin, int64_t end,
+                                    int64_t* counts, int64_t* offsets, int64_t* events, int64_t capacity,
+                                    int64_t* total, cudaStream_t s) {
+    if ((begin & 31) != 0 || (end & 31) != 0) return cudaErrorInvalidValue;
+    int64_t len = end > begin ? end - begin : 0;
+    int64_t nchunks = (len + kPulseChunk - 1) / kPulseChunk;
+    if (nchunks == 0) {
+        cudaMemsetAsync(total, 0, sizeof(int64_t), s);
+        return cudaGetLastError();
+    }
+    cudaError_t e = cudaMemsetAsync(offsets, 0, sizeof(int64_t), s);   // the last-CTA ticket
+    if (e != cudaSuccess) return e;
+    k_pulse_bits<false><<<(unsigned)nchunks, kPT, 0, s>>>(cond, hold, begin, end, counts, offsets, nullptr, 0,
+                                                         total, nchunks);
+    k_pulse_bits<true><<<(unsigned)nchunks, kPT, 0, s>>>(cond, hold, begin, end, counts, offsets, events,
+                                                        capacity, total, nchunks);
+    return cudaGetLastError();
+}
 
 template <typename T>
 cudaError_t launch_pulse_events_range(const T* ref, int64_t begin, int64_t end, double high,

@@ -49,6 +49,11 @@ struct FastDemodParams {
     int* repair_count;         // counts blocks that took the spike-repair path
     SubDeemph sub;             // sub-deemphasis (sub.high == nullptr: off)
     int fft_plan;              // radix plans: bits 0-1 the 8192-point, bits 2-3 the 16384-point transform
+    // optional pulse-scan bits of the sync stream (one bit per stream sample,
+    // 32 per word): v <= sync_thr, and NaN (hold); null: not written
+    unsigned* sync_cond;
+    unsigned* sync_hold;
+    float sync_thr;
 };
 // Radix plans the fused kernel is compiled for (8192-point plan | 16384-point
 // plan << 2): 16x16x32 | 16x32x32, 32x16x16 | 16x32x32, 16x16x32 | 32x32x16,
@@ -100,6 +105,13 @@ cudaError_t launch_pulse_events(const T* ref, int64_t n, double high, int64_t* c
 // Same over stream positions [begin, end) of `ref`; the state entering `begin`
 // is taken from the samples before it, so consecutive ranges give exactly the
 // events of one pass over their union.  Scratch holds pulse_count_slots(end - begin).
+// Same events from the pulse-scan bits of FastDemodParams (cond: v <= the
+// exact float threshold, hold: NaN), [begin, end) multiples of 32.
+cudaError_t launch_pulse_bits_range(const unsigned* cond, const unsigned* hold, int64_t begin, int64_t end,
+                                    int64_t* counts, int64_t* offsets_scratch, int64_t* events,
+                                    int64_t capacity, int64_t* total, cudaStream_t stream);
+// Exact float threshold of a double pulse threshold: v <= high <=> v <= it.
+float pulse_float_threshold(double high);
 template <typename T>
 cudaError_t launch_pulse_events_range(const T* ref, int64_t begin, int64_t end, double high,
                                       int64_t* counts, int64_t* offsets_scratch, int64_t* events,

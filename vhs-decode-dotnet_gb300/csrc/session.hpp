@@ -134,6 +134,7 @@ struct vhsdecode_gb300_session {
     // device data
     DevBuf<int16_t> rf;
     DevBuf<float> v32, s32, e32;
+    DevBuf<unsigned> sync_cond, sync_hold;   // pulse-scan bits of s32 (FP32 path)
     DevBuf<double> v64, s64, e64;
     DevBuf<float> rfv32;
     DevBuf<float2> vid32, syn32, sub32, tw_hi, tw_lo;
