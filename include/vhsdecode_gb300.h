@@ -34,7 +34,7 @@
 #  define VHSDECODE_GB300_CALL
 #endif
 
-#define VHSDECODE_GB300_ABI_VERSION 0x00010002u
+#define VHSDECODE_GB300_ABI_VERSION 0x00010003u
 #define VHSDECODE_GB300_NAME_CAPACITY 128u
 
 #ifdef __cplusplus
@@ -89,9 +89,11 @@ typedef enum vhsdecode_gb300_precision {
 } vhsdecode_gb300_precision;
 
 /* Callbacks: shapes of vhsdecode_cuda_fast_read_callback / cancel_callback (:55-62).
- * read: copy up to sample_count int16 samples starting at sample_offset into
- * destination and return the count; a short count means end of input, 0 means
- * end of input or failure. cancel: return nonzero to cancel. */
+ * read: copy up to sample_count samples (int16, or float for input format
+ * FLOAT32) starting at sample_offset into destination and return the count; a
+ * short count means end of input, 0 means end of input or failure.  Offsets and
+ * counts are source samples (before any device decimation). cancel: return
+ * nonzero to cancel. */
 typedef size_t (VHSDECODE_GB300_CALL *vhsdecode_gb300_read_callback)(
     void* user_data, void* destination, uint64_t sample_offset, size_t sample_count);
 typedef int32_t (VHSDECODE_GB300_CALL *vhsdecode_gb300_cancel_callback)(void* user_data);
@@ -115,13 +117,13 @@ typedef struct vhsdecode_gb300_config_v1 {
     uint32_t profile;
     uint32_t tape_speed;
     int32_t device_id;
-    double sample_rate_mhz;
-    uint64_t total_samples;
+    double sample_rate_mhz;     /* decode rate (the source runs at factor x this) */
+    uint64_t total_samples;     /* source samples */
     const char* output_base_utf8;
     int32_t overwrite;
     uint32_t input_sample_format;
     uint32_t maximum_output_fields;
-    uint32_t device_decimation_factor;
+    uint32_t device_decimation_factor;  /* 1, or 2: 2:1 half-band FIR on the device */
     vhsdecode_gb300_read_callback read_callback;
     vhsdecode_gb300_cancel_callback cancel_callback;
     void* user_data;
@@ -170,12 +172,16 @@ typedef struct vhsdecode_gb300_session_config_v1 {
     uint32_t precision;         /* vhsdecode_gb300_precision */
     uint32_t max_fields;        /* 0 = derived from max_samples */
     uint32_t tape_format;       /* vhsdecode_gb300_tape_format */
-    uint32_t reserved;
+    uint32_t decimation;        /* 0 or 1: none.  2: decode's samples are at twice
+                                   sample_rate_mhz and pass the device 2:1 half-band
+                                   decimator first (config_v1.device_decimation_factor);
+                                   max_samples counts them */
 } vhsdecode_gb300_session_config_v1;
 
 /* flags for vhsdecode_gb300_session_decode */
 #define VHSDECODE_GB300_DECODE_DEVICE_INPUT 0x1u /* rf is a device pointer (16-byte aligned) */
 #define VHSDECODE_GB300_DECODE_DEMOD_ONLY   0x2u /* stop after the block demodulator */
+#define VHSDECODE_GB300_DECODE_FLOAT_INPUT  0x4u /* rf holds float samples (input format FLOAT32) */
 
 typedef struct vhsdecode_gb300_decode_result_v1 {
     uint32_t struct_size;
@@ -245,9 +251,10 @@ VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_session_set_str
     vhsdecode_gb300_session* session, void* cuda_stream);
 
 /* Decode one capture/window (counterpart of
- * vhsdecode_cuda_fast_preview_decode_window, :292-295).  rf is int16. */
+ * vhsdecode_cuda_fast_preview_decode_window, :292-295).  rf holds int16
+ * samples, or float ones with VHSDECODE_GB300_DECODE_FLOAT_INPUT. */
 VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_session_decode(
-    vhsdecode_gb300_session* session, const int16_t* rf, uint64_t sample_count,
+    vhsdecode_gb300_session* session, const void* rf, uint64_t sample_count,
     uint32_t max_fields, uint32_t flags, vhsdecode_gb300_decode_result_v1* result);
 
 VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_session_get_field(
@@ -326,6 +333,14 @@ VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_replace_spikes(
 /* Device polynomial atan2 (the FM demodulator's angle) for n float pairs. */
 VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_vhs_angles(
     const float* real, const float* imaginary, uint64_t n, float* angles);
+
+/* Device 2:1 decimation of a whole host capture (cuda_fast_read_upload_half_rate,
+ * src/VHSDecode.CudaFast.Native/include/cuda_fast_decimator.h:27-36, over one
+ * window covering the capture): source_count int16 (input_sample_format 1) or
+ * float (0) samples in, source_count / 2 float samples out, sample i the
+ * half-band FIR centred on source sample 2 i with zeros outside the capture. */
+VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_decimate_half_rate(
+    const void* source, uint32_t input_sample_format, uint64_t source_count, float* destination);
 
 /* ---------------------------------------------------------------- serving
  * Window server: continuous batching of decode windows from many client

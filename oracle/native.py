@@ -51,6 +51,8 @@ def lib():
                                            ctypes.c_double, ctypes.c_int64, ctypes.c_int64, _i64p,
                                            _i64p, ctypes.c_int64]
         L.oracle_find_dropouts.restype = ctypes.c_int64
+        L.oracle_decimate_half_s16.argtypes = [ctypes.POINTER(ctypes.c_int16), ctypes.c_int64, _fp]
+        L.oracle_decimate_half_f32.argtypes = [_fp, ctypes.c_int64, _fp]
         _lib = L
     return _lib
 
@@ -147,3 +149,17 @@ def sinc_lut():
         lib().oracle_build_sinc_lut(ptr(lut, _fp))
         _LUT = lut
     return _LUT
+
+
+def decimate_half(src):
+    """2:1 half-band decimation (cuda-fast 20-MSPS reader mode) of an int16 or
+    float32 capture: len(src) // 2 float32 samples."""
+    src = np.ascontiguousarray(src)
+    out = np.zeros(len(src) // 2, np.float32)
+    if src.dtype == np.int16:
+        lib().oracle_decimate_half_s16(ptr(src, ctypes.POINTER(ctypes.c_int16)), len(src), ptr(out, _fp))
+    elif src.dtype == np.float32:
+        lib().oracle_decimate_half_f32(ptr(src, _fp), len(src), ptr(out, _fp))
+    else:
+        raise TypeError("int16 or float32 capture expected")
+    return out

@@ -339,3 +339,45 @@ int64_t oracle_find_dropouts(const double *env, int64_t start, int64_t end, doub
     }
     return k;
 }
+
+/* 2:1 decimation of the cuda-fast reader's 20-MSPS mode
+ * (src/VHSDecode.CudaFast.Native/src/cuda_fast_decimator.cu:27-64, window
+ * :67-100 over one window that covers the capture): y[i] is the half-band FIR
+ * centred on source sample 2 i, sources outside [0, n) read as zero, n / 2
+ * outputs.  The reference's `value += c * (a + b)` runs on the GPU, where
+ * nvcc's default -fmad=true contracts it: the oracle writes that fused
+ * multiply-add out with fmaf.  The filter table is the reference's. */
+static const float half_band[8] = {
+    0.5000046374907835f,    0.3126333216205309f,    -0.09010692207961689f,  0.040107417651266825f,
+    -0.017917030421899405f, 0.007100857132041433f,  -0.0022302855185240434f, 0.00041032287080936366f};
+
+static float dec_at_s16(const int16_t *x, int64_t n, int64_t g) { return (g >= 0 && g < n) ? (float)x[g] : 0.0f; }
+static float dec_at_f32(const float *x, int64_t n, int64_t g) { return (g >= 0 && g < n) ? x[g] : 0.0f; }
+
+void oracle_decimate_half_s16(const int16_t *x, int64_t n, float *out)
+{
+    for (int64_t i = 0; i < n / 2; i++) {
+        int64_t c = 2 * i;
+        float v = half_band[0] * dec_at_s16(x, n, c);
+        for (int t = 1; t < 8; t++) {
+            int64_t o = 2 * t - 1;
+            float pair = dec_at_s16(x, n, c - o) + dec_at_s16(x, n, c + o);
+            v = fmaf(half_band[t], pair, v);
+        }
+        out[i] = v;
+    }
+}
+
+void oracle_decimate_half_f32(const float *x, int64_t n, float *out)
+{
+    for (int64_t i = 0; i < n / 2; i++) {
+        int64_t c = 2 * i;
+        float v = half_band[0] * dec_at_f32(x, n, c);
+        for (int t = 1; t < 8; t++) {
+            int64_t o = 2 * t - 1;
+            float pair = dec_at_f32(x, n, c - o) + dec_at_f32(x, n, c + o);
+            v = fmaf(half_band[t], pair, v);
+        }
+        out[i] = v;
+    }
+}

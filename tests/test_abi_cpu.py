@@ -73,24 +73,43 @@ def test_null_pointer_status(lib):
 
 
 def test_run_rejects_unsupported_options(lib):
+    # vhsdecode_cuda_fast.cpp:255-275: input format FLOAT32 or INT16,
+    # decimation factor 1 or 2 (2 with a decode rate the source halves to)
     from vhsd_gb300 import native
     cfg = native.RunConfig()
     cfg.struct_size = ctypes.sizeof(cfg)
     cfg.profile = native.PROFILE_PAL
     cfg.sample_rate_mhz = 40.0
     cfg.output_base_utf8 = b"/tmp/x"
-    cfg.input_sample_format = native.INPUT_FLOAT32
+    cfg.input_sample_format = 2
     cfg.device_decimation_factor = 1
     cfg.read_callback = native.READ_CB(lambda u, d, o, c: 0)
     res = native.RunResult()
     res.struct_size = ctypes.sizeof(res)
-    assert lib.vhsdecode_gb300_run(ctypes.byref(cfg), ctypes.byref(res)) == native.STATUS_INVALID_ARGUMENT
+
+    def run():
+        return lib.vhsdecode_gb300_run(ctypes.byref(cfg), ctypes.byref(res))
+    assert run() == native.STATUS_INVALID_ARGUMENT
     cfg.input_sample_format = native.INPUT_INT16
+    cfg.device_decimation_factor = 3
+    assert run() == native.STATUS_INVALID_ARGUMENT
     cfg.device_decimation_factor = 2
-    assert lib.vhsdecode_gb300_run(ctypes.byref(cfg), ctypes.byref(res)) == native.STATUS_INVALID_ARGUMENT
-    cfg.device_decimation_factor = 1
+    cfg.sample_rate_mhz = 60.0
+    assert run() == native.STATUS_INVALID_ARGUMENT
+    # accepted options reach the read: an empty capture is an input error
+    for fmt, factor, mhz in [(native.INPUT_FLOAT32, 1, 40.0), (native.INPUT_INT16, 2, 20.0),
+                             (native.INPUT_FLOAT32, 2, 20.0)]:
+        cfg.input_sample_format, cfg.device_decimation_factor, cfg.sample_rate_mhz = fmt, factor, mhz
+        assert run() == native.STATUS_INPUT_ERROR
     cfg.struct_size = 8
-    assert lib.vhsdecode_gb300_run(ctypes.byref(cfg), ctypes.byref(res)) == native.STATUS_INVALID_ARGUMENT
+    assert run() == native.STATUS_INVALID_ARGUMENT
+
+
+def test_session_rejects_bad_decimation(lib):
+    from vhsd_gb300 import native
+    with pytest.raises(native.NativeError) as e:
+        native.Session(native.PROFILE_NTSC, 1 << 20, sample_rate_mhz=20.0, decimation=3)
+    assert e.value.status in (native.STATUS_INVALID_ARGUMENT, native.STATUS_CUDA_UNAVAILABLE)
 
 
 @pytest.mark.parametrize("system,tape", [("PAL", "VHS"), ("NTSC", "VHS"), ("PAL", "SVHS"),

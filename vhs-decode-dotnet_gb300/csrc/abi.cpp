@@ -120,6 +120,8 @@ void session_init(vhsdecode_gb300_session* s, const vhsdecode_gb300_session_conf
     if (!(c.sample_rate_mhz >= 10.0 && c.sample_rate_mhz <= 100.0))
         throw Failure(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "sample_rate_mhz must be within 10..100");
     if (c.precision > 1) throw Failure(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "unknown precision");
+    if (c.decimation > 2) throw Failure(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "decimation must be 0, 1 or 2");
+    s->decim = c.decimation == 2 ? 2 : 1;
     s->fs = c.sample_rate_mhz * 1e6;
     s->precision = (int)c.precision;
     s->device = c.device_id;
@@ -147,11 +149,14 @@ void session_init(vhsdecode_gb300_session* s, const vhsdecode_gb300_session_conf
     ck(cudaStreamCreateWithFlags(&s->aux_stream, cudaStreamNonBlocking), "cudaStreamCreate");
     ck(cudaStreamCreateWithFlags(&s->field_stream, cudaStreamNonBlocking), "cudaStreamCreate");
     ck(cudaEventCreateWithFlags(&s->field_end, cudaEventDisableTiming), "cudaEventCreate");
+    ck(cudaStreamCreateWithFlags(&s->drop_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    for (cudaEvent_t* e : {&s->drop_fork, &s->drop_hsync, &s->drop_join})
+        ck(cudaEventCreateWithFlags(e, cudaEventDisableTiming), "cudaEventCreate");
     for (auto& e : s->stage_ev) ck(cudaEventCreate(&e), "cudaEventCreate");
     s->stage_timing = std::getenv("VHSD_STAGE_TIMING") != nullptr;
     s->stream = s->own_stream;
     for (auto& ev : s->ev) ck(cudaEventCreate(&ev), "cudaEventCreate");
-    s->max_blocks = block_count(c.max_samples);
+    s->max_blocks = block_count(c.max_samples / (uint64_t)s->decim);
     int64_t stream_cap = std::max<int64_t>(1, s->max_blocks) * kStride;
     double field_samples = s->fs / (2.0 * s->fmt.fps);
     s->max_fields = c.max_fields ? (int)c.max_fields
@@ -329,6 +334,9 @@ void session_free(vhsdecode_gb300_session* s) {
     if (s->aux_stream) cudaStreamDestroy(s->aux_stream);
     if (s->field_stream) cudaStreamDestroy(s->field_stream);
     if (s->field_end) cudaEventDestroy(s->field_end);
+    if (s->drop_stream) cudaStreamDestroy(s->drop_stream);
+    for (cudaEvent_t e : {s->drop_fork, s->drop_hsync, s->drop_join})
+        if (e) cudaEventDestroy(e);
     for (auto& e : s->stage_ev) if (e) cudaEventDestroy(e);
     if (s->own_stream) cudaStreamDestroy(s->own_stream);
 }
@@ -396,6 +404,7 @@ int tuned_fft_plan(vhsdecode_gb300_session* s, FastDemodParams base) {
     ck(cudaEventCreate(&e1), "cudaEventCreate");
     FastDemodParams p = base;
     p.rf = rf.p;
+    p.rf_f32 = nullptr;
     p.first_block = 0;
     p.nblocks = nb;
     p.sync_cond = nullptr;   // the tuning blocks are not the session's stream
@@ -459,6 +468,8 @@ FastDemodParams fp32_params(vhsdecode_gb300_session* s, const int16_t* rf_dev) {
         p.sub.high = s->sub32.p;
     }
     p.fft_plan = s->fft_plan;
+    p.rf_f32 = s->in_f32;
+    if (s->in_f32) p.rf = nullptr;
     p.sync_cond = s->sync_cond.p;
     p.sync_hold = s->sync_hold.p;
     p.sync_thr = pulse_float_threshold(s->sp.ire_to_hz(s->sp.vsync_ire / 2.0));
@@ -474,7 +485,8 @@ void run_demod(vhsdecode_gb300_session* s, const int16_t* rf_dev, int64_t nblock
         ck(launch_demod_fp32(p, s->num_sms / 2, s->stream), "demod fp32 launch");
     } else {
         PlainDemodParams p{};
-        p.rf = rf_dev;
+        p.rf = s->in_f32 ? nullptr : rf_dev;
+        p.rf_f32 = s->in_f32;
         p.rf_video = s->rfv64.p;
         p.video = s->vid64.p;
         p.sync = s->syn64.p;
@@ -498,7 +510,7 @@ void run_demod(vhsdecode_gb300_session* s, const int16_t* rf_dev, int64_t nblock
         }
         // The capture lives in s->rf or a caller buffer; the graph bakes the
         // pointer, so rebuild it when the input pointer changes.
-        if (!s->plain_graph || s->graph_rf != rf_dev) {
+        if (!s->plain_graph || s->graph_rf != p.rf || s->graph_rf32 != p.rf_f32) {
             if (s->plain_graph) { cudaGraphExecDestroy(s->plain_graph); s->plain_graph = nullptr; }
             cudaStream_t cs;
             ck(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "stream");
@@ -511,7 +523,8 @@ void run_demod(vhsdecode_gb300_session* s, const int16_t* rf_dev, int64_t nblock
             ck(ce, "end capture");
             ck(cudaGraphInstantiate(&s->plain_graph, g, 0), "graph instantiate");
             cudaGraphDestroy(g);
-            s->graph_rf = rf_dev;
+            s->graph_rf = p.rf;
+            s->graph_rf32 = p.rf_f32;
         }
         int64_t zero = 0;
         ck(cudaMemcpyAsync(s->pblk.p, &zero, sizeof(int64_t), cudaMemcpyHostToDevice, s->stream), "blk");
@@ -617,6 +630,40 @@ void launch_field_batch(vhsdecode_gb300_session* s, int f0, int f1, const T* vid
     ck(cudaMemcpyAsync(s->start_line_d.p + f0, sline.data(), nf * sizeof(int), cudaMemcpyHostToDevice, fs), "h2d");
     ck(cudaMemcpyAsync(s->end_line_d.p + f0, eline.data(), nf * sizeof(int), cudaMemcpyHostToDevice, fs), "h2d");
     ck(cudaMemcpyAsync(s->line_off_d.p + f0, loff.data(), nf * sizeof(int), cudaMemcpyHostToDevice, fs), "h2d");
+    const int nch = dropout_chunks(s->span_len);
+    DropoutParams dp{};
+    dp.nfields = nf;
+    dp.span_start = s->span_start_d.p + f0;
+    dp.span_len = s->span_len_d.p + f0;
+    dp.max_span_len = s->span_len;
+    dp.locs = s->locs_out.p + f0 * L;
+    dp.lines = s->lines;
+    dp.start_line = s->start_line_d.p + f0;
+    dp.end_line = s->end_line_d.p + f0;
+    dp.line_offset = s->line_off_d.p + f0;
+    dp.outlen = s->outlen;
+    dp.range = s->drop_range.p + 2 * (size_t)f0;
+    dp.frac = 0.18f;
+    dp.hyst = 1.25;
+    dp.merge = 30;
+    dp.min_len = 10;
+    dp.mean_out = s->drop_mean.p + f0;
+    dp.events = s->drop_events.p + (size_t)f0 * nch * s->drop_cap;
+    dp.cap = s->drop_cap;
+    dp.out = s->drop_out.p + (size_t)f0 * s->drop_out_cap * 3;
+    dp.out_cap = s->drop_out_cap;
+    dp.out_count = s->drop_out_count.p + f0;
+    dp.status = s->drop_status.p + f0;
+    // The dropout chain runs beside hsync and TBC on drop_stream: the envelope
+    // means need only the spans, the detection waits for the refined lines.
+    // (With per-stage timing everything stays on `fs`, in order.)
+    const bool timing = s->stage_timing;
+    cudaStream_t ds = timing ? fs : s->drop_stream;
+    if (!timing) {
+        ck(cudaEventRecord(s->drop_fork, fs), "event");
+        ck(cudaStreamWaitEvent(ds, s->drop_fork, 0), "wait");
+    }
+    ck(launch_drop_mean<T>(env, stream_len, dp, s->drop_partial.p + (size_t)f0 * nch, ds), "dropout launch");
     HsyncParams hp{};
     hp.nfields = nf;
     hp.lines = s->lines;
@@ -640,11 +687,16 @@ void launch_field_batch(vhsdecode_gb300_session* s, int f0, int f1, const T* vid
         ck(cudaMemsetAsync(s->hsync_misses.p, 0, sizeof(int), fs), "memset");
         hp.misses = s->hsync_misses.p;
     }
-    const bool timing = s->stage_timing;
     if (timing) ck(cudaEventRecord(s->stage_ev[0], fs), "event");
     ck(launch_hsync_refine<T>(sync, stream_len, hp, fs), "hsync launch");
     s->launches += kHsyncKernels;
     if (timing) ck(cudaEventRecord(s->stage_ev[1], fs), "event");
+    if (!timing) {
+        ck(cudaEventRecord(s->drop_hsync, fs), "event");
+        ck(cudaStreamWaitEvent(ds, s->drop_hsync, 0), "wait");
+        ck(launch_drop_detect<T>(env, stream_len, dp, s->drop_counts.p + (size_t)f0 * nch, ds), "dropout launch");
+        ck(cudaEventRecord(s->drop_join, ds), "event");
+    }
     TbcParams tp{};
     tp.nfields = nf;
     tp.lines = s->lines;
@@ -672,32 +724,11 @@ void launch_field_batch(vhsdecode_gb300_session* s, int f0, int f1, const T* vid
     ck(launch_tbc_pw<T>(video, stream_len, tp, s->pw.p, fs), "tbc launch");
     s->launches += tp.line_consts ? kTbcFastKernels : kTbcKernels;
     if (timing) ck(cudaEventRecord(s->stage_ev[2], fs), "event");
-    const int nch = dropout_chunks(s->span_len);
-    DropoutParams dp{};
-    dp.nfields = nf;
-    dp.span_start = s->span_start_d.p + f0;
-    dp.span_len = s->span_len_d.p + f0;
-    dp.max_span_len = s->span_len;
-    dp.locs = s->locs_out.p + f0 * L;
-    dp.lines = s->lines;
-    dp.start_line = s->start_line_d.p + f0;
-    dp.end_line = s->end_line_d.p + f0;
-    dp.line_offset = s->line_off_d.p + f0;
-    dp.outlen = s->outlen;
-    dp.range = s->drop_range.p + 2 * (size_t)f0;
-    dp.frac = 0.18f;
-    dp.hyst = 1.25;
-    dp.merge = 30;
-    dp.min_len = 10;
-    dp.mean_out = s->drop_mean.p + f0;
-    dp.events = s->drop_events.p + (size_t)f0 * nch * s->drop_cap;
-    dp.cap = s->drop_cap;
-    dp.out = s->drop_out.p + (size_t)f0 * s->drop_out_cap * 3;
-    dp.out_cap = s->drop_out_cap;
-    dp.out_count = s->drop_out_count.p + f0;
-    dp.status = s->drop_status.p + f0;
-    ck(launch_dropouts_full<T>(env, stream_len, dp, s->drop_partial.p + (size_t)f0 * nch,
-                               s->drop_counts.p + (size_t)f0 * nch, fs), "dropout launch");
+    if (timing) {
+        ck(launch_drop_detect<T>(env, stream_len, dp, s->drop_counts.p + (size_t)f0 * nch, fs), "dropout launch");
+    } else {
+        ck(cudaStreamWaitEvent(fs, s->drop_join, 0), "wait");
+    }
     s->launches += kDropoutKernels;
     if (timing) {
         ck(cudaEventRecord(s->stage_ev[3], fs), "event");
@@ -873,7 +904,8 @@ void decode_fp32_pipelined(vhsdecode_gb300_session* s, const int16_t* rf, uint64
     }
     if (carry && carry->no_graph) graphable = false;
     if (graphable && nseg > 0) {
-        PipeKey key{rf, n, host_input, demod_only};
+        PipeKey key{s->in_f32 ? (const void*)s->in_f32 : (const void*)rf, n, host_input, demod_only,
+                    s->in_f32 != nullptr};
         if (!s->pipe_exec || !(s->pipe_key == key)) {
             if (s->pipe_exec) { cudaGraphExecDestroy(s->pipe_exec); s->pipe_exec = nullptr; }
             FastDemodParams p0 = fp32_params(s, s->rf.p);
@@ -980,17 +1012,65 @@ void decode_plain(vhsdecode_gb300_session* s, const int16_t* rf_dev, uint64_t n,
     ck(cudaEventElapsedTime(&demod_ms, s->ev[1], s->ev[2]), "elapsed");
 }
 
-int32_t decode_impl(vhsdecode_gb300_session* s, const int16_t* rf, uint64_t n, uint32_t max_fields,
+// Float or decimated input: the float capture at the decode rate, queued on
+// the session stream.  Host input is copied in first; the decimator (cuda-fast
+// reader's 20-MSPS mode, src/VHSDecode.CudaFast.Native/src/cuda_fast_decimator.cu:160-319)
+// turns n source samples into n / 2.
+const float* stage_float_input(vhsdecode_gb300_session* s, const void* rf, uint64_t n, bool f32_in,
+                               bool host_input) {
+    cudaStream_t cs = s->stream;
+    const uint64_t nd = n / (uint64_t)s->decim;
+    auto ensure = [&](DevBuf<float>& b, uint64_t count) {
+        if (b.n < count) b.alloc(count);
+    };
+    if (s->decim == 1) {   // float input at the decode rate
+        if (!host_input) return static_cast<const float*>(rf);
+        ensure(s->rf_f32, std::max<uint64_t>(s->max_samples, 16));
+        if (n > 0) ck(cudaMemcpyAsync(s->rf_f32.p, rf, n * sizeof(float), cudaMemcpyHostToDevice, cs), "h2d rf");
+        return s->rf_f32.p;
+    }
+    ensure(s->rf_f32, std::max<uint64_t>(s->max_samples / 2, 16));
+    const int16_t* src16 = nullptr;
+    const float* src32 = nullptr;
+    if (f32_in) {
+        if (host_input) {
+            ensure(s->src_f32, std::max<uint64_t>(s->max_samples, 16));
+            if (n > 0)
+                ck(cudaMemcpyAsync(s->src_f32.p, rf, n * sizeof(float), cudaMemcpyHostToDevice, cs), "h2d rf");
+            src32 = s->src_f32.p;
+        } else {
+            src32 = static_cast<const float*>(rf);
+        }
+    } else {
+        if (host_input) {
+            if (n > 0)
+                ck(cudaMemcpyAsync(s->rf.p, rf, n * sizeof(int16_t), cudaMemcpyHostToDevice, cs), "h2d rf");
+            src16 = s->rf.p;
+        } else {
+            src16 = static_cast<const int16_t*>(rf);
+        }
+    }
+    if (nd > 0) {
+        ck(launch_decimate_half(src16, src32, (int64_t)n, s->rf_f32.p, (int64_t)nd, cs), "decimate launch");
+        s->launches += kDecimateKernels;
+    }
+    return s->rf_f32.p;
+}
+
+int32_t decode_impl(vhsdecode_gb300_session* s, const void* rf_in, uint64_t n_in, uint32_t max_fields,
                     uint32_t flags, vhsdecode_gb300_decode_result_v1* res,
                     const std::atomic<bool>* cancel, DecodeCarry* carry) {
-    if (n > s->max_samples)
+    if (n_in > s->max_samples)
         throw Failure(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "sample_count exceeds the session capacity");
     ck(cudaSetDevice(s->device), "cudaSetDevice");
     cudaStream_t cs = s->stream;
-    const bool host_input = !(flags & VHSDECODE_GB300_DECODE_DEVICE_INPUT);
+    bool host_input = !(flags & VHSDECODE_GB300_DECODE_DEVICE_INPUT);
     const bool demod_only = (flags & VHSDECODE_GB300_DECODE_DEMOD_ONLY) != 0;
-    if (!host_input && ((uintptr_t)rf & 15u) != 0)
+    const bool f32_in = (flags & VHSDECODE_GB300_DECODE_FLOAT_INPUT) != 0;
+    if (!host_input && ((uintptr_t)rf_in & 15u) != 0)
         throw Failure(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "device rf pointer must be 16-byte aligned");
+    // samples at the decode rate
+    const uint64_t n = n_in / (uint64_t)s->decim;
     int64_t nblocks = block_count(n);
     uint32_t stop = 0;
     double host_ms = 0.0;
@@ -1000,6 +1080,14 @@ int32_t decode_impl(vhsdecode_gb300_session* s, const int16_t* rf, uint64_t n, u
     s->segments = 0;
     s->stage_ms[0] = s->stage_ms[1] = s->stage_ms[2] = 0.0f;
     ck(cudaEventRecord(s->ev[0], cs), "event");
+    const int16_t* rf = static_cast<const int16_t*>(rf_in);
+    s->in_f32 = nullptr;
+    if (f32_in || s->decim == 2) {
+        // the demodulators read the float capture from the device
+        s->in_f32 = stage_float_input(s, rf_in, n_in, f32_in, host_input);
+        rf = nullptr;
+        host_input = false;
+    }
     if (s->fp32()) {
         decode_fp32_pipelined(s, rf, n, host_input, demod_only, max_fields, stop, host_ms, demod_ms, cancel,
                               carry);
@@ -1156,32 +1244,42 @@ VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_run(
         if (!config->read_callback) return fail(VHSDECODE_GB300_STATUS_NULL_POINTER, "read_callback is null");
         if (!config->output_base_utf8 || !config->output_base_utf8[0])
             return fail(VHSDECODE_GB300_STATUS_NULL_POINTER, "output_base_utf8 is null");
-        if (config->input_sample_format != VHSDECODE_GB300_INPUT_INT16)
-            return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "only int16 input is supported");
-        if (config->device_decimation_factor != 1)
-            return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "device_decimation_factor must be 1");
+        if (config->input_sample_format > VHSDECODE_GB300_INPUT_INT16)
+            return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "unknown input_sample_format");
+        // vhsdecode_cuda_fast.cpp:255-275: factor 1 or 2; the source runs at
+        // factor x sample_rate_mhz
+        const uint32_t factor = config->device_decimation_factor;
+        if (factor != 1 && factor != 2)
+            return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "device_decimation_factor must be 1 or 2");
+        if (factor == 2 && !(config->sample_rate_mhz >= 10.0 && config->sample_rate_mhz <= 50.0))
+            return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT,
+                        "device_decimation_factor 2 needs a decode rate of 10..50 MHz");
+        const bool f32_in = config->input_sample_format == VHSDECODE_GB300_INPUT_FLOAT32;
+        const size_t esz = f32_in ? sizeof(float) : sizeof(int16_t);
         auto t0 = std::chrono::steady_clock::now();
         std::string base = config->output_base_utf8;
         std::string tbc_path = base + ".tbc", json_path = base + ".tbc.json";
         if (!config->overwrite && (file_exists(tbc_path) || file_exists(json_path)))
             return fail(VHSDECODE_GB300_STATUS_OUTPUT_ERROR, "output exists and overwrite is off");
         auto cancelled = [&]() { return config->cancel_callback && config->cancel_callback(config->user_data) != 0; };
-        // pull the capture through the callback
-        std::vector<int16_t> rf;
+        // pull the capture through the callback (source samples of esz bytes)
+        std::vector<unsigned char> rf;
+        size_t have = 0;
         const size_t chunk = (size_t)1 << 22;
         uint64_t want = config->total_samples;
-        while (want == 0 || rf.size() < want) {
+        while (want == 0 || have < want) {
             if (cancelled()) return fail(VHSDECODE_GB300_STATUS_CANCELLED, "decode cancelled");
             size_t ask = chunk;
-            if (want) ask = (size_t)std::min<uint64_t>(chunk, want - rf.size());
-            size_t old = rf.size();
-            rf.resize(old + ask);
-            size_t got = config->read_callback(config->user_data, rf.data() + old, old, ask);
+            if (want) ask = (size_t)std::min<uint64_t>(chunk, want - have);
+            rf.resize((have + ask) * esz);
+            size_t got = config->read_callback(config->user_data, rf.data() + have * esz, have, ask);
             if (got > ask) return fail(VHSDECODE_GB300_STATUS_INPUT_ERROR, "read callback overran its buffer");
-            rf.resize(old + got);
+            have += got;
+            rf.resize(have * esz);
             if (got < ask) break;
         }
-        if (rf.size() < (size_t)kBlock) return fail(VHSDECODE_GB300_STATUS_INPUT_ERROR, "input shorter than one block");
+        if (have / factor < (size_t)kBlock)
+            return fail(VHSDECODE_GB300_STATUS_INPUT_ERROR, "input shorter than one block");
         vhsdecode_gb300_session_config_v1 sc{};
         sc.struct_size = sizeof(sc);
         sc.profile = config->profile;
@@ -1189,15 +1287,17 @@ VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_run(
         sc.tape_format = tape_format;
         sc.device_id = config->device_id;
         sc.sample_rate_mhz = config->sample_rate_mhz;
-        sc.max_samples = rf.size();
+        sc.max_samples = have;
         sc.precision = VHSDECODE_GB300_PRECISION_FP32_FUSED;
+        sc.decimation = factor;
         SessionHolder h;
         h.s = new vhsdecode_gb300_session();
         session_init(h.s, sc);
         if (cancelled()) return fail(VHSDECODE_GB300_STATUS_CANCELLED, "decode cancelled");
         vhsdecode_gb300_decode_result_v1 dr{};
         dr.struct_size = sizeof(dr);
-        decode_impl(h.s, rf.data(), rf.size(), config->maximum_output_fields, 0, &dr);
+        decode_impl(h.s, rf.data(), have, config->maximum_output_fields,
+                    f32_in ? VHSDECODE_GB300_DECODE_FLOAT_INPUT : 0u, &dr);
         if (cancelled()) return fail(VHSDECODE_GB300_STATUS_CANCELLED, "decode cancelled");
         size_t per = (size_t)h.s->out_lines * h.s->outlen;
         std::vector<uint16_t> tbc(per * h.s->fields.size());
@@ -1255,7 +1355,7 @@ VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_session_set_str
 }
 
 VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_session_decode(
-    vhsdecode_gb300_session* s, const int16_t* rf, uint64_t n, uint32_t max_fields, uint32_t flags,
+    vhsdecode_gb300_session* s, const void* rf, uint64_t n, uint32_t max_fields, uint32_t flags,
     vhsdecode_gb300_decode_result_v1* res) {
     return guard([&]() -> int32_t {
         if (!s || (!rf && n > 0)) return fail(VHSDECODE_GB300_STATUS_NULL_POINTER, "null argument");

@@ -2,7 +2,8 @@
 // thread-block cluster, every intermediate spectrum kept in the two CTAs'
 // shared memory and exchanged through distributed shared memory.
 //
-// Per block b (RF samples x[n] = rf[b*30720 + n], n < 32768) it computes what
+// Per block b (RF samples x[n] = rf[b*30720 + n], n < 32768, from an int16
+// capture or a float one such as the 2:1 decimator's output) it computes what
 // the reference's exact VHS path computes per block
 // (Core/Dsp/RfDemodulator.cs:288-918, exact backend):
 //   X  = rfft(x);  Y = X * RfVideo                         (stage 1)
@@ -402,30 +403,67 @@ __device__ __forceinline__ float sub_gain(float amp, const SubDeemph& s) {
     return amp;
 }
 
-// One RF block (read from the prefetch copy in shared memory) into this
-// rank's packed DIF input: rank 0 gets a + b, rank 1
-// (a - b) W^(2p), p in [0, 8192), where a / b are the complex pairs of the
-// block's first / second half.  W^(2p) = W^(8v) W^(2e) for p = 4v + e.
+// Complex product with every operation rounded on its own (no contraction).
+__device__ __forceinline__ float2 cmul_rn(float2 a, float2 b) {
+    return make_float2(__fsub_rn(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)),
+                       __fadd_rn(__fmul_rn(a.x, b.y), __fmul_rn(a.y, b.x)));
+}
+
+// Samples 8 v .. 8 v + 7 of the block's first (ha) and second (hb) half into
+// this rank's packed DIF input elements p = 4 v + e: rank 0 gets a + b, rank 1
+// (a - b) W^(2p), where a / b are the complex pairs of the two halves and
+// W^(2p) = W^(8v) W^(2e).  The arithmetic is spelled out rounding by rounding,
+// so an int16 capture and a float capture of the same values pack to the
+// same bits.
+__device__ __forceinline__ void pack_rf(float2* buf, const float* ha, const float* hb, int vi, int rank,
+                                        const Tw& tw) {
+    float2 w8 = make_float2(1.0f, 0.0f);
+    if (rank) w8 = cmul_rn(tw.hi[vi >> 4], tw.lo8[vi & 15]);
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+        const int pp = 4 * vi + e;
+        float2 r;
+        if (rank == 0) {
+            r = make_float2(__fadd_rn(ha[2 * e], hb[2 * e]), __fadd_rn(ha[2 * e + 1], hb[2 * e + 1]));
+        } else {
+            const float2 d = make_float2(__fsub_rn(ha[2 * e], hb[2 * e]), __fsub_rn(ha[2 * e + 1], hb[2 * e + 1]));
+            r = cmul_rn(d, e == 0 ? w8 : cmul_rn(w8, tw.lo[2 * e]));
+        }
+        buf[sx(pp)] = r;
+    }
+}
+
+// One int16 RF block from the prefetch copy in shared memory.
 __device__ __forceinline__ void load_rf(float2* buf, const int16_t* x, int rank, const Tw& tw, int tid) {
 #pragma unroll
     for (int it = 0; it < 4; it++) {
-        int vi = tid + it * T;  // vector index in [0, 2048)
-        int4 va = reinterpret_cast<const int4*>(x)[vi];
-        int4 vb = reinterpret_cast<const int4*>(x + 16384)[vi];
-        const int16_t* ha = reinterpret_cast<const int16_t*>(&va);
-        const int16_t* hb = reinterpret_cast<const int16_t*>(&vb);
-        float2 w8 = make_float2(1.0f, 0.0f);
-        if (rank) w8 = cmul(tw.hi[vi >> 4], tw.lo8[vi & 15]);
+        const int vi = tid + it * T;  // vector index in [0, 2048)
+        const int4 va = reinterpret_cast<const int4*>(x)[vi];
+        const int4 vb = reinterpret_cast<const int4*>(x + 16384)[vi];
+        const int16_t* a16 = reinterpret_cast<const int16_t*>(&va);
+        const int16_t* b16 = reinterpret_cast<const int16_t*>(&vb);
+        float ha[8], hb[8];
 #pragma unroll
-        for (int e = 0; e < 4; e++) {
-            int pp = 4 * vi + e;
-            float2 ca = make_float2((float)ha[2 * e], (float)ha[2 * e + 1]);
-            float2 cb = make_float2((float)hb[2 * e], (float)hb[2 * e + 1]);
-            float2 r;
-            if (rank == 0) r = cadd(ca, cb);
-            else r = cmul(csub(ca, cb), e == 0 ? w8 : cmul(w8, tw.lo[2 * e]));
-            buf[sx(pp)] = r;
+        for (int k = 0; k < 8; k++) {
+            ha[k] = (float)a16[k];
+            hb[k] = (float)b16[k];
         }
+        pack_rf(buf, ha, hb, vi, rank, tw);
+    }
+}
+
+// One float RF block (decimated or float input) from global memory; no
+// prefetch: two 16-byte loads per half and vector index.
+__device__ __forceinline__ void load_rf_f32(float2* buf, const float* x, int rank, const Tw& tw, int tid) {
+#pragma unroll
+    for (int it = 0; it < 4; it++) {
+        const int vi = tid + it * T;  // vector index in [0, 2048)
+        const float4* xa = reinterpret_cast<const float4*>(x) + 2 * vi;
+        const float4* xb = reinterpret_cast<const float4*>(x + 16384) + 2 * vi;
+        const float4 a0 = __ldg(xa), a1 = __ldg(xa + 1), b0 = __ldg(xb), b1 = __ldg(xb + 1);
+        const float ha[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+        const float hb[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+        pack_rf(buf, ha, hb, vi, rank, tw);
     }
 }
 
@@ -507,6 +545,7 @@ __device__ __noinline__ void repair_block(Shared& sh, Shared* rsh, const FastDem
     }
     __syncthreads();
 }
+
 
 // Bits 0..15 of x to the even bit positions of the result.
 __device__ __forceinline__ unsigned spread16(unsigned x) {
@@ -590,15 +629,19 @@ vhsd_demod_fp32_kernel(FastDemodParams p) {
     // the RF of each block is prefetched into sh.theta (free from the demod's
     // last read until the next block's angles) while the previous block
     // finishes
+    // (int16 captures only; a float capture is read from global memory)
     const int16_t* rf_smem = reinterpret_cast<const int16_t*>(sh.theta);
-    if (cluster_id < p.nblocks) prefetch_rf(sh.theta, p.rf + (cluster_id + p.first_block) * (int64_t)S, tid);
+    const bool f32_in = p.rf_f32 != nullptr;
+    if (cluster_id < p.nblocks && !f32_in)
+        prefetch_rf(sh.theta, p.rf + (cluster_id + p.first_block) * (int64_t)S, tid);
     for (int64_t blk = cluster_id; blk < p.nblocks; blk += nclusters) {
-        const bool has_next = blk + nclusters < p.nblocks;
-        const int16_t* x_next = p.rf + (blk + nclusters + p.first_block) * (int64_t)S;
+        const bool has_next = blk + nclusters < p.nblocks && !f32_in;
+        const int16_t* x_next = f32_in ? nullptr : p.rf + (blk + nclusters + p.first_block) * (int64_t)S;
         // ---------------- stage 1: RF forward FFT (packed, DIF split) -----
         prefetch_wait();
         __syncthreads();
-        load_rf(buf, rf_smem, rank, sh.tw, tid);
+        if (f32_in) load_rf_f32(buf, p.rf_f32 + (blk + p.first_block) * (int64_t)S, rank, sh.tw, tid);
+        else load_rf(buf, rf_smem, rank, sh.tw, tid);
         __syncthreads();
         fft8192<false, 1, PLAN>(buf, sh.tw, tid);
         // X * RfVideo * Hilbert / N  (Hilbert: 1 at 0 and N/2, 2 between)

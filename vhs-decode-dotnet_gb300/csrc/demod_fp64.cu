@@ -63,10 +63,12 @@ void fft(double2* a, double2* b, cudaStream_t s) {
 }
 
 
-__global__ void k_load(const int16_t* rf, const int64_t* blk, double2* out) {
+// int16 capture, or a float one when rf32 is set
+__global__ void k_load(const int16_t* rf, const float* rf32, const int64_t* blk, double2* out) {
     int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= N) return;
-    out[n] = make_double2((double)rf[blk[0] * kStride + n], 0.0);
+    const int64_t i = blk[0] * kStride + n;
+    out[n] = make_double2(rf32 ? (double)rf32[i] : (double)rf[i], 0.0);
 }
 
 // analytic spectrum: X * RfVideo * Hilbert / N  (bins > N/2 zero)
@@ -406,7 +408,7 @@ cudaError_t launch_demod_fp64_block(const PlainDemodParams& p, cudaStream_t s) {
     int* flag = p.flag;
     unsigned* mask = p.mask;
     int64_t* blk = p.blk;
-    k_load<<<G, B, 0, s>>>(p.rf, blk, w0);
+    k_load<<<G, B, 0, s>>>(p.rf, p.rf_f32, blk, w0);
     fft<false>(w0, w1, s);                         // X in w1
     k_analytic_spec<<<G, B, 0, s>>>(w1, p.rf_video, w2);
     fft<true>(w2, w3, s);                          // z in w3

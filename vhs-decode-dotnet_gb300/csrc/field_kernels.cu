@@ -1658,14 +1658,23 @@ __global__ void k_drop_finish(DropoutParams p, int nchunk, const int* chunk_coun
 int dropout_chunks(int64_t span_len) { return (int)((span_len + kDChunk - 1) / kDChunk); }
 
 template <typename T>
-cudaError_t launch_dropouts_full(const T* stream, int64_t stream_len, const DropoutParams& p,
-                                 float* partial, int* chunk_counts, cudaStream_t s) {
+cudaError_t launch_drop_mean(const T* stream, int64_t stream_len, const DropoutParams& p, float* partial,
+                             cudaStream_t s) {
+    if (p.nfields <= 0) return cudaSuccess;
+    int nchunk = dropout_chunks(p.max_span_len);
+    dim3 g(nchunk, p.nfields);
+    k_env_partial<T><<<g, kDT, 0, s>>>(stream, stream_len, p, partial, nchunk);
+    k_env_mean<<<p.nfields, 32, 0, s>>>(p, partial, nchunk, stream_len);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_drop_detect(const T* stream, int64_t stream_len, const DropoutParams& p, int* chunk_counts,
+                               cudaStream_t s) {
     if (p.nfields <= 0) return cudaSuccess;
     int nchunk = dropout_chunks(p.max_span_len);
     k_drop_ranges<<<(p.nfields + 127) / 128, 128, 0, s>>>(p, stream_len);
     dim3 g(nchunk, p.nfields);
-    k_env_partial<T><<<g, kDT, 0, s>>>(stream, stream_len, p, partial, nchunk);
-    k_env_mean<<<p.nfields, 32, 0, s>>>(p, partial, nchunk, stream_len);
     k_drop_events<T><<<g, kDT, 0, s>>>(stream, stream_len, p, nchunk, chunk_counts);
     size_t smem = drop_finish_smem(p.lines, nchunk);
     if (smem > 48 * 1024) {
@@ -1676,7 +1685,19 @@ cudaError_t launch_dropouts_full(const T* stream, int64_t stream_len, const Drop
     k_drop_finish<<<p.nfields, 128, smem, s>>>(p, nchunk, chunk_counts);
     return cudaGetLastError();
 }
+
+template <typename T>
+cudaError_t launch_dropouts_full(const T* stream, int64_t stream_len, const DropoutParams& p,
+                                 float* partial, int* chunk_counts, cudaStream_t s) {
+    cudaError_t e = launch_drop_mean<T>(stream, stream_len, p, partial, s);
+    if (e != cudaSuccess) return e;
+    return launch_drop_detect<T>(stream, stream_len, p, chunk_counts, s);
+}
 template cudaError_t launch_dropouts_full<float>(const float*, int64_t, const DropoutParams&, float*, int*, cudaStream_t);
 template cudaError_t launch_dropouts_full<double>(const double*, int64_t, const DropoutParams&, float*, int*, cudaStream_t);
+template cudaError_t launch_drop_mean<float>(const float*, int64_t, const DropoutParams&, float*, cudaStream_t);
+template cudaError_t launch_drop_mean<double>(const double*, int64_t, const DropoutParams&, float*, cudaStream_t);
+template cudaError_t launch_drop_detect<float>(const float*, int64_t, const DropoutParams&, int*, cudaStream_t);
+template cudaError_t launch_drop_detect<double>(const double*, int64_t, const DropoutParams&, int*, cudaStream_t);
 
 }  // namespace vhsd

@@ -30,6 +30,7 @@ using SubDeemph64 = SubDeemphT<double, double2>;
 
 struct FastDemodParams {
     const int16_t* rf;         // capture, 16-byte aligned
+    const float* rf_f32;       // float capture (16-byte aligned), read instead of rf when set
     int64_t first_block;       // first 32768-sample block to decode
     int64_t nblocks;           // number of blocks
     const float* rf_video;     // [kHalf] real RF band-pass gain
@@ -65,9 +66,16 @@ constexpr int kFftPlans[kFftPlanCount] = {0, 1, 4, 5};
 size_t fp32_smem_bytes();
 cudaError_t launch_demod_fp32(const FastDemodParams& p, int num_clusters, cudaStream_t stream);
 
+// 2:1 half-band decimation of a capture (exactly one of src16 / src32, 16-byte
+// aligned): out_len float samples, output i centred on source sample 2 i.
+constexpr int kDecimateKernels = 1;
+cudaError_t launch_decimate_half(const int16_t* src16, const float* src32, int64_t src_len, float* dst,
+                                 int64_t out_len, cudaStream_t s);
+
 // ---------------------------------------------------------------- FP64 plain
 struct PlainDemodParams {
     const int16_t* rf;
+    const float* rf_f32;       // float capture, read instead of rf when set
     int64_t block;             // block index
     const double* rf_video;    // [kHalf]
     const double2* video;      // [kHalf]
@@ -203,5 +211,15 @@ constexpr int kDropoutKernels = 5;
 template <typename T>
 cudaError_t launch_dropouts_full(const T* env_stream, int64_t stream_len, const DropoutParams& p,
                                  float* partial, int* chunk_counts, cudaStream_t stream);
+// The two halves of launch_dropouts_full: the envelope mean of each field span
+// (needs only the spans: 2 kernels), then the detection and TBC mapping
+// (needs the refined line locations: 3 kernels).
+constexpr int kDropMeanKernels = 2;
+template <typename T>
+cudaError_t launch_drop_mean(const T* env_stream, int64_t stream_len, const DropoutParams& p, float* partial,
+                             cudaStream_t stream);
+template <typename T>
+cudaError_t launch_drop_detect(const T* env_stream, int64_t stream_len, const DropoutParams& p,
+                               int* chunk_counts, cudaStream_t stream);
 
 }  // namespace vhsd

@@ -80,9 +80,9 @@ struct DevBuf {
 struct PipeKey {
     const void* rf = nullptr;
     uint64_t n = 0;
-    bool host_input = false, demod_only = false;
+    bool host_input = false, demod_only = false, f32 = false;
     bool operator==(const PipeKey& o) const {
-        return rf == o.rf && n == o.n && host_input == o.host_input && demod_only == o.demod_only;
+        return rf == o.rf && n == o.n && host_input == o.host_input && demod_only == o.demod_only && f32 == o.f32;
     }
 };
 
@@ -128,11 +128,15 @@ struct vhsdecode_gb300_session {
     int outlen = 0;
     int num_sms = 0;
     int fft_plan = 0;    // radix plans of the fused demodulator (tuned per device)
+    int decim = 1;       // 2: decode input passes the 2:1 half-band decimator
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[6] = {};
     // device data
     DevBuf<int16_t> rf;
+    DevBuf<float> rf_f32;                    // float capture at the decode rate (decimated or float input)
+    DevBuf<float> src_f32;                   // float source ahead of the decimator
+    const float* in_f32 = nullptr;           // the current decode's float capture, if any
     DevBuf<float> v32, s32, e32;
     DevBuf<unsigned> sync_cond, sync_hold;   // pulse-scan bits of s32 (FP32 path)
     DevBuf<double> v64, s64, e64;
@@ -149,7 +153,8 @@ struct vhsdecode_gb300_session {
     DevBuf<unsigned> pmask;
     DevBuf<int64_t> pblk;
     cudaGraphExec_t plain_graph = nullptr;
-    const int16_t* graph_rf = nullptr;   // input pointer baked into plain_graph
+    const int16_t* graph_rf = nullptr;   // input pointers baked into plain_graph
+    const float* graph_rf32 = nullptr;
     DevBuf<int64_t> pc_counts, pc_offsets, pc_events, pc_total;
     DevBuf<int64_t> pc_counts_alt, pc_offsets_alt;   // scan scratch of odd segments
     int64_t pc_capacity = 0;
@@ -177,6 +182,8 @@ struct vhsdecode_gb300_session {
     double enqueue_ms = 0.0;             // host time to queue the pipelined demod
     cudaStream_t field_stream = nullptr; // field batches, concurrent with later demod segments
     cudaEvent_t field_end = nullptr;
+    cudaStream_t drop_stream = nullptr;  // a field batch's dropout chain, beside its hsync and TBC
+    cudaEvent_t drop_fork = nullptr, drop_hsync = nullptr, drop_join = nullptr;
     bool stage_timing = false;           // VHSD_STAGE_TIMING set: per-stage kernel times to stderr
     cudaEvent_t stage_ev[4] = {};
     float stage_ms[3] = {};
@@ -217,7 +224,7 @@ struct DecodeCarry {
 
 void session_init(vhsdecode_gb300_session* s, const vhsdecode_gb300_session_config_v1& c);
 void session_free(vhsdecode_gb300_session* s);
-int32_t decode_impl(vhsdecode_gb300_session* s, const int16_t* rf, uint64_t n, uint32_t max_fields,
+int32_t decode_impl(vhsdecode_gb300_session* s, const void* rf, uint64_t n, uint32_t max_fields,
                     uint32_t flags, vhsdecode_gb300_decode_result_v1* res,
                     const std::atomic<bool>* cancel = nullptr, DecodeCarry* carry = nullptr);
 

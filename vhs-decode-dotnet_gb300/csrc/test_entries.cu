@@ -109,6 +109,30 @@ VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_vhs_angles(
     return set_last_error(VHSDECODE_GB300_STATUS_OK, "");
 }
 
+VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_decimate_half_rate(
+    const void* source, uint32_t input_sample_format, uint64_t source_count, float* destination) {
+    if ((!source || !destination) && source_count > 1)
+        return set_last_error(VHSDECODE_GB300_STATUS_NULL_POINTER, "null argument");
+    if (input_sample_format > VHSDECODE_GB300_INPUT_INT16)
+        return set_last_error(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "unknown input_sample_format");
+    if (!have_device()) return set_last_error(VHSDECODE_GB300_STATUS_CUDA_UNAVAILABLE, "no CUDA device available");
+    const uint64_t nd = source_count / 2;
+    if (nd == 0) return set_last_error(VHSDECODE_GB300_STATUS_OK, "");
+    const bool s16 = input_sample_format == VHSDECODE_GB300_INPUT_INT16;
+    const size_t esz = s16 ? sizeof(int16_t) : sizeof(float);
+    Scoped sc;
+    unsigned char* dsrc = sc.alloc<unsigned char>(source_count * esz);
+    float* dout = sc.alloc<float>(nd);
+    if (!dsrc || !dout) return set_last_error(VHSDECODE_GB300_STATUS_INTERNAL_ERROR, "cudaMalloc failed");
+    CUDA_OR_RETURN(cudaMemcpy(dsrc, source, source_count * esz, cudaMemcpyHostToDevice), "h2d");
+    CUDA_OR_RETURN(launch_decimate_half(s16 ? reinterpret_cast<const int16_t*>(dsrc) : nullptr,
+                                        s16 ? nullptr : reinterpret_cast<const float*>(dsrc),
+                                        (int64_t)source_count, dout, (int64_t)nd, 0),
+                   "decimate launch");
+    CUDA_OR_RETURN(cudaMemcpy(destination, dout, nd * sizeof(float), cudaMemcpyDeviceToHost), "d2h");
+    return set_last_error(VHSDECODE_GB300_STATUS_OK, "");
+}
+
 VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_vhs_demod(
     const float* re, const float* im, uint64_t n, double sample_rate_hz, float* out) {
     if ((!re || !im || !out) && n) return set_last_error(VHSDECODE_GB300_STATUS_NULL_POINTER, "null argument");

@@ -13,7 +13,7 @@ import os
 
 import numpy as np
 
-ABI_VERSION = 0x00010002
+ABI_VERSION = 0x00010003
 STATUS_OK = 0
 STATUS_NULL_POINTER = -20000
 STATUS_INVALID_ARGUMENT = -20001
@@ -31,6 +31,7 @@ INPUT_FLOAT32, INPUT_INT16 = 0, 1
 PRECISION_FP32_FUSED, PRECISION_FP64_PLAIN = 0, 1
 DECODE_DEVICE_INPUT = 0x1
 DECODE_DEMOD_ONLY = 0x2
+DECODE_FLOAT_INPUT = 0x4
 
 LIB_PATH = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "lib",
                         "libvhsdecode_gb300.so")
@@ -48,6 +49,7 @@ EXPORTS = [
     "vhsdecode_gb300_pulse_events_noalloc", "vhsdecode_gb300_vhs_demod",
     "vhsdecode_gb300_server_create", "vhsdecode_gb300_server_submit", "vhsdecode_gb300_server_wait",
     "vhsdecode_gb300_server_destroy", "vhsdecode_gb300_replace_spikes",
+    "vhsdecode_gb300_decimate_half_rate",
 ]
 
 
@@ -104,7 +106,7 @@ class SessionConfig(ctypes.Structure):
                 ("tape_speed", ctypes.c_uint32), ("device_id", ctypes.c_int32),
                 ("sample_rate_mhz", ctypes.c_double), ("max_samples", ctypes.c_uint64),
                 ("precision", ctypes.c_uint32), ("max_fields", ctypes.c_uint32),
-                ("tape_format", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+                ("tape_format", ctypes.c_uint32), ("decimation", ctypes.c_uint32)]
 
 
 class DecodeResult(ctypes.Structure):
@@ -198,6 +200,7 @@ def load(path: str = LIB_PATH):
     L.vhsdecode_gb300_vhs_angles.argtypes = [_vp, _vp, ctypes.c_uint64, _vp]
     L.vhsdecode_gb300_vhs_demod.argtypes = [_vp, _vp, ctypes.c_uint64, ctypes.c_double, _vp]
     L.vhsdecode_gb300_replace_spikes.argtypes = [_vp, _vp, ctypes.c_uint64, ctypes.c_float]
+    L.vhsdecode_gb300_decimate_half_rate.argtypes = [_vp, ctypes.c_uint32, ctypes.c_uint64, _vp]
     L.vhsdecode_gb300_server_create.argtypes = [_P(ServerConfig), _P(_vp)]
     L.vhsdecode_gb300_server_submit.argtypes = [_vp, _P(Window), _P(ctypes.c_uint64)]
     L.vhsdecode_gb300_server_wait.argtypes = [_vp, ctypes.c_uint64, _P(WindowResult)]
@@ -311,6 +314,21 @@ def vhs_demod(re, im, fs):
     return out
 
 
+def decimate_half_rate(source):
+    """Device 2:1 half-band decimation of an int16 or float32 capture
+    (len // 2 float32 samples)."""
+    src = np.ascontiguousarray(source)
+    if src.dtype == np.int16:
+        fmt = INPUT_INT16
+    elif src.dtype == np.float32:
+        fmt = INPUT_FLOAT32
+    else:
+        raise TypeError("int16 or float32 capture expected")
+    out = np.zeros(len(src) // 2, np.float32)
+    check(load().vhsdecode_gb300_decimate_half_rate(_ptr(src), fmt, len(src), _ptr(out)))
+    return out
+
+
 def replace_spikes(demod, diffed, max_value):
     d = np.ascontiguousarray(demod, np.float32).copy()
     f = np.ascontiguousarray(diffed, np.float32)
@@ -322,7 +340,7 @@ class Session:
     """Device-resident decode context (session API of include/vhsdecode_gb300.h)."""
 
     def __init__(self, profile, max_samples, precision=PRECISION_FP32_FUSED, device=0,
-                 sample_rate_mhz=40.0, max_fields=0, tape_format=FORMAT_VHS):
+                 sample_rate_mhz=40.0, max_fields=0, tape_format=FORMAT_VHS, decimation=1):
         L = load()
         cfg = SessionConfig()
         cfg.struct_size = ctypes.sizeof(SessionConfig)
@@ -334,6 +352,7 @@ class Session:
         cfg.max_samples = int(max_samples)
         cfg.precision = precision
         cfg.max_fields = max_fields
+        cfg.decimation = decimation
         h = ctypes.c_void_p()
         check(L.vhsdecode_gb300_session_create(ctypes.byref(cfg), ctypes.byref(h)))
         self._h = h
@@ -360,15 +379,23 @@ class Session:
     def set_stream(self, stream_handle):
         check(load().vhsdecode_gb300_session_set_stream(self._h, ctypes.c_void_p(stream_handle)))
 
-    def decode(self, rf, max_fields=0, demod_only=False, device_ptr=None, count=None):
+    def decode(self, rf, max_fields=0, demod_only=False, device_ptr=None, count=None, float_input=None):
+        """Decode int16 samples (or float32 ones: a float32 array, or
+        ``float_input=True`` with ``device_ptr``)."""
         r = DecodeResult()
         r.struct_size = ctypes.sizeof(DecodeResult)
         flags = DECODE_DEMOD_ONLY if demod_only else 0
         if device_ptr is not None:
             flags |= DECODE_DEVICE_INPUT
             ptr, n = ctypes.c_void_p(device_ptr), int(count)
+            if float_input:
+                flags |= DECODE_FLOAT_INPUT
         else:
-            rf = np.ascontiguousarray(rf, np.int16)
+            if float_input or (float_input is None and np.asarray(rf).dtype == np.float32):
+                rf = np.ascontiguousarray(rf, np.float32)
+                flags |= DECODE_FLOAT_INPUT
+            else:
+                rf = np.ascontiguousarray(rf, np.int16)
             ptr, n = _ptr(rf), len(rf)
         check(load().vhsdecode_gb300_session_decode(self._h, ptr, n, max_fields, flags,
                                                     ctypes.byref(r)))
