@@ -1527,8 +1527,12 @@ size_t drop_finish_smem(int lines, int nchunk) {
 }
 
 // One CTA per field.  The field's line locations, chunk offsets and (when they
-// fit) its events are staged in shared memory; thread 0 then runs the merge
-// state machine, the minimum length rule and the TBC mapping.
+// fit) its events are staged in shared memory, each event gathered by one
+// thread (its chunk found by binary search over the chunk offsets).  Warp 0
+// then runs the merge state machine, the minimum length rule and the TBC
+// mapping, every lane in step (lane 0 writes): the mapping's search for the
+// line holding a dropout start tests 32 lines per ballot, in line order, so it
+// finds the same line as the reference's walk (MapTapeRfToTbc).
 __global__ void k_drop_finish(DropoutParams p, int nchunk, const int* chunk_counts) {
     extern __shared__ __align__(16) unsigned char dsm[];
     double* sloc = reinterpret_cast<double*>(dsm);
@@ -1557,16 +1561,22 @@ __global__ void k_drop_finish(DropoutParams p, int nchunk, const int* chunk_coun
         if (lane == 0) { soff[nchunk] = carry; s_status = st; }
     }
     __syncthreads();
-    const bool fits = soff[nchunk] <= kDropSmemEvents;
+    const int total = soff[nchunk];
+    const bool fits = total <= kDropSmemEvents;
     if (fits) {
-        for (int c = 0; c < nchunk; c++) {
-            int cnt = soff[c + 1] - soff[c];
-            const int64_t* ev = p.events + ((int64_t)f * nchunk + c) * p.cap;
-            for (int e = threadIdx.x; e < cnt; e += blockDim.x) sev[soff[c] + e] = ev[e];
+        for (int e = threadIdx.x; e < total; e += blockDim.x) {
+            // the last chunk starting at or before e holds it (empty chunks share offsets)
+            int lo = 0, hi = nchunk - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (soff[mid] <= e) lo = mid;
+                else hi = mid - 1;
+            }
+            sev[e] = p.events[((int64_t)f * nchunk + lo) * p.cap + (e - soff[lo])];
         }
     }
     __syncthreads();
-    if (threadIdx.x != 0) return;
+    if (threadIdx.x >= 32) return;
     const int64_t r1 = p.range[2 * f + 1];
     int32_t* out = p.out + (int64_t)f * p.out_cap * 3;
     int nout = 0;
@@ -1581,7 +1591,7 @@ __global__ void k_drop_finish(DropoutParams p, int nchunk, const int* chunk_coun
     bool map_done = !map_ok;
     auto emit = [&](int line, int sx, int ex) {
         if (nout < p.out_cap) {
-            out[3 * nout] = line; out[3 * nout + 1] = sx; out[3 * nout + 2] = ex;
+            if (lane == 0) { out[3 * nout] = line; out[3 * nout + 1] = sx; out[3 * nout + 2] = ex; }
         } else {
             status = 1;
         }
@@ -1589,21 +1599,25 @@ __global__ void k_drop_finish(DropoutParams p, int nchunk, const int* chunk_coun
     };
     auto map_range = [&](double ds, double de) {
         if (map_done) return;
-        bool found = false;
-        int cur_line = 0, cur_sx = 0;
-        while (li < el) {
-            double ll = le - ls;
-            if ((ds >= ls || li == sl) && ds < le && ll > 0.0) {
-                int sx = (int)floor(((ds - ls) / ll) * p.outlen);
-                cur_line = li - off;
-                cur_sx = sx > 0 ? sx : 0;
-                found = true;
-                break;
+        // first line k >= li whose span holds ds (the first line also takes a
+        // ds before it); none: the walk ran off the field
+        int k = -1;
+        for (int base = li; base < el; base += 32) {
+            const int kk = base + lane;
+            bool hit = false;
+            if (kk < el) {
+                const double a = loc[kk], b = loc[kk + 1];
+                hit = (ds >= a || kk == sl) && ds < b && b - a > 0.0;
             }
-            li++;
-            if (li < el) { ls = loc[li]; le = loc[li + 1]; }
+            const unsigned m = __ballot_sync(0xffffffffu, hit);
+            if (m) { k = base + __ffs(m) - 1; break; }
         }
-        if (!found) { map_done = true; return; }
+        if (k < 0) { li = el; map_done = true; return; }
+        li = k;
+        ls = loc[li];
+        le = loc[li + 1];
+        const int sx = (int)floor(((ds - ls) / (le - ls)) * p.outlen);
+        int cur_line = li - off, cur_sx = sx > 0 ? sx : 0;
         while (li < el) {
             double ll = le - ls;
             if (de < le && ll > 0.0) {
@@ -1622,36 +1636,43 @@ __global__ void k_drop_finish(DropoutParams p, int nchunk, const int* chunk_coun
     };
     bool have = false, open = false, pending = false;
     int64_t start = 0, last_end = 0, cand = 0;
-    for (int c = 0; c < nchunk; c++) {
-        int cnt = soff[c + 1] - soff[c];
-        const int64_t* ev = fits ? sev + soff[c] : p.events + ((int64_t)f * nchunk + c) * p.cap;
-        for (int e = 0; e < cnt; e++) {
-            int64_t pos = ev[e] >> 2;
-            int type = (int)(ev[e] & 3);
-            if (type == 0) {
-                if (!have) { start = pos; open = true; have = true; }
-                else if (!open) {
-                    int64_t c2 = last_end + p.merge + 1;
-                    cand = pos > c2 ? pos : c2;
-                    pending = true;
-                }
-            } else if (type == 1) {
-                if (pending) {
-                    if (cand < pos) { start = cand; open = true; }
-                    pending = false;
-                }
-            } else {
-                if (have && open) {
-                    open = false;
-                    last_end = pos;
-                    if (pos - start > p.min_len) map_range((double)start, (double)pos);
-                }
+    auto step = [&](int64_t evv) {
+        const int64_t pos = evv >> 2;
+        const int type = (int)(evv & 3);
+        if (type == 0) {
+            if (!have) { start = pos; open = true; have = true; }
+            else if (!open) {
+                int64_t c2 = last_end + p.merge + 1;
+                cand = pos > c2 ? pos : c2;
+                pending = true;
             }
+        } else if (type == 1) {
+            if (pending) {
+                if (cand < pos) { start = cand; open = true; }
+                pending = false;
+            }
+        } else {
+            if (have && open) {
+                open = false;
+                last_end = pos;
+                if (pos - start > p.min_len) map_range((double)start, (double)pos);
+            }
+        }
+    };
+    if (fits) {
+        for (int e = 0; e < total; e++) step(sev[e]);
+    } else {
+        for (int c = 0; c < nchunk; c++) {
+            const int cnt = soff[c + 1] - soff[c];
+            const int64_t* ev = p.events + ((int64_t)f * nchunk + c) * p.cap;
+            for (int e = 0; e < cnt; e++) step(ev[e]);
         }
     }
     if (have && open && r1 - start > p.min_len) map_range((double)start, (double)r1);
-    p.out_count[f] = nout;
-    p.status[f] = status;
+    if (lane == 0) {
+        p.out_count[f] = nout;
+        p.status[f] = status;
+    }
 }
 }  // namespace
 
