@@ -378,7 +378,9 @@ typedef struct vhsdecode_gb300_window_v1 {
     uint16_t* tbc_out;              /* host destination for the fields' TBC, or NULL */
     uint64_t tbc_capacity;          /* uint16 elements at tbc_out */
     uint32_t tape_format;           /* vhsdecode_gb300_tape_format */
-    uint32_t reserved;
+    uint32_t decimation;            /* 0 or 1: none; 2: samples run at twice sample_rate_mhz and
+                                       pass the device 2:1 decimator (the reference preview's
+                                       40 -> 20 MSPS mode); counts and offsets stay source samples */
 } vhsdecode_gb300_window_v1;
 
 typedef struct vhsdecode_gb300_window_result_v1 {

@@ -124,3 +124,33 @@ def test_unsupported_window_is_rejected(gpu, pal_capture):
         assert e.value.status == native.STATUS_INVALID_ARGUMENT
         with pytest.raises(native.NativeError):
             sv.submit(0, native.PROFILE_PAL, pal[:1 << 22])   # longer than the slots
+
+
+def test_decimated_windows_match_the_session(gpu, ntsc_capture, pal_capture):
+    # preview mode of the reference (40-MSPS windows decoded at 20 MSPS through
+    # the device decimator) beside full-rate windows in one server: each
+    # window's fields equal a decimating session's decode of the same samples
+    from vhsd_gb300 import native
+    ntsc, _ = ntsc_capture
+    pal, _ = pal_capture
+    length = 1_400_000
+    per = 263 * 910
+    wins = _windows(ntsc, 2, length)
+    with native.Server(length, workers=3) as sv:
+        tickets, outs = [], []
+        for k, (off, x) in enumerate(wins):
+            out = np.zeros(2 * per, np.uint16)
+            tickets.append(sv.submit(k, native.PROFILE_NTSC, x, source_offset=off, seek=True, max_fields=2,
+                                     tbc_out=out, sample_rate_mhz=20.0, decimation=2))
+            outs.append(out)
+        pal_out = np.zeros(2 * 313 * 1135, np.uint16)
+        tp = sv.submit(9, native.PROFILE_PAL, pal[:length], seek=True, max_fields=2, tbc_out=pal_out)
+        res = [sv.wait(t) for t in tickets]
+        assert sv.wait(tp).fields > 0
+    with native.Session(native.PROFILE_NTSC, length, sample_rate_mhz=20.0, decimation=2) as s:
+        for (off, x), r, out in zip(wins, res, outs):
+            d = s.decode(x, max_fields=2)
+            assert r.status == 0 and r.fields == d.fields > 0
+            assert out[:d.fields * per].tobytes() == s.tbc()[:d.fields].tobytes()
+            # continuation offsets are source samples: twice the decode-rate grid
+            assert (r.next_source_offset - off) % (2 * 983040) == 0

@@ -6,7 +6,8 @@
 // that arrive while others are on the GPU are admitted as soon as a worker
 // and device memory are free and their kernels overlap on the device.
 //
-// Slots are created on demand for a (profile, tape speed, tape format, sample rate) and
+// Slots are created on demand for a (profile, tape speed, tape format, sample
+// rate, decimation) and
 // kept; a new slot is admitted only while the device-memory footprint of all
 // slots stays inside the server's budget, otherwise an idle slot of another
 // format is released or the window waits in the queue.  Windows of one
@@ -44,7 +45,7 @@ double ms_between(Clock::time_point a, Clock::time_point b) {
 
 struct Slot {
     vhsdecode_gb300_session* s = nullptr;
-    uint32_t profile = 0, speed = 0, tape_format = 0;
+    uint32_t profile = 0, speed = 0, tape_format = 0, decim = 1;
     double mhz = 0.0;
     size_t bytes = 0;
     bool busy = false;
@@ -60,7 +61,7 @@ struct Request {
 struct History {
     bool valid = false;
     FieldState state;
-    uint64_t next_abs = 0;  // absolute stitched-stream index of the next field span
+    uint64_t next_abs = 0;  // source-sample position of the next field span (stream coordinates)
     bool busy = false;
 };
 
@@ -83,9 +84,11 @@ struct vhsdecode_gb300_server {
 
 namespace {
 
+uint32_t window_decim(const vhsdecode_gb300_window_v1& w) { return w.decimation == 2 ? 2u : 1u; }
+
 bool same_format(const Slot& sl, const vhsdecode_gb300_window_v1& w) {
     return sl.profile == w.profile && sl.speed == w.tape_speed && sl.tape_format == w.tape_format &&
-           sl.mhz == w.sample_rate_mhz;
+           sl.mhz == w.sample_rate_mhz && sl.decim == window_decim(w);
 }
 
 // Device footprint of one slot, measured when the first slot of a format is
@@ -139,6 +142,7 @@ bool pick(vhsdecode_gb300_server* sv, Request& out, Slot*& slot, std::vector<Slo
             found->speed = it->w.tape_speed;
             found->tape_format = it->w.tape_format;
             found->mhz = it->w.sample_rate_mhz;
+            found->decim = window_decim(it->w);
             found->bytes = need;   // reserved now, corrected after creation
             sv->used += need;
             sv->slots.push_back(found);
@@ -163,6 +167,7 @@ void create_slot(vhsdecode_gb300_server* sv, Slot* sl) {
     c.sample_rate_mhz = sl->mhz;
     c.max_samples = sv->cfg.max_window_samples;
     c.precision = VHSDECODE_GB300_PRECISION_FP32_FUSED;
+    c.decimation = sl->decim;
     size_t f0 = 0, f1 = 0, total = 0;
     std::lock_guard<std::mutex> create_lock(sv->create_m);
     ck(cudaSetDevice(sv->cfg.device_id), "cudaSetDevice");
@@ -196,12 +201,14 @@ void destroy_slot(Slot* sl) {
 void run_window(vhsdecode_gb300_server* sv, Slot* sl, const Request& rq, History hist,
                 vhsdecode_gb300_window_result_v1& r, History& out_hist) {
     const vhsdecode_gb300_window_v1& w = rq.w;
+    // stream positions are source samples; the decode runs at source / decim
+    const uint64_t decim = window_decim(w);
     DecodeCarry carry;
     carry.no_graph = true;   // every window has its own input pointer
     bool cont = !w.seek && hist.valid && hist.next_abs >= w.source_offset;
     if (cont) {
         carry.state = hist.state;
-        carry.start = (int64_t)(hist.next_abs - w.source_offset);
+        carry.start = (int64_t)((hist.next_abs - w.source_offset) / decim);
     }
     vhsdecode_gb300_decode_result_v1 dr{};
     dr.struct_size = sizeof(dr);
@@ -218,14 +225,15 @@ void run_window(vhsdecode_gb300_server* sv, Slot* sl, const Request& rq, History
     r.first_field_is_first = (dr.fields && s->fields[0].sync.first_field) ? 1u : 0u;
     r.continued = cont ? 1u : 0u;
     // A window that starts on the stream's block and span grid (multiples of
-    // lcm(30720, 32768) = 983040 samples from where the stream began) decodes
-    // its fields exactly as one decode of the whole stream would.
+    // lcm(30720, 32768) = 983040 decoded samples from where the stream began)
+    // decodes its fields exactly as one decode of the whole stream would
+    // (decimated windows: up to the decimator's zero taps before the window).
     const int64_t grid = 983040;
     int64_t back = std::max<int64_t>(0, carry.next - 2 * kBlock);
-    r.next_source_offset = w.source_offset + (uint64_t)((back / grid) * grid);
+    r.next_source_offset = w.source_offset + decim * (uint64_t)((back / grid) * grid);
     out_hist.valid = dr.fields > 0;
     out_hist.state = carry.state;
-    out_hist.next_abs = w.source_offset + (uint64_t)std::max<int64_t>(0, carry.next);
+    out_hist.next_abs = w.source_offset + decim * (uint64_t)std::max<int64_t>(0, carry.next);
 }
 
 void worker_main(vhsdecode_gb300_server* sv) {
@@ -284,7 +292,8 @@ bool supported(const vhsdecode_gb300_window_v1& w) {
     return (w.profile == VHSDECODE_GB300_PROFILE_PAL || w.profile == VHSDECODE_GB300_PROFILE_NTSC) &&
            w.tape_speed == VHSDECODE_GB300_TAPE_SPEED_SP &&
            (w.tape_format == VHSDECODE_GB300_TAPE_FORMAT_VHS || w.tape_format == VHSDECODE_GB300_TAPE_FORMAT_SVHS) &&
-           w.sample_rate_mhz >= 10.0 && w.sample_rate_mhz <= 100.0;
+           w.sample_rate_mhz >= 10.0 && w.sample_rate_mhz <= 100.0 && w.decimation <= 2 &&
+           (w.decimation != 2 || w.sample_rate_mhz <= 50.0);
 }
 
 }  // namespace

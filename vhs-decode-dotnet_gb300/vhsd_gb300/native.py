@@ -141,7 +141,7 @@ class Window(ctypes.Structure):
                 ("sample_count", ctypes.c_uint64), ("source_offset", ctypes.c_uint64),
                 ("seek", ctypes.c_uint32), ("max_fields", ctypes.c_uint32),
                 ("tbc_out", ctypes.c_void_p), ("tbc_capacity", ctypes.c_uint64),
-                ("tape_format", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+                ("tape_format", ctypes.c_uint32), ("decimation", ctypes.c_uint32)]
 
 
 class WindowResult(ctypes.Structure):
@@ -465,13 +465,14 @@ class Server:
         self._keep = {}
 
     def submit(self, stream_id, profile, rf, source_offset=0, seek=False, max_fields=0, tbc_out=None,
-               sample_rate_mhz=40.0, tape_speed=TAPE_SP, tape_format=FORMAT_VHS):
-        """Queue a window (``rf``: int16 host array, kept alive until ``wait``); returns a ticket."""
+               sample_rate_mhz=40.0, tape_speed=TAPE_SP, tape_format=FORMAT_VHS, decimation=1):
+        """Queue a window (``rf``: int16 host array, kept alive until ``wait``); returns a ticket.
+        With ``decimation=2`` the samples run at twice ``sample_rate_mhz``."""
         rf = np.ascontiguousarray(rf, np.int16)
         w = Window(ctypes.sizeof(Window), stream_id, profile, tape_speed, float(sample_rate_mhz),
                    rf.ctypes.data, len(rf), int(source_offset), 1 if seek else 0, int(max_fields),
                    tbc_out.ctypes.data if tbc_out is not None else None,
-                   tbc_out.size if tbc_out is not None else 0, int(tape_format), 0)
+                   tbc_out.size if tbc_out is not None else 0, int(tape_format), int(decimation))
         t = ctypes.c_uint64(0)
         check(load().vhsdecode_gb300_server_submit(self._h, ctypes.byref(w), ctypes.byref(t)))
         self._keep[t.value] = (rf, tbc_out)
