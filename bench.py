@@ -299,6 +299,9 @@ def run_ours(args, world, rank, local):
         plain = {"value": round(n / (pms / 1e3) / 1e6, 3), "unit": "MSPS",
                  "ms_per_step": round(pms, 3), "ratio_fp32_over_plain": round(value / world / (n / (pms / 1e3) / 1e6), 2)}
         ps.close()
+    decimated = None
+    if rank == 0 and world == 1 and not args.skip_decimated:
+        decimated = run_decimated(args, local, rf, prof, tfmt, stream)
     cpu = None
     if rank == 0 and world == 1 and not args.skip_cpu:
         procs = os.cpu_count() or 1
@@ -334,6 +337,7 @@ def run_ours(args, world, rank, local):
                              "algorithmic_bytes": int(DEMOD_BYTES_PER_BLOCK * nblocks)},
                 "cpu_baseline": cpu,
                 "plain_fp64": plain,
+                "decimated": decimated,
                 "serving": serving,
                 "gpu_launches": int(launches),
                 "clocks": clk,
@@ -460,16 +464,50 @@ def run_serving(args, local):
             "data": "synthetic, 8-field recordings repeated to 6 s per format; TBC copied to pinned host"}
 
 
+def run_decimated(args, local, rf, prof, tfmt, stream):
+    """The same capture decoded at half its rate through the device 2:1
+    decimator (the reference's --decode-at-20msps / preview mode): whole
+    decodes from device-resident int16, source samples per second."""
+    import torch
+    from vhsd_gb300 import native
+    n = len(rf)
+    ds = native.Session(prof, n, device=local, tape_format=tfmt, sample_rate_mhz=20.0, decimation=2)
+    ds.set_stream(stream.cuda_stream)
+    d_rf = torch.from_numpy(rf).to("cuda")
+    for _ in range(3):
+        ds.decode(None, device_ptr=d_rf.data_ptr(), count=n)
+    torch.cuda.synchronize()
+    q0 = torch.cuda.Event(enable_timing=True)
+    q1 = torch.cuda.Event(enable_timing=True)
+    steps = max(1, args.steps)
+    q0.record(stream)
+    for _ in range(steps):
+        r = ds.decode(None, device_ptr=d_rf.data_ptr(), count=n)
+    q1.record(stream)
+    torch.cuda.synchronize()
+    ms = q0.elapsed_time(q1) / steps
+    ds.close()
+    return {"value": round(n / (ms / 1e3) / 1e6, 3), "unit": "MSPS (source samples)",
+            "ms_per_step": round(ms, 3), "decode_rate_mhz": 20.0, "fields": int(r.fields),
+            "kernel_launches": int(r.kernel_launches)}
+
+
 def run_profile_demod(args, local):
     """Demod-only decodes of the workload (one fused demodulator launch each),
-    for kernel captures: warm-up, then --steps decodes; prints the kernel times."""
+    for kernel captures: warm-up, then --steps decodes; prints the kernel times.
+    With --decimate the workload is tiled 3x (larger than L2) and decoded at half
+    its rate through the device decimator."""
     import torch
     from vhsd_gb300 import native
     desc, system, tape = WORKLOADS[args.workload]
     prof = native.PROFILE_PAL if system == "PAL" else native.PROFILE_NTSC
     rf = workload(args.workload)
+    extra = {}
+    if args.decimate:
+        rf = np.tile(rf, 3)
+        extra = {"sample_rate_mhz": 20.0, "decimation": 2}
     sess = native.Session(prof, len(rf), device=local,
-                          tape_format=native.FORMAT_SVHS if tape == "SVHS" else native.FORMAT_VHS)
+                          tape_format=native.FORMAT_SVHS if tape == "SVHS" else native.FORMAT_VHS, **extra)
     d_rf = torch.from_numpy(rf).to("cuda")
     for _ in range(args.warmup):
         sess.decode(None, device_ptr=d_rf.data_ptr(), count=len(rf), demod_only=True)
@@ -495,8 +533,11 @@ def main():
     ap.add_argument("--serve-rate", type=float, default=200.0, help="window arrivals per second")
     ap.add_argument("--serve-seconds", type=float, default=3.0)
     ap.add_argument("--serve-workers", type=int, default=4)
+    ap.add_argument("--skip-decimated", action="store_true")
     ap.add_argument("--profile-demod", action="store_true",
                     help="only demod-only decodes of the workload (for kernel captures)")
+    ap.add_argument("--decimate", action="store_true",
+                    help="with --profile-demod: the workload tiled 3x through the 2:1 decimator")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
