@@ -208,6 +208,7 @@ void session_init(vhsdecode_gb300_session* s, const vhsdecode_gb300_session_conf
         s->pc_counts_alt.alloc(pulse_count_slots(kSegBlocks * kStride));
         s->pc_offsets_alt.alloc(pulse_count_slots(kSegBlocks * kStride));
         s->seg_total.alloc((size_t)s->nseg_max);
+        s->blk_counters.alloc((size_t)s->nseg_max + 1);   // one per segment launch, the last for run_demod
         ck(cudaHostAlloc((void**)&s->h_events, (size_t)s->nseg_max * s->seg_cap * sizeof(int64_t),
                          cudaHostAllocDefault), "cudaHostAlloc");
         ck(cudaHostAlloc((void**)&s->h_totals, (size_t)s->nseg_max * sizeof(int64_t), cudaHostAllocDefault),
@@ -470,6 +471,7 @@ FastDemodParams fp32_params(vhsdecode_gb300_session* s, const int16_t* rf_dev) {
     p.fft_plan = s->fft_plan;
     p.rf_f32 = s->in_f32;
     if (s->in_f32) p.rf = nullptr;
+    p.block_counter = nullptr;
     p.sync_cond = s->sync_cond.p;
     p.sync_hold = s->sync_hold.p;
     p.sync_thr = pulse_float_threshold(s->sp.ire_to_hz(s->sp.vsync_ire / 2.0));
@@ -481,6 +483,8 @@ void run_demod(vhsdecode_gb300_session* s, const int16_t* rf_dev, int64_t nblock
     if (s->fp32()) {
         FastDemodParams p = fp32_params(s, rf_dev);
         p.nblocks = nblocks;
+        p.block_counter = s->blk_counters.p + s->nseg_max;
+        ck(cudaMemsetAsync(p.block_counter, 0, sizeof(unsigned), s->stream), "memset");
         ck(cudaMemsetAsync(s->repair.p, 0, sizeof(int), s->stream), "memset");
         ck(launch_demod_fp32(p, s->num_sms / 2, s->stream), "demod fp32 launch");
     } else {
@@ -838,6 +842,8 @@ void enqueue_pipeline(vhsdecode_gb300_session* s, const int16_t* rf, uint64_t n,
         p.nblocks = b1 - b0;
         const size_t half = (size_t)(s->num_sms / 2) * kBlock;
         p.scratch = s->scratch.p + (k & 1) * 2 * half;
+        p.block_counter = s->blk_counters.p + k;
+        ck(cudaMemsetAsync(p.block_counter, 0, sizeof(unsigned), ks), "memset");
         rec(s->seg_dem[(size_t)(2 * k)], ks, true);
         ck(launch_demod_fp32(p, s->num_sms / 2, ks), "demod fp32 launch");
         rec(s->seg_dem[(size_t)(2 * k + 1)], ks, true);
@@ -949,8 +955,10 @@ void decode_fp32_pipelined(vhsdecode_gb300_session* s, const int16_t* rf, uint64
                 kdone++;
             }
         };
-        // The field kernels are latency bound per field (the hsync chain walks
-        // a field's lines in order), so they run as one batch over all fields.
+        // The field kernels run as one batch over all fields after the host
+        // loop: batches launched from the host loop while the closing segments
+        // demodulate were slower (host launch and copy time lands on the
+        // field analysis, and their CTAs take SMs from the demod).
         host_field_loop<float>(s, s->s32.p, stream_len, max_fields, feed, stop, cancel, carry);
         host_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
         ck(cudaEventRecord(s->ev[2], cs), "event");

@@ -192,6 +192,7 @@ struct Shared {
     float tail_re[2][4];     // last four Re z of each local chunk
     int flag;
     int pad_;
+    long long next_blk[2];   // the cluster's next block, by iteration parity
 };
 
 // Half-spectrum post-processing of a real FFT computed as a packed complex
@@ -634,9 +635,20 @@ vhsd_demod_fp32_kernel(FastDemodParams p) {
     const bool f32_in = p.rf_f32 != nullptr;
     if (cluster_id < p.nblocks && !f32_in)
         prefetch_rf(sh.theta, p.rf + (cluster_id + p.first_block) * (int64_t)S, tid);
-    for (int64_t blk = cluster_id; blk < p.nblocks; blk += nclusters) {
-        const bool has_next = blk + nclusters < p.nblocks && !f32_in;
-        const int16_t* x_next = f32_in ? nullptr : p.rf + (blk + nclusters + p.first_block) * (int64_t)S;
+    // Blocks: each cluster starts on block cluster_id and then claims the next
+    // unclaimed block from the launch's counter, so clusters that start late
+    // (their SMs busy with other work) or take the slow repair path simply
+    // take fewer blocks.  Rank 0 claims at the top of a block and publishes the
+    // index to both CTAs (slot by iteration parity); both read it after the
+    // next cluster barrier, so the two ranks always agree.
+    int par = 0;
+    for (int64_t blk = cluster_id; blk < p.nblocks;) {
+        if (rank == 0 && tid == 0) {
+            const long long nb = p.block_counter ? (long long)nclusters + atomicAdd(p.block_counter, 1)
+                                                 : (long long)(blk + nclusters);
+            sh.next_blk[par] = nb;
+            rsh->next_blk[par] = nb;
+        }
         // ---------------- stage 1: RF forward FFT (packed, DIF split) -----
         prefetch_wait();
         __syncthreads();
@@ -659,6 +671,9 @@ vhsd_demod_fp32_kernel(FastDemodParams p) {
         __syncthreads();
         fft16384<true, PLAN>(buf, sh.tw, tid);
         cluster.sync();
+        const int64_t nxt = sh.next_blk[par];
+        const bool has_next = nxt < p.nblocks && !f32_in;
+        const int16_t* x_next = has_next ? p.rf + (nxt + p.first_block) * (int64_t)S : nullptr;
         {
             // z[n] = A[n] + W^-n B[n], z[n+16384] = A[n] - W^-n B[n]; the
             // analytic signal stays in buf (chunk rank at local 0..8191,
@@ -949,6 +964,8 @@ vhsd_demod_fp32_kernel(FastDemodParams p) {
                           });
         }
         cluster.sync();
+        blk = nxt;
+        par ^= 1;
     }
 }
 

@@ -31,6 +31,7 @@ using SubDeemph64 = SubDeemphT<double, double2>;
 struct FastDemodParams {
     const int16_t* rf;         // capture, 16-byte aligned
     const float* rf_f32;       // float capture (16-byte aligned), read instead of rf when set
+    unsigned* block_counter;   // zeroed before the launch: dynamic block claims (null: static schedule)
     int64_t first_block;       // first 32768-sample block to decode
     int64_t nblocks;           // number of blocks
     const float* rf_video;     // [kHalf] real RF band-pass gain

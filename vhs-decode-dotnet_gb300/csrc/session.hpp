@@ -174,6 +174,7 @@ struct vhsdecode_gb300_session {
     int nseg_max = 0;
     int64_t seg_cap = 0;                 // pulse events per segment
     DevBuf<int64_t> seg_events, seg_total;
+    DevBuf<unsigned> blk_counters;       // demod block claims, one counter per launch
     int64_t* h_events = nullptr;         // pinned [nseg_max * seg_cap]
     int64_t* h_totals = nullptr;         // pinned [nseg_max]
     int rescue_fetches = 0;
