@@ -265,14 +265,33 @@ void session_init(vhsdecode_gb300_session* s, const vhsdecode_gb300_session_conf
     s->pc_events.alloc(s->pc_capacity);
     s->pc_total.alloc(1);
     size_t fl = (size_t)s->max_fields * s->lines;
-    s->locs_in.alloc(fl); s->locs_out.alloc(fl);
-    s->fill_in.alloc(fl); s->fill_out.alloc(fl);
+    {
+        // per-field inputs: locs (double), spans (int64 x 2), line indices
+        // (int x 4), fill flags (uint8), each array 8-byte aligned
+        const size_t mf = (size_t)s->max_fields;
+        const size_t o_locs = 0, o_ss = o_locs + fl * 8, o_sl = o_ss + mf * 8, o_fl = o_sl + mf * 8;
+        const size_t a4 = (mf * 4 + 7) & ~(size_t)7;
+        const size_t o_st = o_fl + a4, o_el = o_st + a4, o_lo = o_el + a4, o_fill = o_lo + a4;
+        s->field_in_bytes = o_fill + ((fl + 7) & ~(size_t)7);
+        s->field_in.alloc(s->field_in_bytes);
+        ck(cudaHostAlloc((void**)&s->h_field_in, s->field_in_bytes, cudaHostAllocDefault), "cudaHostAlloc");
+        unsigned char* b = s->field_in.p;
+        s->locs_in.p = reinterpret_cast<double*>(b + o_locs);
+        s->span_start_d.p = reinterpret_cast<int64_t*>(b + o_ss);
+        s->span_len_d.p = reinterpret_cast<int64_t*>(b + o_sl);
+        s->first_line_d.p = reinterpret_cast<int*>(b + o_fl);
+        s->start_line_d.p = reinterpret_cast<int*>(b + o_st);
+        s->end_line_d.p = reinterpret_cast<int*>(b + o_el);
+        s->line_off_d.p = reinterpret_cast<int*>(b + o_lo);
+        s->fill_in.p = b + o_fill;
+        // results: refined lines, dropout counts and status, early dropout triplets
+        const size_t out_bytes = fl * 8 + mf * 8 + mf * (size_t)kDropEarly * 3 * 4;
+        ck(cudaHostAlloc((void**)&s->h_field_out, out_bytes, cudaHostAllocDefault), "cudaHostAlloc");
+    }
+    s->locs_out.alloc(fl);
+    s->fill_out.alloc(fl);
     s->hsync_work.alloc(hsync_work_bytes(s->max_fields, s->lines));
     s->hsync_misses.alloc(1);
-    s->span_start_d.alloc(s->max_fields);
-    s->span_len_d.alloc(s->max_fields);
-    s->first_line_d.alloc(s->max_fields); s->start_line_d.alloc(s->max_fields);
-    s->end_line_d.alloc(s->max_fields); s->line_off_d.alloc(s->max_fields);
     static const std::vector<float> lut = build_sinc_lut();   // built once per process
     s->lut.alloc(lut.size());
     ck(cudaMemcpy(s->lut.p, lut.data(), lut.size() * sizeof(float), cudaMemcpyHostToDevice), "upload");
@@ -322,6 +341,8 @@ void session_free(vhsdecode_gb300_session* s) {
     for (auto* v : {&s->seg_done, &s->seg_copied, &s->seg_pulsed, &s->seg_dem, &s->seg_demod_end})
         for (auto& ev : *v) if (ev) cudaEventDestroy(ev);
     if (s->h_events) cudaFreeHost(s->h_events);
+    if (s->h_field_in) cudaFreeHost(s->h_field_in);
+    if (s->h_field_out) cudaFreeHost(s->h_field_out);
     if (s->h_totals) cudaFreeHost(s->h_totals);
     if (s->copy_stream) cudaStreamDestroy(s->copy_stream);
     if (s->d2h_stream) cudaStreamDestroy(s->d2h_stream);
@@ -610,30 +631,35 @@ void launch_field_batch(vhsdecode_gb300_session* s, int f0, int f1, const T* vid
     const int nf = f1 - f0;
     if (nf <= 0) return;
     const size_t L = (size_t)s->lines;
-    std::vector<double> locs((size_t)nf * L);
-    std::vector<uint8_t> fill((size_t)nf * L);
-    std::vector<int64_t> span((size_t)nf), slens((size_t)nf);
-    std::vector<int> fline(nf), sline(nf), eline(nf), loff(nf);
+    // the pinned mirror of a device view (same offset in the field_in block)
+    auto host = [&](auto v) { return reinterpret_cast<decltype(v.p)>(s->h_field_in + ((unsigned char*)v.p - s->field_in.p)); };
+    double* locs = host(s->locs_in) + f0 * L;
+    uint8_t* fill = host(s->fill_in) + f0 * L;
+    int64_t* span = host(s->span_start_d) + f0;
+    int64_t* slens = host(s->span_len_d) + f0;
+    int* fline = host(s->first_line_d) + f0;
+    int* sline = host(s->start_line_d) + f0;
+    int* eline = host(s->end_line_d) + f0;
+    int* loff = host(s->line_off_d) + f0;
     for (int i = 0; i < nf; i++) {
         const FieldSync& fsy = s->fields[(size_t)(f0 + i)].sync;
-        std::copy(fsy.locs.begin(), fsy.locs.end(), locs.begin() + (size_t)i * L);
-        std::copy(fsy.filled.begin(), fsy.filled.end(), fill.begin() + (size_t)i * L);
-        span[(size_t)i] = s->fields[(size_t)(f0 + i)].span_start;
-        slens[(size_t)i] = s->fields[(size_t)(f0 + i)].span_len;
+        double* lr = locs + (size_t)i * L;
+        uint8_t* fr = fill + (size_t)i * L;
+        const size_t nl = std::min(L, fsy.locs.size()), nfl = std::min(L, fsy.filled.size());
+        std::copy(fsy.locs.begin(), fsy.locs.begin() + nl, lr);
+        std::fill(lr + nl, lr + L, 0.0);
+        std::copy(fsy.filled.begin(), fsy.filled.begin() + nfl, fr);
+        std::fill(fr + nfl, fr + L, (uint8_t)0);
+        span[i] = s->fields[(size_t)(f0 + i)].span_start;
+        slens[i] = s->fields[(size_t)(f0 + i)].span_len;
         fline[i] = sp.pal ? (fsy.first_field ? 3 : 4) : 1;
         loff[i] = sp.pal ? (fsy.first_field ? 2 : 3) : 0;
         sline[i] = loff[i] + 1;
         eline[i] = std::min(s->lines - 1, sp.field_lines(fsy.first_field) + sline[i] + 1);
     }
-    // pageable sources: each copy has been staged by the time the call returns
-    ck(cudaMemcpyAsync(s->locs_in.p + f0 * L, locs.data(), locs.size() * sizeof(double), cudaMemcpyHostToDevice, fs), "h2d");
-    ck(cudaMemcpyAsync(s->fill_in.p + f0 * L, fill.data(), fill.size(), cudaMemcpyHostToDevice, fs), "h2d");
-    ck(cudaMemcpyAsync(s->span_start_d.p + f0, span.data(), nf * sizeof(int64_t), cudaMemcpyHostToDevice, fs), "h2d");
-    ck(cudaMemcpyAsync(s->span_len_d.p + f0, slens.data(), nf * sizeof(int64_t), cudaMemcpyHostToDevice, fs), "h2d");
-    ck(cudaMemcpyAsync(s->first_line_d.p + f0, fline.data(), nf * sizeof(int), cudaMemcpyHostToDevice, fs), "h2d");
-    ck(cudaMemcpyAsync(s->start_line_d.p + f0, sline.data(), nf * sizeof(int), cudaMemcpyHostToDevice, fs), "h2d");
-    ck(cudaMemcpyAsync(s->end_line_d.p + f0, eline.data(), nf * sizeof(int), cudaMemcpyHostToDevice, fs), "h2d");
-    ck(cudaMemcpyAsync(s->line_off_d.p + f0, loff.data(), nf * sizeof(int), cudaMemcpyHostToDevice, fs), "h2d");
+    // one asynchronous copy of the whole block from pinned memory (the mirror
+    // is not written again before this decode's results are collected)
+    ck(cudaMemcpyAsync(s->field_in.p, s->h_field_in, s->field_in_bytes, cudaMemcpyHostToDevice, fs), "h2d");
     const int nch = dropout_chunks(s->span_len);
     DropoutParams dp{};
     dp.nfields = nf;
@@ -750,11 +776,20 @@ void launch_field_batch(vhsdecode_gb300_session* s, int f0, int f1, const T* vid
 void collect_field_results(vhsdecode_gb300_session* s, cudaStream_t fs) {
     int nf = (int)s->fields.size();
     if (nf == 0) return;
-    std::vector<double> refined((size_t)nf * s->lines);
-    std::vector<int> dcount(nf), dstat(nf);
-    ck(cudaMemcpyAsync(refined.data(), s->locs_out.p, refined.size() * sizeof(double), cudaMemcpyDeviceToHost, fs), "d2h");
-    ck(cudaMemcpyAsync(dcount.data(), s->drop_out_count.p, nf * sizeof(int), cudaMemcpyDeviceToHost, fs), "d2h");
-    ck(cudaMemcpyAsync(dstat.data(), s->drop_status.p, nf * sizeof(int), cudaMemcpyDeviceToHost, fs), "d2h");
+    const size_t L = (size_t)s->lines, mf = (size_t)s->max_fields;
+    // pinned landing area: one round trip for the refined lines, the dropout
+    // counts and status, and up to kDropEarly dropout triplets per field
+    double* refined = reinterpret_cast<double*>(s->h_field_out);
+    int* dcount = reinterpret_cast<int*>(refined + mf * L);
+    int* dstat = dcount + mf;
+    int32_t* early = dstat + mf;
+    const int ke = std::min(kDropEarly, s->drop_out_cap);
+    const size_t row = (size_t)s->drop_out_cap * 3 * sizeof(int32_t);
+    ck(cudaMemcpyAsync(refined, s->locs_out.p, (size_t)nf * L * sizeof(double), cudaMemcpyDeviceToHost, fs), "d2h");
+    ck(cudaMemcpyAsync(dcount, s->drop_out_count.p, nf * sizeof(int), cudaMemcpyDeviceToHost, fs), "d2h");
+    ck(cudaMemcpyAsync(dstat, s->drop_status.p, nf * sizeof(int), cudaMemcpyDeviceToHost, fs), "d2h");
+    ck(cudaMemcpy2DAsync(early, (size_t)ke * 3 * sizeof(int32_t), s->drop_out.p, row, (size_t)ke * 3 * sizeof(int32_t),
+                         (size_t)nf, cudaMemcpyDeviceToHost, fs), "d2h dropouts");
     ck(cudaStreamSynchronize(fs), "sync");
     int maxc = 0;
     for (int f = 0; f < nf; f++) {
@@ -762,19 +797,21 @@ void collect_field_results(vhsdecode_gb300_session* s, cudaStream_t fs) {
             throw Failure(VHSDECODE_GB300_STATUS_DECODE_ERROR, "dropout event capacity exceeded");
         maxc = std::max(maxc, std::min(dcount[f], s->drop_out_cap));
     }
-    // one strided copy of the first maxc triplets of every field
-    std::vector<int32_t> drops((size_t)nf * maxc * 3);
-    if (maxc > 0) {
-        ck(cudaMemcpy2DAsync(drops.data(), (size_t)maxc * 3 * sizeof(int32_t), s->drop_out.p,
-                             (size_t)s->drop_out_cap * 3 * sizeof(int32_t), (size_t)maxc * 3 * sizeof(int32_t),
-                             (size_t)nf, cudaMemcpyDeviceToHost, fs), "d2h dropouts");
+    // a field with more dropouts than the early copy holds: a second strided
+    // copy of the first maxc triplets of every field
+    std::vector<int32_t> late;
+    if (maxc > ke) {
+        late.resize((size_t)nf * maxc * 3);
+        ck(cudaMemcpy2DAsync(late.data(), (size_t)maxc * 3 * sizeof(int32_t), s->drop_out.p, row,
+                             (size_t)maxc * 3 * sizeof(int32_t), (size_t)nf, cudaMemcpyDeviceToHost, fs),
+           "d2h dropouts");
         ck(cudaStreamSynchronize(fs), "sync");
     }
     for (int f = 0; f < nf; f++) {
         FieldRec& r = s->fields[(size_t)f];
-        r.refined.assign(refined.begin() + (size_t)f * s->lines, refined.begin() + (size_t)(f + 1) * s->lines);
+        r.refined.assign(refined + (size_t)f * L, refined + (size_t)(f + 1) * L);
         int c = std::min(dcount[f], s->drop_out_cap);
-        const int32_t* src = drops.data() + (size_t)f * maxc * 3;
+        const int32_t* src = late.empty() ? early + (size_t)f * ke * 3 : late.data() + (size_t)f * maxc * 3;
         r.drop.assign(src, src + (size_t)c * 3);
     }
     if (s->stage_timing) {

@@ -76,6 +76,12 @@ struct DevBuf {
     ~DevBuf() { release(); }
 };
 
+// A typed pointer into a DevBuf<unsigned char> owned elsewhere.
+template <typename T>
+struct View {
+    T* p = nullptr;
+};
+
 // Identity of a captured pipeline graph: the graph bakes these in.
 struct PipeKey {
     const void* rf = nullptr;
@@ -96,6 +102,7 @@ struct FieldRec {
 
 constexpr int64_t kFirstSegBlocks = 40;   // about 1.2 M stream samples
 constexpr int64_t kSegBlocks = 128;        // about 3.9 M stream samples
+constexpr int kDropEarly = 64;             // dropout triplets per field fetched with the other results
 
 inline int64_t block_count(uint64_t n) {
     return n < (uint64_t)kBlock ? 0 : (int64_t)((n - kBlock) / kStride + 1);
@@ -105,6 +112,7 @@ inline int64_t block_count(uint64_t n) {
 }  // namespace vhsd
 
 using vhsd::detail::DevBuf;
+using vhsd::detail::View;
 using vhsd::detail::PipeKey;
 using vhsd::detail::FieldRec;
 using vhsd::FormatParams;
@@ -158,8 +166,20 @@ struct vhsdecode_gb300_session {
     DevBuf<int64_t> pc_counts, pc_offsets, pc_events, pc_total;
     DevBuf<int64_t> pc_counts_alt, pc_offsets_alt;   // scan scratch of odd segments
     int64_t pc_capacity = 0;
-    DevBuf<double> locs_in, locs_out;
-    DevBuf<uint8_t> fill_in, fill_out;
+    // the field stage's per-field inputs, carved from one device block that is
+    // filled from its pinned host mirror (same layout) by one copy per decode
+    DevBuf<unsigned char> field_in;
+    unsigned char* h_field_in = nullptr;
+    size_t field_in_bytes = 0;
+    View<double> locs_in;
+    View<uint8_t> fill_in;
+    View<int64_t> span_start_d, span_len_d;
+    View<int> first_line_d, start_line_d, end_line_d, line_off_d;
+    DevBuf<double> locs_out;
+    DevBuf<uint8_t> fill_out;
+    // pinned landing area of the field stage's results: refined lines, dropout
+    // counts and status, and the first kDropEarly dropout triplets of each field
+    unsigned char* h_field_out = nullptr;
     DevBuf<unsigned char> hsync_work;
     // pipelined FP32 decode: per-segment pulse events, pinned host copies
     cudaStream_t aux_stream = nullptr;   // rescue fetches while the session stream is busy
@@ -190,8 +210,6 @@ struct vhsdecode_gb300_session {
     float stage_ms[3] = {};
     uint32_t segments = 0;
     DevBuf<int> hsync_misses;
-    DevBuf<int64_t> span_start_d, span_len_d;
-    DevBuf<int> first_line_d, start_line_d, end_line_d, line_off_d;
     DevBuf<float> lut, lut_pair;
     DevBuf<float2> pw_ff;
     DevBuf<double> pw, level_work;
