@@ -991,14 +991,45 @@ namespace {
 
 // Per field: line factors, median / MAD outlier replacement, smoothing chain.
 // level_work per field: [2 * maxl] = (adjusted factor, value before the line)
+// Order-preserving int64 keys of doubles (ascending key = ascending value for
+// non-NaN values; -0 sorts before +0), so the median sorts compare on the
+// integer ALU instead of GB300's narrow FP64 pipe.
+__device__ __forceinline__ long long dkey(double v) {
+    const long long b = __double_as_longlong(v);
+    return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+__device__ __forceinline__ double dval(long long k) {
+    return __longlong_as_double(k ^ ((k >> 63) & 0x7fffffffffffffffLL));
+}
+
+// Bitonic sort of 512 entries: int64 keys, or (as_double) raw double bits
+// compared as doubles, the form that keeps NaN's no-swap behaviour.
+__device__ __forceinline__ void bitonic512(long long* a, bool as_double) {
+    for (int k = 2; k <= 512; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = threadIdx.x; i < 512; i += blockDim.x) {
+                int ixj = i ^ j;
+                if (ixj > i) {
+                    bool up = (i & k) == 0;
+                    long long x = a[i], y = a[ixj];
+                    bool gt = as_double ? (__longlong_as_double(x) > __longlong_as_double(y)) : (x > y);
+                    if (gt == up) { a[i] = y; a[ixj] = x; }
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
 __global__ void k_tbc_levels(TbcParams p, const double* pw_outlen) {
     __shared__ double fac[512];
-    __shared__ double srt[512];
+    __shared__ long long srt[512];
     const int f = blockIdx.x;
     const int fl = p.first_line[f];
     const int nl = fl + p.out_lines;          // lines covered by the plan incl. prefix
     const double* loc = p.locs + (int64_t)f * p.lines;
     const double inv = 1.0 / p.nominal;
+    int nan_here = 0;
     for (int l = threadIdx.x; l < 512; l += blockDim.x) {
         double v = INFINITY;
         if (l < nl) {
@@ -1006,46 +1037,26 @@ __global__ void k_tbc_levels(TbcParams p, const double* pw_outlen) {
             v = __dsub_rn(__dmul_rn(loc[left + 1], inv), __dmul_rn(loc[left], inv));
         }
         fac[l] = v;
-        srt[l] = v;
+        nan_here |= v != v;
     }
+    // a NaN factor keeps the double comparisons (and their NaN behaviour)
+    const bool as_double = __syncthreads_or(nan_here) != 0;
+    auto enc = [&](double v) { return as_double ? __double_as_longlong(v) : dkey(v); };
+    auto dec = [&](long long k) { return as_double ? __longlong_as_double(k) : dval(k); };
+    for (int l = threadIdx.x; l < 512; l += blockDim.x) srt[l] = enc(fac[l]);
     __syncthreads();
-    // bitonic sort of srt[0..512)
-    for (int k = 2; k <= 512; k <<= 1) {
-        for (int j = k >> 1; j > 0; j >>= 1) {
-            for (int i = threadIdx.x; i < 512; i += blockDim.x) {
-                int ixj = i ^ j;
-                if (ixj > i) {
-                    bool up = (i & k) == 0;
-                    double a = srt[i], b = srt[ixj];
-                    if ((a > b) == up) { srt[i] = b; srt[ixj] = a; }
-                }
-            }
-            __syncthreads();
-        }
-    }
+    bitonic512(srt, as_double);
     __shared__ double med_s, mad_s;
     if (threadIdx.x == 0) {
-        med_s = (nl & 1) ? srt[nl / 2] : (srt[nl / 2 - 1] + srt[nl / 2]) / 2.0;
+        med_s = (nl & 1) ? dec(srt[nl / 2]) : (dec(srt[nl / 2 - 1]) + dec(srt[nl / 2])) / 2.0;
     }
     __syncthreads();
     double med = med_s;
-    for (int l = threadIdx.x; l < 512; l += blockDim.x) srt[l] = l < nl ? fabs(fac[l] - med) : INFINITY;
+    for (int l = threadIdx.x; l < 512; l += blockDim.x) srt[l] = enc(l < nl ? fabs(fac[l] - med) : INFINITY);
     __syncthreads();
-    for (int k = 2; k <= 512; k <<= 1) {
-        for (int j = k >> 1; j > 0; j >>= 1) {
-            for (int i = threadIdx.x; i < 512; i += blockDim.x) {
-                int ixj = i ^ j;
-                if (ixj > i) {
-                    bool up = (i & k) == 0;
-                    double a = srt[i], b = srt[ixj];
-                    if ((a > b) == up) { srt[i] = b; srt[ixj] = a; }
-                }
-            }
-            __syncthreads();
-        }
-    }
+    bitonic512(srt, as_double);
     if (threadIdx.x == 0) {
-        mad_s = (nl & 1) ? srt[nl / 2] : (srt[nl / 2 - 1] + srt[nl / 2]) / 2.0;
+        mad_s = (nl & 1) ? dec(srt[nl / 2]) : (dec(srt[nl / 2 - 1]) + dec(srt[nl / 2])) / 2.0;
     }
     __syncthreads();
     double mad = mad_s;
@@ -1229,6 +1240,7 @@ __global__ void __launch_bounds__(kTbcFastMaxThreads) k_tbc_fast(const float* st
     const int ol = blockIdx.x;
     const int64_t s0 = p.span_start[f];
     const int64_t n = min(p.span_len[f], stream_len - s0);
+    const int n32 = (int)n;
     const float* src = stream + s0;
     const TbcLineConsts& c = *reinterpret_cast<const TbcLineConsts*>(
         p.line_consts + ((int64_t)f * p.out_lines + ol) * kTbcLineConstsBytes);
@@ -1283,10 +1295,11 @@ __global__ void __launch_bounds__(kTbcFastMaxThreads) k_tbc_fast(const float* st
 #pragma unroll
             for (int r = 0; r < 4; r++) {
                 float wt = __fmaf_rn(al_o, __fsub_rn(wev[r], wsv[r]), wsv[r]);
-                int64_t idx = (int64_t)st_o + 4 * sub + r;
+                // 32-bit tap index: a field span is far below 2^31 samples
+                int idx = st_o + 4 * sub + r;
                 if (!in_o) {
-                    if (idx < 0) idx += n;
-                    idx = idx < 0 ? 0 : (idx > n - 1 ? n - 1 : idx);
+                    if (idx < 0) idx += n32;
+                    idx = idx < 0 ? 0 : (idx > n32 - 1 ? n32 - 1 : idx);
                 }
                 float prod = __fmul_rn(__ldg(src + idx), wt);
                 float s, e;
