@@ -81,42 +81,76 @@ def profile_traffic_per_block(workload="ntsc60"):
 
 
 class ClockSampler:
+    """nvidia-smi in loop mode (every 20 ms) from start() to stop(); the
+    samples that arrive inside the windows between mark() pairs are the ones
+    reported (the timed regions)."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
     def __init__(self):
-        self.samples = []
-        self._stop = threading.Event()
+        self.samples = []          # (arrival time, fields)
+        self.windows = []
+        self._proc = None
         self._t = None
+        self._open = None
 
     def start(self):
+        try:
+            self._proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits", "-i", "0",
+                 "-lms", "20"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True, bufsize=1)
+        except Exception:
+            self._proc = None
+            return
+
         def run():
-            q = ("nvidia-smi --query-gpu=clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
-                 "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
-                 "clocks_event_reasons.sw_power_cap --format=csv,noheader,nounits -i 0")
-            while not self._stop.is_set():
-                try:
-                    out = subprocess.run(q, shell=True, capture_output=True, text=True, timeout=5).stdout
-                    line = out.strip().splitlines()[0]
-                    self.samples.append([x.strip() for x in line.split(",")])
-                except Exception:
-                    pass
-                self._stop.wait(0.2)
+            for line in self._proc.stdout:
+                self.samples.append((time.monotonic(), [x.strip() for x in line.split(",")]))
         self._t = threading.Thread(target=run, daemon=True)
         self._t.start()
 
+    def wait_first(self, timeout=3.0):
+        """Blocks until the sampler has produced a line (or timeout)."""
+        t0 = time.monotonic()
+        while self._proc is not None and not self.samples and time.monotonic() - t0 < timeout:
+            time.sleep(0.01)
+
+    def mark(self):
+        """Opens, then closes, a timed window."""
+        now = time.monotonic()
+        if self._open is None:
+            self._open = now
+        else:
+            self.windows.append((self._open, now))
+            self._open = None
+
     def stop(self):
-        self._stop.set()
+        if self._proc is not None:
+            time.sleep(0.05)
+            self._proc.terminate()
+            try:
+                self._proc.wait(timeout=5)
+            except Exception:
+                self._proc.kill()
         if self._t:
-            self._t.join(timeout=10)
-        sm = [float(s[0]) for s in self.samples if s and s[0].replace(".", "").isdigit()]
-        mx = [float(s[1]) for s in self.samples if len(s) > 1 and s[1].replace(".", "").isdigit()]
+            self._t.join(timeout=5)
+        inside = [f for (t, f) in self.samples if any(a <= t <= b for a, b in self.windows)]
+        if not inside and self.windows:   # windows shorter than the sampling period: the next sample
+            after = [f for (t, f) in self.samples if t >= self.windows[0][0]]
+            inside = after[:1]
+        sm = [float(s[0]) for s in inside if s and s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in inside if len(s) > 1 and s[1].replace(".", "").isdigit()]
         reasons = set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for s in self.samples:
+        for s in inside:
             for name, v in zip(names, s[2:6]):
                 if v.strip().lower() == "active":
                     reasons.add(name)
         return {"sm_mhz": statistics.median(sm) if sm else None,
                 "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
-                "samples": len(self.samples)}
+                "samples": len(inside), "period_ms": 20}
 
 
 def dist_init(args):
@@ -232,12 +266,13 @@ def run_ours(args, world, rank, local):
     stream = torch.cuda.current_stream()
     sess.set_stream(stream.cuda_stream)
     d_rf = torch.from_numpy(rf).to("cuda")
+    clocks = ClockSampler()
+    clocks.start()
     # device-resident value
     for _ in range(max(3, args.warmup)):
         sess.decode(None, device_ptr=d_rf.data_ptr(), count=n)
     torch.cuda.synchronize()
-    clocks = ClockSampler()
-    clocks.start()
+    clocks.wait_first()
     barrier(world)
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
@@ -245,6 +280,7 @@ def run_ours(args, world, rank, local):
     demod_ms = []
     fields = 0
     launches = 0
+    clocks.mark()
     e0.record(stream)
     for _ in range(args.steps):
         r = sess.decode(None, device_ptr=d_rf.data_ptr(), count=n)
@@ -253,6 +289,7 @@ def run_ours(args, world, rank, local):
         launches += r.kernel_launches
     e1.record(stream)
     torch.cuda.synchronize()
+    clocks.mark()
     barrier(world)
     ms = e0.elapsed_time(e1) / args.steps
     ms = max_over_ranks(ms, world, "cuda")
@@ -269,12 +306,14 @@ def run_ours(args, world, rank, local):
     barrier(world)
     f0 = torch.cuda.Event(enable_timing=True)
     f1 = torch.cuda.Event(enable_timing=True)
+    clocks.mark()
     f0.record(stream)
     for _ in range(args.steps):
         sess.decode(h_rf.numpy())
         sess.tbc_into(0, fields, h_tbc.data_ptr())
     f1.record(stream)
     torch.cuda.synchronize()
+    clocks.mark()
     clk = clocks.stop()
     e2e_ms = max_over_ranks(f0.elapsed_time(f1) / args.steps, world, "cuda")
     e2e_value = world * n / (e2e_ms / 1e3) / 1e6
@@ -523,7 +562,7 @@ def run_profile_demod(args, local):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="ntsc60", choices=sorted(WORKLOADS))
