@@ -553,25 +553,29 @@ __device__ __forceinline__ void store_thr(LineWork& w, int k, Thr<double> t) { w
 __device__ __forceinline__ Thr<float> load_thr(const LineWork& w, int k, const float*) { return {w.tlo[k], w.thi[k]}; }
 __device__ __forceinline__ Thr<double> load_thr(const LineWork& w, int k, const double*) { return {w.tlod[k], w.thid[k]}; }
 
-// 32 lines per CTA of 32 warps: warp w runs the sample searches and
-// reductions of line w (the 32 lines proceed concurrently); warp 0 runs the
-// binary64 arithmetic of all 32 lines lane-parallel between the phases.
+// kHsyncLines lines per CTA, one warp each: warp w runs the sample searches
+// and reductions of line w (the lines proceed concurrently); lanes
+// 0..kHsyncLines-1 of warp 0 run the binary64 arithmetic of the CTA's lines
+// lane-parallel between the phases.  16 lines per CTA keep four CTAs per SM,
+// so one CTA's searches overlap another's binary64 steps.
 // Per line: threshold crossing from round(loc - 1 us), area and level checks,
 // own-porch midpoint crossing, and the right-edge candidate -- the per-line
 // part of RefineLineLocationsFromHSync.
+constexpr int kHsyncLines = 16;
+
 template <typename T>
-__global__ void __launch_bounds__(1024) k_hsync_lines(const T* stream, int64_t stream_len, HsyncParams p,
-                                                      LineInfo* info) {
-    __shared__ LineWork lw[32];
+__global__ void __launch_bounds__(32 * kHsyncLines) k_hsync_lines(const T* stream, int64_t stream_len,
+                                                                  HsyncParams p, LineInfo* info) {
+    __shared__ LineWork lw[32];   // entries kHsyncLines.. are written by idle lanes of warp 0 only
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t total = (int64_t)p.nfields * p.lines;
     const int one = p.one_us, normal = p.normal_hsync;
     const int search = one * 2 > 1 ? one * 2 : 1;
     auto ire_hz = [&](double ire) { return p.ire0 + p.hz_ire * ire; };
     const Thr<T> th0 = make_thr(p.threshold, (const T*)nullptr);
-    // warp 0, lane l <-> line g = 32 blockIdx + l
-    const int64_t g = (int64_t)blockIdx.x * 32 + lane;
-    const bool have = g < total;
+    // warp 0, lane l <-> line g = kHsyncLines blockIdx + l
+    const int64_t g = (int64_t)blockIdx.x * kHsyncLines + lane;
+    const bool have = lane < kHsyncLines && g < total;
     LineInfo li;
     double crossing = NAN, rcx = NAN, target_own = 0.0, target_r = 0.0, r_porch = 0.0;
     int flags = 0;
@@ -973,7 +977,8 @@ cudaError_t launch_hsync_refine(const T* stream, int64_t stream_len, const Hsync
     const int threads = 1024;
     const unsigned blocks = (unsigned)((lines + 31) / 32);
     LineInfo* info = reinterpret_cast<LineInfo*>(p.work);
-    k_hsync_lines<T><<<blocks, threads, 0, s>>>(stream, stream_len, p, info);
+    k_hsync_lines<T><<<(unsigned)((lines + kHsyncLines - 1) / kHsyncLines), 32 * kHsyncLines, 0, s>>>(
+        stream, stream_len, p, info);
     k_hsync_spec<T><<<blocks, threads, 0, s>>>(stream, stream_len, p, info);
     k_hsync_chain<T><<<p.nfields, 32 * kChainWarps, p.lines * sizeof(LineInfo), s>>>(stream, stream_len, p,
                                                                                      info, p.misses);
