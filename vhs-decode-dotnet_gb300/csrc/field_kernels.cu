@@ -1026,7 +1026,7 @@ __device__ __forceinline__ void bitonic512(long long* a, bool as_double) {
     }
 }
 
-__global__ void k_tbc_levels(TbcParams p, const double* pw_outlen) {
+__global__ void __launch_bounds__(512) k_tbc_levels(TbcParams p, const double* pw_outlen) {
     __shared__ double fac[512];
     __shared__ long long srt[512];
     const int f = blockIdx.x;
@@ -1071,17 +1071,44 @@ __global__ void k_tbc_levels(TbcParams p, const double* pw_outlen) {
         fac[l] = fabs(v - med) > thr ? med : v;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        double* w = p.level_work + (int64_t)f * 1024;
-        double prev = fac[0];
-        double rN = pw_outlen ? pw_outlen[p.outlen - 1] : 1.0;  // (1-alpha)^outlen
-        for (int l = 0; l < nl; l++) {
-            double a = fac[l];
-            w[2 * l] = a;
-            w[2 * l + 1] = (l == 0) ? a : prev;
-            if (p.smoothing > 0.0 && l > 0) prev = a + rN * (prev - a);
-            else prev = a;
+    // Line-rate smoothing chain: prev_0 = a_0, prev_l = a_l + rN (prev_{l-1} - a_l)
+    // (rN = (1 - alpha)^outlen, the per-sample chain of the reference over one
+    // line in closed form, like the per-sample levels in the TBC kernels), as an
+    // inclusive scan of the affine maps x -> rN x + (1 - rN) a_l: 9 dependent
+    // steps instead of one binary64 chain through every line (a few ulps of
+    // double from the sequential order, far below the float rounding of the
+    // levels' use).  One thread per line slot (512 threads).
+    __shared__ double sm_m[512], sm_c[512];
+    const bool smooth = p.smoothing > 0.0;
+    const double rN = pw_outlen ? pw_outlen[p.outlen - 1] : 1.0;   // (1-alpha)^outlen
+    const int l = threadIdx.x;
+    double m = 1.0, c = 0.0;                                        // identity at l = 0 and past nl
+    if (l >= 1 && l < nl) { m = rN; c = __dmul_rn(__dsub_rn(1.0, rN), fac[l]); }
+    sm_m[l] = m;
+    sm_c[l] = c;
+    __syncthreads();
+    for (int d = 1; d < 512; d <<= 1) {
+        double pm = 1.0, pc = 0.0;
+        if (l >= d) { pm = sm_m[l - d]; pc = sm_c[l - d]; }
+        __syncthreads();
+        if (l >= d) {
+            c = __fma_rn(m, pc, c);
+            m = __dmul_rn(m, pm);
+            sm_m[l] = m;
+            sm_c[l] = c;
         }
+        __syncthreads();
+    }
+    // prev_l = m_l a_0 + c_l (the composition of the maps 1..l applied to a_0)
+    if (l < nl) {
+        double* w = p.level_work + (int64_t)f * 1024;
+        const double a0 = fac[0];
+        double before;
+        if (l == 0) before = a0;
+        else if (!smooth) before = fac[l - 1];
+        else before = l == 1 ? a0 : __fma_rn(sm_m[l - 1], a0, sm_c[l - 1]);
+        w[2 * l] = fac[l];
+        w[2 * l + 1] = before;
     }
 }
 
@@ -1364,7 +1391,7 @@ template <typename T>
 cudaError_t launch_tbc_pw(const T* stream, int64_t stream_len, const TbcParams& p, const double* pw,
                           cudaStream_t s) {
     if (p.nfields <= 0) return cudaSuccess;
-    k_tbc_levels<<<p.nfields, 256, 0, s>>>(p, pw);
+    k_tbc_levels<<<p.nfields, 512, 0, s>>>(p, pw);   // one compare-exchange per thread per sort stage
     dim3 grid(p.out_lines, p.nfields);
     if (sizeof(T) == sizeof(float) && p.out_u16 && !p.out_hz && (p.smoothing <= 0.0 || p.pw_ff) &&
         p.line_consts) {
