@@ -148,3 +148,22 @@ def test_run_input_formats_and_half_rate(gpu, ntsc_capture, tmp_path):
     assert h.fields_written == 2
     assert (h.output_line_length, h.output_field_lines) == (910, 263)
     assert os.path.getsize(tmp_path / "half.tbc") == 2 * 910 * 263 * 2
+    # the metadata keys of the cuda-fast writer (tbc_writer.cpp:209-310)
+    import json
+    for base, res in (("s16", b), ("half", h)):
+        meta = json.loads((tmp_path / (base + ".tbc.json")).read_text())
+        vp = meta["videoParameters"]
+        assert vp["system"] == "NTSC" and vp["isSourcePal"] is False and vp["tapeFormat"] == "VHS"
+        assert vp["numberOfSequentialFields"] == res.fields_written == len(meta["fields"])
+        assert (vp["fieldWidth"], vp["fieldHeight"]) == (910, 263)
+        assert (vp["colourBurstStart"], vp["colourBurstEnd"]) == (76, 112)
+        assert (vp["activeVideoStart"], vp["activeVideoEnd"]) == (134, 894)
+        assert vp["sampleRate"] == 14318182 and vp["black16bIre"] < vp["white16bIre"]
+        for k, fld in enumerate(meta["fields"]):
+            assert fld["seqNo"] == k + 1 and isinstance(fld["isFirstField"], bool)
+            d = fld["dropOuts"]
+            assert len(d["fieldLine"]) == len(d["startx"]) == len(d["endx"])
+        locs = [fld["fileLoc"] for fld in meta["fields"]]
+        assert locs == sorted(locs)
+        assert [f["isFirstField"] for f in meta["fields"][:2]] != [True, True]
+    assert not (tmp_path / "s16.tbc.json.tmp").exists()

@@ -1192,36 +1192,57 @@ bool file_exists(const std::string& path) {
     return false;
 }
 
+// The cuda-fast backend's metadata file (src/VHSDecode.CudaFast.Native/src/tbc_writer.cpp:209-310):
+// the same keys and number formats, written to a temporary file and renamed
+// into place.  Levels carry the writer's default 10 % adjust; the burst window
+// comes from the format's colorBurstUS, the active video window is the
+// writer's per-system constant.
 void write_json(const std::string& path, const vhsdecode_gb300_session* s) {
-    FILE* f = std::fopen(path.c_str(), "wb");
-    if (!f) throw Failure(VHSDECODE_GB300_STATUS_OUTPUT_ERROR, "cannot open " + path);
+    const std::string tmp = path + ".tmp";
+    FILE* f = std::fopen(tmp.c_str(), "wb");
+    if (!f) throw Failure(VHSDECODE_GB300_STATUS_OUTPUT_ERROR, "cannot open " + tmp);
     const FormatParams& fm = s->fmt;
-    std::fprintf(f, "{\n  \"videoParameters\": {\"system\": \"%s\", \"fieldWidth\": %d, "
-                    "\"fieldHeight\": %d, \"sampleRate\": %.1f, \"numberOfSequentialFields\": %zu, "
-                    "\"isSourcePal\": %s, \"black16bIre\": %d, \"white16bIre\": %d},\n  \"fields\": [",
-                 fm.pal ? "PAL" : "NTSC", s->outlen, s->out_lines, fm.outfreq_mhz * 1e6, s->fields.size(),
-                 fm.pal ? "true" : "false",
-                 (int)std::lround(fm.output_zero + (0.0 - fm.vsync_ire) * output_scale(fm)),
-                 (int)std::lround(fm.output_zero + (100.0 - fm.vsync_ire) * output_scale(fm)));
+    const double scale = output_scale(fm), rate = fm.outfreq_mhz * 1e6;
+    const double level_adjust = 0.1;
+    const double black16 = ((0.0 - fm.vsync_ire) * scale + fm.output_zero) * (1.0 - level_adjust);
+    const double white16 = ((100.0 - fm.vsync_ire) * scale + fm.output_zero) * (1.0 + level_adjust);
+    const int burst_start = (int)(fm.burst_start_us * 1e-6 * rate + 0.5);
+    const int burst_end = (int)(fm.burst_end_us * 1e-6 * rate + 0.5);
+    const int active_start = fm.pal ? 185 : 134, active_end = fm.pal ? 1107 : 894;
+    std::fprintf(f, "{\n  \"videoParameters\": {\n");
+    std::fprintf(f, "    \"system\": \"%s\",\n", fm.pal ? "PAL" : "NTSC");
+    std::fprintf(f, "    \"isSubcarrierLocked\": false,\n");
+    std::fprintf(f, "    \"isSourcePal\": %s,\n", fm.pal ? "true" : "false");
+    std::fprintf(f, "    \"numberOfSequentialFields\": %zu,\n", s->fields.size());
+    std::fprintf(f, "    \"black16bIre\": %.1f,\n", black16);
+    std::fprintf(f, "    \"white16bIre\": %.1f,\n", white16);
+    std::fprintf(f, "    \"sampleRate\": %.0f,\n", rate);
+    std::fprintf(f, "    \"fieldWidth\": %d,\n", s->outlen);
+    std::fprintf(f, "    \"fieldHeight\": %d,\n", s->out_lines);
+    std::fprintf(f, "    \"colourBurstStart\": %d,\n", burst_start);
+    std::fprintf(f, "    \"colourBurstEnd\": %d,\n", burst_end);
+    std::fprintf(f, "    \"activeVideoStart\": %d,\n", active_start);
+    std::fprintf(f, "    \"activeVideoEnd\": %d,\n", active_end);
+    std::fprintf(f, "    \"tapeFormat\": \"%s\",\n", fm.custom_luma_table ? "SVHS" : "VHS");
+    std::fprintf(f, "    \"isMapped\": false\n  },\n  \"fields\": [\n");
     for (size_t i = 0; i < s->fields.size(); i++) {
         const FieldRec& r = s->fields[i];
         long long file_loc = (long long)std::floor(r.span_start + r.sync.line0 + kCut);
-        std::fprintf(f, "%s\n    {\"seqNo\": %zu, \"isFirstField\": %s, \"fileLoc\": %lld",
-                     i ? "," : "", i + 1, r.sync.first_field ? "true" : "false", file_loc);
-        size_t nd = r.drop.size() / 3;
-        if (nd) {
-            std::fprintf(f, ", \"dropOuts\": {\"fieldLine\": [");
-            for (size_t k = 0; k < nd; k++) std::fprintf(f, "%s%d", k ? ", " : "", r.drop[3 * k]);
-            std::fprintf(f, "], \"startx\": [");
-            for (size_t k = 0; k < nd; k++) std::fprintf(f, "%s%d", k ? ", " : "", r.drop[3 * k + 1]);
-            std::fprintf(f, "], \"endx\": [");
-            for (size_t k = 0; k < nd; k++) std::fprintf(f, "%s%d", k ? ", " : "", r.drop[3 * k + 2]);
-            std::fprintf(f, "]}");
-        }
-        std::fprintf(f, "}");
+        std::fprintf(f, "    {\n      \"isFirstField\": %s,\n      \"seqNo\": %zu,\n      \"fileLoc\": %lld,\n",
+                     r.sync.first_field ? "true" : "false", i + 1, file_loc);
+        const size_t nd = r.drop.size() / 3;
+        std::fprintf(f, "      \"dropOuts\": {\n        \"fieldLine\": [");
+        for (size_t k = 0; k < nd; k++) std::fprintf(f, "%s%d", k ? ", " : "", r.drop[3 * k]);
+        std::fprintf(f, "],\n        \"startx\": [");
+        for (size_t k = 0; k < nd; k++) std::fprintf(f, "%s%d", k ? ", " : "", r.drop[3 * k + 1]);
+        std::fprintf(f, "],\n        \"endx\": [");
+        for (size_t k = 0; k < nd; k++) std::fprintf(f, "%s%d", k ? ", " : "", r.drop[3 * k + 2]);
+        std::fprintf(f, "]\n      }\n    }%s\n", i + 1 < s->fields.size() ? "," : "");
     }
-    std::fprintf(f, "\n  ]\n}\n");
-    if (std::fclose(f) != 0) throw Failure(VHSDECODE_GB300_STATUS_OUTPUT_ERROR, "cannot write " + path);
+    std::fprintf(f, "  ]\n}\n");
+    if (std::fclose(f) != 0) throw Failure(VHSDECODE_GB300_STATUS_OUTPUT_ERROR, "cannot write " + tmp);
+    if (std::rename(tmp.c_str(), path.c_str()) != 0)
+        throw Failure(VHSDECODE_GB300_STATUS_OUTPUT_ERROR, "cannot rename " + tmp);
 }
 
 }  // namespace detail

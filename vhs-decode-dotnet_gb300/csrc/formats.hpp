@@ -18,6 +18,7 @@ struct FormatParams {
     double hsync_us, eq_us, vsync_us;
     int num_pulses, outlinelen, frame_lines, output_zero;
     double outfreq_mhz, fsc_mhz;
+    double burst_start_us, burst_end_us;   // sysparams colorBurstUS (TBC metadata)
     // RF video band-pass
     double bpf_low, bpf_high;
     int bpf_order;                // 0 = none (magnitude path), >0 Butterworth band-pass
@@ -56,6 +57,7 @@ inline FormatParams pal_vhs_sp() {
     f.line_period_us = 64.0; f.hsync_us = 4.7; f.eq_us = 2.35; f.vsync_us = 27.3;
     f.num_pulses = 5; f.outlinelen = 1135; f.frame_lines = 625; f.output_zero = 256;
     f.outfreq_mhz = 17.734475; f.fsc_mhz = 4.43361875;
+    f.burst_start_us = 5.6; f.burst_end_us = 7.85;
     f.bpf_low = 1300000.0; f.bpf_high = 5780000.0; f.bpf_order = 0;
     f.lpf_extra = 5910000.0; f.lpf_extra_order = 20;
     f.hpf_extra = 1320000.0; f.hpf_extra_order = 12;
@@ -75,6 +77,7 @@ inline FormatParams ntsc_vhs_sp() {
     f.vsync_ire = -40.0; f.line_period_us = 63.55555555555555; f.hsync_us = 4.7; f.eq_us = 2.3;
     f.vsync_us = 27.1; f.num_pulses = 6; f.outlinelen = 910; f.frame_lines = 525;
     f.output_zero = 1024; f.outfreq_mhz = 14.318181818181818; f.fsc_mhz = 3.5795454545454546;
+    f.burst_start_us = 5.3; f.burst_end_us = 7.8;
     f.bpf_low = 500000.0; f.bpf_high = 6500000.0; f.bpf_order = 8;
     f.lpf_extra = 6000000.0; f.lpf_extra_order = 25;
     f.hpf_extra = 1200000.0; f.hpf_extra_order = 20;
