@@ -167,3 +167,6 @@ def test_run_input_formats_and_half_rate(gpu, ntsc_capture, tmp_path):
         assert locs == sorted(locs)
         assert [f["isFirstField"] for f in meta["fields"][:2]] != [True, True]
     assert not (tmp_path / "s16.tbc.json.tmp").exists()
+    # neutral chroma in the luma geometry (the managed finalisation truncates both files)
+    chroma = np.fromfile(tmp_path / "half_chroma.tbc", np.uint16)
+    assert chroma.size == 2 * 910 * 263 and np.all(chroma == 32767)

@@ -1324,8 +1324,8 @@ VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_run(
         const size_t esz = f32_in ? sizeof(float) : sizeof(int16_t);
         auto t0 = std::chrono::steady_clock::now();
         std::string base = config->output_base_utf8;
-        std::string tbc_path = base + ".tbc", json_path = base + ".tbc.json";
-        if (!config->overwrite && (file_exists(tbc_path) || file_exists(json_path)))
+        std::string tbc_path = base + ".tbc", json_path = base + ".tbc.json", chroma_path = base + "_chroma.tbc";
+        if (!config->overwrite && (file_exists(tbc_path) || file_exists(json_path) || file_exists(chroma_path)))
             return fail(VHSDECODE_GB300_STATUS_OUTPUT_ERROR, "output exists and overwrite is off");
         auto cancelled = [&]() { return config->cancel_callback && config->cancel_callback(config->user_data) != 0; };
         // pull the capture through the callback (source samples of esz bytes)
@@ -1374,6 +1374,21 @@ VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_run(
         size_t wrote = tbc.empty() ? 0 : std::fwrite(tbc.data(), sizeof(uint16_t), tbc.size(), f);
         int cerr = std::fclose(f);
         if (wrote != tbc.size() || cerr != 0) return fail(VHSDECODE_GB300_STATUS_OUTPUT_ERROR, "cannot write " + tbc_path);
+        {
+            // Chroma is not decoded by this backend: the chroma file carries
+            // neutral chroma (zero chroma + 32767, VhsChromaDecoder.ChromaToU16,
+            // Core/Decode/VhsChromaDecoder.cs:455-500) in the luma file's
+            // geometry, which the managed finalisation opens and truncates
+            // with it (Core/Dsp/CudaFast/CudaFastDecodeRunner.cs:345,427).
+            FILE* fc = std::fopen(chroma_path.c_str(), "wb");
+            if (!fc) return fail(VHSDECODE_GB300_STATUS_OUTPUT_ERROR, "cannot open " + chroma_path);
+            std::vector<uint16_t> neutral(per, (uint16_t)32767);
+            bool ok = true;
+            for (size_t k = 0; k < h.s->fields.size() && ok; k++)
+                ok = std::fwrite(neutral.data(), sizeof(uint16_t), per, fc) == per;
+            if (std::fclose(fc) != 0 || !ok)
+                return fail(VHSDECODE_GB300_STATUS_OUTPUT_ERROR, "cannot write " + chroma_path);
+        }
         write_json(json_path, h.s);
         result->fields_written = (uint32_t)h.s->fields.size();
         result->output_line_length = (uint32_t)h.s->outlen;
