@@ -902,7 +902,7 @@ __device__ __forceinline__ void chain_step(const LineInfo& li, ChainState& cs, c
 // warp 0 compares each guess with the state the previous segment actually
 // left and re-walks the segments whose guess differed, in order.  The result
 // is the sequential walk's, bit for bit.
-constexpr int kChainWarps = 8;
+constexpr int kChainWarps = 16;
 constexpr int kChainWarm = 12;
 
 template <typename T>
