@@ -420,6 +420,8 @@ VHSDECODE_GB300_API void VHSDECODE_GB300_CALL vhsdecode_gb300_server_destroy(vhs
  * written).  `stream` is a cudaStream_t (NULL = legacy default stream).
  * Limit: length <= 16777216 samples, else INVALID_ARGUMENT.  The first call on
  * a device sets up its fixed scratch: make it before capturing a stream.
+ * Every call outside a stream capture looks the scratch address up again, so
+ * a context recreated after cudaDeviceReset is followed.
  * Calls on one device share that scratch and must not overlap. */
 VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_pulse_events_noalloc(
     const float* sync, int64_t length, double high, int64_t* events, int64_t capacity,

@@ -109,6 +109,82 @@ def demod_block(x, filters, fs, diff_max, return_debug=False):
     return video, vlp, envelope, weak, dbg
 
 
+def unwrap_conjugate_product(z, fs):
+    """``PortedMath.UnwrapHilbertConjugateProduct`` (Core/Dsp/PortedMath.cs:38-68): binary64
+    atan2 of z[i]·conj(z[i-1]), wrapped into [0, 2π), times fs/2π; output[0] = 0."""
+    z = np.asarray(z, np.complex128)
+    out = np.zeros(len(z))
+    if len(z) < 2:
+        return out
+    cr, ci = z.real[1:], z.imag[1:]
+    pr, pi = z.real[:-1], z.imag[:-1]
+    re = (cr * pr) + (ci * pi)
+    im = (ci * pr) - (cr * pi)
+    d = np.arctan2(im, re)
+    d = np.where(d < 0.0, d + 2.0 * np.pi, d)
+    out[1:] = d * (fs / (2.0 * np.pi))
+    return out
+
+
+def clip_demod_for_video(demod, fs):
+    """``RfDemodulator.ClipDemodForVideo`` (Core/Dsp/RfDemodulator.cs:1891-1901)."""
+    return np.clip(np.asarray(demod, np.float64), 1_500_000.0, fs * 0.75)
+
+
+def demod_block_complex(x, rf_video, video_filter, video_lp, fs, video_lp_offset=0,
+                        rf_mtf=None, clip_for_video=False):
+    """The full-spectrum (non-VHS, conjugate-product) branch of ``RfDemodulator.DemodulateCore``
+    (Core/Dsp/RfDemodulator.cs:564-605, 756, 779-784, 814-833, 858-874): complex FFT of the
+    block × RfVideo (× MTF) × Hilbert → inverse = analytic; FP64 conjugate-product FM demod;
+    envelope |analytic|; video and sync reference as real parts of complex-spectrum inverses;
+    the sync reference rolled by −offset.  Returns (video, demod_raw, analytic, envelope, vlp)."""
+    x = np.asarray(x, np.float64)
+    n = len(x)
+    spec = np.fft.fft(x) * np.asarray(rf_video, np.complex128)
+    if rf_mtf is not None:
+        spec = spec * np.asarray(rf_mtf, np.complex128)
+    hilbert = np.zeros(n)
+    hilbert[0] = 1.0
+    if n % 2 == 0:
+        hilbert[n // 2] = 1.0
+        hilbert[1:n // 2] = 2.0
+    else:
+        hilbert[1:(n + 1) // 2] = 2.0
+    analytic = np.fft.ifft(spec * hilbert)
+    demod_raw = unwrap_conjugate_product(analytic, fs)
+    envelope = np.abs(analytic)
+    source = clip_demod_for_video(demod_raw, fs) if clip_for_video else demod_raw
+    dspec = np.fft.fft(source)
+    video = np.fft.ifft(dspec * np.asarray(video_filter, np.complex128)).real
+    vlp = np.fft.ifft(dspec * np.asarray(video_lp, np.complex128)).real
+    if video_lp_offset:
+        vlp = np.roll(vlp, -video_lp_offset)
+    return video, demod_raw, analytic, envelope, vlp
+
+
+def stitch_span(rf, block_fn, block_len, cut, cut_end, begin, length):
+    """Overlap-save read of stream samples [begin, begin+length) (``RfBlockStreamDecoder.ReadCore`` /
+    ``CopyTrimmedWindow``, Core/Decode/RfBlockStreamDecoder.cs:418-560, 1586-1610).
+
+    Block b processes RF [b·S, b·S+N) with S = N − cut − cut_end and contributes its samples
+    [cut, cut+S) to stream [b·S, b·S+S), so stream sample s is block-local sample
+    s − b·S + cut and lines up with RF sample s + cut.  ``block_fn`` maps one RF block to a tuple
+    of equal-length channels; returns the stitched channels."""
+    stride = block_len - cut - cut_end
+    first = begin // stride
+    last = (begin + length - 1) // stride
+    out = None
+    for b in range(first, last + 1):
+        chans = block_fn(np.asarray(rf[b * stride: b * stride + block_len], np.float64))
+        if out is None:
+            out = [np.empty(length) for _ in chans]
+        lo = max(begin, b * stride)
+        hi = min(begin + length, (b + 1) * stride)
+        for o, c in zip(out, chans):
+            o[lo - begin:hi - begin] = c[lo - b * stride + cut: hi - b * stride + cut]
+    return out
+
+
 def block_count(total_samples):
     """Number of whole 32768-sample blocks a capture of ``total_samples`` RF samples holds."""
     if total_samples < BLOCK:

@@ -37,6 +37,7 @@ def lib():
         L.oracle_vhs_rust_angles.argtypes = [_fp, _fp, ctypes.c_int64, _fp]
         L.oracle_vhs_envelope.argtypes = [_dp, ctypes.c_int64, ctypes.c_double, ctypes.c_double,
                                           ctypes.c_double, _dp, _fp]
+        L.oracle_vhs_raw_envelope.argtypes = [_dp, ctypes.c_int64, _fp]
         L.oracle_filtfilt1_f64.argtypes = [_dp, ctypes.c_int64, ctypes.c_double, ctypes.c_double,
                                            ctypes.c_double, _dp, _dp]
         L.oracle_find_pulses.argtypes = [_dp, ctypes.c_int64, ctypes.c_double, ctypes.c_int64,
@@ -83,6 +84,13 @@ def vhs_envelope(filtered, b0, b1, a1):
     work = np.empty(len(filtered) + 12, np.float32)
     lib().oracle_vhs_envelope(ptr(filtered, _dp), len(filtered), b0, b1, a1, ptr(out, _dp),
                               ptr(work, _fp))
+    return out
+
+
+def vhs_raw_envelope(filtered):
+    filtered = np.ascontiguousarray(filtered, np.float64)
+    out = np.empty(len(filtered), np.float32)
+    lib().oracle_vhs_raw_envelope(ptr(filtered, _dp), len(filtered), ptr(out, _fp))
     return out
 
 

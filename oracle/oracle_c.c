@@ -70,16 +70,24 @@ void oracle_vhs_rust_angles(const float *re, const float *im, int64_t n, float *
  * steady-state zi scaled by the first / last extended value, float32 DF2T.
  * `work` must hold n + 12 floats.
  */
+/* RfDemodulator.BuildVhsRawEnvelope / FillVhsRawEnvelope (Core/Dsp/RfDemodulator.cs:1784-1839):
+ * raw[(i + 4) mod n] = |float(filtered[i])|. */
+void oracle_vhs_raw_envelope(const double *filtered, int64_t n, float *raw)
+{
+    if (n <= 0) return;
+    int64_t shift = 4 % n;
+    int64_t split = n - shift;
+    for (int64_t i = 0; i < split; i++) raw[i + shift] = fabsf((float)filtered[i]);
+    for (int64_t w = split; w < n; w++) raw[w - split] = fabsf((float)filtered[w]);
+}
+
 void oracle_vhs_envelope(const double *filtered, int64_t n, double b0d, double b1d,
                          double a1d, double *out, float *work)
 {
     const int edge = 6;
-    int64_t shift = 4 % n;
-    int64_t split = n - shift;
     float *ext = work;
     float *raw = work + edge;  /* raw occupies ext[edge .. edge+n) */
-    for (int64_t i = 0; i < split; i++) raw[i + shift] = fabsf((float)filtered[i]);
-    for (int64_t w = split; w < n; w++) raw[w - split] = fabsf((float)filtered[w]);
+    oracle_vhs_raw_envelope(filtered, n, raw);
     /* odd extension (float32 form reading the float raw values) */
     float first = raw[0];
     float tmp_left[6], tmp_right[6];

@@ -83,12 +83,20 @@ def in_range(v, lo, hi):
     return lo <= v <= hi
 
 
-def estimate_timing(sp, raw):
-    """``SyncAnalyzer.EstimateTiming`` with the VHS empty-median unit quirk (SyncAnalysis.cs:131-167)."""
+def estimate_timing(sp, raw, vhs_empty_median_units=True):
+    """``SyncAnalyzer.EstimateTiming`` (SyncAnalysis.cs:131-167).
+
+    The VHS field path passes ``preserveVhsEmptyHSyncMedianUnits``: with no
+    hsync-length candidate the median falls back to the pulse width in
+    microseconds, not samples.  ``vhs_empty_median_units=False`` is the
+    analyser's default (samples)."""
     lo = sp.usec(sp.hsync_us - 1.75)
     hi = sp.usec(sp.hsync_us + 2.0)
     lens = [ln for (_, ln) in raw if in_range(ln, lo, hi)]
-    med = np_median(lens) if lens else sp.hsync_us
+    if lens:
+        med = np_median(lens)
+    else:
+        med = sp.hsync_us if vhs_empty_median_units else sp.usec(sp.hsync_us)
     off = med - sp.usec(sp.hsync_us)
     return {
         "hsync": (med - sp.usec(sp.hsync_tol), med + sp.usec(sp.hsync_tol)),
@@ -240,7 +248,7 @@ def refine_pulses(sp, raw, timing, ref, rescue_step_hz):
 
 
 def mean_line_length(sp, pulses):
-    """``SyncAnalyzer.ComputeMeanLineLength`` (SyncAnalysis.cs:456-500)."""
+    """``SyncAnalyzer.ComputeMeanLineLength`` (SyncAnalysis.cs:490-538)."""
     run_start, run_len, cur_start, cur_len = -1, -1, -1, 0
     for i, p in enumerate(pulses):
         if p[0] != HSYNC:
@@ -457,8 +465,12 @@ def resolve_cadence(sp, pulses, mll, previous_first, min_conf, has_previous_hsyn
     return first
 
 
-def build_upstream_line_locations(pulses, ref_pulse, ref_line, mll, processed):
-    """``SyncAnalyzer.BuildUpstreamLineLocations`` (SyncAnalysis.cs:551-614)."""
+def build_upstream_line_locations(pulses, ref_pulse, ref_line, mll, processed, prefer_earlier=False):
+    """``SyncAnalyzer.BuildUpstreamLineLocations`` (SyncAnalysis.cs:585-660).
+
+    ``prefer_earlier`` is ``preferEarlierPulseOnEqualDistance``, which only the
+    PAL CVBS line-0 anchor sets (TbcFieldDecodePipeline.cs:1286-1294); VHS
+    leaves it off."""
     locs_p = sorted(float(p[1]) for p in pulses)
     out = [0.0] * processed
     cur = 0
@@ -478,7 +490,7 @@ def build_upstream_line_locations(pulses, ref_pulse, ref_line, mll, processed):
                 cur = si
                 sel = locs_p[si]
             nd = abs(locs_p[si + 1] - expected)
-            if nd > cd:
+            if nd > cd or (prefer_earlier and nd == cd):
                 break
             cd = nd
             si += 1

@@ -1,8 +1,8 @@
 """Regenerate the golden fixtures in this folder from the reference checkout.
 
-Run in a container that has the reference at REFERENCE_ROOT (default
-/root/reference); the outputs are committed so nothing reads the reference at
-test time.
+Run with the reference checkout given as the first argument or in the
+REFERENCE_ROOT environment variable; the outputs are committed so nothing
+reads the reference at test time.
 
 * format_params.json: the keys of the frozen upstream parameter snapshot
   (src/VHSDecode.Core/Formats/format-params.snapshot.json) that the RF -> TBC
@@ -22,7 +22,9 @@ import sys
 
 import numpy as np
 
-REF = os.environ.get("REFERENCE_ROOT", "/root/reference")
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("REFERENCE_ROOT")
+if not REF or not os.path.isdir(REF):
+    sys.exit("usage: %s REFERENCE_ROOT (or set REFERENCE_ROOT)" % os.path.basename(__file__))
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 SYS_KEYS = ["FPS", "ire0", "hz_ire", "vsync_ire", "line_period", "hsyncPulseUS", "eqPulseUS",

@@ -85,7 +85,7 @@ def test_decimated_decode_matches_oracle(gpu, precision, ntsc_capture, decimated
         r = s.decode(rf, demod_only=True)
         assert r.stream_samples == len(video)
         v = s.stream(0, 0, len(video))
-        assert np.quantile(np.abs(v - video), 0.999) < FREQ_TOL_HZ
+        assert np.max(np.abs(v - video)) < FREQ_TOL_HZ
         assert np.median(np.abs(v - video)) < 2.0
         r = s.decode(rf)
         assert r.fields == len(good)

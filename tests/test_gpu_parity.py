@@ -142,8 +142,8 @@ def test_stream_channels_match_oracle(gpu, system, precision, request):
         e = s.stream(2, 0, n)
     dv = np.abs(v - video)
     dy = np.abs(y - vlp)
-    assert np.quantile(dv, 0.999) < FREQ_TOL_HZ, np.max(dv)
-    assert np.quantile(dy, 0.999) < FREQ_TOL_HZ, np.max(dy)
+    assert np.max(dv) < FREQ_TOL_HZ, np.max(dv)
+    assert np.max(dy) < FREQ_TOL_HZ, np.max(dy)
     assert np.median(dv) < 2.0 and np.median(dy) < 2.0, (np.median(dv), np.median(dy))
     de = np.abs(e - env) / np.maximum(np.abs(env), 1.0)
     assert np.quantile(de, 0.999) < 1e-3
@@ -251,7 +251,7 @@ def test_20msps_fields_match_oracle(gpu, precision, ntsc20_capture, ntsc20_oracl
     with native.Session(native.PROFILE_NTSC, len(rf), precision=precision, sample_rate_mhz=20.0) as s:
         r = s.decode(rf, demod_only=True)
         v = s.stream(0, 0, len(video))
-        assert np.quantile(np.abs(v - video), 0.999) < FREQ_TOL_HZ
+        assert np.max(np.abs(v - video)) < FREQ_TOL_HZ
         r = s.decode(rf)
         assert r.fields == len(good)
         tb = s.tbc()
@@ -287,8 +287,8 @@ def test_svhs_matches_oracle(gpu, system, precision, request):
         e = s.stream(2, 0, n)
         dv = np.abs(v - video)
         dy = np.abs(y - vlp)
-        assert np.quantile(dv, 0.999) < FREQ_TOL_HZ, np.max(dv)
-        assert np.quantile(dy, 0.999) < FREQ_TOL_HZ, np.max(dy)
+        assert np.max(dv) < FREQ_TOL_HZ, np.max(dv)
+        assert np.max(dy) < FREQ_TOL_HZ, np.max(dy)
         # no systematic offset (FP32 rounding alone is well under 2 Hz)
         assert np.median(dv) < 2.0 and np.median(dy) < 2.0, (np.median(dv), np.median(dy))
         de = np.abs(e - env) / np.maximum(np.abs(env), 1.0)
@@ -324,7 +324,7 @@ def test_svhs_sub_deemphasis_changes_the_video(gpu, svhs_capture):
         s.decode(rf, demod_only=True)
         got = s.stream(0, 10 * 30720, 30720)
     keep = slice(1024, 1024 + 30720)
-    assert np.quantile(np.abs(got - v_sub[keep]), 0.999) < FREQ_TOL_HZ
+    assert np.max(np.abs(got - v_sub[keep])) < FREQ_TOL_HZ
     assert np.quantile(np.abs(v_sub[keep] - v_lin[keep]), 0.9) > 10 * FREQ_TOL_HZ
 
 
@@ -342,6 +342,6 @@ def test_every_fft_radix_plan_matches_oracle(gpu, plan, pal_capture, pal_oracle,
         v = s.stream(0, 0, n)
         y = s.stream(1, 0, n)
         e = s.stream(2, 0, n)
-    assert np.quantile(np.abs(v - video), 0.999) < FREQ_TOL_HZ
-    assert np.quantile(np.abs(y - vlp), 0.999) < FREQ_TOL_HZ
+    assert np.max(np.abs(v - video)) < FREQ_TOL_HZ
+    assert np.max(np.abs(y - vlp)) < FREQ_TOL_HZ
     assert np.quantile(np.abs(e - env) / np.maximum(np.abs(env), 1.0), 0.999) < 1e-3

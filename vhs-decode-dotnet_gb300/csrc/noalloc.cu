@@ -11,9 +11,9 @@
 //
 // Limits and rules of use:
 // * at most kNoAllocMaxSamples samples per call; longer inputs are rejected;
-// * the first call on a device (any arguments, n = 0 included) looks up the
-//   scratch array's address with that device current; make that first call
-//   before any stream capture begins;
+// * every call made outside a stream capture (any arguments, n = 0 included)
+//   looks up the scratch array's address with the current device; the first
+//   call on a device must be such a call, made before any stream capture;
 // * the scratch array is shared by every call on a device, so calls must not
 //   overlap: issue them on one stream, or order them, never from two streams
 //   or threads at once;
@@ -45,15 +45,27 @@ constexpr int kMaxDevices = 64;
 std::mutex g_mutex;
 int64_t* g_scratch_ptr[kMaxDevices] = {};
 
-int32_t scratch_for_current_device(int64_t** out) {
+// The address is looked up again on every call made outside a stream capture,
+// so a context that was torn down and recreated (cudaDeviceReset) gets the
+// reloaded module's address; a call inside a capture uses the address of the
+// last call made outside one.
+int32_t scratch_for_current_device(cudaStream_t stream, int64_t** out) {
     int dev = -1;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess || dev < 0)
         return set_last_error(VHSDECODE_GB300_STATUS_CUDA_UNAVAILABLE, "no current CUDA device");
     if (dev >= kMaxDevices)
         return set_last_error(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "device index above 63");
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    e = cudaStreamIsCapturing(stream, &cap);
+    if (e != cudaSuccess)
+        return set_last_error(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT,
+                              (std::string("stream query: ") + cudaGetErrorString(e)).c_str());
     std::lock_guard<std::mutex> lock(g_mutex);
-    if (!g_scratch_ptr[dev]) {
+    if (cap == cudaStreamCaptureStatusNone || !g_scratch_ptr[dev]) {
+        if (cap != cudaStreamCaptureStatusNone)
+            return set_last_error(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT,
+                                  "first no-allocation call on this device made inside a stream capture");
         void* p = nullptr;
         e = cudaGetSymbolAddress(&p, g_pulse_scratch);
         if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver)
@@ -75,7 +87,8 @@ VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_pulse_events_no
     const float* sync, int64_t length, double high, int64_t* events, int64_t capacity,
     int64_t* total, void* stream) {
     int64_t* scratch = nullptr;
-    int32_t st = scratch_for_current_device(&scratch);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    int32_t st = scratch_for_current_device(s, &scratch);
     if (st != VHSDECODE_GB300_STATUS_OK) return st;
     if (length < 0 || capacity < 0)
         return set_last_error(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "negative length or capacity");
@@ -84,7 +97,6 @@ VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_pulse_events_no
                               "length above the 16777216-sample limit of the no-allocation pulse scan");
     if (!total || (length && !sync) || (capacity && !events))
         return set_last_error(VHSDECODE_GB300_STATUS_NULL_POINTER, "null argument");
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
     cudaError_t e = launch_pulse_events<float>(sync, length, high, scratch, scratch + kNoAllocSlots,
                                                events, capacity, total, s);
     if (e != cudaSuccess)

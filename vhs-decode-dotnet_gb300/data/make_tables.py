@@ -13,14 +13,17 @@ nearest binary64 (as .NET's double.Parse does) and written as little-endian
 float64 (re, im) pairs.  The decoder library reads these files at session
 creation; nothing reads the reference at run time.
 
-Run where the reference is checked out at REFERENCE_ROOT (default /root/reference).
+Run with the reference checkout given as the first argument or in the
+REFERENCE_ROOT environment variable.
 """
 import hashlib
 import os
 import struct
 import sys
 
-REF = os.environ.get("REFERENCE_ROOT", "/root/reference")
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("REFERENCE_ROOT")
+if not REF or not os.path.isdir(REF):
+    sys.exit("usage: %s REFERENCE_ROOT (or set REFERENCE_ROOT)" % os.path.basename(__file__))
 HERE = os.path.dirname(os.path.abspath(__file__))
 RATES = (40000000, 17734475)
 BINS = 16385
