@@ -61,7 +61,8 @@ typedef enum vhsdecode_gb300_profile {
     VHSDECODE_GB300_PROFILE_PAL_M = 2
 } vhsdecode_gb300_profile;
 
-/* vhsdecode_cuda_fast_tape_speed (:44-48); only SP parameters are built in. */
+/* vhsdecode_cuda_fast_tape_speed (:44-48).  LP and EP apply the format's
+ * sub-deemphasis to VHS (S-VHS LP/EP equal S-VHS SP). */
 typedef enum vhsdecode_gb300_tape_speed {
     VHSDECODE_GB300_TAPE_SPEED_SP = 0,
     VHSDECODE_GB300_TAPE_SPEED_LP = 1,

@@ -2,8 +2,9 @@
 
 The values restate the frozen upstream snapshot the reference embeds
 (``src/VHSDecode.Core/Formats/format-params.snapshot.json``, cases
-``PAL/VHS/sp``, ``NTSC/VHS/sp``, ``PAL/SVHS/sp`` and ``NTSC/SVHS/sp``; read
-through ``FormatCatalog.cs:46-112``).
+PAL and NTSC, VHS and SVHS, at ``sp``, ``lp`` and ``ep``; read through
+``FormatCatalog.cs:46-112``).  VHS LP/EP switch the sub-deemphasis on and
+narrow the NTSC RF filters; S-VHS LP/EP equal S-VHS SP.
 Only the keys the RF -> TBC luma path reads are kept.  ``tests/golden/
 format_params.json`` (written by ``tests/golden/make_golden.py`` from the
 reference snapshot) pins this table.
@@ -93,8 +94,34 @@ def _svhs(base, ire0, hz_ire):
 PAL_SVHS_SP = _svhs(PAL_VHS_SP, 5880000.0, 11200.0)
 NTSC_SVHS_SP = _svhs(NTSC_VHS_SP, 5857142.857142857, 11428.57142857143)
 
+_VHS_LONG_PLAY_RF = {
+    "use_sub_deemphasis": True, "nonlinear_highpass_freq": 820000.0,
+    "nonlinear_exp_scaling": 0.12, "nonlinear_scaling_1": 0.1,
+}
+
+
+def _long_play(base, speed, ntsc_lpf_extra=None, ntsc_bpf_high=None):
+    fmt = {"system": base["system"], "tape_format": base["tape_format"], "tape_speed": speed,
+           "sys": dict(base["sys"]), "rf": dict(base["rf"])}
+    if base["tape_format"] == "VHS":
+        fmt["rf"].update(_VHS_LONG_PLAY_RF)
+        if ntsc_lpf_extra is not None:
+            fmt["rf"]["video_lpf_extra"] = ntsc_lpf_extra
+        if ntsc_bpf_high is not None:
+            fmt["rf"]["video_bpf_high"] = ntsc_bpf_high
+    return fmt
+
+
 FORMATS = {("PAL", "VHS", "sp"): PAL_VHS_SP, ("NTSC", "VHS", "sp"): NTSC_VHS_SP,
-           ("PAL", "SVHS", "sp"): PAL_SVHS_SP, ("NTSC", "SVHS", "sp"): NTSC_SVHS_SP}
+           ("PAL", "SVHS", "sp"): PAL_SVHS_SP, ("NTSC", "SVHS", "sp"): NTSC_SVHS_SP,
+           ("PAL", "VHS", "lp"): _long_play(PAL_VHS_SP, "lp"),
+           ("PAL", "VHS", "ep"): _long_play(PAL_VHS_SP, "ep"),
+           ("NTSC", "VHS", "lp"): _long_play(NTSC_VHS_SP, "lp", 5900000.0),
+           ("NTSC", "VHS", "ep"): _long_play(NTSC_VHS_SP, "ep", 5800000.0, 6400000.0),
+           ("PAL", "SVHS", "lp"): _long_play(PAL_SVHS_SP, "lp"),
+           ("PAL", "SVHS", "ep"): _long_play(PAL_SVHS_SP, "ep"),
+           ("NTSC", "SVHS", "lp"): _long_play(NTSC_SVHS_SP, "lp"),
+           ("NTSC", "SVHS", "ep"): _long_play(NTSC_SVHS_SP, "ep")}
 
 
 def get(system: str, tape_format: str = "VHS", speed: str = "sp") -> dict:

@@ -6,9 +6,8 @@ reads the reference at test time.
 
 * format_params.json: the keys of the frozen upstream parameter snapshot
   (src/VHSDecode.Core/Formats/format-params.snapshot.json) that the RF -> TBC
-  luma path reads, for the PAL/VHS/sp, NTSC/VHS/sp, PAL/SVHS/sp and
-  NTSC/SVHS/sp cases, and the SHA-256 of the S-VHS custom luma tables
-  (src/VHSDecode.Core/Formats/custom/*.txt) converted as
+  luma path reads, for PAL and NTSC, VHS and SVHS, at sp, lp and ep, and the
+  SHA-256 of the S-VHS custom luma tables (src/VHSDecode.Core/Formats/custom/*.txt) converted as
   vhs-decode-dotnet_gb300/data/make_tables.py converts them.
 * sinc_lut_rows.json: the rows of the reference's 65537 x 16 sinc LUT
   (src/VHSDecode.Core/Tbc/Resources/sinc_lut.npz) that the three
@@ -73,8 +72,8 @@ def main():
     out = {}
     for c in snap["cases"]:
         key = (c["system"], c["tape_format"], c["tape_speed"])
-        if key in (("PAL", "VHS", "sp"), ("NTSC", "VHS", "sp"), ("PAL", "SVHS", "sp"),
-                   ("NTSC", "SVHS", "sp")):
+        if (key[0] in ("PAL", "NTSC") and key[1] in ("VHS", "SVHS")
+                and key[2] in ("sp", "lp", "ep")):
             out["/".join(key)] = {"sys": {k: c["sysparams"].get(k) for k in SYS_KEYS + SYS_KEYS_SUB},
                                   "rf": {k: c["rfparams"].get(k) for k in RF_KEYS}}
     import hashlib

@@ -112,15 +112,19 @@ def test_session_rejects_bad_decimation(lib):
     assert e.value.status in (native.STATUS_INVALID_ARGUMENT, native.STATUS_CUDA_UNAVAILABLE)
 
 
-@pytest.mark.parametrize("system,tape", [("PAL", "VHS"), ("NTSC", "VHS"), ("PAL", "SVHS"),
-                                         ("NTSC", "SVHS")])
-def test_filter_design_matches_oracle(lib, system, tape):
+@pytest.mark.parametrize("system,tape,speed", [
+    ("PAL", "VHS", "sp"), ("NTSC", "VHS", "sp"), ("PAL", "SVHS", "sp"), ("NTSC", "SVHS", "sp"),
+    ("PAL", "VHS", "lp"), ("PAL", "VHS", "ep"), ("NTSC", "VHS", "lp"), ("NTSC", "VHS", "ep"),
+    ("NTSC", "SVHS", "ep")])
+def test_filter_design_matches_oracle(lib, system, tape, speed):
     from vhsd_gb300 import native
     from oracle import filters, formats
     prof = native.PROFILE_PAL if system == "PAL" else native.PROFILE_NTSC
     fmt_id = native.FORMAT_SVHS if tape == "SVHS" else native.FORMAT_VHS
-    rv, v, s, env, sub_high, sub_env = native.design_filters(prof, tape_format=fmt_id, sub=True)
-    fl = filters.FilterSet(formats.get(system, tape), 40e6)
+    spd = {"sp": native.TAPE_SP, "lp": native.TAPE_LP, "ep": native.TAPE_EP}[speed]
+    rv, v, s, env, sub_high, sub_env = native.design_filters(prof, tape_format=fmt_id, sub=True,
+                                                             tape_speed=spd)
+    fl = filters.FilterSet(formats.get(system, tape, speed), 40e6)
 
     def rel(a, b):
         return np.max(np.abs(a - b)) / np.max(np.abs(b))
@@ -130,8 +134,9 @@ def test_filter_design_matches_oracle(lib, system, tape):
     assert rel(v, fl.half("video")) < 1e-10
     assert rel(s, fl.half("video_lp05")) < 1e-10
     np.testing.assert_allclose(env, [fl.env_b[0], fl.env_b[1], fl.env_a1], rtol=1e-15)
-    if tape == "SVHS":
-        # Video carries the measured S-VHS luma table and the 2 MHz high shelf
+    if tape == "SVHS" or speed != "sp":
+        # S-VHS: Video carries the measured S-VHS luma table and the 2 MHz high shelf;
+        # VHS LP/EP: the plain VHS Video filter with the 820 kHz sub-deemphasis high-pass
         assert rel(sub_high, (fl.video * fl.sub_highpass)[:16385]) < 1e-10
         np.testing.assert_allclose(sub_env, [fl.sub_amp_b[0], fl.sub_amp_b[1], fl.sub_amp_a1],
                                    rtol=1e-15)

@@ -345,3 +345,42 @@ def test_every_fft_radix_plan_matches_oracle(gpu, plan, pal_capture, pal_oracle,
     assert np.max(np.abs(v - video)) < FREQ_TOL_HZ
     assert np.max(np.abs(y - vlp)) < FREQ_TOL_HZ
     assert np.quantile(np.abs(e - env) / np.maximum(np.abs(env), 1.0), 0.999) < 1e-3
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp32_fused", "fp64_plain"])
+@pytest.mark.parametrize("system,speed", [("PAL", "lp"), ("NTSC", "ep")])
+def test_long_play_matches_oracle(gpu, system, speed, precision, request):
+    # VHS LP/EP: the format's sub-deemphasis on every block (820 kHz high-pass,
+    # exponent 0.12, first scale 0.1) and, for NTSC EP, the narrower RF filters
+    from oracle import field, formats
+    from vhsd_gb300 import native
+    rf, _ = request.getfixturevalue("pal_capture" if system == "PAL" else "ntsc_capture")
+    fields, (video, vlp, env, _) = field.decode_capture(rf, formats.get(system, "VHS", speed))
+    good = [f for f in fields if "error" not in f]
+    assert len(good) >= 2
+    prof = native.PROFILE_PAL if system == "PAL" else native.PROFILE_NTSC
+    spd = native.TAPE_LP if speed == "lp" else native.TAPE_EP
+    with native.Session(prof, len(rf), precision=precision, tape_speed=spd) as s:
+        r = s.decode(rf, demod_only=True)
+        n = len(video)
+        v = s.stream(0, 0, n)
+        y = s.stream(1, 0, n)
+        assert np.max(np.abs(v - video)) < FREQ_TOL_HZ
+        assert np.max(np.abs(y - vlp)) < FREQ_TOL_HZ
+        assert np.median(np.abs(v - video)) < 2.0
+        r = s.decode(rf)
+        assert r.fields == len(good)
+        tb = s.tbc()
+        for i, f in enumerate(good):
+            info = s.field(i)
+            assert bool(info.is_first_field) == f["first_field"]
+            assert info.span_start == f["span_start"]
+            assert np.max(np.abs(s.lines(i) - f["locs"])) < LINE_TOL
+            d = np.abs(tb[i].astype(np.int64).ravel() - f["tbc"].astype(np.int64))
+            assert np.mean(d <= 1) >= LSB_FRACTION, (i, np.mean(d <= 1), d.max())
+            assert s.dropouts(i) == [tuple(x) for x in f["dropouts"]]
+    # the long-play decode differs from the SP decode of the same capture
+    with native.Session(prof, len(rf), precision=precision) as s:
+        s.decode(rf, demod_only=True)
+        v_sp = s.stream(0, 0, n)
+    assert np.quantile(np.abs(v - v_sp), 0.9) > 10.0 * 1000.0 / 100.0

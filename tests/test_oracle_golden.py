@@ -122,8 +122,10 @@ def test_replace_spikes_known_answers():
 
 def test_format_table_matches_snapshot():
     g = json.load(open(os.path.join(GOLDEN, "format_params.json")))
-    for key, fmt in (("PAL/VHS/sp", formats.PAL_VHS_SP), ("NTSC/VHS/sp", formats.NTSC_VHS_SP),
-                     ("PAL/SVHS/sp", formats.PAL_SVHS_SP), ("NTSC/SVHS/sp", formats.NTSC_SVHS_SP)):
+    keys = [k for k in g if k.count("/") == 2]
+    assert len(keys) == 12   # PAL/NTSC x VHS/SVHS x sp/lp/ep
+    for key in keys:
+        fmt = formats.get(*key.split("/"))
         sub = bool(g[key]["rf"].get("use_sub_deemphasis"))
         for k, v in g[key]["sys"].items():
             assert fmt["sys"].get(k) == v, (key, k)

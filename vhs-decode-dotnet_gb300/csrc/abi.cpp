@@ -49,10 +49,12 @@ thread_local std::string g_last_error;
 namespace {
 
 bool format_for(uint32_t profile, uint32_t speed, uint32_t tape_format, FormatParams& f) {
-    if (speed != VHSDECODE_GB300_TAPE_SPEED_SP) return false;
+    if (speed != VHSDECODE_GB300_TAPE_SPEED_SP && speed != VHSDECODE_GB300_TAPE_SPEED_LP &&
+        speed != VHSDECODE_GB300_TAPE_SPEED_EP)
+        return false;
     const bool pal = profile == VHSDECODE_GB300_PROFILE_PAL, ntsc = profile == VHSDECODE_GB300_PROFILE_NTSC;
     if (!pal && !ntsc) return false;
-    if (tape_format == VHSDECODE_GB300_TAPE_FORMAT_VHS) { f = pal ? pal_vhs_sp() : ntsc_vhs_sp(); return true; }
+    if (tape_format == VHSDECODE_GB300_TAPE_FORMAT_VHS) { f = vhs_format(pal, (int)speed); return true; }
     if (tape_format == VHSDECODE_GB300_TAPE_FORMAT_SVHS) { f = pal ? pal_svhs_sp() : ntsc_svhs_sp(); return true; }
     return false;
 }
@@ -116,7 +118,7 @@ int tuned_fft_plan(vhsdecode_gb300_session* s, FastDemodParams base);
 void session_init(vhsdecode_gb300_session* s, const vhsdecode_gb300_session_config_v1& c) {
     if (!format_for(c.profile, c.tape_speed, c.tape_format, s->fmt))
         throw Failure(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT,
-                      "unsupported profile / tape speed / tape format (PAL or NTSC, SP, VHS or SVHS)");
+                      "unsupported profile / tape speed / tape format (PAL or NTSC; SP, LP or EP; VHS or SVHS)");
     if (!(c.sample_rate_mhz >= 10.0 && c.sample_rate_mhz <= 100.0))
         throw Failure(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "sample_rate_mhz must be within 10..100");
     if (c.precision > 1) throw Failure(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "unknown precision");

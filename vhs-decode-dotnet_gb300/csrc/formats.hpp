@@ -1,8 +1,8 @@
 // Format parameters for the supported tape formats.
 //
 // Values restate the frozen upstream parameter snapshot the reference embeds
-// (src/VHSDecode.Core/Formats/format-params.snapshot.json, cases PAL/VHS/sp,
-// NTSC/VHS/sp, PAL/SVHS/sp and NTSC/SVHS/sp, read by
+// (src/VHSDecode.Core/Formats/format-params.snapshot.json, cases PAL and NTSC
+// VHS and SVHS at sp, lp and ep, read by
 // Core/Formats/FormatCatalog.cs:46-112); only the keys the RF -> TBC luma path
 // reads are kept.
 #pragma once
@@ -125,6 +125,37 @@ inline FormatParams ntsc_svhs_sp() {
     FormatParams f = ntsc_vhs_sp();
     f.ire0 = 5857142.857142857; f.hz_ire = 11428.57142857143;
     svhs_common(f);
+    return f;
+}
+
+// VHS LP and EP (snapshot cases PAL/VHS/lp|ep and NTSC/VHS/lp|ep): the SP
+// parameters with the format's sub-deemphasis switched on (use_sub_deemphasis:
+// a first-order 820 kHz high-pass of the video, the amplitude low-pass at its
+// 700 kHz default, nonlinear_exp_scaling 0.12, nonlinear_scaling_1 0.1, no
+// second scale, logistic or static factor) and, for NTSC, a lower extra RF
+// low-pass (LP 5.9 MHz, EP 5.8 MHz) and an EP band-pass top of 6.4 MHz.
+inline void vhs_long_play(FormatParams& f, bool ep) {
+    f.sub_deemph = true;
+    f.sub_hp_freq = 820000.0;
+    f.sub_amp_lpf = 700000.0;
+    f.sub_deviation = f.hz_ire * (100.0 + -f.vsync_ire);
+    f.sub_exp = 0.12;
+    f.sub_scale1 = 0.1;
+    f.sub_scale2 = NAN;
+    f.sub_logistic_mid = NAN;
+    f.sub_logistic_rate = NAN;
+    f.sub_static = 0.0;
+    if (!f.pal) {
+        f.lpf_extra = ep ? 5800000.0 : 5900000.0;
+        if (ep) f.bpf_high = 6400000.0;
+    }
+}
+
+// speed: 0 SP, 1 LP, 2 EP (the reference's tape_speed values).  S-VHS LP and EP
+// carry the S-VHS SP parameters unchanged.
+inline FormatParams vhs_format(bool pal, int speed) {
+    FormatParams f = pal ? pal_vhs_sp() : ntsc_vhs_sp();
+    if (speed != 0) vhs_long_play(f, speed == 2);
     return f;
 }
 

@@ -290,7 +290,7 @@ void worker_main(vhsdecode_gb300_server* sv) {
 
 bool supported(const vhsdecode_gb300_window_v1& w) {
     return (w.profile == VHSDECODE_GB300_PROFILE_PAL || w.profile == VHSDECODE_GB300_PROFILE_NTSC) &&
-           w.tape_speed == VHSDECODE_GB300_TAPE_SPEED_SP &&
+           w.tape_speed <= VHSDECODE_GB300_TAPE_SPEED_EP &&
            (w.tape_format == VHSDECODE_GB300_TAPE_FORMAT_VHS || w.tape_format == VHSDECODE_GB300_TAPE_FORMAT_SVHS) &&
            w.sample_rate_mhz >= 10.0 && w.sample_rate_mhz <= 100.0 && w.decimation <= 2 &&
            (w.decimation != 2 || w.sample_rate_mhz <= 50.0);

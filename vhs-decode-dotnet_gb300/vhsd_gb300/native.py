@@ -340,12 +340,13 @@ class Session:
     """Device-resident decode context (session API of include/vhsdecode_gb300.h)."""
 
     def __init__(self, profile, max_samples, precision=PRECISION_FP32_FUSED, device=0,
-                 sample_rate_mhz=40.0, max_fields=0, tape_format=FORMAT_VHS, decimation=1):
+                 sample_rate_mhz=40.0, max_fields=0, tape_format=FORMAT_VHS, decimation=1,
+                 tape_speed=TAPE_SP):
         L = load()
         cfg = SessionConfig()
         cfg.struct_size = ctypes.sizeof(SessionConfig)
         cfg.profile = profile
-        cfg.tape_speed = TAPE_SP
+        cfg.tape_speed = tape_speed
         cfg.tape_format = tape_format
         cfg.device_id = device
         cfg.sample_rate_mhz = sample_rate_mhz
