@@ -202,3 +202,67 @@ def test_unsupported_formats_are_rejected(lib):
         with pytest.raises(native.NativeError) as ei:
             native.Session(prof, 1 << 20, tape_format=tape)
         assert ei.value.status == native.STATUS_INVALID_ARGUMENT
+
+
+def _host_run(lib, read, cancel=None, total=0, base="/tmp/vhsd_host_run"):
+    from vhsd_gb300 import native
+    cfg = native.RunConfig()
+    cfg.struct_size = ctypes.sizeof(cfg)
+    cfg.profile = native.PROFILE_PAL
+    cfg.sample_rate_mhz = 40.0
+    cfg.total_samples = total
+    cfg.output_base_utf8 = base.encode()
+    cfg.overwrite = 1
+    cfg.input_sample_format = native.INPUT_INT16
+    cfg.device_decimation_factor = 1
+    keep = [native.READ_CB(read)]
+    cfg.read_callback = keep[0]
+    if cancel is not None:
+        keep.append(native.CANCEL_CB(cancel))
+        cfg.cancel_callback = keep[1]
+    res = native.RunResult()
+    res.struct_size = ctypes.sizeof(res)
+    return lib.vhsdecode_gb300_run(ctypes.byref(cfg), ctypes.byref(res))
+
+
+def _no_outputs(base):
+    import glob
+    return not glob.glob(base + "*")
+
+
+def test_run_cancel_before_startup_writes_nothing(lib, tmp_path):
+    # cancellation is polled before any device work (vhsdecode_cuda_fast.cpp:280-284)
+    from vhsd_gb300 import native
+    base = str(tmp_path / "c0")
+    calls = []
+    st = _host_run(lib, lambda u, d, o, c: calls.append(c) or 0, cancel=lambda u: 1, base=base)
+    assert st == native.STATUS_CANCELLED
+    assert not calls and _no_outputs(base)
+
+
+def test_run_cancel_during_prefetch(lib, tmp_path, monkeypatch):
+    # a cancel callback that flips after two reads: the prefetch thread polls it
+    # before each read and stops; the run reports CANCELLED and leaves no files
+    from vhsd_gb300 import native
+    monkeypatch.setenv("VHSD_RUN_WINDOW_GRIDS", "40")   # the first window needs 10 reads
+    base = str(tmp_path / "c2")
+    reads = []
+
+    def read(u, d, off, count):
+        reads.append((off, count))
+        ctypes.memset(d, 0, count * 2)
+        return count
+
+    st = _host_run(lib, read, cancel=lambda u: 1 if len(reads) >= 2 else 0, base=base)
+    assert st == native.STATUS_CANCELLED
+    assert len(reads) == 2 and reads[1][0] == reads[0][1]   # in order, contiguous
+    assert _no_outputs(base)
+
+
+def test_run_read_overrun_is_an_input_error(lib, tmp_path):
+    from vhsd_gb300 import native
+    base = str(tmp_path / "ov")
+    st = _host_run(lib, lambda u, d, o, c: c + 1, base=base)
+    assert st == native.STATUS_INPUT_ERROR
+    assert b"overran" in lib.vhsdecode_gb300_get_last_error()
+    assert _no_outputs(base)

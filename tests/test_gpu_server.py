@@ -120,7 +120,10 @@ def test_unsupported_window_is_rejected(gpu, pal_capture):
     pal, _ = pal_capture
     with native.Server(1 << 21, workers=1) as sv:
         with pytest.raises(native.NativeError) as e:
-            sv.submit(0, native.PROFILE_PAL, pal[:1 << 20], tape_speed=native.TAPE_LP)
+            sv.submit(0, native.PROFILE_PAL, pal[:1 << 20], tape_speed=3)   # no VP parameters
+        assert e.value.status == native.STATUS_INVALID_ARGUMENT
+        with pytest.raises(native.NativeError) as e:
+            sv.submit(0, native.PROFILE_PAL_M, pal[:1 << 20])
         assert e.value.status == native.STATUS_INVALID_ARGUMENT
         with pytest.raises(native.NativeError):
             sv.submit(0, native.PROFILE_PAL, pal[:1 << 22])   # longer than the slots

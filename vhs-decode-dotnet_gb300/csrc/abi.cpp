@@ -1175,78 +1175,6 @@ int32_t decode_impl(vhsdecode_gb300_session* s, const void* rf_in, uint64_t n_in
     return VHSDECODE_GB300_STATUS_OK;
 }
 
-// RAII owner of a session for run().
-struct SessionHolder {
-    vhsdecode_gb300_session* s = nullptr;
-    ~SessionHolder() {
-        if (s) {
-            cudaSetDevice(s->device);
-            if (s->stream) cudaStreamSynchronize(s->stream);
-            session_free(s);
-            delete s;
-        }
-    }
-};
-
-bool file_exists(const std::string& path) {
-    FILE* f = std::fopen(path.c_str(), "rb");
-    if (f) { std::fclose(f); return true; }
-    return false;
-}
-
-// The cuda-fast backend's metadata file (src/VHSDecode.CudaFast.Native/src/tbc_writer.cpp:209-310):
-// the same keys and number formats, written to a temporary file and renamed
-// into place.  Levels carry the writer's default 10 % adjust; the burst window
-// comes from the format's colorBurstUS, the active video window is the
-// writer's per-system constant.
-void write_json(const std::string& path, const vhsdecode_gb300_session* s) {
-    const std::string tmp = path + ".tmp";
-    FILE* f = std::fopen(tmp.c_str(), "wb");
-    if (!f) throw Failure(VHSDECODE_GB300_STATUS_OUTPUT_ERROR, "cannot open " + tmp);
-    const FormatParams& fm = s->fmt;
-    const double scale = output_scale(fm), rate = fm.outfreq_mhz * 1e6;
-    const double level_adjust = 0.1;
-    const double black16 = ((0.0 - fm.vsync_ire) * scale + fm.output_zero) * (1.0 - level_adjust);
-    const double white16 = ((100.0 - fm.vsync_ire) * scale + fm.output_zero) * (1.0 + level_adjust);
-    const int burst_start = (int)(fm.burst_start_us * 1e-6 * rate + 0.5);
-    const int burst_end = (int)(fm.burst_end_us * 1e-6 * rate + 0.5);
-    const int active_start = fm.pal ? 185 : 134, active_end = fm.pal ? 1107 : 894;
-    std::fprintf(f, "{\n  \"videoParameters\": {\n");
-    std::fprintf(f, "    \"system\": \"%s\",\n", fm.pal ? "PAL" : "NTSC");
-    std::fprintf(f, "    \"isSubcarrierLocked\": false,\n");
-    std::fprintf(f, "    \"isSourcePal\": %s,\n", fm.pal ? "true" : "false");
-    std::fprintf(f, "    \"numberOfSequentialFields\": %zu,\n", s->fields.size());
-    std::fprintf(f, "    \"black16bIre\": %.1f,\n", black16);
-    std::fprintf(f, "    \"white16bIre\": %.1f,\n", white16);
-    std::fprintf(f, "    \"sampleRate\": %.0f,\n", rate);
-    std::fprintf(f, "    \"fieldWidth\": %d,\n", s->outlen);
-    std::fprintf(f, "    \"fieldHeight\": %d,\n", s->out_lines);
-    std::fprintf(f, "    \"colourBurstStart\": %d,\n", burst_start);
-    std::fprintf(f, "    \"colourBurstEnd\": %d,\n", burst_end);
-    std::fprintf(f, "    \"activeVideoStart\": %d,\n", active_start);
-    std::fprintf(f, "    \"activeVideoEnd\": %d,\n", active_end);
-    std::fprintf(f, "    \"tapeFormat\": \"%s\",\n", fm.custom_luma_table ? "SVHS" : "VHS");
-    std::fprintf(f, "    \"isMapped\": false\n  },\n  \"fields\": [\n");
-    for (size_t i = 0; i < s->fields.size(); i++) {
-        const FieldRec& r = s->fields[i];
-        long long file_loc = (long long)std::floor(r.span_start + r.sync.line0 + kCut);
-        std::fprintf(f, "    {\n      \"isFirstField\": %s,\n      \"seqNo\": %zu,\n      \"fileLoc\": %lld,\n",
-                     r.sync.first_field ? "true" : "false", i + 1, file_loc);
-        const size_t nd = r.drop.size() / 3;
-        std::fprintf(f, "      \"dropOuts\": {\n        \"fieldLine\": [");
-        for (size_t k = 0; k < nd; k++) std::fprintf(f, "%s%d", k ? ", " : "", r.drop[3 * k]);
-        std::fprintf(f, "],\n        \"startx\": [");
-        for (size_t k = 0; k < nd; k++) std::fprintf(f, "%s%d", k ? ", " : "", r.drop[3 * k + 1]);
-        std::fprintf(f, "],\n        \"endx\": [");
-        for (size_t k = 0; k < nd; k++) std::fprintf(f, "%s%d", k ? ", " : "", r.drop[3 * k + 2]);
-        std::fprintf(f, "]\n      }\n    }%s\n", i + 1 < s->fields.size() ? "," : "");
-    }
-    std::fprintf(f, "  ]\n}\n");
-    if (std::fclose(f) != 0) throw Failure(VHSDECODE_GB300_STATUS_OUTPUT_ERROR, "cannot write " + tmp);
-    if (std::rename(tmp.c_str(), path.c_str()) != 0)
-        throw Failure(VHSDECODE_GB300_STATUS_OUTPUT_ERROR, "cannot rename " + tmp);
-}
-
 }  // namespace detail
 }  // namespace vhsd
 
@@ -1292,111 +1220,6 @@ VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_get_runtime_inf
         info->total_vram_bytes = tot;
         info->free_vram_bytes = fr;
         std::snprintf(info->device_name, VHSDECODE_GB300_NAME_CAPACITY, "%s", p.name);
-        return VHSDECODE_GB300_STATUS_OK;
-    });
-}
-
-VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_run(
-    const vhsdecode_gb300_config_v1* config, vhsdecode_gb300_result_v1* result) {
-    return guard([&]() -> int32_t {
-        if (!config || !result) return fail(VHSDECODE_GB300_STATUS_NULL_POINTER, "null argument");
-        if (config->struct_size != sizeof(vhsdecode_gb300_config_v1) &&
-            config->struct_size != sizeof(vhsdecode_gb300_config_v2))
-            return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "config struct_size mismatch");
-        const uint32_t tape_format =
-            config->struct_size == sizeof(vhsdecode_gb300_config_v2)
-                ? reinterpret_cast<const vhsdecode_gb300_config_v2*>(config)->tape_format
-                : (uint32_t)VHSDECODE_GB300_TAPE_FORMAT_VHS;
-        if (result->struct_size != sizeof(vhsdecode_gb300_result_v1))
-            return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "result struct_size mismatch");
-        if (!config->read_callback) return fail(VHSDECODE_GB300_STATUS_NULL_POINTER, "read_callback is null");
-        if (!config->output_base_utf8 || !config->output_base_utf8[0])
-            return fail(VHSDECODE_GB300_STATUS_NULL_POINTER, "output_base_utf8 is null");
-        if (config->input_sample_format > VHSDECODE_GB300_INPUT_INT16)
-            return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "unknown input_sample_format");
-        // vhsdecode_cuda_fast.cpp:255-275: factor 1 or 2; the source runs at
-        // factor x sample_rate_mhz
-        const uint32_t factor = config->device_decimation_factor;
-        if (factor != 1 && factor != 2)
-            return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "device_decimation_factor must be 1 or 2");
-        if (factor == 2 && !(config->sample_rate_mhz >= 10.0 && config->sample_rate_mhz <= 50.0))
-            return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT,
-                        "device_decimation_factor 2 needs a decode rate of 10..50 MHz");
-        const bool f32_in = config->input_sample_format == VHSDECODE_GB300_INPUT_FLOAT32;
-        const size_t esz = f32_in ? sizeof(float) : sizeof(int16_t);
-        auto t0 = std::chrono::steady_clock::now();
-        std::string base = config->output_base_utf8;
-        std::string tbc_path = base + ".tbc", json_path = base + ".tbc.json", chroma_path = base + "_chroma.tbc";
-        if (!config->overwrite && (file_exists(tbc_path) || file_exists(json_path) || file_exists(chroma_path)))
-            return fail(VHSDECODE_GB300_STATUS_OUTPUT_ERROR, "output exists and overwrite is off");
-        auto cancelled = [&]() { return config->cancel_callback && config->cancel_callback(config->user_data) != 0; };
-        // pull the capture through the callback (source samples of esz bytes)
-        std::vector<unsigned char> rf;
-        size_t have = 0;
-        const size_t chunk = (size_t)1 << 22;
-        uint64_t want = config->total_samples;
-        while (want == 0 || have < want) {
-            if (cancelled()) return fail(VHSDECODE_GB300_STATUS_CANCELLED, "decode cancelled");
-            size_t ask = chunk;
-            if (want) ask = (size_t)std::min<uint64_t>(chunk, want - have);
-            rf.resize((have + ask) * esz);
-            size_t got = config->read_callback(config->user_data, rf.data() + have * esz, have, ask);
-            if (got > ask) return fail(VHSDECODE_GB300_STATUS_INPUT_ERROR, "read callback overran its buffer");
-            have += got;
-            rf.resize(have * esz);
-            if (got < ask) break;
-        }
-        if (have / factor < (size_t)kBlock)
-            return fail(VHSDECODE_GB300_STATUS_INPUT_ERROR, "input shorter than one block");
-        vhsdecode_gb300_session_config_v1 sc{};
-        sc.struct_size = sizeof(sc);
-        sc.profile = config->profile;
-        sc.tape_speed = config->tape_speed;
-        sc.tape_format = tape_format;
-        sc.device_id = config->device_id;
-        sc.sample_rate_mhz = config->sample_rate_mhz;
-        sc.max_samples = have;
-        sc.precision = VHSDECODE_GB300_PRECISION_FP32_FUSED;
-        sc.decimation = factor;
-        SessionHolder h;
-        h.s = new vhsdecode_gb300_session();
-        session_init(h.s, sc);
-        if (cancelled()) return fail(VHSDECODE_GB300_STATUS_CANCELLED, "decode cancelled");
-        vhsdecode_gb300_decode_result_v1 dr{};
-        dr.struct_size = sizeof(dr);
-        decode_impl(h.s, rf.data(), have, config->maximum_output_fields,
-                    f32_in ? VHSDECODE_GB300_DECODE_FLOAT_INPUT : 0u, &dr);
-        if (cancelled()) return fail(VHSDECODE_GB300_STATUS_CANCELLED, "decode cancelled");
-        size_t per = (size_t)h.s->out_lines * h.s->outlen;
-        std::vector<uint16_t> tbc(per * h.s->fields.size());
-        if (!tbc.empty())
-            ck(cudaMemcpy(tbc.data(), h.s->tbc.p, tbc.size() * sizeof(uint16_t), cudaMemcpyDeviceToHost), "d2h tbc");
-        FILE* f = std::fopen(tbc_path.c_str(), "wb");
-        if (!f) return fail(VHSDECODE_GB300_STATUS_OUTPUT_ERROR, "cannot open " + tbc_path);
-        size_t wrote = tbc.empty() ? 0 : std::fwrite(tbc.data(), sizeof(uint16_t), tbc.size(), f);
-        int cerr = std::fclose(f);
-        if (wrote != tbc.size() || cerr != 0) return fail(VHSDECODE_GB300_STATUS_OUTPUT_ERROR, "cannot write " + tbc_path);
-        {
-            // Chroma is not decoded by this backend: the chroma file carries
-            // neutral chroma (zero chroma + 32767, VhsChromaDecoder.ChromaToU16,
-            // Core/Decode/VhsChromaDecoder.cs:455-500) in the luma file's
-            // geometry, which the managed finalisation opens and truncates
-            // with it (Core/Dsp/CudaFast/CudaFastDecodeRunner.cs:345,427).
-            FILE* fc = std::fopen(chroma_path.c_str(), "wb");
-            if (!fc) return fail(VHSDECODE_GB300_STATUS_OUTPUT_ERROR, "cannot open " + chroma_path);
-            std::vector<uint16_t> neutral(per, (uint16_t)32767);
-            bool ok = true;
-            for (size_t k = 0; k < h.s->fields.size() && ok; k++)
-                ok = std::fwrite(neutral.data(), sizeof(uint16_t), per, fc) == per;
-            if (std::fclose(fc) != 0 || !ok)
-                return fail(VHSDECODE_GB300_STATUS_OUTPUT_ERROR, "cannot write " + chroma_path);
-        }
-        write_json(json_path, h.s);
-        result->fields_written = (uint32_t)h.s->fields.size();
-        result->output_line_length = (uint32_t)h.s->outlen;
-        result->output_field_lines = (uint32_t)h.s->out_lines;
-        result->elapsed_seconds =
-            std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         return VHSDECODE_GB300_STATUS_OK;
     });
 }
