@@ -77,10 +77,15 @@ typedef enum vhsdecode_gb300_tape_format {
     VHSDECODE_GB300_TAPE_FORMAT_SVHS = 1
 } vhsdecode_gb300_tape_format;
 
-/* vhsdecode_cuda_fast_input_sample_format (:50-53); run() accepts INT16. */
+/* vhsdecode_cuda_fast_input_sample_format (:50-53), plus FLAC: the read
+ * callback delivers the bytes of a FLAC stream of 16-bit mono samples (a .ldf
+ * capture), sample_offset and sample_count counting bytes, and the stream is
+ * decoded on the device.  The reference decodes .ldf on the managed side
+ * through libsndfile or ffmpeg (Core/Rf/RfLoaderFactory.cs:35,136). */
 typedef enum vhsdecode_gb300_input_sample_format {
     VHSDECODE_GB300_INPUT_FLOAT32 = 0,
-    VHSDECODE_GB300_INPUT_INT16 = 1
+    VHSDECODE_GB300_INPUT_INT16 = 1,
+    VHSDECODE_GB300_INPUT_FLAC = 2
 } vhsdecode_gb300_input_sample_format;
 
 /* Arithmetic of the block demodulator. */
@@ -411,6 +416,34 @@ VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_server_wait(
     vhsdecode_gb300_server* server, uint64_t ticket, vhsdecode_gb300_window_result_v1* result);
 /* Finishes the windows being decoded, cancels queued ones, frees the slots. */
 VHSDECODE_GB300_API void VHSDECODE_GB300_CALL vhsdecode_gb300_server_destroy(vhsdecode_gb300_server* server);
+
+/* STREAMINFO of a FLAC stream (Core/Rf/RawFlacStreamInfo.cs; the reference's
+ * loader accepts a stream only when it starts with "fLaC" and a 34-byte
+ * STREAMINFO block, LibsndfilePcm16SampleLoaderTests.cs:1038-1110). */
+typedef struct vhsdecode_gb300_flac_info_v1 {
+    uint32_t struct_size;
+    uint32_t sample_rate;
+    uint32_t channels;
+    uint32_t bits_per_sample;
+    uint32_t min_block;
+    uint32_t max_block;
+    uint64_t total_samples;
+    uint64_t first_frame_offset;   /* bytes */
+} vhsdecode_gb300_flac_info_v1;
+
+/* Parses the STREAMINFO of `bytes` bytes of FLAC (host only, no GPU). */
+VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_flac_info(
+    const uint8_t* data, uint64_t bytes, vhsdecode_gb300_flac_info_v1* info);
+
+/* Decodes a whole FLAC stream of 16-bit mono samples held in host memory on
+ * device `device_id` (frames found and decoded in parallel, each checked
+ * against its CRC-16); copies up to `capacity` samples to `out` and returns
+ * the stream's sample count in *samples.  Replaces the libsndfile / ffmpeg
+ * .ldf loaders (Core/Rf/LibsndfilePcm16SampleLoader.cs,
+ * Core/Rf/FfmpegPcm16SampleLoader.cs).  INPUT_ERROR for a corrupt stream. */
+VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_flac_decode(
+    const uint8_t* data, uint64_t bytes, int16_t* out, uint64_t capacity, uint64_t* samples,
+    int32_t device_id);
 
 /* Sync-pulse edge events over `length` float samples already on the device,
  * with no device memory allocated by the call.  No counterpart in the

@@ -73,7 +73,7 @@ def test_null_pointer_status(lib):
 
 
 def test_run_rejects_unsupported_options(lib):
-    # vhsdecode_cuda_fast.cpp:255-275: input format FLOAT32 or INT16,
+    # vhsdecode_cuda_fast.cpp:255-275: input format FLOAT32 or INT16 (or FLAC here),
     # decimation factor 1 or 2 (2 with a decode rate the source halves to)
     from vhsd_gb300 import native
     cfg = native.RunConfig()
@@ -81,7 +81,7 @@ def test_run_rejects_unsupported_options(lib):
     cfg.profile = native.PROFILE_PAL
     cfg.sample_rate_mhz = 40.0
     cfg.output_base_utf8 = b"/tmp/x"
-    cfg.input_sample_format = 2
+    cfg.input_sample_format = 3   # FLOAT32, INT16 and FLAC are defined
     cfg.device_decimation_factor = 1
     cfg.read_callback = native.READ_CB(lambda u, d, o, c: 0)
     res = native.RunResult()
@@ -266,3 +266,52 @@ def test_run_read_overrun_is_an_input_error(lib, tmp_path):
     assert st == native.STATUS_INPUT_ERROR
     assert b"overran" in lib.vhsdecode_gb300_get_last_error()
     assert _no_outputs(base)
+
+
+def test_flac_stream_info_matches_reference_header_cases(lib):
+    # LibsndfilePcm16SampleLoaderTests.cs:1038-1075: STREAMINFO packing, and the
+    # headers the reference's loader refuses
+    import struct
+    from vhsd_gb300 import native
+
+    def header(rate, channels, bits, total):
+        b = bytearray(4 + 4 + 34)
+        b[:4] = b"fLaC"
+        b[4] = 0x80
+        b[7] = 34
+        packed = (rate << 44) | ((channels - 1) << 41) | ((bits - 1) << 36) | total
+        b[18:26] = struct.pack(">Q", packed)
+        return bytes(b)
+
+    info = native.flac_info(header(40_000, 1, 16, 123_456_789))
+    assert (info.sample_rate, info.channels, info.bits_per_sample, info.total_samples) == \
+        (40_000, 1, 16, 123_456_789)
+    assert info.first_frame_offset == 42
+
+    def invalid(block_type, block_len, payload):
+        b = bytearray(8 + payload)
+        b[:4] = b"fLaC"
+        b[4] = block_type
+        b[7] = block_len
+        return bytes(b)
+
+    for bad in (b"OggS" + bytes(40), b"fLaC", invalid(0x81, 0x22, 34), invalid(0x80, 0x22, 33),
+                invalid(0x80, 0x21, 33)):
+        with pytest.raises(native.NativeError) as e:
+            native.flac_info(bad)
+        assert e.value.status == native.STATUS_INPUT_ERROR
+
+
+def test_flac_writer_and_reader_round_trip():
+    # the test-side writer covers every subframe and residual form; its
+    # stream decodes (by the bit-level reader) to the samples it was given
+    from oracle import flac
+    rng = np.random.default_rng(3)
+    t = np.arange(70_000)
+    x = (6000 * np.sin(2 * np.pi * 0.11 * t) + rng.normal(0, 300, len(t))).astype(np.int16)
+    x[4096 * 3:4096 * 4] &= ~1          # a frame with a wasted bit
+    x[4096 * 6:4096 * 7] = -1234         # a constant frame
+    for bs in (4096, 1152, 4608):
+        data = flac.encode(x, blocksize=bs, seed=bs, wasted_frames=(3,))
+        assert flac.stream_info(data)["total_samples"] == len(x)
+        assert np.array_equal(flac.decode(data), x)

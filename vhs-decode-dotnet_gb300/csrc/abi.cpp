@@ -156,6 +156,10 @@ void session_init(vhsdecode_gb300_session* s, const vhsdecode_gb300_session_conf
         ck(cudaEventCreateWithFlags(e, cudaEventDisableTiming), "cudaEventCreate");
     for (auto& e : s->stage_ev) ck(cudaEventCreate(&e), "cudaEventCreate");
     s->stage_timing = std::getenv("VHSD_STAGE_TIMING") != nullptr;
+    if (std::getenv("VHSD_DEMOD_TIMING")) {
+        ck(cudaMalloc(&s->demod_cycles, 2 * kDemodStages * sizeof(unsigned long long)), "cudaMalloc");
+        ck(cudaMemset(s->demod_cycles, 0, 2 * kDemodStages * sizeof(unsigned long long)), "memset");
+    }
     s->stream = s->own_stream;
     for (auto& ev : s->ev) ck(cudaEventCreate(&ev), "cudaEventCreate");
     s->max_blocks = block_count(c.max_samples / (uint64_t)s->decim);
@@ -338,6 +342,7 @@ void session_init(vhsdecode_gb300_session* s, const vhsdecode_gb300_session_conf
 }
 
 void session_free(vhsdecode_gb300_session* s) {
+    if (s->demod_cycles) cudaFree(s->demod_cycles);
     if (s->plain_graph) cudaGraphExecDestroy(s->plain_graph);
     for (auto& ev : s->ev) if (ev) cudaEventDestroy(ev);
     for (auto* v : {&s->seg_done, &s->seg_copied, &s->seg_pulsed, &s->seg_dem, &s->seg_demod_end})
@@ -462,6 +467,13 @@ int tuned_fft_plan(vhsdecode_gb300_session* s, FastDemodParams base) {
     return best;
 }
 
+// The fused demodulator, or (VHSD_DEMOD_TIMING set) its timed diagnostic build.
+cudaError_t launch_fused(vhsdecode_gb300_session* s, FastDemodParams p, cudaStream_t st) {
+    if (!s->demod_cycles) return launch_demod_fp32(p, s->num_sms / 2, st);
+    p.stage_cycles = s->demod_cycles;
+    return launch_demod_fp32_timed(p, s->num_sms / 2, st);
+}
+
 FastDemodParams fp32_params(vhsdecode_gb300_session* s, const int16_t* rf_dev) {
     FastDemodParams p{};
     p.rf = rf_dev;
@@ -509,7 +521,7 @@ void run_demod(vhsdecode_gb300_session* s, const int16_t* rf_dev, int64_t nblock
         p.block_counter = s->blk_counters.p + s->nseg_max;
         ck(cudaMemsetAsync(p.block_counter, 0, sizeof(unsigned), s->stream), "memset");
         ck(cudaMemsetAsync(s->repair.p, 0, sizeof(int), s->stream), "memset");
-        ck(launch_demod_fp32(p, s->num_sms / 2, s->stream), "demod fp32 launch");
+        ck(launch_fused(s, p, s->stream), "demod fp32 launch");
     } else {
         PlainDemodParams p{};
         p.rf = s->in_f32 ? nullptr : rf_dev;
@@ -884,7 +896,7 @@ void enqueue_pipeline(vhsdecode_gb300_session* s, const int16_t* rf, uint64_t n,
         p.block_counter = s->blk_counters.p + k;
         ck(cudaMemsetAsync(p.block_counter, 0, sizeof(unsigned), ks), "memset");
         rec(s->seg_dem[(size_t)(2 * k)], ks, true);
-        ck(launch_demod_fp32(p, s->num_sms / 2, ks), "demod fp32 launch");
+        ck(launch_fused(s, p, ks), "demod fp32 launch");
         rec(s->seg_dem[(size_t)(2 * k + 1)], ks, true);
         rec(s->seg_demod_end[(size_t)k], ks, false);   // dependency edge (the timing record above is external)
         if (!demod_only) {
@@ -954,7 +966,7 @@ void decode_fp32_pipelined(vhsdecode_gb300_session* s, const int16_t* rf, uint64
         if (!s->pipe_exec || !(s->pipe_key == key)) {
             if (s->pipe_exec) { cudaGraphExecDestroy(s->pipe_exec); s->pipe_exec = nullptr; }
             FastDemodParams p0 = fp32_params(s, s->rf.p);
-            ck(launch_demod_fp32(p0, s->num_sms / 2, s->cap_stream), "demod attribute");  // nblocks 0: sets attributes only
+            ck(launch_fused(s, p0, s->cap_stream), "demod attribute");  // nblocks 0: sets attributes only
             ck(cudaStreamBeginCapture(s->cap_stream, cudaStreamCaptureModeThreadLocal), "begin capture");
             cudaGraph_t g = nullptr;
             try {
@@ -1153,6 +1165,18 @@ int32_t decode_impl(vhsdecode_gb300_session* s, const void* rf_in, uint64_t n_in
         ck(cudaMemcpy(&rep, s->repair.p, sizeof(int), cudaMemcpyDeviceToHost), "d2h");
     s->last_blocks = nblocks;
     s->last_repairs = rep;
+    if (s->demod_cycles && s->fp32() && nblocks > 0) {
+        // diagnostics: the decode's per-stage demod cycles per block, to stderr
+        const size_t nb = 2 * kDemodStages * sizeof(unsigned long long);
+        std::vector<unsigned long long> h(2 * kDemodStages);
+        ck(cudaMemcpy(h.data(), s->demod_cycles, nb, cudaMemcpyDeviceToHost), "d2h");
+        ck(cudaMemset(s->demod_cycles, 0, nb), "memset");
+        std::fprintf(stderr, "vhsd demod stage cycles per block (rank0 rank1), %lld blocks, %d repaired:\n",
+                     (long long)nblocks, rep);
+        for (int k = 0; k < kDemodStages; k++)
+            std::fprintf(stderr, "  stage %2d %10.0f %10.0f\n", k, (double)h[k] / nblocks,
+                         (double)h[kDemodStages + k] / nblocks);
+    }
     if (res) {
         float t_all = 0, t_fld = 0;
         cudaEventElapsedTime(&t_all, s->ev[0], s->ev[3]);

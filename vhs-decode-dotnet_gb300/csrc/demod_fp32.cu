@@ -603,9 +603,23 @@ __device__ __forceinline__ void prefetch_wait() { asm volatile("cp.async.wait_gr
 using namespace vhsd;
 using namespace vhsd::fp32;
 
-template <int PLAN>
+// Stage marks of the timed diagnostic build: thread 0 of each CTA adds the
+// cycles since the previous mark to stage_cycles[rank][k].
+#define VHSD_MARK(k)                                                                             \
+    do {                                                                                         \
+        if constexpr (TIMED) {                                                                   \
+            if (tid == 0) {                                                                      \
+                const long long c_ = clock64();                                                  \
+                atomicAdd(p.stage_cycles + rank * kDemodStages + (k), (unsigned long long)(c_ - t_mark)); \
+                t_mark = c_;                                                                     \
+            }                                                                                    \
+        }                                                                                        \
+    } while (0)
+
+template <int PLAN, bool TIMED>
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(T, 1)
 vhsd_demod_fp32_kernel(FastDemodParams p) {
+    long long t_mark = 0;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Shared& sh = *reinterpret_cast<Shared*>(smem_raw);
     cg::cluster_group cluster = cg::this_cluster();
@@ -652,15 +666,19 @@ vhsd_demod_fp32_kernel(FastDemodParams p) {
         // ---------------- stage 1: RF forward FFT (packed, DIF split) -----
         prefetch_wait();
         __syncthreads();
+        if constexpr (TIMED) t_mark = clock64();
         if (f32_in) load_rf_f32(buf, p.rf_f32 + (blk + p.first_block) * (int64_t)S, rank, sh.tw, tid);
         else load_rf(buf, rf_smem, rank, sh.tw, tid);
         __syncthreads();
+        VHSD_MARK(0);
         fft8192<false, 1, PLAN>(buf, sh.tw, tid);
+        VHSD_MARK(1);
         // X * RfVideo * Hilbert / N  (Hilbert: 1 at 0 and N/2, 2 between)
         post_half(sh, rank, tid, [&](int k, float2 v) {
             float g = __ldg(p.rf_video + k) * ((k == 0 || k == M) ? inv_n : 2.0f * inv_n);
             return make_float2(v.x * g, v.y * g);
         });
+        VHSD_MARK(2);
         // ---------------- stage 2: analytic inverse FFT -----------------
         if (rank == 0) {
             if (tid == 0) buf[sx(8192)] = sh.nyq;
@@ -669,8 +687,11 @@ vhsd_demod_fp32_kernel(FastDemodParams p) {
             for (int i = 8192 + tid; i < M; i += T) buf[sx(i)] = make_float2(0.f, 0.f);
         }
         __syncthreads();
+        VHSD_MARK(3);
         fft16384<true, PLAN>(buf, sh.tw, tid);
+        VHSD_MARK(4);
         cluster.sync();
+        VHSD_MARK(5);
         const int64_t nxt = sh.next_blk[par];
         const bool has_next = nxt < p.nblocks && !f32_in;
         const int16_t* x_next = has_next ? p.rf + (nxt + p.first_block) * (int64_t)S : nullptr;
@@ -702,6 +723,7 @@ vhsd_demod_fp32_kernel(FastDemodParams p) {
             }
         }
         __syncthreads();
+        VHSD_MARK(6);
         // ---------------- stage 3: demod, spike check ----------------------
         if (tid < 2) {
             int i_last = tid * 8192 + 8191;
@@ -734,8 +756,10 @@ vhsd_demod_fp32_kernel(FastDemodParams p) {
         int any = __syncthreads_or(spike ? 1 : 0);
         if (tid == 0) sh.flag = any;
         cluster.sync();
+        VHSD_MARK(7);
         any = sh.flag | rsh->flag;
         if (any) repair_block(sh, rsh, p, cluster_id, rank);
+        VHSD_MARK(8);
         // buf <- (demod, raw envelope |Re z[n-4]|)
         {
             float dv[32], rv[32];
@@ -754,6 +778,7 @@ vhsd_demod_fp32_kernel(FastDemodParams p) {
             for (int t = 0; t < 32; t++) buf[sx(tid + t * T)] = make_float2(dv[t], rv[t]);
         }
         cluster.sync();   // the envelope halos read the partner's buf
+        VHSD_MARK(9);
         // ---------------- envelope: 700 kHz filtfilt of |Re z[n-4]| ----------
         {
             float* envo = p.env_out + (blk + p.first_block) * (int64_t)S - CUT;
@@ -767,6 +792,7 @@ vhsd_demod_fp32_kernel(FastDemodParams p) {
                               }
                           });
         }
+        VHSD_MARK(10);
         if (has_next && p.sub.high == nullptr) prefetch_rf(sh.theta, x_next, tid);
         // ---------------- stage 4: forward FFT of (demod - ire0) -----------
         {
@@ -792,8 +818,11 @@ vhsd_demod_fp32_kernel(FastDemodParams p) {
             }
             cluster.sync();
         }
+        VHSD_MARK(11);
         fft8192<false, 1, PLAN>(buf, sh.tw, tid);
+        VHSD_MARK(12);
         post_half(sh, rank, tid, [&](int k, float2 v) { return v; });
+        VHSD_MARK(13);
         const bool sub = p.sub.high != nullptr;
         float2* xs = reinterpret_cast<float2*>(sh.theta);   // D kept for stage 6
         if (sub) {
@@ -847,8 +876,11 @@ vhsd_demod_fp32_kernel(FastDemodParams p) {
                 }
             }
             __syncthreads();
+            VHSD_MARK(14);
             fft8192<true, 2, PLAN>(buf, sh.tw, tid);
+            VHSD_MARK(15);
             cluster.sync();
+            VHSD_MARK(16);
             float* vout = p.video_out + (blk + p.first_block) * (int64_t)S - CUT;
             float* sout = p.sync_out + (blk + p.first_block) * (int64_t)S - CUT - 32;
             // the removed DC returns through each filter's DC gain
@@ -889,6 +921,7 @@ vhsd_demod_fp32_kernel(FastDemodParams p) {
                 }
             }
         }
+        VHSD_MARK(17);
         if (sub) {
             // ---------------- stage 6: S-VHS sub-deemphasis -------------------
             // A[k] = D[k] Video[k] HighPass[k] (x2 for 0 < k < N/2, real part
@@ -963,7 +996,9 @@ vhsd_demod_fp32_kernel(FastDemodParams p) {
                               }
                           });
         }
+        VHSD_MARK(18);
         cluster.sync();
+        VHSD_MARK(19);
         blk = nxt;
         par ^= 1;
     }
@@ -973,20 +1008,31 @@ namespace vhsd {
 
 size_t fp32_smem_bytes() { return sizeof(fp32::Shared); }
 
-template <int PLAN>
+template <int PLAN, bool TIMED = false>
 static cudaError_t launch_plan(const FastDemodParams& p, int clusters, cudaStream_t stream, int dev) {
     static std::atomic<uint64_t> attr_set{0};
     size_t smem = sizeof(fp32::Shared);
     const uint64_t bit = dev < 64 ? (uint64_t)1 << dev : 0;
     if (!bit || !(attr_set.load() & bit)) {
-        cudaError_t e = cudaFuncSetAttribute(vhsd_demod_fp32_kernel<PLAN>,
+        cudaError_t e = cudaFuncSetAttribute(vhsd_demod_fp32_kernel<PLAN, TIMED>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         attr_set.fetch_or(bit);
     }
     if (p.nblocks <= 0) return cudaSuccess;
-    vhsd_demod_fp32_kernel<PLAN><<<2 * clusters, fp32::T, smem, stream>>>(p);
+    vhsd_demod_fp32_kernel<PLAN, TIMED><<<2 * clusters, fp32::T, smem, stream>>>(p);
     return cudaGetLastError();
+}
+
+cudaError_t launch_demod_fp32_timed(const FastDemodParams& p, int num_clusters, cudaStream_t stream) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (!p.stage_cycles) return cudaErrorInvalidValue;
+    int clusters = num_clusters;
+    if (p.nblocks > 0 && clusters > p.nblocks) clusters = (int)p.nblocks;
+    if (clusters < 1) clusters = 1;
+    return launch_plan<0, true>(p, clusters, stream, dev);
 }
 
 // The shared-memory attribute is set once per device and plan (the first call

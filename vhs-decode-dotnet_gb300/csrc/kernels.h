@@ -56,7 +56,11 @@ struct FastDemodParams {
     unsigned* sync_cond;
     unsigned* sync_hold;
     float sync_thr;
+    // diagnostics only (launch_demod_fp32_timed): per-rank cycle sums of the
+    // kernel's stages, [rank * kDemodStages + stage]
+    unsigned long long* stage_cycles;
 };
+constexpr int kDemodStages = 20;
 // Radix plans the fused kernel is compiled for (8192-point plan | 16384-point
 // plan << 2): 16x16x32 | 16x32x32, 32x16x16 | 16x32x32, 16x16x32 | 32x32x16,
 // 32x16x16 | 32x32x16.  The other plans of the transforms (16x32x16, 8x32x32;
@@ -66,6 +70,8 @@ constexpr int kFftPlans[kFftPlanCount] = {0, 1, 4, 5};
 
 size_t fp32_smem_bytes();
 cudaError_t launch_demod_fp32(const FastDemodParams& p, int num_clusters, cudaStream_t stream);
+// The same kernel (plan 0) with clock64() stage marks summed into p.stage_cycles.
+cudaError_t launch_demod_fp32_timed(const FastDemodParams& p, int num_clusters, cudaStream_t stream);
 
 // 2:1 half-band decimation of a capture (exactly one of src16 / src32, 16-byte
 // aligned): out_len float samples, output i centred on source sample 2 i.

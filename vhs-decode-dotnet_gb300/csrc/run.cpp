@@ -42,6 +42,7 @@
 #include <vector>
 
 #include "../../include/vhsdecode_gb300.h"
+#include "flac.hpp"
 #include "formats.hpp"
 #include "kernels.h"
 #include "session.hpp"
@@ -330,7 +331,7 @@ VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_run(
         if (!config->read_callback) return fail(VHSDECODE_GB300_STATUS_NULL_POINTER, "read_callback is null");
         if (!config->output_base_utf8 || !config->output_base_utf8[0])
             return fail(VHSDECODE_GB300_STATUS_NULL_POINTER, "output_base_utf8 is null");
-        if (config->input_sample_format > VHSDECODE_GB300_INPUT_INT16)
+        if (config->input_sample_format > VHSDECODE_GB300_INPUT_FLAC)
             return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "unknown input_sample_format");
         // vhsdecode_cuda_fast.cpp:255-275: factor 1 or 2; the source runs at
         // factor x sample_rate_mhz
@@ -341,6 +342,9 @@ VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_run(
             return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT,
                         "device_decimation_factor 2 needs a decode rate of 10..50 MHz");
         const bool f32_in = config->input_sample_format == VHSDECODE_GB300_INPUT_FLOAT32;
+        // FLAC input: the callback reads bytes of the stream, decoded on the
+        // device into int16 samples as they arrive
+        const bool flac_in = config->input_sample_format == VHSDECODE_GB300_INPUT_FLAC;
         const size_t esz = f32_in ? sizeof(float) : sizeof(int16_t);
         const auto t0 = std::chrono::steady_clock::now();
         Outputs out;
@@ -357,18 +361,46 @@ VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_run(
         // window geometry in source samples (decode samples x factor)
         const int64_t grid_src = kGrid * (int64_t)factor;
         const int64_t win_src = window_grids() * grid_src;
-        const uint64_t total = config->total_samples;
+        const uint64_t total = flac_in ? 0 : config->total_samples;   // FLAC: total_samples counts bytes
         const uint64_t cap_src = total ? std::min<uint64_t>((uint64_t)win_src, total) : (uint64_t)win_src;
         if (cap_src / factor < (uint64_t)kBlock && total)
             return fail(VHSDECODE_GB300_STATUS_INPUT_ERROR, "input shorter than one block");
 
-        Prefetch pre(config, esz, latch);
+        Prefetch pre(config, flac_in ? 1 : esz, latch);
         std::vector<unsigned char> buf;   // source samples [buf_off, buf_off + buf.size() / esz)
         uint64_t buf_off = 0;
         bool eof = false;
+        FlacStreamDecoder flac;
+        std::vector<unsigned char> fbytes;   // FLAC bytes not decoded yet
+        std::vector<int16_t> pcm;
+        bool flac_started = false;
+        if (flac_in) flac.init(config->device_id);
         auto fill_to = [&](uint64_t end) {
-            while (!eof && buf_off + buf.size() / esz < end)
-                if (!pre.next(buf)) eof = true;
+            while (!eof && buf_off + buf.size() / esz < end) {
+                if (!flac_in) {
+                    if (!pre.next(buf)) eof = true;
+                    continue;
+                }
+                const bool more = pre.next(fbytes);
+                if (!flac_started) {
+                    FlacInfo fi{};
+                    if (fbytes.size() < 4096 && more) continue;   // the metadata first
+                    if (flac_stream_info(fbytes.data(), fbytes.size(), fi) != VHSDECODE_GB300_STATUS_OK) {
+                        if (more) continue;
+                        throw Failure(VHSDECODE_GB300_STATUS_INPUT_ERROR, g_last_error);
+                    }
+                    if (fi.channels != 1 || fi.bits_per_sample != 16)
+                        throw Failure(VHSDECODE_GB300_STATUS_INPUT_ERROR, "FLAC stream is not 16-bit mono");
+                    fbytes.erase(fbytes.begin(), fbytes.begin() + (std::ptrdiff_t)fi.first_frame);
+                    flac_started = true;
+                }
+                pcm.clear();
+                const size_t used = flac.decode(fbytes.data(), fbytes.size(), !more, pcm);
+                fbytes.erase(fbytes.begin(), fbytes.begin() + (std::ptrdiff_t)used);
+                const unsigned char* pb = reinterpret_cast<const unsigned char*>(pcm.data());
+                buf.insert(buf.end(), pb, pb + pcm.size() * sizeof(int16_t));
+                if (!more) eof = true;
+            }
         };
         fill_to((uint64_t)win_src);
         if (latch.requested.load()) return fail(VHSDECODE_GB300_STATUS_CANCELLED, "decode cancelled");

@@ -206,6 +206,7 @@ struct vhsdecode_gb300_session {
     cudaStream_t drop_stream = nullptr;  // a field batch's dropout chain, beside its hsync and TBC
     cudaEvent_t drop_fork = nullptr, drop_hsync = nullptr, drop_join = nullptr;
     bool stage_timing = false;           // VHSD_STAGE_TIMING set: per-stage kernel times to stderr
+    unsigned long long* demod_cycles = nullptr;   // VHSD_DEMOD_TIMING set: fused-demod stage cycles
     cudaEvent_t stage_ev[4] = {};
     float stage_ms[3] = {};
     uint32_t segments = 0;

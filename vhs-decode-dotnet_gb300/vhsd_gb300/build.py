@@ -18,7 +18,7 @@ OBJ = os.path.join(LIB_DIR, "obj")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["demod_fp32.cu", "demod_fp64.cu", "field_kernels.cu", "test_entries.cu", "decimate.cu",
            "abi.cpp", "control.cpp", "filters.cpp", "noalloc.cu",
-           "server.cpp", "run.cpp"]
+           "server.cpp", "run.cpp", "flac.cu"]
 
 
 def nvcc():

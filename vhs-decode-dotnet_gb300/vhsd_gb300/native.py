@@ -27,7 +27,7 @@ STATUS_INTERNAL_ERROR = -20007
 PROFILE_NTSC, PROFILE_PAL, PROFILE_PAL_M = 0, 1, 2
 TAPE_SP, TAPE_LP, TAPE_EP = 0, 1, 2
 FORMAT_VHS, FORMAT_SVHS = 0, 1
-INPUT_FLOAT32, INPUT_INT16 = 0, 1
+INPUT_FLOAT32, INPUT_INT16, INPUT_FLAC = 0, 1, 2
 PRECISION_FP32_FUSED, PRECISION_FP64_PLAIN = 0, 1
 DECODE_DEVICE_INPUT = 0x1
 DECODE_DEMOD_ONLY = 0x2
@@ -37,6 +37,7 @@ LIB_PATH = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__
                         "libvhsdecode_gb300.so")
 
 EXPORTS = [
+    "vhsdecode_gb300_flac_info", "vhsdecode_gb300_flac_decode",
     "vhsdecode_gb300_get_abi_version", "vhsdecode_gb300_get_runtime_info", "vhsdecode_gb300_run",
     "vhsdecode_gb300_get_last_error", "vhsdecode_gb300_session_create",
     "vhsdecode_gb300_session_destroy", "vhsdecode_gb300_session_set_stream",
@@ -70,6 +71,13 @@ class BackendUnavailable(NativeError):
 READ_CB = ctypes.CFUNCTYPE(ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64,
                            ctypes.c_size_t)
 CANCEL_CB = ctypes.CFUNCTYPE(ctypes.c_int32, ctypes.c_void_p)
+
+
+class FlacInfo(ctypes.Structure):
+    _fields_ = [("struct_size", ctypes.c_uint32), ("sample_rate", ctypes.c_uint32),
+                ("channels", ctypes.c_uint32), ("bits_per_sample", ctypes.c_uint32),
+                ("min_block", ctypes.c_uint32), ("max_block", ctypes.c_uint32),
+                ("total_samples", ctypes.c_uint64), ("first_frame_offset", ctypes.c_uint64)]
 
 
 class RuntimeInfo(ctypes.Structure):
@@ -208,6 +216,9 @@ def load(path: str = LIB_PATH):
     L.vhsdecode_gb300_server_destroy.restype = None
     L.vhsdecode_gb300_pulse_events_noalloc.argtypes = [_vp, ctypes.c_int64, ctypes.c_double, _vp,
                                                        ctypes.c_int64, _vp, _vp]
+    L.vhsdecode_gb300_flac_info.argtypes = [_vp, ctypes.c_uint64, _P(FlacInfo)]
+    L.vhsdecode_gb300_flac_decode.argtypes = [_vp, ctypes.c_uint64, _vp, ctypes.c_uint64,
+                                              _P(ctypes.c_uint64), ctypes.c_int32]
     for name in EXPORTS:
         if not hasattr(L, name):
             raise NativeError(STATUS_INTERNAL_ERROR, "missing export " + name)
@@ -230,6 +241,27 @@ def check(status):
 
 def _ptr(a):
     return ctypes.c_void_p(a.ctypes.data)
+
+
+def flac_info(data):
+    """STREAMINFO of a FLAC stream (bytes), through the C ABI (no GPU needed)."""
+    info = FlacInfo()
+    info.struct_size = ctypes.sizeof(FlacInfo)
+    buf = np.frombuffer(bytes(data), np.uint8)
+    check(load().vhsdecode_gb300_flac_info(_ptr(buf), len(buf), ctypes.byref(info)))
+    return info
+
+
+def flac_decode(data, device=0):
+    """int16 samples of a 16-bit mono FLAC stream, decoded on the GPU."""
+    buf = np.frombuffer(bytes(data), np.uint8)
+    n = ctypes.c_uint64(0)
+    L = load()
+    check(L.vhsdecode_gb300_flac_decode(_ptr(buf), len(buf), None, 0, ctypes.byref(n), device))
+    out = np.empty(n.value, np.int16)
+    check(L.vhsdecode_gb300_flac_decode(_ptr(buf), len(buf), _ptr(out), len(out), ctypes.byref(n),
+                                        device))
+    return out
 
 
 def runtime_info(device=0):
