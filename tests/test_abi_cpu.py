@@ -306,12 +306,13 @@ def test_flac_writer_and_reader_round_trip():
     # the test-side writer covers every subframe and residual form; its
     # stream decodes (by the bit-level reader) to the samples it was given
     from oracle import flac
+    from vhsd_gb300 import ldf
     rng = np.random.default_rng(3)
     t = np.arange(70_000)
     x = (6000 * np.sin(2 * np.pi * 0.11 * t) + rng.normal(0, 300, len(t))).astype(np.int16)
     x[4096 * 3:4096 * 4] &= ~1          # a frame with a wasted bit
     x[4096 * 6:4096 * 7] = -1234         # a constant frame
     for bs in (4096, 1152, 4608):
-        data = flac.encode(x, blocksize=bs, seed=bs, wasted_frames=(3,))
+        data = ldf.write(x, blocksize=bs, seed=bs, wasted_frames=(3,))
         assert flac.stream_info(data)["total_samples"] == len(x)
         assert np.array_equal(flac.decode(data), x)

@@ -1,9 +1,10 @@
 """Device FLAC decoding of .ldf RF captures, through the C ABI.
 
 FLAC is lossless: the device decoder must return exactly the int16 samples the
-test-side writer (oracle/flac.py, RFC 9639) was given, for every subframe and
+.ldf writer (vhsd_gb300/ldf.py, RFC 9639) was given, for every subframe and
 residual form the writer produces, at several block sizes and at the full size
-of the 60-field NTSC workload.  A damaged stream is an input error, and run()
+of the 60-field NTSC workload (the bit-level reader oracle/flac.py reads the
+writer's streams back the same way, tests/test_abi_cpu.py).  A damaged stream is an input error, and run()
 fed FLAC bytes writes the same files as run() fed the int16 samples.
 """
 import ctypes
@@ -27,9 +28,8 @@ def rf_small():
 
 @pytest.mark.parametrize("blocksize", [4096, 1152, 4608])
 def test_flac_round_trip_is_bit_exact(gpu, rf_small, blocksize):
-    from oracle import flac
-    from vhsd_gb300 import native
-    data = flac.encode(rf_small, blocksize=blocksize, seed=blocksize, wasted_frames=(3,))
+    from vhsd_gb300 import ldf, native
+    data = ldf.write(rf_small, blocksize=blocksize, seed=blocksize, wasted_frames=(3,))
     info = native.flac_info(data)
     assert info.total_samples == len(rf_small) and info.channels == 1
     got = native.flac_decode(data)
@@ -39,18 +39,16 @@ def test_flac_round_trip_is_bit_exact(gpu, rf_small, blocksize):
 def test_flac_full_size_round_trip(gpu):
     # the 41 M-sample NTSC workload: lossless at full size
     import bench
-    from oracle import flac
-    from vhsd_gb300 import native
+    from vhsd_gb300 import ldf, native
     rf = bench.workload("ntsc60")
-    data = flac.encode(rf, seed=60)
+    data = ldf.write(rf, seed=60)
     got = native.flac_decode(data)
     assert np.array_equal(got, rf)
 
 
 def test_damaged_flac_is_an_input_error(gpu, rf_small):
-    from oracle import flac
-    from vhsd_gb300 import native
-    data = bytearray(flac.encode(rf_small[:200_000], seed=1))
+    from vhsd_gb300 import ldf, native
+    data = bytearray(ldf.write(rf_small[:200_000], seed=1))
     # a flipped bit in the middle of the stream: the frame's CRC-16 (or its
     # structure) no longer matches
     data[len(data) // 2] ^= 0x10
@@ -58,7 +56,7 @@ def test_damaged_flac_is_an_input_error(gpu, rf_small):
         native.flac_decode(bytes(data))
     assert e.value.status == native.STATUS_INPUT_ERROR
     # a stream cut inside its last frame
-    good = flac.encode(rf_small[:200_000], seed=1)
+    good = ldf.write(rf_small[:200_000], seed=1)
     with pytest.raises(native.NativeError):
         native.flac_decode(good[:-100])
 
@@ -100,10 +98,9 @@ def _run(data, base, fmt, monkeypatch, grids="3"):
 def test_run_from_flac_bytes_equals_int16(gpu, tmp_path, monkeypatch):
     # a 12-field capture: its FLAC stream spans several read chunks and the
     # decode several windows
-    from oracle import flac
-    from vhsd_gb300 import native, synth
+    from vhsd_gb300 import ldf, native, synth
     rf, _ = synth.generate(synth.config("pal_small", fields=12, seed=12))
-    data = flac.encode(rf, seed=12)
+    data = ldf.write(rf, seed=12)
     assert len(data) > (1 << 22)
     a = _run(data, str(tmp_path / "flac"), native.INPUT_FLAC, monkeypatch)
     b = _run(rf, str(tmp_path / "s16"), native.INPUT_INT16, monkeypatch)
