@@ -376,6 +376,9 @@ def run_ours(args, world, rank, local):
     serving = None
     if rank == 0 and world == 1 and not args.skip_serve:
         serving = run_serving(args, local)
+    flac_leg = None
+    if rank == 0 and world == 1 and not args.skip_flac:
+        flac_leg = run_flac(rf)
     if rank == 0:
         line = {"metric": METRIC, "value": round(value, 3), "unit": "MSPS", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
@@ -408,6 +411,7 @@ def run_ours(args, world, rank, local):
                 "plain_fp64": plain,
                 "decimated": decimated,
                 "serving": serving,
+                "flac_decode": flac_leg,
                 "gpu_launches": int(launches),
                 "clocks": clk,
                 "stage_ms": {"demod": round(avg_demod, 4), "field_kernels_and_host": round(r.field_ms, 4),
@@ -519,18 +523,68 @@ def run_serving(args, local):
                                  tbc_out=outs[st["system"]][k % 8], tape_format=tfmt[st["tape"]]))
     res = [sv.wait(t) for t in tickets]
     t_end = time.perf_counter() - t0
+    # capacity: the same mix closed-loop, two windows per worker always in
+    # flight, for a few seconds; headroom = capacity / offered load - 1
+    inflight = []
+    cap_samples = 0
+    t1 = time.perf_counter()
+    k = 0
+    while time.perf_counter() - t1 < args.serve_capacity_seconds or inflight:
+        while len(inflight) < 2 * args.serve_workers and time.perf_counter() - t1 < args.serve_capacity_seconds:
+            si = int(rng.integers(0, nstreams))
+            st = streams[si]
+            x, off, seek = window(st)
+            cap_samples += len(x)
+            inflight.append(sv.submit(si, prof[st["system"]], x, off, seek=seek, sample_rate_mhz=st["mhz"],
+                                      tbc_out=outs[st["system"]][k % 8], tape_format=tfmt[st["tape"]]))
+            k += 1
+        sv.wait(inflight.pop(0))
+    cap_s = time.perf_counter() - t1
     sv.close()
+    capacity = cap_samples / cap_s / 1e6
+    offered = samples / dur / 1e6
     lat = np.array([r.latency_ms for r in res])
     ok = sum(1 for r in res if r.status == 0)
     return {"windows": len(res), "ok": ok, "offered_windows_per_s": rate, "streams": nstreams,
             "window_s": win_s, "workers": args.serve_workers, "seconds": round(t_end, 3),
+            "capacity_msps": round(capacity, 1), "headroom": round(capacity / offered - 1.0, 3),
             "p50_ms": round(float(np.percentile(lat, 50)), 2), "p99_ms": round(float(np.percentile(lat, 99)), 2),
             "mean_queue_ms": round(float(np.mean([r.queue_ms for r in res])), 2),
             "msps": round(samples / t_end / 1e6, 1),
-            "offered_msps": round(samples / dur / 1e6, 1),
+            "offered_msps": round(offered, 1),
             "fields": int(sum(r.fields for r in res)),
             "mix": [m[4] for m in SERVE_MIX],
             "data": "synthetic, 8-field recordings repeated to 6 s per format; TBC copied to pinned host"}
+
+
+def run_flac(rf):
+    """Device FLAC decoding of the workload written as a 16-bit mono FLAC stream
+    (vhsd_gb300.ldf writer, 4096-sample frames; cached in /tmp): samples per
+    second through vhsdecode_gb300_flac_decode, host bytes in, host samples
+    out (the copies inside the timed calls)."""
+    from vhsd_gb300 import native
+    cache = os.path.join("/tmp", "vhsd_workload_flac_%d.bin" % len(rf))
+    if os.path.exists(cache):
+        data = open(cache, "rb").read()
+    else:
+        from vhsd_gb300 import ldf   # the writer makes the input; it is not timed
+        data = ldf.write(rf, seed=60)
+        try:
+            open(cache, "wb").write(data)
+        except OSError:
+            pass
+    got = native.flac_decode(data)   # warm-up, and a check that it is lossless
+    if not np.array_equal(got, rf):
+        raise RuntimeError("FLAC decode differs from the capture")
+    times = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        native.flac_decode(data)
+        times.append(time.perf_counter() - t0)
+    t = min(times)
+    return {"value": round(len(rf) / t / 1e6, 1), "unit": "MSPS", "ms": round(t * 1e3, 2),
+            "compressed_bytes": len(data), "frames": (len(rf) + 4095) // 4096,
+            "note": "host FLAC bytes in, host int16 out, best of 3; bit-exact to the capture"}
 
 
 def run_decimated(args, local, rf, prof, tfmt, stream):
@@ -600,7 +654,9 @@ def main():
     ap.add_argument("--skip-plain", action="store_true")
     ap.add_argument("--skip-serve", action="store_true")
     ap.add_argument("--serve-rate", type=float, default=200.0, help="window arrivals per second")
-    ap.add_argument("--serve-seconds", type=float, default=3.0)
+    ap.add_argument("--serve-seconds", type=float, default=20.0)
+    ap.add_argument("--serve-capacity-seconds", type=float, default=4.0)
+    ap.add_argument("--skip-flac", action="store_true")
     ap.add_argument("--serve-workers", type=int, default=4)
     ap.add_argument("--skip-decimated", action="store_true")
     ap.add_argument("--profile-demod", action="store_true",

@@ -101,6 +101,7 @@ def test_run_from_flac_bytes_equals_int16(gpu, tmp_path, monkeypatch):
     from vhsd_gb300 import ldf, native, synth
     rf, _ = synth.generate(synth.config("pal_small", fields=12, seed=12))
     data = ldf.write(rf, seed=12)
+    monkeypatch.setenv("VHSD_RUN_FLAC_CHUNK", str(1 << 20))   # frames straddle the chunk joins
     assert len(data) > (1 << 22)
     a = _run(data, str(tmp_path / "flac"), native.INPUT_FLAC, monkeypatch)
     b = _run(rf, str(tmp_path / "s16"), native.INPUT_INT16, monkeypatch)

@@ -13,10 +13,13 @@
 //   its number continues the stream's sequence, so a sync pattern inside
 //   compressed data (which also needs a matching CRC-8) is skipped;
 // * k_flac_frames decodes each frame on its own thread (the residual is a
-//   bit-serial Rice code and the LPC restoration a recurrence, so a frame is
-//   sequential work; captures have thousands of frames per second of RF),
-//   checks that the subframe ends where the next frame begins and that the
-//   frame's CRC-16 matches, and writes int16 samples in place.
+//   bit-serial Rice code and the prediction a recurrence, so a frame is
+//   sequential work; captures have thousands of frames per second of RF):
+//   each residual value is read and predicted at once, the predictor's
+//   coefficients and history held in registers (one code path per predictor
+//   order), frames handed to threads sorted by subframe type so a warp's lanes
+//   run the same path; it checks that the subframe ends where the next frame
+//   begins and that the frame's CRC-16 matches, and writes int16 samples.
 //
 // Only what RF captures use is accepted: one channel of 16 bits per sample.
 #include <cuda_runtime.h>
@@ -24,6 +27,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -181,49 +185,132 @@ __global__ void k_flac_sync(const uint8_t* __restrict__ p, int64_t n, int64_t* c
     if (k < cap) cand[k] = at;
 }
 
-constexpr int kHist = 32;   // LPC history ring
-
-__device__ __forceinline__ int residual(BitReader& r, int32_t* out, int block, int order, int bps_limit) {
-    const int method = (int)r.get(2);
-    if (method > 1) return 1;
-    const int pbits = method == 0 ? 4 : 5;
-    const int esc = (1 << pbits) - 1;
-    const int porder = (int)r.get(4);
-    const int parts = 1 << porder;
-    if ((block >> porder) < order || (block & (parts - 1))) return 2;
-    int i = 0;
-    for (int pt = 0; pt < parts; pt++) {
-        const int cnt = (block >> porder) - (pt == 0 ? order : 0);
-        const int k = (int)r.get(pbits);
-        if (k == esc) {
-            const int width = (int)r.get(5);
-            for (int j = 0; j < cnt; j++) out[i++] = r.sget(width);
-        } else {
-            for (int j = 0; j < cnt; j++) {
-                const int32_t q = r.unary(1 << 20);
-                if (q < 0) return 3;
-                const uint32_t u = ((uint32_t)q << k) | r.get(k);
-                out[i++] = (int32_t)(u >> 1) ^ -(int32_t)(u & 1);
-            }
-        }
-        if (r.overrun()) return 4;
+// Residual of a subframe (RFC 9639 section 9.2.7), read one value at a time:
+// partitions of Rice (4-bit parameters) or Rice2 (5-bit) codes, or escaped
+// partitions of raw signed values.
+struct Residual {
+    int pbits, esc, porder, part, parts, left, k, width, order, block;
+    bool escaped;
+    __device__ int init(BitReader& r, int block_, int order_) {
+        block = block_;
+        order = order_;
+        const int method = (int)r.get(2);
+        if (method > 1) return 1;
+        pbits = method == 0 ? 4 : 5;
+        esc = (1 << pbits) - 1;
+        porder = (int)r.get(4);
+        parts = 1 << porder;
+        if ((block >> porder) < order || (block & (parts - 1))) return 2;
+        part = -1;
+        left = 0;
+        return 0;
     }
-    (void)bps_limit;
+    // next residual value; false on a malformed or overrunning stream
+    __device__ __forceinline__ bool next(BitReader& r, int32_t& v) {
+        while (left == 0) {
+            if (++part >= parts) return false;
+            left = (block >> porder) - (part == 0 ? order : 0);
+            k = (int)r.get(pbits);
+            escaped = k == esc;
+            if (escaped) width = (int)r.get(5);
+            if (r.overrun()) return false;
+        }
+        left--;
+        if (escaped) {
+            v = r.sget(width);
+            return true;
+        }
+        const int32_t q = r.unary(1 << 20);
+        if (q < 0) return false;
+        const uint32_t u = ((uint32_t)q << k) | r.get(k);
+        v = (int32_t)(u >> 1) ^ -(int32_t)(u & 1);
+        return true;
+    }
+};
+
+// Fixed predictor of order O (RFC 9639 section 9.2.5), history in registers.
+template <int O>
+__device__ int fixed_subframe(BitReader& r, int block, int bps, int wasted, int16_t* o) {
+    int32_t h[O > 0 ? O : 1];   // h[0]: the latest sample
+#pragma unroll
+    for (int j = O - 1; j >= 0; j--) {
+        h[j] = r.sget(bps);
+        o[O - 1 - j] = (int16_t)(h[j] << wasted);
+    }
+    Residual res;
+    if (int e = res.init(r, block, O)) return e;
+    for (int i = O; i < block; i++) {
+        int32_t e;
+        if (!res.next(r, e)) return 5;
+        int32_t x = e;
+        if (O == 1) x += h[0];
+        if (O == 2) x += 2 * h[0] - h[1];
+        if (O == 3) x += 3 * h[0] - 3 * h[1] + h[2];
+        if (O == 4) x += 4 * h[0] - 6 * h[1] + 4 * h[2] - h[3];
+#pragma unroll
+        for (int j = O - 1; j > 0; j--) h[j] = h[j - 1];
+        if (O > 0) h[0] = x;
+        o[i] = (int16_t)(x << wasted);
+    }
     return 0;
 }
 
-// One frame per thread.  Residuals are decoded into the frame's own output
-// slots (as int32 scratch in `work`), then restored in place.
-__global__ void k_flac_frames(const uint32_t* __restrict__ words, int64_t nbytes, const FlacFrame* frames,
-                              int nframes, int32_t* work, int16_t* out, int* status) {
+// Linear predictor of order P (RFC 9639 section 9.2.6): coefficients and
+// history in registers, products accumulated in 64 bits.
+template <int P>
+__device__ int lpc_subframe(BitReader& r, int block, int bps, int wasted, int16_t* o) {
+    int32_t h[P];
+#pragma unroll
+    for (int j = P - 1; j >= 0; j--) {
+        h[j] = r.sget(bps);
+        o[P - 1 - j] = (int16_t)(h[j] << wasted);
+    }
+    const int prec = (int)r.get(4) + 1;
+    if (prec == 16) return 6;
+    const int shift = r.sget(5);
+    if (shift < 0) return 7;
+    int32_t c[P];
+#pragma unroll
+    for (int j = 0; j < P; j++) c[j] = r.sget(prec);
+    Residual res;
+    if (int e = res.init(r, block, P)) return e;
+    for (int i = P; i < block; i++) {
+        int32_t e;
+        if (!res.next(r, e)) return 5;
+        int64_t acc = 0;
+#pragma unroll
+        for (int j = 0; j < P; j++) acc += (int64_t)c[j] * h[j];
+        const int32_t x = e + (int32_t)(acc >> shift);
+#pragma unroll
+        for (int j = P - 1; j > 0; j--) h[j] = h[j - 1];
+        h[0] = x;
+        o[i] = (int16_t)(x << wasted);
+    }
+    return 0;
+}
+
+template <int P = 1>
+__device__ int lpc_dispatch(int order, BitReader& r, int block, int bps, int wasted, int16_t* o) {
+    if constexpr (P > 32) {
+        return 8;
+    } else {
+        if (order == P) return lpc_subframe<P>(r, block, bps, wasted, o);
+        return lpc_dispatch<P + 1>(order, r, block, bps, wasted, o);
+    }
+}
+
+// One frame per thread, frames taken in the order `order_idx` gives (sorted
+// by subframe type, so the lanes of a warp run the same predictor).
+__global__ void __launch_bounds__(128) k_flac_frames(const uint32_t* __restrict__ words, const FlacFrame* frames,
+                                                     const int* order_idx, int nframes, int16_t* out, int* status) {
     __shared__ uint16_t t16[256];   // per-thread table indices: shared, not constant, memory
     for (int i = threadIdx.x; i < 256; i += blockDim.x) t16[i] = c_crc16[i];
     __syncthreads();
-    const int f = blockIdx.x * blockDim.x + threadIdx.x;
-    if (f >= nframes) return;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nframes) return;
+    const int f = order_idx[t];
     const FlacFrame fr = frames[f];
     const uint8_t* bytes = reinterpret_cast<const uint8_t*>(words);
-    int32_t* res = work + fr.sample0;
     int16_t* o = out + fr.sample0;
     int err = 0;
     BitReader r;
@@ -231,7 +318,7 @@ __global__ void k_flac_frames(const uint32_t* __restrict__ words, int64_t nbytes
     const int block = fr.block;
     do {
         if (r.get(1) != 0) { err = 10; break; }
-        const int t = (int)r.get(6);
+        const int type = (int)r.get(6);
         int wasted = 0;
         if (r.get(1)) {
             const int32_t z = r.unary(15);
@@ -240,44 +327,28 @@ __global__ void k_flac_frames(const uint32_t* __restrict__ words, int64_t nbytes
         }
         const int bps = 16 - wasted;
         if (bps <= 0) { err = 12; break; }
-        if (t == 0) {
+        if (type == 0) {
             const int32_t v = r.sget(bps);
             for (int i = 0; i < block; i++) o[i] = (int16_t)(v << wasted);
-        } else if (t == 1) {
+        } else if (type == 1) {
             for (int i = 0; i < block; i++) o[i] = (int16_t)(r.sget(bps) << wasted);
-        } else if (t >= 8 && t <= 12) {
-            const int order = t - 8;
-            if (order > block) { err = 13; break; }
-            for (int i = 0; i < order; i++) res[i] = r.sget(bps);
-            const int e = residual(r, res + order, block, order, bps);
+        } else if (type >= 8 && type <= 12) {
+            const int ord = type - 8;
+            if (ord > block) { err = 13; break; }
+            int e = 0;
+            switch (ord) {
+            case 0: e = fixed_subframe<0>(r, block, bps, wasted, o); break;
+            case 1: e = fixed_subframe<1>(r, block, bps, wasted, o); break;
+            case 2: e = fixed_subframe<2>(r, block, bps, wasted, o); break;
+            case 3: e = fixed_subframe<3>(r, block, bps, wasted, o); break;
+            default: e = fixed_subframe<4>(r, block, bps, wasted, o); break;
+            }
             if (e) { err = 20 + e; break; }
-            for (int i = order; i < block; i++) {
-                int32_t pred = 0;
-                if (order == 1) pred = res[i - 1];
-                else if (order == 2) pred = 2 * res[i - 1] - res[i - 2];
-                else if (order == 3) pred = 3 * res[i - 1] - 3 * res[i - 2] + res[i - 3];
-                else if (order == 4) pred = 4 * res[i - 1] - 6 * res[i - 2] + 4 * res[i - 3] - res[i - 4];
-                res[i] += pred;
-            }
-            for (int i = 0; i < block; i++) o[i] = (int16_t)(res[i] << wasted);
-        } else if (t >= 32) {
-            const int order = t - 31;
-            if (order > block) { err = 14; break; }
-            for (int i = 0; i < order; i++) res[i] = r.sget(bps);
-            const int prec = (int)r.get(4) + 1;
-            if (prec == 16) { err = 15; break; }
-            const int shift = r.sget(5);
-            if (shift < 0) { err = 16; break; }
-            int32_t c[kHist];
-            for (int j = 0; j < order; j++) c[j] = r.sget(prec);
-            const int e = residual(r, res + order, block, order, bps);
+        } else if (type >= 32) {
+            const int ord = type - 31;
+            if (ord > block) { err = 14; break; }
+            const int e = lpc_dispatch(ord, r, block, bps, wasted, o);
             if (e) { err = 30 + e; break; }
-            for (int i = order; i < block; i++) {
-                int64_t acc = 0;
-                for (int j = 0; j < order; j++) acc += (int64_t)c[j] * res[i - 1 - j];
-                res[i] += (int32_t)(acc >> shift);
-            }
-            for (int i = 0; i < block; i++) o[i] = (int16_t)(res[i] << wasted);
         } else {
             err = 17;
             break;
@@ -292,7 +363,6 @@ __global__ void k_flac_frames(const uint32_t* __restrict__ words, int64_t nbytes
             crc = (uint16_t)((crc << 8) ^ t16[(crc >> 8) ^ bytes[i]]);
         if (crc != (uint16_t)((bytes[end_byte] << 8) | bytes[end_byte + 1])) { err = 40; break; }
     } while (false);
-    (void)nbytes;
     if (err) atomicCAS(status, 0, (f << 8) | err);
 }
 
@@ -417,10 +487,10 @@ void FlacStreamDecoder::reserve(size_t bytes, size_t samples, size_t frames) {
         ck(cudaMalloc(p, want), "cudaMalloc");
         have = want;
     };
-    grow((void**)&d_bytes, cap_bytes, (bytes + 64) & ~(size_t)15);
+    grow((void**)&d_bytes, cap_bytes, (bytes + 96) & ~(size_t)15);
     grow((void**)&d_cand, cap_cand, std::max<size_t>(frames, 1024) * sizeof(int64_t));
     grow((void**)&d_frames, cap_frames, std::max<size_t>(frames + 16, 64) * sizeof(FlacFrame));
-    grow((void**)&d_work, cap_work, std::max<size_t>(samples, 1) * sizeof(int32_t));
+    grow((void**)&d_work, cap_work, std::max<size_t>(frames, 1) * sizeof(int32_t));   // frame order
     grow((void**)&d_out, cap_out, std::max<size_t>(samples, 1) * sizeof(int16_t));
 }
 
@@ -431,7 +501,7 @@ size_t FlacStreamDecoder::decode(const uint8_t* p, size_t n, bool at_eof, std::v
     // compressed data that also pass the CRC-8 are about 1 in 2^24 positions)
     const size_t max_frames = n / 64 + 1024;
     reserve(n, 0, max_frames);
-    ck(cudaMemsetAsync(d_bytes, 0, (n + 64) & ~(size_t)15, stream), "memset");
+    ck(cudaMemsetAsync(d_bytes + (n & ~(size_t)15), 0, 80, stream), "memset");   // zero pad after the data
     ck(cudaMemcpyAsync(d_bytes, p, n, cudaMemcpyHostToDevice, stream), "h2d flac");
     ck(cudaMemsetAsync(d_misc, 0, 2 * sizeof(int), stream), "memset");
     const int cap = (int)(cap_cand / sizeof(int64_t));
@@ -491,11 +561,19 @@ size_t FlacStreamDecoder::decode(const uint8_t* p, size_t n, bool at_eof, std::v
     }
     const size_t nsamp = (size_t)(next_sample - sample_base);
     reserve(n, nsamp, frames.size());
+    // frames sorted by subframe type (the byte after the frame header), so the
+    // lanes of a warp decode with the same predictor
+    std::vector<int> idx(frames.size());
+    for (size_t i = 0; i < idx.size(); i++) idx[i] = (int)i;
+    std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) {
+        return (p[frames[(size_t)a].off + frames[(size_t)a].header_len] & 0x7E) <
+               (p[frames[(size_t)b].off + frames[(size_t)b].header_len] & 0x7E);
+    });
     ck(cudaMemcpyAsync(d_frames, frames.data(), frames.size() * sizeof(FlacFrame), cudaMemcpyHostToDevice, stream),
        "h2d frames");
-    k_flac_frames<<<(unsigned)((frames.size() + 63) / 64), 64, 0, stream>>>(
-        reinterpret_cast<const uint32_t*>(d_bytes), (int64_t)n, d_frames, (int)frames.size(), d_work, d_out,
-        d_misc + 1);
+    ck(cudaMemcpyAsync(d_work, idx.data(), idx.size() * sizeof(int), cudaMemcpyHostToDevice, stream), "h2d order");
+    k_flac_frames<<<(unsigned)((frames.size() + 127) / 128), 128, 0, stream>>>(
+        reinterpret_cast<const uint32_t*>(d_bytes), d_frames, d_work, (int)frames.size(), d_out, d_misc + 1);
     ck(cudaGetLastError(), "flac decode launch");
     int st = 0;
     const size_t old = out.size();
@@ -549,8 +627,25 @@ VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_flac_decode(
         if (st != VHSDECODE_GB300_STATUS_OK) return st;
         if (fi.channels != 1 || fi.bits_per_sample != 16)
             return fail(VHSDECODE_GB300_STATUS_INPUT_ERROR, "FLAC stream is not 16-bit mono");
-        FlacStreamDecoder dec;
-        dec.init(device_id);
+        // one decoder (device buffers, stream) per device, reused across calls;
+        // calls on one device are serialised
+        static std::mutex m;
+        static FlacStreamDecoder* decoders[64] = {};
+        if (device_id < 0 || device_id >= 64) return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "device_id out of range");
+        std::lock_guard<std::mutex> lk(m);
+        if (!decoders[device_id]) {
+            auto* d = new FlacStreamDecoder();
+            try {
+                d->init(device_id);
+            } catch (...) {
+                delete d;
+                throw;
+            }
+            decoders[device_id] = d;
+        }
+        FlacStreamDecoder& dec = *decoders[device_id];
+        ck(cudaSetDevice(device_id), "cudaSetDevice");
+        dec.reset();
         std::vector<int16_t> pcm;
         dec.decode(data + fi.first_frame, bytes - fi.first_frame, true, pcm);
         *samples = pcm.size();

@@ -33,6 +33,8 @@ public:
     ~FlacStreamDecoder();
     void init(int device);
     size_t decode(const uint8_t* p, size_t n, bool at_eof, std::vector<int16_t>& out);
+    // starts a new stream (the next chunk begins with its first frame)
+    void reset() { next_frame = next_sample = sample_base = decoded_frames = 0; }
     uint64_t decoded_frames = 0;
 
 private:
@@ -41,7 +43,7 @@ private:
     uint8_t* d_bytes = nullptr;
     int64_t* d_cand = nullptr;
     FlacFrame* d_frames = nullptr;
-    int32_t* d_work = nullptr;
+    int* d_work = nullptr;      // frame order of the decode launch
     int16_t* d_out = nullptr;
     int* d_misc = nullptr;
     size_t cap_bytes = 0, cap_cand = 0, cap_frames = 0, cap_work = 0, cap_out = 0;

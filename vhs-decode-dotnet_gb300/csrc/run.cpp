@@ -8,8 +8,9 @@
 // 330-355; src/cancellation_latch.h; CMakeLists.txt:453-480).  Here:
 //
 // * a prefetch thread reads the capture in order, in chunks of kReadChunk
-//   source samples, at most kPrefetchChunks ahead of the decode, and polls the
-//   cancel callback before each read;
+//   source samples (kFlacReadChunk bytes of a FLAC stream), at most
+//   kPrefetchChunks ahead of the decode, and polls the cancel callback before
+//   each read;
 // * a watcher thread polls the cancel callback while the GPU works, so the
 //   decode's field loop sees a cancellation within a field;
 // * the capture is decoded in windows of a fixed number of grid steps
@@ -57,6 +58,7 @@ constexpr int64_t kDefaultWindowGrids = 40;    // 39.3 M decode samples (about 0
 constexpr int64_t kMinWindowGrids = 3;         // room for two fields and the continuation
 constexpr size_t kReadChunk = (size_t)1 << 22; // source samples per read callback call
 constexpr size_t kPrefetchChunks = 4;
+constexpr size_t kFlacReadChunk = (size_t)1 << 25; // bytes per read callback call for FLAC input
 
 // Window length in grid steps; VHSD_RUN_WINDOW_GRIDS overrides the default
 // (tests use small windows to exercise many window joins on short captures).
@@ -64,6 +66,14 @@ int64_t window_grids() {
     const char* e = std::getenv("VHSD_RUN_WINDOW_GRIDS");
     int64_t g = e ? std::atoll(e) : kDefaultWindowGrids;
     return std::max<int64_t>(kMinWindowGrids, g > 0 ? g : kDefaultWindowGrids);
+}
+
+// Bytes per read of a FLAC stream; VHSD_RUN_FLAC_CHUNK overrides the default
+// (tests use small chunks so that frames straddle chunk joins).
+size_t flac_read_chunk() {
+    const char* e = std::getenv("VHSD_RUN_FLAC_CHUNK");
+    const long long v = e ? std::atoll(e) : 0;
+    return v >= 4096 ? (size_t)v : kFlacReadChunk;
 }
 
 // Monotonic cancellation latch polled from the decode, watcher and prefetch
@@ -84,8 +94,8 @@ struct Latch {
 // In-order reader of the capture on its own thread.
 class Prefetch {
 public:
-    Prefetch(const vhsdecode_gb300_config_v1* cfg, size_t esz, Latch& latch)
-        : cfg_(cfg), esz_(esz), latch_(latch), th_([this] { loop(); }) {}
+    Prefetch(const vhsdecode_gb300_config_v1* cfg, size_t esz, size_t chunk, Latch& latch)
+        : cfg_(cfg), esz_(esz), chunk_(chunk), latch_(latch), th_([this] { loop(); }) {}
     ~Prefetch() {
         {
             std::lock_guard<std::mutex> lk(m_);
@@ -123,7 +133,7 @@ private:
                 if (stop_) break;
             }
             if (latch_.poll()) break;
-            size_t ask = kReadChunk;
+            size_t ask = chunk_;
             if (total) {
                 if (off >= total) break;
                 ask = (size_t)std::min<uint64_t>(ask, total - off);
@@ -150,7 +160,7 @@ private:
     }
 
     const vhsdecode_gb300_config_v1* cfg_;
-    size_t esz_;
+    size_t esz_, chunk_;
     Latch& latch_;
     std::mutex m_;
     std::condition_variable cv_;
@@ -366,7 +376,9 @@ VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_run(
         if (cap_src / factor < (uint64_t)kBlock && total)
             return fail(VHSDECODE_GB300_STATUS_INPUT_ERROR, "input shorter than one block");
 
-        Prefetch pre(config, flac_in ? 1 : esz, latch);
+        // FLAC bytes come in larger chunks (about 45 M samples each), so each
+        // device decode launch has thousands of frames to spread over the SMs
+        Prefetch pre(config, flac_in ? 1 : esz, flac_in ? flac_read_chunk() : kReadChunk, latch);
         std::vector<unsigned char> buf;   // source samples [buf_off, buf_off + buf.size() / esz)
         uint64_t buf_off = 0;
         bool eof = false;
