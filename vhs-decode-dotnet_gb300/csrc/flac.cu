@@ -26,7 +26,10 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -228,14 +231,46 @@ struct Residual {
     }
 };
 
+// Output of one frame's samples: four int16 packed per 8-byte store when the
+// frame's first sample is 8-byte aligned (a thread's stores go to its own
+// frame, so a warp's scalar stores would touch 32 lines each).
+struct Out4 {
+    int16_t* o;
+    uint64_t a;
+    int i, n;
+    bool vec;
+    __device__ void init(int16_t* o_) {
+        o = o_;
+        a = 0;
+        i = n = 0;
+        vec = ((uintptr_t)o_ & 7) == 0;
+    }
+    __device__ __forceinline__ void put(int32_t x) {
+        if (!vec) {
+            o[i++] = (int16_t)x;
+            return;
+        }
+        a = (a >> 16) | ((uint64_t)(uint16_t)x << 48);
+        i++;
+        if (++n == 4) {
+            *reinterpret_cast<uint64_t*>(o + i - 4) = a;
+            n = 0;
+        }
+    }
+    __device__ __forceinline__ void flush() {
+        for (int k = 0; k < n; k++) o[i - n + k] = (int16_t)(a >> (16 * (4 - n + k)));
+        n = 0;
+    }
+};
+
 // Fixed predictor of order O (RFC 9639 section 9.2.5), history in registers.
 template <int O>
-__device__ int fixed_subframe(BitReader& r, int block, int bps, int wasted, int16_t* o) {
+__device__ int fixed_subframe(BitReader& r, int block, int bps, int wasted, Out4& o) {
     int32_t h[O > 0 ? O : 1];   // h[0]: the latest sample
 #pragma unroll
     for (int j = O - 1; j >= 0; j--) {
         h[j] = r.sget(bps);
-        o[O - 1 - j] = (int16_t)(h[j] << wasted);
+        o.put(h[j] << wasted);
     }
     Residual res;
     if (int e = res.init(r, block, O)) return e;
@@ -250,7 +285,7 @@ __device__ int fixed_subframe(BitReader& r, int block, int bps, int wasted, int1
 #pragma unroll
         for (int j = O - 1; j > 0; j--) h[j] = h[j - 1];
         if (O > 0) h[0] = x;
-        o[i] = (int16_t)(x << wasted);
+        o.put(x << wasted);
     }
     return 0;
 }
@@ -258,12 +293,12 @@ __device__ int fixed_subframe(BitReader& r, int block, int bps, int wasted, int1
 // Linear predictor of order P (RFC 9639 section 9.2.6): coefficients and
 // history in registers, products accumulated in 64 bits.
 template <int P>
-__device__ int lpc_subframe(BitReader& r, int block, int bps, int wasted, int16_t* o) {
+__device__ int lpc_subframe(BitReader& r, int block, int bps, int wasted, Out4& o) {
     int32_t h[P];
 #pragma unroll
     for (int j = P - 1; j >= 0; j--) {
         h[j] = r.sget(bps);
-        o[P - 1 - j] = (int16_t)(h[j] << wasted);
+        o.put(h[j] << wasted);
     }
     const int prec = (int)r.get(4) + 1;
     if (prec == 16) return 6;
@@ -277,20 +312,21 @@ __device__ int lpc_subframe(BitReader& r, int block, int bps, int wasted, int16_
     for (int i = P; i < block; i++) {
         int32_t e;
         if (!res.next(r, e)) return 5;
-        int64_t acc = 0;
+        // four partial sums, so the products do not form one dependent chain
+        int64_t acc[4] = {0, 0, 0, 0};
 #pragma unroll
-        for (int j = 0; j < P; j++) acc += (int64_t)c[j] * h[j];
-        const int32_t x = e + (int32_t)(acc >> shift);
+        for (int j = 0; j < P; j++) acc[j & 3] += (int64_t)c[j] * h[j];
+        const int32_t x = e + (int32_t)(((acc[0] + acc[1]) + (acc[2] + acc[3])) >> shift);
 #pragma unroll
         for (int j = P - 1; j > 0; j--) h[j] = h[j - 1];
         h[0] = x;
-        o[i] = (int16_t)(x << wasted);
+        o.put(x << wasted);
     }
     return 0;
 }
 
 template <int P = 1>
-__device__ int lpc_dispatch(int order, BitReader& r, int block, int bps, int wasted, int16_t* o) {
+__device__ int lpc_dispatch(int order, BitReader& r, int block, int bps, int wasted, Out4& o) {
     if constexpr (P > 32) {
         return 8;
     } else {
@@ -301,7 +337,7 @@ __device__ int lpc_dispatch(int order, BitReader& r, int block, int bps, int was
 
 // One frame per thread, frames taken in the order `order_idx` gives (sorted
 // by subframe type, so the lanes of a warp run the same predictor).
-__global__ void __launch_bounds__(128) k_flac_frames(const uint32_t* __restrict__ words, const FlacFrame* frames,
+__global__ void __launch_bounds__(64, 1) k_flac_frames(const uint32_t* __restrict__ words, const FlacFrame* frames,
                                                      const int* order_idx, int nframes, int16_t* out, int* status) {
     __shared__ uint16_t t16[256];   // per-thread table indices: shared, not constant, memory
     for (int i = threadIdx.x; i < 256; i += blockDim.x) t16[i] = c_crc16[i];
@@ -311,7 +347,8 @@ __global__ void __launch_bounds__(128) k_flac_frames(const uint32_t* __restrict_
     const int f = order_idx[t];
     const FlacFrame fr = frames[f];
     const uint8_t* bytes = reinterpret_cast<const uint8_t*>(words);
-    int16_t* o = out + fr.sample0;
+    Out4 o;
+    o.init(out + fr.sample0);
     int err = 0;
     BitReader r;
     r.init(words, fr.off + fr.header_len, fr.end);
@@ -329,9 +366,9 @@ __global__ void __launch_bounds__(128) k_flac_frames(const uint32_t* __restrict_
         if (bps <= 0) { err = 12; break; }
         if (type == 0) {
             const int32_t v = r.sget(bps);
-            for (int i = 0; i < block; i++) o[i] = (int16_t)(v << wasted);
+            for (int i = 0; i < block; i++) o.put(v << wasted);
         } else if (type == 1) {
-            for (int i = 0; i < block; i++) o[i] = (int16_t)(r.sget(bps) << wasted);
+            for (int i = 0; i < block; i++) o.put(r.sget(bps) << wasted);
         } else if (type >= 8 && type <= 12) {
             const int ord = type - 8;
             if (ord > block) { err = 13; break; }
@@ -353,6 +390,7 @@ __global__ void __launch_bounds__(128) k_flac_frames(const uint32_t* __restrict_
             err = 17;
             break;
         }
+        o.flush();
         if (r.overrun()) { err = 18; break; }
         // byte alignment, then the frame's CRC-16 must end the frame
         const int64_t bit = r.bitpos();
@@ -495,6 +533,15 @@ void FlacStreamDecoder::reserve(size_t bytes, size_t samples, size_t frames) {
 }
 
 size_t FlacStreamDecoder::decode(const uint8_t* p, size_t n, bool at_eof, std::vector<int16_t>& out) {
+    return decode_to(p, n, at_eof, [&](size_t count) {
+        const size_t old = out.size();
+        out.resize(old + count);
+        return out.data() + old;
+    });
+}
+
+size_t FlacStreamDecoder::decode_to(const uint8_t* p, size_t n, bool at_eof,
+                                    const std::function<int16_t*(size_t)>& dest) {
     if (n == 0) return 0;
     // header candidates: real frames of RF captures hold thousands of bytes; a
     // chunk may hold up to one candidate per 64 bytes (false sync patterns in
@@ -504,9 +551,15 @@ size_t FlacStreamDecoder::decode(const uint8_t* p, size_t n, bool at_eof, std::v
     ck(cudaMemsetAsync(d_bytes + (n & ~(size_t)15), 0, 80, stream), "memset");   // zero pad after the data
     ck(cudaMemcpyAsync(d_bytes, p, n, cudaMemcpyHostToDevice, stream), "h2d flac");
     ck(cudaMemsetAsync(d_misc, 0, 2 * sizeof(int), stream), "memset");
+    const bool timing = std::getenv("VHSD_STAGE_TIMING") != nullptr;
+    cudaEvent_t ev[4] = {};
+    if (timing)
+        for (auto& e : ev) ck(cudaEventCreate(&e), "event");
+    if (timing) ck(cudaEventRecord(ev[0], stream), "event");
     const int cap = (int)(cap_cand / sizeof(int64_t));
     k_flac_sync<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(d_bytes, (int64_t)n, d_cand, d_misc, cap);
     ck(cudaGetLastError(), "flac sync launch");
+    if (timing) ck(cudaEventRecord(ev[1], stream), "event");
     int count = 0;
     ck(cudaMemcpyAsync(&count, d_misc, sizeof(int), cudaMemcpyDeviceToHost, stream), "d2h");
     ck(cudaStreamSynchronize(stream), "sync");
@@ -572,15 +625,24 @@ size_t FlacStreamDecoder::decode(const uint8_t* p, size_t n, bool at_eof, std::v
     ck(cudaMemcpyAsync(d_frames, frames.data(), frames.size() * sizeof(FlacFrame), cudaMemcpyHostToDevice, stream),
        "h2d frames");
     ck(cudaMemcpyAsync(d_work, idx.data(), idx.size() * sizeof(int), cudaMemcpyHostToDevice, stream), "h2d order");
-    k_flac_frames<<<(unsigned)((frames.size() + 127) / 128), 128, 0, stream>>>(
+    if (timing) ck(cudaEventRecord(ev[2], stream), "event");
+    k_flac_frames<<<(unsigned)((frames.size() + 63) / 64), 64, 0, stream>>>(
         reinterpret_cast<const uint32_t*>(d_bytes), d_frames, d_work, (int)frames.size(), d_out, d_misc + 1);
+    if (timing) ck(cudaEventRecord(ev[3], stream), "event");
     ck(cudaGetLastError(), "flac decode launch");
     int st = 0;
-    const size_t old = out.size();
-    out.resize(old + nsamp);
-    ck(cudaMemcpyAsync(out.data() + old, d_out, nsamp * sizeof(int16_t), cudaMemcpyDeviceToHost, stream), "d2h");
+    int16_t* dst = dest(nsamp);
+    if (dst) ck(cudaMemcpyAsync(dst, d_out, nsamp * sizeof(int16_t), cudaMemcpyDeviceToHost, stream), "d2h");
     ck(cudaMemcpyAsync(&st, d_misc + 1, sizeof(int), cudaMemcpyDeviceToHost, stream), "d2h");
     ck(cudaStreamSynchronize(stream), "sync");
+    if (timing) {
+        float t_sync = 0, t_frames = 0;
+        cudaEventElapsedTime(&t_sync, ev[0], ev[1]);
+        cudaEventElapsedTime(&t_frames, ev[2], ev[3]);
+        std::fprintf(stderr, "vhsd flac: %zu bytes, %zu frames, header scan %.3f ms, frame decode %.3f ms\n", n,
+                     frames.size(), t_sync, t_frames);
+        for (auto& e : ev) cudaEventDestroy(e);
+    }
     if (st) {
         char msg[128];
         std::snprintf(msg, sizeof msg, "corrupt FLAC frame %lld (code %d)",
@@ -646,10 +708,18 @@ VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_flac_decode(
         FlacStreamDecoder& dec = *decoders[device_id];
         ck(cudaSetDevice(device_id), "cudaSetDevice");
         dec.reset();
-        std::vector<int16_t> pcm;
-        dec.decode(data + fi.first_frame, bytes - fi.first_frame, true, pcm);
-        *samples = pcm.size();
-        if (capacity) std::memcpy(out, pcm.data(), std::min<uint64_t>(capacity, pcm.size()) * sizeof(int16_t));
+        // the samples go straight to the caller's buffer when they fit
+        std::vector<int16_t> spill;
+        uint64_t produced = 0;
+        dec.decode_to(data + fi.first_frame, bytes - fi.first_frame, true, [&](size_t count) -> int16_t* {
+            produced = count;
+            if (count <= capacity) return out;
+            if (!capacity) return nullptr;
+            spill.resize(count);
+            return spill.data();
+        });
+        *samples = produced;
+        if (!spill.empty()) std::memcpy(out, spill.data(), capacity * sizeof(int16_t));
         return VHSDECODE_GB300_STATUS_OK;
     });
 }

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <functional>
 #include <vector>
 
 namespace vhsd {
@@ -33,6 +34,8 @@ public:
     ~FlacStreamDecoder();
     void init(int device);
     size_t decode(const uint8_t* p, size_t n, bool at_eof, std::vector<int16_t>& out);
+    // the same, with the chunk's samples copied to dest(count) (null: not copied)
+    size_t decode_to(const uint8_t* p, size_t n, bool at_eof, const std::function<int16_t*(size_t)>& dest);
     // starts a new stream (the next chunk begins with its first frame)
     void reset() { next_frame = next_sample = sample_base = decoded_frames = 0; }
     uint64_t decoded_frames = 0;

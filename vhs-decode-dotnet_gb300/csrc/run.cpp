@@ -58,7 +58,7 @@ constexpr int64_t kDefaultWindowGrids = 40;    // 39.3 M decode samples (about 0
 constexpr int64_t kMinWindowGrids = 3;         // room for two fields and the continuation
 constexpr size_t kReadChunk = (size_t)1 << 22; // source samples per read callback call
 constexpr size_t kPrefetchChunks = 4;
-constexpr size_t kFlacReadChunk = (size_t)1 << 25; // bytes per read callback call for FLAC input
+constexpr size_t kFlacReadChunk = (size_t)1 << 27; // bytes per read callback call for FLAC input
 
 // Window length in grid steps; VHSD_RUN_WINDOW_GRIDS overrides the default
 // (tests use small windows to exercise many window joins on short captures).
@@ -376,8 +376,9 @@ VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_run(
         if (cap_src / factor < (uint64_t)kBlock && total)
             return fail(VHSDECODE_GB300_STATUS_INPUT_ERROR, "input shorter than one block");
 
-        // FLAC bytes come in larger chunks (about 45 M samples each), so each
-        // device decode launch has thousands of frames to spread over the SMs
+        // FLAC bytes come in larger chunks (about 180 M samples each): a frame
+        // decodes serially on one thread, so a launch needs tens of thousands
+        // of frames to keep the SMs busy
         Prefetch pre(config, flac_in ? 1 : esz, flac_in ? flac_read_chunk() : kReadChunk, latch);
         std::vector<unsigned char> buf;   // source samples [buf_off, buf_off + buf.size() / esz)
         uint64_t buf_off = 0;

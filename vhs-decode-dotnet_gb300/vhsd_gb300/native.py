@@ -253,15 +253,19 @@ def flac_info(data):
 
 
 def flac_decode(data, device=0):
-    """int16 samples of a 16-bit mono FLAC stream, decoded on the GPU."""
+    """int16 samples of a 16-bit mono FLAC stream, decoded on the GPU (one call
+    when STREAMINFO states the length; a second, larger one when it is short)."""
     buf = np.frombuffer(bytes(data), np.uint8)
     n = ctypes.c_uint64(0)
     L = load()
-    check(L.vhsdecode_gb300_flac_decode(_ptr(buf), len(buf), None, 0, ctypes.byref(n), device))
-    out = np.empty(n.value, np.int16)
+    out = np.empty(max(1, flac_info(data).total_samples), np.int16)
     check(L.vhsdecode_gb300_flac_decode(_ptr(buf), len(buf), _ptr(out), len(out), ctypes.byref(n),
                                         device))
-    return out
+    if n.value > len(out):
+        out = np.empty(n.value, np.int16)
+        check(L.vhsdecode_gb300_flac_decode(_ptr(buf), len(buf), _ptr(out), len(out),
+                                            ctypes.byref(n), device))
+    return out[:n.value]
 
 
 def runtime_info(device=0):
