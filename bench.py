@@ -479,7 +479,7 @@ def run_serving(args, local):
     per_field = {"PAL": 313 * 1135, "NTSC": 263 * 910}
     outs = {sysn: [torch.empty(130 * per_field[sysn], dtype=torch.int16).pin_memory().numpy().view(np.uint16)
                    for _ in range(8)] for sysn in ("PAL", "NTSC")}
-    sv = native.Server(max_win, workers=args.serve_workers, device=local)
+    sv = native.Server(max_win, workers=args.serve_workers, device=local, max_batch=args.serve_batch)
 
     def window(st):
         src = sources[(st["system"], st["tape"], st["mhz"])]
@@ -546,7 +546,8 @@ def run_serving(args, local):
     lat = np.array([r.latency_ms for r in res])
     ok = sum(1 for r in res if r.status == 0)
     return {"windows": len(res), "ok": ok, "offered_windows_per_s": rate, "streams": nstreams,
-            "window_s": win_s, "workers": args.serve_workers, "seconds": round(t_end, 3),
+            "window_s": win_s, "workers": args.serve_workers, "max_batch": args.serve_batch,
+            "mean_batch": round(float(np.mean([r.batched for r in res])), 2), "seconds": round(t_end, 3),
             "capacity_msps": round(capacity, 1), "headroom": round(capacity / offered - 1.0, 3),
             "p50_ms": round(float(np.percentile(lat, 50)), 2), "p99_ms": round(float(np.percentile(lat, 99)), 2),
             "mean_queue_ms": round(float(np.mean([r.queue_ms for r in res])), 2),
@@ -656,6 +657,8 @@ def main():
     ap.add_argument("--serve-rate", type=float, default=200.0, help="window arrivals per second")
     ap.add_argument("--serve-seconds", type=float, default=20.0)
     ap.add_argument("--serve-capacity-seconds", type=float, default=4.0)
+    ap.add_argument("--serve-batch", type=int, default=1,
+                    help="windows a free worker demodulates in one launch (1: no batching)")
     ap.add_argument("--skip-flac", action="store_true")
     ap.add_argument("--serve-workers", type=int, default=4)
     ap.add_argument("--skip-decimated", action="store_true")

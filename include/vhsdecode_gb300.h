@@ -34,7 +34,7 @@
 #  define VHSDECODE_GB300_CALL
 #endif
 
-#define VHSDECODE_GB300_ABI_VERSION 0x00010003u
+#define VHSDECODE_GB300_ABI_VERSION 0x00010004u
 #define VHSDECODE_GB300_NAME_CAPACITY 128u
 
 #ifdef __cplusplus
@@ -365,7 +365,10 @@ typedef struct vhsdecode_gb300_server_config_v1 {
     uint32_t struct_size;
     int32_t device_id;
     uint32_t workers;               /* windows decoded at once (0 = 4) */
-    uint32_t reserved;
+    uint32_t max_batch;             /* 0 or 1: each window has its own launches; n > 1: a free
+                                       worker takes up to n waiting windows (any streams and
+                                       formats, not decimated) and demodulates all their blocks
+                                       in one persistent launch */
     uint64_t max_window_samples;    /* longest window accepted; sizes every slot */
     uint64_t memory_budget_bytes;   /* device memory for slots (0 = 80 % of free memory) */
 } vhsdecode_gb300_server_config_v1;
@@ -404,6 +407,8 @@ typedef struct vhsdecode_gb300_window_result_v1 {
     double queue_ms;                /* submit to start of decode */
     double decode_ms;
     double latency_ms;              /* submit to result */
+    uint32_t batched;               /* windows in the launch that demodulated this one */
+    uint32_t reserved;
 } vhsdecode_gb300_window_result_v1;
 
 VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_server_create(

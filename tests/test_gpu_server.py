@@ -157,3 +157,55 @@ def test_decimated_windows_match_the_session(gpu, ntsc_capture, pal_capture):
             assert out[:d.fields * per].tobytes() == s.tbc()[:d.fields].tobytes()
             # continuation offsets are source samples: twice the decode-rate grid
             assert (r.next_source_offset - off) % (2 * 983040) == 0
+
+
+def test_batched_windows_equal_alone(gpu, pal_capture, ntsc_capture, ntsc20_capture, svhs_capture):
+    # cross-stream batching: windows of different streams and formats (PAL VHS,
+    # NTSC VHS at 40 and 20 MSPS, PAL S-VHS with sub-deemphasis, NTSC VHS LP)
+    # queued behind one worker are demodulated in one persistent launch; each
+    # window's result equals its decode alone, bit for bit
+    from vhsd_gb300 import native
+    pal, _ = pal_capture
+    ntsc, _ = ntsc_capture
+    ntsc20, _ = ntsc20_capture
+    svhs, _ = svhs_capture
+    per_field = {native.PROFILE_PAL: 313 * 1135, native.PROFILE_NTSC: 263 * 910}
+    length = 1_400_000
+    jobs = []   # (stream, profile, offset, samples, max fields, tape format, MSPS, speed)
+    for k, (off, x) in enumerate(_windows(pal, 2, length)):
+        jobs.append((k, native.PROFILE_PAL, off, x, 2, native.FORMAT_VHS, 40.0, native.TAPE_SP))
+    for k, (off, x) in enumerate(_windows(ntsc, 2, length)):
+        jobs.append((10 + k, native.PROFILE_NTSC, off, x, 2, native.FORMAT_VHS, 40.0, native.TAPE_SP))
+    for k, (off, x) in enumerate(_windows(ntsc20, 1, 900_000)):
+        jobs.append((20 + k, native.PROFILE_NTSC, off, x, 2, native.FORMAT_VHS, 20.0, native.TAPE_SP))
+    for k, (off, x) in enumerate(_windows(svhs, 2, length)):
+        jobs.append((30 + k, native.PROFILE_PAL, off, x, 2, native.FORMAT_SVHS, 40.0, native.TAPE_SP))
+    off, x = _windows(ntsc, 1, length)[0]
+    jobs.append((40, native.PROFILE_NTSC, off, x, 2, native.FORMAT_VHS, 40.0, native.TAPE_LP))
+
+    def run(server):
+        outs, tickets = [], []
+        for stream, prof, off, x, mf, tape, mhz, speed in jobs:
+            out = np.zeros(mf * per_field[prof], np.uint16)
+            tickets.append(server.submit(stream, prof, x, source_offset=off, seek=True, max_fields=mf,
+                                         tbc_out=out, tape_format=tape, sample_rate_mhz=mhz,
+                                         tape_speed=speed))
+            outs.append(out)
+        return [server.wait(t) for t in tickets], outs
+
+    with native.Server(length, workers=1) as sv:
+        alone = []
+        for j in range(len(jobs)):
+            saved = list(jobs)
+            jobs[:] = [saved[j]]
+            r, o = run(sv)
+            jobs[:] = saved
+            alone.append((r[0], o[0]))
+    with native.Server(length, workers=1, max_batch=8) as sv:
+        res, outs = run(sv)
+    assert max(r.batched for r in res) >= 4   # the queued windows went into one launch
+    for (ra, oa), rb, ob in zip(alone, res, outs):
+        assert ra.status == 0 and rb.status == 0
+        assert ra.fields == rb.fields > 0
+        assert ra.first_field_is_first == rb.first_field_is_first
+        assert oa.tobytes() == ob.tobytes()

@@ -1199,6 +1199,157 @@ int32_t decode_impl(vhsdecode_gb300_session* s, const void* rf_in, uint64_t n_in
     return VHSDECODE_GB300_STATUS_OK;
 }
 
+// ---------------------------------------------------------------- batched windows
+// Cross-stream batching for the window server: the blocks of several windows
+// (each on its own session, of any format and sample rate) are demodulated by
+// one persistent launch of the fused kernel, which claims blocks from one
+// counter across a table of per-window parameters; then each window's pulse
+// scan, field loop and field stage run on its own session.  A window's
+// results equal its own decode: every block is computed by the same kernel
+// code from the same samples, and the pulse scan over the whole stream gives
+// the events the segmented scans give.
+
+BatchScratch::~BatchScratch() {
+    if (d_jobs) cudaFree(d_jobs);
+    if (d_start) cudaFree(d_start);
+    if (d_counter) cudaFree(d_counter);
+    if (h_jobs) cudaFreeHost(h_jobs);
+    if (h_start) cudaFreeHost(h_start);
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+}
+
+void BatchScratch::init(int max_windows) {
+    cap = max_windows;
+    ck(cudaEventCreate(&ev0), "cudaEventCreate");
+    ck(cudaEventCreate(&ev1), "cudaEventCreate");
+    ck(cudaMalloc(&d_jobs, (size_t)cap * sizeof(FastDemodParams)), "cudaMalloc");
+    ck(cudaMalloc(&d_start, (size_t)(cap + 1) * sizeof(int64_t)), "cudaMalloc");
+    ck(cudaMalloc(&d_counter, sizeof(unsigned)), "cudaMalloc");
+    ck(cudaHostAlloc((void**)&h_jobs, (size_t)cap * sizeof(FastDemodParams), cudaHostAllocDefault), "cudaHostAlloc");
+    ck(cudaHostAlloc((void**)&h_start, (size_t)(cap + 1) * sizeof(int64_t), cudaHostAllocDefault), "cudaHostAlloc");
+}
+
+bool batchable(const vhsdecode_gb300_session* s) { return s->fp32() && s->decim == 1; }
+
+// The FP32 decode after its demod has run: pulse events over the whole
+// stream, the host field loop, the field stage, the results.
+void decode_after_demod(vhsdecode_gb300_session* s, uint64_t n, uint32_t max_fields, DecodeCarry* carry,
+                        vhsdecode_gb300_decode_result_v1* res, float demod_ms) {
+    cudaStream_t cs = s->stream;
+    const int64_t nblocks = block_count(n);
+    const int64_t stream_len = nblocks * kStride;
+    uint32_t stop = 0;
+    double host_ms = 0.0;
+    if (nblocks > 0) {
+        ck(launch_pulse_bits_range(s->sync_cond.p, s->sync_hold.p, 0, stream_len, s->pc_counts.p, s->pc_offsets.p,
+                                   s->pc_events.p, s->pc_capacity, s->pc_total.p, cs), "pulse launch");
+        s->launches += kPulseKernels;
+        int64_t total = 0;
+        ck(cudaMemcpyAsync(&total, s->pc_total.p, sizeof(int64_t), cudaMemcpyDeviceToHost, cs), "d2h");
+        ck(cudaStreamSynchronize(cs), "sync");
+        if (total > s->pc_capacity)
+            throw Failure(VHSDECODE_GB300_STATUS_DECODE_ERROR, "sync pulse event capacity exceeded");
+        EventFeed feed;
+        feed.events.resize((size_t)total);
+        if (total)
+            ck(cudaMemcpy(feed.events.data(), s->pc_events.p, (size_t)total * sizeof(int64_t),
+                          cudaMemcpyDeviceToHost), "d2h events");
+        feed.upto = [](int64_t) {};
+        auto t0 = std::chrono::steady_clock::now();
+        host_field_loop<float>(s, s->s32.p, stream_len, max_fields, feed, stop, nullptr, carry);
+        host_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        ck(cudaEventRecord(s->ev[2], cs), "event");
+        launch_field_batch<float>(s, 0, (int)s->fields.size(), s->v32.p, s->s32.p, s->e32.p, stream_len,
+                                  s->field_stream);
+        collect_field_results(s, s->field_stream);
+        ck(cudaEventRecord(s->field_end, s->field_stream), "event");
+        ck(cudaStreamWaitEvent(cs, s->field_end, 0), "wait");
+    } else {
+        s->fields.clear();
+        if (carry) carry->next = carry->start;
+        ck(cudaEventRecord(s->ev[2], cs), "event");
+    }
+    ck(cudaEventRecord(s->ev[3], cs), "event");
+    ck(cudaEventSynchronize(s->ev[3]), "sync");
+    int rep = 0;
+    if (nblocks > 0) ck(cudaMemcpy(&rep, s->repair.p, sizeof(int), cudaMemcpyDeviceToHost), "d2h");
+    s->last_blocks = nblocks;
+    s->last_repairs = rep;
+    if (res) {
+        float t_all = 0, t_fld = 0;
+        cudaEventElapsedTime(&t_all, s->ev[0], s->ev[3]);
+        cudaEventElapsedTime(&t_fld, s->ev[2], s->ev[3]);
+        res->fields = (uint32_t)s->fields.size();
+        res->output_line_length = (uint32_t)s->outlen;
+        res->output_field_lines = (uint32_t)s->out_lines;
+        res->blocks = (uint64_t)nblocks;
+        res->stream_samples = (uint64_t)(nblocks * kStride);
+        res->repaired_blocks = (uint32_t)rep;
+        res->stop_reason = stop;
+        res->device_ms = t_all;
+        res->demod_ms = demod_ms;
+        res->field_ms = t_fld;
+        res->host_ms = host_ms;
+        res->kernel_launches = s->launches;
+        res->segments = 1;
+        res->fft_plan = (uint32_t)s->fft_plan;
+    }
+}
+
+void decode_batched(std::vector<BatchWindow>& wins, BatchScratch& bs, cudaStream_t st) {
+    if (wins.empty()) return;
+    if ((int)wins.size() > bs.cap) throw Failure(VHSDECODE_GB300_STATUS_INTERNAL_ERROR, "batch larger than its table");
+    vhsdecode_gb300_session* s0 = wins[0].s;
+    ck(cudaSetDevice(s0->device), "cudaSetDevice");
+    int64_t total = 0;
+    for (size_t i = 0; i < wins.size(); i++) {
+        BatchWindow& w = wins[i];
+        vhsdecode_gb300_session* s = w.s;
+        if (!batchable(s) || s->device != s0->device || s->fft_plan != s0->fft_plan)
+            throw Failure(VHSDECODE_GB300_STATUS_INTERNAL_ERROR, "window not batchable");
+        if (w.n > s->max_samples)
+            throw Failure(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "sample_count exceeds the session capacity");
+        s->fields.clear();
+        s->launches = 1;   // this window's share of the batched launch
+        s->segments = 1;
+        s->in_f32 = nullptr;
+        // the session's own stream waits for the batch stream before its field work
+        ck(cudaEventRecord(s->ev[0], st), "event");
+        if (w.n > 0)
+            ck(cudaMemcpyAsync(s->rf.p, w.samples, w.n * sizeof(int16_t), cudaMemcpyHostToDevice, st), "h2d rf");
+        ck(cudaMemsetAsync(s->repair.p, 0, sizeof(int), st), "memset");
+        const int64_t nb = block_count(w.n);
+        FastDemodParams p = fp32_params(s, s->rf.p);
+        p.first_block = 0;
+        p.nblocks = nb;
+        p.scratch = s0->scratch.p;   // per cluster of the launch
+        p.block_counter = nullptr;
+        bs.h_jobs[i] = p;
+        bs.h_start[i] = total;
+        total += nb;
+    }
+    bs.h_start[wins.size()] = total;
+    FastDemodParams m = bs.h_jobs[0];
+    m.nblocks = total;
+    m.block_counter = bs.d_counter;
+    m.batch_jobs = bs.d_jobs;
+    m.batch_start = bs.d_start;
+    m.batch_njobs = (int)wins.size();
+    ck(cudaMemcpyAsync(bs.d_jobs, bs.h_jobs, wins.size() * sizeof(FastDemodParams), cudaMemcpyHostToDevice, st),
+       "h2d jobs");
+    ck(cudaMemcpyAsync(bs.d_start, bs.h_start, (wins.size() + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, st),
+       "h2d jobs");
+    ck(cudaMemsetAsync(bs.d_counter, 0, sizeof(unsigned), st), "memset");
+    ck(cudaEventRecord(bs.ev0, st), "event");
+    ck(launch_demod_fp32_batched(m, s0->num_sms / 2, st), "batched demod launch");
+    ck(cudaEventRecord(bs.ev1, st), "event");
+    ck(cudaEventSynchronize(bs.ev1), "sync");
+    float demod_ms = 0.0f;
+    cudaEventElapsedTime(&demod_ms, bs.ev0, bs.ev1);
+    for (BatchWindow& w : wins) decode_after_demod(w.s, w.n, w.max_fields, w.carry, w.res, demod_ms);
+}
+
 }  // namespace detail
 }  // namespace vhsd
 

@@ -193,6 +193,9 @@ struct Shared {
     int flag;
     int pad_;
     long long next_blk[2];   // the cluster's next block, by iteration parity
+    int next_job[2];         // batched launch: the next block's window
+    int cur_job;
+    FastDemodParams job;     // batched launch: the current window's parameters
 };
 
 // Half-spectrum post-processing of a real FFT computed as a packed complex
@@ -616,9 +619,20 @@ using namespace vhsd::fp32;
         }                                                                                        \
     } while (0)
 
-template <int PLAN, bool TIMED>
+// Window of global block g in a batched launch (the last job starting at or before g).
+__device__ __forceinline__ int batch_job_of(const FastDemodParams& pk, int64_t g) {
+    int lo = 0, hi = pk.batch_njobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (pk.batch_start[mid] <= g) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+template <int PLAN, bool TIMED, bool BATCHED>
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(T, 1)
-vhsd_demod_fp32_kernel(FastDemodParams p) {
+vhsd_demod_fp32_kernel(FastDemodParams pk) {
     long long t_mark = 0;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Shared& sh = *reinterpret_cast<Shared*>(smem_raw);
@@ -630,25 +644,34 @@ vhsd_demod_fp32_kernel(FastDemodParams p) {
     Shared* rsh = cluster.map_shared_rank(&sh, rank ^ 1);
     float2* rbuf = rsh->buf;
 
-    for (int i = tid; i < 256; i += T) sh.tw.hi[i] = p.tw_hi[i];
-    for (int i = tid; i < 128; i += T) sh.tw.lo[i] = p.tw_lo[i];
-    for (int i = tid; i < 16; i += T) sh.tw.lo8[i] = p.tw_lo[8 * i];
+    for (int i = tid; i < 256; i += T) sh.tw.hi[i] = pk.tw_hi[i];
+    for (int i = tid; i < 128; i += T) sh.tw.lo[i] = pk.tw_lo[i];
+    for (int i = tid; i < 16; i += T) sh.tw.lo8[i] = pk.tw_lo[8 * i];
+    if constexpr (BATCHED) {
+        if (tid == 0) sh.cur_job = (blockIdx.x >> 1) < pk.nblocks ? batch_job_of(pk, blockIdx.x >> 1) : 0;
+    }
     __syncthreads();
 
     const int cluster_id = blockIdx.x >> 1;
     const int nclusters = gridDim.x >> 1;
     const float inv_n = 1.0f / (float)N;
     const float inv_m = 1.0f / (float)M;
-    const float freq = p.fs;
-
     // the RF of each block is prefetched into sh.theta (free from the demod's
     // last read until the next block's angles) while the previous block
     // finishes
     // (int16 captures only; a float capture is read from global memory)
+    // (batched launches take int16 captures only)
     const int16_t* rf_smem = reinterpret_cast<const int16_t*>(sh.theta);
-    const bool f32_in = p.rf_f32 != nullptr;
-    if (cluster_id < p.nblocks && !f32_in)
-        prefetch_rf(sh.theta, p.rf + (cluster_id + p.first_block) * (int64_t)S, tid);
+    const bool f32_in = !BATCHED && pk.rf_f32 != nullptr;
+    if (cluster_id < pk.nblocks && !f32_in) {
+        if constexpr (BATCHED) {
+            const FastDemodParams& j0 = pk.batch_jobs[sh.cur_job];
+            prefetch_rf(sh.theta, j0.rf + (cluster_id - pk.batch_start[sh.cur_job] + j0.first_block) * (int64_t)S,
+                        tid);
+        } else {
+            prefetch_rf(sh.theta, pk.rf + (cluster_id + pk.first_block) * (int64_t)S, tid);
+        }
+    }
     // Blocks: each cluster starts on block cluster_id and then claims the next
     // unclaimed block from the launch's counter, so clusters that start late
     // (their SMs busy with other work) or take the slow repair path simply
@@ -656,12 +679,33 @@ vhsd_demod_fp32_kernel(FastDemodParams p) {
     // index to both CTAs (slot by iteration parity); both read it after the
     // next cluster barrier, so the two ranks always agree.
     int par = 0;
-    for (int64_t blk = cluster_id; blk < p.nblocks;) {
+    int job = -1;
+    for (int64_t g = cluster_id; g < pk.nblocks;) {
+        // g: the block's index in the launch; blk: its index in its window
+        int64_t blk = g;
+        if constexpr (BATCHED) {
+            const int j = sh.cur_job;
+            if (j != job) {   // every thread of both CTAs is past the previous block
+                const unsigned long long* src = reinterpret_cast<const unsigned long long*>(pk.batch_jobs + j);
+                unsigned long long* dst = reinterpret_cast<unsigned long long*>(&sh.job);
+                for (int i = tid; i < (int)(sizeof(FastDemodParams) / 8); i += T) dst[i] = src[i];
+                job = j;
+                __syncthreads();
+            }
+            blk = g - pk.batch_start[j];
+        }
+        const FastDemodParams& p = BATCHED ? sh.job : pk;
+        const float freq = p.fs;
         if (rank == 0 && tid == 0) {
-            const long long nb = p.block_counter ? (long long)nclusters + atomicAdd(p.block_counter, 1)
-                                                 : (long long)(blk + nclusters);
+            const long long nb = pk.block_counter ? (long long)nclusters + atomicAdd(pk.block_counter, 1)
+                                                  : (long long)(g + nclusters);
             sh.next_blk[par] = nb;
             rsh->next_blk[par] = nb;
+            if constexpr (BATCHED) {
+                const int nj = nb < pk.nblocks ? batch_job_of(pk, nb) : 0;
+                sh.next_job[par] = nj;
+                rsh->next_job[par] = nj;
+            }
         }
         // ---------------- stage 1: RF forward FFT (packed, DIF split) -----
         prefetch_wait();
@@ -693,8 +737,17 @@ vhsd_demod_fp32_kernel(FastDemodParams p) {
         cluster.sync();
         VHSD_MARK(5);
         const int64_t nxt = sh.next_blk[par];
-        const bool has_next = nxt < p.nblocks && !f32_in;
-        const int16_t* x_next = has_next ? p.rf + (nxt + p.first_block) * (int64_t)S : nullptr;
+        const bool has_next = nxt < pk.nblocks && !f32_in;
+        const int16_t* x_next = nullptr;
+        if (has_next) {
+            if constexpr (BATCHED) {
+                const int nj = sh.next_job[par];
+                const FastDemodParams& jn = pk.batch_jobs[nj];
+                x_next = jn.rf + (nxt - pk.batch_start[nj] + jn.first_block) * (int64_t)S;
+            } else {
+                x_next = pk.rf + (nxt + pk.first_block) * (int64_t)S;
+            }
+        }
         {
             // z[n] = A[n] + W^-n B[n], z[n+16384] = A[n] - W^-n B[n]; the
             // analytic signal stays in buf (chunk rank at local 0..8191,
@@ -999,7 +1052,11 @@ vhsd_demod_fp32_kernel(FastDemodParams p) {
         VHSD_MARK(18);
         cluster.sync();
         VHSD_MARK(19);
-        blk = nxt;
+        if constexpr (BATCHED) {
+            if (tid == 0) sh.cur_job = sh.next_job[par];
+            __syncthreads();
+        }
+        g = nxt;
         par ^= 1;
     }
 }
@@ -1008,20 +1065,37 @@ namespace vhsd {
 
 size_t fp32_smem_bytes() { return sizeof(fp32::Shared); }
 
-template <int PLAN, bool TIMED = false>
+template <int PLAN, bool TIMED = false, bool BATCHED = false>
 static cudaError_t launch_plan(const FastDemodParams& p, int clusters, cudaStream_t stream, int dev) {
     static std::atomic<uint64_t> attr_set{0};
     size_t smem = sizeof(fp32::Shared);
     const uint64_t bit = dev < 64 ? (uint64_t)1 << dev : 0;
     if (!bit || !(attr_set.load() & bit)) {
-        cudaError_t e = cudaFuncSetAttribute(vhsd_demod_fp32_kernel<PLAN, TIMED>,
+        cudaError_t e = cudaFuncSetAttribute(vhsd_demod_fp32_kernel<PLAN, TIMED, BATCHED>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         attr_set.fetch_or(bit);
     }
     if (p.nblocks <= 0) return cudaSuccess;
-    vhsd_demod_fp32_kernel<PLAN, TIMED><<<2 * clusters, fp32::T, smem, stream>>>(p);
+    vhsd_demod_fp32_kernel<PLAN, TIMED, BATCHED><<<2 * clusters, fp32::T, smem, stream>>>(p);
     return cudaGetLastError();
+}
+
+cudaError_t launch_demod_fp32_batched(const FastDemodParams& p, int num_clusters, cudaStream_t stream) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (p.nblocks > 0 && (!p.batch_jobs || !p.batch_start || p.batch_njobs <= 0)) return cudaErrorInvalidValue;
+    int clusters = num_clusters;
+    if (p.nblocks > 0 && clusters > p.nblocks) clusters = (int)p.nblocks;
+    if (clusters < 1) clusters = 1;
+    switch (p.fft_plan) {
+    case kFftPlans[0]: return launch_plan<kFftPlans[0], false, true>(p, clusters, stream, dev);
+    case kFftPlans[1]: return launch_plan<kFftPlans[1], false, true>(p, clusters, stream, dev);
+    case kFftPlans[2]: return launch_plan<kFftPlans[2], false, true>(p, clusters, stream, dev);
+    case kFftPlans[3]: return launch_plan<kFftPlans[3], false, true>(p, clusters, stream, dev);
+    default: return cudaErrorInvalidValue;
+    }
 }
 
 cudaError_t launch_demod_fp32_timed(const FastDemodParams& p, int num_clusters, cudaStream_t stream) {

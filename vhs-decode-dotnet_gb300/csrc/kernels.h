@@ -59,6 +59,13 @@ struct FastDemodParams {
     // diagnostics only (launch_demod_fp32_timed): per-rank cycle sums of the
     // kernel's stages, [rank * kDemodStages + stage]
     unsigned long long* stage_cycles;
+    // batched launch (launch_demod_fp32_batched): the blocks of several
+    // windows, each with its own parameters (capture, filters, format,
+    // outputs; int16 input) in batch_jobs[j], job j owning the global blocks
+    // [batch_start[j], batch_start[j + 1]); nblocks is then the total
+    const FastDemodParams* batch_jobs;
+    const int64_t* batch_start;
+    int batch_njobs;
 };
 constexpr int kDemodStages = 20;
 // Radix plans the fused kernel is compiled for (8192-point plan | 16384-point
@@ -72,6 +79,10 @@ size_t fp32_smem_bytes();
 cudaError_t launch_demod_fp32(const FastDemodParams& p, int num_clusters, cudaStream_t stream);
 // The same kernel (plan 0) with clock64() stage marks summed into p.stage_cycles.
 cudaError_t launch_demod_fp32_timed(const FastDemodParams& p, int num_clusters, cudaStream_t stream);
+// One persistent launch over the blocks of p.batch_njobs windows (p: the
+// shared twiddles, block counter, repair scratch and plan; the total in
+// p.nblocks).  Each block is computed exactly as in its window's own launch.
+cudaError_t launch_demod_fp32_batched(const FastDemodParams& p, int num_clusters, cudaStream_t stream);
 
 // 2:1 half-band decimation of a capture (exactly one of src16 / src32, 16-byte
 // aligned): out_len float samples, output i centred on source sample 2 i.

@@ -100,10 +100,12 @@ size_t estimate_slot_bytes(const vhsdecode_gb300_server* sv) {
 // Picks the first queued window whose stream is idle and for which a slot can
 // be had: an idle slot of its format, a new slot inside the budget, or a new
 // slot after releasing idle slots of other formats.  Returns false if none.
-bool pick(vhsdecode_gb300_server* sv, Request& out, Slot*& slot, std::vector<Slot*>& release) {
+bool pick(vhsdecode_gb300_server* sv, Request& out, Slot*& slot, std::vector<Slot*>& release,
+          bool batch_only = false) {
     for (auto it = sv->queue.begin(); it != sv->queue.end(); ++it) {
         History& h = sv->streams[it->w.stream_id];
         if (h.busy) continue;
+        if (batch_only && window_decim(it->w) != 1) continue;   // decimated windows decode alone
         Slot* found = nullptr;
         for (Slot* sl : sv->slots)
             if (!sl->busy && same_format(*sl, it->w)) { found = sl; break; }
@@ -198,22 +200,27 @@ void destroy_slot(Slot* sl) {
     delete sl;
 }
 
-void run_window(vhsdecode_gb300_server* sv, Slot* sl, const Request& rq, History hist,
-                vhsdecode_gb300_window_result_v1& r, History& out_hist) {
-    const vhsdecode_gb300_window_v1& w = rq.w;
-    // stream positions are source samples; the decode runs at source / decim
+// The decode carry of a window: a window that continues its stream (no seek,
+// starting at or before the stream's next field) resumes the stream's field
+// sequence at that field.
+bool window_carry(const vhsdecode_gb300_window_v1& w, const History& hist, DecodeCarry& carry) {
     const uint64_t decim = window_decim(w);
-    DecodeCarry carry;
+    carry = DecodeCarry{};
     carry.no_graph = true;   // every window has its own input pointer
-    bool cont = !w.seek && hist.valid && hist.next_abs >= w.source_offset;
+    const bool cont = !w.seek && hist.valid && hist.next_abs >= w.source_offset;
     if (cont) {
         carry.state = hist.state;
         carry.start = (int64_t)((hist.next_abs - w.source_offset) / decim);
     }
-    vhsdecode_gb300_decode_result_v1 dr{};
-    dr.struct_size = sizeof(dr);
-    decode_impl(sl->s, w.samples, w.sample_count, w.max_fields, 0, &dr, nullptr, &carry);
-    vhsdecode_gb300_session* s = sl->s;
+    return cont;
+}
+
+// Results of a decoded window: its TBC to the client's buffer, the window
+// result and the stream's history after it.
+void window_finish(vhsdecode_gb300_session* s, const vhsdecode_gb300_window_v1& w, const DecodeCarry& carry,
+                   bool cont, const vhsdecode_gb300_decode_result_v1& dr, vhsdecode_gb300_window_result_v1& r,
+                   History& out_hist) {
+    const uint64_t decim = window_decim(w);
     size_t per_field = (size_t)s->out_lines * s->outlen;
     if (w.tbc_out && dr.fields) {
         size_t nf = std::min<size_t>(dr.fields, w.tbc_capacity / per_field);
@@ -236,56 +243,133 @@ void run_window(vhsdecode_gb300_server* sv, Slot* sl, const Request& rq, History
     out_hist.next_abs = w.source_offset + decim * (uint64_t)std::max<int64_t>(0, carry.next);
 }
 
+void run_window(Slot* sl, const Request& rq, const History& hist, vhsdecode_gb300_window_result_v1& r,
+                History& out_hist) {
+    DecodeCarry carry;
+    const bool cont = window_carry(rq.w, hist, carry);
+    vhsdecode_gb300_decode_result_v1 dr{};
+    dr.struct_size = sizeof(dr);
+    decode_impl(sl->s, rq.w.samples, rq.w.sample_count, rq.w.max_fields, 0, &dr, nullptr, &carry);
+    window_finish(sl->s, rq.w, carry, cont, dr, r, out_hist);
+}
+
+// A window picked by a worker, with its slot, history and result.
+struct Item {
+    Request rq;
+    Slot* sl = nullptr;
+    History hist, out_hist;
+    vhsdecode_gb300_window_result_v1 r{};
+    DecodeCarry carry;
+    bool cont = false;
+    vhsdecode_gb300_decode_result_v1 dr{};
+};
+
 void worker_main(vhsdecode_gb300_server* sv) {
     cudaSetDevice(sv->cfg.device_id);
+    // cross-stream batching: the windows waiting when this worker becomes
+    // free (up to max_batch) are demodulated by one persistent launch
+    int max_batch = sv->cfg.max_batch > 1 ? (int)std::min<uint32_t>(sv->cfg.max_batch, 16u) : 1;
+    BatchScratch bs;
+    cudaStream_t bstream = nullptr;
+    if (max_batch > 1) {
+        try {
+            bs.init(max_batch);
+            ck(cudaStreamCreateWithFlags(&bstream, cudaStreamNonBlocking), "cudaStreamCreate");
+        } catch (...) {
+            max_batch = 1;   // no batching resources: windows decode one at a time
+        }
+    }
     for (;;) {
-        Request rq;
-        Slot* sl = nullptr;
+        std::vector<Item> items;
         std::vector<Slot*> release;
-        History hist;
         {
+            Item first;
             std::unique_lock<std::mutex> lk(sv->m);
-            sv->cv_work.wait(lk, [&] { return sv->stop || pick(sv, rq, sl, release); });
-            if (!sl) return;   // stopping
-            hist = sv->streams[rq.w.stream_id];
+            sv->cv_work.wait(lk, [&] { return sv->stop || pick(sv, first.rq, first.sl, release); });
+            if (!first.sl) break;   // stopping
+            items.push_back(first);
+            if (max_batch > 1 && window_decim(first.rq.w) == 1) {
+                for (;;) {
+                    if ((int)items.size() >= max_batch) break;
+                    Item more;
+                    if (!pick(sv, more.rq, more.sl, release, true)) break;
+                    items.push_back(more);
+                }
+            }
+            for (Item& it : items) it.hist = sv->streams[it.rq.w.stream_id];
         }
         for (Slot* old : release) destroy_slot(old);
-        vhsdecode_gb300_window_result_v1 r{};
-        r.struct_size = sizeof(r);
-        r.ticket = rq.ticket;
-        r.stream_id = rq.w.stream_id;
-        r.sample_count = rq.w.sample_count;
-        History out_hist = hist;
-        out_hist.busy = false;
+        for (Item& it : items) {
+            it.r.struct_size = sizeof(it.r);
+            it.r.ticket = it.rq.ticket;
+            it.r.stream_id = it.rq.w.stream_id;
+            it.r.sample_count = it.rq.w.sample_count;
+            it.out_hist = it.hist;
+            it.out_hist.busy = false;
+        }
         auto t_start = Clock::now();
-        r.status = guard([&] {
-            if (!sl->s) create_slot(sv, sl);
-            run_window(sv, sl, rq, hist, r, out_hist);
-            return VHSDECODE_GB300_STATUS_OK;
-        });
-        auto t_end = Clock::now();
-        r.queue_ms = ms_between(rq.submitted, t_start);
-        r.decode_ms = ms_between(t_start, t_end);
-        r.latency_ms = ms_between(rq.submitted, t_end);
+        std::vector<Clock::time_point> t_end(items.size());
+        if (items.size() == 1) {
+            Item& it = items[0];
+            it.r.status = guard([&] {
+                if (!it.sl->s) create_slot(sv, it.sl);
+                run_window(it.sl, it.rq, it.hist, it.r, it.out_hist);
+                return VHSDECODE_GB300_STATUS_OK;
+            });
+            t_end[0] = Clock::now();
+        } else {
+            int32_t st = guard([&] {
+                for (Item& it : items)
+                    if (!it.sl->s) create_slot(sv, it.sl);
+                std::vector<BatchWindow> wins;
+                for (Item& it : items) {
+                    it.cont = window_carry(it.rq.w, it.hist, it.carry);
+                    it.dr = vhsdecode_gb300_decode_result_v1{};
+                    it.dr.struct_size = sizeof(it.dr);
+                    wins.push_back(BatchWindow{it.sl->s, static_cast<const int16_t*>(it.rq.w.samples),
+                                               it.rq.w.sample_count, it.rq.w.max_fields, &it.carry, &it.dr});
+                }
+                decode_batched(wins, bs, bstream);
+                for (size_t i = 0; i < items.size(); i++) {
+                    Item& it = items[i];
+                    window_finish(it.sl->s, it.rq.w, it.carry, it.cont, it.dr, it.r, it.out_hist);
+                    t_end[i] = Clock::now();
+                }
+                return VHSDECODE_GB300_STATUS_OK;
+            });
+            for (size_t i = 0; i < items.size(); i++) {
+                items[i].r.status = st;
+                if (st != VHSDECODE_GB300_STATUS_OK) t_end[i] = Clock::now();
+            }
+        }
         {
             std::lock_guard<std::mutex> lk(sv->m);
-            if (r.status != VHSDECODE_GB300_STATUS_OK) out_hist.valid = false;
-            History& h = sv->streams[rq.w.stream_id];
-            h = out_hist;
-            h.busy = false;
-            if (!sl->s) {   // creation failed: drop the reservation
-                sv->slots.erase(std::find(sv->slots.begin(), sv->slots.end(), sl));
-                sv->used -= sl->bytes;
-                delete sl;
-            } else {
-                sl->busy = false;
-                sl->last_used = t_end;
+            for (size_t i = 0; i < items.size(); i++) {
+                Item& it = items[i];
+                it.r.queue_ms = ms_between(it.rq.submitted, t_start);
+                it.r.decode_ms = ms_between(t_start, t_end[i]);
+                it.r.latency_ms = ms_between(it.rq.submitted, t_end[i]);
+                it.r.batched = (uint32_t)items.size();
+                if (it.r.status != VHSDECODE_GB300_STATUS_OK) it.out_hist.valid = false;
+                History& h = sv->streams[it.rq.w.stream_id];
+                h = it.out_hist;
+                h.busy = false;
+                Slot* sl = it.sl;
+                if (!sl->s) {   // creation failed: drop the reservation
+                    sv->slots.erase(std::find(sv->slots.begin(), sv->slots.end(), sl));
+                    sv->used -= sl->bytes;
+                    delete sl;
+                } else {
+                    sl->busy = false;
+                    sl->last_used = t_end[i];
+                }
+                sv->done[it.rq.ticket] = it.r;
             }
-            sv->done[rq.ticket] = r;
         }
         sv->cv_done.notify_all();
         sv->cv_work.notify_all();
     }
+    if (bstream) cudaStreamDestroy(bstream);
 }
 
 bool supported(const vhsdecode_gb300_window_v1& w) {

@@ -242,6 +242,35 @@ struct DecodeCarry {
     bool no_graph = false;     // queue the pipeline directly (inputs change every call)
 };
 
+// One window of a batched decode (decode_batched): int16 host samples of a
+// window for an FP32 session without decimation.
+struct BatchWindow {
+    vhsdecode_gb300_session* s;
+    const int16_t* samples;
+    uint64_t n;
+    uint32_t max_fields;
+    DecodeCarry* carry;
+    vhsdecode_gb300_decode_result_v1* res;
+};
+
+// Device job table, block counter and staging of one batching thread.
+struct BatchScratch {
+    int cap = 0;
+    FastDemodParams* d_jobs = nullptr;
+    int64_t* d_start = nullptr;
+    unsigned* d_counter = nullptr;
+    FastDemodParams* h_jobs = nullptr;
+    int64_t* h_start = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    ~BatchScratch();
+    void init(int max_windows);
+};
+
+bool batchable(const vhsdecode_gb300_session* s);
+// Demodulates the blocks of all `wins` in one persistent launch on `st`, then
+// finishes each window on its own session (results as from decode_impl).
+void decode_batched(std::vector<BatchWindow>& wins, BatchScratch& bs, cudaStream_t st);
+
 void session_init(vhsdecode_gb300_session* s, const vhsdecode_gb300_session_config_v1& c);
 void session_free(vhsdecode_gb300_session* s);
 int32_t decode_impl(vhsdecode_gb300_session* s, const void* rf, uint64_t n, uint32_t max_fields,

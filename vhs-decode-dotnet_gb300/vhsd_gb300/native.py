@@ -13,7 +13,7 @@ import os
 
 import numpy as np
 
-ABI_VERSION = 0x00010003
+ABI_VERSION = 0x00010004
 STATUS_OK = 0
 STATUS_NULL_POINTER = -20000
 STATUS_INVALID_ARGUMENT = -20001
@@ -138,7 +138,7 @@ class FieldInfo(ctypes.Structure):
 
 class ServerConfig(ctypes.Structure):
     _fields_ = [("struct_size", ctypes.c_uint32), ("device_id", ctypes.c_int32),
-                ("workers", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+                ("workers", ctypes.c_uint32), ("max_batch", ctypes.c_uint32),
                 ("max_window_samples", ctypes.c_uint64), ("memory_budget_bytes", ctypes.c_uint64)]
 
 
@@ -158,7 +158,8 @@ class WindowResult(ctypes.Structure):
                 ("first_field_is_first", ctypes.c_uint32), ("continued", ctypes.c_uint32),
                 ("ticket", ctypes.c_uint64), ("sample_count", ctypes.c_uint64),
                 ("next_source_offset", ctypes.c_uint64), ("queue_ms", ctypes.c_double),
-                ("decode_ms", ctypes.c_double), ("latency_ms", ctypes.c_double)]
+                ("decode_ms", ctypes.c_double), ("latency_ms", ctypes.c_double),
+                ("batched", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
 
 
 _lib = None
@@ -492,10 +493,10 @@ class Server:
     """Window server (serving API of include/vhsdecode_gb300.h): windows of many
     client streams decoded concurrently on one GPU, in order per stream."""
 
-    def __init__(self, max_window_samples, workers=4, memory_budget=0, device=0):
+    def __init__(self, max_window_samples, workers=4, memory_budget=0, device=0, max_batch=1):
         L = load()
-        cfg = ServerConfig(ctypes.sizeof(ServerConfig), device, workers, 0, int(max_window_samples),
-                           int(memory_budget))
+        cfg = ServerConfig(ctypes.sizeof(ServerConfig), device, workers, max_batch,
+                           int(max_window_samples), int(memory_budget))
         h = _vp()
         check(L.vhsdecode_gb300_server_create(ctypes.byref(cfg), ctypes.byref(h)))
         self._h = h
