@@ -34,7 +34,7 @@
 #  define VHSDECODE_GB300_CALL
 #endif
 
-#define VHSDECODE_GB300_ABI_VERSION 0x00010004u
+#define VHSDECODE_GB300_ABI_VERSION 0x00010005u
 #define VHSDECODE_GB300_NAME_CAPACITY 128u
 
 #ifdef __cplusplus
@@ -188,6 +188,12 @@ typedef struct vhsdecode_gb300_session_config_v1 {
 #define VHSDECODE_GB300_DECODE_DEVICE_INPUT 0x1u /* rf is a device pointer (16-byte aligned) */
 #define VHSDECODE_GB300_DECODE_DEMOD_ONLY   0x2u /* stop after the block demodulator */
 #define VHSDECODE_GB300_DECODE_FLOAT_INPUT  0x4u /* rf holds float samples (input format FLOAT32) */
+#define VHSDECODE_GB300_DECODE_CHROMA       0x8u /* colour-under chroma as the reference's default
+                                                    decode does it: the burst phase refines the line
+                                                    locations (so the luma moves too) and each field
+                                                    gets a uint16 chroma field (session_copy_chroma);
+                                                    without it the decode is the reference's
+                                                    --skip_chroma one */
 
 typedef struct vhsdecode_gb300_decode_result_v1 {
     uint32_t struct_size;
@@ -270,6 +276,11 @@ VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_session_get_fie
 VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_session_copy_tbc(
     vhsdecode_gb300_session* session, uint32_t first, uint32_t count, uint16_t* destination);
 
+/* Copy `count` fields of uint16 chroma (the _chroma.tbc payload) starting at
+ * `first`; the last decode must have asked for VHSDECODE_GB300_DECODE_CHROMA. */
+VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_session_copy_chroma(
+    vhsdecode_gb300_session* session, uint32_t first, uint32_t count, uint16_t* destination);
+
 /* Refined line locations of one field (span-relative samples). */
 VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_session_copy_lines(
     vhsdecode_gb300_session* session, uint32_t field, double* destination, uint32_t capacity);
@@ -279,7 +290,8 @@ VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_session_copy_dr
     vhsdecode_gb300_session* session, uint32_t field, int32_t* line, int32_t* start_x,
     int32_t* end_x, uint32_t capacity, uint32_t* count);
 
-/* Stitched stream channel (0 video Hz, 1 sync reference Hz, 2 envelope) as double. */
+/* Stitched stream channel (0 video Hz, 1 sync reference Hz, 2 envelope, 3 chroma
+ * after a VHSDECODE_GB300_DECODE_CHROMA decode) as double. */
 VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_session_copy_stream(
     vhsdecode_gb300_session* session, uint32_t channel, uint64_t start, uint64_t count,
     double* destination);
@@ -298,6 +310,17 @@ VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_session_tbc_dev
 VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_design_filters(
     uint32_t profile, uint32_t tape_speed, uint32_t tape_format, double sample_rate_mhz,
     double* rf_video, double* video, double* sync, double* sub_high, double* env);
+
+/* Chroma filters and tables for a format at a sample rate; host only.
+ * rf_sos / final_sos receive 4 x 6 section coefficients (b0 b1 b2 a0 a1 a2) of
+ * the RF chroma band-pass and the final / burst-probe band-pass (the
+ * reference's IirFilterDesign.ButterworthBandPassSos designs); geometry gets
+ * burst start, burst end (output samples), chroma offset roll, RF and final
+ * pad lengths, the two chroma_rotation values and the field sample count.
+ * heterodyne (4 x field), burst_sin and burst_cos (field) may be NULL. */
+VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_design_chroma(
+    uint32_t profile, uint32_t tape_speed, uint32_t tape_format, double sample_rate_mhz, double* rf_sos,
+    double* final_sos, int32_t* geometry, float* heterodyne, float* burst_sin, float* burst_cos);
 
 /* Host control plane on given raw pulses of one span; host only.
  * state[0] = previous first-field flag (-1 unknown), state[1] = has previous

@@ -5,7 +5,9 @@ Core/Decode/TbcFieldDecodePipeline.cs:1071-1440, standard VHS branch):
 pulses on the sync reference at IreToHz(vsync_ire/2) -> timing -> classify ->
 refine -> mean line length -> cadence -> VBlank line 0 -> upstream line
 locations (output lines + 10) -> next-field offset -> hsync refinement ->
-NTSC fsc phase shift -> sinc TBC of the output lines -> uint16 -> dropouts.
+(chroma on: chroma TBC from line 1 -> burst phase sequence -> burst refinement
+of the line locations) -> NTSC fsc phase shift -> sinc TBC of the output lines
+-> uint16 -> dropouts (chroma on: chroma TBC -> uint16 chroma field).
 
 Sequencing follows ``DecodeReadWindowPlanner`` (Core/Decode/DecodeReadWindowPlanner.cs:14-64)
 and ``EstimateNextFieldStart`` (Core/Decode/TbcFieldSequenceDecodeEngine.cs:1934-1941).
@@ -14,7 +16,7 @@ import math
 
 import numpy as np
 
-from . import demod, formats, sync, tbc, native
+from . import chroma, demod, formats, sync, tbc, native
 from .filters import FilterSet
 
 
@@ -53,6 +55,16 @@ class FieldState:
         self.prev_first = None
         self.has_prev_hsync = False
         self.pulses_seen = False   # _vhsPulseSearchInitialized
+        self.chroma_rot = 0        # _chromaRotationIndex (null -> 0)
+        self.vhs_number = None     # _previousVhsFieldNumber
+        self.vhs_loc = None        # _previousVhsFieldReadLocation
+
+
+def vhs_field_number(state, read_location):
+    """``ResolveVhsFieldNumber`` (Core/Decode/TbcFieldDecodePipeline.cs:860-874)."""
+    if state.vhs_number is None or state.vhs_loc is None:
+        return 0
+    return state.vhs_number + 1 if read_location > state.vhs_loc else state.vhs_number
 
 
 def _single_estimate(fe, le, has_prev):
@@ -77,8 +89,13 @@ def line_offset(sp, first_field):
     return 2 if first_field else 3
 
 
-def decode_field(sp, fmt, video, vlp, env, state, want_tbc=True):
-    """Decode one field from span channels (arrays relative to the span start)."""
+def decode_field(sp, fmt, video, vlp, env, state, want_tbc=True, chroma_span=None, cp=None, field_number=0):
+    """Decode one field from span channels (arrays relative to the span start).
+
+    With ``cp`` (chroma on, the reference's default for colour-under tapes) the
+    burst phase of the chroma channel refines the line locations before the
+    NTSC fsc shift (TbcFieldDecodePipeline.cs:1366-1399) and the field's
+    chroma is decoded to uint16 (``res["chroma"]``)."""
     threshold = sp.ire_to_hz(sp.vsync_ire / 2.0)
     raw = sync.find_raw_pulses(sp, vlp, threshold)
     if not raw:
@@ -113,18 +130,32 @@ def decode_field(sp, fmt, video, vlp, env, state, want_tbc=True):
     next_loc = sync.next_field_location(sp, first_field, field_lines, mll, fh)
     next_off = next_loc - 8.0 * sp.nominal + demod.CUT
     locs, filled = sync.refine_hsync(sp, vlp, locs, filled, threshold)
+    smoothing = fmt["sys"]["frame_lines"] / 2.0
+    nominal_in = float(round(fmt["sys"]["line_period"] * sp.mhz))
+    phase = None
+    if cp is not None:
+        ana = tbc.resample_field(chroma_span, locs, chroma.ANALYSIS_FIRST_LINE, sp.output_lines,
+                                 sp.outlinelen, nominal_in, smoothing)
+        input_line = max(1, int(round(sp.nominal)))
+        phase = chroma.analyze_field_phase(ana, cp, locs, input_line, rot_index=state.chroma_rot)
+        state.chroma_rot = phase["next_index"]
+        locs = chroma.refine_from_burst(locs, sp.outlinelen, cp.fsc_ratio, phase, cp.ntsc)
     if sp.system == "NTSC":
         locs = locs - ((117.25 / 360.0) / sp.fsc_mhz) * sp.mhz
     res = {"first_field": first_field, "line0": line0, "first_hsync": fh, "mean_line": mll,
            "locs": locs, "next_offset": next_off, "pulses": raw, "refined": refined}
+    if phase is not None:
+        res["phase"] = phase
+        res["field_number"] = field_number
     if want_tbc:
         ofl = output_first_line(sp, first_field)
-        smoothing = fmt["sys"]["frame_lines"] / 2.0
-        nominal_in = float(round(fmt["sys"]["line_period"] * sp.mhz))
         hz = tbc.resample_field(video, locs, ofl, sp.output_lines, sp.outlinelen, nominal_in, smoothing)
         res["tbc_hz"] = hz
         res["tbc"] = tbc.to_u16(hz, sp, formats.output_scale(fmt), fmt["sys"]["outputZero"])
         res["dropouts"] = dropouts(sp, env, locs, first_field)
+        if phase is not None:
+            c = tbc.resample_field(chroma_span, locs, ofl, sp.output_lines, sp.outlinelen, nominal_in, smoothing)
+            res["chroma"] = chroma.decode_field_chroma(c, cp, phase, first_field, field_number, ofl)
     return res
 
 
@@ -181,14 +212,22 @@ def map_rf_to_tbc(ranges, locs, outlen, start_line, end_line, off):
     return out
 
 
-def decode_capture(rf, fmt, fs=40e6, max_fields=None, want_tbc=True, channels=None):
-    """Decode a whole int16 capture; returns (fields, channels)."""
+def decode_capture(rf, fmt, fs=40e6, max_fields=None, want_tbc=True, channels=None, with_chroma=False,
+                   chroma_channel=None):
+    """Decode a whole int16 capture; returns (fields, channels).
+
+    ``with_chroma`` runs the reference's default colour-under chroma path
+    (burst refinement of the lines and a uint16 chroma field); without it the
+    decode is the reference's ``--skip_chroma`` one."""
     sp = sync.SyncParams(fmt, fs)
     filt = FilterSet(fmt, fs)
     diff_max = (sp.ire0 + sp.hz_ire * 100.0) * 2.0
     if channels is None:
         channels = demod.demod_stream(rf, filt, fs, diff_max)
     video, vlp, env, _ = channels
+    cp = chroma.ChromaParams(fmt, fs) if with_chroma else None
+    if cp is not None and chroma_channel is None:
+        chroma_channel = chroma.chroma_stream(rf, cp)
     avail = len(video)
     rl = read_length(sp)
     state = FieldState()
@@ -199,12 +238,17 @@ def decode_capture(rf, fmt, fs=40e6, max_fields=None, want_tbc=True, channels=No
         if s0 + slen > avail:
             break
         sl = slice(s0, s0 + slen)
+        number = vhs_field_number(state, s0)
         try:
-            f = decode_field(sp, fmt, video[sl], vlp[sl], env[sl], state, want_tbc)
+            f = decode_field(sp, fmt, video[sl], vlp[sl], env[sl], state, want_tbc,
+                             chroma_channel[sl] if cp is not None else None, cp, number)
         except FieldError as exc:
             fields.append({"error": str(exc), "span_start": s0, "recovery": exc.offset})
             intended = max(0, intended + exc.offset)
+            # v0.4.0 restarts the VHS field number after an invalid field
+            state.vhs_number = state.vhs_loc = None
             continue
+        state.vhs_number, state.vhs_loc = number, s0
         f["span_start"] = s0
         fields.append(f)
         intended = s0 + max(1, int(sync.round_away(f["next_offset"])))

@@ -5,7 +5,7 @@ The values restate the frozen upstream snapshot the reference embeds
 PAL and NTSC, VHS and SVHS, at ``sp``, ``lp`` and ``ep``; read through
 ``FormatCatalog.cs:46-112``).  VHS LP/EP switch the sub-deemphasis on and
 narrow the NTSC RF filters; S-VHS LP/EP equal S-VHS SP.
-Only the keys the RF -> TBC luma path reads are kept.  ``tests/golden/
+Only the keys the RF -> TBC luma and chroma paths read are kept.  ``tests/golden/
 format_params.json`` (written by ``tests/golden/make_golden.py`` from the
 reference snapshot) pins this table.
 """
@@ -18,7 +18,7 @@ PAL_VHS_SP = {
         "hsyncPulseUS": 4.7, "eqPulseUS": 2.35, "vsyncPulseUS": 27.3,
         "numPulses": 5, "outlinelen": 1135, "outfreq": 17.734475,
         "frame_lines": 625, "field_lines": [312, 313], "outputZero": 256,
-        "fsc_mhz": 4.43361875,
+        "fsc_mhz": 4.43361875, "colorBurstUS": [5.6, 7.85], "burst_abs_ref": 5000,
     },
     "rf": {
         "video_bpf_low": 1300000.0, "video_bpf_high": 5780000.0,
@@ -34,6 +34,7 @@ PAL_VHS_SP = {
         "deemph_gain": 13.9794, "deemph_mid": 273755.82,
         "deemph_q": 0.462088186,
         "color_under_carrier": 626953.0,
+        "chroma_bpf_upper": 1300000, "chroma_rotation": [0, -1],
     },
 }
 
@@ -46,7 +47,7 @@ NTSC_VHS_SP = {
         "eqPulseUS": 2.3, "vsyncPulseUS": 27.1, "numPulses": 6,
         "outlinelen": 910, "outfreq": 14.318181818181818,
         "frame_lines": 525, "field_lines": [263, 262], "outputZero": 1024,
-        "fsc_mhz": 3.5795454545454546,
+        "fsc_mhz": 3.5795454545454546, "colorBurstUS": [5.3, 7.8], "burst_abs_ref": 4416,
     },
     "rf": {
         "video_bpf_low": 500000.0, "video_bpf_high": 6500000.0,
@@ -62,6 +63,7 @@ NTSC_VHS_SP = {
         "deemph_gain": 13.9794, "deemph_mid": 273755.82,
         "deemph_q": 0.462088186,
         "color_under_carrier": 629370.6293706294,
+        "chroma_bpf_upper": 1200000, "chroma_rotation": [-1, 1],
     },
 }
 
@@ -100,9 +102,11 @@ _VHS_LONG_PLAY_RF = {
 }
 
 
-def _long_play(base, speed, ntsc_lpf_extra=None, ntsc_bpf_high=None):
+def _long_play(base, speed, ntsc_lpf_extra=None, ntsc_bpf_high=None, burst_abs_ref=None):
     fmt = {"system": base["system"], "tape_format": base["tape_format"], "tape_speed": speed,
            "sys": dict(base["sys"]), "rf": dict(base["rf"])}
+    if burst_abs_ref is not None:
+        fmt["sys"]["burst_abs_ref"] = burst_abs_ref
     if base["tape_format"] == "VHS":
         fmt["rf"].update(_VHS_LONG_PLAY_RF)
         if ntsc_lpf_extra is not None:
@@ -116,7 +120,7 @@ FORMATS = {("PAL", "VHS", "sp"): PAL_VHS_SP, ("NTSC", "VHS", "sp"): NTSC_VHS_SP,
            ("PAL", "SVHS", "sp"): PAL_SVHS_SP, ("NTSC", "SVHS", "sp"): NTSC_SVHS_SP,
            ("PAL", "VHS", "lp"): _long_play(PAL_VHS_SP, "lp"),
            ("PAL", "VHS", "ep"): _long_play(PAL_VHS_SP, "ep"),
-           ("NTSC", "VHS", "lp"): _long_play(NTSC_VHS_SP, "lp", 5900000.0),
+           ("NTSC", "VHS", "lp"): _long_play(NTSC_VHS_SP, "lp", 5900000.0, burst_abs_ref=2208.0),
            ("NTSC", "VHS", "ep"): _long_play(NTSC_VHS_SP, "ep", 5800000.0, 6400000.0),
            ("PAL", "SVHS", "lp"): _long_play(PAL_SVHS_SP, "lp"),
            ("PAL", "SVHS", "ep"): _long_play(PAL_SVHS_SP, "ep"),

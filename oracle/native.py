@@ -54,6 +54,22 @@ def lib():
         L.oracle_find_dropouts.restype = ctypes.c_int64
         L.oracle_decimate_half_s16.argtypes = [ctypes.POINTER(ctypes.c_int16), ctypes.c_int64, _fp]
         L.oracle_decimate_half_f32.argtypes = [_fp, ctypes.c_int64, _fp]
+        L.oracle_sosfiltfilt_f32.argtypes = [_dp, ctypes.c_int64, _dp, ctypes.c_int, ctypes.c_int64, _fp, _fp]
+        L.oracle_sosfiltfilt_f64.argtypes = [_dp, ctypes.c_int64, _dp, ctypes.c_int, ctypes.c_int64, _dp, _dp]
+        L.oracle_mean_f32_fast.argtypes = [_fp, ctypes.c_int64]
+        L.oracle_mean_f32_fast.restype = ctypes.c_float
+        L.oracle_chroma_heterodyne.argtypes = [ctypes.c_int64, ctypes.c_double, ctypes.c_double, _dp]
+        L.oracle_chroma_carrier.argtypes = [ctypes.c_int64, ctypes.c_double, _dp, _dp]
+        L.oracle_chroma_burst_value.argtypes = [_dp, ctypes.c_int64, _dp, _dp, ctypes.c_int, ctypes.c_double,
+                                                ctypes.c_int64, _dp]
+        L.oracle_chroma_upconvert_ntsc.argtypes = [_dp, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, _i64p,
+                                                   _i64p, _dp, ctypes.c_int64, ctypes.c_double, ctypes.c_double,
+                                                   ctypes.c_double, ctypes.c_double, _dp]
+        L.oracle_chroma_agc_comb_u16.argtypes = [_dp, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
+                                                 ctypes.c_int64, ctypes.c_int64, ctypes.c_double, ctypes.c_int64,
+                                                 ctypes.c_int64, ctypes.c_int, ctypes.c_int, _u16p, _dp]
+        L.oracle_chroma_rms.argtypes = [_dp, ctypes.c_int64, ctypes.c_int]
+        L.oracle_chroma_rms.restype = ctypes.c_double
         _lib = L
     return _lib
 
@@ -171,3 +187,83 @@ def decimate_half(src):
     else:
         raise TypeError("int16 or float32 capture expected")
     return out
+
+
+def sosfiltfilt_f32(x, sos, edge):
+    """Float32 forward-backward SOS cascade (``SosFilter.ApplyForwardBackwardFloat32``)."""
+    x = np.ascontiguousarray(x, np.float64)
+    sos = np.ascontiguousarray(sos, np.float64)
+    n = len(x)
+    if n <= edge:
+        raise ValueError("input length must be greater than the pad length")
+    out = np.empty(n, np.float32)
+    work = np.empty(n + 2 * edge, np.float32)
+    lib().oracle_sosfiltfilt_f32(ptr(x, _dp), n, ptr(sos, _dp), len(sos), edge, ptr(out, _fp), ptr(work, _fp))
+    return out
+
+
+def sosfiltfilt_f64(x, sos, edge):
+    """Binary64 forward-backward SOS cascade (``SosFilter.ApplyForwardBackward``)."""
+    x = np.ascontiguousarray(x, np.float64)
+    sos = np.ascontiguousarray(sos, np.float64)
+    n = len(x)
+    if edge != 0 and n <= edge:
+        raise ValueError("input length must be greater than the pad length")
+    out = np.empty(n)
+    work = np.empty(n + 2 * edge)
+    lib().oracle_sosfiltfilt_f64(ptr(x, _dp), n, ptr(sos, _dp), len(sos), edge, ptr(out, _dp), ptr(work, _dp))
+    return out
+
+
+def mean_f32_fast(v):
+    v = np.ascontiguousarray(v, np.float32)
+    return float(lib().oracle_mean_f32_fast(ptr(v, _fp), len(v)))
+
+
+def chroma_heterodyne(n, scale, offset):
+    out = np.empty(n)
+    lib().oracle_chroma_heterodyne(n, scale, offset, ptr(out, _dp))
+    return out
+
+
+def chroma_carrier(n, wave_scale):
+    s = np.empty(n)
+    c = np.empty(n)
+    lib().oracle_chroma_carrier(n, wave_scale, ptr(s, _dp), ptr(c, _dp))
+    return s, c
+
+
+def chroma_burst_value(burst, bsin, bcos, f32, line_scale, start_minus_line):
+    out = np.empty(5)
+    lib().oracle_chroma_burst_value(ptr(burst, _dp), len(burst), ptr(bsin, _dp), ptr(bcos, _dp), int(bool(f32)),
+                                    float(line_scale), int(start_minus_line), ptr(out, _dp))
+    return out
+
+
+def chroma_upconvert_ntsc(chroma, line_offset, line_length, lines, rots, phases, cu_hz, fsc_mhz,
+                          target_even, target_odd):
+    chroma = np.ascontiguousarray(chroma, np.float64)
+    lines = np.ascontiguousarray(lines, np.int64)
+    rots = np.ascontiguousarray(rots, np.int64)
+    phases = np.ascontiguousarray(phases, np.float64)
+    out = np.empty(len(chroma))
+    lib().oracle_chroma_upconvert_ntsc(ptr(chroma, _dp), len(chroma), line_offset, line_length, ptr(lines, _i64p),
+                                       ptr(rots, _i64p), ptr(phases, _dp), len(lines), cu_hz, fsc_mhz,
+                                       target_even, target_odd, ptr(out, _dp))
+    return out
+
+
+def chroma_agc_comb_u16(chroma, lines, line_length, burst_start, burst_end, burst_abs_ref, burst_line, dist,
+                        retain_f32, f32_rms):
+    chroma = np.ascontiguousarray(chroma, np.float64)
+    out = np.empty(len(chroma), np.uint16)
+    work = np.empty(line_length)
+    lib().oracle_chroma_agc_comb_u16(ptr(chroma, _dp), len(chroma), lines, line_length, burst_start, burst_end,
+                                     burst_abs_ref, burst_line, dist, int(bool(retain_f32)), int(bool(f32_rms)),
+                                     ptr(out, _u16p), ptr(work, _dp))
+    return out
+
+
+def chroma_rms(v, f32):
+    v = np.ascontiguousarray(v, np.float64)
+    return float(lib().oracle_chroma_rms(ptr(v, _dp), len(v), int(bool(f32))))

@@ -6,7 +6,7 @@ reads the reference at test time.
 
 * format_params.json: the keys of the frozen upstream parameter snapshot
   (src/VHSDecode.Core/Formats/format-params.snapshot.json) that the RF -> TBC
-  luma path reads, for PAL and NTSC, VHS and SVHS, at sp, lp and ep, and the
+  luma and chroma paths read, for PAL and NTSC, VHS and SVHS, at sp, lp and ep, and the
   SHA-256 of the S-VHS custom luma tables (src/VHSDecode.Core/Formats/custom/*.txt) converted as
   vhs-decode-dotnet_gb300/data/make_tables.py converts them.
 * sinc_lut_rows.json: the rows of the reference's 65537 x 16 sinc LUT
@@ -28,7 +28,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 
 SYS_KEYS = ["FPS", "ire0", "hz_ire", "vsync_ire", "line_period", "hsyncPulseUS", "eqPulseUS",
             "vsyncPulseUS", "numPulses", "outlinelen", "outfreq", "frame_lines", "field_lines",
-            "outputZero", "fsc_mhz"]
+            "outputZero", "fsc_mhz", "colorBurstUS", "burst_abs_ref"]
 RF_KEYS = ["video_bpf_low", "video_bpf_high", "video_bpf_order", "video_bpf_supergauss",
            "video_lpf_extra", "video_lpf_extra_order", "video_hpf_extra", "video_hpf_extra_order",
            "video_rf_peak_freq", "video_rf_peak_gain", "video_rf_peak_bandwidth",
@@ -38,7 +38,9 @@ RF_KEYS = ["video_bpf_low", "video_bpf_high", "video_bpf_order", "video_bpf_supe
            "use_sub_deemphasis", "nonlinear_highpass_freq", "nonlinear_bandpass_upper",
            "nonlinear_bandpass_order", "nonlinear_amp_lpf_freq", "nonlinear_exp_scaling",
            "nonlinear_scaling_1", "nonlinear_scaling_2", "nonlinear_logistic_mid",
-           "nonlinear_logistic_rate", "nonlinear_static_factor"]
+           "nonlinear_logistic_rate", "nonlinear_static_factor", "chroma_bpf_upper",
+           "chroma_bpf_lower", "chroma_bpf_order", "chroma_rotation", "chroma_offset",
+           "chroma_audio_notch_freq"]
 SYS_KEYS_SUB = ["nonlinear_deviation"]
 
 # (name, source length, locations, first line, line count, outlen, expected SHA-256)

@@ -316,3 +316,25 @@ def test_flac_writer_and_reader_round_trip():
         data = ldf.write(x, blocksize=bs, seed=bs, wasted_frames=(3,))
         assert flac.stream_info(data)["total_samples"] == len(x)
         assert np.array_equal(flac.decode(data), x)
+
+
+@pytest.mark.parametrize("system,fs", [("PAL", 40.0), ("NTSC", 40.0), ("PAL", 20.0), ("NTSC", 28.0)])
+def test_chroma_design_matches_oracle(lib, system, fs):
+    # the library's chroma filters, burst window and tables equal the oracle's bit for bit
+    from oracle import chroma, formats
+    from vhsd_gb300 import native
+    prof = native.PROFILE_PAL if system == "PAL" else native.PROFILE_NTSC
+    d = native.design_chroma(prof, fs, tables=(fs == 40.0))
+    cp = chroma.ChromaParams(formats.get(system), fs * 1e6)
+    assert np.array_equal(d["rf_sos"], cp.rf_sos)
+    assert np.array_equal(d["final_sos"], cp.final_sos)
+    assert (d["burst_start"], d["burst_end"], d["move"]) == (cp.burst_start, cp.burst_end, cp.offset)
+    assert d["rf_edge"] == chroma.default_pad_length(cp.rf_sos) == 27
+    assert d["final_edge"] == chroma.default_pad_length(cp.final_sos) == 27
+    assert d["rotation"] == cp.rotation and d["field_samples"] == cp.field_samples
+    if fs == 40.0:
+        het, bsin, bcos = cp.tables()
+        for p in range(4):
+            assert np.array_equal(d["heterodyne"][p].astype(np.float64), het[p])
+        assert np.array_equal(d["burst_sin"].astype(np.float64), bsin)
+        assert np.array_equal(d["burst_cos"].astype(np.float64), bcos)

@@ -277,7 +277,8 @@ void session_init(vhsdecode_gb300_session* s, const vhsdecode_gb300_session_conf
         const size_t mf = (size_t)s->max_fields;
         const size_t o_locs = 0, o_ss = o_locs + fl * 8, o_sl = o_ss + mf * 8, o_fl = o_sl + mf * 8;
         const size_t a4 = (mf * 4 + 7) & ~(size_t)7;
-        const size_t o_st = o_fl + a4, o_el = o_st + a4, o_lo = o_el + a4, o_fill = o_lo + a4;
+        const size_t o_st = o_fl + a4, o_el = o_st + a4, o_lo = o_el + a4;
+        const size_t o_ff = o_lo + a4, o_fn = o_ff + a4, o_rot = o_fn + a4, o_fill = o_rot + 8;
         s->field_in_bytes = o_fill + ((fl + 7) & ~(size_t)7);
         s->field_in.alloc(s->field_in_bytes);
         ck(cudaHostAlloc((void**)&s->h_field_in, s->field_in_bytes, cudaHostAllocDefault), "cudaHostAlloc");
@@ -289,9 +290,13 @@ void session_init(vhsdecode_gb300_session* s, const vhsdecode_gb300_session_conf
         s->start_line_d.p = reinterpret_cast<int*>(b + o_st);
         s->end_line_d.p = reinterpret_cast<int*>(b + o_el);
         s->line_off_d.p = reinterpret_cast<int*>(b + o_lo);
+        s->first_field_d.p = reinterpret_cast<int*>(b + o_ff);
+        s->field_number_d.p = reinterpret_cast<int*>(b + o_fn);
+        s->rot_in_d.p = reinterpret_cast<int*>(b + o_rot);
         s->fill_in.p = b + o_fill;
-        // results: refined lines, dropout counts and status, early dropout triplets
-        const size_t out_bytes = fl * 8 + mf * 8 + mf * (size_t)kDropEarly * 3 * 4;
+        // results: refined lines, dropout counts and status, early dropout
+        // triplets, then the chroma rotation index and status
+        const size_t out_bytes = fl * 8 + mf * 8 + mf * (size_t)kDropEarly * 3 * 4 + 16;
         ck(cudaHostAlloc((void**)&s->h_field_out, out_bytes, cudaHostAllocDefault), "cudaHostAlloc");
     }
     s->locs_out.alloc(fl);
@@ -341,7 +346,64 @@ void session_init(vhsdecode_gb300_session* s, const vhsdecode_gb300_session_conf
     s->drop_status.alloc(s->max_fields);
 }
 
+// Chroma tables and buffers, made by the first decode that renders chroma.
+void ensure_chroma(vhsdecode_gb300_session* s) {
+    if (s->chroma_alloc) return;
+    s->cd = vhsd::design_chroma(s->fmt, s->fs);
+    const vhsd::ChromaDesign& d = s->cd;
+    if (2 * d.burst_start - d.burst_end < 0 || d.burst_start + d.burst_end > d.outlen ||
+        d.rf.edge >= kBlock || d.out_lines != s->out_lines || d.outlen != s->outlen)
+        throw Failure(VHSDECODE_GB300_STATUS_INTERNAL_ERROR, "chroma burst window does not fit the line");
+    const size_t mf = (size_t)s->max_fields, field = (size_t)d.field_samples;
+    const size_t win = (size_t)(2 * d.burst_end - d.burst_start);
+    s->c32.alloc((size_t)std::max<int64_t>(1, s->max_blocks) * kStride);
+    s->c_scratch.alloc((size_t)std::max<int64_t>(1, s->max_blocks) * (kBlock + 2 * d.rf.edge));
+    std::vector<float> het, bsin, bcos;
+    vhsd::chroma_tables(d, het, bsin, bcos);
+    s->c_het.alloc(het.size());
+    s->c_bsin.alloc(bsin.size());
+    s->c_bcos.alloc(bcos.size());
+    ck(cudaMemcpy(s->c_het.p, het.data(), het.size() * sizeof(float), cudaMemcpyHostToDevice), "upload");
+    ck(cudaMemcpy(s->c_bsin.p, bsin.data(), bsin.size() * sizeof(float), cudaMemcpyHostToDevice), "upload");
+    ck(cudaMemcpy(s->c_bcos.p, bcos.data(), bcos.size() * sizeof(float), cudaMemcpyHostToDevice), "upload");
+    s->c_ana.alloc(mf * s->out_lines * win);
+    s->c_field.alloc(mf * field);
+    s->c_up.alloc(mf * field);
+    s->c_fwd.alloc(mf * (field + 2 * (size_t)d.fin.edge));
+    s->c_probe.alloc(mf * 2 * s->out_lines * 5);
+    s->c_summary.alloc(mf * 4);
+    s->locs_final.alloc(mf * s->lines);
+    s->c_flip.alloc(mf * 2);
+    s->c_chosen.alloc(mf);
+    s->c_state.alloc(4);
+    s->c_ones.alloc(mf);
+    std::vector<int> ones(mf, 1);
+    ck(cudaMemcpy(s->c_ones.p, ones.data(), mf * sizeof(int), cudaMemcpyHostToDevice), "upload");
+    s->chroma.alloc(mf * field);
+    ck(cudaEventCreateWithFlags(&s->chroma_refined, cudaEventDisableTiming), "cudaEventCreate");
+    s->chroma_alloc = true;
+}
+
+// The chroma channel of blocks [b0, b1) on stream `st` (the capture must be on
+// the device: rf16 or the session's float capture).
+void launch_chroma_blocks_for(vhsdecode_gb300_session* s, const int16_t* rf16, int64_t nblocks, cudaStream_t st) {
+    ChromaBlockParams cb{};
+    cb.rf16 = s->in_f32 ? nullptr : rf16;
+    cb.rf32 = s->in_f32;
+    cb.first_block = 0;
+    cb.nblocks = nblocks;
+    std::memcpy(cb.c.sec, s->cd.rf.sec, sizeof(cb.c.sec));
+    std::memcpy(cb.c.zi, s->cd.rf.zi, sizeof(cb.c.zi));
+    cb.c.edge = s->cd.rf.edge;
+    cb.move = s->cd.move;
+    cb.scratch = s->c_scratch.p;
+    cb.out = s->c32.p;
+    ck(launch_chroma_blocks(cb, st), "chroma block launch");
+    s->launches += kChromaBlockKernels;
+}
+
 void session_free(vhsdecode_gb300_session* s) {
+    if (s->chroma_refined) cudaEventDestroy(s->chroma_refined);
     if (s->demod_cycles) cudaFree(s->demod_cycles);
     if (s->plain_graph) cudaGraphExecDestroy(s->plain_graph);
     for (auto& ev : s->ev) if (ev) cudaEventDestroy(ev);
@@ -592,6 +654,7 @@ void host_field_loop(vhsdecode_gb300_session* s, const T* sync, int64_t stream_l
     int64_t min_len = std::max<int64_t>(0, (int64_t)std::ceil(sp.usec(sp.eq_us) / 8.0));
     int64_t max_len = std::max<int64_t>(1, (int64_t)(sp.nominal * 5.0));
     FieldState st = carry ? carry->state : FieldState{};
+    s->chroma_rot_start = s->chroma_rot_end = st.chroma_rot;
     int64_t intended = carry ? std::max<int64_t>(0, carry->start) : 0;
     s->fields.clear();
     s->rescue_fetches = 0;
@@ -617,15 +680,24 @@ void host_field_loop(vhsdecode_gb300_session* s, const T* sync, int64_t stream_l
             s->rescue_fetches++;
         };
         FieldRec rec;
+        // ResolveVhsFieldNumber (TbcFieldDecodePipeline.cs:860-874)
+        const int number = (st.vhs_number < 0 || st.vhs_loc < 0) ? 0
+                           : (s0 > st.vhs_loc ? st.vhs_number + 1 : st.vhs_number);
         rec.sync = analyse_field(sp, raw, slen, st, fetch);
         rec.span_start = s0;
         rec.span_len = slen;
         if (!rec.sync.ok) {
-            // the reference engine moves on and tries again (TbcFieldSequenceDecodeEngine.cs:804-847)
+            // the reference engine moves on and tries again (TbcFieldSequenceDecodeEngine.cs:804-847);
+            // v0.4.0 restarts the VHS field number after an invalid field
             intended = std::max<int64_t>(0, intended + rec.sync.recover_offset);
             s->recoveries++;
+            st.vhs_number = -1;
+            st.vhs_loc = -1;
             continue;
         }
+        st.vhs_number = number;
+        st.vhs_loc = s0;
+        rec.field_number = number;
         intended = s0 + std::max<int64_t>(1, (int64_t)round_away(rec.sync.next_offset));
         s->fields.push_back(std::move(rec));
     }
@@ -655,6 +727,10 @@ void launch_field_batch(vhsdecode_gb300_session* s, int f0, int f1, const T* vid
     int* sline = host(s->start_line_d) + f0;
     int* eline = host(s->end_line_d) + f0;
     int* loff = host(s->line_off_d) + f0;
+    int* ffirst = host(s->first_field_d) + f0;
+    int* fnum = host(s->field_number_d) + f0;
+    *host(s->rot_in_d) = s->chroma_rot_start;
+    const bool chroma = s->want_chroma;
     for (int i = 0; i < nf; i++) {
         const FieldSync& fsy = s->fields[(size_t)(f0 + i)].sync;
         double* lr = locs + (size_t)i * L;
@@ -670,7 +746,12 @@ void launch_field_batch(vhsdecode_gb300_session* s, int f0, int f1, const T* vid
         loff[i] = sp.pal ? (fsy.first_field ? 2 : 3) : 0;
         sline[i] = loff[i] + 1;
         eline[i] = std::min(s->lines - 1, sp.field_lines(fsy.first_field) + sline[i] + 1);
+        ffirst[i] = fsy.first_field ? 1 : 0;
+        fnum[i] = s->fields[(size_t)(f0 + i)].field_number;
     }
+    // with chroma the burst refinement moves the lines the TBC and the dropout
+    // mapping read (and the NTSC fsc shift comes after it)
+    double* final_locs = chroma ? s->locs_final.p + f0 * L : s->locs_out.p + f0 * L;
     // one asynchronous copy of the whole block from pinned memory (the mirror
     // is not written again before this decode's results are collected)
     ck(cudaMemcpyAsync(s->field_in.p, s->h_field_in, s->field_in_bytes, cudaMemcpyHostToDevice, fs), "h2d");
@@ -680,7 +761,7 @@ void launch_field_batch(vhsdecode_gb300_session* s, int f0, int f1, const T* vid
     dp.span_start = s->span_start_d.p + f0;
     dp.span_len = s->span_len_d.p + f0;
     dp.max_span_len = s->span_len;
-    dp.locs = s->locs_out.p + f0 * L;
+    dp.locs = final_locs;
     dp.lines = s->lines;
     dp.start_line = s->start_line_d.p + f0;
     dp.end_line = s->end_line_d.p + f0;
@@ -724,7 +805,8 @@ void launch_field_batch(vhsdecode_gb300_session* s, int f0, int f1, const T* vid
     hp.mhz32 = (double)(float)sp.mhz;
     hp.ire0 = sp.ire0;
     hp.hz_ire = sp.hz_ire;
-    hp.ntsc_shift = sp.pal ? 0.0 : ((117.25 / 360.0) / sp.fsc_mhz) * sp.mhz;
+    const double ntsc_shift = sp.pal ? 0.0 : ((117.25 / 360.0) / sp.fsc_mhz) * sp.mhz;
+    hp.ntsc_shift = chroma ? 0.0 : ntsc_shift;
     hp.work = s->hsync_work.p + hsync_work_bytes(f0, s->lines);
     hp.misses = nullptr;
     if (s->stage_timing) {
@@ -734,20 +816,11 @@ void launch_field_batch(vhsdecode_gb300_session* s, int f0, int f1, const T* vid
     if (timing) ck(cudaEventRecord(s->stage_ev[0], fs), "event");
     ck(launch_hsync_refine<T>(sync, stream_len, hp, fs), "hsync launch");
     s->launches += kHsyncKernels;
-    if (timing) ck(cudaEventRecord(s->stage_ev[1], fs), "event");
-    if (!timing) {
-        ck(cudaEventRecord(s->drop_hsync, fs), "event");
-        ck(cudaStreamWaitEvent(ds, s->drop_hsync, 0), "wait");
-        ck(launch_drop_detect<T>(env, stream_len, dp, s->drop_counts.p + (size_t)f0 * nch, ds), "dropout launch");
-        ck(cudaEventRecord(s->drop_join, ds), "event");
-    }
     TbcParams tp{};
     tp.nfields = nf;
     tp.lines = s->lines;
-    tp.locs = s->locs_out.p + f0 * L;
     tp.span_start = s->span_start_d.p + f0;
     tp.span_len = s->span_len_d.p + f0;
-    tp.first_line = s->first_line_d.p + f0;
     tp.out_lines = s->out_lines;
     tp.outlen = s->outlen;
     tp.nominal = std::nearbyint(s->fmt.line_period_us * sp.mhz);
@@ -755,18 +828,101 @@ void launch_field_batch(vhsdecode_gb300_session* s, int f0, int f1, const T* vid
     tp.lut = s->lut.p;
     tp.lut_pair = s->lut_pair.p;
     tp.pw_ff = s->pw_ff.p;
+    tp.level_work = s->level_work.p + (size_t)f0 * 1024;
+    tp.line_consts = s->tbc_consts.p + (size_t)f0 * s->out_lines * kTbcLineConstsBytes;
+    ChromaFieldParams cp{};
+    if (chroma) {
+        // the line-1 chroma TBC at the probe windows, the burst phase
+        // sequences and the burst refinement of the lines (then the NTSC shift)
+        const vhsd::ChromaDesign& d = s->cd;
+        cp.nfields = nf;
+        cp.lines = s->lines;
+        cp.locs = s->locs_out.p + f0 * L;
+        cp.locs_out = final_locs;
+        cp.ntsc_shift = ntsc_shift;
+        cp.ntsc = d.ntsc ? 1 : 0;
+        cp.out_lines = s->out_lines;
+        cp.outlen = s->outlen;
+        cp.bs = d.burst_start;
+        cp.be = d.burst_end;
+        cp.win0 = 2 * d.burst_start - d.burst_end;
+        cp.win = 2 * d.burst_end - d.burst_start;
+        cp.input_line = std::max(1, (int)std::nearbyint(sp.nominal));
+        cp.fsc_ratio = d.fsc_ratio;
+        cp.rot0 = d.rot[0];
+        cp.rot1 = d.rot[1];
+        std::memcpy(cp.fin.sec, d.fin.sec, sizeof(cp.fin.sec));
+        std::memcpy(cp.fin.zi, d.fin.zi, sizeof(cp.fin.zi));
+        cp.fin.edge = d.fin.edge;
+        cp.het = s->c_het.p;
+        cp.bsin = s->c_bsin.p;
+        cp.bcos = s->c_bcos.p;
+        cp.ana = s->c_ana.p + (size_t)f0 * s->out_lines * cp.win;
+        cp.probe = s->c_probe.p + (size_t)f0 * 2 * s->out_lines * 5;
+        cp.flip = s->c_flip.p + 2 * (size_t)f0;
+        cp.chosen = s->c_chosen.p + f0;
+        cp.rot_in = s->rot_in_d.p;
+        cp.rot_out = s->c_state.p;
+        cp.status = s->c_state.p + 1;
+        cp.summary = s->c_summary.p + 4 * (size_t)f0;
+        cp.first_line = s->first_line_d.p + f0;
+        cp.first_field = s->first_field_d.p + f0;
+        cp.field_number = s->field_number_d.p + f0;
+        const size_t field = (size_t)d.field_samples;
+        cp.cfield = s->c_field.p + (size_t)f0 * field;
+        cp.up = s->c_up.p + (size_t)f0 * field;
+        cp.fwd = s->c_fwd.p + (size_t)f0 * (field + 2 * (size_t)d.fin.edge);
+        cp.out = s->chroma.p + (size_t)f0 * field;
+        cp.cu_hz = d.cu_hz;
+        cp.fsc_mhz = d.fsc_mhz;
+        cp.burst_abs_ref = d.burst_abs_ref;
+        ck(cudaMemsetAsync(s->c_state.p + 1, 0, sizeof(int), fs), "memset");
+        TbcParams ta = tp;
+        ta.locs = cp.locs;
+        ta.first_line = s->c_ones.p;
+        ta.out_f32 = s->c_ana.p + (size_t)f0 * s->out_lines * cp.win;
+        ta.x0 = cp.win0;
+        ta.x1 = cp.win0 + cp.win;
+        ta.out_stride = cp.win;
+        ck(launch_tbc_pw<float>(s->c32.p, stream_len, ta, s->pw.p, fs), "chroma tbc launch");
+        s->launches += kTbcFastKernels;
+        ck(launch_chroma_phase(cp, fs), "chroma phase launch");
+        s->launches += kChromaPhaseKernels;
+    }
+    if (timing) ck(cudaEventRecord(s->stage_ev[1], fs), "event");
+    if (!timing) {
+        ck(cudaEventRecord(s->drop_hsync, fs), "event");
+        ck(cudaStreamWaitEvent(ds, s->drop_hsync, 0), "wait");
+        ck(launch_drop_detect<T>(env, stream_len, dp, s->drop_counts.p + (size_t)f0 * nch, ds), "dropout launch");
+        ck(cudaEventRecord(s->drop_join, ds), "event");
+    }
+    tp.locs = final_locs;
+    tp.first_line = s->first_line_d.p + f0;
     tp.ire0 = s->fmt.ire0;
     tp.output_scale = output_scale(s->fmt);
     tp.inv_hz_ire = 1.0 / s->fmt.hz_ire;
     tp.offset = (s->fmt.output_zero + 0.5) - (s->fmt.vsync_ire * tp.output_scale);
     tp.out_u16 = s->tbc.p + (size_t)f0 * s->out_lines * s->outlen;
     tp.out_hz = nullptr;
-    tp.level_work = s->level_work.p + (size_t)f0 * 1024;
     tp.line_consts = std::is_same<T, float>::value
                          ? s->tbc_consts.p + (size_t)f0 * s->out_lines * kTbcLineConstsBytes
                          : nullptr;
     ck(launch_tbc_pw<T>(video, stream_len, tp, s->pw.p, fs), "tbc launch");
     s->launches += tp.line_consts ? kTbcFastKernels : kTbcKernels;
+    if (chroma) {
+        // the chroma TBC of the output lines and the field decode to uint16
+        TbcParams tc = tp;
+        tc.out_u16 = nullptr;
+        tc.out_f32 = s->c_field.p + (size_t)f0 * s->cd.field_samples;
+        tc.x0 = 0;
+        tc.x1 = 0;
+        tc.out_stride = s->outlen;
+        tc.line_consts = s->tbc_consts.p + (size_t)f0 * s->out_lines * kTbcLineConstsBytes;
+        ck(launch_tbc_pw<float>(s->c32.p, stream_len, tc, s->pw.p, fs), "chroma tbc launch");
+        s->launches += kTbcFastKernels;
+        ck(launch_chroma_decode(cp, fs), "chroma decode launch");
+        s->launches += kChromaDecodeKernels;
+    }
     if (timing) ck(cudaEventRecord(s->stage_ev[2], fs), "event");
     if (timing) {
         ck(launch_drop_detect<T>(env, stream_len, dp, s->drop_counts.p + (size_t)f0 * nch, fs), "dropout launch");
@@ -785,6 +941,12 @@ void launch_field_batch(vhsdecode_gb300_session* s, int f0, int f1, const T* vid
     }
 }
 
+// The chroma rotation index and status slot at the end of the pinned results.
+unsigned char* h_field_out_chroma(vhsdecode_gb300_session* s) {
+    const size_t fl = (size_t)s->max_fields * s->lines, mf = (size_t)s->max_fields;
+    return s->h_field_out + fl * 8 + mf * 8 + mf * (size_t)kDropEarly * 3 * 4;
+}
+
 // Refined line locations and dropout lists of every field back to the host
 // once `fs` has finished the field stage.
 void collect_field_results(vhsdecode_gb300_session* s, cudaStream_t fs) {
@@ -799,12 +961,20 @@ void collect_field_results(vhsdecode_gb300_session* s, cudaStream_t fs) {
     int32_t* early = dstat + mf;
     const int ke = std::min(kDropEarly, s->drop_out_cap);
     const size_t row = (size_t)s->drop_out_cap * 3 * sizeof(int32_t);
-    ck(cudaMemcpyAsync(refined, s->locs_out.p, (size_t)nf * L * sizeof(double), cudaMemcpyDeviceToHost, fs), "d2h");
+    const double* final_locs = s->want_chroma ? s->locs_final.p : s->locs_out.p;
+    ck(cudaMemcpyAsync(refined, final_locs, (size_t)nf * L * sizeof(double), cudaMemcpyDeviceToHost, fs), "d2h");
+    int* cstate = reinterpret_cast<int*>(h_field_out_chroma(s));
+    if (s->want_chroma) ck(cudaMemcpyAsync(cstate, s->c_state.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, fs), "d2h");
     ck(cudaMemcpyAsync(dcount, s->drop_out_count.p, nf * sizeof(int), cudaMemcpyDeviceToHost, fs), "d2h");
     ck(cudaMemcpyAsync(dstat, s->drop_status.p, nf * sizeof(int), cudaMemcpyDeviceToHost, fs), "d2h");
     ck(cudaMemcpy2DAsync(early, (size_t)ke * 3 * sizeof(int32_t), s->drop_out.p, row, (size_t)ke * 3 * sizeof(int32_t),
                          (size_t)nf, cudaMemcpyDeviceToHost, fs), "d2h dropouts");
     ck(cudaStreamSynchronize(fs), "sync");
+    if (s->want_chroma) {
+        if (cstate[1] != 0)
+            throw Failure(VHSDECODE_GB300_STATUS_DECODE_ERROR, "no valid chroma burst samples for phase averaging");
+        s->chroma_rot_end = cstate[0];
+    }
     int maxc = 0;
     for (int f = 0; f < nf; f++) {
         if (dstat[f] != 0)
@@ -1013,6 +1183,7 @@ void decode_fp32_pipelined(vhsdecode_gb300_session* s, const int16_t* rf, uint64
         host_field_loop<float>(s, s->s32.p, stream_len, max_fields, feed, stop, cancel, carry);
         host_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
         ck(cudaEventRecord(s->ev[2], cs), "event");
+        if (s->want_chroma) launch_chroma_blocks_for(s, host_input ? s->rf.p : rf, nblocks, s->field_stream);
         launch_field_batch<float>(s, 0, (int)s->fields.size(), s->v32.p, s->s32.p, s->e32.p,
                                   stream_len, s->field_stream);
         collect_field_results(s, s->field_stream);
@@ -1020,6 +1191,7 @@ void decode_fp32_pipelined(vhsdecode_gb300_session* s, const int16_t* rf, uint64
         ck(cudaStreamWaitEvent(cs, s->field_end, 0), "wait");
     } else {
         ck(cudaEventRecord(s->ev[2], cs), "event");
+        if (s->want_chroma && nblocks > 0) launch_chroma_blocks_for(s, host_input ? s->rf.p : rf, nblocks, cs);
     }
     ck(cudaStreamSynchronize(s->d2h_stream), "sync");
     ck(cudaEventSynchronize(s->seg_dem[(size_t)(2 * std::max(0, nseg - 1) + 1)]), "sync");
@@ -1064,8 +1236,11 @@ void decode_plain(vhsdecode_gb300_session* s, const int16_t* rf_dev, uint64_t n,
         auto t0 = std::chrono::steady_clock::now();
         host_field_loop<double>(s, s->s64.p, stream_len, max_fields, feed, stop, cancel, carry);
         host_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        if (s->want_chroma) launch_chroma_blocks_for(s, rf_dev, nblocks, cs);
         launch_field_batch<double>(s, 0, (int)s->fields.size(), s->v64.p, s->s64.p, s->e64.p, stream_len, cs);
         collect_field_results(s, cs);
+    } else if (s->want_chroma && nblocks > 0) {
+        launch_chroma_blocks_for(s, rf_dev, nblocks, cs);
     }
     ck(cudaEventSynchronize(s->ev[2]), "sync");
     ck(cudaEventElapsedTime(&demod_ms, s->ev[1], s->ev[2]), "elapsed");
@@ -1126,6 +1301,8 @@ int32_t decode_impl(vhsdecode_gb300_session* s, const void* rf_in, uint64_t n_in
     bool host_input = !(flags & VHSDECODE_GB300_DECODE_DEVICE_INPUT);
     const bool demod_only = (flags & VHSDECODE_GB300_DECODE_DEMOD_ONLY) != 0;
     const bool f32_in = (flags & VHSDECODE_GB300_DECODE_FLOAT_INPUT) != 0;
+    s->want_chroma = (flags & VHSDECODE_GB300_DECODE_CHROMA) != 0;
+    if (s->want_chroma) ensure_chroma(s);
     if (!host_input && ((uintptr_t)rf_in & 15u) != 0)
         throw Failure(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "device rf pointer must be 16-byte aligned");
     // samples at the decode rate
@@ -1160,6 +1337,7 @@ int32_t decode_impl(vhsdecode_gb300_session* s, const void* rf_in, uint64_t n_in
     }
     ck(cudaEventRecord(s->ev[3], cs), "event");
     ck(cudaEventSynchronize(s->ev[3]), "sync");
+    if (carry && s->want_chroma) carry->state.chroma_rot = s->chroma_rot_end;
     int rep = 0;
     if (s->fp32() && nblocks > 0)
         ck(cudaMemcpy(&rep, s->repair.p, sizeof(int), cudaMemcpyDeviceToHost), "d2h");
@@ -1241,6 +1419,7 @@ void decode_after_demod(vhsdecode_gb300_session* s, uint64_t n, uint32_t max_fie
     const int64_t stream_len = nblocks * kStride;
     uint32_t stop = 0;
     double host_ms = 0.0;
+    s->want_chroma = false;   // batched windows render luma only
     if (nblocks > 0) {
         ck(launch_pulse_bits_range(s->sync_cond.p, s->sync_hold.p, 0, stream_len, s->pc_counts.p, s->pc_offsets.p,
                                    s->pc_events.p, s->pc_capacity, s->pc_total.p, cs), "pulse launch");
@@ -1272,6 +1451,7 @@ void decode_after_demod(vhsdecode_gb300_session* s, uint64_t n, uint32_t max_fie
     }
     ck(cudaEventRecord(s->ev[3], cs), "event");
     ck(cudaEventSynchronize(s->ev[3]), "sync");
+    if (carry && s->want_chroma) carry->state.chroma_rot = s->chroma_rot_end;
     int rep = 0;
     if (nblocks > 0) ck(cudaMemcpy(&rep, s->repair.p, sizeof(int), cudaMemcpyDeviceToHost), "d2h");
     s->last_blocks = nblocks;
@@ -1482,6 +1662,22 @@ VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_session_copy_tb
     });
 }
 
+VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_session_copy_chroma(
+    vhsdecode_gb300_session* s, uint32_t first, uint32_t count, uint16_t* dst) {
+    return guard([&]() -> int32_t {
+        if (!s || (!dst && count)) return fail(VHSDECODE_GB300_STATUS_NULL_POINTER, "null argument");
+        if (!s->want_chroma) return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "the last decode rendered no chroma");
+        if ((uint64_t)first + count > s->fields.size())
+            return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "field range out of range");
+        size_t per = (size_t)s->out_lines * s->outlen;
+        if (count)
+            ck(cudaMemcpyAsync(dst, s->chroma.p + (size_t)first * per, (size_t)count * per * sizeof(uint16_t),
+                               cudaMemcpyDeviceToHost, s->stream), "d2h chroma");
+        ck(cudaStreamSynchronize(s->stream), "sync");
+        return VHSDECODE_GB300_STATUS_OK;
+    });
+}
+
 VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_session_copy_lines(
     vhsdecode_gb300_session* s, uint32_t field, double* dst, uint32_t cap) {
     return guard([&]() -> int32_t {
@@ -1514,11 +1710,17 @@ VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_session_copy_st
     vhsdecode_gb300_session* s, uint32_t channel, uint64_t start, uint64_t count, double* dst) {
     return guard([&]() -> int32_t {
         if (!s || (!dst && count)) return fail(VHSDECODE_GB300_STATUS_NULL_POINTER, "null argument");
-        if (channel > 2) return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "channel must be 0..2");
+        if (channel > 3) return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "channel must be 0..3");
+        if (channel == 3 && !s->want_chroma)
+            return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "the last decode rendered no chroma");
         uint64_t len = (uint64_t)s->last_blocks * kStride;
         if (start + count > len) return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "range beyond the stream");
         ck(cudaStreamSynchronize(s->stream), "sync");
-        if (s->fp32()) {
+        if (channel == 3) {   // the chroma channel is float in both precisions
+            std::vector<float> tmp(count);
+            ck(cudaMemcpy(tmp.data(), s->c32.p + start, count * sizeof(float), cudaMemcpyDeviceToHost), "d2h");
+            for (uint64_t i = 0; i < count; i++) dst[i] = tmp[i];
+        } else if (s->fp32()) {
             const float* src = channel == 0 ? s->v32.p : channel == 1 ? s->s32.p : s->e32.p;
             std::vector<float> tmp(count);
             ck(cudaMemcpy(tmp.data(), src + start, count * sizeof(float), cudaMemcpyDeviceToHost), "d2h");
@@ -1576,6 +1778,33 @@ VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_design_filters(
         env[0] = fs.env_b0;
         env[1] = fs.env_b1;
         env[2] = fs.env_a1;
+        return VHSDECODE_GB300_STATUS_OK;
+    });
+}
+
+VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_design_chroma(
+    uint32_t profile, uint32_t tape_speed, uint32_t tape_format, double sample_rate_mhz, double* rf_sos,
+    double* final_sos, int32_t* geometry, float* heterodyne, float* burst_sin, float* burst_cos) {
+    return guard([&]() -> int32_t {
+        if (!rf_sos || !final_sos || !geometry) return fail(VHSDECODE_GB300_STATUS_NULL_POINTER, "null argument");
+        FormatParams f;
+        if (!format_for(profile, tape_speed, tape_format, f))
+            return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "unsupported format");
+        if (!(sample_rate_mhz >= 10.0 && sample_rate_mhz <= 100.0))
+            return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "sample_rate_mhz must be within 10..100");
+        vhsd::ChromaDesign d = vhsd::design_chroma(f, sample_rate_mhz * 1e6);
+        std::copy(d.rf_sos.begin(), d.rf_sos.end(), rf_sos);
+        std::copy(d.final_sos.begin(), d.final_sos.end(), final_sos);
+        const int32_t g[8] = {d.burst_start, d.burst_end, d.move, d.rf.edge, d.fin.edge, d.rot[0], d.rot[1],
+                              (int32_t)d.field_samples};
+        std::copy(g, g + 8, geometry);
+        if (heterodyne || burst_sin || burst_cos) {
+            std::vector<float> het, bs, bc;
+            vhsd::chroma_tables(d, het, bs, bc);
+            if (heterodyne) std::copy(het.begin(), het.end(), heterodyne);
+            if (burst_sin) std::copy(bs.begin(), bs.end(), burst_sin);
+            if (burst_cos) std::copy(bc.begin(), bc.end(), burst_cos);
+        }
         return VHSDECODE_GB300_STATUS_OK;
     });
 }

@@ -1,0 +1,580 @@
+// Colour-under chroma on the device (the reference's exact backend, v0.4.0
+// defaults; Core/Decode/VhsChromaDecoder.cs, Core/Decode/RfBlockDecodePipeline.cs).
+//
+// Block stage: the float32 forward-backward chroma band-pass of each RF block
+// (SosFilter.ApplyForwardBackwardFloat32, Core/Dsp/SosFilter.cs:369-538) is a
+// recurrence, so each block is one 4-lane group: lane s runs section s, one
+// sample behind lane s - 1, and the input is staged through shared memory a
+// 32-sample tile ahead.  The result is bit-identical to the reference's
+// sample-by-sample loop (same operations, same order, one rounding each).
+// The roll by the chroma offset and the removal of the float mean
+// (ShiftChromaAndRemoveDcFloat32InPlace, VhsChromaDecoder.cs:2517-2533,
+// MeanFloat32FastMath :3751-3791) then stitch the block into the stream.
+//
+// Field stage: burst probes of the line-1 chroma TBC for both rotation
+// sequences of every field (ProbeUpconvertedBurstValue + DemodBurstFloat32,
+// :1438-1713), the track-flip test (:4164-4217), the rotation index carried
+// from field to field, the phase averages (:4219-4290) and the burst
+// refinement of the line locations (:2342-2428, v0.4.0 form); after the TBC of
+// the output lines, up-conversion (:2009-2248), the final float32
+// band-pass and the automatic gain with the comb to uint16 (:3480-3659).
+// The final band-pass runs on 1024-sample chunks, each started 448 samples
+// early from zero state (its poles are inside radius 0.94: the dropped
+// history weighs below 1e-12), so it equals the sequential filter to float
+// rounding rather than bit for bit.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "kernels.h"
+
+namespace vhsd {
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kTile = 32;          // samples staged per group per tile
+constexpr int kGroupsPerWarp = 8;  // 4-lane groups
+constexpr int kIirWarps = 4;       // warps per CTA of the cascade kernels
+constexpr int kChunk = 1024;       // final band-pass chunk
+constexpr int kWarmup = 448;       // zero-state lead of a chunk
+
+__device__ __forceinline__ float sos_step(const float* c, float v, float& z1, float& z2) {
+    float f = __fadd_rn(__fmul_rn(c[0], v), z1);
+    z1 = __fadd_rn(__fsub_rn(__fmul_rn(c[1], v), __fmul_rn(c[4], f)), z2);
+    z2 = __fsub_rn(__fmul_rn(c[2], v), __fmul_rn(c[5], f));
+    return f;
+}
+
+// One pass of the 4-section cascade over samples 0 .. len-1 of a sequence,
+// run by a 4-lane group (lane s = section s) of a warp whose groups all loop
+// `steps` times (warp-uniform, >= every group's len + 3).  load(i) returns
+// sample i of the pass; store(i, v) receives the cascade output of sample i
+// (from lane 3).  The initial state is zi * x0.  `tile` is the group's
+// 2 x kTile staging area in shared memory.
+template <typename Load, typename Store>
+__device__ __forceinline__ void cascade(const ChromaCascade& c, int s, float* tile, int64_t steps, int64_t len,
+                                        float x0, Load load, Store store) {
+    float z1 = __fmul_rn(c.zi[s][0], x0), z2 = __fmul_rn(c.zi[s][1], x0);
+    float sec[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) sec[k] = c.sec[s][k];
+    float carry = 0.0f;
+    // stage tile 0
+#pragma unroll
+    for (int k = 0; k < kTile / 4; k++) {
+        int64_t i = s * (kTile / 4) + k;
+        tile[s * (kTile / 4) + k] = i < len ? load(i) : 0.0f;
+    }
+    __syncwarp();
+    for (int64_t base = 0; base < steps; base += kTile) {
+        const int cur = (int)((base / kTile) & 1);
+        // stage the next tile while this one is filtered
+        float nxt[kTile / 4];
+#pragma unroll
+        for (int k = 0; k < kTile / 4; k++) {
+            int64_t i = base + kTile + s * (kTile / 4) + k;
+            nxt[k] = i < len ? load(i) : 0.0f;
+        }
+        const float* tl = tile + cur * kTile;
+#pragma unroll 8
+        for (int j = 0; j < kTile; j++) {
+            const int64_t t = base + j;
+            float prev = __shfl_up_sync(kFull, carry, 1, 4);
+            float v = s == 0 ? tl[j] : prev;
+            const int64_t i = t - s;
+            if (i >= 0 && i < len) {
+                carry = sos_step(sec, v, z1, z2);
+                if (s == 3) store(i, carry);
+            }
+        }
+        float* tn = tile + (cur ^ 1) * kTile;
+#pragma unroll
+        for (int k = 0; k < kTile / 4; k++) tn[s * (kTile / 4) + k] = nxt[k];
+        __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------- block stage
+
+// One 4-lane group per RF block: the forward pass over the odd extension of
+// the block into scratch, then the backward pass in place (a sample's slot
+// is overwritten three steps after it was read).
+__global__ void __launch_bounds__(32 * kIirWarps) k_chroma_block_iir(ChromaBlockParams p) {
+    __shared__ float tiles[kIirWarps * kGroupsPerWarp * 2 * kTile];
+    const int lane = threadIdx.x & 31, s = lane & 3, g = lane >> 2;
+    const int64_t j = ((int64_t)blockIdx.x * kIirWarps + (threadIdx.x >> 5)) * kGroupsPerWarp + g;
+    const bool active = j < p.nblocks;
+    float* tile = tiles + ((threadIdx.x >> 5) * kGroupsPerWarp + g) * 2 * kTile;
+    const int edge = p.c.edge;
+    const int64_t len = (int64_t)kBlock + 2 * edge;
+    const int64_t b = p.first_block + (active ? j : 0);
+    const int64_t base = b * kStride;
+    float* ext = p.scratch + (active ? j : 0) * len;
+    auto x_at = [&](int64_t i) -> float { return p.rf32 ? p.rf32[base + i] : (float)p.rf16[base + i]; };
+    const float first = x_at(0), last = x_at(kBlock - 1);
+    auto in_at = [&](int64_t e) -> float {
+        if (e < edge) return __fsub_rn(__fmul_rn(2.0f, first), x_at(edge - e));
+        if (e < edge + kBlock) return x_at(e - edge);
+        return __fsub_rn(__fmul_rn(2.0f, last), x_at(kBlock - 2 - (e - edge - kBlock)));
+    };
+    const int64_t steps = len + 3;
+    cascade(p.c, s, tile, steps, len, in_at(0), in_at, [&](int64_t i, float v) {
+        if (active) ext[i] = v;
+    });
+    __syncwarp();
+    const float xl = ext[len - 1];
+    cascade(p.c, s, tile, steps, len, xl, [&](int64_t i) { return ext[len - 1 - i]; },
+            [&](int64_t i, float v) {
+                if (active) ext[len - 1 - i] = v;
+            });
+}
+
+// One warp per block: the float mean of the rolled block in the reference's
+// 32-accumulator order, then the stitched span minus the mean.
+__global__ void __launch_bounds__(32) k_chroma_block_dc(ChromaBlockParams p) {
+    const int64_t j = blockIdx.x;
+    const int lane = threadIdx.x;
+    const int edge = p.c.edge;
+    const float* y = p.scratch + j * ((int64_t)kBlock + 2 * edge) + edge;
+    const int move = p.move;
+    float acc = 0.0f;
+    for (int i = lane; i < kBlock; i += 32) acc = __fadd_rn(acc, y[(i - move) & (kBlock - 1)]);
+    // lanes[l] = (acc[l] + acc[8 + l]) + (acc[16 + l] + acc[24 + l]), then a tree over 8 lanes
+    float t = __fadd_rn(acc, __shfl_down_sync(kFull, acc, 8));
+    float l8 = __fadd_rn(t, __shfl_down_sync(kFull, t, 16));
+    for (int c = 8; c > 1; c /= 2) l8 = __fadd_rn(l8, __shfl_down_sync(kFull, l8, c / 2));
+    const float mean = __fdiv_rn(__shfl_sync(kFull, l8, 0), (float)kBlock);
+    float* out = p.out + (p.first_block + j) * kStride;
+    for (int i = lane; i < kStride; i += 32) out[i] = __fsub_rn(y[(kCut + i - move) & (kBlock - 1)], mean);
+}
+
+// ---------------------------------------------------------------- burst probes
+
+__device__ __forceinline__ double positive_degrees(double d) {
+    double r = fmod(d, 360.0);
+    return r < 0.0 ? r + 360.0 : r;
+}
+
+__device__ __forceinline__ int positive_mod4(int v) {
+    int r = v % 4;
+    return r < 0 ? r + 4 : r;
+}
+
+// One 4-lane group per (field, rotation sequence, line): the probe window of
+// the line times the heterodyne of its phase rotation, the float32
+// forward-backward final band-pass over it (odd extension, in shared memory),
+// and the I/Q demodulation of the burst against the carrier tables.
+__global__ void __launch_bounds__(128) k_chroma_probe(ChromaFieldParams p) {
+    extern __shared__ float smem[];
+    const int lane = threadIdx.x & 31, s = lane & 3;
+    const int gi = threadIdx.x >> 2;   // group in the CTA
+    const int64_t pid = (int64_t)blockIdx.x * (blockDim.x >> 2) + gi;
+    const int64_t nprobe = (int64_t)p.nfields * 2 * p.out_lines;
+    const bool active = pid < nprobe;
+    const int64_t q = active ? pid : 0;
+    const int f = (int)(q / (2 * p.out_lines));
+    const int cnd = (int)((q / p.out_lines) % 2);
+    const int pl = (int)(q % p.out_lines);   // sequence index; line = pl + 1
+    const int edge = p.fin.edge;
+    const int win = p.win;
+    const int len = win + 2 * edge;
+    float* buf = smem + (size_t)gi * (len + 2 * kTile);
+    float* tile = buf + len;
+    const int64_t field = (int64_t)p.out_lines * p.outlen;
+    const int rot = positive_mod4((cnd == 0 ? p.rot0 : p.rot1) * (pl + 1));
+    const int64_t line_start = (int64_t)pl * p.outlen;
+    const int64_t p0 = line_start + p.win0;
+    const float* het = p.het + (int64_t)rot * field + p0;
+    const float* ana = p.ana + ((int64_t)f * p.out_lines + pl) * win;
+    // mixed samples into buf[edge .. edge + win), then the odd extension
+    for (int i = s; i < win; i += 4) buf[edge + i] = __fmul_rn(het[i], ana[i]);
+    __syncwarp();
+    {
+        const float first = buf[edge], last = buf[edge + win - 1];
+        for (int e = s; e < edge; e += 4) {
+            buf[e] = __fsub_rn(__fmul_rn(2.0f, first), buf[edge + edge - e]);
+            buf[edge + win + e] = __fsub_rn(__fmul_rn(2.0f, last), buf[edge + win - 2 - e]);
+        }
+    }
+    __syncwarp();
+    const int64_t steps = len + 3;
+    cascade(p.fin, s, tile, steps, len, buf[0], [&](int64_t i) { return buf[i]; },
+            [&](int64_t i, float v) { buf[i] = v; });
+    __syncwarp();
+    const float xl = buf[len - 1];
+    __syncwarp();
+    cascade(p.fin, s, tile, steps, len, xl, [&](int64_t i) { return buf[len - 1 - i]; },
+            [&](int64_t i, float v) { buf[len - 1 - i] = v; });
+    __syncwarp();
+    // DemodBurstFloat32: burst = filtered[pad, win - pad), tables from line_start + bs
+    const int pad = p.be - p.bs;
+    const int n = win - 2 * pad;
+    const float* burst = buf + edge + pad;
+    const float* bc = p.bcos + line_start + p.bs;
+    const float* bsn = p.bsin + line_start + p.bs;
+    const int main_end = n & ~15, epi_end = n & ~3;
+    double I[4] = {0, 0, 0, 0}, Q[4] = {0, 0, 0, 0};   // groups 0..3 of this lane
+    for (int k = 0; k < main_end; k += 16) {
+#pragma unroll
+        for (int gr = 0; gr < 4; gr++) {
+            const int idx = k + s + 4 * gr;
+            const float sm = burst[idx];
+            I[gr] = __dadd_rn(I[gr], (double)__fmul_rn(sm, bc[idx]));
+            Q[gr] = __dadd_rn(Q[gr], (double)__fmul_rn(sm, bsn[idx]));
+        }
+    }
+    const unsigned gmask = kFull;
+    double li = __dadd_rn(__dadd_rn(__dadd_rn(I[1], I[0]), I[2]), I[3]);
+    double lq = __dadd_rn(__dadd_rn(__dadd_rn(Q[1], Q[0]), Q[2]), Q[3]);
+    auto fold4 = [&](double v) {
+        // (l0 + l2) + (l1 + l3) within the group
+        double v2 = __shfl_down_sync(gmask, v, 2, 4);
+        double a = __dadd_rn(v, v2);   // lane 0: l0 + l2, lane 1: l1 + l3
+        double b = __shfl_down_sync(gmask, a, 1, 4);
+        return __shfl_sync(gmask, __dadd_rn(a, b), 0, 4);
+    };
+    double ic = fold4(li), qc = fold4(lq);
+    if (epi_end > main_end) {
+        double ei = s == 0 ? ic : 0.0, eq = s == 0 ? qc : 0.0;
+        for (int k = main_end; k < epi_end; k += 4) {
+            const float sm = burst[k + s];
+            ei = __dadd_rn(ei, (double)__fmul_rn(sm, bc[k + s]));
+            eq = __dadd_rn(eq, (double)__fmul_rn(sm, bsn[k + s]));
+        }
+        ic = fold4(ei);
+        qc = fold4(eq);
+    }
+    if (s == 0 && active) {
+        for (int k = epi_end; k < n; k++) {
+            ic = __dadd_rn(ic, (double)__fmul_rn(burst[k], bc[k]));
+            qc = __dadd_rn(qc, (double)__fmul_rn(burst[k], bsn[k]));
+        }
+        const int line = pl + 1;
+        const double* loc = p.locs + (int64_t)f * p.lines;
+        const double scale = pl < p.out_lines - 1 ? __ddiv_rn(__dsub_rn(loc[line + 1], loc[line]), (double)p.input_line)
+                                                  : 1.0;
+        double* o = p.probe + q * 5;
+        o[0] = positive_degrees(atan2(qc, ic) * (180.0 / 3.141592653589793));
+        o[1] = positive_degrees((double)p.bs * __fma_rn(-scale, 90.0, 90.0));
+        o[2] = hypot(ic, qc);
+        o[3] = ic;
+        o[4] = qc;
+    }
+}
+
+// ShouldFlipTrackPhase for each (field, rotation sequence): phase-step buckets
+// between neighbouring lines away from the field edges.
+__global__ void __launch_bounds__(128) k_chroma_flip(ChromaFieldParams p) {
+    __shared__ int cnt[4];
+    if (threadIdx.x < 4) cnt[threadIdx.x] = 0;
+    __syncthreads();
+    const int fc = blockIdx.x;   // field * 2 + sequence
+    const double* pr = p.probe + (int64_t)fc * p.out_lines * 5;
+    const int end = p.out_lines + 1;
+    for (int k = 1 + threadIdx.x; k < p.out_lines; k += blockDim.x) {
+        const int line = k + 1;
+        if (line <= 16 || line >= end - 16) continue;
+        double delta = positive_degrees(__dsub_rn(pr[k * 5], pr[(k - 1) * 5]));
+        int bucket = ((int)floor(__dadd_rn(delta, 45.0) / 90.0)) % 4;
+        atomicAdd(&cnt[bucket], 1);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+        p.flip[fc] = p.ntsc ? (cnt[0] < cnt[2]) : ((cnt[1] + cnt[3]) < (cnt[0] + cnt[2]));
+}
+
+// The rotation index runs from field to field: a field starts with index c
+// and keeps sequence c, or the other one when that one flips; the next field
+// starts with the other index unless the field flipped.
+__global__ void k_chroma_chain(ChromaFieldParams p) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    int c = *p.rot_in;
+    for (int f = 0; f < p.nfields; f++) {
+        const int fl = p.flip[f * 2 + c];
+        p.chosen[f] = fl ? 1 - c : c;
+        c = fl ? c : 1 - c;
+    }
+    *p.rot_out = c;
+}
+
+// SummarizePhaseSequence of each field's kept sequence (line order sums).
+__global__ void k_chroma_summary(ChromaFieldParams p) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= p.nfields) return;
+    const double* pr = p.probe + ((int64_t)f * 2 + p.chosen[f]) * p.out_lines * 5;
+    const int end = p.out_lines + 1;
+    double ei = 0.0, eq = 0.0, oi = 0.0, oq = 0.0, msum = 0.0;
+    int count = 0;
+    for (int k = 0; k < p.out_lines; k++) {
+        const int line = k + 1;
+        const double mag = pr[k * 5 + 2];
+        if (line <= 16 || line >= end - 16 || mag == 0.0) continue;
+        const double ni = __ddiv_rn(pr[k * 5 + 3], mag), nq = __ddiv_rn(pr[k * 5 + 4], mag);
+        count++;
+        msum = __dadd_rn(msum, mag);
+        if (line & 1) {
+            oi = __dadd_rn(oi, ni);
+            oq = __dadd_rn(oq, nq);
+        } else {
+            ei = __dadd_rn(ei, ni);
+            eq = __dadd_rn(eq, nq);
+        }
+    }
+    double* o = p.summary + (int64_t)f * 4;
+    if (count == 0) {
+        atomicExch(p.status, 1);
+        o[0] = o[1] = o[2] = o[3] = 0.0;
+        return;
+    }
+    const double k180 = 180.0, pi = 3.141592653589793;
+    o[0] = positive_degrees(__ddiv_rn(__dmul_rn(atan2(__dadd_rn(eq, oq), __dadd_rn(ei, oi)), k180), pi));
+    o[1] = positive_degrees(__ddiv_rn(__dmul_rn(atan2(eq, ei), k180), pi));
+    o[2] = positive_degrees(__ddiv_rn(__dmul_rn(atan2(oq, oi), k180), pi));
+    o[3] = __ddiv_rn(msum, (double)count);
+}
+
+// RefineLineLocationsFromBurst (v0.4.0) from sequence index 9 on, then the
+// NTSC fsc shift of every location.
+__global__ void k_chroma_refine(ChromaFieldParams p) {
+    const int f = blockIdx.x;
+    const double* loc = p.locs + (int64_t)f * p.lines;
+    double* out = p.locs_out + (int64_t)f * p.lines;
+    const double* pr = p.probe + ((int64_t)f * 2 + p.chosen[f]) * p.out_lines * 5;
+    const double* sm = p.summary + (int64_t)f * 4;
+    for (int L = threadIdx.x; L < p.lines; L += blockDim.x) {
+        double v = loc[L];
+        const int k = L - 1;
+        if (k >= 9 && k < p.out_lines && L + 1 < p.lines) {
+            const double target = p.ntsc ? sm[0] : ((L & 1) ? sm[2] : sm[1]);
+            const double delta =
+                __dsub_rn(positive_degrees(__dadd_rn(__dadd_rn(__dsub_rn(target, pr[k * 5]), pr[k * 5 + 1]), 180.0)),
+                          180.0);
+            const double scale = __ddiv_rn(__dsub_rn(loc[L + 1], loc[L]), (double)p.outlen);
+            v = __dadd_rn(v, __dmul_rn(__dmul_rn(__ddiv_rn(delta, 360.0), p.fsc_ratio), scale));
+        }
+        out[L] = p.ntsc ? __dsub_rn(v, p.ntsc_shift) : v;
+    }
+}
+
+// ---------------------------------------------------------------- field decode
+
+// Up-conversion of one output line.  PAL: the line written by sequence entry
+// L (NumPy slice of line L - first_line, negative indices from the end; the
+// one that lands on -1 is empty) times the heterodyne of its rotation.  NTSC:
+// the burst de-emphasis (x2 from burst end + 5) and the phase-compensated
+// carrier -cos(theta), theta advanced per sample as the reference's four
+// lanes do (closed form; cosine in float after an exact turn reduction).
+__global__ void __launch_bounds__(256) k_chroma_upconvert(ChromaFieldParams p) {
+    const int f = blockIdx.y;
+    const int o = blockIdx.x;
+    const int64_t field = (int64_t)p.out_lines * p.outlen;
+    const int ofl = p.first_line[f];
+    const float* src = p.cfield + (int64_t)f * field + (int64_t)o * p.outlen;
+    float* dst = p.up + (int64_t)f * field + (int64_t)o * p.outlen;
+    int L;
+    if (o <= p.out_lines - ofl) L = o + ofl;
+    else if (o >= p.out_lines + 1 - ofl && o < p.out_lines - 1) L = o + ofl - p.out_lines;
+    else L = -1;
+    if (L < 1 || L > p.out_lines) {
+        for (int k = threadIdx.x; k < p.outlen; k += blockDim.x) dst[k] = 0.0f;
+        return;
+    }
+    const int c = p.chosen[f];
+    const int rot = positive_mod4((c == 0 ? p.rot0 : p.rot1) * L);
+    if (!p.ntsc) {
+        const float* het = p.het + (int64_t)rot * field + (int64_t)o * p.outlen;
+        for (int k = threadIdx.x; k < p.outlen; k += blockDim.x) dst[k] = __fmul_rn(src[k], het[k]);
+        return;
+    }
+    const double* pr = p.probe + ((int64_t)f * 2 + c) * p.out_lines * 5 + (int64_t)(L - 1) * 5;
+    const double half_pi = 1.5707963267948966, deg = 0.017453292519943295;
+    const double carrier_term = __dmul_rn(p.cu_hz, 1.5707963267948965e-6);
+    const double h = __dadd_rn(__ddiv_rn(carrier_term, p.fsc_mhz), half_pi);
+    // NtscFieldPhaseTarget (:3915-3925): -33 degrees in the first colour frame
+    // of the four-field sequence, 147 in the second, whatever the parity
+    const bool second = ((p.field_number[f] / 2) & 1) == 1;
+    const double target = second ? 147.0 : -33.0;
+    const int64_t ls = (int64_t)(L - ofl) * p.outlen;
+    double theta = __fma_rn((double)ls, h, (double)rot * half_pi);
+    theta = __fma_rn(__dadd_rn(target, pr[0]), deg, theta);
+    const int vc = p.outlen & ~3;
+    const double h4 = __dmul_rn(h, 4.0);
+    const double lane_off[4] = {__dmul_rn(h, 0.0), h, __dmul_rn(h, 2.0), __dmul_rn(h, 3.0)};
+    const double tail0 = __dadd_rn(theta, __dmul_rn(h, (double)vc));
+    const int first_doubled = p.be + 5;
+    const double two_pi = 6.283185307179586;
+    for (int k = threadIdx.x; k < p.outlen; k += blockDim.x) {
+        double th = k < vc ? __fma_rn((double)(k >> 2), h4, __dadd_rn(theta, lane_off[k & 3]))
+                           : __fma_rn((double)(k - vc), h, tail0);
+        const double turns = rint(th / two_pi);
+        const float r = (float)__fma_rn(-turns, two_pi, th);
+        const double carrier = -(double)cosf(r);
+        double v = (double)src[k];
+        if (k >= first_doubled) v = __dmul_rn(v, 2.0);
+        dst[k] = __double2float_rn(__dmul_rn(v, carrier));
+    }
+}
+
+// Final band-pass, forward: one 4-lane group per 1024-sample chunk of the odd
+// extension of a field's up-converted chroma; chunks past the first
+// kWarmup samples start kWarmup early from zero state.
+__global__ void __launch_bounds__(32 * kIirWarps) k_chroma_final_fwd(ChromaFieldParams p, int64_t chunks_per_field) {
+    __shared__ float tiles[kIirWarps * kGroupsPerWarp * 2 * kTile];
+    const int lane = threadIdx.x & 31, s = lane & 3, g = lane >> 2;
+    const int64_t gid = ((int64_t)blockIdx.x * kIirWarps + (threadIdx.x >> 5)) * kGroupsPerWarp + g;
+    const bool active = gid < (int64_t)p.nfields * chunks_per_field;
+    const int64_t q = active ? gid : 0;
+    const int f = (int)(q / chunks_per_field);
+    const int64_t ch = q % chunks_per_field;
+    float* tile = tiles + ((threadIdx.x >> 5) * kGroupsPerWarp + g) * 2 * kTile;
+    const int64_t field = (int64_t)p.out_lines * p.outlen;
+    const int edge = p.fin.edge;
+    const int64_t E = field + 2 * edge;
+    const float* x = p.up + (int64_t)f * field;
+    float* fwd = p.fwd + (int64_t)f * E;
+    const float first = x[0], last = x[field - 1];
+    auto ext = [&](int64_t e) -> float {
+        if (e < edge) return __fsub_rn(__fmul_rn(2.0f, first), x[edge - e]);
+        if (e < edge + field) return x[e - edge];
+        return __fsub_rn(__fmul_rn(2.0f, last), x[field - 2 - (e - edge - field)]);
+    };
+    const int64_t c0 = ch * kChunk, c1 = min(E, c0 + kChunk);
+    const int64_t start = c0 <= kWarmup ? 0 : c0 - kWarmup;
+    const int64_t len = active ? c1 - start : 0;
+    const float x0 = start == 0 ? ext(0) : 0.0f;
+    cascade(p.fin, s, tile, (int64_t)kChunk + kWarmup + 3, len, x0, [&](int64_t i) { return ext(start + i); },
+            [&](int64_t i, float v) {
+                if (start + i >= c0) fwd[start + i] = v;
+            });
+}
+
+// Final band-pass, backward over the forward output, chunks started kWarmup
+// late from zero state except the last; the output samples land in `up`.
+__global__ void __launch_bounds__(32 * kIirWarps) k_chroma_final_bwd(ChromaFieldParams p, int64_t chunks_per_field) {
+    __shared__ float tiles[kIirWarps * kGroupsPerWarp * 2 * kTile];
+    const int lane = threadIdx.x & 31, s = lane & 3, g = lane >> 2;
+    const int64_t gid = ((int64_t)blockIdx.x * kIirWarps + (threadIdx.x >> 5)) * kGroupsPerWarp + g;
+    const bool active = gid < (int64_t)p.nfields * chunks_per_field;
+    const int64_t q = active ? gid : 0;
+    const int f = (int)(q / chunks_per_field);
+    const int64_t ch = q % chunks_per_field;
+    float* tile = tiles + ((threadIdx.x >> 5) * kGroupsPerWarp + g) * 2 * kTile;
+    const int64_t field = (int64_t)p.out_lines * p.outlen;
+    const int edge = p.fin.edge;
+    const int64_t E = field + 2 * edge;
+    const float* fwd = p.fwd + (int64_t)f * E;
+    float* y = p.up + (int64_t)f * field;
+    const int64_t c0 = ch * kChunk, c1 = min(E, c0 + kChunk);
+    const int64_t stop = c1 + kWarmup >= E ? E : c1 + kWarmup;   // exclusive upper end of the pass
+    const int64_t len = active ? stop - c0 : 0;
+    const float x0 = stop == E ? fwd[E - 1] : 0.0f;
+    cascade(p.fin, s, tile, (int64_t)kChunk + kWarmup + 3, len, x0, [&](int64_t i) { return fwd[stop - 1 - i]; },
+            [&](int64_t i, float v) {
+                const int64_t e = stop - 1 - i;
+                if (e < c1 && e >= edge && e < edge + field) y[e - edge] = v;
+            });
+}
+
+__device__ __forceinline__ uint16_t u16_saturate(double shifted) {
+    if (!isfinite(shifted) || shifted <= 0.0) return 0;
+    if (shifted >= 65535.0) return 65535;
+    return (uint16_t)shifted;
+}
+
+// The reference's scalar tail (the field's last n mod 4 samples): (ushort)(long)x.
+__device__ __forceinline__ uint16_t u16_wrap(double shifted) {
+    if (!isfinite(shifted) || shifted < -9223372036854775808.0 || shifted > 9223372036854775807.0) return 0;
+    return (uint16_t)(uint64_t)(int64_t)shifted;
+}
+
+// ApplyAutomaticChromaGainWithCombToU16: lines below 16 neutral; from line 16
+// the comb of the line with the lines `dist` before and after it (not for the
+// last two lines), scaled so its burst RMS is burst_abs_ref.
+__global__ void __launch_bounds__(256) k_chroma_gain(ChromaFieldParams p) {
+    extern __shared__ float line[];
+    __shared__ double scale_s;
+    const int f = blockIdx.y, o = blockIdx.x;
+    const int64_t field = (int64_t)p.out_lines * p.outlen;
+    const float* x = p.up + (int64_t)f * field;
+    uint16_t* out = p.out + (int64_t)f * field + (int64_t)o * p.outlen;
+    if (o < 16) {
+        for (int k = threadIdx.x; k < p.outlen; k += blockDim.x) out[k] = 32767;
+        return;
+    }
+    const int dist = p.ntsc ? 1 : 2;
+    const float* cur = x + (int64_t)o * p.outlen;
+    if (o < p.out_lines - 2) {
+        const float* adv = x + (int64_t)(o + dist) * p.outlen;
+        const float* del = x + (int64_t)(o - dist) * p.outlen;
+        for (int k = threadIdx.x; k < p.outlen; k += blockDim.x) {
+            double c = __dmul_rn((double)cur[k], 2.0);
+            c = __dsub_rn(__dsub_rn(c, (double)adv[k]), (double)del[k]);
+            line[k] = __double2float_rn(__ddiv_rn(c, 4.0));
+        }
+    } else {
+        for (int k = threadIdx.x; k < p.outlen; k += blockDim.x) line[k] = cur[k];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        // RmsFloat32 (VhsChromaDecoder.cs:4400-4423)
+        const int n = p.be - p.bs;
+        float mean = 0.0f;
+        for (int k = 0; k < n; k++) mean = __fadd_rn(mean, line[p.bs + k]);
+        mean = __fdiv_rn(mean, (float)n);
+        float ss = 0.0f;
+        for (int k = 0; k < n; k++) {
+            float c = __fsub_rn(line[p.bs + k], mean);
+            ss = __fadd_rn(ss, __fmul_rn(c, c));
+        }
+        const float rms = n > 0 ? __fsqrt_rn(__fdiv_rn(ss, (float)n)) : 0.0f;
+        scale_s = rms != 0.0f ? __ddiv_rn(p.burst_abs_ref, (double)rms) : 1.0;
+    }
+    __syncthreads();
+    const double scale = scale_s;
+    const int64_t vec_len = field & ~(int64_t)3;
+    for (int k = threadIdx.x; k < p.outlen; k += blockDim.x) {
+        const double shifted = __dadd_rn(__dmul_rn((double)line[k], scale), 32767.0);
+        const int64_t gi = (int64_t)o * p.outlen + k;
+        out[k] = gi < vec_len ? u16_saturate(shifted) : u16_wrap(shifted);
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_chroma_blocks(const ChromaBlockParams& p, cudaStream_t s) {
+    if (p.nblocks <= 0) return cudaSuccess;
+    const int64_t per_cta = (int64_t)kIirWarps * kGroupsPerWarp;
+    k_chroma_block_iir<<<(unsigned)((p.nblocks + per_cta - 1) / per_cta), 32 * kIirWarps, 0, s>>>(p);
+    k_chroma_block_dc<<<(unsigned)p.nblocks, 32, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_chroma_phase(const ChromaFieldParams& p, cudaStream_t s) {
+    if (p.nfields <= 0) return cudaSuccess;
+    const int64_t nprobe = (int64_t)p.nfields * 2 * p.out_lines;
+    const int groups = 32;   // 128 threads
+    const size_t smem = (size_t)groups * (p.win + 2 * p.fin.edge + 2 * kTile) * sizeof(float);
+    k_chroma_probe<<<(unsigned)((nprobe + groups - 1) / groups), groups * 4, smem, s>>>(p);
+    k_chroma_flip<<<(unsigned)(p.nfields * 2), 128, 0, s>>>(p);
+    k_chroma_chain<<<1, 1, 0, s>>>(p);
+    k_chroma_summary<<<(unsigned)((p.nfields + 63) / 64), 64, 0, s>>>(p);
+    k_chroma_refine<<<(unsigned)p.nfields, 256, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_chroma_decode(const ChromaFieldParams& p, cudaStream_t s) {
+    if (p.nfields <= 0) return cudaSuccess;
+    dim3 lines(p.out_lines, p.nfields);
+    k_chroma_upconvert<<<lines, 256, 0, s>>>(p);
+    const int64_t field = (int64_t)p.out_lines * p.outlen;
+    const int64_t chunks = (field + 2 * p.fin.edge + kChunk - 1) / kChunk;
+    const int64_t groups = (int64_t)p.nfields * chunks;
+    const int64_t per_cta = (int64_t)kIirWarps * kGroupsPerWarp;
+    const unsigned grid = (unsigned)((groups + per_cta - 1) / per_cta);
+    k_chroma_final_fwd<<<grid, 32 * kIirWarps, 0, s>>>(p, chunks);
+    k_chroma_final_bwd<<<grid, 32 * kIirWarps, 0, s>>>(p, chunks);
+    k_chroma_gain<<<lines, 256, (size_t)p.outlen * sizeof(float), s>>>(p);
+    return cudaGetLastError();
+}
+
+}  // namespace vhsd

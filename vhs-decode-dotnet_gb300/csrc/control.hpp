@@ -49,6 +49,12 @@ struct FieldState {
     int prev_first = -1;   // -1 unknown, else 0/1
     bool has_prev_hsync = false;
     bool pulses_seen = false;   // a span with raw pulses was analysed (_vhsPulseSearchInitialized)
+    // chroma: the rotation index carried from field to field (_chromaRotationIndex,
+    // null = 0) and the VHS field number (ResolveVhsFieldNumber,
+    // Core/Decode/TbcFieldDecodePipeline.cs:860-874; -1 = none, after a failed field)
+    int chroma_rot = 0;
+    int vhs_number = -1;
+    int64_t vhs_loc = -1;
 };
 
 struct FieldSync {

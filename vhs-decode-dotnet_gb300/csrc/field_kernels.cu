@@ -1166,7 +1166,8 @@ __global__ void k_tbc(const T* stream, int64_t stream_len, TbcParams p, const do
     const double adj = w[2 * line], before = w[2 * line + 1];
     const double ll = loc[line];
     const double delta = __dsub_rn(loc[line + 1], ll);
-    for (int k = threadIdx.x; k < p.outlen; k += blockDim.x) {
+    const int kx1 = p.x1 > 0 ? p.x1 : p.outlen;
+    for (int k = p.x0 + threadIdx.x; k < kx1; k += blockDim.x) {
         int64_t idx = (int64_t)line * p.outlen + k;
         double scaled = __dmul_rn((double)idx, out_scale);
         double frac = __ddiv_rn(__dsub_rn(scaled, __dmul_rn((double)line, nominal)), nominal);
@@ -1178,6 +1179,7 @@ __global__ void k_tbc(const T* stream, int64_t stream_len, TbcParams p, const do
         double outv = (double)__double2float_rn(__dmul_rn(v, la));
         int64_t o = ((int64_t)f * p.out_lines + ol) * p.outlen + k;
         if (p.out_hz) p.out_hz[o] = outv;
+        if (p.out_f32) p.out_f32[((int64_t)f * p.out_lines + ol) * p.out_stride + (k - p.x0)] = (float)outv;
         if (p.out_u16) {
             double sd = __dmul_rn(p.output_scale, __dsub_rn(outv, p.ire0));
             double val = __fma_rn(sd, p.inv_hz_ire, p.offset);
@@ -1278,7 +1280,9 @@ __global__ void __launch_bounds__(kTbcFastMaxThreads) k_tbc_fast(const float* st
         p.line_consts + ((int64_t)f * p.out_lines + ol) * kTbcLineConstsBytes);
     const float4* lut4 = reinterpret_cast<const float4*>(p.lut);
     const float4* pair4 = reinterpret_cast<const float4*>(p.lut_pair);
-    uint16_t* out = p.out_u16 + ((int64_t)f * p.out_lines + ol) * p.outlen;
+    uint16_t* out = p.out_u16 ? p.out_u16 + ((int64_t)f * p.out_lines + ol) * p.outlen : nullptr;
+    float* outf32 = p.out_f32 ? p.out_f32 + ((int64_t)f * p.out_lines + ol) * p.out_stride - p.x0 : nullptr;
+    const int kx1 = p.x1 > 0 ? p.x1 : p.outlen;
     // Each lane owns one output sample (position, level and conversion done
     // once); the 16-tap sums are gathered cooperatively: in round r the quad
     // q of lanes works on the sample of lane 8 r + q, lane `sub` reading taps
@@ -1286,9 +1290,9 @@ __global__ void __launch_bounds__(kTbcFastMaxThreads) k_tbc_fast(const float* st
     // quad in two coalesced accesses instead of eight scattered ones.
     const int lane = threadIdx.x & 31;
     const int q = lane >> 2, sub = lane & 3;
-    for (int k0 = 0; k0 < p.outlen; k0 += blockDim.x) {
+    for (int k0 = p.x0; k0 < kx1; k0 += blockDim.x) {
         const int k = k0 + threadIdx.x;
-        const bool valid = k < p.outlen;
+        const bool valid = k < kx1;
         const float kf = (float)(valid ? k : 0);
         float2 kb = ff_mul(kf, 0.0f, c.b.x, c.b.y);
         float2 pos = ff_add(c.a.x, c.a.y, kb.x, kb.y);
@@ -1361,6 +1365,10 @@ __global__ void __launch_bounds__(kTbcFastMaxThreads) k_tbc_fast(const float* st
         }
         float2 v = ff_mul(hi_own, lo_own, la.x, la.y);
         float outf = __fadd_rn(v.x, v.y);
+        if (outf32) {
+            outf32[k] = outf;   // float output (the chroma channel): no conversion
+            continue;
+        }
         if (!isfinite(outf)) {
             out[k] = outf > 0.0f ? 65535 : 0;
             continue;
@@ -1393,14 +1401,16 @@ cudaError_t launch_tbc_pw(const T* stream, int64_t stream_len, const TbcParams& 
     if (p.nfields <= 0) return cudaSuccess;
     k_tbc_levels<<<p.nfields, 512, 0, s>>>(p, pw);   // one compare-exchange per thread per sort stage
     dim3 grid(p.out_lines, p.nfields);
-    if (sizeof(T) == sizeof(float) && p.out_u16 && !p.out_hz && (p.smoothing <= 0.0 || p.pw_ff) &&
+    const bool one_out = (p.out_u16 != nullptr) != (p.out_f32 != nullptr);
+    if (sizeof(T) == sizeof(float) && one_out && !p.out_hz && (p.smoothing <= 0.0 || p.pw_ff) &&
         p.line_consts) {
         const int64_t nl = (int64_t)p.nfields * p.out_lines;
         k_tbc_consts<<<(unsigned)((nl + 127) / 128), 128, 0, s>>>(p);
         // a line in the fewest passes of at most 384 lanes, with the fewest idle
         // lanes in the last pass (NTSC 910 samples: 3 x 320, PAL 1135: 3 x 384)
-        const int passes = (p.outlen + kTbcFastMaxThreads - 1) / kTbcFastMaxThreads;
-        const int threads = ((p.outlen + passes - 1) / passes + 31) / 32 * 32;
+        const int width = (p.x1 > 0 ? p.x1 : p.outlen) - p.x0;
+        const int passes = (width + kTbcFastMaxThreads - 1) / kTbcFastMaxThreads;
+        const int threads = ((width + passes - 1) / passes + 31) / 32 * 32;
         k_tbc_fast<<<grid, threads, 0, s>>>(reinterpret_cast<const float*>(stream), stream_len, p);
     } else {
         k_tbc<T><<<grid, 256, 0, s>>>(stream, stream_len, p, pw);

@@ -3,8 +3,8 @@
 // Values restate the frozen upstream parameter snapshot the reference embeds
 // (src/VHSDecode.Core/Formats/format-params.snapshot.json, cases PAL and NTSC
 // VHS and SVHS at sp, lp and ep, read by
-// Core/Formats/FormatCatalog.cs:46-112); only the keys the RF -> TBC luma path
-// reads are kept.
+// Core/Formats/FormatCatalog.cs:46-112); only the keys the RF -> TBC luma and
+// chroma paths read are kept.
 #pragma once
 #include <cmath>
 #include <cstdint>
@@ -34,6 +34,11 @@ struct FormatParams {
     bool video_lpf_supergauss;
     double deemph_gain, deemph_mid, deemph_q;
     double color_under;
+    // colour-under chroma (BuildChromaFieldOptions / BuildChromaBurstSos,
+    // TbcFieldDecodePipeline.cs:2626-2760, DecodeFilterSet.cs:563-599)
+    double burst_abs_ref;                    // sysparams burst_abs_ref
+    double chroma_bpf_upper;                 // RF chroma band-pass top (Hz); bottom 60 kHz, order 4
+    int chroma_rot0, chroma_rot1;            // rfparams chroma_rotation
     // video_custom_luma_filters (DecodeFilterSet.cs:1560-1609): the measured
     // "svhs-sp-linear-subdeemphasis" response (used where a table exists for
     // the sample rate) and a high shelf designed at half the sample rate
@@ -67,6 +72,7 @@ inline FormatParams pal_vhs_sp() {
     f.video_lpf_freq = 3400000.0; f.video_lpf_order = 6; f.video_lpf_supergauss = false;
     f.deemph_gain = 13.9794; f.deemph_mid = 273755.82; f.deemph_q = 0.462088186;
     f.color_under = 626953.0;
+    f.burst_abs_ref = 5000.0; f.chroma_bpf_upper = 1300000.0; f.chroma_rot0 = 0; f.chroma_rot1 = -1;
     return f;
 }
 
@@ -87,6 +93,7 @@ inline FormatParams ntsc_vhs_sp() {
     f.video_lpf_freq = 6600000.0; f.video_lpf_order = 9; f.video_lpf_supergauss = true;
     f.deemph_gain = 13.9794; f.deemph_mid = 273755.82; f.deemph_q = 0.462088186;
     f.color_under = 629370.6293706294;
+    f.burst_abs_ref = 4416.0; f.chroma_bpf_upper = 1200000.0; f.chroma_rot0 = -1; f.chroma_rot1 = 1;
     return f;
 }
 
@@ -133,7 +140,8 @@ inline FormatParams ntsc_svhs_sp() {
 // a first-order 820 kHz high-pass of the video, the amplitude low-pass at its
 // 700 kHz default, nonlinear_exp_scaling 0.12, nonlinear_scaling_1 0.1, no
 // second scale, logistic or static factor) and, for NTSC, a lower extra RF
-// low-pass (LP 5.9 MHz, EP 5.8 MHz) and an EP band-pass top of 6.4 MHz.
+// low-pass (LP 5.9 MHz, EP 5.8 MHz), an EP band-pass top of 6.4 MHz and an LP
+// burst reference of 2208.
 inline void vhs_long_play(FormatParams& f, bool ep) {
     f.sub_deemph = true;
     f.sub_hp_freq = 820000.0;
@@ -148,6 +156,7 @@ inline void vhs_long_play(FormatParams& f, bool ep) {
     if (!f.pal) {
         f.lpf_extra = ep ? 5800000.0 : 5900000.0;
         if (ep) f.bpf_high = 6400000.0;
+        else f.burst_abs_ref = 2208.0;   // NTSC VHS LP: half the SP burst reference
     }
 }
 

@@ -186,6 +186,9 @@ struct TbcParams {
     double ire0, output_scale, inv_hz_ire, offset;  // uint16 conversion
     uint16_t* out_u16;          // [nfields * out_lines * outlen] or null
     double* out_hz;             // optional float output (values rounded to float)
+    float* out_f32;             // optional float output [nfields * out_lines * out_stride]:
+                                // samples x0 .. x1-1 of each line at (k - x0)
+    int x0, x1, out_stride;     // line window of out_f32 (x1 = 0: the whole line)
     double* level_work;         // [nfields * (max_first_line + out_lines)] line factors
     unsigned char* line_consts; // [nfields * out_lines * kTbcLineConstsBytes] float-pair line plans
                                 // of the fast float kernel (null: binary64 kernel)
@@ -197,6 +200,71 @@ constexpr int kTbcFastKernels = 3;  // levels + line plans + sinc (float kernel)
 template <typename T>
 cudaError_t launch_tbc_pw(const T* video_stream, int64_t stream_len, const TbcParams& p,
                           const double* pw, cudaStream_t stream);
+
+// ---------------------------------------------------------------- chroma
+// A float32 section cascade run forward-backward (SosFilter.ApplyForwardBackwardFloat32,
+// Core/Dsp/SosFilter.cs:369-538): four sections (b0 b1 b2 a0 a1 a2), the
+// steady-state initial conditions and the odd-extension length.
+struct ChromaCascade {
+    float sec[4][6];
+    float zi[4][2];
+    int edge;
+};
+
+// Chroma channel of blocks [first_block, first_block + nblocks): the RF block
+// band-passed, rolled by `move` and its float mean removed, stitched like the
+// demodulated channels (stream index b*30720 + n - 1024).
+struct ChromaBlockParams {
+    const int16_t* rf16;       // capture at the decode rate (int16), or
+    const float* rf32;         //   float (read when set)
+    int64_t first_block, nblocks;
+    ChromaCascade c;
+    int move;
+    float* scratch;            // [nblocks * (kBlock + 2 * c.edge)]
+    float* out;                // stitched chroma stream
+};
+constexpr int kChromaBlockKernels = 2;
+cudaError_t launch_chroma_blocks(const ChromaBlockParams& p, cudaStream_t stream);
+
+// Per-field chroma stages of a field batch (every array offset to the batch).
+struct ChromaFieldParams {
+    int nfields;
+    int lines;                  // line locations per field
+    const double* locs;         // [nfields * lines] hsync-refined, before the NTSC shift
+    double* locs_out;           // [nfields * lines] burst-refined, NTSC-shifted
+    double ntsc_shift;          // subtracted from every location after the refinement
+    int ntsc;
+    int out_lines, outlen;
+    int bs, be;                 // burst window of an output line
+    int win0, win;              // burst-probe window of a line: [2 bs - be, bs + be)
+    int input_line;             // round(nominal input line length)
+    double fsc_ratio;
+    int rot0, rot1;             // chroma_rotation
+    ChromaCascade fin;          // final / burst-probe band-pass
+    const float* het;           // [4 * field] heterodyne tables
+    const float* bsin;          // [field] burst carrier tables
+    const float* bcos;
+    const float* ana;           // [nfields * out_lines * win] chroma TBC from line 1, probe windows
+    double* probe;              // [nfields * 2 * out_lines * 5] phase, offset, magnitude, I, Q
+    int* flip;                  // [nfields * 2]
+    int* chosen;                // [nfields] rotation index of the kept sequence
+    const int* rot_in;          // rotation index before the first field
+    int* rot_out;               // rotation index after the last field
+    double* summary;            // [nfields * 4] average, even, odd phase, mean magnitude
+    int* status;                // nonzero: a field had no burst to average
+    const int* first_line;      // [nfields] output first line
+    const int* first_field;     // [nfields] 1: first field
+    const int* field_number;    // [nfields] VHS field number (NTSC colour frame)
+    const float* cfield;        // [nfields * field] chroma TBC of the output lines
+    float* up;                  // [nfields * field] up-converted, then band-passed in place
+    float* fwd;                 // [nfields * (field + 2 fin.edge)] forward pass
+    uint16_t* out;              // [nfields * field] uint16 chroma
+    double cu_hz, fsc_mhz, burst_abs_ref;
+};
+constexpr int kChromaPhaseKernels = 5;    // probes, flips, rotation chain, averages, refinement
+constexpr int kChromaDecodeKernels = 4;   // up-conversion, forward, backward, gain
+cudaError_t launch_chroma_phase(const ChromaFieldParams& p, cudaStream_t stream);
+cudaError_t launch_chroma_decode(const ChromaFieldParams& p, cudaStream_t stream);
 
 // ---------------------------------------------------------------- dropouts
 struct DropoutParams {

@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "../../include/vhsdecode_gb300.h"
+#include "chroma.hpp"
 #include "control.hpp"
 #include "filters.hpp"
 #include "formats.hpp"
@@ -96,6 +97,7 @@ struct FieldRec {
     FieldSync sync;
     int64_t span_start;
     int64_t span_len;
+    int field_number = 0;       // VHS field number (NTSC chroma colour frame)
     std::vector<double> refined;
     std::vector<int32_t> drop;  // triplets
 };
@@ -222,6 +224,21 @@ struct vhsdecode_gb300_session {
     DevBuf<int32_t> drop_out;
     int drop_cap = 1024, drop_out_cap = 4096;
     int64_t span_len = 0;
+    // colour-under chroma (allocated by the first decode that asks for it)
+    bool chroma_alloc = false;
+    bool want_chroma = false;            // the current decode renders chroma
+    vhsd::ChromaDesign cd;
+    DevBuf<float> c32;                   // stitched chroma stream
+    DevBuf<float> c_scratch;             // block band-pass passes [max_blocks * (kBlock + 2 edge)]
+    DevBuf<float> c_het, c_bsin, c_bcos; // field tables
+    DevBuf<float> c_ana;                 // line-1 chroma TBC, probe windows
+    DevBuf<float> c_field, c_up, c_fwd;  // output-line chroma TBC, up-converted / filtered, forward pass
+    DevBuf<double> c_probe, c_summary, locs_final;
+    DevBuf<int> c_flip, c_chosen, c_state, c_ones;   // c_state: rotation out, status
+    DevBuf<uint16_t> chroma;             // uint16 chroma fields
+    View<int> first_field_d, field_number_d, rot_in_d;
+    int chroma_rot_start = 0, chroma_rot_end = 0;
+    cudaEvent_t chroma_refined = nullptr;
     // host results
     std::vector<FieldRec> fields;
     int64_t last_blocks = 0;

@@ -18,7 +18,7 @@ OBJ = os.path.join(LIB_DIR, "obj")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["demod_fp32.cu", "demod_fp64.cu", "field_kernels.cu", "test_entries.cu", "decimate.cu",
            "abi.cpp", "control.cpp", "filters.cpp", "noalloc.cu",
-           "server.cpp", "run.cpp", "flac.cu"]
+           "server.cpp", "run.cpp", "flac.cu", "chroma.cu", "chroma_design.cpp"]
 
 
 def nvcc():
@@ -35,8 +35,9 @@ def _compile(src):
     deps.append(os.path.join(os.path.dirname(PKG), "include", "vhsdecode_gb300.h"))
     if os.path.exists(out) and os.path.getmtime(out) >= max(os.path.getmtime(d) for d in deps):
         return out
+    # host floating point exactly as written (no fused multiply-adds on Arm)
     common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
-              "-I", CSRC]
+              "-Xcompiler", "-ffp-contract=off", "-I", CSRC]
     if src.endswith(".cu"):
         cmd = [nvcc()] + ARCH + common + ["-lineinfo", "-c", srcp, "-o", out]
     else:

@@ -13,7 +13,7 @@ import os
 
 import numpy as np
 
-ABI_VERSION = 0x00010004
+ABI_VERSION = 0x00010005
 STATUS_OK = 0
 STATUS_NULL_POINTER = -20000
 STATUS_INVALID_ARGUMENT = -20001
@@ -32,6 +32,7 @@ PRECISION_FP32_FUSED, PRECISION_FP64_PLAIN = 0, 1
 DECODE_DEVICE_INPUT = 0x1
 DECODE_DEMOD_ONLY = 0x2
 DECODE_FLOAT_INPUT = 0x4
+DECODE_CHROMA = 0x8
 
 LIB_PATH = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "lib",
                         "libvhsdecode_gb300.so")
@@ -45,6 +46,7 @@ EXPORTS = [
     "vhsdecode_gb300_session_copy_tbc", "vhsdecode_gb300_session_copy_lines",
     "vhsdecode_gb300_session_copy_dropouts", "vhsdecode_gb300_session_copy_stream",
     "vhsdecode_gb300_session_tbc_device", "vhsdecode_gb300_design_filters",
+    "vhsdecode_gb300_session_copy_chroma", "vhsdecode_gb300_design_chroma",
     "vhsdecode_gb300_field_sync", "vhsdecode_gb300_tbc_resample_lines",
     "vhsdecode_gb300_find_pulses", "vhsdecode_gb300_vhs_angles",
     "vhsdecode_gb300_pulse_events_noalloc", "vhsdecode_gb300_vhs_demod",
@@ -188,6 +190,9 @@ def load(path: str = LIB_PATH):
                                                  ctypes.c_uint32, _P(DecodeResult)]
     L.vhsdecode_gb300_session_get_field.argtypes = [_vp, ctypes.c_uint32, _P(FieldInfo)]
     L.vhsdecode_gb300_session_copy_tbc.argtypes = [_vp, ctypes.c_uint32, ctypes.c_uint32, _vp]
+    L.vhsdecode_gb300_session_copy_chroma.argtypes = [_vp, ctypes.c_uint32, ctypes.c_uint32, _vp]
+    L.vhsdecode_gb300_design_chroma.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                                ctypes.c_double, _vp, _vp, _vp, _vp, _vp, _vp]
     L.vhsdecode_gb300_session_copy_lines.argtypes = [_vp, ctypes.c_uint32, _vp, ctypes.c_uint32]
     L.vhsdecode_gb300_session_copy_dropouts.argtypes = [_vp, ctypes.c_uint32, _vp, _vp, _vp,
                                                         ctypes.c_uint32, _P(ctypes.c_uint32)]
@@ -290,6 +295,29 @@ def design_filters(profile, sample_rate_mhz=40.0, tape_speed=TAPE_SP, tape_forma
     out = (rv, v[0::2] + 1j * v[1::2], s[0::2] + 1j * s[1::2], env[:3])
     if sub:
         out = out + (h[0::2] + 1j * h[1::2], env[3:])
+    return out
+
+
+def design_chroma(profile, sample_rate_mhz=40.0, tape_speed=TAPE_SP, tape_format=FORMAT_VHS, tables=False):
+    """Chroma design of the library: dict with rf_sos and final_sos (4 x 6),
+    burst_start, burst_end, move, rf_edge, final_edge, rotation, field_samples
+    and, with ``tables``, the heterodyne (4 x field) and burst sin/cos tables."""
+    rf = np.zeros(24)
+    fin = np.zeros(24)
+    g = np.zeros(8, np.int32)
+    check(load().vhsdecode_gb300_design_chroma(profile, tape_speed, tape_format, sample_rate_mhz, _ptr(rf),
+                                               _ptr(fin), _ptr(g), None, None, None))
+    out = {"rf_sos": rf.reshape(4, 6), "final_sos": fin.reshape(4, 6), "burst_start": int(g[0]),
+           "burst_end": int(g[1]), "move": int(g[2]), "rf_edge": int(g[3]), "final_edge": int(g[4]),
+           "rotation": [int(g[5]), int(g[6])], "field_samples": int(g[7])}
+    if tables:
+        n = out["field_samples"]
+        het = np.zeros(4 * n, np.float32)
+        bs = np.zeros(n, np.float32)
+        bc = np.zeros(n, np.float32)
+        check(load().vhsdecode_gb300_design_chroma(profile, tape_speed, tape_format, sample_rate_mhz, _ptr(rf),
+                                                   _ptr(fin), _ptr(g), _ptr(het), _ptr(bs), _ptr(bc)))
+        out.update(heterodyne=het.reshape(4, n), burst_sin=bs, burst_cos=bc)
     return out
 
 
@@ -417,12 +445,17 @@ class Session:
     def set_stream(self, stream_handle):
         check(load().vhsdecode_gb300_session_set_stream(self._h, ctypes.c_void_p(stream_handle)))
 
-    def decode(self, rf, max_fields=0, demod_only=False, device_ptr=None, count=None, float_input=None):
+    def decode(self, rf, max_fields=0, demod_only=False, device_ptr=None, count=None, float_input=None,
+               chroma=False):
         """Decode int16 samples (or float32 ones: a float32 array, or
-        ``float_input=True`` with ``device_ptr``)."""
+        ``float_input=True`` with ``device_ptr``); ``chroma`` renders the
+        colour-under chroma (and refines the lines from the burst) as the
+        reference's default decode does."""
         r = DecodeResult()
         r.struct_size = ctypes.sizeof(DecodeResult)
         flags = DECODE_DEMOD_ONLY if demod_only else 0
+        if chroma:
+            flags |= DECODE_CHROMA
         if device_ptr is not None:
             flags |= DECODE_DEVICE_INPUT
             ptr, n = ctypes.c_void_p(device_ptr), int(count)
@@ -453,6 +486,15 @@ class Session:
         if out is None:
             out = np.zeros(n, np.uint16)
         check(load().vhsdecode_gb300_session_copy_tbc(self._h, first, count, _ptr(out)))
+        return out.reshape(count, self.last.output_field_lines, self.last.output_line_length)
+
+    def chroma(self, first=0, count=None, out=None):
+        if count is None:
+            count = self.last.fields - first
+        n = count * self.last.output_field_lines * self.last.output_line_length
+        if out is None:
+            out = np.zeros(n, np.uint16)
+        check(load().vhsdecode_gb300_session_copy_chroma(self._h, first, count, _ptr(out)))
         return out.reshape(count, self.last.output_field_lines, self.last.output_line_length)
 
     def tbc_into(self, first, count, host_ptr):
