@@ -281,6 +281,17 @@ VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_session_copy_tb
 VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_session_copy_chroma(
     vhsdecode_gb300_session* session, uint32_t first, uint32_t count, uint16_t* destination);
 
+/* Chroma stages of one field of the last chroma decode, as double (tests):
+ * 0 chroma TBC of the output lines, 1 the up-converted chroma after the final
+ * band-pass (field samples each), 2 the line-1 chroma TBC at the burst-probe
+ * windows (lines x window), 3 the kept burst sequence (lines x phase, offset,
+ * magnitude, I, Q, then its rotation index), 4 the phase averages (all, even,
+ * odd, mean magnitude), 5 the hsync-refined line locations the burst
+ * refinement started from.  *count receives the values written. */
+VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_session_copy_chroma_stage(
+    vhsdecode_gb300_session* session, uint32_t field, uint32_t stage, double* destination, uint64_t capacity,
+    uint64_t* count);
+
 /* Refined line locations of one field (span-relative samples). */
 VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_session_copy_lines(
     vhsdecode_gb300_session* session, uint32_t field, double* destination, uint32_t capacity);

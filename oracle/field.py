@@ -250,6 +250,7 @@ def decode_capture(rf, fmt, fs=40e6, max_fields=None, want_tbc=True, channels=No
             continue
         state.vhs_number, state.vhs_loc = number, s0
         f["span_start"] = s0
+        f["span_len"] = slen
         fields.append(f)
         intended = s0 + max(1, int(sync.round_away(f["next_offset"])))
     return fields, channels

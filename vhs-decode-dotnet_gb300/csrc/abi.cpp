@@ -1678,6 +1678,51 @@ VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_session_copy_ch
     });
 }
 
+VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_session_copy_chroma_stage(
+    vhsdecode_gb300_session* s, uint32_t field, uint32_t stage, double* dst, uint64_t capacity, uint64_t* count) {
+    return guard([&]() -> int32_t {
+        if (!s || !dst || !count) return fail(VHSDECODE_GB300_STATUS_NULL_POINTER, "null argument");
+        if (!s->want_chroma) return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "the last decode rendered no chroma");
+        if (field >= s->fields.size()) return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "field index out of range");
+        const size_t fsz = (size_t)s->cd.field_samples;
+        const size_t win = (size_t)(2 * s->cd.burst_end - s->cd.burst_start);
+        ck(cudaStreamSynchronize(s->stream), "sync");
+        std::vector<float> tf;
+        const float* fsrc = nullptr;
+        size_t n = 0;
+        if (stage == 0) { fsrc = s->c_field.p + field * fsz; n = fsz; }
+        else if (stage == 1) { fsrc = s->c_up.p + field * fsz; n = fsz; }
+        else if (stage == 2) { fsrc = s->c_ana.p + field * (size_t)s->out_lines * win; n = (size_t)s->out_lines * win; }
+        if (fsrc) {
+            if (capacity < n) return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "capacity too small");
+            tf.resize(n);
+            ck(cudaMemcpy(tf.data(), fsrc, n * sizeof(float), cudaMemcpyDeviceToHost), "d2h");
+            for (size_t i = 0; i < n; i++) dst[i] = tf[i];
+        } else if (stage == 3) {
+            int c = 0;
+            ck(cudaMemcpy(&c, s->c_chosen.p + field, sizeof(int), cudaMemcpyDeviceToHost), "d2h");
+            n = (size_t)s->out_lines * 5 + 1;
+            if (capacity < n) return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "capacity too small");
+            ck(cudaMemcpy(dst, s->c_probe.p + ((size_t)field * 2 + c) * s->out_lines * 5,
+                          (n - 1) * sizeof(double), cudaMemcpyDeviceToHost), "d2h");
+            dst[n - 1] = c;
+        } else if (stage == 4) {
+            n = 4;
+            if (capacity < n) return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "capacity too small");
+            ck(cudaMemcpy(dst, s->c_summary.p + (size_t)field * 4, 4 * sizeof(double), cudaMemcpyDeviceToHost), "d2h");
+        } else if (stage == 5) {
+            n = (size_t)s->lines;
+            if (capacity < n) return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "capacity too small");
+            ck(cudaMemcpy(dst, s->locs_out.p + (size_t)field * s->lines, n * sizeof(double), cudaMemcpyDeviceToHost),
+               "d2h");
+        } else {
+            return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "stage must be 0..5");
+        }
+        *count = n;
+        return VHSDECODE_GB300_STATUS_OK;
+    });
+}
+
 VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_session_copy_lines(
     vhsdecode_gb300_session* s, uint32_t field, double* dst, uint32_t cap) {
     return guard([&]() -> int32_t {

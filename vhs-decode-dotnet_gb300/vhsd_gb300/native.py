@@ -47,6 +47,7 @@ EXPORTS = [
     "vhsdecode_gb300_session_copy_dropouts", "vhsdecode_gb300_session_copy_stream",
     "vhsdecode_gb300_session_tbc_device", "vhsdecode_gb300_design_filters",
     "vhsdecode_gb300_session_copy_chroma", "vhsdecode_gb300_design_chroma",
+    "vhsdecode_gb300_session_copy_chroma_stage",
     "vhsdecode_gb300_field_sync", "vhsdecode_gb300_tbc_resample_lines",
     "vhsdecode_gb300_find_pulses", "vhsdecode_gb300_vhs_angles",
     "vhsdecode_gb300_pulse_events_noalloc", "vhsdecode_gb300_vhs_demod",
@@ -191,6 +192,8 @@ def load(path: str = LIB_PATH):
     L.vhsdecode_gb300_session_get_field.argtypes = [_vp, ctypes.c_uint32, _P(FieldInfo)]
     L.vhsdecode_gb300_session_copy_tbc.argtypes = [_vp, ctypes.c_uint32, ctypes.c_uint32, _vp]
     L.vhsdecode_gb300_session_copy_chroma.argtypes = [_vp, ctypes.c_uint32, ctypes.c_uint32, _vp]
+    L.vhsdecode_gb300_session_copy_chroma_stage.argtypes = [_vp, ctypes.c_uint32, ctypes.c_uint32, _vp,
+                                                            ctypes.c_uint64, _P(ctypes.c_uint64)]
     L.vhsdecode_gb300_design_chroma.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
                                                 ctypes.c_double, _vp, _vp, _vp, _vp, _vp, _vp]
     L.vhsdecode_gb300_session_copy_lines.argtypes = [_vp, ctypes.c_uint32, _vp, ctypes.c_uint32]
@@ -496,6 +499,18 @@ class Session:
             out = np.zeros(n, np.uint16)
         check(load().vhsdecode_gb300_session_copy_chroma(self._h, first, count, _ptr(out)))
         return out.reshape(count, self.last.output_field_lines, self.last.output_line_length)
+
+    def chroma_stage(self, field, stage):
+        """Intermediate chroma of one field (0 TBC, 1 band-passed up-conversion,
+        2 probe windows, 3 kept burst sequence + rotation index, 4 averages,
+        5 hsync-refined lines before the burst refinement)."""
+        n = max(self.last.output_field_lines * self.last.output_line_length,
+                self.last.output_field_lines * 5 + 1, 1 << 20)
+        out = np.zeros(n)
+        cnt = ctypes.c_uint64(0)
+        check(load().vhsdecode_gb300_session_copy_chroma_stage(self._h, field, stage, _ptr(out), n,
+                                                               ctypes.byref(cnt)))
+        return out[:cnt.value]
 
     def tbc_into(self, first, count, host_ptr):
         check(load().vhsdecode_gb300_session_copy_tbc(self._h, first, count,

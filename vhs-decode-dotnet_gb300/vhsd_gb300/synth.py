@@ -4,8 +4,9 @@ Builds composite luma (IRE) with the PAL 625/50 or NTSC 525/60 sync structure
 (equalising / broad pulses at half-line spacing, hsync, active video), applies
 the VHS FM pre-emphasis (the high shelf whose inverse the decoder uses as its
 de-emphasis), FM-modulates it with f = ire0 + hz_ire * IRE, adds the
-colour-under carrier, optional carrier dropouts, timebase wobble and head
-switching jumps, Gaussian noise at a stated SNR, and quantises to int16 with a
+line-locked colour-under chroma (burst and colour bars, heterodyned down with
+the format's per-line phase rotation), optional carrier dropouts, timebase
+wobble and head switching jumps, Gaussian noise at a stated SNR, and quantises to int16 with a
 +/-12000 peak.  Everything is driven by one ``numpy.random.Generator`` seed.
 
 The pulse geometry (half-line positions of the equalising and broad pulses
@@ -229,9 +230,8 @@ def generate(cfg: SynthConfig):
             amp[s:s + int(ln)] = cfg.dropout_level
         carrier = carrier * amp
     chroma_amp = 10.0 ** (cfg.chroma_db / 20.0)
-    cphase = 2 * np.pi * cfg.chroma_hz * n / fs + rng.uniform(0, 2 * np.pi)
-    cmod = 1.0 + 0.3 * np.sin(2 * np.pi * 7.8e3 * n / fs)
-    rf = carrier + chroma_amp * cmod * np.cos(cphase)
+    chroma = _colour_under(cfg, g, fs, frame_no, frame_line, tau_l, field_index, x, act_win, is_active, edge)
+    rf = carrier + chroma_amp * chroma
     sig_rms = math.sqrt(0.5 + 0.5 * chroma_amp ** 2)
     noise_std = sig_rms / (10.0 ** (cfg.snr_db / 20.0))
     rf = rf + rng.normal(0.0, noise_std, size=total)
@@ -240,6 +240,50 @@ def generate(cfg: SynthConfig):
     info = {"line_len": line_len, "field_samples": field_samples, "lead": lead,
             "total": total, "scale": scale}
     return out, info
+
+
+# 75 % colour bars: (U, V) of white, yellow, cyan, green, magenta, red, blue, black
+_BARS_UV = 0.75 * np.array([[0.0, 0.0], [-0.436, 0.100], [0.147, -0.615], [-0.289, -0.515],
+                            [0.289, 0.515], [-0.147, 0.615], [0.436, -0.100], [0.0, 0.0]])
+
+
+def _colour_under(cfg, g, fs, frame_no, frame_line, tau_l, field_index, x, act_win, is_active, edge):
+    """Line-locked colour-under chroma, as a VCR records it: the composite
+    chroma (burst, and the colour bars' U/V on 'bars' fields) is heterodyned
+    down to the colour-under carrier with the format's per-line phase rotation
+    (PAL: 0 or -90 degrees a line on alternate fields; NTSC: -90 or +90).  In
+    the decoder's 4 fSC domain, up-converting with the same rotation gives the
+    burst and the bars back at fSC.  Amplitude 1 is the peak chroma."""
+    pal = cfg.system == "PAL"
+    us = 1e6 / fs
+    frame_lines = g["lines"]
+    line_index = frame_no * frame_lines + (frame_line - 1)       # running line count
+    rot = np.where(field_index % 2 == 0, 0, -1) if pal else np.where(field_index % 2 == 0, -1, 1)
+    quarter = np.mod(rot * line_index, 4)
+    # burst: PAL +-135 degrees (alternate lines), NTSC 180 degrees
+    b0, b1 = (5.6, 7.85) if pal else (5.3, 7.8)
+    bwin = _smoothstep(tau_l - b0 / us, edge) * (1.0 - _smoothstep(tau_l - b1 / us, edge))
+    vsw = np.where(line_index % 2 == 0, 1.0, -1.0) if pal else np.ones_like(tau_l)
+    burst_phase = np.where(vsw > 0, 0.75 * np.pi, 1.25 * np.pi) if pal else np.full_like(tau_l, np.pi)
+    # active picture: the bars' chroma on 'bars' fields
+    bars_field = np.zeros_like(tau_l, dtype=bool)
+    for fi in np.unique(field_index):
+        if cfg.patterns[int(fi) % len(cfg.patterns)] == "bars":
+            bars_field |= field_index == fi
+    idx = np.clip((x * 8).astype(np.int64), 0, 7)
+    u = _BARS_UV[idx, 0]
+    v = _BARS_UV[idx, 1] * vsw
+    amp_act = np.hypot(u, v) * act_win * is_active * bars_field
+    hue = np.arctan2(v, u)
+    amp = 0.3 * bwin + amp_act
+    theta = np.where(bwin > amp_act, burst_phase, hue)
+    # colour-under phase of the line: rotation, the carrier's advance over one
+    # output line of the 4 fSC time base (outlinelen samples; about 40.125
+    # cycles PAL, 40 NTSC) and the composite phase, reversed by the down-conversion
+    outlen, fsc = (1135, 4.43361875e6) if pal else (910, 315e6 / 88.0)
+    per_line = 2.0 * np.pi * cfg.chroma_hz * outlen / (4.0 * fsc)
+    psi = np.pi + quarter * (np.pi / 2.0) - theta + per_line * line_index
+    return amp * np.cos(2.0 * np.pi * cfg.chroma_hz * tau_l / fs + psi)
 
 
 def _gauss_smooth(x, sigma_samples):
