@@ -198,8 +198,9 @@ def make_pool(procs):
     return mp.get_context("spawn").Pool(procs)
 
 
-def cpu_oracle_msps(rf, system, procs, pool=None, tape="VHS"):
-    """Oracle decode of the capture: block demod over a spawn pool, field path sequential."""
+def cpu_oracle_msps(rf, system, procs, pool=None, tape="VHS", chroma=True):
+    """Oracle decode of the capture: block demod (and the chroma block band-pass)
+    over a spawn pool, field path (with the chroma field decode) sequential."""
     from oracle import demod, field, formats
     fmt = formats.get(system, tape)
     nblocks = demod.block_count(len(rf))
@@ -210,7 +211,7 @@ def cpu_oracle_msps(rf, system, procs, pool=None, tape="VHS"):
     chunks = np.array_split(np.arange(nblocks), procs * 4)
     try:
         parts = pool.map(_oracle_demod_part,
-                         [(rf[int(c[0]) * STRIDE: (int(c[-1]) * STRIDE + BLOCK)], system, tape, len(c))
+                         [(rf[int(c[0]) * STRIDE: (int(c[-1]) * STRIDE + BLOCK)], system, tape, len(c), chroma)
                           for c in chunks if len(c)])
     finally:
         if own:
@@ -218,7 +219,9 @@ def cpu_oracle_msps(rf, system, procs, pool=None, tape="VHS"):
     video = np.concatenate([p[0] for p in parts])
     vlp = np.concatenate([p[1] for p in parts])
     env = np.concatenate([p[2] for p in parts])
-    fields, _ = field.decode_capture(rf, fmt, channels=(video, vlp, env, False))
+    cch = np.concatenate([p[3] for p in parts]) if chroma else None
+    fields, _ = field.decode_capture(rf, fmt, channels=(video, vlp, env, False), with_chroma=chroma,
+                                     chroma_channel=cch)
     dt = time.perf_counter() - t0
     return len(rf) / dt / 1e6, dt, len([f for f in fields if "error" not in f])
 
@@ -227,15 +230,17 @@ _FILTERS = {}
 
 
 def _oracle_demod_part(args):
-    rf, system, tape, nb = args
-    from oracle import demod, formats
+    rf, system, tape, nb, chroma = args
+    from oracle import chroma as ochroma, demod, formats
     from oracle.filters import FilterSet
     fmt = formats.get(system, tape)
     if (system, tape) not in _FILTERS:
-        _FILTERS[(system, tape)] = FilterSet(fmt, 40e6)
+        _FILTERS[(system, tape)] = (FilterSet(fmt, 40e6), ochroma.ChromaParams(fmt, 40e6))
+    filt, cp = _FILTERS[(system, tape)]
     dmax = (fmt["sys"]["ire0"] + fmt["sys"]["hz_ire"] * 100.0) * 2.0
-    v, l, e, _ = demod.demod_stream(rf, _FILTERS[(system, tape)], 40e6, dmax, 0, nb)
-    return v, l, e
+    v, l, e, _ = demod.demod_stream(rf, filt, 40e6, dmax, 0, nb)
+    c = ochroma.chroma_stream(rf, cp, 0, nb) if chroma else None
+    return v, l, e, c
 
 
 def run_reference(args, world, rank):
@@ -245,11 +250,12 @@ def run_reference(args, world, rank):
     desc, system, tape = WORKLOADS[args.workload]
     procs = os.cpu_count() or 1
     pool = make_pool(procs)
+    chroma = not args.luma_only
     for _ in range(args.warmup):
-        cpu_oracle_msps(rf[: 4 * 1048576], system, procs, pool, tape)
+        cpu_oracle_msps(rf[: 4 * 1048576], system, procs, pool, tape, chroma)
     times = []
     for _ in range(args.steps):
-        msps, dt, nf = cpu_oracle_msps(rf, system, procs, pool, tape)
+        msps, dt, nf = cpu_oracle_msps(rf, system, procs, pool, tape, chroma)
         times.append(dt)
     pool.close()
     avg = sum(times) / len(times)
@@ -261,7 +267,8 @@ def run_reference(args, world, rank):
             "config": {"workload": args.workload, "description": desc, "samples": int(len(rf))},
             "cpu_baseline": {"value": round(value, 3), "unit": "MSPS", "cores": procs, "kind": "port",
                              "sample": "whole workload capture per step (oracle restatement: "
-                                       "numpy FFT block demod over a spawn pool + sequential field path)"},
+                                       "numpy FFT block demod%s over a spawn pool + sequential field path)"
+                                       % (" and chroma band-pass" if chroma else "")},
             "e2e": {"value": round(value, 3), "unit": "MSPS", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -282,9 +289,11 @@ def run_ours(args, world, rank, local):
     d_rf = torch.from_numpy(rf).to("cuda")
     clocks = ClockSampler(local)
     clocks.start()
-    # device-resident value
+    # device-resident value: the reference's default decode (luma and
+    # colour-under chroma) unless --luma-only
+    chroma = not args.luma_only
     for _ in range(max(3, args.warmup)):
-        sess.decode(None, device_ptr=d_rf.data_ptr(), count=n)
+        sess.decode(None, device_ptr=d_rf.data_ptr(), count=n, chroma=chroma)
     torch.cuda.synchronize()
     clocks.wait_first()
     barrier(world)
@@ -297,7 +306,7 @@ def run_ours(args, world, rank, local):
     clocks.mark()
     e0.record(stream)
     for _ in range(args.steps):
-        r = sess.decode(None, device_ptr=d_rf.data_ptr(), count=n)
+        r = sess.decode(None, device_ptr=d_rf.data_ptr(), count=n, chroma=chroma)
         demod_ms.append(r.demod_ms)
         fields = r.fields
         launches += r.kernel_launches
@@ -309,13 +318,37 @@ def run_ours(args, world, rank, local):
     ms = max_over_ranks(ms, world, "cuda")
     nblocks = int(r.blocks)
     value = world * n / (ms / 1e3) / 1e6
+    stage = r
+    # the same decode without chroma (the reference's --skip_chroma decode)
+    other = None
+    if chroma:
+        for _ in range(2):
+            sess.decode(None, device_ptr=d_rf.data_ptr(), count=n)
+        torch.cuda.synchronize()
+        g0 = torch.cuda.Event(enable_timing=True)
+        g1 = torch.cuda.Event(enable_timing=True)
+        g0.record(stream)
+        for _ in range(args.steps):
+            sess.decode(None, device_ptr=d_rf.data_ptr(), count=n)
+        g1.record(stream)
+        torch.cuda.synchronize()
+        lms = max_over_ranks(g0.elapsed_time(g1) / args.steps, world, "cuda")
+        other = {"value": round(world * n / (lms / 1e3) / 1e6, 3), "unit": "MSPS", "ms_per_step": round(lms, 3),
+                 "decode": "luma only (the reference's --skip_chroma decode: no chroma, no burst refinement)"}
     # e2e through the C ABI: pinned host in, TBC out
     h_rf = torch.from_numpy(rf).pin_memory()
     tbc_elems = fields * r.output_field_lines * r.output_line_length
     h_tbc = torch.empty(max(1, tbc_elems), dtype=torch.int16).pin_memory()
-    for _ in range(2):
-        sess.decode(h_rf.numpy())
+    h_chroma = torch.empty(max(1, tbc_elems), dtype=torch.int16).pin_memory()
+
+    def e2e_step():
+        sess.decode(h_rf.numpy(), chroma=chroma)
         sess.tbc_into(0, fields, h_tbc.data_ptr())
+        if chroma:
+            sess.chroma_into(0, fields, h_chroma.data_ptr())
+
+    for _ in range(2):
+        e2e_step()
     torch.cuda.synchronize()
     barrier(world)
     f0 = torch.cuda.Event(enable_timing=True)
@@ -323,8 +356,7 @@ def run_ours(args, world, rank, local):
     clocks.mark()
     f0.record(stream)
     for _ in range(args.steps):
-        sess.decode(h_rf.numpy())
-        sess.tbc_into(0, fields, h_tbc.data_ptr())
+        e2e_step()
     f1.record(stream)
     torch.cuda.synchronize()
     clocks.mark()
@@ -348,12 +380,12 @@ def run_ours(args, world, rank, local):
     if not args.skip_plain:
         ps = native.Session(prof, n, precision=native.PRECISION_FP64_PLAIN, device=local, tape_format=tfmt)
         ps.set_stream(stream.cuda_stream)
-        ps.decode(None, device_ptr=d_rf.data_ptr(), count=n)
+        ps.decode(None, device_ptr=d_rf.data_ptr(), count=n, chroma=chroma)
         torch.cuda.synchronize()
         p0 = torch.cuda.Event(enable_timing=True)
         p1 = torch.cuda.Event(enable_timing=True)
         p0.record(stream)
-        ps.decode(None, device_ptr=d_rf.data_ptr(), count=n)
+        ps.decode(None, device_ptr=d_rf.data_ptr(), count=n, chroma=chroma)
         p1.record(stream)
         torch.cuda.synchronize()
         pms = p0.elapsed_time(p1)
@@ -367,12 +399,13 @@ def run_ours(args, world, rank, local):
     if rank == 0 and world == 1 and not args.skip_cpu:
         procs = os.cpu_count() or 1
         pool = make_pool(procs)
-        cpu_oracle_msps(rf[: 4 * 1048576], system, procs, pool, tape)
-        msps, dt, nf = cpu_oracle_msps(rf, system, procs, pool, tape)
+        cpu_oracle_msps(rf[: 4 * 1048576], system, procs, pool, tape, chroma)
+        msps, dt, nf = cpu_oracle_msps(rf, system, procs, pool, tape, chroma)
         pool.close()
         cpu = {"value": round(msps, 3), "unit": "MSPS", "cores": procs, "kind": "port",
                "sample": "whole workload capture (%d samples, %.1f s): oracle restatement, block "
-                         "demod over %d spawn processes + sequential field path" % (n, dt, procs)}
+                         "demod%s over %d spawn processes + sequential field path"
+                         % (n, dt, " and chroma band-pass" if chroma else "", procs)}
     serving = None
     if rank == 0 and world == 1 and not args.skip_serve:
         serving = run_serving(args, local)
@@ -380,6 +413,8 @@ def run_ours(args, world, rank, local):
     if rank == 0 and world == 1 and not args.skip_flac:
         flac_leg = run_flac(rf)
     if rank == 0:
+        decode = ("luma and colour-under chroma (the reference's default decode: burst-refined lines, "
+                  "uint16 luma and chroma fields)" if chroma else "luma only (--skip_chroma)")
         line = {"metric": METRIC, "value": round(value, 3), "unit": "MSPS", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -387,12 +422,13 @@ def run_ours(args, world, rank, local):
                 "config": {"workload": args.workload, "description": desc, "samples": int(n),
                            "blocks": nblocks, "fields": int(fields),
                            "precision": "fp32 fused demod, fp64 sync/TBC",
+                           "decode": decode,
                            "fft_plan": int(r.fft_plan),
                            "l2": "inputs and streams larger than L2 (no flush)",
                            "parallelism": "replicas" if world > 1 else "single"},
                 "e2e": {"value": round(e2e_value, 3), "unit": "MSPS",
                         "h2d_bytes_per_step": int(n * 2),
-                        "d2h_bytes_per_step": int(tbc_elems * 2)},
+                        "d2h_bytes_per_step": int(tbc_elems * 2 * (2 if chroma else 1))},
                 "roofline": {"bound": "hbm", "achieved": round(single_achieved, 1), "peak": peak,
                              "unit": "GB/s", "frac": round(single_achieved / peak, 4),
                              "traffic": (round(tpb * nblocks) if tpb else None),
@@ -408,14 +444,15 @@ def run_ours(args, world, rank, local):
                                          "their summed durations exceed the step's wall time, so "
                                          "this is not a per-launch rate"}},
                 "cpu_baseline": cpu,
+                "luma_only": other,
                 "plain_fp64": plain,
                 "decimated": decimated,
                 "serving": serving,
                 "flac_decode": flac_leg,
                 "gpu_launches": int(launches),
                 "clocks": clk,
-                "stage_ms": {"demod": round(avg_demod, 4), "field_kernels_and_host": round(r.field_ms, 4),
-                             "host_control": round(r.host_ms, 4)}}
+                "stage_ms": {"demod": round(avg_demod, 4), "field_kernels_and_host": round(stage.field_ms, 4),
+                             "host_control": round(stage.host_ms, 4)}}
         print(json.dumps(line))
     sess.close()
 
@@ -660,6 +697,8 @@ def main():
     ap.add_argument("--serve-batch", type=int, default=1,
                     help="windows a free worker demodulates in one launch (1: no batching)")
     ap.add_argument("--skip-flac", action="store_true")
+    ap.add_argument("--luma-only", action="store_true",
+                    help="decode without chroma (the reference's --skip_chroma); default: luma and chroma")
     ap.add_argument("--serve-workers", type=int, default=4)
     ap.add_argument("--skip-decimated", action="store_true")
     ap.add_argument("--profile-demod", action="store_true",

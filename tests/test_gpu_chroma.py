@@ -152,7 +152,13 @@ def test_fp32_chroma_stages_match_oracle(gpu, pal_capture, ntsc_capture, system)
         # the field decode from the device's final lines and burst sequence
         ofl = field.output_first_line(sp, f["first_field"])
         c = tbc.resample_field(span, final, ofl, cp.out_lines, cp.outlen, nominal, smoothing)
-        assert np.array_equal(s.chroma_stage(i, 0), c.astype(np.float32).astype(np.float64))
+        # the float-pair tap sums round like the binary64 ones except within
+        # about 2^-46 of a float rounding boundary: at most one float ulp, rarely
+        tb = s.chroma_stage(i, 0)
+        cf = c.astype(np.float32).astype(np.float64)
+        off = tb != cf
+        assert np.mean(off) < 1e-4
+        assert np.all(np.abs(tb[off] - cf[off]) <= np.spacing(np.abs(cf[off]).astype(np.float32)).astype(np.float64))
         want = chroma.decode_field_chroma(c, cp, dict(summ, seq=seq), f["first_field"], f["field_number"], ofl)
         chd = np.abs(dev["chroma"][i].astype(np.int64).ravel() - want.astype(np.int64))
         assert np.mean(chd <= 1) >= LSB_FRACTION, (i, np.mean(chd <= 1), chd.max())

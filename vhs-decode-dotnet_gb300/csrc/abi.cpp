@@ -380,7 +380,27 @@ void ensure_chroma(vhsdecode_gb300_session* s) {
     std::vector<int> ones(mf, 1);
     ck(cudaMemcpy(s->c_ones.p, ones.data(), mf * sizeof(int), cudaMemcpyHostToDevice), "upload");
     s->chroma.alloc(mf * field);
+    {
+        // NTSC up-conversion: the phase advance of sample k of a line as the
+        // reference's four lanes step theta (UpconvertChromaPhaseCompensated,
+        // VhsChromaDecoder.cs:2182-2246), reduced by whole turns
+        const double h = ((d.cu_hz * 1.5707963267948965e-6) / d.fsc_mhz) + 1.5707963267948966;
+        const double two_pi = 6.283185307179586, inv = 0.15915494309189535;
+        const int vc = d.outlen & ~3;
+        const double lane[4] = {h * 0.0, h, h * 2.0, h * 3.0};
+        std::vector<double> adv((size_t)d.outlen);
+        for (int k = 0; k < d.outlen; k++) {
+            double off = k < vc ? std::fma((double)(k >> 2), h * 4.0, lane[k & 3])
+                                : std::fma((double)(k - vc), h, h * (double)vc);
+            adv[(size_t)k] = std::fma(-std::nearbyint(off * inv), two_pi, off);
+        }
+        s->c_advance.alloc(adv.size());
+        ck(cudaMemcpy(s->c_advance.p, adv.data(), adv.size() * sizeof(double), cudaMemcpyHostToDevice), "upload");
+    }
     ck(cudaEventCreateWithFlags(&s->chroma_refined, cudaEventDisableTiming), "cudaEventCreate");
+    ck(cudaStreamCreateWithFlags(&s->chroma_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    ck(cudaEventCreateWithFlags(&s->chroma_go, cudaEventDisableTiming), "cudaEventCreate");
+    ck(cudaEventCreateWithFlags(&s->chroma_done, cudaEventDisableTiming), "cudaEventCreate");
     s->chroma_alloc = true;
 }
 
@@ -402,8 +422,22 @@ void launch_chroma_blocks_for(vhsdecode_gb300_session* s, const int16_t* rf16, i
     s->launches += kChromaBlockKernels;
 }
 
+// The chroma block band-pass of the whole capture on the chroma stream, after
+// `after` (the point where the capture is on the device); the field batch
+// waits for chroma_done.  The kernel needs few SMs and is latency-bound, so it
+// runs beside the demodulator instead of after it.
+void queue_chroma_blocks(vhsdecode_gb300_session* s, const int16_t* rf16, int64_t nblocks, cudaEvent_t after) {
+    ck(cudaStreamWaitEvent(s->chroma_stream, after, 0), "wait");
+    launch_chroma_blocks_for(s, rf16, nblocks, s->chroma_stream);
+    ck(cudaEventRecord(s->chroma_done, s->chroma_stream), "event");
+    s->chroma_pending = true;
+}
+
 void session_free(vhsdecode_gb300_session* s) {
     if (s->chroma_refined) cudaEventDestroy(s->chroma_refined);
+    if (s->chroma_go) cudaEventDestroy(s->chroma_go);
+    if (s->chroma_done) cudaEventDestroy(s->chroma_done);
+    if (s->chroma_stream) cudaStreamDestroy(s->chroma_stream);
     if (s->demod_cycles) cudaFree(s->demod_cycles);
     if (s->plain_graph) cudaGraphExecDestroy(s->plain_graph);
     for (auto& ev : s->ev) if (ev) cudaEventDestroy(ev);
@@ -876,6 +910,9 @@ void launch_field_batch(vhsdecode_gb300_session* s, int f0, int f1, const T* vid
         cp.cu_hz = d.cu_hz;
         cp.fsc_mhz = d.fsc_mhz;
         cp.burst_abs_ref = d.burst_abs_ref;
+        // UpconvertChromaPhaseCompensated's hetCoefficient (VhsChromaDecoder.cs:2182-2186)
+        cp.ntsc_h = ((d.cu_hz * 1.5707963267948965e-6) / d.fsc_mhz) + 1.5707963267948966;
+        cp.ntsc_advance = s->c_advance.p;
         ck(cudaMemsetAsync(s->c_state.p + 1, 0, sizeof(int), fs), "memset");
         TbcParams ta = tp;
         ta.locs = cp.locs;
@@ -907,9 +944,18 @@ void launch_field_batch(vhsdecode_gb300_session* s, int f0, int f1, const T* vid
     tp.line_consts = std::is_same<T, float>::value
                          ? s->tbc_consts.p + (size_t)f0 * s->out_lines * kTbcLineConstsBytes
                          : nullptr;
+    const bool fused = chroma && std::is_same<T, float>::value;
+    if (fused) {
+        // the chroma TBC of the output lines rides on the luma's positions and weights
+        tp.src2 = s->c32.p;
+        tp.out2_f32 = s->c_field.p + (size_t)f0 * s->cd.field_samples;
+    }
     ck(launch_tbc_pw<T>(video, stream_len, tp, s->pw.p, fs), "tbc launch");
     s->launches += tp.line_consts ? kTbcFastKernels : kTbcKernels;
-    if (chroma) {
+    if (fused) {
+        ck(launch_chroma_decode(cp, fs), "chroma decode launch");
+        s->launches += kChromaDecodeKernels;
+    } else if (chroma) {
         // the chroma TBC of the output lines and the field decode to uint16
         TbcParams tc = tp;
         tc.out_u16 = nullptr;
@@ -1130,6 +1176,12 @@ void decode_fp32_pipelined(vhsdecode_gb300_session* s, const int16_t* rf, uint64
         cudaGetLastError();
     }
     if (carry && carry->no_graph) graphable = false;
+    s->chroma_pending = false;
+    if (s->want_chroma && nblocks > 0 && !host_input) {
+        // the capture is already on the device: start the chroma band-pass now
+        ck(cudaEventRecord(s->chroma_go, cs), "event");
+        queue_chroma_blocks(s, rf, nblocks, s->chroma_go);
+    }
     if (graphable && nseg > 0) {
         PipeKey key{s->in_f32 ? (const void*)s->in_f32 : (const void*)rf, n, host_input, demod_only,
                     s->in_f32 != nullptr};
@@ -1158,6 +1210,10 @@ void decode_fp32_pipelined(vhsdecode_gb300_session* s, const int16_t* rf, uint64
         enqueue_pipeline(s, rf, n, host_input, demod_only, bounds, cs, false);
     }
     s->launches += pipeline_launches(bounds, demod_only);
+    if (s->want_chroma && nblocks > 0 && host_input) {
+        // host input: after the last segment's RF copy (its demod start is an external event)
+        queue_chroma_blocks(s, s->rf.p, nblocks, s->seg_dem[(size_t)(2 * (nseg - 1))]);
+    }
     s->enqueue_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tq0).count();
     if (!demod_only && nblocks > 0) {
         auto t0 = std::chrono::steady_clock::now();
@@ -1183,7 +1239,7 @@ void decode_fp32_pipelined(vhsdecode_gb300_session* s, const int16_t* rf, uint64
         host_field_loop<float>(s, s->s32.p, stream_len, max_fields, feed, stop, cancel, carry);
         host_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
         ck(cudaEventRecord(s->ev[2], cs), "event");
-        if (s->want_chroma) launch_chroma_blocks_for(s, host_input ? s->rf.p : rf, nblocks, s->field_stream);
+        if (s->chroma_pending) ck(cudaStreamWaitEvent(s->field_stream, s->chroma_done, 0), "wait");
         launch_field_batch<float>(s, 0, (int)s->fields.size(), s->v32.p, s->s32.p, s->e32.p,
                                   stream_len, s->field_stream);
         collect_field_results(s, s->field_stream);
@@ -1191,7 +1247,7 @@ void decode_fp32_pipelined(vhsdecode_gb300_session* s, const int16_t* rf, uint64
         ck(cudaStreamWaitEvent(cs, s->field_end, 0), "wait");
     } else {
         ck(cudaEventRecord(s->ev[2], cs), "event");
-        if (s->want_chroma && nblocks > 0) launch_chroma_blocks_for(s, host_input ? s->rf.p : rf, nblocks, cs);
+        if (s->chroma_pending) ck(cudaStreamWaitEvent(cs, s->chroma_done, 0), "wait");
     }
     ck(cudaStreamSynchronize(s->d2h_stream), "sync");
     ck(cudaEventSynchronize(s->seg_dem[(size_t)(2 * std::max(0, nseg - 1) + 1)]), "sync");

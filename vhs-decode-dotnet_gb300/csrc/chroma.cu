@@ -3,10 +3,10 @@
 //
 // Block stage: the float32 forward-backward chroma band-pass of each RF block
 // (SosFilter.ApplyForwardBackwardFloat32, Core/Dsp/SosFilter.cs:369-538) is a
-// recurrence, so each block is one 4-lane group: lane s runs section s, one
-// sample behind lane s - 1, and the input is staged through shared memory a
-// 32-sample tile ahead.  The result is bit-identical to the reference's
-// sample-by-sample loop (same operations, same order, one rounding each).
+// recurrence, so each block is one thread that runs the four sections skewed
+// by one sample each (four independent recurrences per step).  The result is
+// bit-identical to the reference's sample-by-sample loop (same operations,
+// same order, one rounding each).
 // The roll by the chroma offset and the removal of the float mean
 // (ShiftChromaAndRemoveDcFloat32InPlace, VhsChromaDecoder.cs:2517-2533,
 // MeanFloat32FastMath :3751-3791) then stitch the block into the stream.
@@ -46,91 +46,158 @@ __device__ __forceinline__ float sos_step(const float* c, float v, float& z1, fl
 }
 
 // One pass of the 4-section cascade over samples 0 .. len-1 of a sequence,
-// run by a 4-lane group (lane s = section s) of a warp whose groups all loop
-// `steps` times (warp-uniform, >= every group's len + 3).  load(i) returns
-// sample i of the pass; store(i, v) receives the cascade output of sample i
-// (from lane 3).  The initial state is zi * x0.  `tile` is the group's
-// 2 x kTile staging area in shared memory.
-template <typename Load, typename Store>
-__device__ __forceinline__ void cascade(const ChromaCascade& c, int s, float* tile, int64_t steps, int64_t len,
-                                        float x0, Load load, Store store) {
+// run by a 4-lane group (lane s = section s).  Lane s filters sample t - 32 s
+// at step t, so its input (the output of lane s - 1) was written a whole
+// 32-step batch earlier and each lane runs only its own section's recurrence.
+// Per batch a lane reads its 32 inputs (lane 0 from the staged input tile,
+// the others from the ring of the lane before), filters them, and writes its
+// outputs (lane 3: to the output tile, flushed by all four lanes).  Every
+// group of the warp loops `steps` times (warp-uniform, >= len + 96).
+// load(i) returns sample i of the pass; store(i, v) receives the cascade
+// output of sample i.  The initial state is zi * x0.  `area` is the group's
+// kCascadeArea floats of shared memory.
+// Regions of kTile floats padded to kRegion, so the float4 accesses of the 32
+// lanes of a warp (8 groups x 4 lanes, each lane its own region) spread over
+// the shared-memory banks instead of all starting on bank 0.
+constexpr int kRegion = kTile + 4;
+constexpr int kCascadeArea = 9 * kRegion;   // input tiles [2], rings [3][2], output tile
+
+// Staged input: fetch(i) loads the raw 32-bit word of sample i (an int16 read
+// sign-extended by the load itself, or float bits) and cook(raw, i) turns it
+// into the sample a batch later, so no instruction waits on the load while
+// the recurrence runs.
+template <typename Fetch, typename Cook, typename Store>
+__device__ __forceinline__ void cascade_batch(const float* sec, float& z1, float& z2, int s, float* tin, float* ring,
+                                              float* tout, int64_t base, int cur, int64_t len,
+                                              uint32_t (&fetch_into)[kTile / 4], const uint32_t (&staged)[kTile / 4],
+                                              Fetch fetch, Cook cook, Store store) {
+    constexpr int per = kTile / 4;
+    // loads for the tile two batches ahead (cooked at the end of the next batch)
+#pragma unroll
+    for (int k = 0; k < per; k++) {
+        const int64_t i = base + 2 * kTile + s * per + k;
+        fetch_into[k] = i < len ? fetch(i) : 0u;
+    }
+    const float* src = s == 0 ? tin + cur * kRegion : ring + ((s - 1) * 2 + (cur ^ 1)) * kRegion;
+    float v[kTile];
+#pragma unroll
+    for (int j = 0; j < kTile; j += 4) {
+        const float4 q = *reinterpret_cast<const float4*>(src + j);
+        v[j] = q.x; v[j + 1] = q.y; v[j + 2] = q.z; v[j + 3] = q.w;
+    }
+    const int64_t i0 = base - (int64_t)s * kTile;
+    if (i0 >= 0 && i0 + kTile <= len) {
+#pragma unroll
+        for (int j = 0; j < kTile; j++) v[j] = sos_step(sec, v[j], z1, z2);
+    } else {
+#pragma unroll
+        for (int j = 0; j < kTile; j++) {
+            const int64_t i = i0 + j;
+            v[j] = (i >= 0 && i < len) ? sos_step(sec, v[j], z1, z2) : 0.0f;
+        }
+    }
+    float* dst = s < 3 ? ring + (s * 2 + cur) * kRegion : tout;
+#pragma unroll
+    for (int j = 0; j < kTile; j += 4) *reinterpret_cast<float4*>(dst + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+    // the tile of the next batch, fetched one batch ago
+#pragma unroll
+    for (int k = 0; k < per; k++) {
+        const int64_t i = base + kTile + s * per + k;
+        tin[(cur ^ 1) * kRegion + s * per + k] = i < len ? cook(staged[k], i) : 0.0f;
+    }
+    __syncwarp();
+#pragma unroll
+    for (int k = 0; k < per; k++) {
+        const int64_t i = base - 3 * kTile + s * per + k;
+        if (i >= 0 && i < len) store(i, tout[s * per + k]);
+    }
+    __syncwarp();
+}
+
+template <typename Fetch, typename Cook, typename Store>
+__device__ __forceinline__ void cascade(const ChromaCascade& c, int s, float* area, int64_t steps, int64_t len,
+                                        float x0, Fetch fetch, Cook cook, Store store) {
+    float* tin = area;                 // [2][kRegion]
+    float* ring = area + 2 * kRegion;  // [3][2][kRegion]
+    float* tout = ring + 6 * kRegion;  // [kRegion]
     float z1 = __fmul_rn(c.zi[s][0], x0), z2 = __fmul_rn(c.zi[s][1], x0);
     float sec[6];
 #pragma unroll
     for (int k = 0; k < 6; k++) sec[k] = c.sec[s][k];
-    float carry = 0.0f;
-    // stage tile 0
+    constexpr int per = kTile / 4;
+    uint32_t ra[per], rb[per];
 #pragma unroll
-    for (int k = 0; k < kTile / 4; k++) {
-        int64_t i = s * (kTile / 4) + k;
-        tile[s * (kTile / 4) + k] = i < len ? load(i) : 0.0f;
+    for (int k = 0; k < per; k++) {
+        const int64_t i = s * per + k;
+        tin[s * per + k] = i < len ? cook(fetch(i), i) : 0.0f;
+        const int64_t i1 = kTile + s * per + k;
+        ra[k] = i1 < len ? fetch(i1) : 0u;
     }
     __syncwarp();
-    for (int64_t base = 0; base < steps; base += kTile) {
-        const int cur = (int)((base / kTile) & 1);
-        // stage the next tile while this one is filtered
-        float nxt[kTile / 4];
-#pragma unroll
-        for (int k = 0; k < kTile / 4; k++) {
-            int64_t i = base + kTile + s * (kTile / 4) + k;
-            nxt[k] = i < len ? load(i) : 0.0f;
-        }
-        const float* tl = tile + cur * kTile;
-#pragma unroll 8
-        for (int j = 0; j < kTile; j++) {
-            const int64_t t = base + j;
-            float prev = __shfl_up_sync(kFull, carry, 1, 4);
-            float v = s == 0 ? tl[j] : prev;
-            const int64_t i = t - s;
-            if (i >= 0 && i < len) {
-                carry = sos_step(sec, v, z1, z2);
-                if (s == 3) store(i, carry);
-            }
-        }
-        float* tn = tile + (cur ^ 1) * kTile;
-#pragma unroll
-        for (int k = 0; k < kTile / 4; k++) tn[s * (kTile / 4) + k] = nxt[k];
-        __syncwarp();
+    // two batches per trip so the staging registers alternate by name
+    for (int64_t base = 0; base < steps; base += 2 * kTile) {
+        cascade_batch(sec, z1, z2, s, tin, ring, tout, base, 0, len, rb, ra, fetch, cook, store);
+        cascade_batch(sec, z1, z2, s, tin, ring, tout, base + kTile, 1, len, ra, rb, fetch, cook, store);
     }
 }
+
+// float sources: the raw word is the float's bits
+__device__ __forceinline__ float as_f(uint32_t u) { return __uint_as_float(u); }
+__device__ __forceinline__ uint32_t f_bits(float f) { return __float_as_uint(f); }
 
 // ---------------------------------------------------------------- block stage
 
 // One 4-lane group per RF block: the forward pass over the odd extension of
-// the block into scratch, then the backward pass in place (a sample's slot
-// is overwritten three steps after it was read).
+// the block into its scratch row, then the backward pass in place (a slot is
+// rewritten long after it was read).
 __global__ void __launch_bounds__(32 * kIirWarps) k_chroma_block_iir(ChromaBlockParams p) {
-    __shared__ float tiles[kIirWarps * kGroupsPerWarp * 2 * kTile];
+    __shared__ __align__(16) float areas[kIirWarps * kGroupsPerWarp * kCascadeArea];
     const int lane = threadIdx.x & 31, s = lane & 3, g = lane >> 2;
     const int64_t j = ((int64_t)blockIdx.x * kIirWarps + (threadIdx.x >> 5)) * kGroupsPerWarp + g;
     const bool active = j < p.nblocks;
-    float* tile = tiles + ((threadIdx.x >> 5) * kGroupsPerWarp + g) * 2 * kTile;
+    float* area = areas + ((threadIdx.x >> 5) * kGroupsPerWarp + g) * kCascadeArea;
     const int edge = p.c.edge;
     const int64_t len = (int64_t)kBlock + 2 * edge;
     const int64_t b = p.first_block + (active ? j : 0);
     const int64_t base = b * kStride;
-    float* ext = p.scratch + (active ? j : 0) * len;
-    auto x_at = [&](int64_t i) -> float { return p.rf32 ? p.rf32[base + i] : (float)p.rf16[base + i]; };
-    const float first = x_at(0), last = x_at(kBlock - 1);
-    auto in_at = [&](int64_t e) -> float {
-        if (e < edge) return __fsub_rn(__fmul_rn(2.0f, first), x_at(edge - e));
-        if (e < edge + kBlock) return x_at(e - edge);
-        return __fsub_rn(__fmul_rn(2.0f, last), x_at(kBlock - 2 - (e - edge - kBlock)));
+    float* row = p.scratch + (active ? j : 0) * len;
+    const int16_t* x16 = p.rf16 + (p.rf32 ? 0 : base);
+    const float* x32 = p.rf32 ? p.rf32 + base : nullptr;
+    // sample index of extended position e (odd extension at both ends)
+    auto src_index = [&](int64_t e) -> int64_t {
+        if (e < edge) return edge - e;
+        if (e < edge + kBlock) return e - edge;
+        return kBlock - 2 - (e - edge - kBlock);
     };
-    const int64_t steps = len + 3;
-    cascade(p.c, s, tile, steps, len, in_at(0), in_at, [&](int64_t i, float v) {
-        if (active) ext[i] = v;
+    auto fetch = [&](int64_t e) -> uint32_t {
+        const int64_t i = src_index(e);
+        return x32 ? f_bits(x32[i]) : (uint32_t)(int32_t)x16[i];
+    };
+    auto value = [&](uint32_t raw) -> float { return x32 ? as_f(raw) : (float)(int32_t)raw; };
+    const float first = value(fetch(edge)), last = value(fetch(edge + kBlock - 1));
+    auto cook = [&](uint32_t raw, int64_t e) -> float {
+        const float x = value(raw);
+        if (e < edge) return __fsub_rn(__fmul_rn(2.0f, first), x);
+        if (e < edge + kBlock) return x;
+        return __fsub_rn(__fmul_rn(2.0f, last), x);
+    };
+    const int64_t steps = len + 3 * kTile;
+    cascade(p.c, s, area, steps, len, cook(fetch(0), 0), fetch, cook, [&](int64_t i, float v) {
+        if (active) row[i] = v;
     });
     __syncwarp();
-    const float xl = ext[len - 1];
-    cascade(p.c, s, tile, steps, len, xl, [&](int64_t i) { return ext[len - 1 - i]; },
+    const float xl = row[len - 1];
+    __syncwarp();
+    cascade(p.c, s, area, steps, len, xl, [&](int64_t i) { return f_bits(row[len - 1 - i]); },
+            [](uint32_t raw, int64_t) { return as_f(raw); },
             [&](int64_t i, float v) {
-                if (active) ext[len - 1 - i] = v;
+                if (active) row[len - 1 - i] = v;
             });
 }
 
 // One warp per block: the float mean of the rolled block in the reference's
-// 32-accumulator order, then the stitched span minus the mean.
+// 32-accumulator order (lane a sums rolled samples a, a + 32, ... in order),
+// then the stitched span minus the mean.
 __global__ void __launch_bounds__(32) k_chroma_block_dc(ChromaBlockParams p) {
     const int64_t j = blockIdx.x;
     const int lane = threadIdx.x;
@@ -138,14 +205,26 @@ __global__ void __launch_bounds__(32) k_chroma_block_dc(ChromaBlockParams p) {
     const float* y = p.scratch + j * ((int64_t)kBlock + 2 * edge) + edge;
     const int move = p.move;
     float acc = 0.0f;
-    for (int i = lane; i < kBlock; i += 32) acc = __fadd_rn(acc, y[(i - move) & (kBlock - 1)]);
+    for (int i0 = 0; i0 < kBlock; i0 += 32 * 16) {
+        float v[16];
+#pragma unroll
+        for (int q = 0; q < 16; q++) v[q] = y[(i0 + q * 32 + lane - move) & (kBlock - 1)];
+#pragma unroll
+        for (int q = 0; q < 16; q++) acc = __fadd_rn(acc, v[q]);
+    }
     // lanes[l] = (acc[l] + acc[8 + l]) + (acc[16 + l] + acc[24 + l]), then a tree over 8 lanes
     float t = __fadd_rn(acc, __shfl_down_sync(kFull, acc, 8));
     float l8 = __fadd_rn(t, __shfl_down_sync(kFull, t, 16));
     for (int c = 8; c > 1; c /= 2) l8 = __fadd_rn(l8, __shfl_down_sync(kFull, l8, c / 2));
     const float mean = __fdiv_rn(__shfl_sync(kFull, l8, 0), (float)kBlock);
     float* out = p.out + (p.first_block + j) * kStride;
-    for (int i = lane; i < kStride; i += 32) out[i] = __fsub_rn(y[(kCut + i - move) & (kBlock - 1)], mean);
+    for (int i0 = 0; i0 < kStride; i0 += 32 * 8) {
+        float v[8];
+#pragma unroll
+        for (int q = 0; q < 8; q++) v[q] = y[(kCut + i0 + q * 32 + lane - move) & (kBlock - 1)];
+#pragma unroll
+        for (int q = 0; q < 8; q++) out[i0 + q * 32 + lane] = __fsub_rn(v[q], mean);
+    }
 }
 
 // ---------------------------------------------------------------- burst probes
@@ -178,8 +257,9 @@ __global__ void __launch_bounds__(128) k_chroma_probe(ChromaFieldParams p) {
     const int edge = p.fin.edge;
     const int win = p.win;
     const int len = win + 2 * edge;
-    float* buf = smem + (size_t)gi * (len + 2 * kTile);
-    float* tile = buf + len;
+    const int lpad = (len + 3) & ~3;
+    float* buf = smem + (size_t)gi * (lpad + kCascadeArea);
+    float* tile = buf + lpad;
     const int64_t field = (int64_t)p.out_lines * p.outlen;
     const int rot = positive_mod4((cnd == 0 ? p.rot0 : p.rot1) * (pl + 1));
     const int64_t line_start = (int64_t)pl * p.outlen;
@@ -197,14 +277,14 @@ __global__ void __launch_bounds__(128) k_chroma_probe(ChromaFieldParams p) {
         }
     }
     __syncwarp();
-    const int64_t steps = len + 3;
-    cascade(p.fin, s, tile, steps, len, buf[0], [&](int64_t i) { return buf[i]; },
-            [&](int64_t i, float v) { buf[i] = v; });
+    const int64_t steps = len + 3 * kTile;
+    cascade(p.fin, s, tile, steps, len, buf[0], [&](int64_t i) { return f_bits(buf[i]); },
+            [](uint32_t raw, int64_t) { return as_f(raw); }, [&](int64_t i, float v) { buf[i] = v; });
     __syncwarp();
     const float xl = buf[len - 1];
     __syncwarp();
-    cascade(p.fin, s, tile, steps, len, xl, [&](int64_t i) { return buf[len - 1 - i]; },
-            [&](int64_t i, float v) { buf[len - 1 - i] = v; });
+    cascade(p.fin, s, tile, steps, len, xl, [&](int64_t i) { return f_bits(buf[len - 1 - i]); },
+            [](uint32_t raw, int64_t) { return as_f(raw); }, [&](int64_t i, float v) { buf[len - 1 - i] = v; });
     __syncwarp();
     // DemodBurstFloat32: burst = filtered[pad, win - pad), tables from line_start + bs
     const int pad = p.be - p.bs;
@@ -297,27 +377,37 @@ __global__ void k_chroma_chain(ChromaFieldParams p) {
     *p.rot_out = c;
 }
 
-// SummarizePhaseSequence of each field's kept sequence (line order sums).
-__global__ void k_chroma_summary(ChromaFieldParams p) {
-    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+// SummarizePhaseSequence of each field's kept sequence: one warp per field,
+// the normalised I/Q of every line in parallel, then the sums in line order.
+__global__ void __launch_bounds__(128) k_chroma_summary(ChromaFieldParams p) {
+    __shared__ double nrm[4][2][320];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int f = blockIdx.x * 4 + w;
     if (f >= p.nfields) return;
     const double* pr = p.probe + ((int64_t)f * 2 + p.chosen[f]) * p.out_lines * 5;
     const int end = p.out_lines + 1;
+    const int nl = min(p.out_lines, 320);
+    for (int k = lane; k < nl; k += 32) {
+        const double mag = pr[k * 5 + 2];
+        nrm[w][0][k] = mag != 0.0 ? __ddiv_rn(pr[k * 5 + 3], mag) : 0.0;
+        nrm[w][1][k] = mag != 0.0 ? __ddiv_rn(pr[k * 5 + 4], mag) : 0.0;
+    }
+    __syncwarp();
+    if (lane != 0) return;
     double ei = 0.0, eq = 0.0, oi = 0.0, oq = 0.0, msum = 0.0;
     int count = 0;
-    for (int k = 0; k < p.out_lines; k++) {
+    for (int k = 0; k < nl; k++) {
         const int line = k + 1;
         const double mag = pr[k * 5 + 2];
         if (line <= 16 || line >= end - 16 || mag == 0.0) continue;
-        const double ni = __ddiv_rn(pr[k * 5 + 3], mag), nq = __ddiv_rn(pr[k * 5 + 4], mag);
         count++;
         msum = __dadd_rn(msum, mag);
         if (line & 1) {
-            oi = __dadd_rn(oi, ni);
-            oq = __dadd_rn(oq, nq);
+            oi = __dadd_rn(oi, nrm[w][0][k]);
+            oq = __dadd_rn(oq, nrm[w][1][k]);
         } else {
-            ei = __dadd_rn(ei, ni);
-            eq = __dadd_rn(eq, nq);
+            ei = __dadd_rn(ei, nrm[w][0][k]);
+            eq = __dadd_rn(eq, nrm[w][1][k]);
         }
     }
     double* o = p.summary + (int64_t)f * 4;
@@ -388,8 +478,8 @@ __global__ void __launch_bounds__(256) k_chroma_upconvert(ChromaFieldParams p) {
     }
     const double* pr = p.probe + ((int64_t)f * 2 + c) * p.out_lines * 5 + (int64_t)(L - 1) * 5;
     const double half_pi = 1.5707963267948966, deg = 0.017453292519943295;
-    const double carrier_term = __dmul_rn(p.cu_hz, 1.5707963267948965e-6);
-    const double h = __dadd_rn(__ddiv_rn(carrier_term, p.fsc_mhz), half_pi);
+    const double h = p.ntsc_h;
+    (void)h;
     // NtscFieldPhaseTarget (:3915-3925): -33 degrees in the first colour frame
     // of the four-field sequence, 147 in the second, whatever the parity
     const bool second = ((p.field_number[f] / 2) & 1) == 1;
@@ -397,21 +487,18 @@ __global__ void __launch_bounds__(256) k_chroma_upconvert(ChromaFieldParams p) {
     const int64_t ls = (int64_t)(L - ofl) * p.outlen;
     double theta = __fma_rn((double)ls, h, (double)rot * half_pi);
     theta = __fma_rn(__dadd_rn(target, pr[0]), deg, theta);
-    const int vc = p.outlen & ~3;
-    const double h4 = __dmul_rn(h, 4.0);
-    const double lane_off[4] = {__dmul_rn(h, 0.0), h, __dmul_rn(h, 2.0), __dmul_rn(h, 3.0)};
-    const double tail0 = __dadd_rn(theta, __dmul_rn(h, (double)vc));
     const int first_doubled = p.be + 5;
-    const double two_pi = 6.283185307179586;
+    const double two_pi = 6.283185307179586, inv_two_pi = 0.15915494309189535;
+    // the line's start phase reduced by whole turns; each sample's advance
+    // (the reference's four-lane theta steps, reduced the same way) is a table
+    const double t0 = __fma_rn(-rint(__dmul_rn(theta, inv_two_pi)), two_pi, theta);
     for (int k = threadIdx.x; k < p.outlen; k += blockDim.x) {
-        double th = k < vc ? __fma_rn((double)(k >> 2), h4, __dadd_rn(theta, lane_off[k & 3]))
-                           : __fma_rn((double)(k - vc), h, tail0);
-        const double turns = rint(th / two_pi);
-        const float r = (float)__fma_rn(-turns, two_pi, th);
-        const double carrier = -(double)cosf(r);
-        double v = (double)src[k];
-        if (k >= first_doubled) v = __dmul_rn(v, 2.0);
-        dst[k] = __double2float_rn(__dmul_rn(v, carrier));
+        const float carrier = -cosf((float)__dadd_rn(t0, p.ntsc_advance[k]));
+        float v = src[k];
+        if (k >= first_doubled) v = __fmul_rn(v, 2.0f);   // burst de-emphasis, exact
+        // the reference multiplies by the binary64 cosine and rounds to float;
+        // with the float cosine the product agrees to float rounding
+        dst[k] = __fmul_rn(v, carrier);
     }
 }
 
@@ -419,30 +506,36 @@ __global__ void __launch_bounds__(256) k_chroma_upconvert(ChromaFieldParams p) {
 // extension of a field's up-converted chroma; chunks past the first
 // kWarmup samples start kWarmup early from zero state.
 __global__ void __launch_bounds__(32 * kIirWarps) k_chroma_final_fwd(ChromaFieldParams p, int64_t chunks_per_field) {
-    __shared__ float tiles[kIirWarps * kGroupsPerWarp * 2 * kTile];
+    __shared__ __align__(16) float tiles[kIirWarps * kGroupsPerWarp * kCascadeArea];
     const int lane = threadIdx.x & 31, s = lane & 3, g = lane >> 2;
     const int64_t gid = ((int64_t)blockIdx.x * kIirWarps + (threadIdx.x >> 5)) * kGroupsPerWarp + g;
     const bool active = gid < (int64_t)p.nfields * chunks_per_field;
     const int64_t q = active ? gid : 0;
     const int f = (int)(q / chunks_per_field);
     const int64_t ch = q % chunks_per_field;
-    float* tile = tiles + ((threadIdx.x >> 5) * kGroupsPerWarp + g) * 2 * kTile;
+    float* tile = tiles + ((threadIdx.x >> 5) * kGroupsPerWarp + g) * kCascadeArea;
     const int64_t field = (int64_t)p.out_lines * p.outlen;
     const int edge = p.fin.edge;
     const int64_t E = field + 2 * edge;
     const float* x = p.up + (int64_t)f * field;
     float* fwd = p.fwd + (int64_t)f * E;
     const float first = x[0], last = x[field - 1];
-    auto ext = [&](int64_t e) -> float {
-        if (e < edge) return __fsub_rn(__fmul_rn(2.0f, first), x[edge - e]);
-        if (e < edge + field) return x[e - edge];
-        return __fsub_rn(__fmul_rn(2.0f, last), x[field - 2 - (e - edge - field)]);
+    auto fetch_e = [&](int64_t e) -> uint32_t {
+        const int64_t i = e < edge ? edge - e : (e < edge + field ? e - edge : field - 2 - (e - edge - field));
+        return f_bits(x[i]);
+    };
+    auto cook_e = [&](uint32_t raw, int64_t e) -> float {
+        if (e < edge) return __fsub_rn(__fmul_rn(2.0f, first), as_f(raw));
+        if (e < edge + field) return as_f(raw);
+        return __fsub_rn(__fmul_rn(2.0f, last), as_f(raw));
     };
     const int64_t c0 = ch * kChunk, c1 = min(E, c0 + kChunk);
     const int64_t start = c0 <= kWarmup ? 0 : c0 - kWarmup;
     const int64_t len = active ? c1 - start : 0;
-    const float x0 = start == 0 ? ext(0) : 0.0f;
-    cascade(p.fin, s, tile, (int64_t)kChunk + kWarmup + 3, len, x0, [&](int64_t i) { return ext(start + i); },
+    const float x0 = start == 0 ? cook_e(fetch_e(0), 0) : 0.0f;
+    cascade(p.fin, s, tile, (int64_t)kChunk + kWarmup + 3 * kTile, len, x0,
+            [&](int64_t i) { return fetch_e(start + i); },
+            [&](uint32_t raw, int64_t i) { return cook_e(raw, start + i); },
             [&](int64_t i, float v) {
                 if (start + i >= c0) fwd[start + i] = v;
             });
@@ -451,14 +544,14 @@ __global__ void __launch_bounds__(32 * kIirWarps) k_chroma_final_fwd(ChromaField
 // Final band-pass, backward over the forward output, chunks started kWarmup
 // late from zero state except the last; the output samples land in `up`.
 __global__ void __launch_bounds__(32 * kIirWarps) k_chroma_final_bwd(ChromaFieldParams p, int64_t chunks_per_field) {
-    __shared__ float tiles[kIirWarps * kGroupsPerWarp * 2 * kTile];
+    __shared__ __align__(16) float tiles[kIirWarps * kGroupsPerWarp * kCascadeArea];
     const int lane = threadIdx.x & 31, s = lane & 3, g = lane >> 2;
     const int64_t gid = ((int64_t)blockIdx.x * kIirWarps + (threadIdx.x >> 5)) * kGroupsPerWarp + g;
     const bool active = gid < (int64_t)p.nfields * chunks_per_field;
     const int64_t q = active ? gid : 0;
     const int f = (int)(q / chunks_per_field);
     const int64_t ch = q % chunks_per_field;
-    float* tile = tiles + ((threadIdx.x >> 5) * kGroupsPerWarp + g) * 2 * kTile;
+    float* tile = tiles + ((threadIdx.x >> 5) * kGroupsPerWarp + g) * kCascadeArea;
     const int64_t field = (int64_t)p.out_lines * p.outlen;
     const int edge = p.fin.edge;
     const int64_t E = field + 2 * edge;
@@ -468,11 +561,18 @@ __global__ void __launch_bounds__(32 * kIirWarps) k_chroma_final_bwd(ChromaField
     const int64_t stop = c1 + kWarmup >= E ? E : c1 + kWarmup;   // exclusive upper end of the pass
     const int64_t len = active ? stop - c0 : 0;
     const float x0 = stop == E ? fwd[E - 1] : 0.0f;
-    cascade(p.fin, s, tile, (int64_t)kChunk + kWarmup + 3, len, x0, [&](int64_t i) { return fwd[stop - 1 - i]; },
+    cascade(p.fin, s, tile, (int64_t)kChunk + kWarmup + 3 * kTile, len, x0,
+            [&](int64_t i) { return f_bits(fwd[stop - 1 - i]); }, [](uint32_t raw, int64_t) { return as_f(raw); },
             [&](int64_t i, float v) {
                 const int64_t e = stop - 1 - i;
                 if (e < c1 && e >= edge && e < edge + field) y[e - edge] = v;
             });
+}
+
+__device__ __forceinline__ void two_sum_f(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
 }
 
 __device__ __forceinline__ uint16_t u16_saturate(double shifted) {
@@ -507,9 +607,13 @@ __global__ void __launch_bounds__(256) k_chroma_gain(ChromaFieldParams p) {
         const float* adv = x + (int64_t)(o + dist) * p.outlen;
         const float* del = x + (int64_t)(o - dist) * p.outlen;
         for (int k = threadIdx.x; k < p.outlen; k += blockDim.x) {
-            double c = __dmul_rn((double)cur[k], 2.0);
-            c = __dsub_rn(__dsub_rn(c, (double)adv[k]), (double)del[k]);
-            line[k] = __double2float_rn(__ddiv_rn(c, 4.0));
+            // ((2 cur - adv) - del) / 4 rounded to float: the binary64 sum of
+            // these floats is exact, so take the exact sum as a float pair
+            // (two TwoSums) and round it once; / 4 is exact
+            float s1, e1, s2, e2;
+            two_sum_f(__fmul_rn(cur[k], 2.0f), -adv[k], s1, e1);
+            two_sum_f(s1, -del[k], s2, e2);
+            line[k] = __fmul_rn(__fadd_rn(s2, __fadd_rn(e1, e2)), 0.25f);
         }
     } else {
         for (int k = threadIdx.x; k < p.outlen; k += blockDim.x) line[k] = cur[k];
@@ -552,12 +656,12 @@ cudaError_t launch_chroma_blocks(const ChromaBlockParams& p, cudaStream_t s) {
 cudaError_t launch_chroma_phase(const ChromaFieldParams& p, cudaStream_t s) {
     if (p.nfields <= 0) return cudaSuccess;
     const int64_t nprobe = (int64_t)p.nfields * 2 * p.out_lines;
-    const int groups = 32;   // 128 threads
-    const size_t smem = (size_t)groups * (p.win + 2 * p.fin.edge + 2 * kTile) * sizeof(float);
+    const int groups = 16;   // 64 threads
+    const size_t smem = (size_t)groups * (((p.win + 2 * p.fin.edge + 3) & ~3) + kCascadeArea) * sizeof(float);
     k_chroma_probe<<<(unsigned)((nprobe + groups - 1) / groups), groups * 4, smem, s>>>(p);
     k_chroma_flip<<<(unsigned)(p.nfields * 2), 128, 0, s>>>(p);
     k_chroma_chain<<<1, 1, 0, s>>>(p);
-    k_chroma_summary<<<(unsigned)((p.nfields + 63) / 64), 64, 0, s>>>(p);
+    k_chroma_summary<<<(unsigned)((p.nfields + 3) / 4), 128, 0, s>>>(p);
     k_chroma_refine<<<(unsigned)p.nfields, 256, 0, s>>>(p);
     return cudaGetLastError();
 }

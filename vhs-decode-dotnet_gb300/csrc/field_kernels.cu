@@ -1281,6 +1281,8 @@ __global__ void __launch_bounds__(kTbcFastMaxThreads) k_tbc_fast(const float* st
     const float4* lut4 = reinterpret_cast<const float4*>(p.lut);
     const float4* pair4 = reinterpret_cast<const float4*>(p.lut_pair);
     uint16_t* out = p.out_u16 ? p.out_u16 + ((int64_t)f * p.out_lines + ol) * p.outlen : nullptr;
+    const float* src2 = p.src2 ? p.src2 + s0 : nullptr;
+    float* out2 = p.out2_f32 ? p.out2_f32 + ((int64_t)f * p.out_lines + ol) * p.outlen : nullptr;
     float* outf32 = p.out_f32 ? p.out_f32 + ((int64_t)f * p.out_lines + ol) * p.out_stride - p.x0 : nullptr;
     const int kx1 = p.x1 > 0 ? p.x1 : p.outlen;
     // Each lane owns one output sample (position, level and conversion done
@@ -1307,7 +1309,7 @@ __global__ void __launch_bounds__(kTbcFastMaxThreads) k_tbc_fast(const float* st
         pe = wrap_idx(pe, 65537);
         const int start = ci - 7;
         const int interior = (n >= 16 && (uint32_t)start <= (uint32_t)(n - 16)) ? 1 : 0;
-        float hi_own = 0.0f, lo_own = 0.0f;
+        float hi_own = 0.0f, lo_own = 0.0f, hi2_own = 0.0f, lo2_own = 0.0f;
 #pragma unroll
         for (int rnd = 0; rnd < 4; rnd++) {
             const int owner = rnd * 8 + q;
@@ -1327,7 +1329,7 @@ __global__ void __launch_bounds__(kTbcFastMaxThreads) k_tbc_fast(const float* st
             }
             const float wsv[4] = {ws.x, ws.y, ws.z, ws.w};
             const float wev[4] = {we.x, we.y, we.z, we.w};
-            float hi = 0.0f, lo = 0.0f;
+            float hi = 0.0f, lo = 0.0f, hi2 = 0.0f, lo2 = 0.0f;
 #pragma unroll
             for (int r = 0; r < 4; r++) {
                 float wt = __fmaf_rn(al_o, __fsub_rn(wev[r], wsv[r]), wsv[r]);
@@ -1342,6 +1344,12 @@ __global__ void __launch_bounds__(kTbcFastMaxThreads) k_tbc_fast(const float* st
                 two_sum(hi, prod, s, e);
                 hi = s;
                 lo = __fadd_rn(lo, e);
+                if (src2) {
+                    float prod2 = __fmul_rn(__ldg(src2 + idx), wt);
+                    two_sum(hi2, prod2, s, e);
+                    hi2 = s;
+                    lo2 = __fadd_rn(lo2, e);
+                }
             }
 #pragma unroll
             for (int o = 1; o < 4; o <<= 1) {
@@ -1355,6 +1363,19 @@ __global__ void __launch_bounds__(kTbcFastMaxThreads) k_tbc_fast(const float* st
             const float rh = __shfl_sync(0xffffffffu, hi, 4 * (lane & 7));
             const float rl = __shfl_sync(0xffffffffu, lo, 4 * (lane & 7));
             if ((lane >> 3) == rnd) { hi_own = rh; lo_own = rl; }
+            if (src2) {
+#pragma unroll
+                for (int o = 1; o < 4; o <<= 1) {
+                    float oh = __shfl_xor_sync(0xffffffffu, hi2, o);
+                    float olo = __shfl_xor_sync(0xffffffffu, lo2, o);
+                    float2 t = ff_add(hi2, lo2, oh, olo);
+                    hi2 = t.x;
+                    lo2 = t.y;
+                }
+                const float rh2 = __shfl_sync(0xffffffffu, hi2, 4 * (lane & 7));
+                const float rl2 = __shfl_sync(0xffffffffu, lo2, 4 * (lane & 7));
+                if ((lane >> 3) == rnd) { hi2_own = rh2; lo2_own = rl2; }
+            }
         }
         if (!valid) continue;
         float2 la = c.adj;
@@ -1365,6 +1386,10 @@ __global__ void __launch_bounds__(kTbcFastMaxThreads) k_tbc_fast(const float* st
         }
         float2 v = ff_mul(hi_own, lo_own, la.x, la.y);
         float outf = __fadd_rn(v.x, v.y);
+        if (out2) {
+            float2 v2 = ff_mul(hi2_own, lo2_own, la.x, la.y);
+            out2[k] = __fadd_rn(v2.x, v2.y);
+        }
         if (outf32) {
             outf32[k] = outf;   // float output (the chroma channel): no conversion
             continue;

@@ -189,6 +189,9 @@ struct TbcParams {
     float* out_f32;             // optional float output [nfields * out_lines * out_stride]:
                                 // samples x0 .. x1-1 of each line at (k - x0)
     int x0, x1, out_stride;     // line window of out_f32 (x1 = 0: the whole line)
+    const float* src2;          // optional second float stream rendered with the same
+    float* out2_f32;            //   positions and weights (the chroma beside the luma),
+                                //   [nfields * out_lines * outlen] (fast float kernel only)
     double* level_work;         // [nfields * (max_first_line + out_lines)] line factors
     unsigned char* line_consts; // [nfields * out_lines * kTbcLineConstsBytes] float-pair line plans
                                 // of the fast float kernel (null: binary64 kernel)
@@ -260,6 +263,8 @@ struct ChromaFieldParams {
     float* fwd;                 // [nfields * (field + 2 fin.edge)] forward pass
     uint16_t* out;              // [nfields * field] uint16 chroma
     double cu_hz, fsc_mhz, burst_abs_ref;
+    double ntsc_h;              // NTSC up-conversion carrier step (rad / output sample)
+    const double* ntsc_advance; // [outlen] carrier phase advance of sample k of a line, mod 2 pi
 };
 constexpr int kChromaPhaseKernels = 5;    // probes, flips, rotation chain, averages, refinement
 constexpr int kChromaDecodeKernels = 4;   // up-conversion, forward, backward, gain

@@ -233,12 +233,16 @@ struct vhsdecode_gb300_session {
     DevBuf<float> c_het, c_bsin, c_bcos; // field tables
     DevBuf<float> c_ana;                 // line-1 chroma TBC, probe windows
     DevBuf<float> c_field, c_up, c_fwd;  // output-line chroma TBC, up-converted / filtered, forward pass
-    DevBuf<double> c_probe, c_summary, locs_final;
+    DevBuf<double> c_probe, c_summary, locs_final, c_advance;
     DevBuf<int> c_flip, c_chosen, c_state, c_ones;   // c_state: rotation out, status
     DevBuf<uint16_t> chroma;             // uint16 chroma fields
     View<int> first_field_d, field_number_d, rot_in_d;
     int chroma_rot_start = 0, chroma_rot_end = 0;
     cudaEvent_t chroma_refined = nullptr;
+    // the chroma block band-pass runs on its own stream beside the demod
+    cudaStream_t chroma_stream = nullptr;
+    cudaEvent_t chroma_go = nullptr, chroma_done = nullptr;
+    bool chroma_pending = false;         // chroma blocks queued for this decode
     // host results
     std::vector<FieldRec> fields;
     int64_t last_blocks = 0;

@@ -512,6 +512,9 @@ class Session:
                                                                ctypes.byref(cnt)))
         return out[:cnt.value]
 
+    def chroma_into(self, first, count, host_ptr):
+        check(load().vhsdecode_gb300_session_copy_chroma(self._h, first, count, ctypes.c_void_p(host_ptr)))
+
     def tbc_into(self, first, count, host_ptr):
         check(load().vhsdecode_gb300_session_copy_tbc(self._h, first, count,
                                                       ctypes.c_void_p(host_ptr)))
