@@ -352,12 +352,14 @@ void ensure_chroma(vhsdecode_gb300_session* s) {
     s->cd = vhsd::design_chroma(s->fmt, s->fs);
     const vhsd::ChromaDesign& d = s->cd;
     if (2 * d.burst_start - d.burst_end < 0 || d.burst_start + d.burst_end > d.outlen ||
-        d.rf.edge >= kBlock || d.out_lines != s->out_lines || d.outlen != s->outlen)
+        d.out_lines != s->out_lines || d.outlen != s->outlen)
         throw Failure(VHSDECODE_GB300_STATUS_INTERNAL_ERROR, "chroma burst window does not fit the line");
+    if (d.rf.edge != kChromaEdge)
+        throw Failure(VHSDECODE_GB300_STATUS_INTERNAL_ERROR, "chroma band-pass pad length is not the block stage's");
     const size_t mf = (size_t)s->max_fields, field = (size_t)d.field_samples;
     const size_t win = (size_t)(2 * d.burst_end - d.burst_start);
     s->c32.alloc((size_t)std::max<int64_t>(1, s->max_blocks) * kStride);
-    s->c_scratch.alloc((size_t)std::max<int64_t>(1, s->max_blocks) * (kBlock + 2 * d.rf.edge));
+    s->c_scratch.alloc((size_t)std::max<int64_t>(1, s->max_blocks) * kChromaRowStride);
     std::vector<float> het, bsin, bcos;
     vhsd::chroma_tables(d, het, bsin, bcos);
     s->c_het.alloc(het.size());

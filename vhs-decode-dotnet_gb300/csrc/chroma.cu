@@ -3,10 +3,10 @@
 //
 // Block stage: the float32 forward-backward chroma band-pass of each RF block
 // (SosFilter.ApplyForwardBackwardFloat32, Core/Dsp/SosFilter.cs:369-538) is a
-// recurrence, so each block is one thread that runs the four sections skewed
-// by one sample each (four independent recurrences per step).  The result is
-// bit-identical to the reference's sample-by-sample loop (same operations,
-// same order, one rounding each).
+// recurrence, so each block is a group of four lanes, lane s running section s
+// a 32-sample batch behind lane s - 1 (four independent recurrences per step).
+// The result is bit-identical to the reference's sample-by-sample loop (same
+// operations, same order, one rounding each).
 // The roll by the chroma offset and the removal of the float mean
 // (ShiftChromaAndRemoveDcFloat32InPlace, VhsChromaDecoder.cs:2517-2533,
 // MeanFloat32FastMath :3751-3791) then stitch the block into the stream.
@@ -147,52 +147,185 @@ __device__ __forceinline__ uint32_t f_bits(float f) { return __float_as_uint(f);
 
 // ---------------------------------------------------------------- block stage
 
+// The block stage runs the same section-per-lane cascade as cascade() above,
+// with its input fed from a ring of 32-sample chunks that cp.async fills
+// kRingDepth - 2 batches ahead (the latency of a global load is longer than
+// a batch of the recurrence), the lane-to-lane hand-over in registers
+// (shuffled as each output is made, consumed a batch later) and 16-byte stores
+// of the last section's outputs.
+constexpr int kExtBatches = kChromaExt / 32 + (kChromaExt % 32 != 0);
+constexpr int kRingDepth = 8;                       // chunks in flight per block
+constexpr int kRingSlot = 128;                      // bytes: 32 floats or 32 int16
+constexpr int kRingBytes = kRingDepth * kRingSlot + 16;   // + 16: blocks start on different banks
+constexpr int kBlockGroups = 32;                    // blocks per CTA (4 warps of 8 groups)
+static_assert(kChromaRowStride == kExtBatches * 32, "scratch rows hold whole chunks");
+
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// Forward input at extended position e near the ends of the block (odd
+// extension: 2 x[0] - x[edge - e] before it, 2 x[last] - x[...] after it),
+// read from the ring (chunk q holds source samples [32 (q - 1), 32 q)).
+template <typename T>
+__device__ __noinline__ float block_edge_input(const uint8_t* ring, int e, float first, float last) {
+    if (e >= kChromaExt) return 0.0f;
+    const bool lo = e < kChromaEdge, hi = e >= kChromaEdge + kBlock;
+    const int i = lo ? kChromaEdge - e : hi ? kBlock - 2 - (e - kChromaEdge - kBlock) : e - kChromaEdge;
+    const float x = (float)reinterpret_cast<const T*>(ring + (((i >> 5) + 1) % kRingDepth) * kRingSlot)[i & 31];
+    return lo ? __fsub_rn(__fmul_rn(2.0f, first), x) : hi ? __fsub_rn(__fmul_rn(2.0f, last), x) : x;
+}
+
+// One pass of the block's 4-section cascade by its 4-lane group: lane s runs
+// section s on batch k - s.  kMode 0: forward over the int16 block, 1: forward
+// over the float block, 2: backward over the forward output in the row.
+// The forward pass writes sample e at row[e]; the backward pass reads row[r]
+// for sample kChromaExt - 1 - r and writes its output at row[r + kChromaRowShift]
+// (every source position is in the ring long before a later sample's output
+// lands on it).
+template <int kMode>
+__device__ __forceinline__ void block_pass(const float (&sec)[6], float zi0, float zi1, int s, bool active,
+                                           const void* src, float* row, uint8_t* ring, float first, float last) {
+    const uint32_t ring_s = (uint32_t)__cvta_generic_to_shared(ring);
+    const float x0 = kMode == 2 ? row[kChromaExt - 1]
+                                : __fsub_rn(__fmul_rn(2.0f, first),
+                                            kMode == 0 ? (float)static_cast<const int16_t*>(src)[kChromaEdge]
+                                                       : static_cast<const float*>(src)[kChromaEdge]);
+    float z1 = __fmul_rn(zi0, x0), z2 = __fmul_rn(zi1, x0);
+    // chunk q into slot q % depth: forward q = 1 .. kBlock/32 (source [32 (q-1), 32 q)),
+    // backward q = 0 .. kExtBatches-1 (row floats [32 m, 32 m + 32), m = kExtBatches - 1 - q)
+    auto issue = [&](int q) {
+        if (active) {
+            const uint32_t slot = ring_s + (q % kRingDepth) * kRingSlot;
+            if (kMode == 0) {
+                if (q >= 1 && q <= kBlock / 32)
+                    cp_async16(slot + 16 * s, static_cast<const int16_t*>(src) + 32 * (q - 1) + 8 * s);
+            } else if (kMode == 1) {
+                if (q >= 1 && q <= kBlock / 32) {
+                    const float* f = static_cast<const float*>(src) + 32 * (q - 1) + 4 * s;
+                    cp_async16(slot + 16 * s, f);
+                    cp_async16(slot + 64 + 16 * s, f + 16);
+                }
+            } else if (q >= 0 && q < kExtBatches) {
+                const float* f = row + 32 * (kExtBatches - 1 - q) + 4 * s;
+                cp_async16(slot + 16 * s, f);
+                cp_async16(slot + 64 + 16 * s, f + 16);
+            }
+        }
+        cp_async_commit();
+    };
+#pragma unroll
+    for (int q = 0; q < kRingDepth - 1; q++) issue(q);
+    float a[32], b[32];
+#pragma unroll
+    for (int q = 0; q < 32; q++) a[q] = b[q] = 0.0f;
+    // batch k: chunks k and k + 1 are complete (the ones after them in flight)
+    auto batch = [&](int k, float (&cur)[32], float (&nxt)[32]) {
+        cp_async_wait<kRingDepth - 3>();
+        __syncwarp();
+        issue(k + kRingDepth - 1);   // into the slot of chunk k - 1, read last batch
+        if (s == 0 && k < kExtBatches) {
+            const uint8_t* r0 = ring + (k % kRingDepth) * kRingSlot;
+            const uint8_t* r1 = ring + ((k + 1) % kRingDepth) * kRingSlot;
+            if (kMode == 2) {
+                constexpr int top = (kChromaExt - 1) % 32;
+                const float* f0 = reinterpret_cast<const float*>(r0);
+                const float* f1 = reinterpret_cast<const float*>(r1);
+#pragma unroll
+                for (int q = 0; q < 32; q++) cur[q] = q <= top ? f0[top - q] : f1[top + 32 - q];
+            } else if (k >= 1 && k < kBlock / 32) {
+                constexpr int lead = 32 - kChromaEdge;
+                if (kMode == 0) {
+                    const int16_t* h0 = reinterpret_cast<const int16_t*>(r0);
+                    const int16_t* h1 = reinterpret_cast<const int16_t*>(r1);
+#pragma unroll
+                    for (int q = 0; q < 32; q++) cur[q] = (float)(q < kChromaEdge ? h0[q + lead] : h1[q - kChromaEdge]);
+                } else {
+                    const float* f0 = reinterpret_cast<const float*>(r0);
+                    const float* f1 = reinterpret_cast<const float*>(r1);
+#pragma unroll
+                    for (int q = 0; q < 32; q++) cur[q] = q < kChromaEdge ? f0[q + lead] : f1[q - kChromaEdge];
+                }
+            } else {
+#pragma unroll
+                for (int q = 0; q < 32; q++)
+                    cur[q] = kMode == 0 ? block_edge_input<int16_t>(ring, 32 * k + q, first, last)
+                                        : block_edge_input<float>(ring, 32 * k + q, first, last);
+            }
+        }
+        const int i0 = 32 * (k - s);
+        if (i0 >= 0 && i0 + 32 <= kChromaExt) {
+#pragma unroll
+            for (int q = 0; q < 32; q++) {
+                cur[q] = sos_step(sec, cur[q], z1, z2);
+                nxt[q] = __shfl_up_sync(kFull, cur[q], 1, 4);
+            }
+        } else {
+#pragma unroll
+            for (int q = 0; q < 32; q++) {
+                const int i = i0 + q;
+                cur[q] = (i >= 0 && i < kChromaExt) ? sos_step(sec, cur[q], z1, z2) : 0.0f;
+                nxt[q] = __shfl_up_sync(kFull, cur[q], 1, 4);
+            }
+        }
+        const int kk = k - 3;   // the last section's batch
+        if (s == 3 && active && kk >= 0 && kk < kExtBatches) {
+            if (kMode != 2) {
+#pragma unroll
+                for (int u = 0; u < 8; u++)
+                    *reinterpret_cast<float4*>(row + 32 * kk + 4 * u) =
+                        make_float4(cur[4 * u], cur[4 * u + 1], cur[4 * u + 2], cur[4 * u + 3]);
+            } else {
+                const int base = kChromaExt + kChromaRowShift - 32 - 32 * kk;   // a multiple of 4
+#pragma unroll
+                for (int u = 0; u < 8; u++)
+                    if (base + 4 * u >= 0)
+                        *reinterpret_cast<float4*>(row + base + 4 * u) =
+                            make_float4(cur[31 - 4 * u], cur[30 - 4 * u], cur[29 - 4 * u], cur[28 - 4 * u]);
+            }
+        }
+    };
+    constexpr int nb = kExtBatches + 3;
+    for (int k = 0; k < nb; k += 2) {
+        batch(k, a, b);
+        batch(k + 1, b, a);
+    }
+    cp_async_wait_all();
+}
+
 // One 4-lane group per RF block: the forward pass over the odd extension of
-// the block into its scratch row, then the backward pass in place (a slot is
-// rewritten long after it was read).
-__global__ void __launch_bounds__(32 * kIirWarps) k_chroma_block_iir(ChromaBlockParams p) {
-    __shared__ __align__(16) float areas[kIirWarps * kGroupsPerWarp * kCascadeArea];
-    const int lane = threadIdx.x & 31, s = lane & 3, g = lane >> 2;
-    const int64_t j = ((int64_t)blockIdx.x * kIirWarps + (threadIdx.x >> 5)) * kGroupsPerWarp + g;
+// the block into its scratch row, then the backward pass in place.
+__global__ void __launch_bounds__(4 * kBlockGroups) k_chroma_block_iir(ChromaBlockParams p) {
+    __shared__ __align__(128) uint8_t rings[kBlockGroups * kRingBytes];
+    const int s = threadIdx.x & 3, g = threadIdx.x >> 2;
+    const int64_t j = (int64_t)blockIdx.x * kBlockGroups + g;
     const bool active = j < p.nblocks;
-    float* area = areas + ((threadIdx.x >> 5) * kGroupsPerWarp + g) * kCascadeArea;
-    const int edge = p.c.edge;
-    const int64_t len = (int64_t)kBlock + 2 * edge;
-    const int64_t b = p.first_block + (active ? j : 0);
-    const int64_t base = b * kStride;
-    float* row = p.scratch + (active ? j : 0) * len;
-    const int16_t* x16 = p.rf16 + (p.rf32 ? 0 : base);
-    const float* x32 = p.rf32 ? p.rf32 + base : nullptr;
-    // sample index of extended position e (odd extension at both ends)
-    auto src_index = [&](int64_t e) -> int64_t {
-        if (e < edge) return edge - e;
-        if (e < edge + kBlock) return e - edge;
-        return kBlock - 2 - (e - edge - kBlock);
-    };
-    auto fetch = [&](int64_t e) -> uint32_t {
-        const int64_t i = src_index(e);
-        return x32 ? f_bits(x32[i]) : (uint32_t)(int32_t)x16[i];
-    };
-    auto value = [&](uint32_t raw) -> float { return x32 ? as_f(raw) : (float)(int32_t)raw; };
-    const float first = value(fetch(edge)), last = value(fetch(edge + kBlock - 1));
-    auto cook = [&](uint32_t raw, int64_t e) -> float {
-        const float x = value(raw);
-        if (e < edge) return __fsub_rn(__fmul_rn(2.0f, first), x);
-        if (e < edge + kBlock) return x;
-        return __fsub_rn(__fmul_rn(2.0f, last), x);
-    };
-    const int64_t steps = len + 3 * kTile;
-    cascade(p.c, s, area, steps, len, cook(fetch(0), 0), fetch, cook, [&](int64_t i, float v) {
-        if (active) row[i] = v;
-    });
+    const int64_t base = (p.first_block + (active ? j : 0)) * kStride;
+    float* row = p.scratch + (active ? j : 0) * kChromaRowStride;
+    uint8_t* ring = rings + g * kRingBytes;
+    // section s of the cascade (selected with constant indices: a dynamic
+    // index into the parameter block would copy it to local memory)
+    float sec[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++)
+        sec[k] = s == 0 ? p.c.sec[0][k] : s == 1 ? p.c.sec[1][k] : s == 2 ? p.c.sec[2][k] : p.c.sec[3][k];
+    const float zi0 = s == 0 ? p.c.zi[0][0] : s == 1 ? p.c.zi[1][0] : s == 2 ? p.c.zi[2][0] : p.c.zi[3][0];
+    const float zi1 = s == 0 ? p.c.zi[0][1] : s == 1 ? p.c.zi[1][1] : s == 2 ? p.c.zi[2][1] : p.c.zi[3][1];
+    if (p.rf32) {
+        const float* x = p.rf32 + base;
+        block_pass<1>(sec, zi0, zi1, s, active, x, row, ring, x[0], x[kBlock - 1]);
+    } else {
+        const int16_t* x = p.rf16 + base;
+        block_pass<0>(sec, zi0, zi1, s, active, x, row, ring, (float)x[0], (float)x[kBlock - 1]);
+    }
+    // the forward outputs of lane 3 before the other lanes' copies of them
+    __threadfence();
     __syncwarp();
-    const float xl = row[len - 1];
-    __syncwarp();
-    cascade(p.c, s, area, steps, len, xl, [&](int64_t i) { return f_bits(row[len - 1 - i]); },
-            [](uint32_t raw, int64_t) { return as_f(raw); },
-            [&](int64_t i, float v) {
-                if (active) row[len - 1 - i] = v;
-            });
+    block_pass<2>(sec, zi0, zi1, s, active, nullptr, row, ring, 0.0f, 0.0f);
 }
 
 // One warp per block: the float mean of the rolled block in the reference's
@@ -201,8 +334,7 @@ __global__ void __launch_bounds__(32 * kIirWarps) k_chroma_block_iir(ChromaBlock
 __global__ void __launch_bounds__(32) k_chroma_block_dc(ChromaBlockParams p) {
     const int64_t j = blockIdx.x;
     const int lane = threadIdx.x;
-    const int edge = p.c.edge;
-    const float* y = p.scratch + j * ((int64_t)kBlock + 2 * edge) + edge;
+    const float* y = p.scratch + j * (int64_t)kChromaRowStride + kChromaEdge + kChromaRowShift;
     const int move = p.move;
     float acc = 0.0f;
     for (int i0 = 0; i0 < kBlock; i0 += 32 * 16) {
@@ -647,8 +779,11 @@ __global__ void __launch_bounds__(256) k_chroma_gain(ChromaFieldParams p) {
 
 cudaError_t launch_chroma_blocks(const ChromaBlockParams& p, cudaStream_t s) {
     if (p.nblocks <= 0) return cudaSuccess;
-    const int64_t per_cta = (int64_t)kIirWarps * kGroupsPerWarp;
-    k_chroma_block_iir<<<(unsigned)((p.nblocks + per_cta - 1) / per_cta), 32 * kIirWarps, 0, s>>>(p);
+    if (p.c.edge != kChromaEdge || (!p.rf32 && !p.rf16) ||
+        (reinterpret_cast<uintptr_t>(p.rf32 ? (const void*)p.rf32 : (const void*)p.rf16) & 15u) != 0 ||
+        (reinterpret_cast<uintptr_t>(p.scratch) & 15u) != 0)
+        return cudaErrorInvalidValue;
+    k_chroma_block_iir<<<(unsigned)((p.nblocks + kBlockGroups - 1) / kBlockGroups), 4 * kBlockGroups, 0, s>>>(p);
     k_chroma_block_dc<<<(unsigned)p.nblocks, 32, 0, s>>>(p);
     return cudaGetLastError();
 }

@@ -214,16 +214,27 @@ struct ChromaCascade {
     int edge;
 };
 
+// The odd extension of an RF block before its chroma band-pass: the default
+// pad length of a 4-section filter with no zero end coefficients,
+// 3 * (2 * 4 + 1).  Scratch rows of the block stage hold the extended block
+// in whole 32-float chunks, the backward pass's output starting kChromaRowShift
+// floats in (so its vector stores are 16-byte aligned).
+constexpr int kChromaEdge = 27;
+constexpr int kChromaExt = kBlock + 2 * kChromaEdge;
+constexpr int kChromaRowStride = (kChromaExt + 31) / 32 * 32;
+constexpr int kChromaRowShift = (4 - kChromaExt % 4) % 4;
+
 // Chroma channel of blocks [first_block, first_block + nblocks): the RF block
 // band-passed, rolled by `move` and its float mean removed, stitched like the
-// demodulated channels (stream index b*30720 + n - 1024).
+// demodulated channels (stream index b*30720 + n - 1024).  The capture pointer
+// is 16-byte aligned.
 struct ChromaBlockParams {
     const int16_t* rf16;       // capture at the decode rate (int16), or
     const float* rf32;         //   float (read when set)
     int64_t first_block, nblocks;
     ChromaCascade c;
     int move;
-    float* scratch;            // [nblocks * (kBlock + 2 * c.edge)]
+    float* scratch;            // [nblocks * kChromaRowStride]
     float* out;                // stitched chroma stream
 };
 constexpr int kChromaBlockKernels = 2;
