@@ -135,8 +135,12 @@ typedef struct vhsdecode_gb300_config_v1 {
     void* user_data;
 } vhsdecode_gb300_config_v1;
 
-/* config_v1 followed by the tape format.  run() takes either struct, told
- * apart by struct_size (config_v1 decodes VHS). */
+/* config_v1 followed by the tape format and decode flags.  run() takes either
+ * struct, told apart by struct_size (config_v1 decodes VHS with neutral
+ * chroma, as cuda-fast).  decode_flags: 0, or VHSDECODE_GB300_DECODE_CHROMA to
+ * decode the colour-under chroma into _chroma.tbc (the managed decoder's
+ * output, whose burst refinement also moves the luma line locations); other
+ * bits must be zero. */
 typedef struct vhsdecode_gb300_config_v2 {
     uint32_t struct_size;
     uint32_t profile;
@@ -153,7 +157,7 @@ typedef struct vhsdecode_gb300_config_v2 {
     vhsdecode_gb300_cancel_callback cancel_callback;
     void* user_data;
     uint32_t tape_format;       /* vhsdecode_gb300_tape_format */
-    uint32_t reserved;
+    uint32_t decode_flags;      /* 0 or VHSDECODE_GB300_DECODE_CHROMA */
 } vhsdecode_gb300_config_v2;
 
 /* vhsdecode_cuda_fast_result_v1 (:100-106). */

@@ -105,6 +105,30 @@ def test_run_rejects_unsupported_options(lib):
     assert run() == native.STATUS_INVALID_ARGUMENT
 
 
+def test_run_v2_decode_flags(lib):
+    # config_v2.decode_flags: 0 or DECODE_CHROMA; any other bit is refused
+    from vhsd_gb300 import native
+    cfg = native.RunConfigV2()
+    cfg.struct_size = ctypes.sizeof(cfg)
+    cfg.profile = native.PROFILE_NTSC
+    cfg.sample_rate_mhz = 40.0
+    cfg.output_base_utf8 = b"/tmp/x"
+    cfg.input_sample_format = native.INPUT_INT16
+    cfg.device_decimation_factor = 1
+    cfg.read_callback = native.READ_CB(lambda u, d, o, c: 0)
+    res = native.RunResult()
+    res.struct_size = ctypes.sizeof(res)
+
+    def run():
+        return lib.vhsdecode_gb300_run(ctypes.byref(cfg), ctypes.byref(res))
+    for bad in (native.DECODE_FLOAT_INPUT, 0x100, native.DECODE_CHROMA | 0x2):
+        cfg.decode_flags = bad
+        assert run() == native.STATUS_INVALID_ARGUMENT
+    for ok in (0, native.DECODE_CHROMA):   # accepted: the empty capture is an input error
+        cfg.decode_flags = ok
+        assert run() == native.STATUS_INPUT_ERROR
+
+
 def test_session_rejects_bad_decimation(lib):
     from vhsd_gb300 import native
     with pytest.raises(native.NativeError) as e:

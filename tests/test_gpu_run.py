@@ -9,7 +9,9 @@ into a 12-field capture.  Checked here:
   dropOuts identical; TBC within 1 LSB on >= 99.9 % of samples);
 * a short read mid-stream ends the input cleanly;
 * a cancellation during the decode returns CANCELLED and leaves no files;
-* a field limit across windows.
+* a field limit across windows;
+* with DECODE_CHROMA, the windowed luma and _chroma.tbc equal one whole
+  chroma decode (PAL and NTSC).
 Faults are made on the host (callbacks), never on the device.
 """
 import ctypes
@@ -34,7 +36,7 @@ def pal12():
     return rf, [f for f in fields if "error" not in f]
 
 
-def _run(rf, base, read=None, cancel=None, max_fields=0, total=None):
+def _run(rf, base, read=None, cancel=None, max_fields=0, total=None, chroma=False, profile=None):
     from vhsd_gb300 import native
     L = native.load()
     data = np.ascontiguousarray(rf, np.int16)
@@ -45,9 +47,12 @@ def _run(rf, base, read=None, cancel=None, max_fields=0, total=None):
             ctypes.memmove(dst, data[off:].ctypes.data, k * 2)
         return k
 
-    cfg = native.RunConfig()
+    cfg = native.RunConfigV2() if chroma else native.RunConfig()
     cfg.struct_size = ctypes.sizeof(cfg)
-    cfg.profile = native.PROFILE_PAL
+    if chroma:
+        cfg.tape_format = native.FORMAT_VHS
+        cfg.decode_flags = native.DECODE_CHROMA
+    cfg.profile = native.PROFILE_PAL if profile is None else profile
     cfg.tape_speed = native.TAPE_SP
     cfg.sample_rate_mhz = 40.0
     cfg.total_samples = len(data) if total is None else total
@@ -108,6 +113,30 @@ def test_windowed_run_equals_whole_decode_and_oracle(gpu, pal12, tmp_path, monke
     assert st == 0
     for ext in (".tbc", ".tbc.json", "_chroma.tbc"):
         assert open(base + ext, "rb").read() == open(str(tmp_path / "w40") + ext, "rb").read()
+
+
+@pytest.mark.parametrize("system", ["PAL", "NTSC"])
+def test_windowed_run_with_chroma_equals_whole_decode(gpu, system, tmp_path, monkeypatch):
+    # chroma through run(): the rotation index and the VHS field number (NTSC's
+    # burst phase target) carry across window joins, so the windowed files
+    # equal one whole-capture decode byte for byte
+    from vhsd_gb300 import native, synth
+    rf, _ = synth.generate(synth.config("pal_small" if system == "PAL" else "ntsc_small", fields=12, seed=21))
+    prof = native.PROFILE_PAL if system == "PAL" else native.PROFILE_NTSC
+    monkeypatch.setenv("VHSD_RUN_WINDOW_GRIDS", "3")
+    base = str(tmp_path / "c3")
+    st, res = _run(rf, base, chroma=True, profile=prof)
+    assert st == 0
+    tbc, meta = _outputs(base)
+    chroma = np.fromfile(base + "_chroma.tbc", np.uint16)
+    with native.Session(prof, len(rf)) as s:
+        r = s.decode(rf, chroma=True)
+        assert res.fields_written == r.fields >= 10
+        assert tbc.tobytes() == s.tbc().tobytes()
+        assert chroma.tobytes() == s.chroma().tobytes()
+        locs = [s.field(i).file_loc for i in range(r.fields)]
+    assert [f["fileLoc"] for f in meta["fields"]] == locs
+    assert chroma.size == tbc.size and np.count_nonzero(chroma != 32767) > chroma.size // 4
 
 
 def test_short_read_mid_stream_ends_input(gpu, pal12, tmp_path, monkeypatch):

@@ -717,8 +717,7 @@ void host_field_loop(vhsdecode_gb300_session* s, const T* sync, int64_t stream_l
         };
         FieldRec rec;
         // ResolveVhsFieldNumber (TbcFieldDecodePipeline.cs:860-874)
-        const int number = (st.vhs_number < 0 || st.vhs_loc < 0) ? 0
-                           : (s0 > st.vhs_loc ? st.vhs_number + 1 : st.vhs_number);
+        const int number = st.vhs_number < 0 ? 0 : (s0 > st.vhs_loc ? st.vhs_number + 1 : st.vhs_number);
         rec.sync = analyse_field(sp, raw, slen, st, fetch);
         rec.span_start = s0;
         rec.span_len = slen;

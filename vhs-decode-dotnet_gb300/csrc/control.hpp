@@ -51,7 +51,9 @@ struct FieldState {
     bool pulses_seen = false;   // a span with raw pulses was analysed (_vhsPulseSearchInitialized)
     // chroma: the rotation index carried from field to field (_chromaRotationIndex,
     // null = 0) and the VHS field number (ResolveVhsFieldNumber,
-    // Core/Decode/TbcFieldDecodePipeline.cs:860-874; -1 = none, after a failed field)
+    // Core/Decode/TbcFieldDecodePipeline.cs:860-874; vhs_number -1 = none, after a
+    // failed field; vhs_loc is the last field's read location in the current
+    // stream, negative when a window join left it behind the window)
     int chroma_rot = 0;
     int vhs_number = -1;
     int64_t vhs_loc = -1;

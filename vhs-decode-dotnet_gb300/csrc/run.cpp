@@ -332,10 +332,13 @@ VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_run(
         if (config->struct_size != sizeof(vhsdecode_gb300_config_v1) &&
             config->struct_size != sizeof(vhsdecode_gb300_config_v2))
             return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "config struct_size mismatch");
-        const uint32_t tape_format =
-            config->struct_size == sizeof(vhsdecode_gb300_config_v2)
-                ? reinterpret_cast<const vhsdecode_gb300_config_v2*>(config)->tape_format
-                : (uint32_t)VHSDECODE_GB300_TAPE_FORMAT_VHS;
+        const bool v2 = config->struct_size == sizeof(vhsdecode_gb300_config_v2);
+        const uint32_t tape_format = v2 ? reinterpret_cast<const vhsdecode_gb300_config_v2*>(config)->tape_format
+                                        : (uint32_t)VHSDECODE_GB300_TAPE_FORMAT_VHS;
+        const uint32_t run_flags = v2 ? reinterpret_cast<const vhsdecode_gb300_config_v2*>(config)->decode_flags : 0u;
+        if (run_flags & ~(uint32_t)VHSDECODE_GB300_DECODE_CHROMA)
+            return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "unknown decode_flags bit");
+        const bool with_chroma = (run_flags & VHSDECODE_GB300_DECODE_CHROMA) != 0;
         if (result->struct_size != sizeof(vhsdecode_gb300_result_v1))
             return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "result struct_size mismatch");
         if (!config->read_callback) return fail(VHSDECODE_GB300_STATUS_NULL_POINTER, "read_callback is null");
@@ -431,7 +434,7 @@ VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_run(
         sc.max_samples = std::min<uint64_t>((uint64_t)win_src, buf.size() / esz);
         sc.precision = VHSDECODE_GB300_PRECISION_FP32_FUSED;
         sc.decimation = factor;
-        PinnedHost win, tbc_host;   // outlive the session, whose teardown waits for the device
+        PinnedHost win, tbc_host, chroma_host;   // outlive the session, whose teardown waits for the device
         SessionHolder h;
         h.s = new vhsdecode_gb300_session();
         session_init(h.s, sc);
@@ -439,6 +442,9 @@ VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_run(
         const size_t per = (size_t)s->out_lines * s->outlen;
         ck(cudaMallocHost((void**)&win.p, (size_t)sc.max_samples * esz), "pinned window");
         ck(cudaMallocHost((void**)&tbc_host.p, (size_t)s->max_fields * per * sizeof(uint16_t)), "pinned tbc");
+        if (with_chroma)
+            ck(cudaMallocHost((void**)&chroma_host.p, (size_t)s->max_fields * per * sizeof(uint16_t)),
+               "pinned chroma");
         out.open();
         const std::vector<uint16_t> neutral(per, (uint16_t)32767);
         std::vector<FieldMeta> meta;
@@ -473,21 +479,28 @@ VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_run(
             }
             vhsdecode_gb300_decode_result_v1 dr{};
             dr.struct_size = sizeof(dr);
-            decode_impl(s, win.p, n, left, f32_in ? VHSDECODE_GB300_DECODE_FLOAT_INPUT : 0u, &dr,
-                        &latch.requested, &carry);
+            const uint32_t dflags = (f32_in ? VHSDECODE_GB300_DECODE_FLOAT_INPUT : 0u) |
+                                    (with_chroma ? VHSDECODE_GB300_DECODE_CHROMA : 0u);
+            decode_impl(s, win.p, n, left, dflags, &dr, &latch.requested, &carry);
             const size_t nf = s->fields.size();
             if (nf) {
                 ck(cudaMemcpy(tbc_host.p, s->tbc.p, nf * per * sizeof(uint16_t), cudaMemcpyDeviceToHost),
                    "d2h tbc");
                 if (std::fwrite(tbc_host.p, sizeof(uint16_t), nf * per, out.ftbc) != nf * per)
                     throw Failure(VHSDECODE_GB300_STATUS_OUTPUT_ERROR, "cannot write " + out.tbc);
+                if (with_chroma) {
+                    ck(cudaMemcpy(chroma_host.p, s->chroma.p, nf * per * sizeof(uint16_t), cudaMemcpyDeviceToHost),
+                       "d2h chroma");
+                    if (std::fwrite(chroma_host.p, sizeof(uint16_t), nf * per, out.fchroma) != nf * per)
+                        throw Failure(VHSDECODE_GB300_STATUS_OUTPUT_ERROR, "cannot write " + out.chroma);
+                }
                 for (size_t k = 0; k < nf; k++) {
-                    // Chroma is not decoded by this backend: neutral chroma (zero
-                    // chroma + 32767, VhsChromaDecoder.ChromaToU16,
+                    // Without chroma, as cuda-fast: neutral chroma (zero chroma +
+                    // 32767, VhsChromaDecoder.ChromaToU16,
                     // Core/Decode/VhsChromaDecoder.cs:455-500) in the luma
                     // geometry, which the managed finalisation truncates with the
                     // luma file (Core/Dsp/CudaFast/CudaFastDecodeRunner.cs:345,427).
-                    if (std::fwrite(neutral.data(), sizeof(uint16_t), per, out.fchroma) != per)
+                    if (!with_chroma && std::fwrite(neutral.data(), sizeof(uint16_t), per, out.fchroma) != per)
                         throw Failure(VHSDECODE_GB300_STATUS_OUTPUT_ERROR, "cannot write " + out.chroma);
                     const FieldRec& r = s->fields[k];
                     FieldMeta m;
@@ -511,6 +524,9 @@ VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_run(
             uint64_t ws_next = ws + (uint64_t)grid_src * (uint64_t)(back / kGrid);
             if (ws_next <= ws) ws_next = ws + (uint64_t)grid_src;   // no field fits: move on a step
             if (next_abs < ws_next) cont = false;
+            // the previous field's read location in the next window's stream
+            // (the VHS field number counts reads that move forward)
+            carry.state.vhs_loc -= (int64_t)((ws_next - ws) / factor);
             ws = ws_next;
         }
         if (latch.poll()) throw Failure(VHSDECODE_GB300_STATUS_CANCELLED, "decode cancelled");

@@ -62,6 +62,7 @@ struct History {
     bool valid = false;
     FieldState state;
     uint64_t next_abs = 0;  // source-sample position of the next field span (stream coordinates)
+    int64_t vhs_abs = 0;    // source-sample position of the last field's read location
     bool busy = false;
 };
 
@@ -210,6 +211,7 @@ bool window_carry(const vhsdecode_gb300_window_v1& w, const History& hist, Decod
     const bool cont = !w.seek && hist.valid && hist.next_abs >= w.source_offset;
     if (cont) {
         carry.state = hist.state;
+        carry.state.vhs_loc = (hist.vhs_abs - (int64_t)w.source_offset) / (int64_t)decim;
         carry.start = (int64_t)((hist.next_abs - w.source_offset) / decim);
     }
     return cont;
@@ -241,6 +243,7 @@ void window_finish(vhsdecode_gb300_session* s, const vhsdecode_gb300_window_v1& 
     out_hist.valid = dr.fields > 0;
     out_hist.state = carry.state;
     out_hist.next_abs = w.source_offset + decim * (uint64_t)std::max<int64_t>(0, carry.next);
+    out_hist.vhs_abs = (int64_t)w.source_offset + (int64_t)decim * carry.state.vhs_loc;
 }
 
 void run_window(Slot* sl, const Request& rq, const History& hist, vhsdecode_gb300_window_result_v1& r,

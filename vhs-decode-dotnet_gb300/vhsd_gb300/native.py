@@ -102,8 +102,8 @@ class RunConfig(ctypes.Structure):
 
 
 class RunConfigV2(ctypes.Structure):
-    """config_v1 followed by the tape format (vhsdecode_gb300_config_v2)."""
-    _fields_ = RunConfig._fields_ + [("tape_format", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+    """config_v1 followed by the tape format and decode flags (vhsdecode_gb300_config_v2)."""
+    _fields_ = RunConfig._fields_ + [("tape_format", ctypes.c_uint32), ("decode_flags", ctypes.c_uint32)]
 
 
 class RunResult(ctypes.Structure):
@@ -182,7 +182,8 @@ def load(path: str = LIB_PATH):
     L.vhsdecode_gb300_get_abi_version.restype = ctypes.c_uint32
     L.vhsdecode_gb300_get_last_error.restype = ctypes.c_char_p
     L.vhsdecode_gb300_get_runtime_info.argtypes = [ctypes.c_int32, _P(RuntimeInfo)]
-    L.vhsdecode_gb300_run.argtypes = [_P(RunConfig), _P(RunResult)]
+    # config_v1 or config_v2, told apart by struct_size
+    L.vhsdecode_gb300_run.argtypes = [ctypes.c_void_p, _P(RunResult)]
     L.vhsdecode_gb300_session_create.argtypes = [_P(SessionConfig), _P(_vp)]
     L.vhsdecode_gb300_session_destroy.argtypes = [_vp]
     L.vhsdecode_gb300_session_destroy.restype = None
