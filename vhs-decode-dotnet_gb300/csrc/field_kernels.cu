@@ -1268,6 +1268,10 @@ __global__ void k_tbc_consts(TbcParams p) {
 }
 
 constexpr int kTbcFastMaxThreads = 384;
+// kPair: a second source (src2 -> out2_f32) summed with the same taps; its own
+// instantiation, so the single-source kernel keeps its register count (two
+// CTAs per SM).
+template <bool kPair>
 __global__ void __launch_bounds__(kTbcFastMaxThreads) k_tbc_fast(const float* stream, int64_t stream_len,
                                                                  TbcParams p) {
     const int f = blockIdx.y;
@@ -1344,7 +1348,7 @@ __global__ void __launch_bounds__(kTbcFastMaxThreads) k_tbc_fast(const float* st
                 two_sum(hi, prod, s, e);
                 hi = s;
                 lo = __fadd_rn(lo, e);
-                if (src2) {
+                if (kPair) {
                     float prod2 = __fmul_rn(__ldg(src2 + idx), wt);
                     two_sum(hi2, prod2, s, e);
                     hi2 = s;
@@ -1363,7 +1367,7 @@ __global__ void __launch_bounds__(kTbcFastMaxThreads) k_tbc_fast(const float* st
             const float rh = __shfl_sync(0xffffffffu, hi, 4 * (lane & 7));
             const float rl = __shfl_sync(0xffffffffu, lo, 4 * (lane & 7));
             if ((lane >> 3) == rnd) { hi_own = rh; lo_own = rl; }
-            if (src2) {
+            if (kPair) {
 #pragma unroll
                 for (int o = 1; o < 4; o <<= 1) {
                     float oh = __shfl_xor_sync(0xffffffffu, hi2, o);
@@ -1386,7 +1390,7 @@ __global__ void __launch_bounds__(kTbcFastMaxThreads) k_tbc_fast(const float* st
         }
         float2 v = ff_mul(hi_own, lo_own, la.x, la.y);
         float outf = __fadd_rn(v.x, v.y);
-        if (out2) {
+        if (kPair) {
             float2 v2 = ff_mul(hi2_own, lo2_own, la.x, la.y);
             out2[k] = __fadd_rn(v2.x, v2.y);
         }
@@ -1436,7 +1440,10 @@ cudaError_t launch_tbc_pw(const T* stream, int64_t stream_len, const TbcParams& 
         const int width = (p.x1 > 0 ? p.x1 : p.outlen) - p.x0;
         const int passes = (width + kTbcFastMaxThreads - 1) / kTbcFastMaxThreads;
         const int threads = ((width + passes - 1) / passes + 31) / 32 * 32;
-        k_tbc_fast<<<grid, threads, 0, s>>>(reinterpret_cast<const float*>(stream), stream_len, p);
+        if (p.src2)
+            k_tbc_fast<true><<<grid, threads, 0, s>>>(reinterpret_cast<const float*>(stream), stream_len, p);
+        else
+            k_tbc_fast<false><<<grid, threads, 0, s>>>(reinterpret_cast<const float*>(stream), stream_len, p);
     } else {
         k_tbc<T><<<grid, 256, 0, s>>>(stream, stream_len, p, pw);
     }
