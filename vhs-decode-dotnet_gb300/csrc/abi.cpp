@@ -370,8 +370,9 @@ void ensure_chroma(vhsdecode_gb300_session* s) {
     ck(cudaMemcpy(s->c_bcos.p, bcos.data(), bcos.size() * sizeof(float), cudaMemcpyHostToDevice), "upload");
     s->c_ana.alloc(mf * s->out_lines * win);
     s->c_field.alloc(mf * field);
-    s->c_up.alloc(mf * field);
-    s->c_fwd.alloc(mf * (field + 2 * (size_t)d.fin.edge));
+    const size_t crow = (size_t)chroma_final_row((int64_t)field, d.fin.edge);
+    s->c_up.alloc(mf * crow);
+    s->c_fwd.alloc(mf * crow);
     s->c_probe.alloc(mf * 2 * s->out_lines * 5);
     s->c_summary.alloc(mf * 4);
     s->locs_final.alloc(mf * s->lines);
@@ -382,22 +383,27 @@ void ensure_chroma(vhsdecode_gb300_session* s) {
     std::vector<int> ones(mf, 1);
     ck(cudaMemcpy(s->c_ones.p, ones.data(), mf * sizeof(int), cudaMemcpyHostToDevice), "upload");
     s->chroma.alloc(mf * field);
+    s->c_line_cs.alloc(mf * s->out_lines);
+    s->c_line_scale.alloc(mf * s->out_lines);
+    s->c_line_scale_f.alloc(mf * s->out_lines);
     {
         // NTSC up-conversion: the phase advance of sample k of a line as the
         // reference's four lanes step theta (UpconvertChromaPhaseCompensated,
-        // VhsChromaDecoder.cs:2182-2246), reduced by whole turns
+        // VhsChromaDecoder.cs:2182-2246), reduced by whole turns, as its
+        // (cos, sin)
         const double h = ((d.cu_hz * 1.5707963267948965e-6) / d.fsc_mhz) + 1.5707963267948966;
         const double two_pi = 6.283185307179586, inv = 0.15915494309189535;
         const int vc = d.outlen & ~3;
         const double lane[4] = {h * 0.0, h, h * 2.0, h * 3.0};
-        std::vector<double> adv((size_t)d.outlen);
+        std::vector<float2> adv((size_t)d.outlen);
         for (int k = 0; k < d.outlen; k++) {
             double off = k < vc ? std::fma((double)(k >> 2), h * 4.0, lane[k & 3])
                                 : std::fma((double)(k - vc), h, h * (double)vc);
-            adv[(size_t)k] = std::fma(-std::nearbyint(off * inv), two_pi, off);
+            const double a = std::fma(-std::nearbyint(off * inv), two_pi, off);
+            adv[(size_t)k] = make_float2((float)std::cos(a), (float)std::sin(a));
         }
         s->c_advance.alloc(adv.size());
-        ck(cudaMemcpy(s->c_advance.p, adv.data(), adv.size() * sizeof(double), cudaMemcpyHostToDevice), "upload");
+        ck(cudaMemcpy(s->c_advance.p, adv.data(), adv.size() * sizeof(float2), cudaMemcpyHostToDevice), "upload");
     }
     ck(cudaEventCreateWithFlags(&s->chroma_refined, cudaEventDisableTiming), "cudaEventCreate");
     ck(cudaStreamCreateWithFlags(&s->chroma_stream, cudaStreamNonBlocking), "cudaStreamCreate");
@@ -905,8 +911,9 @@ void launch_field_batch(vhsdecode_gb300_session* s, int f0, int f1, const T* vid
         cp.field_number = s->field_number_d.p + f0;
         const size_t field = (size_t)d.field_samples;
         cp.cfield = s->c_field.p + (size_t)f0 * field;
-        cp.up = s->c_up.p + (size_t)f0 * field;
-        cp.fwd = s->c_fwd.p + (size_t)f0 * (field + 2 * (size_t)d.fin.edge);
+        cp.crow = chroma_final_row((int64_t)field, d.fin.edge);
+        cp.up = s->c_up.p + (size_t)f0 * (size_t)cp.crow;
+        cp.fwd = s->c_fwd.p + (size_t)f0 * (size_t)cp.crow;
         cp.out = s->chroma.p + (size_t)f0 * field;
         cp.cu_hz = d.cu_hz;
         cp.fsc_mhz = d.fsc_mhz;
@@ -914,6 +921,9 @@ void launch_field_batch(vhsdecode_gb300_session* s, int f0, int f1, const T* vid
         // UpconvertChromaPhaseCompensated's hetCoefficient (VhsChromaDecoder.cs:2182-2186)
         cp.ntsc_h = ((d.cu_hz * 1.5707963267948965e-6) / d.fsc_mhz) + 1.5707963267948966;
         cp.ntsc_advance = s->c_advance.p;
+        cp.line_cs = s->c_line_cs.p + (size_t)f0 * s->out_lines;
+        cp.line_scale = s->c_line_scale.p + (size_t)f0 * s->out_lines;
+        cp.line_scale_f = s->c_line_scale_f.p + (size_t)f0 * s->out_lines;
         ck(cudaMemsetAsync(s->c_state.p + 1, 0, sizeof(int), fs), "memset");
         TbcParams ta = tp;
         ta.locs = cp.locs;
@@ -1748,7 +1758,10 @@ VHSDECODE_GB300_API int32_t VHSDECODE_GB300_CALL vhsdecode_gb300_session_copy_ch
         const float* fsrc = nullptr;
         size_t n = 0;
         if (stage == 0) { fsrc = s->c_field.p + field * fsz; n = fsz; }
-        else if (stage == 1) { fsrc = s->c_up.p + field * fsz; n = fsz; }
+        else if (stage == 1) {
+            fsrc = s->c_up.p + field * (size_t)chroma_final_row((int64_t)fsz, s->cd.fin.edge) + s->cd.fin.edge;
+            n = fsz;
+        }
         else if (stage == 2) { fsrc = s->c_ana.p + field * (size_t)s->out_lines * win; n = (size_t)s->out_lines * win; }
         if (fsrc) {
             if (capacity < n) return fail(VHSDECODE_GB300_STATUS_INVALID_ARGUMENT, "capacity too small");

@@ -32,9 +32,6 @@ namespace vhsd {
 namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
-constexpr int kTile = 32;          // samples staged per group per tile
-constexpr int kGroupsPerWarp = 8;  // 4-lane groups
-constexpr int kIirWarps = 4;       // warps per CTA of the cascade kernels
 constexpr int kChunk = 1024;       // final band-pass chunk
 constexpr int kWarmup = 448;       // zero-state lead of a chunk
 
@@ -45,109 +42,47 @@ __device__ __forceinline__ float sos_step(const float* c, float v, float& z1, fl
     return f;
 }
 
-// One pass of the 4-section cascade over samples 0 .. len-1 of a sequence,
-// run by a 4-lane group (lane s = section s).  Lane s filters sample t - 32 s
-// at step t, so its input (the output of lane s - 1) was written a whole
-// 32-step batch earlier and each lane runs only its own section's recurrence.
-// Per batch a lane reads its 32 inputs (lane 0 from the staged input tile,
-// the others from the ring of the lane before), filters them, and writes its
-// outputs (lane 3: to the output tile, flushed by all four lanes).  Every
-// group of the warp loops `steps` times (warp-uniform, >= len + 96).
-// load(i) returns sample i of the pass; store(i, v) receives the cascade
-// output of sample i.  The initial state is zi * x0.  `area` is the group's
-// kCascadeArea floats of shared memory.
-// Regions of kTile floats padded to kRegion, so the float4 accesses of the 32
-// lanes of a warp (8 groups x 4 lanes, each lane its own region) spread over
-// the shared-memory banks instead of all starting on bank 0.
-constexpr int kRegion = kTile + 4;
-constexpr int kCascadeArea = 9 * kRegion;   // input tiles [2], rings [3][2], output tile
+// The 4-section cascade run by one lane: at step t section s filters sample
+// t - s, so the four recurrences of a step are independent.  Each section
+// sees its samples in order with its own state, so the outputs are those of
+// the sample-by-sample loop.  The coefficients stay in the parameter bank
+// (constant indices).
+struct LaneCascade {
+    float z[4][2];
+    float v1, v2, v3;   // outputs of sections 0..2 waiting for the next section
 
-// Staged input: fetch(i) loads the raw 32-bit word of sample i (an int16 read
-// sign-extended by the load itself, or float bits) and cook(raw, i) turns it
-// into the sample a batch later, so no instruction waits on the load while
-// the recurrence runs.
-template <typename Fetch, typename Cook, typename Store>
-__device__ __forceinline__ void cascade_batch(const float* sec, float& z1, float& z2, int s, float* tin, float* ring,
-                                              float* tout, int64_t base, int cur, int64_t len,
-                                              uint32_t (&fetch_into)[kTile / 4], const uint32_t (&staged)[kTile / 4],
-                                              Fetch fetch, Cook cook, Store store) {
-    constexpr int per = kTile / 4;
-    // loads for the tile two batches ahead (cooked at the end of the next batch)
+    __device__ __forceinline__ void init(const ChromaCascade& c, float x0) {
 #pragma unroll
-    for (int k = 0; k < per; k++) {
-        const int64_t i = base + 2 * kTile + s * per + k;
-        fetch_into[k] = i < len ? fetch(i) : 0u;
-    }
-    const float* src = s == 0 ? tin + cur * kRegion : ring + ((s - 1) * 2 + (cur ^ 1)) * kRegion;
-    float v[kTile];
-#pragma unroll
-    for (int j = 0; j < kTile; j += 4) {
-        const float4 q = *reinterpret_cast<const float4*>(src + j);
-        v[j] = q.x; v[j + 1] = q.y; v[j + 2] = q.z; v[j + 3] = q.w;
-    }
-    const int64_t i0 = base - (int64_t)s * kTile;
-    if (i0 >= 0 && i0 + kTile <= len) {
-#pragma unroll
-        for (int j = 0; j < kTile; j++) v[j] = sos_step(sec, v[j], z1, z2);
-    } else {
-#pragma unroll
-        for (int j = 0; j < kTile; j++) {
-            const int64_t i = i0 + j;
-            v[j] = (i >= 0 && i < len) ? sos_step(sec, v[j], z1, z2) : 0.0f;
+        for (int q = 0; q < 4; q++) {
+            z[q][0] = __fmul_rn(c.zi[q][0], x0);
+            z[q][1] = __fmul_rn(c.zi[q][1], x0);
         }
+        v1 = v2 = v3 = 0.0f;
     }
-    float* dst = s < 3 ? ring + (s * 2 + cur) * kRegion : tout;
-#pragma unroll
-    for (int j = 0; j < kTile; j += 4) *reinterpret_cast<float4*>(dst + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
-    // the tile of the next batch, fetched one batch ago
-#pragma unroll
-    for (int k = 0; k < per; k++) {
-        const int64_t i = base + kTile + s * per + k;
-        tin[(cur ^ 1) * kRegion + s * per + k] = i < len ? cook(staged[k], i) : 0.0f;
+    // steps 0, 1, 2: only the sections that have a sample yet
+    __device__ __forceinline__ void prime(const ChromaCascade& c, float x0, float x1, float x2) {
+        v1 = sos_step(c.sec[0], x0, z[0][0], z[0][1]);
+        v2 = sos_step(c.sec[1], v1, z[1][0], z[1][1]);
+        v1 = sos_step(c.sec[0], x1, z[0][0], z[0][1]);
+        v3 = sos_step(c.sec[2], v2, z[2][0], z[2][1]);
+        v2 = sos_step(c.sec[1], v1, z[1][0], z[1][1]);
+        v1 = sos_step(c.sec[0], x2, z[0][0], z[0][1]);
     }
-    __syncwarp();
-#pragma unroll
-    for (int k = 0; k < per; k++) {
-        const int64_t i = base - 3 * kTile + s * per + k;
-        if (i >= 0 && i < len) store(i, tout[s * per + k]);
+    // step t >= 3: takes sample t, returns the cascade output of sample t - 3
+    __device__ __forceinline__ float step(const ChromaCascade& c, float x) {
+        const float y = sos_step(c.sec[3], v3, z[3][0], z[3][1]);
+        v3 = sos_step(c.sec[2], v2, z[2][0], z[2][1]);
+        v2 = sos_step(c.sec[1], v1, z[1][0], z[1][1]);
+        v1 = sos_step(c.sec[0], x, z[0][0], z[0][1]);
+        return y;
     }
-    __syncwarp();
-}
+};
 
-template <typename Fetch, typename Cook, typename Store>
-__device__ __forceinline__ void cascade(const ChromaCascade& c, int s, float* area, int64_t steps, int64_t len,
-                                        float x0, Fetch fetch, Cook cook, Store store) {
-    float* tin = area;                 // [2][kRegion]
-    float* ring = area + 2 * kRegion;  // [3][2][kRegion]
-    float* tout = ring + 6 * kRegion;  // [kRegion]
-    float z1 = __fmul_rn(c.zi[s][0], x0), z2 = __fmul_rn(c.zi[s][1], x0);
-    float sec[6];
-#pragma unroll
-    for (int k = 0; k < 6; k++) sec[k] = c.sec[s][k];
-    constexpr int per = kTile / 4;
-    uint32_t ra[per], rb[per];
-#pragma unroll
-    for (int k = 0; k < per; k++) {
-        const int64_t i = s * per + k;
-        tin[s * per + k] = i < len ? cook(fetch(i), i) : 0.0f;
-        const int64_t i1 = kTile + s * per + k;
-        ra[k] = i1 < len ? fetch(i1) : 0u;
-    }
-    __syncwarp();
-    // two batches per trip so the staging registers alternate by name
-    for (int64_t base = 0; base < steps; base += 2 * kTile) {
-        cascade_batch(sec, z1, z2, s, tin, ring, tout, base, 0, len, rb, ra, fetch, cook, store);
-        cascade_batch(sec, z1, z2, s, tin, ring, tout, base + kTile, 1, len, ra, rb, fetch, cook, store);
-    }
-}
-
-// float sources: the raw word is the float's bits
-__device__ __forceinline__ float as_f(uint32_t u) { return __uint_as_float(u); }
-__device__ __forceinline__ uint32_t f_bits(float f) { return __float_as_uint(f); }
 
 // ---------------------------------------------------------------- block stage
 
-// The block stage runs the same section-per-lane cascade as cascade() above,
+// The block stage runs the 4-section cascade as a group of four lanes per
+// block, lane s running section s one 32-sample batch behind lane s - 1,
 // with its input fed from a ring of 32-sample chunks that cp.async fills
 // kRingDepth - 2 batches ahead (the latency of a global load is longer than
 // a batch of the recurrence), the lane-to-lane hand-over in registers
@@ -371,96 +306,133 @@ __device__ __forceinline__ int positive_mod4(int v) {
     return r < 0 ? r + 4 : r;
 }
 
-// One 4-lane group per (field, rotation sequence, line): the probe window of
-// the line times the heterodyne of its phase rotation, the float32
-// forward-backward final band-pass over it (odd extension, in shared memory),
-// and the I/Q demodulation of the burst against the carrier tables.
-__global__ void __launch_bounds__(128) k_chroma_probe(ChromaFieldParams p) {
+// One lane per (field, rotation sequence, line): the probe window of the
+// line times the heterodyne of its phase rotation, the float32
+// forward-backward final band-pass over it (odd extension, in place in the
+// lane's shared-memory row; LaneCascade), and the I/Q demodulation of the
+// burst against the carrier tables.  A warp fills its 32 rows together, each
+// window read by the whole warp (coalesced); rows have an odd stride, so the
+// lanes' own passes over their rows hit 32 different banks.
+__global__ void __launch_bounds__(32) k_chroma_probe(ChromaFieldParams p) {
     extern __shared__ float smem[];
-    const int lane = threadIdx.x & 31, s = lane & 3;
-    const int gi = threadIdx.x >> 2;   // group in the CTA
-    const int64_t pid = (int64_t)blockIdx.x * (blockDim.x >> 2) + gi;
-    const int64_t nprobe = (int64_t)p.nfields * 2 * p.out_lines;
-    const bool active = pid < nprobe;
-    const int64_t q = active ? pid : 0;
-    const int f = (int)(q / (2 * p.out_lines));
-    const int cnd = (int)((q / p.out_lines) % 2);
-    const int pl = (int)(q % p.out_lines);   // sequence index; line = pl + 1
+    const int lane = threadIdx.x;
     const int edge = p.fin.edge;
     const int win = p.win;
     const int len = win + 2 * edge;
-    const int lpad = (len + 3) & ~3;
-    float* buf = smem + (size_t)gi * (lpad + kCascadeArea);
-    float* tile = buf + lpad;
+    const int stride = len | 1;
+    const int64_t nprobe = (int64_t)p.nfields * 2 * p.out_lines;
+    const int64_t base = (int64_t)blockIdx.x * 32;
     const int64_t field = (int64_t)p.out_lines * p.outlen;
-    const int rot = positive_mod4((cnd == 0 ? p.rot0 : p.rot1) * (pl + 1));
-    const int64_t line_start = (int64_t)pl * p.outlen;
-    const int64_t p0 = line_start + p.win0;
-    const float* het = p.het + (int64_t)rot * field + p0;
-    const float* ana = p.ana + ((int64_t)f * p.out_lines + pl) * win;
-    // mixed samples into buf[edge .. edge + win), then the odd extension
-    for (int i = s; i < win; i += 4) buf[edge + i] = __fmul_rn(het[i], ana[i]);
-    __syncwarp();
-    {
-        const float first = buf[edge], last = buf[edge + win - 1];
-        for (int e = s; e < edge; e += 4) {
-            buf[e] = __fsub_rn(__fmul_rn(2.0f, first), buf[edge + edge - e]);
-            buf[edge + win + e] = __fsub_rn(__fmul_rn(2.0f, last), buf[edge + win - 2 - e]);
-        }
+    for (int j = 0; j < 32; j++) {
+        const int64_t qj = base + j;
+        if (qj >= nprobe) break;
+        const int fj = (int)(qj / (2 * p.out_lines));
+        const int cj = (int)((qj / p.out_lines) % 2);
+        const int lj = (int)(qj % p.out_lines);
+        const int rot = positive_mod4((cj == 0 ? p.rot0 : p.rot1) * (lj + 1));
+        const float* het = p.het + (int64_t)rot * field + (int64_t)lj * p.outlen + p.win0;
+        const float* ana = p.ana + ((int64_t)fj * p.out_lines + lj) * win;
+        float* row = smem + j * stride + edge;
+#pragma unroll 4
+        for (int i = lane; i < win; i += 32) row[i] = __fmul_rn(het[i], ana[i]);
     }
     __syncwarp();
-    const int64_t steps = len + 3 * kTile;
-    cascade(p.fin, s, tile, steps, len, buf[0], [&](int64_t i) { return f_bits(buf[i]); },
-            [](uint32_t raw, int64_t) { return as_f(raw); }, [&](int64_t i, float v) { buf[i] = v; });
-    __syncwarp();
-    const float xl = buf[len - 1];
-    __syncwarp();
-    cascade(p.fin, s, tile, steps, len, xl, [&](int64_t i) { return f_bits(buf[len - 1 - i]); },
-            [](uint32_t raw, int64_t) { return as_f(raw); }, [&](int64_t i, float v) { buf[len - 1 - i] = v; });
-    __syncwarp();
-    // DemodBurstFloat32: burst = filtered[pad, win - pad), tables from line_start + bs
+    const bool active = base + lane < nprobe;
+    const int64_t q = active ? base + lane : 0;
+    const int f = (int)(q / (2 * p.out_lines));
+    const int pl = (int)(q % p.out_lines);   // sequence index; line = pl + 1
+    const int64_t line_start = (int64_t)pl * p.outlen;
+    float* buf = smem + lane * stride;
+    if (active) {
+        const float first = buf[edge], last = buf[edge + win - 1];
+        for (int e = 0; e < edge; e++) {
+            buf[e] = __fsub_rn(__fmul_rn(2.0f, first), buf[2 * edge - e]);
+            buf[edge + win + e] = __fsub_rn(__fmul_rn(2.0f, last), buf[edge + win - 2 - e]);
+        }
+        // in place over the row, forward then backward: sequence sample t at
+        // row index pos(t); step t writes sample t - 3.  Tiles of 8 samples are
+        // read a tile ahead (before the writes that reach them), so no step
+        // waits on its shared-memory load.
+        auto lane_pass = [&](auto pos) {
+            LaneCascade lc;
+            lc.init(p.fin, buf[pos(0)]);
+            const int ntile = (len + 3 + 7) / 8;
+            float x[8], nx[8];
+#pragma unroll
+            for (int j = 0; j < 8; j++) x[j] = buf[pos(j)];
+            for (int k = 0; k < ntile; k++) {
+#pragma unroll
+                for (int j = 0; j < 8; j++) {
+                    const int t = 8 * (k + 1) + j;
+                    nx[j] = t < len ? buf[pos(t)] : 0.0f;
+                }
+                int j0 = 0;
+                if (k == 0) {
+                    lc.prime(p.fin, x[0], x[1], x[2]);
+                    j0 = 3;
+                }
+#pragma unroll
+                for (int j = 0; j < 8; j++) {
+                    if (j < j0) continue;
+                    const float y = lc.step(p.fin, x[j]);
+                    const int u = 8 * k + j - 3;
+                    if (u < len) buf[pos(u)] = y;
+                }
+#pragma unroll
+                for (int j = 0; j < 8; j++) x[j] = nx[j];
+            }
+        };
+        lane_pass([](int t) { return t; });
+        lane_pass([len](int t) { return len - 1 - t; });
+    }
+    // DemodBurstFloat32: burst = filtered[pad, win - pad), tables from
+    // line_start + bs; 16 accumulators (accumulator a takes samples
+    // k + a), folded as the reference's lanes fold them, then the 4-wide
+    // epilogue and the scalar tail
+    if (!active) return;
     const int pad = p.be - p.bs;
     const int n = win - 2 * pad;
     const float* burst = buf + edge + pad;
     const float* bc = p.bcos + line_start + p.bs;
     const float* bsn = p.bsin + line_start + p.bs;
     const int main_end = n & ~15, epi_end = n & ~3;
-    double I[4] = {0, 0, 0, 0}, Q[4] = {0, 0, 0, 0};   // groups 0..3 of this lane
+    double I[16], Q[16];
+#pragma unroll
+    for (int a = 0; a < 16; a++) I[a] = Q[a] = 0.0;
     for (int k = 0; k < main_end; k += 16) {
 #pragma unroll
-        for (int gr = 0; gr < 4; gr++) {
-            const int idx = k + s + 4 * gr;
-            const float sm = burst[idx];
-            I[gr] = __dadd_rn(I[gr], (double)__fmul_rn(sm, bc[idx]));
-            Q[gr] = __dadd_rn(Q[gr], (double)__fmul_rn(sm, bsn[idx]));
+        for (int a = 0; a < 16; a++) {
+            const float sm = burst[k + a];
+            I[a] = __dadd_rn(I[a], (double)__fmul_rn(sm, bc[k + a]));
+            Q[a] = __dadd_rn(Q[a], (double)__fmul_rn(sm, bsn[k + a]));
         }
     }
-    const unsigned gmask = kFull;
-    double li = __dadd_rn(__dadd_rn(__dadd_rn(I[1], I[0]), I[2]), I[3]);
-    double lq = __dadd_rn(__dadd_rn(__dadd_rn(Q[1], Q[0]), Q[2]), Q[3]);
-    auto fold4 = [&](double v) {
-        // (l0 + l2) + (l1 + l3) within the group
-        double v2 = __shfl_down_sync(gmask, v, 2, 4);
-        double a = __dadd_rn(v, v2);   // lane 0: l0 + l2, lane 1: l1 + l3
-        double b = __shfl_down_sync(gmask, a, 1, 4);
-        return __shfl_sync(gmask, __dadd_rn(a, b), 0, 4);
-    };
-    double ic = fold4(li), qc = fold4(lq);
+    double li[4], lq[4];
+#pragma unroll
+    for (int g = 0; g < 4; g++) {
+        li[g] = __dadd_rn(__dadd_rn(__dadd_rn(I[g + 4], I[g]), I[g + 8]), I[g + 12]);
+        lq[g] = __dadd_rn(__dadd_rn(__dadd_rn(Q[g + 4], Q[g]), Q[g + 8]), Q[g + 12]);
+    }
+    double ic = __dadd_rn(__dadd_rn(li[0], li[2]), __dadd_rn(li[1], li[3]));
+    double qc = __dadd_rn(__dadd_rn(lq[0], lq[2]), __dadd_rn(lq[1], lq[3]));
     if (epi_end > main_end) {
-        double ei = s == 0 ? ic : 0.0, eq = s == 0 ? qc : 0.0;
+        double ei[4] = {ic, 0.0, 0.0, 0.0}, eq[4] = {qc, 0.0, 0.0, 0.0};
         for (int k = main_end; k < epi_end; k += 4) {
-            const float sm = burst[k + s];
-            ei = __dadd_rn(ei, (double)__fmul_rn(sm, bc[k + s]));
-            eq = __dadd_rn(eq, (double)__fmul_rn(sm, bsn[k + s]));
+#pragma unroll
+            for (int g = 0; g < 4; g++) {
+                const float sm = burst[k + g];
+                ei[g] = __dadd_rn(ei[g], (double)__fmul_rn(sm, bc[k + g]));
+                eq[g] = __dadd_rn(eq[g], (double)__fmul_rn(sm, bsn[k + g]));
+            }
         }
-        ic = fold4(ei);
-        qc = fold4(eq);
+        ic = __dadd_rn(__dadd_rn(ei[0], ei[2]), __dadd_rn(ei[1], ei[3]));
+        qc = __dadd_rn(__dadd_rn(eq[0], eq[2]), __dadd_rn(eq[1], eq[3]));
     }
-    if (s == 0 && active) {
-        for (int k = epi_end; k < n; k++) {
-            ic = __dadd_rn(ic, (double)__fmul_rn(burst[k], bc[k]));
-            qc = __dadd_rn(qc, (double)__fmul_rn(burst[k], bsn[k]));
-        }
+    for (int k = epi_end; k < n; k++) {
+        ic = __dadd_rn(ic, (double)__fmul_rn(burst[k], bc[k]));
+        qc = __dadd_rn(qc, (double)__fmul_rn(burst[k], bsn[k]));
+    }
+    {
         const int line = pl + 1;
         const double* loc = p.locs + (int64_t)f * p.lines;
         const double scale = pl < p.out_lines - 1 ? __ddiv_rn(__dsub_rn(loc[line + 1], loc[line]), (double)p.input_line)
@@ -511,10 +483,10 @@ __global__ void k_chroma_chain(ChromaFieldParams p) {
 
 // SummarizePhaseSequence of each field's kept sequence: one warp per field,
 // the normalised I/Q of every line in parallel, then the sums in line order.
-__global__ void __launch_bounds__(128) k_chroma_summary(ChromaFieldParams p) {
-    __shared__ double nrm[4][2][320];
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int f = blockIdx.x * 4 + w;
+__global__ void __launch_bounds__(32) k_chroma_summary(ChromaFieldParams p) {
+    __shared__ double nrm[1][3][320];   // I / mag, Q / mag, mag
+    const int w = 0, lane = threadIdx.x;
+    const int f = blockIdx.x;
     if (f >= p.nfields) return;
     const double* pr = p.probe + ((int64_t)f * 2 + p.chosen[f]) * p.out_lines * 5;
     const int end = p.out_lines + 1;
@@ -523,36 +495,47 @@ __global__ void __launch_bounds__(128) k_chroma_summary(ChromaFieldParams p) {
         const double mag = pr[k * 5 + 2];
         nrm[w][0][k] = mag != 0.0 ? __ddiv_rn(pr[k * 5 + 3], mag) : 0.0;
         nrm[w][1][k] = mag != 0.0 ? __ddiv_rn(pr[k * 5 + 4], mag) : 0.0;
+        nrm[w][2][k] = mag;
     }
     __syncwarp();
-    if (lane != 0) return;
-    double ei = 0.0, eq = 0.0, oi = 0.0, oq = 0.0, msum = 0.0;
+    // Five ordered sums in line order, each in its own lane (lane 0: even-line
+    // I, 1: even Q, 2: odd I, 3: odd Q, 4: magnitudes), so one binary64 add per
+    // line serves all five chains.  The values come from shared memory only.
+    const bool used = lane < 5;
+    const int comp = lane == 4 ? 2 : (lane & 1);    // nrm row
+    const int parity = lane < 2 ? 0 : 1;            // even lines: lanes 0, 1; odd: 2, 3
+    double acc = 0.0;
     int count = 0;
-    for (int k = 0; k < nl; k++) {
-        const int line = k + 1;
-        const double mag = pr[k * 5 + 2];
-        if (line <= 16 || line >= end - 16 || mag == 0.0) continue;
-        count++;
-        msum = __dadd_rn(msum, mag);
-        if (line & 1) {
-            oi = __dadd_rn(oi, nrm[w][0][k]);
-            oq = __dadd_rn(oq, nrm[w][1][k]);
-        } else {
-            ei = __dadd_rn(ei, nrm[w][0][k]);
-            eq = __dadd_rn(eq, nrm[w][1][k]);
+    if (used) {
+        for (int k = 0; k < nl; k++) {
+            const int line = k + 1;
+            const double mag = nrm[w][2][k];
+            if (line <= 16 || line >= end - 16 || mag == 0.0) continue;
+            count++;
+            if (lane == 4 || (line & 1) == parity) acc = __dadd_rn(acc, nrm[w][comp][k]);
         }
     }
+    const double ei = __shfl_sync(kFull, acc, 0), eq = __shfl_sync(kFull, acc, 1);
+    const double oi = __shfl_sync(kFull, acc, 2), oq = __shfl_sync(kFull, acc, 3);
+    const double msum = __shfl_sync(kFull, acc, 4);
+    count = __shfl_sync(kFull, count, 4);
     double* o = p.summary + (int64_t)f * 4;
     if (count == 0) {
-        atomicExch(p.status, 1);
-        o[0] = o[1] = o[2] = o[3] = 0.0;
+        if (lane == 0) {
+            atomicExch(p.status, 1);
+            o[0] = o[1] = o[2] = o[3] = 0.0;
+        }
         return;
     }
+    // the three phase averages in three lanes
     const double k180 = 180.0, pi = 3.141592653589793;
-    o[0] = positive_degrees(__ddiv_rn(__dmul_rn(atan2(__dadd_rn(eq, oq), __dadd_rn(ei, oi)), k180), pi));
-    o[1] = positive_degrees(__ddiv_rn(__dmul_rn(atan2(eq, ei), k180), pi));
-    o[2] = positive_degrees(__ddiv_rn(__dmul_rn(atan2(oq, oi), k180), pi));
-    o[3] = __ddiv_rn(msum, (double)count);
+    if (lane < 3) {
+        const double y = lane == 0 ? __dadd_rn(eq, oq) : lane == 1 ? eq : oq;
+        const double x = lane == 0 ? __dadd_rn(ei, oi) : lane == 1 ? ei : oi;
+        o[lane] = positive_degrees(__ddiv_rn(__dmul_rn(atan2(y, x), k180), pi));
+    } else if (lane == 3) {
+        o[3] = __ddiv_rn(msum, (double)count);
+    }
 }
 
 // RefineLineLocationsFromBurst (v0.4.0) from sequence index 9 on, then the
@@ -580,132 +563,200 @@ __global__ void k_chroma_refine(ChromaFieldParams p) {
 
 // ---------------------------------------------------------------- field decode
 
-// Up-conversion of one output line.  PAL: the line written by sequence entry
-// L (NumPy slice of line L - first_line, negative indices from the end; the
-// one that lands on -1 is empty) times the heterodyne of its rotation.  NTSC:
-// the burst de-emphasis (x2 from burst end + 5) and the phase-compensated
-// carrier -cos(theta), theta advanced per sample as the reference's four
-// lanes do (closed form; cosine in float after an exact turn reduction).
+// Knuth's TwoSum: s + e == a + b exactly.
+__device__ __forceinline__ void two_sum_f(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+
+// The sequence line L written to output line o (-1: none).  PAL follows the
+// NumPy slice of line L - first_line with negative indices from the end; the
+// one that lands on -1 is empty.
+__device__ __forceinline__ int upconvert_source_line(const ChromaFieldParams& p, int o, int ofl) {
+    int L;
+    if (o <= p.out_lines - ofl) L = o + ofl;
+    else if (o >= p.out_lines + 1 - ofl && o < p.out_lines - 1) L = o + ofl - p.out_lines;
+    else L = -1;
+    return (L < 1 || L > p.out_lines) ? -1 : L;
+}
+
+// NTSC, one lane per output line: the carrier phase theta at the line start
+// (the reference's binary64 expression, reduced by whole turns) and its
+// (cos, sin).  One lane per line keeps the binary64 work to one warp
+// instruction per 32 lines.
+__global__ void __launch_bounds__(128) k_chroma_up_lines(ChromaFieldParams p) {
+    const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (!p.ntsc || id >= (int64_t)p.nfields * p.out_lines) return;
+    const int f = (int)(id / p.out_lines), o = (int)(id % p.out_lines);
+    const int ofl = p.first_line[f];
+    const int L = upconvert_source_line(p, o, ofl);
+    if (L < 0) {
+        p.line_cs[id] = make_float2(1.0f, 0.0f);
+        return;
+    }
+    const int c = p.chosen[f];
+    const int rot = positive_mod4((c == 0 ? p.rot0 : p.rot1) * L);
+    const double* pr = p.probe + ((int64_t)f * 2 + c) * p.out_lines * 5 + (int64_t)(L - 1) * 5;
+    const double half_pi = 1.5707963267948966, deg = 0.017453292519943295;
+    // NtscFieldPhaseTarget (:3915-3925): -33 degrees in the first colour frame
+    // of the four-field sequence, 147 in the second, whatever the parity
+    const bool second = ((p.field_number[f] / 2) & 1) == 1;
+    const double target = second ? 147.0 : -33.0;
+    const int64_t ls = (int64_t)(L - ofl) * p.outlen;
+    double theta = __fma_rn((double)ls, p.ntsc_h, (double)rot * half_pi);
+    theta = __fma_rn(__dadd_rn(target, pr[0]), deg, theta);
+    const double two_pi = 6.283185307179586, inv_two_pi = 0.15915494309189535;
+    const double t0 = __fma_rn(-rint(__dmul_rn(theta, inv_two_pi)), two_pi, theta);
+    double sn, cs;
+    sincos(t0, &sn, &cs);
+    p.line_cs[id] = make_float2(__double2float_rn(cs), __double2float_rn(sn));
+}
+
+// Up-conversion of one output line.  PAL: the sequence line times the
+// heterodyne of its rotation.  NTSC: the burst de-emphasis (x2 from burst end
+// + 5) times the phase-compensated carrier -cos(theta_line + a_k), taken as
+// -(cos theta_line cos a_k - sin theta_line sin a_k) from the line's and the
+// per-sample (cos, sin); the reference multiplies by the binary64 cosine and
+// rounds to float, which this agrees with to a few float ulps.
 __global__ void __launch_bounds__(256) k_chroma_upconvert(ChromaFieldParams p) {
     const int f = blockIdx.y;
     const int o = blockIdx.x;
     const int64_t field = (int64_t)p.out_lines * p.outlen;
     const int ofl = p.first_line[f];
     const float* src = p.cfield + (int64_t)f * field + (int64_t)o * p.outlen;
-    float* dst = p.up + (int64_t)f * field + (int64_t)o * p.outlen;
-    int L;
-    if (o <= p.out_lines - ofl) L = o + ofl;
-    else if (o >= p.out_lines + 1 - ofl && o < p.out_lines - 1) L = o + ofl - p.out_lines;
-    else L = -1;
-    if (L < 1 || L > p.out_lines) {
+    float* dst = p.up + (int64_t)f * p.crow + p.fin.edge + (int64_t)o * p.outlen;
+    const int L = upconvert_source_line(p, o, ofl);
+    if (L < 0) {
         for (int k = threadIdx.x; k < p.outlen; k += blockDim.x) dst[k] = 0.0f;
         return;
     }
-    const int c = p.chosen[f];
-    const int rot = positive_mod4((c == 0 ? p.rot0 : p.rot1) * L);
     if (!p.ntsc) {
+        const int c = p.chosen[f];
+        const int rot = positive_mod4((c == 0 ? p.rot0 : p.rot1) * L);
         const float* het = p.het + (int64_t)rot * field + (int64_t)o * p.outlen;
         for (int k = threadIdx.x; k < p.outlen; k += blockDim.x) dst[k] = __fmul_rn(src[k], het[k]);
         return;
     }
-    const double* pr = p.probe + ((int64_t)f * 2 + c) * p.out_lines * 5 + (int64_t)(L - 1) * 5;
-    const double half_pi = 1.5707963267948966, deg = 0.017453292519943295;
-    const double h = p.ntsc_h;
-    (void)h;
-    // NtscFieldPhaseTarget (:3915-3925): -33 degrees in the first colour frame
-    // of the four-field sequence, 147 in the second, whatever the parity
-    const bool second = ((p.field_number[f] / 2) & 1) == 1;
-    const double target = second ? 147.0 : -33.0;
-    const int64_t ls = (int64_t)(L - ofl) * p.outlen;
-    double theta = __fma_rn((double)ls, h, (double)rot * half_pi);
-    theta = __fma_rn(__dadd_rn(target, pr[0]), deg, theta);
+    const float2 cs = p.line_cs[(int64_t)f * p.out_lines + o];
     const int first_doubled = p.be + 5;
-    const double two_pi = 6.283185307179586, inv_two_pi = 0.15915494309189535;
-    // the line's start phase reduced by whole turns; each sample's advance
-    // (the reference's four-lane theta steps, reduced the same way) is a table
-    const double t0 = __fma_rn(-rint(__dmul_rn(theta, inv_two_pi)), two_pi, theta);
     for (int k = threadIdx.x; k < p.outlen; k += blockDim.x) {
-        const float carrier = -cosf((float)__dadd_rn(t0, p.ntsc_advance[k]));
+        const float2 a = p.ntsc_advance[k];
+        const float carrier = __fsub_rn(__fmul_rn(cs.y, a.y), __fmul_rn(cs.x, a.x));
         float v = src[k];
         if (k >= first_doubled) v = __fmul_rn(v, 2.0f);   // burst de-emphasis, exact
-        // the reference multiplies by the binary64 cosine and rounds to float;
-        // with the float cosine the product agrees to float rounding
         dst[k] = __fmul_rn(v, carrier);
     }
 }
 
-// Final band-pass, forward: one 4-lane group per 1024-sample chunk of the odd
-// extension of a field's up-converted chroma; chunks past the first
-// kWarmup samples start kWarmup early from zero state.
-__global__ void __launch_bounds__(32 * kIirWarps) k_chroma_final_fwd(ChromaFieldParams p, int64_t chunks_per_field) {
-    __shared__ __align__(16) float tiles[kIirWarps * kGroupsPerWarp * kCascadeArea];
-    const int lane = threadIdx.x & 31, s = lane & 3, g = lane >> 2;
-    const int64_t gid = ((int64_t)blockIdx.x * kIirWarps + (threadIdx.x >> 5)) * kGroupsPerWarp + g;
+// The odd extension of each field's up-converted chroma in its row: edge
+// samples before the field (2 x[0] - x[edge - e]) and after it, so the
+// forward pass of the final band-pass reads one plain sequence.
+__global__ void __launch_bounds__(64) k_chroma_extend(ChromaFieldParams p) {
+    const int f = blockIdx.x;
+    const int field = p.out_lines * p.outlen;
+    const int edge = p.fin.edge;
+    float* row = p.up + (int64_t)f * p.crow;
+    const float first = row[edge], last = row[edge + field - 1];
+    for (int e = threadIdx.x; e < edge; e += blockDim.x) {
+        row[e] = __fsub_rn(__fmul_rn(2.0f, first), row[2 * edge - e]);
+        row[edge + field + e] = __fsub_rn(__fmul_rn(2.0f, last), row[edge + field - 2 - e]);
+    }
+}
+
+// The final band-pass over the odd-extended field, E = field + 2 edge
+// samples, in chunks of kChunk samples each started kWarmup samples early
+// from zero state (the first from the reference's initial state), one lane
+// per chunk (LaneCascade).  kFwd: the forward pass over the extended row of
+// up, written in reverse order into fwd; else the backward pass, i.e. the
+// same recurrence over that reversed sequence, written back in reverse into
+// up at the field's samples.  Sample t of a pass's sequence lands at row
+// position E - 1 - t.  A lane's tiles of 32 samples are whole 128-byte lines
+// (chunk starts are multiples of 32), read with 16-byte loads a tile ahead
+// into registers; outputs leave in 16-byte stores, aligned for kM = E mod 4.
+// One copy of the tile body keeps the loop in the instruction cache.
+template <bool kFwd, int kM>
+__global__ void __launch_bounds__(128) k_chroma_final(ChromaFieldParams p, int chunks_per_field) {
+    const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const bool active = gid < (int64_t)p.nfields * chunks_per_field;
     const int64_t q = active ? gid : 0;
     const int f = (int)(q / chunks_per_field);
-    const int64_t ch = q % chunks_per_field;
-    float* tile = tiles + ((threadIdx.x >> 5) * kGroupsPerWarp + g) * kCascadeArea;
-    const int64_t field = (int64_t)p.out_lines * p.outlen;
+    const int ch = (int)(q % chunks_per_field);
+    const int field = p.out_lines * p.outlen;
     const int edge = p.fin.edge;
-    const int64_t E = field + 2 * edge;
-    const float* x = p.up + (int64_t)f * field;
-    float* fwd = p.fwd + (int64_t)f * E;
-    const float first = x[0], last = x[field - 1];
-    auto fetch_e = [&](int64_t e) -> uint32_t {
-        const int64_t i = e < edge ? edge - e : (e < edge + field ? e - edge : field - 2 - (e - edge - field));
-        return f_bits(x[i]);
+    const int E = field + 2 * edge;
+    const float* src = (kFwd ? p.up : p.fwd) + (int64_t)f * p.crow;
+    float* dst = (kFwd ? p.fwd : p.up) + (int64_t)f * p.crow;
+    const int c0 = ch * kChunk, c1 = min(E, c0 + kChunk);
+    const int start = c0 <= kWarmup ? 0 : c0 - kWarmup;
+    const int n = active ? c1 - start : 0;
+    // outputs kept: sequence samples [lo, hi) of this lane's run
+    int lo = c0 - start, hi = c1 - start;
+    if (!kFwd) {
+        lo = max(c0, edge) - start;
+        hi = min(c1, E - edge) - start;
+    }
+    if (!active) hi = lo;
+    const float* run = src + start;
+    LaneCascade lc;
+    lc.init(p.fin, start != 0 ? 0.0f : run[0]);
+    const int ntile = __reduce_max_sync(kFull, (n + 3 + 31) / 32);
+    constexpr int JH = (kM + 2) & 3;   // top sample of each aligned group of four outputs
+    constexpr int NC = 3 - JH;         // outputs carried into the next tile's first group
+    float cr[3] = {0.0f, 0.0f, 0.0f};
+    // a lane touches no tile past its own run (steps up to n + 2), so every
+    // access stays inside its row (crow >= E + 64)
+    auto has = [&](int k) { return 32 * k <= n + 2; };
+    auto load = [&](int k, float (&x)[32]) {
+        if (has(k)) {
+            const float4* in4 = reinterpret_cast<const float4*>(run + 32 * k);
+#pragma unroll
+            for (int g = 0; g < 8; g++) {
+                const float4 v = in4[g];
+                x[4 * g] = v.x; x[4 * g + 1] = v.y; x[4 * g + 2] = v.z; x[4 * g + 3] = v.w;
+            }
+        }
     };
-    auto cook_e = [&](uint32_t raw, int64_t e) -> float {
-        if (e < edge) return __fsub_rn(__fmul_rn(2.0f, first), as_f(raw));
-        if (e < edge + field) return as_f(raw);
-        return __fsub_rn(__fmul_rn(2.0f, last), as_f(raw));
-    };
-    const int64_t c0 = ch * kChunk, c1 = min(E, c0 + kChunk);
-    const int64_t start = c0 <= kWarmup ? 0 : c0 - kWarmup;
-    const int64_t len = active ? c1 - start : 0;
-    const float x0 = start == 0 ? cook_e(fetch_e(0), 0) : 0.0f;
-    cascade(p.fin, s, tile, (int64_t)kChunk + kWarmup + 3 * kTile, len, x0,
-            [&](int64_t i) { return fetch_e(start + i); },
-            [&](uint32_t raw, int64_t i) { return cook_e(raw, start + i); },
-            [&](int64_t i, float v) {
-                if (start + i >= c0) fwd[start + i] = v;
-            });
+    float x[32], nx[32];
+#pragma unroll
+    for (int j = 0; j < 32; j++) x[j] = nx[j] = 0.0f;
+    load(0, x);
+    for (int k = 0; k < ntile; k++) {
+        load(k + 1, nx);   // a tile ahead: in flight while this tile runs
+        int j0 = 0;
+        if (k == 0) {
+            lc.prime(p.fin, x[0], x[1], x[2]);
+            x[0] = x[1] = x[2] = 0.0f;
+            j0 = 3;
+        }
+        // x[j] becomes the output of sample 32 k + j - 3
+#pragma unroll
+        for (int j = 0; j < 32; j++)
+            if (j >= j0) x[j] = lc.step(p.fin, x[j]);
+#pragma unroll
+        for (int g = 0; JH + 4 * g <= 31; g++) {
+            const int jt = JH + 4 * g;
+            float v[4];
+#pragma unroll
+            for (int m = 0; m < 4; m++) v[m] = jt - m >= 0 ? x[jt - m] : cr[NC + jt - m];
+            const int ut = 32 * k + jt - 3;   // the group's samples ut - 3 .. ut
+            float* d = dst + (E - 1 - start - ut);
+            if (ut - 3 >= lo && ut < hi) {
+                *reinterpret_cast<float4*>(d) = make_float4(v[0], v[1], v[2], v[3]);
+            } else if (ut >= lo && ut - 3 < hi) {
+#pragma unroll
+                for (int m = 0; m < 4; m++)
+                    if (ut - m >= lo && ut - m < hi) d[m] = v[m];
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < NC; i++) cr[i] = x[32 - NC + i];
+#pragma unroll
+        for (int j = 0; j < 32; j++) x[j] = nx[j];
+    }
 }
 
-// Final band-pass, backward over the forward output, chunks started kWarmup
-// late from zero state except the last; the output samples land in `up`.
-__global__ void __launch_bounds__(32 * kIirWarps) k_chroma_final_bwd(ChromaFieldParams p, int64_t chunks_per_field) {
-    __shared__ __align__(16) float tiles[kIirWarps * kGroupsPerWarp * kCascadeArea];
-    const int lane = threadIdx.x & 31, s = lane & 3, g = lane >> 2;
-    const int64_t gid = ((int64_t)blockIdx.x * kIirWarps + (threadIdx.x >> 5)) * kGroupsPerWarp + g;
-    const bool active = gid < (int64_t)p.nfields * chunks_per_field;
-    const int64_t q = active ? gid : 0;
-    const int f = (int)(q / chunks_per_field);
-    const int64_t ch = q % chunks_per_field;
-    float* tile = tiles + ((threadIdx.x >> 5) * kGroupsPerWarp + g) * kCascadeArea;
-    const int64_t field = (int64_t)p.out_lines * p.outlen;
-    const int edge = p.fin.edge;
-    const int64_t E = field + 2 * edge;
-    const float* fwd = p.fwd + (int64_t)f * E;
-    float* y = p.up + (int64_t)f * field;
-    const int64_t c0 = ch * kChunk, c1 = min(E, c0 + kChunk);
-    const int64_t stop = c1 + kWarmup >= E ? E : c1 + kWarmup;   // exclusive upper end of the pass
-    const int64_t len = active ? stop - c0 : 0;
-    const float x0 = stop == E ? fwd[E - 1] : 0.0f;
-    cascade(p.fin, s, tile, (int64_t)kChunk + kWarmup + 3 * kTile, len, x0,
-            [&](int64_t i) { return f_bits(fwd[stop - 1 - i]); }, [](uint32_t raw, int64_t) { return as_f(raw); },
-            [&](int64_t i, float v) {
-                const int64_t e = stop - 1 - i;
-                if (e < c1 && e >= edge && e < edge + field) y[e - edge] = v;
-            });
-}
-
-__device__ __forceinline__ void two_sum_f(float a, float b, float& s, float& e) {
-    s = __fadd_rn(a, b);
-    const float bb = __fsub_rn(s, a);
-    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
-}
 
 __device__ __forceinline__ uint16_t u16_saturate(double shifted) {
     if (!isfinite(shifted) || shifted <= 0.0) return 0;
@@ -719,59 +770,116 @@ __device__ __forceinline__ uint16_t u16_wrap(double shifted) {
     return (uint16_t)(uint64_t)(int64_t)shifted;
 }
 
-// ApplyAutomaticChromaGainWithCombToU16: lines below 16 neutral; from line 16
-// the comb of the line with the lines `dist` before and after it (not for the
-// last two lines), scaled so its burst RMS is burst_abs_ref.
+// uint16 of (double)v * scale + 32767 as the reference converts it (saturated,
+// truncated).  The value is formed as a float pair (Dekker's product of v and
+// scale split into two floats, then TwoSum with 32767): it differs from the
+// binary64 value by < 1e-9 for every in-range sample, so the floor is the
+// same unless the value lies within 1e-6 of an integer; those samples and
+// non-finite inputs take the binary64 path.
+__device__ __forceinline__ uint16_t gain_u16(float v, float sh, float sl, double scale) {
+    if (isfinite(v)) {
+        const float ph = __fmul_rn(v, sh);
+        const float pl = __fmaf_rn(v, sl, __fmaf_rn(v, sh, -ph));
+        float s, e;
+        two_sum_f(ph, 32767.0f, s, e);
+        const float lo = __fadd_rn(e, pl);
+        const float hi = __fadd_rn(s, lo);
+        const float lo2 = __fsub_rn(lo, __fsub_rn(hi, s));
+        const float r = rintf(hi);
+        const float d = __fadd_rn(__fsub_rn(hi, r), lo2);   // value - r
+        if (fabsf(d) > 1e-6f && fabsf(hi) < 1e9f) {
+            const float fl = d > 0.0f ? r : __fsub_rn(r, 1.0f);
+            return (uint16_t)fminf(fmaxf(fl, 0.0f), 65535.0f);
+        }
+    }
+    return u16_saturate(__dadd_rn(__dmul_rn((double)v, scale), 32767.0));
+}
+
+// The comb of output line o at sample k: ((2 cur - adv) - del) / 4 with the
+// lines `dist` after and before it (not for the last two lines).  The
+// reference sums these floats in binary64, where the sum is exact, and rounds
+// to float: the exact sum as a float pair (two TwoSums) rounded once; / 4 is
+// exact.
+__device__ __forceinline__ float comb_at(const float* x, int o, int k, const ChromaFieldParams& p) {
+    const float* cur = x + (int64_t)o * p.outlen;
+    if (o >= p.out_lines - 2) return cur[k];
+    const int dist = p.ntsc ? 1 : 2;
+    const float adv = x[(int64_t)(o + dist) * p.outlen + k], del = x[(int64_t)(o - dist) * p.outlen + k];
+    float s1, e1, s2, e2;
+    two_sum_f(__fmul_rn(cur[k], 2.0f), -adv, s1, e1);
+    two_sum_f(s1, -del, s2, e2);
+    return __fmul_rn(__fadd_rn(s2, __fadd_rn(e1, e2)), 0.25f);
+}
+
+// ApplyAutomaticChromaGainWithCombToU16, per line from 16: the RMS of the
+// combed burst window (RmsFloat32, VhsChromaDecoder.cs:4400-4423, in its
+// order) and the scale that brings it to burst_abs_ref, in binary64 and as a
+// float pair.  A warp takes 32 lines: the combed windows of all of them
+// together (independent loads), then each lane the ordered sums and the
+// binary64 division of its own line.
+constexpr int kBurstMax = 64;   // burst window samples (PAL 56, NTSC 52)
+__global__ void __launch_bounds__(32) k_chroma_gain_lines(ChromaFieldParams p) {
+    __shared__ float comb[32][kBurstMax + 1];
+    const int lane = threadIdx.x;
+    const int64_t total = (int64_t)p.nfields * p.out_lines;
+    const int64_t id0 = (int64_t)blockIdx.x * 32;
+    const int n = p.be - p.bs;
+    {
+        const int nj = (int)min((int64_t)32, total - id0);
+        const int f0 = (int)(id0 / p.out_lines), o0 = (int)(id0 % p.out_lines);
+        int j = 0, k = lane;   // element e = j * n + k
+        for (int e = lane; e < nj * n; e += 32) {
+            while (k >= n) {
+                k -= n;
+                j++;
+            }
+            int f = f0, o = o0 + j;   // 32 lines cross at most one field end
+            if (o >= p.out_lines) {
+                o -= p.out_lines;
+                f++;
+            }
+            if (o >= 16) comb[j][k] = comb_at(p.up + (int64_t)f * p.crow + p.fin.edge, o, p.bs + k, p);
+            k += 32;
+        }
+    }
+    __syncwarp();
+    const int64_t id = id0 + lane;
+    if (id >= total || (int)(id % p.out_lines) < 16) return;
+    float mean = 0.0f;
+    for (int k = 0; k < n; k++) mean = __fadd_rn(mean, comb[lane][k]);
+    mean = __fdiv_rn(mean, (float)n);
+    float ss = 0.0f;
+    for (int k = 0; k < n; k++) {
+        const float c = __fsub_rn(comb[lane][k], mean);
+        ss = __fadd_rn(ss, __fmul_rn(c, c));
+    }
+    const float rms = n > 0 ? __fsqrt_rn(__fdiv_rn(ss, (float)n)) : 0.0f;
+    const double scale = rms != 0.0f ? __ddiv_rn(p.burst_abs_ref, (double)rms) : 1.0;
+    const float sh = __double2float_rn(scale);
+    p.line_scale[id] = scale;
+    p.line_scale_f[id] = make_float2(sh, __double2float_rn(__dsub_rn(scale, (double)sh)));
+}
+
+// The uint16 chroma: lines below 16 neutral (32767), the others combed and
+// scaled by their line's gain.
 __global__ void __launch_bounds__(256) k_chroma_gain(ChromaFieldParams p) {
-    extern __shared__ float line[];
-    __shared__ double scale_s;
     const int f = blockIdx.y, o = blockIdx.x;
     const int64_t field = (int64_t)p.out_lines * p.outlen;
-    const float* x = p.up + (int64_t)f * field;
+    const float* x = p.up + (int64_t)f * p.crow + p.fin.edge;
     uint16_t* out = p.out + (int64_t)f * field + (int64_t)o * p.outlen;
     if (o < 16) {
         for (int k = threadIdx.x; k < p.outlen; k += blockDim.x) out[k] = 32767;
         return;
     }
-    const int dist = p.ntsc ? 1 : 2;
-    const float* cur = x + (int64_t)o * p.outlen;
-    if (o < p.out_lines - 2) {
-        const float* adv = x + (int64_t)(o + dist) * p.outlen;
-        const float* del = x + (int64_t)(o - dist) * p.outlen;
-        for (int k = threadIdx.x; k < p.outlen; k += blockDim.x) {
-            // ((2 cur - adv) - del) / 4 rounded to float: the binary64 sum of
-            // these floats is exact, so take the exact sum as a float pair
-            // (two TwoSums) and round it once; / 4 is exact
-            float s1, e1, s2, e2;
-            two_sum_f(__fmul_rn(cur[k], 2.0f), -adv[k], s1, e1);
-            two_sum_f(s1, -del[k], s2, e2);
-            line[k] = __fmul_rn(__fadd_rn(s2, __fadd_rn(e1, e2)), 0.25f);
-        }
-    } else {
-        for (int k = threadIdx.x; k < p.outlen; k += blockDim.x) line[k] = cur[k];
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        // RmsFloat32 (VhsChromaDecoder.cs:4400-4423)
-        const int n = p.be - p.bs;
-        float mean = 0.0f;
-        for (int k = 0; k < n; k++) mean = __fadd_rn(mean, line[p.bs + k]);
-        mean = __fdiv_rn(mean, (float)n);
-        float ss = 0.0f;
-        for (int k = 0; k < n; k++) {
-            float c = __fsub_rn(line[p.bs + k], mean);
-            ss = __fadd_rn(ss, __fmul_rn(c, c));
-        }
-        const float rms = n > 0 ? __fsqrt_rn(__fdiv_rn(ss, (float)n)) : 0.0f;
-        scale_s = rms != 0.0f ? __ddiv_rn(p.burst_abs_ref, (double)rms) : 1.0;
-    }
-    __syncthreads();
-    const double scale = scale_s;
+    const int64_t id = (int64_t)f * p.out_lines + o;
+    const double scale = p.line_scale[id];
+    const float2 sp = p.line_scale_f[id];
     const int64_t vec_len = field & ~(int64_t)3;
     for (int k = threadIdx.x; k < p.outlen; k += blockDim.x) {
-        const double shifted = __dadd_rn(__dmul_rn((double)line[k], scale), 32767.0);
+        const float v = comb_at(x, o, k, p);
         const int64_t gi = (int64_t)o * p.outlen + k;
-        out[k] = gi < vec_len ? u16_saturate(shifted) : u16_wrap(shifted);
+        out[k] = gi < vec_len ? gain_u16(v, sp.x, sp.y, scale)
+                              : u16_wrap(__dadd_rn(__dmul_rn((double)v, scale), 32767.0));
     }
 }
 
@@ -791,28 +899,45 @@ cudaError_t launch_chroma_blocks(const ChromaBlockParams& p, cudaStream_t s) {
 cudaError_t launch_chroma_phase(const ChromaFieldParams& p, cudaStream_t s) {
     if (p.nfields <= 0) return cudaSuccess;
     const int64_t nprobe = (int64_t)p.nfields * 2 * p.out_lines;
-    const int groups = 16;   // 64 threads
-    const size_t smem = (size_t)groups * (((p.win + 2 * p.fin.edge + 3) & ~3) + kCascadeArea) * sizeof(float);
-    k_chroma_probe<<<(unsigned)((nprobe + groups - 1) / groups), groups * 4, smem, s>>>(p);
+    const size_t smem = (size_t)32 * ((p.win + 2 * p.fin.edge) | 1) * sizeof(float);
+    // all of the SM's shared memory for the probe rows: the warps of a decode
+    // then fit in one wave
+    static const cudaError_t carve =
+        cudaFuncSetAttribute(k_chroma_probe, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    if (carve != cudaSuccess) return carve;
+    k_chroma_probe<<<(unsigned)((nprobe + 31) / 32), 32, smem, s>>>(p);
     k_chroma_flip<<<(unsigned)(p.nfields * 2), 128, 0, s>>>(p);
     k_chroma_chain<<<1, 1, 0, s>>>(p);
-    k_chroma_summary<<<(unsigned)((p.nfields + 3) / 4), 128, 0, s>>>(p);
+    // one warp per field, each on its own SM: the binary64 divisions and
+    // ordered sums share an SM's few FP64 units with nothing else
+    k_chroma_summary<<<(unsigned)p.nfields, 32, 0, s>>>(p);
     k_chroma_refine<<<(unsigned)p.nfields, 256, 0, s>>>(p);
     return cudaGetLastError();
 }
 
 cudaError_t launch_chroma_decode(const ChromaFieldParams& p, cudaStream_t s) {
     if (p.nfields <= 0) return cudaSuccess;
+    if (p.be - p.bs > kBurstMax || p.be <= p.bs) return cudaErrorInvalidValue;
     dim3 lines(p.out_lines, p.nfields);
+    const unsigned line_grid = (unsigned)(((int64_t)p.nfields * p.out_lines + 127) / 128);
+    k_chroma_up_lines<<<line_grid, 128, 0, s>>>(p);   // NTSC only (returns at once for PAL)
     k_chroma_upconvert<<<lines, 256, 0, s>>>(p);
     const int64_t field = (int64_t)p.out_lines * p.outlen;
-    const int64_t chunks = (field + 2 * p.fin.edge + kChunk - 1) / kChunk;
-    const int64_t groups = (int64_t)p.nfields * chunks;
-    const int64_t per_cta = (int64_t)kIirWarps * kGroupsPerWarp;
-    const unsigned grid = (unsigned)((groups + per_cta - 1) / per_cta);
-    k_chroma_final_fwd<<<grid, 32 * kIirWarps, 0, s>>>(p, chunks);
-    k_chroma_final_bwd<<<grid, 32 * kIirWarps, 0, s>>>(p, chunks);
-    k_chroma_gain<<<lines, 256, (size_t)p.outlen * sizeof(float), s>>>(p);
+    const int64_t E = field + 2 * p.fin.edge;
+    const int chunks = (int)((E + kChunk - 1) / kChunk);
+    const unsigned grid = (unsigned)(((int64_t)p.nfields * chunks + 127) / 128);
+    if (p.crow != chroma_final_row(field, p.fin.edge) || (reinterpret_cast<uintptr_t>(p.up) & 15u) != 0 ||
+        (reinterpret_cast<uintptr_t>(p.fwd) & 15u) != 0 || E > (int64_t)1 << 30)
+        return cudaErrorInvalidValue;
+    k_chroma_extend<<<(unsigned)p.nfields, 64, 0, s>>>(p);
+    switch ((int)(E & 3)) {
+    case 0: k_chroma_final<true, 0><<<grid, 128, 0, s>>>(p, chunks); k_chroma_final<false, 0><<<grid, 128, 0, s>>>(p, chunks); break;
+    case 1: k_chroma_final<true, 1><<<grid, 128, 0, s>>>(p, chunks); k_chroma_final<false, 1><<<grid, 128, 0, s>>>(p, chunks); break;
+    case 2: k_chroma_final<true, 2><<<grid, 128, 0, s>>>(p, chunks); k_chroma_final<false, 2><<<grid, 128, 0, s>>>(p, chunks); break;
+    default: k_chroma_final<true, 3><<<grid, 128, 0, s>>>(p, chunks); k_chroma_final<false, 3><<<grid, 128, 0, s>>>(p, chunks); break;
+    }
+    k_chroma_gain_lines<<<(unsigned)(((int64_t)p.nfields * p.out_lines + 31) / 32), 32, 0, s>>>(p);
+    k_chroma_gain<<<lines, 256, 0, s>>>(p);
     return cudaGetLastError();
 }
 

@@ -270,15 +270,25 @@ struct ChromaFieldParams {
     const int* first_field;     // [nfields] 1: first field
     const int* field_number;    // [nfields] VHS field number (NTSC colour frame)
     const float* cfield;        // [nfields * field] chroma TBC of the output lines
-    float* up;                  // [nfields * field] up-converted, then band-passed in place
-    float* fwd;                 // [nfields * (field + 2 fin.edge)] forward pass
+    float* up;                  // [nfields * crow] up-converted field at offset fin.edge of each
+                                //   row, then the band-passed field in the same place
+    float* fwd;                 // [nfields * crow] forward pass, in reverse order
+    int64_t crow;               // row stride of up and fwd: chroma_final_row(field, fin.edge)
     uint16_t* out;              // [nfields * field] uint16 chroma
     double cu_hz, fsc_mhz, burst_abs_ref;
     double ntsc_h;              // NTSC up-conversion carrier step (rad / output sample)
-    const double* ntsc_advance; // [outlen] carrier phase advance of sample k of a line, mod 2 pi
+    const float2* ntsc_advance; // [outlen] (cos, sin) of the carrier phase advance of sample k of a line
+    float2* line_cs;            // [nfields * out_lines] NTSC: (cos, sin) of the carrier phase at the line start
+    double* line_scale;         // [nfields * out_lines] gain scale of the line (lines from 16)
+    float2* line_scale_f;       //   the same as a float pair
 };
 constexpr int kChromaPhaseKernels = 5;    // probes, flips, rotation chain, averages, refinement
-constexpr int kChromaDecodeKernels = 4;   // up-conversion, forward, backward, gain
+constexpr int kChromaDecodeKernels = 7;   // line phases, up-conversion, extension, forward, backward,
+                                          // line gains, gain
+// Row of the final band-pass buffers: the odd-extended field (field + 2 edge
+// samples) rounded up to whole 32-float tiles, plus the tiles a pass reads
+// past its end.
+inline int64_t chroma_final_row(int64_t field, int edge) { return (field + 2 * edge + 31) / 32 * 32 + 64; }
 cudaError_t launch_chroma_phase(const ChromaFieldParams& p, cudaStream_t stream);
 cudaError_t launch_chroma_decode(const ChromaFieldParams& p, cudaStream_t stream);
 
