@@ -349,6 +349,7 @@ void session_init(vhsdecode_gb300_session* s, const vhsdecode_gb300_session_conf
 // Chroma tables and buffers, made by the first decode that renders chroma.
 void ensure_chroma(vhsdecode_gb300_session* s) {
     if (s->chroma_alloc) return;
+    ck(prepare_chroma_kernels(), "chroma kernel attributes");
     s->cd = vhsd::design_chroma(s->fmt, s->fs);
     const vhsd::ChromaDesign& d = s->cd;
     if (2 * d.burst_start - d.burst_end < 0 || d.burst_start + d.burst_end > d.outlen ||

@@ -92,7 +92,8 @@ constexpr int kExtBatches = kChromaExt / 32 + (kChromaExt % 32 != 0);
 constexpr int kRingDepth = 8;                       // chunks in flight per block
 constexpr int kRingSlot = 128;                      // bytes: 32 floats or 32 int16
 constexpr int kRingBytes = kRingDepth * kRingSlot + 16;   // + 16: blocks start on different banks
-constexpr int kBlockGroups = 32;                    // blocks per CTA (4 warps of 8 groups)
+constexpr int kBlockGroups = 64;                    // blocks per CTA (8 warps of 8 groups): two warps per
+                                                    // scheduler, so the stage holds few SMs beside the demod
 static_assert(kChromaRowStride == kExtBatches * 32, "scratch rows hold whole chunks");
 
 __device__ __forceinline__ void cp_async16(uint32_t dst, const void* src) {
@@ -235,7 +236,7 @@ __device__ __forceinline__ void block_pass(const float (&sec)[6], float zi0, flo
 // One 4-lane group per RF block: the forward pass over the odd extension of
 // the block into its scratch row, then the backward pass in place.
 __global__ void __launch_bounds__(4 * kBlockGroups) k_chroma_block_iir(ChromaBlockParams p) {
-    __shared__ __align__(128) uint8_t rings[kBlockGroups * kRingBytes];
+    extern __shared__ __align__(128) uint8_t rings[];   // [kBlockGroups * kRingBytes]
     const int s = threadIdx.x & 3, g = threadIdx.x >> 2;
     const int64_t j = (int64_t)blockIdx.x * kBlockGroups + g;
     const bool active = j < p.nblocks;
@@ -885,13 +886,24 @@ __global__ void __launch_bounds__(256) k_chroma_gain(ChromaFieldParams p) {
 
 }  // namespace
 
+cudaError_t prepare_chroma_kernels() {
+    // the block stage's rings above the default 48 KB of shared memory; all of
+    // the SM's shared memory for the probe rows, so a decode's probe warps fit
+    // in one wave
+    cudaError_t e = cudaFuncSetAttribute(k_chroma_block_iir, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         kBlockGroups * kRingBytes);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(k_chroma_probe, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+}
+
 cudaError_t launch_chroma_blocks(const ChromaBlockParams& p, cudaStream_t s) {
     if (p.nblocks <= 0) return cudaSuccess;
     if (p.c.edge != kChromaEdge || (!p.rf32 && !p.rf16) ||
         (reinterpret_cast<uintptr_t>(p.rf32 ? (const void*)p.rf32 : (const void*)p.rf16) & 15u) != 0 ||
         (reinterpret_cast<uintptr_t>(p.scratch) & 15u) != 0)
         return cudaErrorInvalidValue;
-    k_chroma_block_iir<<<(unsigned)((p.nblocks + kBlockGroups - 1) / kBlockGroups), 4 * kBlockGroups, 0, s>>>(p);
+    constexpr int smem = kBlockGroups * kRingBytes;   // opted in by prepare_chroma_kernels
+    k_chroma_block_iir<<<(unsigned)((p.nblocks + kBlockGroups - 1) / kBlockGroups), 4 * kBlockGroups, smem, s>>>(p);
     k_chroma_block_dc<<<(unsigned)p.nblocks, 32, 0, s>>>(p);
     return cudaGetLastError();
 }
@@ -900,11 +912,6 @@ cudaError_t launch_chroma_phase(const ChromaFieldParams& p, cudaStream_t s) {
     if (p.nfields <= 0) return cudaSuccess;
     const int64_t nprobe = (int64_t)p.nfields * 2 * p.out_lines;
     const size_t smem = (size_t)32 * ((p.win + 2 * p.fin.edge) | 1) * sizeof(float);
-    // all of the SM's shared memory for the probe rows: the warps of a decode
-    // then fit in one wave
-    static const cudaError_t carve =
-        cudaFuncSetAttribute(k_chroma_probe, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-    if (carve != cudaSuccess) return carve;
     k_chroma_probe<<<(unsigned)((nprobe + 31) / 32), 32, smem, s>>>(p);
     k_chroma_flip<<<(unsigned)(p.nfields * 2), 128, 0, s>>>(p);
     k_chroma_chain<<<1, 1, 0, s>>>(p);

@@ -238,6 +238,8 @@ struct ChromaBlockParams {
     float* out;                // stitched chroma stream
 };
 constexpr int kChromaBlockKernels = 2;
+// Kernel attributes of the chroma kernels (once per device, outside any capture).
+cudaError_t prepare_chroma_kernels();
 cudaError_t launch_chroma_blocks(const ChromaBlockParams& p, cudaStream_t stream);
 
 // Per-field chroma stages of a field batch (every array offset to the batch).
