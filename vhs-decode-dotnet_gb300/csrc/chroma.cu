@@ -18,10 +18,11 @@
 // refinement of the line locations (:2342-2428, v0.4.0 form); after the TBC of
 // the output lines, up-conversion (:2009-2248), the final float32
 // band-pass and the automatic gain with the comb to uint16 (:3480-3659).
-// The final band-pass runs on 1024-sample chunks, each started 448 samples
-// early from zero state (its poles are inside radius 0.94: the dropped
-// history weighs below 1e-12), so it equals the sequential filter to float
-// rounding rather than bit for bit.
+// The final band-pass runs on 512-sample chunks, each started 384 samples
+// early from zero state (the absolute sum of its impulse response beyond 384
+// samples is below 1e-11 for PAL and NTSC, so the dropped history weighs
+// under a thousandth of a float ulp), so it equals the sequential filter to
+// float rounding rather than bit for bit.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
@@ -32,8 +33,8 @@ namespace vhsd {
 namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
-constexpr int kChunk = 1024;       // final band-pass chunk
-constexpr int kWarmup = 448;       // zero-state lead of a chunk
+constexpr int kChunk = 512;        // final band-pass chunk (a multiple of 32)
+constexpr int kWarmup = 384;       // zero-state lead of a chunk (a multiple of 32)
 
 __device__ __forceinline__ float sos_step(const float* c, float v, float& z1, float& z2) {
     float f = __fadd_rn(__fmul_rn(c[0], v), z1);
