@@ -407,9 +407,15 @@ void ensure_chroma(vhsdecode_gb300_session* s) {
         ck(cudaMemcpy(s->c_advance.p, adv.data(), adv.size() * sizeof(float2), cudaMemcpyHostToDevice), "upload");
     }
     ck(cudaEventCreateWithFlags(&s->chroma_refined, cudaEventDisableTiming), "cudaEventCreate");
-    ck(cudaStreamCreateWithFlags(&s->chroma_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    // the block stage's stream has the highest priority: its CTAs take the
+    // first SMs that a finishing demod segment frees, ahead of the next
+    // segment's queued clusters
+    int least = 0, greatest = 0;
+    ck(cudaDeviceGetStreamPriorityRange(&least, &greatest), "cudaDeviceGetStreamPriorityRange");
+    ck(cudaStreamCreateWithPriority(&s->chroma_stream, cudaStreamNonBlocking, greatest), "cudaStreamCreate");
     ck(cudaEventCreateWithFlags(&s->chroma_go, cudaEventDisableTiming), "cudaEventCreate");
     ck(cudaEventCreateWithFlags(&s->chroma_done, cudaEventDisableTiming), "cudaEventCreate");
+    for (auto& e : s->chroma_t) ck(cudaEventCreate(&e), "cudaEventCreate");
     s->chroma_alloc = true;
 }
 
@@ -437,7 +443,9 @@ void launch_chroma_blocks_for(vhsdecode_gb300_session* s, const int16_t* rf16, i
 // runs beside the demodulator instead of after it.
 void queue_chroma_blocks(vhsdecode_gb300_session* s, const int16_t* rf16, int64_t nblocks, cudaEvent_t after) {
     ck(cudaStreamWaitEvent(s->chroma_stream, after, 0), "wait");
+    if (s->stage_timing) ck(cudaEventRecord(s->chroma_t[0], s->chroma_stream), "event");
     launch_chroma_blocks_for(s, rf16, nblocks, s->chroma_stream);
+    if (s->stage_timing) ck(cudaEventRecord(s->chroma_t[1], s->chroma_stream), "event");
     ck(cudaEventRecord(s->chroma_done, s->chroma_stream), "event");
     s->chroma_pending = true;
 }
@@ -446,6 +454,8 @@ void session_free(vhsdecode_gb300_session* s) {
     if (s->chroma_refined) cudaEventDestroy(s->chroma_refined);
     if (s->chroma_go) cudaEventDestroy(s->chroma_go);
     if (s->chroma_done) cudaEventDestroy(s->chroma_done);
+    for (auto& e : s->chroma_t)
+        if (e) cudaEventDestroy(e);
     if (s->chroma_stream) cudaStreamDestroy(s->chroma_stream);
     if (s->demod_cycles) cudaFree(s->demod_cycles);
     if (s->plain_graph) cudaGraphExecDestroy(s->plain_graph);
@@ -574,9 +584,10 @@ int tuned_fft_plan(vhsdecode_gb300_session* s, FastDemodParams base) {
 
 // The fused demodulator, or (VHSD_DEMOD_TIMING set) its timed diagnostic build.
 cudaError_t launch_fused(vhsdecode_gb300_session* s, FastDemodParams p, cudaStream_t st) {
-    if (!s->demod_cycles) return launch_demod_fp32(p, s->num_sms / 2, st);
+    const int clusters = s->demod_clusters > 0 ? s->demod_clusters : s->num_sms / 2;
+    if (!s->demod_cycles) return launch_demod_fp32(p, clusters, st);
     p.stage_cycles = s->demod_cycles;
-    return launch_demod_fp32_timed(p, s->num_sms / 2, st);
+    return launch_demod_fp32_timed(p, clusters, st);
 }
 
 FastDemodParams fp32_params(vhsdecode_gb300_session* s, const int16_t* rf_dev) {
@@ -1062,6 +1073,14 @@ void collect_field_results(vhsdecode_gb300_session* s, cudaStream_t fs) {
         std::fprintf(stderr, "[gb300 stage] fields=%d hsync=%.3f ms tbc=%.3f ms dropouts=%.3f ms "
                      "rescue_fetches=%d enqueue=%.3f ms segments=%u porch_misses=%d\n", nf, s->stage_ms[0],
                      s->stage_ms[1], s->stage_ms[2], s->rescue_fetches, s->enqueue_ms, s->segments, miss);
+        if (s->chroma_pending) {
+            float c0 = 0, c1 = 0;
+            ck(cudaEventSynchronize(s->chroma_t[1]), "sync");
+            ck(cudaEventElapsedTime(&c0, s->ev[0], s->chroma_t[0]), "elapsed");
+            ck(cudaEventElapsedTime(&c1, s->ev[0], s->chroma_t[1]), "elapsed");
+            std::fprintf(stderr, "[gb300 stage] chroma block stage from %.3f to %.3f ms after the decode start\n",
+                         c0, c1);
+        }
     }
 }
 
@@ -1189,6 +1208,36 @@ void decode_fp32_pipelined(vhsdecode_gb300_session* s, const int16_t* rf, uint64
     }
     if (carry && carry->no_graph) graphable = false;
     s->chroma_pending = false;
+    if (s->want_chroma && nblocks > 0 && host_input) {
+        // The chroma block stage needs the whole capture and SMs of its own
+        // for its whole run; queued behind the persistent demodulator it gets
+        // them only as the demodulation ends.  Pinned input: the stage reads
+        // the capture where it is (mapped host memory) from the start, beside
+        // the pipeline's own copies.  Pageable input: the capture is copied
+        // first and the device-input schedule follows.
+        cudaPointerAttributes attr{};
+        const bool mapped = cudaPointerGetAttributes(&attr, rf) == cudaSuccess &&
+                            attr.type == cudaMemoryTypeHost && attr.devicePointer != nullptr &&
+                            ((uintptr_t)attr.devicePointer & 15u) == 0;
+        cudaGetLastError();
+        if (mapped) {
+            ck(cudaEventRecord(s->chroma_go, cs), "event");
+            queue_chroma_blocks(s, static_cast<const int16_t*>(attr.devicePointer), nblocks, s->chroma_go);
+        } else {
+            ck(cudaMemcpyAsync(s->rf.p, rf, (size_t)n * sizeof(int16_t), cudaMemcpyHostToDevice, cs), "h2d rf");
+            rf = s->rf.p;
+            host_input = false;
+            graphable = !(carry && carry->no_graph);
+        }
+    }
+    // The chroma block stage holds an SM per CTA for its whole (latency-bound)
+    // run, and the persistent demodulator's clusters hold every SM they get:
+    // the demodulator leaves the block stage its SMs (at most a quarter).
+    s->demod_clusters = 0;
+    if (s->want_chroma && nblocks > 0 && !demod_only) {
+        const int reserve = std::min(chroma_block_ctas(nblocks), s->num_sms / 4);
+        s->demod_clusters = std::max(1, (s->num_sms - reserve) / 2);
+    }
     if (s->want_chroma && nblocks > 0 && !host_input) {
         // the capture is already on the device: start the chroma band-pass now
         ck(cudaEventRecord(s->chroma_go, cs), "event");
@@ -1196,7 +1245,7 @@ void decode_fp32_pipelined(vhsdecode_gb300_session* s, const int16_t* rf, uint64
     }
     if (graphable && nseg > 0) {
         PipeKey key{s->in_f32 ? (const void*)s->in_f32 : (const void*)rf, n, host_input, demod_only,
-                    s->in_f32 != nullptr};
+                    s->in_f32 != nullptr, s->demod_clusters};
         if (!s->pipe_exec || !(s->pipe_key == key)) {
             if (s->pipe_exec) { cudaGraphExecDestroy(s->pipe_exec); s->pipe_exec = nullptr; }
             FastDemodParams p0 = fp32_params(s, s->rf.p);
@@ -1222,10 +1271,6 @@ void decode_fp32_pipelined(vhsdecode_gb300_session* s, const int16_t* rf, uint64
         enqueue_pipeline(s, rf, n, host_input, demod_only, bounds, cs, false);
     }
     s->launches += pipeline_launches(bounds, demod_only);
-    if (s->want_chroma && nblocks > 0 && host_input) {
-        // host input: after the last segment's RF copy (its demod start is an external event)
-        queue_chroma_blocks(s, s->rf.p, nblocks, s->seg_dem[(size_t)(2 * (nseg - 1))]);
-    }
     s->enqueue_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tq0).count();
     if (!demod_only && nblocks > 0) {
         auto t0 = std::chrono::steady_clock::now();

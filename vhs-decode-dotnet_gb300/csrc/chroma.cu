@@ -887,6 +887,8 @@ __global__ void __launch_bounds__(256) k_chroma_gain(ChromaFieldParams p) {
 
 }  // namespace
 
+int chroma_block_ctas(int64_t nblocks) { return (int)((nblocks + kBlockGroups - 1) / kBlockGroups); }
+
 cudaError_t prepare_chroma_kernels() {
     // the block stage's rings above the default 48 KB of shared memory; all of
     // the SM's shared memory for the probe rows, so a decode's probe warps fit

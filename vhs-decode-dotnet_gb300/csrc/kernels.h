@@ -240,6 +240,8 @@ struct ChromaBlockParams {
 constexpr int kChromaBlockKernels = 2;
 // Kernel attributes of the chroma kernels (once per device, outside any capture).
 cudaError_t prepare_chroma_kernels();
+// CTAs (one per SM) of the chroma block stage for nblocks blocks.
+int chroma_block_ctas(int64_t nblocks);
 cudaError_t launch_chroma_blocks(const ChromaBlockParams& p, cudaStream_t stream);
 
 // Per-field chroma stages of a field batch (every array offset to the batch).

@@ -88,8 +88,10 @@ struct PipeKey {
     const void* rf = nullptr;
     uint64_t n = 0;
     bool host_input = false, demod_only = false, f32 = false;
+    int clusters = 0;   // the fused demodulator's clusters (fewer while the chroma block stage runs)
     bool operator==(const PipeKey& o) const {
-        return rf == o.rf && n == o.n && host_input == o.host_input && demod_only == o.demod_only && f32 == o.f32;
+        return rf == o.rf && n == o.n && host_input == o.host_input && demod_only == o.demod_only && f32 == o.f32 &&
+               clusters == o.clusters;
     }
 };
 
@@ -190,6 +192,8 @@ struct vhsdecode_gb300_session {
     cudaStream_t alt_stream = nullptr;   // odd segments, so a segment's straggler blocks overlap the next one
     cudaStream_t cap_stream = nullptr;   // origin of the pipeline graph capture
     cudaEvent_t alt_start = nullptr, alt_end = nullptr, copy_end = nullptr, d2h_end = nullptr;
+    cudaEvent_t chroma_t[2] = {nullptr, nullptr};   // stage timing: the block stage's start and end
+    int demod_clusters = 0;            // clusters of the pipelined demod launches (0: one per SM pair)
     cudaGraphExec_t pipe_exec = nullptr; // captured segment pipeline
     PipeKey pipe_key{};
     std::vector<cudaEvent_t> seg_done, seg_copied, seg_pulsed, seg_dem, seg_demod_end;
