@@ -10,7 +10,8 @@ Tolerances:
   an exact turn reduction: each agrees with the reference to float rounding);
 * field count, field order and dropout decisions identical.
 
-The uint16 chroma bar holds end to end for the FP64 plain path.  The FP32
+The uint16 chroma bar holds end to end for the FP64 plain path (PAL and NTSC
+VHS SP, PAL and NTSC S-VHS, NTSC EP).  The FP32
 fused path's line locations differ from the FP64 oracle's by about 1e-4
 sample (its demodulated sync is within 1 kHz, not exact), and the reference
 TBC rounds each source position to float32, a 1/32-sample grid at the
@@ -37,13 +38,15 @@ def _oracle(rf, system, fs=40e6, tape_format="VHS"):
     return fields, ch
 
 
-def _decode(rf, profile, chroma=True, fs_mhz=40.0, tape_format=None, precision=None):
+def _decode(rf, profile, chroma=True, fs_mhz=40.0, tape_format=None, precision=None, tape_speed=None):
     from vhsd_gb300 import native
     kw = {}
     if tape_format is not None:
         kw["tape_format"] = tape_format
     if precision is not None:
         kw["precision"] = precision
+    if tape_speed is not None:
+        kw["tape_speed"] = tape_speed
     s = native.Session(profile, len(rf), sample_rate_mhz=fs_mhz, **kw)
     r = s.decode(rf, chroma=chroma)
     out = {"fields": r.fields, "tbc": s.tbc().copy(), "first": [], "locs": [], "drops": []}
@@ -90,6 +93,29 @@ def test_fp64_chroma_fields_match_oracle(gpu, pal_capture, ntsc_capture, system)
     good = [f for f in fields if "error" not in f]
     prof = native.PROFILE_PAL if system == "PAL" else native.PROFILE_NTSC
     dev = _decode(rf, prof, precision=native.PRECISION_FP64_PLAIN)
+    _check_fields(dev, good, 320 if system == "PAL" else 270)
+    dev["session"].close()
+
+
+@pytest.mark.parametrize("case", ["pal_svhs", "ntsc_svhs", "ntsc_ep"])
+def test_fp64_chroma_other_formats_match_oracle(gpu, case, request):
+    # the same colour-under chroma behind S-VHS's own luma path (sub-deemphasis,
+    # custom luma filters) and behind NTSC EP's narrower RF filters and
+    # long-play burst level: the FP64 path end to end against the oracle
+    from oracle import field, formats
+    from vhsd_gb300 import native
+    fixture, system, tape, speed = {
+        "pal_svhs": ("svhs_capture", "PAL", "SVHS", "sp"),
+        "ntsc_svhs": ("svhs_ntsc_capture", "NTSC", "SVHS", "sp"),
+        "ntsc_ep": ("ntsc_capture", "NTSC", "VHS", "ep"),
+    }[case]
+    rf, _ = request.getfixturevalue(fixture)
+    fields, _ = field.decode_capture(rf, formats.get(system, tape, speed), with_chroma=True)
+    good = [f for f in fields if "error" not in f]
+    prof = native.PROFILE_PAL if system == "PAL" else native.PROFILE_NTSC
+    dev = _decode(rf, prof, precision=native.PRECISION_FP64_PLAIN,
+                  tape_format=native.FORMAT_SVHS if tape == "SVHS" else native.FORMAT_VHS,
+                  tape_speed=native.TAPE_EP if speed == "ep" else native.TAPE_SP)
     _check_fields(dev, good, 320 if system == "PAL" else 270)
     dev["session"].close()
 
