@@ -11,7 +11,7 @@ Tolerances:
 * field count, field order and dropout decisions identical.
 
 The uint16 chroma bar holds end to end for the FP64 plain path (PAL and NTSC
-VHS SP, PAL and NTSC S-VHS, NTSC EP).  The FP32
+VHS SP, PAL and NTSC S-VHS, NTSC EP, NTSC at 20 MSPS).  The FP32
 fused path's line locations differ from the FP64 oracle's by about 1e-4
 sample (its demodulated sync is within 1 kHz, not exact), and the reference
 TBC rounds each source position to float32, a 1/32-sample grid at the
@@ -117,6 +117,19 @@ def test_fp64_chroma_other_formats_match_oracle(gpu, case, request):
                   tape_format=native.FORMAT_SVHS if tape == "SVHS" else native.FORMAT_VHS,
                   tape_speed=native.TAPE_EP if speed == "ep" else native.TAPE_SP)
     _check_fields(dev, good, 320 if system == "PAL" else 270)
+    dev["session"].close()
+
+
+def test_fp64_chroma_at_20_msps_matches_oracle(gpu, ntsc20_capture):
+    # the chroma filters and burst geometry designed for a 20 MSPS decode
+    # (the chroma offset, the band-pass edges and pad length at that rate)
+    from oracle import field, formats
+    from vhsd_gb300 import native
+    rf, _ = ntsc20_capture
+    fields, _ = field.decode_capture(rf, formats.get("NTSC"), fs=20e6, with_chroma=True)
+    good = [f for f in fields if "error" not in f]
+    dev = _decode(rf, native.PROFILE_NTSC, fs_mhz=20.0, precision=native.PRECISION_FP64_PLAIN)
+    _check_fields(dev, good, 270)
     dev["session"].close()
 
 
