@@ -11,7 +11,8 @@ Tolerances:
 * field count, field order and dropout decisions identical.
 
 The uint16 chroma bar holds end to end for the FP64 plain path (PAL and NTSC
-VHS SP, PAL and NTSC S-VHS, NTSC EP, NTSC at 20 MSPS).  The FP32
+VHS SP, PAL and NTSC S-VHS, NTSC EP, NTSC at 20 MSPS directly and through the
+device decimator); float32 input gives the int16 decode's bits.  The FP32
 fused path's line locations differ from the FP64 oracle's by about 1e-4
 sample (its demodulated sync is within 1 kHz, not exact), and the reference
 TBC rounds each source position to float32, a 1/32-sample grid at the
@@ -222,3 +223,41 @@ def test_chroma_off_is_the_skip_chroma_decode(gpu, pal_capture, pal_oracle):
     with pytest.raises(native.NativeError):
         dev["session"].chroma()
     dev["session"].close()
+
+
+def test_float_input_chroma_equals_int16(gpu, ntsc_capture):
+    # the block stage's float-source pass: a float32 capture of the int16
+    # values decodes to the same luma and chroma bits, host and device input
+    import torch
+    from vhsd_gb300 import native
+    rf, _ = ntsc_capture
+    with native.Session(native.PROFILE_NTSC, len(rf)) as s:
+        s.decode(rf, chroma=True)
+        tb, ch = s.tbc().copy(), s.chroma().copy()
+        s.decode(rf.astype(np.float32), chroma=True)
+        assert s.tbc().tobytes() == tb.tobytes()
+        assert s.chroma().tobytes() == ch.tobytes()
+        d = torch.from_numpy(rf.astype(np.float32)).cuda()
+        s.decode(None, device_ptr=d.data_ptr(), count=len(rf), float_input=True, chroma=True)
+        assert s.chroma().tobytes() == ch.tobytes()
+
+
+def test_fp64_decimated_chroma_matches_oracle(gpu, ntsc_capture):
+    # 40 MSPS through the device 2:1 decimator, chroma decoded at 20 MSPS from
+    # the float capture: against the oracle's chroma decode of the oracle's
+    # decimated capture
+    from oracle import field, formats
+    from oracle import native as onative
+    from vhsd_gb300 import native
+    rf, _ = ntsc_capture
+    plane = onative.decimate_half(rf)
+    fields, _ = field.decode_capture(plane, formats.get("NTSC"), fs=20e6, with_chroma=True)
+    good = [f for f in fields if "error" not in f]
+    with native.Session(native.PROFILE_NTSC, len(rf), precision=native.PRECISION_FP64_PLAIN,
+                        sample_rate_mhz=20.0, decimation=2) as s:
+        r = s.decode(rf, chroma=True)
+        dev = {"fields": r.fields, "tbc": s.tbc().copy(), "chroma": s.chroma().copy(),
+               "first": [bool(s.field(i).is_first_field) for i in range(r.fields)],
+               "locs": [s.lines(i) for i in range(r.fields)],
+               "drops": [s.dropouts(i) for i in range(r.fields)]}
+    _check_fields(dev, good, 270)
