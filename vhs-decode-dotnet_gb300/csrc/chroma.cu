@@ -308,6 +308,8 @@ __device__ __forceinline__ int positive_mod4(int v) {
     return r < 0 ? r + 4 : r;
 }
 
+constexpr int kProbeWinMax = 224;   // probe window samples (PAL 206, NTSC 174)
+
 // One lane per (field, rotation sequence, line): the probe window of the
 // line times the heterodyne of its phase rotation, the float32
 // forward-backward final band-pass over it (odd extension, in place in the
@@ -325,18 +327,41 @@ __global__ void __launch_bounds__(32) k_chroma_probe(ChromaFieldParams p) {
     const int64_t nprobe = (int64_t)p.nfields * 2 * p.out_lines;
     const int64_t base = (int64_t)blockIdx.x * 32;
     const int64_t field = (int64_t)p.out_lines * p.outlen;
-    for (int j = 0; j < 32; j++) {
-        const int64_t qj = base + j;
-        if (qj >= nprobe) break;
-        const int fj = (int)(qj / (2 * p.out_lines));
-        const int cj = (int)((qj / p.out_lines) % 2);
-        const int lj = (int)(qj % p.out_lines);
-        const int rot = positive_mod4((cj == 0 ? p.rot0 : p.rot1) * (lj + 1));
-        const float* het = p.het + (int64_t)rot * field + (int64_t)lj * p.outlen + p.win0;
-        const float* ana = p.ana + ((int64_t)fj * p.out_lines + lj) * win;
-        float* row = smem + j * stride + edge;
-#pragma unroll 4
-        for (int i = lane; i < win; i += 32) row[i] = __fmul_rn(het[i], ana[i]);
+    // four probes' windows at a time, every load of them issued before the
+    // products are stored (win <= kProbeWinMax)
+    for (int j0 = 0; j0 < 32; j0 += 4) {
+        const float* hp[4];
+        const float* ap[4];
+        bool ok[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const int64_t qj = base + j0 + u;
+            ok[u] = qj < nprobe;
+            const int64_t qq = ok[u] ? qj : 0;
+            const int fj = (int)(qq / (2 * p.out_lines));
+            const int cj = (int)((qq / p.out_lines) % 2);
+            const int lj = (int)(qq % p.out_lines);
+            const int rot = positive_mod4((cj == 0 ? p.rot0 : p.rot1) * (lj + 1));
+            hp[u] = p.het + (int64_t)rot * field + (int64_t)lj * p.outlen + p.win0;
+            ap[u] = p.ana + ((int64_t)fj * p.out_lines + lj) * win;
+        }
+        float h[4][kProbeWinMax / 32], a[4][kProbeWinMax / 32];
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+#pragma unroll
+            for (int m = 0; m < kProbeWinMax / 32; m++) {
+                const int i = 32 * m + lane;
+                const bool in = ok[u] && i < win;
+                h[u][m] = in ? hp[u][i] : 0.0f;
+                a[u][m] = in ? ap[u][i] : 0.0f;
+            }
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+#pragma unroll
+            for (int m = 0; m < kProbeWinMax / 32; m++) {
+                const int i = 32 * m + lane;
+                if (ok[u] && i < win) smem[(j0 + u) * stride + edge + i] = __fmul_rn(h[u][m], a[u][m]);
+            }
     }
     __syncwarp();
     const bool active = base + lane < nprobe;
@@ -913,6 +938,7 @@ cudaError_t launch_chroma_blocks(const ChromaBlockParams& p, cudaStream_t s) {
 
 cudaError_t launch_chroma_phase(const ChromaFieldParams& p, cudaStream_t s) {
     if (p.nfields <= 0) return cudaSuccess;
+    if (p.win > kProbeWinMax || p.win <= 32) return cudaErrorInvalidValue;
     const int64_t nprobe = (int64_t)p.nfields * 2 * p.out_lines;
     const size_t smem = (size_t)32 * ((p.win + 2 * p.fin.edge) | 1) * sizeof(float);
     k_chroma_probe<<<(unsigned)((nprobe + 31) / 32), 32, smem, s>>>(p);
