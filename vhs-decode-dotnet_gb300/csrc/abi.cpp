@@ -375,6 +375,7 @@ void ensure_chroma(vhsdecode_gb300_session* s) {
     s->c_up.alloc(mf * crow);
     s->c_fwd.alloc(mf * crow);
     s->c_probe.alloc(mf * 2 * s->out_lines * 5);
+    s->c_probe_nrm.alloc(mf * 2 * s->out_lines * 2);
     s->c_summary.alloc(mf * 4);
     s->locs_final.alloc(mf * s->lines);
     s->c_flip.alloc(mf * 2);
@@ -912,6 +913,7 @@ void launch_field_batch(vhsdecode_gb300_session* s, int f0, int f1, const T* vid
         cp.bcos = s->c_bcos.p;
         cp.ana = s->c_ana.p + (size_t)f0 * s->out_lines * cp.win;
         cp.probe = s->c_probe.p + (size_t)f0 * 2 * s->out_lines * 5;
+        cp.probe_nrm = s->c_probe_nrm.p + (size_t)f0 * 2 * s->out_lines * 2;
         cp.flip = s->c_flip.p + 2 * (size_t)f0;
         cp.chosen = s->c_chosen.p + f0;
         cp.rot_in = s->rot_in_d.p;

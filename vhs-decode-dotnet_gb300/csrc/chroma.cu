@@ -465,11 +465,16 @@ __global__ void __launch_bounds__(32) k_chroma_probe(ChromaFieldParams p) {
         const double scale = pl < p.out_lines - 1 ? __ddiv_rn(__dsub_rn(loc[line + 1], loc[line]), (double)p.input_line)
                                                   : 1.0;
         double* o = p.probe + q * 5;
+        const double mag = hypot(ic, qc);
         o[0] = positive_degrees(atan2(qc, ic) * (180.0 / 3.141592653589793));
         o[1] = positive_degrees((double)p.bs * __fma_rn(-scale, 90.0, 90.0));
-        o[2] = hypot(ic, qc);
+        o[2] = mag;
         o[3] = ic;
         o[4] = qc;
+        // the normalised I/Q of the phase averages, divided here, a lane per
+        // probe, instead of in the per-field summary
+        p.probe_nrm[q * 2] = mag != 0.0 ? __ddiv_rn(ic, mag) : 0.0;
+        p.probe_nrm[q * 2 + 1] = mag != 0.0 ? __ddiv_rn(qc, mag) : 0.0;
     }
 }
 
@@ -509,20 +514,22 @@ __global__ void k_chroma_chain(ChromaFieldParams p) {
 }
 
 // SummarizePhaseSequence of each field's kept sequence: one warp per field,
-// the normalised I/Q of every line in parallel, then the sums in line order.
+// the lines' normalised I/Q (divided by the probes) and magnitudes into shared
+// memory, then the sums in line order.
 __global__ void __launch_bounds__(32) k_chroma_summary(ChromaFieldParams p) {
     __shared__ double nrm[1][3][320];   // I / mag, Q / mag, mag
     const int w = 0, lane = threadIdx.x;
     const int f = blockIdx.x;
     if (f >= p.nfields) return;
-    const double* pr = p.probe + ((int64_t)f * 2 + p.chosen[f]) * p.out_lines * 5;
+    const int64_t row = ((int64_t)f * 2 + p.chosen[f]) * p.out_lines;
+    const double* pr = p.probe + row * 5;
+    const double* pn = p.probe_nrm + row * 2;
     const int end = p.out_lines + 1;
     const int nl = min(p.out_lines, 320);
     for (int k = lane; k < nl; k += 32) {
-        const double mag = pr[k * 5 + 2];
-        nrm[w][0][k] = mag != 0.0 ? __ddiv_rn(pr[k * 5 + 3], mag) : 0.0;
-        nrm[w][1][k] = mag != 0.0 ? __ddiv_rn(pr[k * 5 + 4], mag) : 0.0;
-        nrm[w][2][k] = mag;
+        nrm[w][0][k] = pn[k * 2];
+        nrm[w][1][k] = pn[k * 2 + 1];
+        nrm[w][2][k] = pr[k * 5 + 2];
     }
     __syncwarp();
     // Five ordered sums in line order, each in its own lane (lane 0: even-line

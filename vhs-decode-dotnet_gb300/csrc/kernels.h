@@ -264,6 +264,7 @@ struct ChromaFieldParams {
     const float* bcos;
     const float* ana;           // [nfields * out_lines * win] chroma TBC from line 1, probe windows
     double* probe;              // [nfields * 2 * out_lines * 5] phase, offset, magnitude, I, Q
+    double* probe_nrm;          // [nfields * 2 * out_lines * 2] I / magnitude, Q / magnitude of each probe
     int* flip;                  // [nfields * 2]
     int* chosen;                // [nfields] rotation index of the kept sequence
     const int* rot_in;          // rotation index before the first field

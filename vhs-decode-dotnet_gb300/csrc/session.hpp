@@ -237,7 +237,7 @@ struct vhsdecode_gb300_session {
     DevBuf<float> c_het, c_bsin, c_bcos; // field tables
     DevBuf<float> c_ana;                 // line-1 chroma TBC, probe windows
     DevBuf<float> c_field, c_up, c_fwd;  // output-line chroma TBC, up-converted / filtered, forward pass
-    DevBuf<double> c_probe, c_summary, locs_final;
+    DevBuf<double> c_probe, c_probe_nrm, c_summary, locs_final;
     DevBuf<float2> c_advance;   // NTSC carrier advance per sample of a line: (cos, sin)
     DevBuf<float2> c_line_cs, c_line_scale_f;
     DevBuf<double> c_line_scale;
