@@ -859,21 +859,33 @@ __global__ void __launch_bounds__(32) k_chroma_gain_lines(ChromaFieldParams p) {
     const int64_t id0 = (int64_t)blockIdx.x * 32;
     const int n = p.be - p.bs;
     {
-        const int nj = (int)min((int64_t)32, total - id0);
+        // eight lines at a time, every load of them issued before the sums
+        // are stored (n <= kBurstMax = 64: two samples per lane per line)
         const int f0 = (int)(id0 / p.out_lines), o0 = (int)(id0 % p.out_lines);
-        int j = 0, k = lane;   // element e = j * n + k
-        for (int e = lane; e < nj * n; e += 32) {
-            while (k >= n) {
-                k -= n;
-                j++;
+        for (int j0 = 0; j0 < 32; j0 += 8) {
+            float v[8][2];
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                int f = f0, o = o0 + j0 + u;   // 32 lines cross at most one field end
+                if (o >= p.out_lines) {
+                    o -= p.out_lines;
+                    f++;
+                }
+                const bool line_ok = id0 + j0 + u < total && o >= 16;
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    const int k = lane + 32 * h;
+                    v[u][h] = line_ok && k < n ? comb_at(p.up + (int64_t)f * p.crow + p.fin.edge, o, p.bs + k, p)
+                                               : 0.0f;
+                }
             }
-            int f = f0, o = o0 + j;   // 32 lines cross at most one field end
-            if (o >= p.out_lines) {
-                o -= p.out_lines;
-                f++;
-            }
-            if (o >= 16) comb[j][k] = comb_at(p.up + (int64_t)f * p.crow + p.fin.edge, o, p.bs + k, p);
-            k += 32;
+#pragma unroll
+            for (int u = 0; u < 8; u++)
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    const int k = lane + 32 * h;
+                    if (k < n) comb[j0 + u][k] = v[u][h];
+                }
         }
     }
     __syncwarp();
@@ -896,7 +908,7 @@ __global__ void __launch_bounds__(32) k_chroma_gain_lines(ChromaFieldParams p) {
 
 // The uint16 chroma: lines below 16 neutral (32767), the others combed and
 // scaled by their line's gain.
-__global__ void __launch_bounds__(256) k_chroma_gain(ChromaFieldParams p) {
+__global__ void __launch_bounds__(320) k_chroma_gain(ChromaFieldParams p) {
     const int f = blockIdx.y, o = blockIdx.x;
     const int64_t field = (int64_t)p.out_lines * p.outlen;
     const float* x = p.up + (int64_t)f * p.crow + p.fin.edge;
@@ -909,11 +921,20 @@ __global__ void __launch_bounds__(256) k_chroma_gain(ChromaFieldParams p) {
     const double scale = p.line_scale[id];
     const float2 sp = p.line_scale_f[id];
     const int64_t vec_len = field & ~(int64_t)3;
-    for (int k = threadIdx.x; k < p.outlen; k += blockDim.x) {
-        const float v = comb_at(x, o, k, p);
+    // four samples per thread (blockDim.x >= outlen / 4), their loads issued together
+    float v[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+        const int k = threadIdx.x + u * blockDim.x;
+        v[u] = k < p.outlen ? comb_at(x, o, k, p) : 0.0f;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+        const int k = threadIdx.x + u * blockDim.x;
+        if (k >= p.outlen) continue;
         const int64_t gi = (int64_t)o * p.outlen + k;
-        out[k] = gi < vec_len ? gain_u16(v, sp.x, sp.y, scale)
-                              : u16_wrap(__dadd_rn(__dmul_rn((double)v, scale), 32767.0));
+        out[k] = gi < vec_len ? gain_u16(v[u], sp.x, sp.y, scale)
+                              : u16_wrap(__dadd_rn(__dmul_rn((double)v[u], scale), 32767.0));
     }
 }
 
@@ -960,7 +981,7 @@ cudaError_t launch_chroma_phase(const ChromaFieldParams& p, cudaStream_t s) {
 
 cudaError_t launch_chroma_decode(const ChromaFieldParams& p, cudaStream_t s) {
     if (p.nfields <= 0) return cudaSuccess;
-    if (p.be - p.bs > kBurstMax || p.be <= p.bs) return cudaErrorInvalidValue;
+    if (p.be - p.bs > kBurstMax || p.be <= p.bs || p.outlen > 4 * 320) return cudaErrorInvalidValue;
     dim3 lines(p.out_lines, p.nfields);
     const unsigned line_grid = (unsigned)(((int64_t)p.nfields * p.out_lines + 127) / 128);
     k_chroma_up_lines<<<line_grid, 128, 0, s>>>(p);   // NTSC only (returns at once for PAL)
@@ -980,7 +1001,8 @@ cudaError_t launch_chroma_decode(const ChromaFieldParams& p, cudaStream_t s) {
     default: k_chroma_final<true, 3><<<grid, 128, 0, s>>>(p, chunks); k_chroma_final<false, 3><<<grid, 128, 0, s>>>(p, chunks); break;
     }
     k_chroma_gain_lines<<<(unsigned)(((int64_t)p.nfields * p.out_lines + 31) / 32), 32, 0, s>>>(p);
-    k_chroma_gain<<<lines, 256, 0, s>>>(p);
+    const int gain_threads = ((p.outlen + 3) / 4 + 31) / 32 * 32;   // four samples per thread
+    k_chroma_gain<<<lines, gain_threads, 0, s>>>(p);
     return cudaGetLastError();
 }
 

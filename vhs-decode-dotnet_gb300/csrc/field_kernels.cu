@@ -1007,9 +1007,11 @@ __device__ __forceinline__ double dval(long long k) {
     return __longlong_as_double(k ^ ((k >> 63) & 0x7fffffffffffffffLL));
 }
 
-// Bitonic sort of 512 entries: int64 keys, or (as_double) raw double bits
-// compared as doubles, the form that keeps NaN's no-swap behaviour.
-__device__ __forceinline__ void bitonic512(long long* a, bool as_double) {
+// Bitonic sort of 512 entries: int64 keys, or (kDouble) raw double bits
+// compared as doubles, the form that keeps NaN's no-swap behaviour.  Two
+// instantiations, so the integer form issues no binary64 compare at all.
+template <bool kDouble>
+__device__ __forceinline__ void bitonic512_t(long long* a) {
     for (int k = 2; k <= 512; k <<= 1) {
         for (int j = k >> 1; j > 0; j >>= 1) {
             for (int i = threadIdx.x; i < 512; i += blockDim.x) {
@@ -1017,13 +1019,17 @@ __device__ __forceinline__ void bitonic512(long long* a, bool as_double) {
                 if (ixj > i) {
                     bool up = (i & k) == 0;
                     long long x = a[i], y = a[ixj];
-                    bool gt = as_double ? (__longlong_as_double(x) > __longlong_as_double(y)) : (x > y);
+                    bool gt = kDouble ? (__longlong_as_double(x) > __longlong_as_double(y)) : (x > y);
                     if (gt == up) { a[i] = y; a[ixj] = x; }
                 }
             }
             __syncthreads();
         }
     }
+}
+__device__ __forceinline__ void bitonic512(long long* a, bool as_double) {
+    if (as_double) bitonic512_t<true>(a);
+    else bitonic512_t<false>(a);
 }
 
 __global__ void __launch_bounds__(512) k_tbc_levels(TbcParams p, const double* pw_outlen) {
@@ -1033,7 +1039,12 @@ __global__ void __launch_bounds__(512) k_tbc_levels(TbcParams p, const double* p
     const int fl = p.first_line[f];
     const int nl = fl + p.out_lines;          // lines covered by the plan incl. prefix
     const double* loc = p.locs + (int64_t)f * p.lines;
-    const double inv = 1.0 / p.nominal;
+    // one binary64 division per CTA: an FP64 warp instruction costs the SM's
+    // FP64 pipe the same whatever its active lanes
+    __shared__ double inv_s;
+    if (threadIdx.x == 0) inv_s = 1.0 / p.nominal;
+    __syncthreads();
+    const double inv = inv_s;
     int nan_here = 0;
     for (int l = threadIdx.x; l < 512; l += blockDim.x) {
         double v = INFINITY;
@@ -1087,11 +1098,12 @@ __global__ void __launch_bounds__(512) k_tbc_levels(TbcParams p, const double* p
     sm_m[l] = m;
     sm_c[l] = c;
     __syncthreads();
+    // only the slots of lines take part (the maps past nl are never read)
     for (int d = 1; d < 512; d <<= 1) {
         double pm = 1.0, pc = 0.0;
-        if (l >= d) { pm = sm_m[l - d]; pc = sm_c[l - d]; }
+        if (l >= d && l < nl) { pm = sm_m[l - d]; pc = sm_c[l - d]; }
         __syncthreads();
-        if (l >= d) {
+        if (l >= d && l < nl) {
             c = __fma_rn(m, pc, c);
             m = __dmul_rn(m, pm);
             sm_m[l] = m;
