@@ -12,6 +12,7 @@ import math
 import struct
 
 import numpy as np
+import pytest
 from oracle import chroma, formats, native
 
 
@@ -296,3 +297,36 @@ def test_pal_phase_sequence_matches_frozen_release_bits():
     frozen = [0x4037E9036918DF9A, 0x40749879C9CA5F7F, 0x4074978FCAA356D3, 0x4074997460E7FB3B]
     for key, b in zip(("mag_avg", "avg", "even", "odd"), frozen):
         assert abs(r[key] - struct.unpack("<d", struct.pack("<Q", b))[0]) < 1e-9, key
+
+
+def _lcg_field(case, n):
+    # the test's chroma field: a 32-bit LCG from 0x12345678 + case * 0x01020304,
+    # (state >> 8) & 0xFFFF centred, / 8 plus a 17-sample ramp, rounded to float
+    state = (0x12345678 + case * 0x01020304) & 0xFFFFFFFF
+    out = np.empty(n, np.float64)
+    for i in range(n):
+        state = (state * 1664525 + 1013904223) & 0xFFFFFFFF
+        signed = ((state >> 8) & 0xFFFF) - 32768
+        out[i] = np.float32(signed / 8.0 + ((i % 17) - 8) * 0.03125)
+    return out
+
+
+@pytest.mark.parametrize("case,system,tape,want", [
+    (25, "PAL", "VHS", "61033C0998FF4B024670D5F0C4074CB8EF49613CA974621ABA38518A60CE3EEE"),
+    (26, "NTSC", "VHS", "B4ACBFE26CE1DD6F2D69C53C30E922B8D287E1EAF4E40BAFB57F8CEDB1EC01C6"),
+    (18, "PAL", "SVHS", "CEFA28AFCE2BF3A2A4FB6BCF7177AE43A77A6A707E4C0892DCD40CF3F8EFEE86"),
+    (22, "NTSC", "SVHS", "97AC5FC2F8AADC8104A271C9B2E2FA961F246143C78FC754F0463F4E9E23225F"),
+])
+def test_field_decode_matches_release_bits(case, system, tape, want):
+    # CompatibilityTests.cs:3775-3877 (FormatSpecificChromaFieldMatchesReleaseBits):
+    # up-conversion, final band-pass, comb and gain of a whole synthetic field
+    # for a synthetic phase sequence, to the SHA-256 of the uint16 field
+    cp = chroma.ChromaParams(formats.get(system, tape))
+    field = _lcg_field(case, cp.out_lines * cp.outlen)
+    line_offset = 1 if system == "NTSC" else 3
+    seq = [{"line": line_offset + k, "rot": ((line_offset + k) * 3 + case + 1) % 4,
+            "phase": float(((line_offset + k) * 17 + case * 23) % 360 - 180.0), "offset": 0.0,
+            "mag": 30000.0, "i": 30000.0, "q": 0.0} for k in range(cp.out_lines)]
+    phase = {"seq": seq, "burst_line": 0, "avg": 0.0, "even": 0.0, "odd": 0.0, "mag_avg": 30000.0}
+    out = chroma.decode_field_chroma(field, cp, phase, True, 0, line_offset)
+    assert hashlib.sha256(np.ascontiguousarray(out, "<u2").tobytes()).hexdigest().upper() == want
