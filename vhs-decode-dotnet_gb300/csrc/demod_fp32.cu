@@ -34,7 +34,8 @@
 // Shared memory per CTA (212 KB, one CTA per SM): 16384 complex floats
 // (padded against bank conflicts), a 16384-float buffer that holds the angles,
 // then the demod, then (S-VHS) the kept spectrum, and in between the next
-// block's RF prefetch; plus twiddle tables.
+// block's RF prefetch and, during the stage-1 transform, the RfVideo table;
+// plus twiddle tables.
 #include <cooperative_groups.h>
 #include <atomic>
 #include <climits>
@@ -216,7 +217,7 @@ template <typename ScaleFn>
 __device__ __forceinline__ void post_half(Shared& sh, int rank, int tid, ScaleFn scale) {
     float2* buf = sh.buf;
     if (rank == 0) {
-        for (int q = tid; q <= 4096; q += T) {
+        for (int q = tid; q < 4096; q += T) {
             int q2 = 8192 - q;
             float2 cq = buf[sx(q)];
             float2 cq2 = (q == 0) ? cq : buf[sx(q2)];
@@ -225,6 +226,9 @@ __device__ __forceinline__ void post_half(Shared& sh, int rank, int tid, ScaleFn
                 float x0 = cq.x + cq.y, xm = cq.x - cq.y;
                 buf[sx(0)] = scale(0, make_float2(x0, 0.0f));
                 sh.nyq = scale(M, make_float2(xm, 0.0f));
+                // the self-paired bin 8192 (q = 4096) here, not in a ninth round
+                const float2 cm = buf[sx(4096)];
+                buf[sx(4096)] = scale(8192, real_post(cm, cm, w32k(sh.tw, 8192)));
             } else {
                 int k = 2 * q, k2 = 2 * q2;
                 float2 xk = real_post(cq, cq2, w32k(sh.tw, k));
@@ -600,6 +604,21 @@ __device__ __forceinline__ void prefetch_rf(void* dst, const int16_t* x, int tid
 }
 __device__ __forceinline__ void prefetch_wait() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
+// RfVideo entries 0..16383 (64 KB, 16-byte aligned) into `dst` with
+// asynchronous 16-byte copies (8 per thread): issued before the stage-1
+// transform, waited for after it, so the stage-1 products read the table from
+// shared memory instead of waiting for L2.
+__device__ __forceinline__ void stage_rf_table(float* dst, const float* tab, int tid) {
+    const char* src = reinterpret_cast<const char*>(tab);
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        const int off = (tid + i * T) * 16;
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d + off), "l"(src + off) : "memory");
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+
 }  // namespace fp32
 }  // namespace vhsd
 
@@ -714,14 +733,21 @@ vhsd_demod_fp32_kernel(FastDemodParams pk) {
         if (f32_in) load_rf_f32(buf, p.rf_f32 + (blk + p.first_block) * (int64_t)S, rank, sh.tw, tid);
         else load_rf(buf, rf_smem, rank, sh.tw, tid);
         __syncthreads();
+        // theta (the RF copy) is consumed: it holds the RfVideo table until the angles
+        stage_rf_table(sh.theta, p.rf_video, tid);
         VHSD_MARK(0);
         fft8192<false, 1, PLAN>(buf, sh.tw, tid);
         VHSD_MARK(1);
+        prefetch_wait();
+        __syncthreads();
         // X * RfVideo * Hilbert / N  (Hilbert: 1 at 0 and N/2, 2 between)
-        post_half(sh, rank, tid, [&](int k, float2 v) {
-            float g = __ldg(p.rf_video + k) * ((k == 0 || k == M) ? inv_n : 2.0f * inv_n);
-            return make_float2(v.x * g, v.y * g);
-        });
+        {
+            const float tab_m = __ldg(p.rf_video + M);
+            post_half(sh, rank, tid, [&](int k, float2 v) {
+                float g = (k < M ? sh.theta[k] : tab_m) * ((k == 0 || k == M) ? inv_n : 2.0f * inv_n);
+                return make_float2(v.x * g, v.y * g);
+            });
+        }
         VHSD_MARK(2);
         // ---------------- stage 2: analytic inverse FFT -----------------
         if (rank == 0) {
@@ -894,7 +920,7 @@ vhsd_demod_fp32_kernel(FastDemodParams pk) {
                 return make_float2(sc * (a.x - bw.y), sc * (a.y + bw.x));
             };
             if (rank == 0) {
-                for (int q = tid; q <= 4096; q += T) {
+                for (int q = tid; q < 4096; q += T) {
                     int q2 = 8192 - q;
                     int k = 2 * q, k2 = 2 * q2;
                     float2 xk = buf[sx(q)];
@@ -908,9 +934,16 @@ vhsd_demod_fp32_kernel(FastDemodParams pk) {
                     float2 pv = prep(fv, fv2, k), ps = prep(fs, fs2, k);
                     buf[sx(q)] = pv;
                     buf[sx(8192 + q)] = ps;
-                    if (q != 0 && q2 != q) {
+                    if (q != 0) {
                         buf[sx(q2)] = prep(fv2, fv, k2);
                         buf[sx(8192 + q2)] = prep(fs2, fs, k2);
+                    } else {
+                        // the self-paired bin 8192 (q = 4096) here, not in a ninth round
+                        const float2 xm = buf[sx(4096)];
+                        const float2 hvm = __ldg(p.video + 8192), hsm = __ldg(p.sync + 8192);
+                        const float2 fvm = cmul(xm, hvm), fsm = cmul(xm, hsm);
+                        buf[sx(4096)] = prep(fvm, fvm, 8192);
+                        buf[sx(8192 + 4096)] = prep(fsm, fsm, 8192);
                     }
                 }
             } else {
