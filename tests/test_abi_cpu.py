@@ -72,6 +72,37 @@ def test_null_pointer_status(lib):
     assert b"null" in lib.vhsdecode_gb300_get_last_error()
 
 
+def test_last_error_is_per_thread(lib):
+    # vhsdecode_cuda_fast.cpp:23-28: the message of a failed call is thread-local,
+    # so a caller reads its own failure even when another thread fails in between
+    import threading
+    from vhsd_gb300 import native
+    both_failed = threading.Barrier(2)
+    seen = {}
+
+    def null_run():
+        st = lib.vhsdecode_gb300_run(None, None)
+        both_failed.wait()
+        seen["run"] = (st, lib.vhsdecode_gb300_get_last_error())
+
+    def bad_info():
+        info = native.RuntimeInfo()
+        info.struct_size = 12
+        st = lib.vhsdecode_gb300_get_runtime_info(0, ctypes.byref(info))
+        both_failed.wait()
+        seen["info"] = (st, lib.vhsdecode_gb300_get_last_error())
+
+    threads = [threading.Thread(target=null_run), threading.Thread(target=bad_info)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join(timeout=30)
+    assert seen["run"][0] == native.STATUS_NULL_POINTER
+    assert b"null" in seen["run"][1] and b"struct_size" not in seen["run"][1]
+    assert seen["info"][0] == native.STATUS_INVALID_ARGUMENT
+    assert b"struct_size" in seen["info"][1]
+
+
 def test_run_rejects_unsupported_options(lib):
     # vhsdecode_cuda_fast.cpp:255-275: input format FLOAT32 or INT16 (or FLAC here),
     # decimation factor 1 or 2 (2 with a decode rate the source halves to)
