@@ -11,7 +11,9 @@ into a 12-field capture.  Checked here:
 * a cancellation during the decode returns CANCELLED and leaves no files;
 * a field limit across windows;
 * with DECODE_CHROMA, the windowed luma and _chroma.tbc equal one whole
-  chroma decode (PAL and NTSC).
+  chroma decode (PAL and NTSC);
+* a chroma workspace allocation forced to fail fails the run and the session
+  decode (no files, an error status) instead of reporting unwritten chroma.
 Faults are made on the host (callbacks), never on the device.
 """
 import ctypes
@@ -188,3 +190,29 @@ def test_field_limit_across_windows(gpu, pal12, tmp_path, monkeypatch):
     assert tbc.tobytes() == whole.tobytes()
     assert len(meta["fields"]) == 7
     assert os.path.getsize(base + "_chroma.tbc") == tbc.size * 2
+
+
+def test_forced_chroma_workspace_failure_fails_closed(gpu, tmp_path, monkeypatch):
+    # tools/build-cuda-fast-native.ps1:290-305: with the chroma workspace
+    # allocation forced to fail, a chroma run must fail instead of reporting
+    # chroma it never wrote.  The session path fails the same way and its
+    # session decodes once the allocation succeeds, with the chroma of a fresh
+    # session.  The fault is made on the host.
+    from vhsd_gb300 import native, synth
+    rf, _ = synth.generate(synth.config("pal_small", fields=4))
+    monkeypatch.setenv("VHSD_FORCE_CHROMA_WORKSPACE_FAILURE", "1")
+    base = str(tmp_path / "fx")
+    st, _ = _run(rf, base, chroma=True)
+    assert st == native.STATUS_INTERNAL_ERROR
+    assert b"chroma workspace" in native.load().vhsdecode_gb300_get_last_error()
+    assert not glob.glob(base + "*")
+    with native.Session(native.PROFILE_PAL, len(rf)) as s:
+        with pytest.raises(native.NativeError, match="chroma workspace"):
+            s.decode(rf, chroma=True)
+        monkeypatch.delenv("VHSD_FORCE_CHROMA_WORKSPACE_FAILURE")
+        r = s.decode(rf, chroma=True)
+        assert r.fields > 0
+        got = s.chroma().copy()
+    with native.Session(native.PROFILE_PAL, len(rf)) as s:
+        s.decode(rf, chroma=True)
+        assert np.array_equal(s.chroma(), got)

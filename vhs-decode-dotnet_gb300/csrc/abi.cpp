@@ -361,6 +361,13 @@ void ensure_chroma(vhsdecode_gb300_session* s) {
     const size_t win = (size_t)(2 * d.burst_end - d.burst_start);
     s->c32.alloc((size_t)std::max<int64_t>(1, s->max_blocks) * kStride);
     s->c_scratch.alloc((size_t)std::max<int64_t>(1, s->max_blocks) * kChromaRowStride);
+    // Host fault injection, the counterpart of the reference build's forced
+    // chroma-workspace failure (CUVHS_FORCE_CHROMA_WORKSPACE_FAILURE,
+    // tools/build-cuda-fast-native.ps1:290-305): the workspace allocation
+    // fails partway, and the decode must fail rather than report chroma it
+    // never wrote.  A later call allocates the workspace afresh.
+    if (const char* f = std::getenv("VHSD_FORCE_CHROMA_WORKSPACE_FAILURE"); f && *f && std::strcmp(f, "0") != 0)
+        throw Failure(VHSDECODE_GB300_STATUS_INTERNAL_ERROR, "chroma workspace cudaMalloc: out of memory (forced)");
     std::vector<float> het, bsin, bcos;
     vhsd::chroma_tables(d, het, bsin, bcos);
     s->c_het.alloc(het.size());
