@@ -185,6 +185,20 @@ def test_decode_is_deterministic(gpu, pal_capture):
     assert a.tobytes() == b.tobytes()
 
 
+def test_chroma_decode_is_deterministic(gpu, pal_capture):
+    # the reference's release gates require identical output bytes run to run;
+    # the default decode (luma and colour-under chroma) twice on one session
+    from vhsd_gb300 import native
+    rf, _ = pal_capture
+    with native.Session(native.PROFILE_PAL, len(rf)) as s:
+        s.decode(rf, chroma=True)
+        a, ca = s.tbc().copy(), s.chroma().copy()
+        s.decode(rf, chroma=True)
+        b, cb = s.tbc(), s.chroma()
+    assert a.tobytes() == b.tobytes()
+    assert ca.tobytes() == cb.tobytes()
+
+
 def test_device_input_pointer_path(gpu, pal_capture):
     import torch
     from vhsd_gb300 import native
