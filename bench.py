@@ -3,12 +3,16 @@
 Workload (default): synthetic NTSC VHS SP RF, 60 fields (~41M int16 samples
 at 40 MSPS, 200 seeded 2-40 us carrier dropouts at 5 %, 38 dB SNR) -- the
 configuration the headline metric is quoted on.  A step decodes the whole
-capture: block demodulation, sync pulses, host field control plane, hsync
-refinement, sinc TBC to 4fSC uint16 and dropout detection.
+capture as the reference's default decode does: block demodulation, sync
+pulses, host field control plane, hsync refinement, sinc TBC to 4fSC uint16,
+dropout detection, and colour-under chroma (block band-pass, burst probes and
+burst refinement of the lines, chroma TBC, up-conversion, comb and gain to
+uint16).  --luma-only times the --skip_chroma decode instead.
 
 value  = RF samples / s with the capture already in HBM (device-resident);
 e2e    = the same through the C ABI with host buffers: pinned host int16 in,
-         uint16 TBC of every field back to pinned host memory, per step;
+         uint16 luma (and chroma) of every field back to pinned host memory,
+         per step;
 roofline = the fused block demodulator against the measured HBM copy peak;
 cpu_baseline = the CPU oracle restatement on the host cores.
 Inputs and intermediate streams (>400 MB) are larger than L2, so no flush
