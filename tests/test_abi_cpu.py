@@ -393,3 +393,22 @@ def test_chroma_design_matches_oracle(lib, system, fs):
             assert np.array_equal(d["heterodyne"][p].astype(np.float64), het[p])
         assert np.array_equal(d["burst_sin"].astype(np.float64), bsin)
         assert np.array_equal(d["burst_cos"].astype(np.float64), bcos)
+
+
+@pytest.mark.parametrize("system", ["PAL", "NTSC"])
+@pytest.mark.parametrize("tape,speed", [("VHS", "lp"), ("VHS", "ep"), ("SVHS", "sp"), ("SVHS", "ep")])
+def test_chroma_design_matches_oracle_per_format(lib, system, tape, speed):
+    # the chroma filters, burst window, offset and rotation follow the format's
+    # RF parameters (band-pass edges, colour-under carrier, rotation, offset),
+    # which differ between tape formats and speeds
+    from oracle import chroma, formats
+    from vhsd_gb300 import native
+    prof = native.PROFILE_PAL if system == "PAL" else native.PROFILE_NTSC
+    sp = {"sp": native.TAPE_SP, "lp": native.TAPE_LP, "ep": native.TAPE_EP}[speed]
+    tf = native.FORMAT_SVHS if tape == "SVHS" else native.FORMAT_VHS
+    d = native.design_chroma(prof, 40.0, tape_speed=sp, tape_format=tf)
+    cp = chroma.ChromaParams(formats.get(system, tape, speed), 40e6)
+    assert np.array_equal(d["rf_sos"], cp.rf_sos)
+    assert np.array_equal(d["final_sos"], cp.final_sos)
+    assert (d["burst_start"], d["burst_end"], d["move"]) == (cp.burst_start, cp.burst_end, cp.offset)
+    assert d["rotation"] == cp.rotation and d["field_samples"] == cp.field_samples
