@@ -23,6 +23,10 @@ def test_empty_and_short_inputs(gpu):
         assert r.blocks == 0 and r.fields == 0 and r.stream_samples == 0
         r = s.decode(np.zeros(32767, np.int16))
         assert r.blocks == 0 and r.fields == 0
+        # the same with colour-under chroma: no blocks, no chroma stages
+        for n in (0, 32767):
+            r = s.decode(np.zeros(n, np.int16), chroma=True)
+            assert r.blocks == 0 and r.fields == 0
 
 
 def test_exactly_one_block_matches_oracle(gpu, pal_capture):
